@@ -1,0 +1,203 @@
+/*
+ * mrmg_gb300.h -- C ABI of the GB300 collision / distance / nearest-neighbour
+ * backend for multi-robot multi-goal planners.
+ *
+ * Conventions
+ *  - Every array argument named d_* is a DEVICE pointer (for example a torch
+ *    tensor's data_ptr()), caller-owned, contiguous, row-major.  Host arrays
+ *    (scene tables) are named h_* and are copied by the library.
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default
+ *    stream.  Calls on one scene handle must be serialised on one stream
+ *    (the handle owns the call's scratch counters).
+ *  - Verdict outputs are uint8: 1 = collision free, 0 = in collision (the
+ *    Python bool of the reference).
+ *  - Every function returns an int status: MRMG_OK (0) or a negative code;
+ *    mrmg_last_error() gives a message for the calling thread.
+ *  - Unless MRMG_FLAG_ASYNC is given, a call synchronises its stream before
+ *    returning, so that device-side input errors are reported as its status.
+ *
+ * Reference paths are inside src/multi_robot_multi_goal_planning/ of
+ * vhartman/multirobot-pathplanning-benchmark.
+ */
+#ifndef MRMG_GB300_H
+#define MRMG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mrmg_scene mrmg_scene;
+
+enum {
+  MRMG_OK = 0,
+  MRMG_ERR_ARG = -1,          /* bad argument or bad input value (ValueError)   */
+  MRMG_ERR_CUDA = -2,         /* CUDA runtime error                             */
+  MRMG_ERR_TIMEOUT = -3,      /* a bounded device wait ran out                  */
+  MRMG_ERR_UNSUPPORTED = -4,  /* shape outside the compiled kernel variants     */
+  MRMG_ERR_N_START = -5       /* N_start > N (the reference asserts)            */
+};
+
+enum { MRMG_F32 = 0, MRMG_F64 = 1 };
+
+/* distance metrics of batch_config_dist (problems/core/configuration.py:332-349) */
+enum {
+  MRMG_METRIC_EUCLIDEAN = 0,
+  MRMG_METRIC_SUM_EUCLIDEAN = 1,
+  MRMG_METRIC_MAX_EUCLIDEAN = 2,
+  MRMG_METRIC_MAX = 3
+};
+
+/* per-agent cost metric and reduction of batch_config_cost
+ * (problems/core/configuration.py:437-510) */
+enum { MRMG_COST_EUCLIDEAN = 0, MRMG_COST_MAX = 1 };
+enum { MRMG_REDUCE_MAX = 0, MRMG_REDUCE_SUM = 1 };
+
+/* call flags */
+enum { MRMG_FLAG_ASYNC = 1 };
+
+const char *mrmg_version(void);
+const char *mrmg_last_error(void);
+
+/* ------------------------------------------------------------------------ */
+/* Scenes                                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* Abstract point-agent scene: spherical agents whose position is their slice
+ * of the configuration, among axis-aligned boxes and sphere obstacles.
+ * Replaces AbstractEnvironment's scene state (problems/abstract_env.py:112-131,
+ * Sphere :41-58, Rectangle :61-109).
+ *   h_agent_offsets[A]      start of agent i's slice in q (all agents have `dim` coords)
+ *   h_agent_radius[A]       agent_radii
+ *   h_pair_threshold[A*A]   agent_radii[i] + agent_radii[j]      (:266)
+ *   h_agent_radius_sq[A]    agent_radii[i] ** 2                  (:84)
+ *   h_box_lo/h_box_hi[nb*dim] Rectangle min_bounds / max_bounds  (:66-67)
+ *   h_sphere_pos[ns*dim], h_sphere_radius[ns]
+ *   h_sphere_threshold[ns*A] sphere.radius + agent_radii[i]      (:47)
+ * dim must be 1..15, A <= 16. */
+int mrmg_abstract_scene_create(int32_t n_agents, int32_t dim, int32_t q_dim,
+                               const int64_t *h_agent_offsets, const double *h_agent_radius,
+                               const double *h_pair_threshold, const double *h_agent_radius_sq,
+                               int32_t n_boxes, const double *h_box_lo, const double *h_box_hi,
+                               int32_t n_spheres, const double *h_sphere_pos,
+                               const double *h_sphere_radius, const double *h_sphere_threshold,
+                               mrmg_scene **out);
+
+/* Sphere-arm scene: R serial DH arms (base kind 0 = fixed pose, 1 = planar
+ * x,y,theta base followed by a fixed mount) carrying collision spheres, among
+ * axis-aligned boxes.  New: the reference delegates robot geometry to external
+ * engines (rai_base_env.py:442-477, pinocchio_env.py:410-500); the per-pair
+ * tests restate Rectangle.collides_with_sphere (abstract_env.py:69-84) and the
+ * agent-agent rule (abstract_env.py:261-268) for every pair of spheres on
+ * different robots.
+ *   h_q_offset[R]        first configuration index of robot r
+ *   h_base_kind[R]       0 fixed, 1 planar (consumes x, y, theta before the arm joints)
+ *   h_base_pose[R*12]    rotation (row-major 3x3) then translation: fixed base pose,
+ *                        or the mount transform applied after the planar base
+ *   h_n_links[R]         DH links (<= 8); joint k of robot r is q[offset(+3) + k]
+ *   h_dh[R*8*4]          per link: a, d, cos(alpha), sin(alpha)  (standard DH,
+ *                        T_k = T_{k-1} Rz(theta) Tz(d) Tx(a) Rx(alpha))
+ *   h_sphere_robot[S], h_sphere_link[S] (0 = base frame, k = after link k)
+ *   h_sphere_local[S*3]  centre in that frame; h_sphere_radius[S]
+ *   h_box_lo/h_box_hi[B*3]
+ *   band                 FP32 re-check band in metres (<= 0: derived from the
+ *                        kinematic reach, see DESIGN)
+ * R <= 16, D <= 96, S <= 1024, B <= 1024. */
+int mrmg_arm_scene_create(int32_t n_robots, int32_t q_dim, const int32_t *h_q_offset,
+                          const int32_t *h_base_kind, const double *h_base_pose,
+                          const int32_t *h_n_links, const double *h_dh, int32_t n_spheres,
+                          const int32_t *h_sphere_robot, const int32_t *h_sphere_link,
+                          const double *h_sphere_local, const double *h_sphere_radius,
+                          int32_t n_boxes, const double *h_box_lo, const double *h_box_hi,
+                          double band, mrmg_scene **out);
+
+int mrmg_scene_destroy(mrmg_scene *scene);
+
+/* Scene facts: [0] kind (0 abstract, 1 arm), [1] q_dim, [2] spheres per group,
+ * [3] groups, [4] inter-robot group pairs, [5] CTAs of the persistent grid,
+ * [6] warps per CTA.  out_band gets the FP32 re-check band. */
+int mrmg_scene_info(const mrmg_scene *scene, int64_t *out7, double *out_band);
+
+/* Launch shape of the persistent kernels (0 = automatic).  Used by the
+ * autotuner; the verdicts never depend on it. */
+int mrmg_scene_set_launch(mrmg_scene *scene, int32_t ctas, int32_t warps_per_cta);
+
+/* ------------------------------------------------------------------------ */
+/* Collision checks                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Per-configuration verdicts for d_q[n, q_dim] (dtype MRMG_F32 or MRMG_F64).
+ * Batched form of BaseProblem.is_collision_free (planning_env.py:1724-1734;
+ * abstract_env.py:255-276); _batch_is_collision_free (abstract_env.py:278-299)
+ * is the AND of these verdicts. */
+int mrmg_is_collision_free_batch(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n,
+                                 uint8_t *d_out, void *stream, int32_t flags);
+
+/* Per-edge verdicts for the linear edges d_q1[n] -> d_q2[n], interpolated at
+ * `resolution` exactly as BaseProblem.is_edge_collision_free
+ * (planning_env.py:1746-1763; abstract_env.py:301-354):
+ *   N = max(2, int(max_k |q1_k - q2_k| / resolution) + 1) unless d_N gives it,
+ *   indices generate_binary_search_indices(N)[N_start : min(N, N_max)]
+ *   (planning_env.py:34-51), endpoints 0 and N-1 skipped unless
+ *   include_endpoints, q = q1 + ((q2 - q1) / (N - 1)) * i in FP64.
+ * d_N may be NULL; N_max < 0 means None.  N_start > N gives MRMG_ERR_N_START. */
+int mrmg_is_edge_collision_free_batch(mrmg_scene *scene, const void *d_q1, const void *d_q2,
+                                      int32_t dtype, int64_t n, double resolution,
+                                      int32_t include_endpoints, const int64_t *d_N,
+                                      int64_t N_start, int64_t N_max, uint8_t *d_out,
+                                      void *stream, int32_t flags);
+
+/* Sphere centres of an arm scene for d_q[n, q_dim]: d_c32[n, S, 3] from the
+ * FP32 bulk path and d_c64[n, S, 3] from the exact FP64 path (either may be
+ * NULL).  Used to verify the FP32 error bound against the re-check band. */
+int mrmg_arm_sphere_centers(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n,
+                            float *d_c32, double *d_c64, void *stream);
+
+/* Statistics of the scene's last completed call: [0] items re-checked in
+ * FP64 (pass two), [1] device error bits, [2] configurations evaluated by the
+ * edge kernel's first pass, [3] reserved. */
+int mrmg_last_call_stats(const mrmg_scene *scene, int64_t *out4);
+
+/* Slot layout of an arm scene: out[slot] = input sphere index or -1 for a
+ * padding slot (rows of mrmg_arm_sphere_centers are per slot).  Returns the
+ * slot count, or a negative status. */
+int mrmg_arm_slot_map(const mrmg_scene *scene, int32_t *out, int64_t cap);
+
+/* Device-side generate_binary_search_indices(N) (planning_env.py:34-51),
+ * written to d_out[N] (int64).  Exposes the edge kernels' index order. */
+int mrmg_binary_search_indices(int64_t N, int64_t *d_out, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Distances and costs (FP64, bit-identical to the reference)                */
+/* ------------------------------------------------------------------------ */
+
+/* d_out[q, m] = batch_config_dist(queries[q], nodes, metric)[m]
+ * (problems/core/configuration.py:342-349 -> NpConfiguration._batch_dist
+ * :303-329): diff = query - node, then
+ *   euclidean      sqrt of the sequential sum of d*d over [0, slices[A-1].end)
+ *   sum_euclidean  sum of the per-agent euclidean norms
+ *   max_euclidean  max of the per-agent euclidean norms (strict '>')
+ *   max            max |d| over all D coordinates
+ * h_slices[A*2] are the agents' (start, end) (NpConfiguration._array_slice).
+ * With Q = 1 this is batch_config_dist itself. */
+int mrmg_config_dist_matrix(const double *d_queries, int64_t Q, const double *d_nodes, int64_t M,
+                            int32_t D, const int64_t *h_slices, int32_t A, int32_t metric,
+                            double *d_out, void *stream, int32_t flags);
+
+/* batch_config_cost (problems/core/configuration.py:437-510): per-agent
+ * euclidean norm or max |d| of the row difference, then max + w * sum
+ * (reduction MRMG_REDUCE_MAX) or the sum.
+ *   mode 0: d_starts is one row, diff = starts - ends[m]   (Configuration x array)
+ *   mode 1: diff = starts[m] - ends[m]                      (array x array + slice)
+ *   mode 2: diff = starts[m + 1] - starts[m], d_ends unused (path form, :460-472) */
+int mrmg_batch_config_cost(const double *d_starts, const double *d_ends, int64_t M, int32_t D,
+                           const int64_t *h_slices, int32_t A, int32_t cost_metric,
+                           int32_t reduction, double w, int32_t mode, double *d_out, void *stream,
+                           int32_t flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MRMG_GB300_H */

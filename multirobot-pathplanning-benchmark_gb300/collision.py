@@ -1,0 +1,185 @@
+"""Device-side scene handles: batched collision checks on the GB300.
+
+``Gb300Scene`` owns one scene of the C library (abstract point agents or
+sphere arms) and exposes the batched entry points.  Inputs may be torch CUDA
+tensors (used in place) or numpy arrays / host tensors (copied to the device).
+Verdicts are uint8 tensors on the device: 1 = collision free.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .scenes import AbstractScene, ArmScene
+
+
+def _dev_tensor(x, dtype=None, device=None):
+    """A contiguous CUDA tensor for x (float32 or float64 kept)."""
+    if isinstance(x, torch.Tensor):
+        t = x
+        if dtype is not None and t.dtype != dtype:
+            t = t.to(dtype)
+        if not t.is_cuda:
+            t = t.to(device or "cuda", non_blocking=t.is_pinned())
+        return t.contiguous()
+    a = np.asarray(x)
+    if dtype is None:
+        dtype = torch.float32 if a.dtype == np.float32 else torch.float64
+        a = a.astype(np.float32 if dtype == torch.float32 else np.float64, copy=False)
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    if t.dtype != dtype:
+        t = t.to(dtype)
+    return t.to(device or "cuda")
+
+
+def _dt_code(t: torch.Tensor) -> int:
+    if t.dtype == torch.float32:
+        return _lib.MRMG_F32
+    if t.dtype == torch.float64:
+        return _lib.MRMG_F64
+    raise TypeError(f"configurations must be float32 or float64, got {t.dtype}")
+
+
+class Gb300Scene:
+    """One scene of libmrmg_gb300 on the current CUDA device."""
+
+    def __init__(self, scene, band: float = 0.0):
+        self.lib = _lib.load()
+        if not torch.cuda.is_available():
+            raise RuntimeError("the GB300 backend needs a CUDA device")
+        torch.cuda.init()
+        self.scene = scene
+        h = C.c_void_p()
+        keep = []
+
+        def P(a):
+            keep.append(a)
+            return a.ctypes.data
+
+        if isinstance(scene, AbstractScene):
+            t = scene.tables()
+            self.kind = 0
+            rc = self.lib.mrmg_abstract_scene_create(
+                len(scene.agent_radii), scene.dim, scene.q_dim, P(t["agent_offsets"]), P(t["agent_radius"]),
+                P(t["pair_threshold"]), P(t["agent_radius_sq"]), len(t["box_lo"]), P(t["box_lo"]), P(t["box_hi"]),
+                len(t["sphere_pos"]), P(t["sphere_pos"]), P(t["sphere_radius"]), P(t["sphere_threshold"]), C.byref(h))
+        elif isinstance(scene, ArmScene):
+            a = scene.arrays()
+            self.kind = 1
+            rc = self.lib.mrmg_arm_scene_create(
+                scene.n_robots, scene.q_dim, P(a["q_offset"]), P(a["base_kind"]), P(a["base_pose"]), P(a["n_links"]),
+                P(a["dh"]), len(a["sphere_radius"]), P(a["sphere_robot"]), P(a["sphere_link"]), P(a["sphere_local"]),
+                P(a["sphere_radius"]), len(a["box_lo"]), P(a["box_lo"]), P(a["box_hi"]), float(band), C.byref(h))
+        else:
+            raise TypeError("scene must be an AbstractScene or an ArmScene")
+        _lib.check(rc, "scene create")
+        self.h = h
+        self.q_dim = scene.q_dim
+        self._slot_map = None
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.mrmg_scene_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------
+    def info(self) -> dict:
+        out = np.zeros(7, dtype=np.int64)
+        band = C.c_double(0)
+        _lib.check(self.lib.mrmg_scene_info(self.h, out.ctypes.data, C.byref(band)))
+        keys = ["kind", "q_dim", "spheres_per_group", "groups", "group_pairs", "ctas", "warps_per_cta"]
+        d = {k: int(v) for k, v in zip(keys, out)}
+        d["band"] = band.value
+        return d
+
+    def set_launch(self, ctas: int = 0, warps_per_cta: int = 0):
+        _lib.check(self.lib.mrmg_scene_set_launch(self.h, int(ctas), int(warps_per_cta)))
+
+    def last_call_stats(self) -> dict:
+        out = np.zeros(4, dtype=np.int64)
+        _lib.check(self.lib.mrmg_last_call_stats(self.h, out.ctypes.data))
+        return {"rechecked_fp64": int(out[0]), "error_bits": int(out[1]), "configs_evaluated": int(out[2])}
+
+    # ------------------------------------------------------------------
+    def is_collision_free_batch(self, q, out=None, stream=None, flags: int = 0) -> torch.Tensor:
+        """Per-configuration verdicts (1 = free) for q[n, q_dim]."""
+        qt = _dev_tensor(q)
+        if qt.dim() == 1:
+            qt = qt.reshape(1, -1)
+        if qt.shape[-1] != self.q_dim:
+            raise ValueError(f"configurations must have {self.q_dim} coordinates")
+        n = qt.shape[0]
+        if out is None:
+            out = torch.empty(n, dtype=torch.uint8, device=qt.device)
+        _lib.check(self.lib.mrmg_is_collision_free_batch(self.h, qt.data_ptr(), _dt_code(qt), n, out.data_ptr(),
+                                                         _lib.stream_handle(stream), flags), "is_collision_free")
+        return out
+
+    def is_edge_collision_free_batch(self, q1, q2, resolution: float, include_endpoints: bool = False, N=None,
+                                     N_start: int = 0, N_max=None, out=None, stream=None, flags: int = 0) -> torch.Tensor:
+        """Per-edge verdicts (1 = free) for the linear edges q1[n] -> q2[n]."""
+        a = _dev_tensor(q1)
+        b = _dev_tensor(q2, dtype=a.dtype, device=a.device)
+        if a.dim() == 1:
+            a, b = a.reshape(1, -1), b.reshape(1, -1)
+        if a.shape != b.shape or a.shape[-1] != self.q_dim:
+            raise ValueError("edge endpoints must be [n, q_dim] arrays of equal shape")
+        n = a.shape[0]
+        Nt = None
+        if N is not None:
+            Nt = _dev_tensor(np.asarray(N, dtype=np.int64).reshape(-1), dtype=torch.int64, device=a.device) \
+                if not isinstance(N, torch.Tensor) else N.to(device=a.device, dtype=torch.int64).contiguous()
+        if out is None:
+            out = torch.empty(n, dtype=torch.uint8, device=a.device)
+        rc = self.lib.mrmg_is_edge_collision_free_batch(
+            self.h, a.data_ptr(), b.data_ptr(), _dt_code(a), n, float(resolution if resolution is not None else 0.0),
+            int(bool(include_endpoints)), None if Nt is None else Nt.data_ptr(), int(N_start),
+            -1 if N_max is None else int(N_max), out.data_ptr(), _lib.stream_handle(stream), flags)
+        _lib.check(rc, "is_edge_collision_free")
+        return out
+
+    # ------------------------------------------------------------------
+    def slot_map(self) -> np.ndarray:
+        if self._slot_map is None:
+            info = self.info()
+            cap = info["groups"] * info["spheres_per_group"]
+            out = np.zeros(cap, dtype=np.int32)
+            _lib.check(self.lib.mrmg_arm_slot_map(self.h, out.ctypes.data, cap))
+            self._slot_map = out
+        return self._slot_map
+
+    def sphere_centers(self, q):
+        """(FP32, FP64) sphere centres [n, S, 3] of the device kinematics, in
+        the scene's sphere order (for the error-bound check)."""
+        if self.kind != 1:
+            raise TypeError("sphere centres exist for arm scenes only")
+        qt = _dev_tensor(q)
+        if qt.dim() == 1:
+            qt = qt.reshape(1, -1)
+        n = qt.shape[0]
+        sm = self.slot_map()
+        c32 = torch.zeros((n, len(sm), 3), dtype=torch.float32, device=qt.device)
+        c64 = torch.zeros((n, len(sm), 3), dtype=torch.float64, device=qt.device)
+        _lib.check(self.lib.mrmg_arm_sphere_centers(self.h, qt.data_ptr(), _dt_code(qt), n, c32.data_ptr(),
+                                                    c64.data_ptr(), _lib.stream_handle(None)))
+        S = int((sm >= 0).sum())
+        order = np.argsort(np.where(sm >= 0, sm, 1 << 30))[:S]
+        idx = torch.from_numpy(order).to(qt.device)
+        return c32[:, idx], c64[:, idx]
+
+
+def binary_search_indices(N: int) -> tuple:
+    """generate_binary_search_indices(N) computed by the device iterator."""
+    lib = _lib.load()
+    out = torch.zeros(max(int(N), 1), dtype=torch.int64, device="cuda")
+    _lib.check(lib.mrmg_binary_search_indices(int(N), out.data_ptr(), _lib.stream_handle(None)))
+    return tuple(out[: int(N)].cpu().tolist())

@@ -1,0 +1,596 @@
+// mrmg_api.cu -- the C ABI: scene handles, per-handle scratch, status codes.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "mrmg_internal.cuh"
+
+using namespace mrmg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(MRMG_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+// One device allocation holding every table of a scene.
+struct DevBlock {
+  std::vector<unsigned char> host;
+  std::vector<std::pair<size_t, void**>> fixups;
+  template <typename T>
+  void add(const T* data, size_t count, const T** dst) {
+    size_t off = (host.size() + 255) & ~(size_t)255;
+    host.resize(off + sizeof(T) * std::max<size_t>(count, 1));
+    if (count) std::memcpy(host.data() + off, data, sizeof(T) * count);
+    fixups.push_back({off, (void**)dst});
+  }
+  cudaError_t upload(void** dev) {
+    cudaError_t e = cudaMalloc(dev, host.size());
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy(*dev, host.data(), host.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    for (auto& f : fixups) *f.second = (unsigned char*)*dev + f.first;
+    return cudaSuccess;
+  }
+};
+
+}  // namespace
+
+struct mrmg_scene {
+  int kind = 0;   // 0 abstract, 1 arm
+  int q_dim = 0;
+  AbstractDev ab{};
+  ArmDev arm{};
+  void* d_tables = nullptr;
+  int* d_ctr = nullptr;
+  long long* d_pend = nullptr;
+  long long pend_cap = 0;
+  int* h_ctr = nullptr;       // pinned mirror of the counters
+  int ctas = 0, warps = 0;    // persistent launch shape (0 = automatic)
+  int num_sms = 0;
+  int device = 0;
+  double band = 0.0;
+  int64_t n_pairs_groups = 0;
+  std::vector<int> slot_to_sphere;   // arm: slot -> input sphere index (-1 padding)
+};
+
+namespace {
+
+int init_common(mrmg_scene* sc) {
+  cudaError_t e = cudaGetDevice(&sc->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  e = cudaDeviceGetAttribute(&sc->num_sms, cudaDevAttrMultiProcessorCount, sc->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  e = cudaMalloc(&sc->d_ctr, sizeof(int) * kNumCtr);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(counters)");
+  e = cudaMallocHost(&sc->h_ctr, sizeof(int) * kNumCtr);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocHost");
+  return MRMG_OK;
+}
+
+int ensure_pending(mrmg_scene* sc, long long n, cudaStream_t st) {
+  if (n <= sc->pend_cap) return MRMG_OK;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cap);
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(MRMG_ERR_ARG, "scratch for %lld items must be reserved before stream capture", n);
+  long long cap_new = std::max(n, 2 * sc->pend_cap);
+  long long* p = nullptr;
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  e = cudaMalloc(&p, sizeof(long long) * cap_new);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(pending)");
+  if (sc->d_pend) cudaFree(sc->d_pend);
+  sc->d_pend = p;
+  sc->pend_cap = cap_new;
+  return MRMG_OK;
+}
+
+LaunchShape shape(mrmg_scene* sc) {
+  LaunchShape ls;
+  ls.num_sms = sc->num_sms;
+  ls.warps = sc->warps > 0 ? sc->warps : 8;
+  if (sc->ctas > 0) ls.ctas = sc->ctas;
+  else if (sc->kind == 1) ls.ctas = sc->num_sms * arm_default_ctas_per_sm(sc->arm, ls.warps);
+  else ls.ctas = sc->num_sms * 8;
+  return ls;
+}
+
+int finish_call(mrmg_scene* sc, cudaStream_t st, int flags) {
+  cudaError_t e = cudaMemcpyAsync(sc->h_ctr, sc->d_ctr, sizeof(int) * kNumCtr, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(status)");
+  if (flags & MRMG_FLAG_ASYNC) return MRMG_OK;
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+  int err = sc->h_ctr[kCtrErr];
+  if (err & E_N_START) return fail(MRMG_ERR_N_START, "N_start > N for at least one edge");
+  if (err & E_BAD_INPUT) return fail(MRMG_ERR_ARG, "non-finite or out-of-range edge length (int() of nan/inf)");
+  if (err & E_TIMEOUT) return fail(MRMG_ERR_TIMEOUT, "a bounded device wait ran out");
+  return MRMG_OK;
+}
+
+float f32_up(double x) {   // FP32 value >= x
+  float f = (float)x;
+  if ((double)f < x) f = nextafterf(f, INFINITY);
+  return f;
+}
+float f32_down(double x) {
+  float f = (float)x;
+  if ((double)f > x) f = nextafterf(f, -INFINITY);
+  return f;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mrmg_version(void) { return "mrmg_gb300 0.1 (sm_103a)"; }
+const char* mrmg_last_error(void) { return g_last_error.c_str(); }
+
+int mrmg_abstract_scene_create(int32_t n_agents, int32_t dim, int32_t q_dim, const int64_t* h_agent_offsets,
+                               const double* h_agent_radius, const double* h_pair_threshold,
+                               const double* h_agent_radius_sq, int32_t n_boxes, const double* h_box_lo,
+                               const double* h_box_hi, int32_t n_spheres, const double* h_sphere_pos,
+                               const double* h_sphere_radius, const double* h_sphere_threshold,
+                               mrmg_scene** out) {
+  if (!out) return fail(MRMG_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (n_agents < 1 || n_agents > kMaxAgents) return fail(MRMG_ERR_UNSUPPORTED, "agents must be 1..%d", kMaxAgents);
+  if (dim < 1 || dim > kMaxAgentDim) return fail(MRMG_ERR_UNSUPPORTED, "agent dimension must be 1..%d", kMaxAgentDim);
+  if (n_boxes < 0 || n_spheres < 0 || n_boxes > 4096 || n_spheres > 4096) return fail(MRMG_ERR_ARG, "obstacle counts");
+  if (q_dim < 1 || q_dim > kMaxAgents * kMaxAgentDim) return fail(MRMG_ERR_UNSUPPORTED, "q_dim out of range");
+  for (int i = 0; i < n_agents; i++)
+    if (h_agent_offsets[i] < 0 || h_agent_offsets[i] + dim > q_dim) return fail(MRMG_ERR_ARG, "agent slice outside q");
+  mrmg_scene* sc = new mrmg_scene();
+  sc->kind = 0;
+  sc->q_dim = q_dim;
+  int rc = init_common(sc);
+  if (rc) { mrmg_scene_destroy(sc); return rc; }
+
+  const int A = n_agents;
+  std::vector<int> off(A);
+  std::vector<float> r32(A), pthr32(A * A), lo32(n_boxes * dim), hi32(n_boxes * dim), sp32(n_spheres * dim),
+      sthr32(n_spheres * A);
+  double omax = 0.0;
+  for (int i = 0; i < A; i++) {
+    off[i] = (int)h_agent_offsets[i];
+    r32[i] = (float)h_agent_radius[i];
+    omax = std::max(omax, std::fabs(h_agent_radius[i]));
+  }
+  for (int i = 0; i < A * A; i++) { pthr32[i] = (float)h_pair_threshold[i]; omax = std::max(omax, std::fabs(h_pair_threshold[i])); }
+  for (int i = 0; i < n_boxes * dim; i++) {
+    lo32[i] = (float)h_box_lo[i];
+    hi32[i] = (float)h_box_hi[i];
+    omax = std::max(omax, std::max(std::fabs(h_box_lo[i]), std::fabs(h_box_hi[i])));
+  }
+  for (int i = 0; i < n_spheres * dim; i++) { sp32[i] = (float)h_sphere_pos[i]; omax = std::max(omax, std::fabs(h_sphere_pos[i])); }
+  for (int i = 0; i < n_spheres * A; i++) { sthr32[i] = (float)h_sphere_threshold[i]; omax = std::max(omax, std::fabs(h_sphere_threshold[i])); }
+  if (!(omax < 1e30)) { mrmg_scene_destroy(sc); return fail(MRMG_ERR_ARG, "non-finite or huge scene values"); }
+
+  AbstractDev& d = sc->ab;
+  d.A = A; d.dim = dim; d.D = q_dim; d.nb = n_boxes; d.ns = n_spheres;
+  d.omax = f32_up(omax * (1.0 + 1e-6) + 1e-30);
+  d.delta_k = (float)(8.0 * dim * std::ldexp(1.0, -24));
+  DevBlock blk;
+  blk.add(off.data(), off.size(), &d.agent_off);
+  blk.add(h_pair_threshold, (size_t)A * A, &d.pair_thr);
+  blk.add(h_agent_radius_sq, (size_t)A, &d.r2);
+  blk.add(h_box_lo, (size_t)n_boxes * dim, &d.box_lo);
+  blk.add(h_box_hi, (size_t)n_boxes * dim, &d.box_hi);
+  blk.add(h_sphere_pos, (size_t)n_spheres * dim, &d.sph_pos);
+  blk.add(h_sphere_threshold, (size_t)n_spheres * A, &d.sph_thr);
+  blk.add(r32.data(), r32.size(), &d.r32);
+  blk.add(pthr32.data(), pthr32.size(), &d.pair_thr32);
+  blk.add(lo32.data(), lo32.size(), &d.box_lo32);
+  blk.add(hi32.data(), hi32.size(), &d.box_hi32);
+  blk.add(sp32.data(), sp32.size(), &d.sph_pos32);
+  blk.add(sthr32.data(), sthr32.size(), &d.sph_thr32);
+  cudaError_t e = blk.upload(&sc->d_tables);
+  if (e != cudaSuccess) { mrmg_scene_destroy(sc); return cuda_fail(e, "upload abstract scene"); }
+  sc->band = d.delta_k * d.omax;
+  *out = sc;
+  return MRMG_OK;
+}
+
+int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const int32_t* h_base_kind,
+                          const double* h_base_pose, const int32_t* h_n_links, const double* h_dh, int32_t S,
+                          const int32_t* h_sphere_robot, const int32_t* h_sphere_link, const double* h_sphere_local,
+                          const double* h_sphere_radius, int32_t B, const double* h_box_lo, const double* h_box_hi,
+                          double band, mrmg_scene** out) {
+  if (!out) return fail(MRMG_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (R < 1 || R > kMaxRobots) return fail(MRMG_ERR_UNSUPPORTED, "robots must be 1..%d", kMaxRobots);
+  if (D < 1 || D > kMaxArmDof) return fail(MRMG_ERR_UNSUPPORTED, "q_dim must be 1..%d", kMaxArmDof);
+  if (S < 1 || S > 1024 || B < 0 || B > 1024) return fail(MRMG_ERR_UNSUPPORTED, "sphere / box counts");
+  uint32_t prism[3] = {0, 0, 0};
+  std::vector<int> used(D, 0);
+  for (int r = 0; r < R; r++) {
+    if (h_n_links[r] < 0 || h_n_links[r] > kMaxLinks) return fail(MRMG_ERR_UNSUPPORTED, "links per robot 0..%d", kMaxLinks);
+    if (h_base_kind[r] != 0 && h_base_kind[r] != 1) return fail(MRMG_ERR_ARG, "base kind must be 0 or 1");
+    int dof = h_n_links[r] + (h_base_kind[r] == 1 ? 3 : 0);
+    if (h_q_offset[r] < 0 || h_q_offset[r] + dof > D) return fail(MRMG_ERR_ARG, "robot %d joints outside q", r);
+    for (int j = 0; j < dof; j++) used[h_q_offset[r] + j]++;
+    if (h_base_kind[r] == 1) {
+      prism[h_q_offset[r] >> 5] |= 1u << (h_q_offset[r] & 31);
+      prism[(h_q_offset[r] + 1) >> 5] |= 1u << ((h_q_offset[r] + 1) & 31);
+    }
+  }
+  for (int j = 0; j < D; j++)
+    if (used[j] > 1) return fail(MRMG_ERR_ARG, "joint %d shared by two robots", j);
+  for (int i = 0; i < S; i++) {
+    int r = h_sphere_robot[i];
+    if (r < 0 || r >= R || h_sphere_link[i] < 0 || h_sphere_link[i] > h_n_links[r])
+      return fail(MRMG_ERR_ARG, "sphere %d: bad robot/link", i);
+    if (!(h_sphere_radius[i] >= 0.0) || !(h_sphere_radius[i] < 1e6)) return fail(MRMG_ERR_ARG, "sphere %d radius", i);
+  }
+
+  // pack spheres into groups (robot, link) of SPG slots for the cheapest
+  // compiled variant that fits in 32 * groups-per-lane groups
+  std::vector<std::vector<int>> by_frame(R * (kMaxLinks + 1));
+  for (int i = 0; i < S; i++) by_frame[h_sphere_robot[i] * (kMaxLinks + 1) + h_sphere_link[i]].push_back(i);
+  int best_spg = -1, best_cost = 1 << 30, best_G = 0;
+  for (int vi = 0; arm_supported_spg(vi) > 0; vi++) {
+    int spg = arm_supported_spg(vi), gpl = arm_gpl_for_spg(spg);
+    int G = 0;
+    for (auto& f : by_frame) G += ((int)f.size() + spg - 1) / spg;
+    if (G > 32 * gpl) continue;
+    int cost = gpl * spg;
+    if (cost < best_cost) { best_cost = cost; best_spg = spg; best_G = G; }
+  }
+  if (best_spg < 0) return fail(MRMG_ERR_UNSUPPORTED, "too many sphere groups for the compiled variants");
+  const int SPG = best_spg, G = best_G;
+  std::vector<int> grp;            // robot | link << 8
+  std::vector<int> grp_robot;
+  std::vector<int> slot_sphere;    // slot -> sphere or -1
+  for (int r = 0; r < R; r++)
+    for (int k = 0; k <= kMaxLinks; k++) {
+      auto& f = by_frame[r * (kMaxLinks + 1) + k];
+      for (size_t s0 = 0; s0 < f.size(); s0 += SPG) {
+        grp.push_back(r | (k << 8));
+        grp_robot.push_back(r);
+        for (int v = 0; v < SPG; v++) slot_sphere.push_back(s0 + v < f.size() ? f[s0 + v] : -1);
+      }
+    }
+  // inter-robot group pairs
+  std::vector<uint32_t> pairs;
+  for (int a = 0; a < G; a++)
+    for (int b = a + 1; b < G; b++)
+      if (grp_robot[a] != grp_robot[b]) pairs.push_back((uint32_t)a | ((uint32_t)b << 16));
+
+  // FP32 band: bounds |FP32 centre - FP64 centre| (see DESIGN): 16 (L+1) 2^-24 times
+  // the largest reach (base translation magnitude + link lengths + sphere offsets)
+  double max_box = 0.0;
+  for (int i = 0; i < 3 * B; i++) max_box = std::max(max_box, std::max(std::fabs(h_box_lo[i]), std::fabs(h_box_hi[i])));
+  if (!(max_box < 1e6)) return fail(MRMG_ERR_ARG, "box coordinates must be finite and < 1e6");
+  const double xy_max = std::max(8.0, 2.0 * max_box);
+  double reach_max = 0.0;
+  int lmax = 0;
+  for (int r = 0; r < R; r++) {
+    const double* bp = h_base_pose + r * 12;
+    double reach = 0.0;
+    if (h_base_kind[r] == 1) reach += xy_max * std::sqrt(2.0) + std::fabs(bp[11]);
+    reach += std::sqrt(bp[9] * bp[9] + bp[10] * bp[10] + bp[11] * bp[11]);
+    for (int k = 0; k < h_n_links[r]; k++) {
+      const double* h = h_dh + (r * kMaxLinks + k) * 4;
+      reach += std::fabs(h[0]) + std::fabs(h[1]);
+    }
+    double loc = 0.0;
+    for (int i = 0; i < S; i++)
+      if (h_sphere_robot[i] == r) {
+        const double* l = h_sphere_local + 3 * i;
+        loc = std::max(loc, std::sqrt(l[0] * l[0] + l[1] * l[1] + l[2] * l[2]));
+      }
+    reach += loc;
+    reach_max = std::max(reach_max, reach);
+    lmax = std::max(lmax, h_n_links[r] + (h_base_kind[r] == 1 ? 1 : 0));
+  }
+  double delta = 16.0 * (lmax + 1) * std::ldexp(1.0, -24) * reach_max + 4.0 * std::ldexp(1.0, -24) * max_box;
+  if (band > delta) delta = band;
+  if (!(delta < 1.0)) return fail(MRMG_ERR_ARG, "kinematic reach too large for the FP32 path");
+
+  // box order: larger boxes first (earlier certain collisions; verdicts do not depend on order)
+  std::vector<int> border(B);
+  std::iota(border.begin(), border.end(), 0);
+  auto vol = [&](int b) {
+    double v = 1.0;
+    for (int k = 0; k < 3; k++) v *= std::max(0.0, h_box_hi[3 * b + k] - h_box_lo[3 * b + k]);
+    return v;
+  };
+  std::stable_sort(border.begin(), border.end(), [&](int a, int b) { return vol(a) > vol(b); });
+
+  mrmg_scene* sc = new mrmg_scene();
+  sc->kind = 1;
+  sc->q_dim = D;
+  int rc = init_common(sc);
+  if (rc) { mrmg_scene_destroy(sc); return rc; }
+  ArmDev& d = sc->arm;
+  d.R = R; d.D = D; d.G = G; d.SPG = SPG; d.B = B; d.NP = (int)pairs.size();
+  d.delta = f32_up(delta);
+  d.xy_max = (float)xy_max;
+  for (int r = 0; r < R; r++) { d.q_off[r] = h_q_offset[r]; d.base_kind[r] = h_base_kind[r]; d.nl[r] = h_n_links[r]; }
+  d.prismatic[0] = prism[0]; d.prismatic[1] = prism[1]; d.prismatic[2] = prism[2];
+
+  std::vector<float4> base32(R * 3), dh32(R * kMaxLinks), sph32(G * SPG), band32(G * SPG), box32(2 * B);
+  std::vector<double> sph64((size_t)G * SPG * 5), box64((size_t)B * 6);
+  for (int r = 0; r < R; r++) {
+    const double* bp = h_base_pose + r * 12;
+    for (int i = 0; i < 3; i++) base32[r * 3 + i] = make_float4((float)bp[3 * i], (float)bp[3 * i + 1], (float)bp[3 * i + 2], (float)bp[9 + i]);
+    for (int k = 0; k < kMaxLinks; k++) {
+      const double* h = h_dh + (r * kMaxLinks + k) * 4;
+      dh32[r * kMaxLinks + k] = make_float4((float)h[0], (float)h[1], (float)h[2], (float)h[3]);
+    }
+  }
+  for (int sl = 0; sl < G * SPG; sl++) {
+    int i = slot_sphere[sl];
+    if (i < 0) {
+      sph32[sl] = make_float4(0.f, 0.f, 0.f, 0.f);
+      band32[sl] = make_float4(-1.f, -1.f, 0.f, 0.f);
+      for (int k = 0; k < 5; k++) sph64[(size_t)sl * 5 + k] = k == 3 ? -1.0 : 0.0;
+      continue;
+    }
+    const double* l = h_sphere_local + 3 * i;
+    const double r = h_sphere_radius[i];
+    sph32[sl] = make_float4((float)l[0], (float)l[1], (float)l[2], (float)r);
+    const double rhi = r + delta, rlo = r - delta;
+    band32[sl] = make_float4(rlo > 0 ? f32_down(rlo * rlo * (1.0 - 1e-6)) : -1.f, f32_up(rhi * rhi * (1.0 + 1e-6)),
+                             f32_up(r + delta), f32_down(r - delta));
+    sph64[(size_t)sl * 5 + 0] = l[0];
+    sph64[(size_t)sl * 5 + 1] = l[1];
+    sph64[(size_t)sl * 5 + 2] = l[2];
+    sph64[(size_t)sl * 5 + 3] = r;
+    sph64[(size_t)sl * 5 + 4] = r * r;
+  }
+  for (int bi = 0; bi < B; bi++) {
+    const int b = border[bi];
+    const double* lo = h_box_lo + 3 * b;
+    const double* hi = h_box_hi + 3 * b;
+    // FP32 centre / half extent; the band absorbs their rounding (|box| < 1e6 m)
+    box32[2 * bi] = make_float4((float)(0.5 * (lo[0] + hi[0])), (float)(0.5 * (lo[1] + hi[1])), (float)(0.5 * (lo[2] + hi[2])), 0.f);
+    box32[2 * bi + 1] = make_float4((float)(0.5 * (hi[0] - lo[0])), (float)(0.5 * (hi[1] - lo[1])), (float)(0.5 * (hi[2] - lo[2])), 0.f);
+    for (int k = 0; k < 3; k++) { box64[(size_t)bi * 6 + k] = lo[k]; box64[(size_t)bi * 6 + 3 + k] = hi[k]; }
+  }
+  DevBlock blk;
+  blk.add(h_base_pose, (size_t)R * 12, &d.base64);
+  blk.add(h_dh, (size_t)R * kMaxLinks * 4, &d.dh64);
+  blk.add(sph64.data(), sph64.size(), &d.sph64);
+  blk.add(box64.data(), box64.size(), &d.box64);
+  blk.add(base32.data(), base32.size(), &d.base32);
+  blk.add(dh32.data(), dh32.size(), &d.dh32);
+  blk.add(sph32.data(), sph32.size(), &d.sph32);
+  blk.add(band32.data(), band32.size(), &d.band32);
+  blk.add(box32.data(), box32.size(), &d.box32);
+  blk.add(grp.data(), grp.size(), &d.grp);
+  blk.add(pairs.data(), pairs.size(), &d.pairs);
+  cudaError_t e = blk.upload(&sc->d_tables);
+  if (e != cudaSuccess) { mrmg_scene_destroy(sc); return cuda_fail(e, "upload arm scene"); }
+  sc->band = d.delta;
+  sc->n_pairs_groups = (int64_t)pairs.size();
+  sc->slot_to_sphere = slot_sphere;
+  *out = sc;
+  return MRMG_OK;
+}
+
+int mrmg_scene_destroy(mrmg_scene* sc) {
+  if (!sc) return MRMG_OK;
+  if (sc->d_tables) cudaFree(sc->d_tables);
+  if (sc->d_ctr) cudaFree(sc->d_ctr);
+  if (sc->d_pend) cudaFree(sc->d_pend);
+  if (sc->h_ctr) cudaFreeHost(sc->h_ctr);
+  delete sc;
+  return MRMG_OK;
+}
+
+int mrmg_scene_info(const mrmg_scene* sc, int64_t* out7, double* out_band) {
+  if (!sc || !out7) return fail(MRMG_ERR_ARG, "NULL argument");
+  LaunchShape ls = shape(const_cast<mrmg_scene*>(sc));
+  out7[0] = sc->kind;
+  out7[1] = sc->q_dim;
+  out7[2] = sc->kind == 1 ? sc->arm.SPG : 0;
+  out7[3] = sc->kind == 1 ? sc->arm.G : 0;
+  out7[4] = sc->n_pairs_groups;
+  out7[5] = ls.ctas;
+  out7[6] = ls.warps;
+  if (out_band) *out_band = sc->band;
+  return MRMG_OK;
+}
+
+int mrmg_scene_set_launch(mrmg_scene* sc, int32_t ctas, int32_t warps) {
+  if (!sc || ctas < 0 || warps < 0 || warps > 8) return fail(MRMG_ERR_ARG, "launch shape");
+  sc->ctas = ctas;
+  sc->warps = warps;
+  return MRMG_OK;
+}
+
+int mrmg_arm_slot_map(const mrmg_scene* sc, int32_t* out, int64_t cap) {
+  if (!sc || sc->kind != 1 || !out) return fail(MRMG_ERR_ARG, "arm scene required");
+  if (cap < (int64_t)sc->slot_to_sphere.size()) return fail(MRMG_ERR_ARG, "capacity too small");
+  for (size_t i = 0; i < sc->slot_to_sphere.size(); i++) out[i] = sc->slot_to_sphere[i];
+  return (int)sc->slot_to_sphere.size();
+}
+
+int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype, int64_t n, uint8_t* d_out,
+                                 void* stream, int32_t flags) {
+  if (!sc) return fail(MRMG_ERR_ARG, "scene is NULL");
+  if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
+  if (n == 0) return MRMG_OK;
+  if (!d_q || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = ensure_pending(sc, n, st);
+  if (rc) return rc;
+  cudaError_t e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  CallScratch cs{sc->d_ctr, sc->d_pend, sc->pend_cap};
+  LaunchShape ls = shape(sc);
+  e = sc->kind == 0 ? abstract_configs(sc->ab, d_q, dtype, n, d_out, cs, ls, st)
+                    : arm_configs(sc->arm, d_q, dtype, n, d_out, cs, ls, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch configs");
+  return finish_call(sc, st, flags);
+}
+
+int mrmg_is_edge_collision_free_batch(mrmg_scene* sc, const void* d_q1, const void* d_q2, int32_t dtype, int64_t n,
+                                      double resolution, int32_t include_endpoints, const int64_t* d_N,
+                                      int64_t N_start, int64_t N_max, uint8_t* d_out, void* stream, int32_t flags) {
+  if (!sc) return fail(MRMG_ERR_ARG, "scene is NULL");
+  if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
+  if (!d_N && !(resolution > 0.0)) return fail(MRMG_ERR_ARG, "resolution must be > 0");
+  if (N_start < 0) return fail(MRMG_ERR_ARG, "N_start must be >= 0");
+  if (n == 0) return MRMG_OK;
+  if (!d_q1 || !d_q2 || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = ensure_pending(sc, n, st);
+  if (rc) return rc;
+  cudaError_t e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  CallScratch cs{sc->d_ctr, sc->d_pend, sc->pend_cap};
+  LaunchShape ls = shape(sc);
+  e = sc->kind == 0
+          ? abstract_edges(sc->ab, d_q1, d_q2, dtype, n, resolution, include_endpoints, (const long long*)d_N,
+                           N_start, N_max, d_out, cs, ls, st)
+          : arm_edges(sc->arm, d_q1, d_q2, dtype, n, resolution, include_endpoints, (const long long*)d_N, N_start,
+                      N_max, d_out, cs, ls, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch edges");
+  return finish_call(sc, st, flags);
+}
+
+int mrmg_last_call_stats(const mrmg_scene* sc, int64_t* out4) {
+  if (!sc || !out4) return fail(MRMG_ERR_ARG, "NULL argument");
+  out4[0] = sc->h_ctr[kCtrPending];
+  out4[1] = sc->h_ctr[kCtrErr];
+  long long cfg;
+  std::memcpy(&cfg, sc->h_ctr + kCtrStat0, sizeof(cfg));
+  out4[2] = cfg;
+  out4[3] = 0;
+  return MRMG_OK;
+}
+
+int mrmg_arm_sphere_centers(mrmg_scene* sc, const void* d_q, int32_t dtype, int64_t n, float* d_c32, double* d_c64,
+                            void* stream) {
+  if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
+  if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
+  if (n == 0) return MRMG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = arm_centers(sc->arm, d_q, dtype, n, d_c32, d_c64, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch centers");
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "centers kernel");
+  return MRMG_OK;
+}
+
+static int device_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+static int make_slices(const int64_t* h_slices, int32_t A, int32_t D, SliceTab* t) {
+  if (D < 1 || A < 1 || A > 64 || !h_slices) return fail(MRMG_ERR_ARG, "slices: 1..64 agents, D >= 1");
+  t->A = A;
+  t->D = D;
+  for (int i = 0; i < A; i++) {
+    int64_t s = h_slices[2 * i], e = h_slices[2 * i + 1];
+    if (s < 0 || e < s || e > D) return fail(MRMG_ERR_ARG, "agent slice %d outside [0, D]", i);
+    t->s[i] = (int)s;
+    t->e[i] = (int)e;
+  }
+  t->end_all = t->e[A - 1];
+  return MRMG_OK;
+}
+
+static int sync_unless_async(cudaStream_t st, int32_t flags, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  if (flags & MRMG_FLAG_ASYNC) return MRMG_OK;
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return MRMG_OK;
+}
+
+int mrmg_config_dist_matrix(const double* d_queries, int64_t Q, const double* d_nodes, int64_t M, int32_t D,
+                            const int64_t* h_slices, int32_t A, int32_t metric, double* d_out, void* stream,
+                            int32_t flags) {
+  if (Q < 0 || M < 0 || metric < 0 || metric > 3) return fail(MRMG_ERR_ARG, "Q / M / metric");
+  SliceTab t;
+  int rc = make_slices(h_slices, A, D, &t);
+  if (rc) return rc;
+  if (Q == 0 || M == 0) return MRMG_OK;
+  if (!d_queries || !d_nodes || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = dist_matrix(d_queries, Q, d_nodes, M, t, metric, d_out, device_sms(), st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch distance matrix");
+  return sync_unless_async(st, flags, "distance matrix");
+}
+
+int mrmg_batch_config_cost(const double* d_starts, const double* d_ends, int64_t M, int32_t D, const int64_t* h_slices,
+                           int32_t A, int32_t cost_metric, int32_t reduction, double w, int32_t mode, double* d_out,
+                           void* stream, int32_t flags) {
+  if (M < 0 || mode < 0 || mode > 2) return fail(MRMG_ERR_ARG, "M / mode");
+  if (cost_metric != MRMG_COST_EUCLIDEAN && cost_metric != MRMG_COST_MAX) return fail(MRMG_ERR_ARG, "cost metric");
+  if (reduction != MRMG_REDUCE_MAX && reduction != MRMG_REDUCE_SUM) return fail(MRMG_ERR_ARG, "reduction");
+  SliceTab t;
+  int rc = make_slices(h_slices, A, D, &t);
+  if (rc) return rc;
+  for (int i = 0; i < A; i++)
+    if (cost_metric == MRMG_COST_MAX && t.e[i] == t.s[i]) return fail(MRMG_ERR_ARG, "empty agent slice");
+  if (M == 0) return MRMG_OK;
+  if (!d_starts || (mode != 2 && !d_ends) || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = batch_cost(d_starts, d_ends, M, t, cost_metric, reduction, w, mode, d_out, device_sms(), st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch cost");
+  return sync_unless_async(st, flags, "cost");
+}
+
+int mrmg_binary_search_indices(int64_t N, int64_t* d_out, void* stream) {
+  if (N < 0 || (N > 0 && !d_out)) return fail(MRMG_ERR_ARG, "N / out");
+  if (N == 0) return MRMG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = binary_indices(N, (long long*)d_out, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch binary indices");
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "binary indices kernel");
+  return MRMG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+namespace mrmg {
+namespace {
+__global__ void binary_indices_kernel(long long N, long long* out) {
+  const int lane = threadIdx.x & 31;
+  BfsChunker ch;
+  ch.init(N);
+  long long v;
+  unsigned m;
+  long long pos0;
+  while (ch.next(lane, &v, &m, &pos0)) {
+    if (v >= 0) out[pos0 + __popc(m & ((1u << lane) - 1u))] = v;
+  }
+}
+}  // namespace
+cudaError_t binary_indices(long long N, long long* out, cudaStream_t st) {
+  binary_indices_kernel<<<1, 32, 0, st>>>(N, out);
+  return cudaGetLastError();
+}
+}  // namespace mrmg

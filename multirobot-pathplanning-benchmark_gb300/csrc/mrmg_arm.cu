@@ -1,0 +1,762 @@
+// mrmg_arm.cu -- collision kernels for sphere-arm scenes: batched forward
+// kinematics of DH arms carrying collision spheres, sphere-box and
+// sphere-sphere (different robots) tests, configuration and edge checks.
+//
+// Mapping: one warp evaluates one configuration.  Lane l owns sphere groups
+// g = l, l+32, ... (a group = up to SPG spheres of one robot link); it runs
+// the robot's kinematic chain up to that link with the joint transforms in
+// registers, then tests its spheres against every box (box tables in shared
+// memory, broadcast reads).  Inter-robot group pairs are dealt round-robin to
+// the lanes and read their spheres from the warp's shared sphere table.  A
+// warp vote after every box and every pair round stops the configuration at
+// its first certain collision.
+//
+// Exactness: the bulk runs in FP32 against per-sphere thresholds widened and
+// narrowed by the band delta, which bounds |FP32 centre - FP64 centre|.  A
+// test inside the band is pending; pass 2 recomputes the chain in FP64 with
+// the operation order of the CPU restatement and decides each pending test
+// exactly (Rectangle.collides_with_sphere, problems/abstract_env.py:69-84;
+// agent-agent norm rule, abstract_env.py:261-268).
+#include <algorithm>
+#include <cstdio>
+
+#include "mrmg_internal.cuh"
+
+namespace mrmg {
+namespace {
+
+constexpr float kFar = 1.0e15f;
+
+__device__ __forceinline__ double ldq(const void* p, int dtype, long long i) {
+  return dtype == MRMG_F32 ? (double)((const float*)p)[i] : ((const double*)p)[i];
+}
+
+// Shared-memory image of the scene (per CTA) --------------------------------
+struct ArmSmem {
+  float4* box;      // [B*2]
+  float4* base;     // [R*3]
+  float4* dh;       // [R*8]
+  float4* sph;      // [G*SPG]
+  float4* band;     // [G*SPG]
+  int* grp;         // [G]
+  uint32_t* pairs;  // [NP]
+  uint32_t prismatic[3];
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline size_t table_bytes(const ArmDev& s) {
+  size_t b = 0;
+  b += align16(sizeof(float4) * s.B * 2);
+  b += align16(sizeof(float4) * s.R * 3);
+  b += align16(sizeof(float4) * s.R * kMaxLinks);
+  b += align16(sizeof(float4) * s.G * s.SPG) * 2;
+  b += align16(sizeof(int) * s.G);
+  b += align16(sizeof(uint32_t) * s.NP);
+  return b;
+}
+
+// per-warp FP32 work area: joint cos/sin, planar translations, sphere table
+__host__ __device__ inline size_t warp32_bytes(const ArmDev& s) {
+  return align16(sizeof(float2) * s.D) + align16(sizeof(float) * s.D) +
+         align16(sizeof(float4) * s.G * s.SPG);
+}
+
+// per-warp FP64 work area for pass 2: joint values, cos/sin, sphere centres
+__host__ __device__ inline size_t warp64_bytes(const ArmDev& s) {
+  return align16(sizeof(double) * s.D) + align16(sizeof(double) * 2 * s.D) +
+         align16(sizeof(double) * 3 * s.G * s.SPG);
+}
+
+__device__ void stage_tables(const ArmDev& s, unsigned char* base, ArmSmem* t) {
+  unsigned char* p = base;
+  t->box = (float4*)p; p += align16(sizeof(float4) * s.B * 2);
+  t->base = (float4*)p; p += align16(sizeof(float4) * s.R * 3);
+  t->dh = (float4*)p; p += align16(sizeof(float4) * s.R * kMaxLinks);
+  t->sph = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
+  t->band = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
+  t->grp = (int*)p; p += align16(sizeof(int) * s.G);
+  t->pairs = (uint32_t*)p;
+  for (int i = threadIdx.x; i < s.B * 2; i += blockDim.x) t->box[i] = s.box32[i];
+  for (int i = threadIdx.x; i < s.R * 3; i += blockDim.x) t->base[i] = s.base32[i];
+  for (int i = threadIdx.x; i < s.R * kMaxLinks; i += blockDim.x) t->dh[i] = s.dh32[i];
+  for (int i = threadIdx.x; i < s.G * s.SPG; i += blockDim.x) {
+    t->sph[i] = s.sph32[i];
+    t->band[i] = s.band32[i];
+  }
+  for (int i = threadIdx.x; i < s.G; i += blockDim.x) t->grp[i] = s.grp[i];
+  for (int i = threadIdx.x; i < s.NP; i += blockDim.x) t->pairs[i] = s.pairs[i];
+  t->prismatic[0] = s.prismatic[0];
+  t->prismatic[1] = s.prismatic[1];
+  t->prismatic[2] = s.prismatic[2];
+}
+
+__device__ __forceinline__ bool is_prismatic(const ArmSmem& t, int j) {
+  return (t.prismatic[j >> 5] >> (j & 31)) & 1u;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 forward kinematics of one group: world frame of (robot r, link k).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void chain32(const ArmDev& s, const ArmSmem& t, const float2* wcs,
+                                        const float* wqv, int r, int k, float R[9], float p[3]) {
+  const float4 b0 = t.base[r * 3 + 0], b1 = t.base[r * 3 + 1], b2 = t.base[r * 3 + 2];
+  int joff = s.q_off[r];
+  if (s.base_kind[r] == 1) {
+    const float x = wqv[joff], y = wqv[joff + 1];
+    const float2 cs = wcs[joff + 2];
+    const float c = cs.x, sn = cs.y;
+    // Rz(theta) * mount
+    R[0] = c * b0.x - sn * b1.x; R[1] = c * b0.y - sn * b1.y; R[2] = c * b0.z - sn * b1.z;
+    R[3] = sn * b0.x + c * b1.x; R[4] = sn * b0.y + c * b1.y; R[5] = sn * b0.z + c * b1.z;
+    R[6] = b2.x; R[7] = b2.y; R[8] = b2.z;
+    p[0] = x + (c * b0.w - sn * b1.w);
+    p[1] = y + (sn * b0.w + c * b1.w);
+    p[2] = b2.w;
+    joff += 3;
+  } else {
+    R[0] = b0.x; R[1] = b0.y; R[2] = b0.z; p[0] = b0.w;
+    R[3] = b1.x; R[4] = b1.y; R[5] = b1.z; p[1] = b1.w;
+    R[6] = b2.x; R[7] = b2.y; R[8] = b2.z; p[2] = b2.w;
+  }
+  for (int j = 0; j < k; j++) {
+    const float2 cs = wcs[joff + j];
+    const float4 h = t.dh[r * kMaxLinks + j];
+    const float c = cs.x, sn = cs.y;
+    const float sca = sn * h.z, cca = c * h.z, ssa = sn * h.w, csa = c * h.w;
+    const float ac = h.x * c, as = h.x * sn;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const float r0 = R[3 * i], r1 = R[3 * i + 1], r2 = R[3 * i + 2];
+      R[3 * i] = r0 * c + r1 * sn;
+      R[3 * i + 1] = r1 * cca - r0 * sca + r2 * h.w;
+      R[3 * i + 2] = r0 * ssa - r1 * csa + r2 * h.z;
+      p[i] = p[i] + (r0 * ac + r1 * as + r2 * h.y);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Exact FP64 chain: identical operation order to the CPU restatement.
+// ---------------------------------------------------------------------------
+__device__ void chain64(const ArmDev& s, const double* wth, const double* wcs, int r, int k,
+                        double R[9], double p[3]) {
+  const double* bp = s.base64 + r * 12;
+  int jo = s.q_off[r];
+  if (s.base_kind[r] == 1) {
+    const double x = wth[jo], y = wth[jo + 1];
+    const double cs = wcs[2 * (jo + 2)], sn = wcs[2 * (jo + 2) + 1];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R[j] = __dsub_rn(__dmul_rn(cs, bp[j]), __dmul_rn(sn, bp[3 + j]));
+      R[3 + j] = __dadd_rn(__dmul_rn(sn, bp[j]), __dmul_rn(cs, bp[3 + j]));
+      R[6 + j] = bp[6 + j];
+    }
+    p[0] = __dadd_rn(x, __dsub_rn(__dmul_rn(cs, bp[9]), __dmul_rn(sn, bp[10])));
+    p[1] = __dadd_rn(y, __dadd_rn(__dmul_rn(sn, bp[9]), __dmul_rn(cs, bp[10])));
+    p[2] = bp[11];
+    jo += 3;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 9; i++) R[i] = bp[i];
+    p[0] = bp[9]; p[1] = bp[10]; p[2] = bp[11];
+  }
+  for (int j = 0; j < k; j++) {
+    const double* h = s.dh64 + (r * kMaxLinks + j) * 4;
+    const double cs = wcs[2 * (jo + j)], sn = wcs[2 * (jo + j) + 1];
+    const double ad = h[0], dd = h[1], ca = h[2], sa = h[3];
+    const double sca = __dmul_rn(sn, ca), cca = __dmul_rn(cs, ca);
+    const double ssa = __dmul_rn(sn, sa), csa = __dmul_rn(cs, sa);
+    const double ac = __dmul_rn(ad, cs), as = __dmul_rn(ad, sn);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const double r0 = R[3 * i], r1 = R[3 * i + 1], r2 = R[3 * i + 2];
+      R[3 * i] = __dadd_rn(__dmul_rn(r0, cs), __dmul_rn(r1, sn));
+      R[3 * i + 1] = __dadd_rn(__dsub_rn(__dmul_rn(r1, cca), __dmul_rn(r0, sca)), __dmul_rn(r2, sa));
+      R[3 * i + 2] = __dadd_rn(__dsub_rn(__dmul_rn(r0, ssa), __dmul_rn(r1, csa)), __dmul_rn(r2, ca));
+      p[i] = __dadd_rn(p[i], __dadd_rn(__dadd_rn(__dmul_rn(r0, ac), __dmul_rn(r1, as)), __dmul_rn(r2, dd)));
+    }
+  }
+}
+
+// exact sphere-box test (numpy order for 3 coordinates)
+__device__ __forceinline__ bool exact_box_hit(const double* c, const double* bx, double r2) {
+  double sq[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    double v = c[k] > bx[k] ? c[k] : bx[k];
+    v = v < bx[3 + k] ? v : bx[3 + k];
+    double e = __dsub_rn(v, c[k]);
+    sq[k] = __dmul_rn(e, e);
+  }
+  return __dadd_rn(__dadd_rn(sq[0], sq[1]), sq[2]) <= r2;
+}
+
+// exact sphere-sphere test: sqrt(ddot) < ra + rb
+__device__ __forceinline__ bool exact_pair_hit(const double* a, const double* b, double ra, double rb) {
+  double ss = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    double d = __dsub_rn(a[k], b[k]);
+    ss = __fma_rn(d, d, ss);
+  }
+  return sqrt(ss) < __dadd_rn(ra, rb);
+}
+
+// every test of the configuration in FP64 (pass 2, when an angle or a planar
+// translation is outside the FP32 path's range)
+__device__ bool exact_all_collide(const ArmDev& s, const double* wc64, int lane) {
+  bool hit = false;
+  const int slots = s.G * s.SPG;
+  for (int sl = lane; sl < slots && !hit; sl += 32) {
+    if (s.sph64[(size_t)sl * 5 + 3] < 0.0) continue;
+    for (int b = 0; b < s.B && !hit; b++)
+      hit |= exact_box_hit(wc64 + (size_t)sl * 3, s.box64 + (size_t)b * 6, s.sph64[(size_t)sl * 5 + 4]);
+  }
+  for (int pi = lane; pi < s.NP && !hit; pi += 32) {
+    const uint32_t pr = s.pairs[pi];
+    const int ga = pr & 0xffff, gb = pr >> 16;
+    for (int v = 0; v < s.SPG && !hit; v++) {
+      const int sa = ga * s.SPG + v;
+      if (s.sph64[(size_t)sa * 5 + 3] < 0.0) continue;
+      for (int w = 0; w < s.SPG && !hit; w++) {
+        const int sb = gb * s.SPG + w;
+        if (s.sph64[(size_t)sb * 5 + 3] < 0.0) continue;
+        hit |= exact_pair_hit(wc64 + (size_t)sa * 3, wc64 + (size_t)sb * 3, s.sph64[(size_t)sa * 5 + 3],
+                              s.sph64[(size_t)sb * 5 + 3]);
+      }
+    }
+  }
+  return __any_sync(MRMG_FULL, hit);
+}
+
+// ---------------------------------------------------------------------------
+// Warp evaluation of one configuration.  `theta(j)` yields joint j in FP64.
+// Returns V_COLLIDE, V_FREE, or (pass 1 only) V_PENDING; warp-uniform.
+// ---------------------------------------------------------------------------
+template <int GPL, int SPG, bool RESOLVE, class Theta>
+__device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, float* wqv,
+                               float4* wsph, double* w64, int lane, Theta theta) {
+  __syncwarp();
+  // --- joint preprocessing (FP32 cos/sin of FP64-reduced angles)
+  bool ok = true;
+  for (int j = lane; j < s.D; j += 32) {
+    const double th = theta(j);
+    if (is_prismatic(t, j)) {
+      wqv[j] = (float)th;
+      ok &= fabs(th) <= (double)s.xy_max;
+      wcs[j] = make_float2(1.f, 0.f);
+    } else {
+      float a;
+      ok &= reduce_angle_f32(th, &a);
+      float sn, cs;
+      sincosf(a, &sn, &cs);
+      wcs[j] = make_float2(cs, sn);
+      wqv[j] = a;
+    }
+  }
+  // --- exact FP64 chain for pass 2 (joint values, cos/sin, centres)
+  double* wth64 = w64;
+  double* wcs64 = w64 + ((s.D + 1) & ~1);
+  double* wc64 = wcs64 + 2 * s.D;
+  if (RESOLVE) {
+    for (int j = lane; j < s.D; j += 32) {
+      const double th = theta(j);
+      wth64[j] = th;
+      double sn, cs;
+      sincos_exact(th, &sn, &cs);
+      wcs64[2 * j] = cs;
+      wcs64[2 * j + 1] = sn;
+    }
+  }
+  const bool all_ok = __all_sync(MRMG_FULL, ok);
+  if (!RESOLVE && !all_ok) return V_PENDING;
+  __syncwarp();
+  if (RESOLVE) {
+#pragma unroll
+    for (int u = 0; u < GPL; u++) {
+      const int g = lane + 32 * u;
+      if (g < s.G) {
+        const int gi = t.grp[g];
+        double R[9], p[3];
+        chain64(s, wth64, wcs64, gi & 0xff, gi >> 8, R, p);
+        for (int v = 0; v < SPG; v++) {
+          const double* l = s.sph64 + (size_t)(g * SPG + v) * 5;
+          double* c = wc64 + (size_t)(g * SPG + v) * 3;
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+            c[i] = __dadd_rn(p[i], __dadd_rn(__dadd_rn(__dmul_rn(R[3 * i], l[0]), __dmul_rn(R[3 * i + 1], l[1])),
+                                             __dmul_rn(R[3 * i + 2], l[2])));
+        }
+      }
+    }
+    __syncwarp();
+    if (!all_ok) return exact_all_collide(s, wc64, lane) ? V_COLLIDE : V_FREE;
+  }
+
+  // --- FP32 chain + sphere centres of the owned groups
+  float cx[GPL][SPG], cy[GPL][SPG], cz[GPL][SPG], rh[GPL][SPG];
+#pragma unroll
+  for (int u = 0; u < GPL; u++) {
+    const int g = lane + 32 * u;
+    if (g < s.G) {
+      const int gi = t.grp[g];
+      float R[9], p[3];
+      chain32(s, t, wcs, wqv, gi & 0xff, gi >> 8, R, p);
+#pragma unroll
+      for (int v = 0; v < SPG; v++) {
+        const float4 l = t.sph[g * SPG + v];
+        const float4 bd = t.band[g * SPG + v];
+        float x = p[0] + (R[0] * l.x + R[1] * l.y + R[2] * l.z);
+        float y = p[1] + (R[3] * l.x + R[4] * l.y + R[5] * l.z);
+        float z = p[2] + (R[6] * l.x + R[7] * l.y + R[8] * l.z);
+        if (bd.y < 0.f) { x = kFar * (float)(g + 1); y = x; z = 0.f; }   // padding slot
+        cx[u][v] = x; cy[u][v] = y; cz[u][v] = z; rh[u][v] = bd.y;
+        wsph[g * SPG + v] = make_float4(x, y, z, bd.z);
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < SPG; v++) {
+        cx[u][v] = kFar * (float)(200 + lane); cy[u][v] = cx[u][v]; cz[u][v] = 0.f; rh[u][v] = -1.f;
+      }
+    }
+  }
+  __syncwarp();
+
+  bool unc = false;
+  // --- spheres against boxes
+  for (int b = 0; b < s.B; b++) {
+    const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
+    float umin = 3.0e38f;
+#pragma unroll
+    for (int u = 0; u < GPL; u++)
+#pragma unroll
+      for (int v = 0; v < SPG; v++) {
+        const float ex = fmaxf(fabsf(cx[u][v] - bc.x) - bh.x, 0.f);
+        const float ey = fmaxf(fabsf(cy[u][v] - bc.y) - bh.y, 0.f);
+        const float ez = fmaxf(fabsf(cz[u][v] - bc.z) - bh.z, 0.f);
+        umin = fminf(umin, fmaf(ez, ez, fmaf(ey, ey, fmaf(ex, ex, -rh[u][v]))));
+      }
+    if (__any_sync(MRMG_FULL, umin <= 0.f)) {
+      bool coll = false;
+      if (umin <= 0.f) {
+#pragma unroll
+        for (int u = 0; u < GPL; u++)
+#pragma unroll
+          for (int v = 0; v < SPG; v++) {
+            const int g = lane + 32 * u;
+            const float ex = fmaxf(fabsf(cx[u][v] - bc.x) - bh.x, 0.f);
+            const float ey = fmaxf(fabsf(cy[u][v] - bc.y) - bh.y, 0.f);
+            const float ez = fmaxf(fabsf(cz[u][v] - bc.z) - bh.z, 0.f);
+            const float ss = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+            if (ss <= rh[u][v]) {
+              const float4 bd = t.band[g * SPG + v];
+              if (ss < bd.x) coll = true;
+              else if (RESOLVE) {
+                const int slot = g * SPG + v;
+                coll |= exact_box_hit(wc64 + (size_t)slot * 3, s.box64 + (size_t)b * 6, s.sph64[(size_t)slot * 5 + 4]);
+              } else {
+                unc = true;
+              }
+            }
+          }
+      }
+      if (__any_sync(MRMG_FULL, coll)) return V_COLLIDE;
+    }
+  }
+
+  // --- spheres of different robots
+  const float d4 = 4.f * s.delta;
+  for (int base = 0; base < s.NP; base += 32) {
+    const int pi = base + lane;
+    float umin = 3.0e38f;
+    uint32_t pr = 0;
+    if (pi < s.NP) {
+      pr = t.pairs[pi];
+      const float4* A = wsph + (pr & 0xffff) * SPG;
+      const float4* Bq = wsph + (pr >> 16) * SPG;
+      float4 a[SPG];
+#pragma unroll
+      for (int v = 0; v < SPG; v++) a[v] = A[v];
+#pragma unroll
+      for (int w = 0; w < SPG; w++) {
+        const float4 bq = Bq[w];
+#pragma unroll
+        for (int v = 0; v < SPG; v++) {
+          const float dx = a[v].x - bq.x, dy = a[v].y - bq.y, dz = a[v].z - bq.z;
+          const float W = a[v].w + bq.w;
+          umin = fminf(umin, fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -W * W))));
+        }
+      }
+    }
+    if (__any_sync(MRMG_FULL, umin <= 0.f)) {
+      bool coll = false;
+      if (umin <= 0.f) {
+        const int ga = pr & 0xffff, gb = pr >> 16;
+        for (int w = 0; w < SPG; w++) {
+          const float4 bq = wsph[gb * SPG + w];
+          for (int v = 0; v < SPG; v++) {
+            const float4 aq = wsph[ga * SPG + v];
+            const float dx = aq.x - bq.x, dy = aq.y - bq.y, dz = aq.z - bq.z;
+            const float W = aq.w + bq.w;
+            const float ss = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            if (ss <= W * W) {
+              const float Wl = W - d4;
+              if (Wl > 0.f && ss < Wl * Wl) coll = true;
+              else if (RESOLVE) {
+                const int sa = ga * SPG + v, sb = gb * SPG + w;
+                coll |= exact_pair_hit(wc64 + (size_t)sa * 3, wc64 + (size_t)sb * 3,
+                                       s.sph64[(size_t)sa * 5 + 3], s.sph64[(size_t)sb * 5 + 3]);
+              } else {
+                unc = true;
+              }
+            }
+          }
+        }
+      }
+      if (__any_sync(MRMG_FULL, coll)) return V_COLLIDE;
+    }
+  }
+  if (RESOLVE) return V_FREE;
+  return __any_sync(MRMG_FULL, unc) ? V_PENDING : V_FREE;
+}
+
+__device__ __forceinline__ void warp_areas(const ArmDev& s, unsigned char* smem_base, size_t tbytes,
+                                           int wib, bool with64, float2** wcs, float** wqv,
+                                           float4** wsph, double** w64) {
+  size_t per = warp32_bytes(s) + (with64 ? warp64_bytes(s) : 0);
+  unsigned char* p = smem_base + tbytes + per * wib;
+  *wcs = (float2*)p; p += align16(sizeof(float2) * s.D);
+  *wqv = (float*)p; p += align16(sizeof(float) * s.D);
+  *wsph = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
+  *w64 = (double*)p;
+}
+
+// ---------------------------------------------------------------------------
+// Configurations (warp per configuration, configurations taken from a work
+// queue in chunks of kCfgChunk).
+// ---------------------------------------------------------------------------
+constexpr int kCfgChunk = 4;
+
+template <int GPL, int SPG, bool RESOLVE>
+__global__ void __launch_bounds__(256) arm_configs_kernel(ArmDev s, const void* q, int dtype, long long n,
+                                                          uint8_t* out, int* ctr, long long* pend) {
+  extern __shared__ __align__(16) unsigned char smem_arm[];
+  ArmSmem t;
+  stage_tables(s, smem_arm, &t);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float2* wcs; float* wqv; float4* wsph; double* w64;
+  warp_areas(s, smem_arm, table_bytes(s), wib, RESOLVE, &wcs, &wqv, &wsph, &w64);
+  const int D = s.D;
+  while (true) {
+    long long k0 = 0;
+    if (lane == 0) k0 = atomicAdd(&ctr[RESOLVE ? kCtrQueue2 : kCtrQueue], RESOLVE ? 1 : kCfgChunk);
+    k0 = __shfl_sync(MRMG_FULL, k0, 0);
+    const long long lim = RESOLVE ? (long long)ctr[kCtrPending] : n;
+    if (k0 >= lim) break;
+    const int cnt = RESOLVE ? 1 : (int)min((long long)kCfgChunk, lim - k0);
+    for (int c = 0; c < cnt; c++) {
+      const long long i = RESOLVE ? pend[k0] : k0 + c;
+      auto theta = [&](int j) { return ldq(q, dtype, i * D + j); };
+      uint8_t v = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, theta);
+      if (lane == 0) {
+        out[i] = v;
+        if (!RESOLVE && v == V_PENDING) {
+          int slot = atomicAdd(&ctr[kCtrPending], 1);
+          pend[slot] = i;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Edges (warp per edge from a work queue; the warp walks the reference's
+// binary-search order one configuration at a time and stops at the first
+// certain collision).
+// ---------------------------------------------------------------------------
+template <int GPL, int SPG, bool RESOLVE>
+__global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1, const void* q2, int dtype,
+                                                        long long n, double res, int incl,
+                                                        const long long* Np, long long N_start,
+                                                        long long N_max, uint8_t* out, int* ctr,
+                                                        long long* pend) {
+  extern __shared__ __align__(16) unsigned char smem_arm[];
+  ArmSmem t;
+  stage_tables(s, smem_arm, &t);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float2* wcs; float* wqv; float4* wsph; double* w64;
+  warp_areas(s, smem_arm, table_bytes(s), wib, RESOLVE, &wcs, &wqv, &wsph, &w64);
+  const int D = s.D;
+  constexpr int JPL = (kMaxArmDof + 31) / 32;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  long long stat_cfg = 0;
+
+  while (true) {
+    long long k = 0;
+    if (lane == 0) k = atomicAdd(&ctr[RESOLVE ? kCtrQueue2 : kCtrQueue], 1);
+    k = __shfl_sync(MRMG_FULL, k, 0);
+    long long e;
+    if (RESOLVE) {
+      if (k >= ctr[kCtrPending]) break;
+      e = pend[k];
+    } else {
+      if (k >= n) break;
+      e = k;
+    }
+    // endpoints in FP64 (lane l holds joints l, l+32, l+64)
+    double a1[JPL], dir[JPL];
+    double mloc = -1.0;
+    bool nan0 = false;
+#pragma unroll
+    for (int u = 0; u < JPL; u++) {
+      const int j = lane + 32 * u;
+      a1[u] = 0.0; dir[u] = 0.0;
+      if (j < D) {
+        const double a = ldq(q1, dtype, e * D + j), b = ldq(q2, dtype, e * D + j);
+        a1[u] = a; dir[u] = b;
+        const double v = fabs(__dsub_rn(a, b));
+        if (j == 0) nan0 = (v != v);
+        mloc = fmax(mloc, v);
+      }
+    }
+    long long N;
+    bool bad = false;
+    if (Np) {
+      N = Np[e];
+      bad = N < 0;
+    } else {
+      const double m = warp_max_d(mloc);
+      nan0 = __any_sync(MRMG_FULL, nan0);
+      const double tq = __ddiv_rn(m, res);
+      if (nan0 || !(tq < 9.0e15)) bad = true;
+      N = bad ? 2 : (long long)tq + 1;
+      if (N < 2) N = 2;
+    }
+    if (bad || N_start > N) {
+      if (lane == 0) { atomicOr(&ctr[kCtrErr], bad ? E_BAD_INPUT : E_N_START); out[e] = 0; }
+      __syncwarp();
+      continue;
+    }
+    const long long nmax = (N_max < 0 || N_max > N) ? N : N_max;
+    const double denom = (double)(N - 1);
+#pragma unroll
+    for (int u = 0; u < JPL; u++) dir[u] = __ddiv_rn(__dsub_rn(dir[u], a1[u]), denom);
+
+    BfsChunker ch;
+    ch.init(N);
+    long long v;
+    unsigned m;
+    long long pos0;
+    bool coll = false, pending = false;
+    while (!coll && ch.next(lane, &v, &m, &pos0)) {
+      if (pos0 >= nmax) break;
+      const long long my_pos = pos0 + __popc(m & lt_mask);
+      const bool active = v >= 0 && my_pos >= N_start && my_pos < nmax && (incl || (v != 0 && v != N - 1));
+      unsigned act = __ballot_sync(MRMG_FULL, active);
+      while (act) {
+        const int src = __ffs(act) - 1;
+        act &= act - 1;
+        const double di = (double)__shfl_sync(MRMG_FULL, v, src);
+        auto theta = [&](int j) {
+          // joint j lives in lane j % 32, slot j / 32 of that lane's registers;
+          // here every lane asks only for its own joints
+          const int u = j >> 5;
+          double a = 0.0, d = 0.0;
+#pragma unroll
+          for (int w = 0; w < JPL; w++)
+            if (w == u) { a = a1[w]; d = dir[w]; }
+          return __dadd_rn(a, __dmul_rn(d, di));
+        };
+        stat_cfg++;
+        const uint8_t code = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, theta);
+        if (code == V_COLLIDE) { coll = true; break; }
+        if (code == V_PENDING) pending = true;
+      }
+    }
+    if (lane == 0) {
+      const uint8_t r = coll ? V_COLLIDE : (pending ? V_PENDING : V_FREE);
+      out[e] = r;
+      if (!RESOLVE && r == V_PENDING) {
+        const int slot = atomicAdd(&ctr[kCtrPending], 1);
+        pend[slot] = e;
+      }
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && !RESOLVE) atomicAdd((unsigned long long*)&ctr[kCtrStat0], (unsigned long long)stat_cfg);
+}
+
+// sphere centres for the error-bound check: warp per configuration
+__global__ void arm_centers_kernel(ArmDev s, const void* q, int dtype, long long n, float* c32, double* c64) {
+  extern __shared__ __align__(16) unsigned char smem_arm[];
+  ArmSmem t;
+  stage_tables(s, smem_arm, &t);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float2* wcs; float* wqv; float4* wsph; double* w64;
+  warp_areas(s, smem_arm, table_bytes(s), wib, true, &wcs, &wqv, &wsph, &w64);
+  const int D = s.D;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (long long i = blockIdx.x * (blockDim.x >> 5) + wib; i < n; i += nw) {
+    for (int j = lane; j < D; j += 32) {
+      const double th = ldq(q, dtype, i * D + j);
+      if (is_prismatic(t, j)) { wqv[j] = (float)th; wcs[j] = make_float2(1.f, 0.f); }
+      else {
+        float a;
+        reduce_angle_f32(th, &a);
+        float sn, cs;
+        sincosf(a, &sn, &cs);
+        wcs[j] = make_float2(cs, sn);
+      }
+      w64[j] = th;
+      double sn, cs;
+      sincos_exact(th, &sn, &cs);
+      w64[((D + 1) & ~1) + 2 * j] = cs;
+      w64[((D + 1) & ~1) + 2 * j + 1] = sn;
+    }
+    __syncwarp();
+    for (int g = lane; g < s.G; g += 32) {
+      const int gi = t.grp[g];
+      float R[9], p[3];
+      chain32(s, t, wcs, wqv, gi & 0xff, gi >> 8, R, p);
+      double Rd[9], pd[3];
+      chain64(s, w64, w64 + ((D + 1) & ~1), gi & 0xff, gi >> 8, Rd, pd);
+      for (int v = 0; v < s.SPG; v++) {
+        const int slot = g * s.SPG + v;
+        const double* l = s.sph64 + (size_t)slot * 5;
+        if (l[3] < 0.0) continue;
+        const long long sid = slot;   // output is per slot; the host maps slots to spheres
+        const float4 lf = t.sph[slot];
+        if (c32) {
+          c32[(i * s.G * s.SPG + sid) * 3 + 0] = p[0] + (R[0] * lf.x + R[1] * lf.y + R[2] * lf.z);
+          c32[(i * s.G * s.SPG + sid) * 3 + 1] = p[1] + (R[3] * lf.x + R[4] * lf.y + R[5] * lf.z);
+          c32[(i * s.G * s.SPG + sid) * 3 + 2] = p[2] + (R[6] * lf.x + R[7] * lf.y + R[8] * lf.z);
+        }
+        if (c64) {
+          for (int k = 0; k < 3; k++)
+            c64[(i * s.G * s.SPG + sid) * 3 + k] =
+                __dadd_rn(pd[k], __dadd_rn(__dadd_rn(__dmul_rn(Rd[3 * k], l[0]), __dmul_rn(Rd[3 * k + 1], l[1])),
+                                           __dmul_rn(Rd[3 * k + 2], l[2])));
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// dispatch over the compiled (groups per lane, spheres per group) variants
+// ---------------------------------------------------------------------------
+template <bool RESOLVE>
+cudaError_t launch_configs(const ArmDev& s, int gpl, const void* q, int dtype, long long n, uint8_t* out,
+                           const CallScratch& sc, int grid, int warps, size_t smem, cudaStream_t st) {
+#define MRMG_ARM_CFG(G_, S_)                                                                       \
+  if (gpl == G_ && s.SPG == S_) {                                                                  \
+    auto k = arm_configs_kernel<G_, S_, RESOLVE>;                                                  \
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
+    k<<<grid, warps * 32, smem, st>>>(s, q, dtype, n, out, sc.ctr, sc.pend);                       \
+    return cudaGetLastError();                                                                     \
+  }
+  MRMG_ARM_CFG(1, 6)
+  MRMG_ARM_CFG(2, 5)
+  MRMG_ARM_CFG(4, 8)
+#undef MRMG_ARM_CFG
+  return cudaErrorInvalidValue;
+}
+
+template <bool RESOLVE>
+cudaError_t launch_edges(const ArmDev& s, int gpl, const void* q1, const void* q2, int dtype, long long n,
+                         double res, int incl, const long long* Np, long long N_start, long long N_max,
+                         uint8_t* out, const CallScratch& sc, int grid, int warps, size_t smem,
+                         cudaStream_t st) {
+#define MRMG_ARM_EDGE(G_, S_)                                                                      \
+  if (gpl == G_ && s.SPG == S_) {                                                                  \
+    auto k = arm_edges_kernel<G_, S_, RESOLVE>;                                                    \
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
+    k<<<grid, warps * 32, smem, st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out,     \
+                                      sc.ctr, sc.pend);                                            \
+    return cudaGetLastError();                                                                     \
+  }
+  MRMG_ARM_EDGE(1, 6)
+  MRMG_ARM_EDGE(2, 5)
+  MRMG_ARM_EDGE(4, 8)
+#undef MRMG_ARM_EDGE
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+int arm_supported_spg(int idx) {
+  static const int v[] = {6, 5, 8, -1};
+  return idx >= 0 && idx < 4 ? v[idx] : -1;
+}
+
+int arm_gpl_for_spg(int spg) { return spg == 6 ? 1 : spg == 5 ? 2 : spg == 8 ? 4 : 0; }
+
+static size_t smem_pass(const ArmDev& s, int warps, bool with64) {
+  return table_bytes(s) + (size_t)warps * (warp32_bytes(s) + (with64 ? warp64_bytes(s) : 0));
+}
+
+int arm_default_ctas_per_sm(const ArmDev& s, int warps) {
+  int gpl = arm_gpl_for_spg(s.SPG);
+  size_t smem = smem_pass(s, warps, false);
+  int blocks = 0;
+  cudaError_t err = cudaErrorInvalidValue;
+#define MRMG_OCC(G_, S_)                                                                           \
+  if (gpl == G_ && s.SPG == S_) {                                                                  \
+    auto k = arm_edges_kernel<G_, S_, false>;                                                      \
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k, warps * 32, smem);             \
+  }
+  MRMG_OCC(1, 6)
+  MRMG_OCC(2, 5)
+  MRMG_OCC(4, 8)
+#undef MRMG_OCC
+  if (err != cudaSuccess || blocks < 1) return 1;
+  return blocks;
+}
+
+cudaError_t arm_configs(const ArmDev& s, const void* q, int dtype, long long n, uint8_t* out,
+                        const CallScratch& sc, const LaunchShape& ls, cudaStream_t st) {
+  const int gpl = arm_gpl_for_spg(s.SPG);
+  const size_t smem1 = smem_pass(s, ls.warps, false);
+  long long want = (n + (long long)ls.warps * kCfgChunk - 1) / ((long long)ls.warps * kCfgChunk);
+  int grid = (int)std::max(1ll, std::min(want, (long long)ls.ctas));
+  cudaError_t e = launch_configs<false>(s, gpl, q, dtype, n, out, sc, grid, ls.warps, smem1, st);
+  if (e != cudaSuccess) return e;
+  const int w2 = 2;
+  return launch_configs<true>(s, gpl, q, dtype, n, out, sc, ls.num_sms, w2, smem_pass(s, w2, true), st);
+}
+
+cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype, long long n,
+                      double res, int incl, const long long* Np, long long N_start,
+                      long long N_max, uint8_t* out, const CallScratch& sc,
+                      const LaunchShape& ls, cudaStream_t st) {
+  const int gpl = arm_gpl_for_spg(s.SPG);
+  const size_t smem1 = smem_pass(s, ls.warps, false);
+  long long want = (n + ls.warps - 1) / ls.warps;
+  int grid = (int)std::max(1ll, std::min(want, (long long)ls.ctas));
+  cudaError_t e = launch_edges<false>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc,
+                                      grid, ls.warps, smem1, st);
+  if (e != cudaSuccess) return e;
+  const int w2 = 2;
+  return launch_edges<true>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc, ls.num_sms,
+                            w2, smem_pass(s, w2, true), st);
+}
+
+cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, float* c32, double* c64,
+                        cudaStream_t st) {
+  const int warps = 4;
+  size_t smem = smem_pass(s, warps, true);
+  cudaFuncSetAttribute(arm_centers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  long long want = (n + warps - 1) / warps;
+  int grid = (int)std::max(1ll, std::min(want, 4096ll));
+  arm_centers_kernel<<<grid, warps * 32, smem, st>>>(s, q, dtype, n, c32, c64);
+  return cudaGetLastError();
+}
+
+}  // namespace mrmg

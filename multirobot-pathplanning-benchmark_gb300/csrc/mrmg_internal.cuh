@@ -1,0 +1,104 @@
+// mrmg_internal.cuh -- scene tables as the kernels see them, and the host-side
+// launchers each translation unit provides to the C ABI layer (mrmg_api.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mrmg_common.cuh"
+
+namespace mrmg {
+
+constexpr int kMaxRobots = 16;
+constexpr int kMaxLinks = 8;
+constexpr int kMaxArmDof = 96;
+constexpr int kMaxAgents = 16;
+constexpr int kMaxAgentDim = 15;
+
+// ---------------------------------------------------------------------------
+// Abstract point-agent scene (problems/abstract_env.py:112-131).
+// ---------------------------------------------------------------------------
+struct AbstractDev {
+  int A, dim, D, nb, ns;
+  const int* agent_off;                         // [A]
+  // exact FP64 tables
+  const double *pair_thr, *r2, *box_lo, *box_hi, *sph_pos, *sph_thr;
+  // FP32 copies for the bulk pass
+  const float *r32, *pair_thr32, *box_lo32, *box_hi32, *sph_pos32, *sph_thr32;
+  float omax;       // max |coordinate| / threshold of any obstacle or agent radius
+  float delta_k;    // FP32 band per unit magnitude: 8 * dim * 2^-24
+};
+
+// ---------------------------------------------------------------------------
+// Sphere-arm scene.  Spheres are packed into groups of SPG slots; a group
+// holds spheres of one (robot, link) frame.  Padding slots never collide.
+// ---------------------------------------------------------------------------
+struct ArmDev {
+  int R, D, G, SPG, B, NP;
+  float delta;      // FP32 re-check band (metres)
+  float xy_max;     // planar base |x|,|y| beyond this -> exact path
+  int q_off[kMaxRobots], base_kind[kMaxRobots], nl[kMaxRobots];
+  uint32_t prismatic[3];   // bit j: joint j is a planar-base translation
+  // exact FP64 tables (global memory)
+  const double* base64;    // [R*12]
+  const double* dh64;      // [R*8*4]  a, d, cos(alpha), sin(alpha)
+  const double* sph64;     // [G*SPG*5] local xyz, radius, radius^2 (radius < 0: padding)
+  const double* box64;     // [B*6]    lo xyz, hi xyz
+  // FP32 tables (staged into shared memory)
+  const float4* base32;    // [R*3]    rows (r0, r1, r2, p_i)
+  const float4* dh32;      // [R*8]    a, d, cos(alpha), sin(alpha)
+  const float4* sph32;     // [G*SPG]  local xyz, radius
+  const float4* band32;    // [G*SPG]  rlo^2, rhi^2, r + delta, r - delta  (padding: -1,-1,0,0)
+  const float4* box32;     // [B*2]    centre xyz, half extents xyz
+  const int* grp;          // [G]      robot | link << 8
+  const uint32_t* pairs;   // [NP]     group a | group b << 16 (different robots)
+};
+
+// per-call scratch counters (device): [0] work queue, [1] pending count,
+// [2] error bits, [3] pass-two queue, [4..7] statistics
+constexpr int kCtrQueue = 0, kCtrPending = 1, kCtrErr = 2, kCtrQueue2 = 3, kCtrStat0 = 4;
+constexpr int kNumCtr = 8;
+
+struct CallScratch {
+  int* ctr;          // [kNumCtr]
+  long long* pend;   // pending item list
+  long long pend_cap;
+};
+
+struct LaunchShape {
+  int ctas, warps;   // persistent grid
+  int num_sms;
+};
+
+// host launchers ------------------------------------------------------------
+cudaError_t abstract_configs(const AbstractDev& s, const void* q, int dtype, long long n,
+                             uint8_t* out, const CallScratch& sc, const LaunchShape& ls,
+                             cudaStream_t st);
+cudaError_t abstract_edges(const AbstractDev& s, const void* q1, const void* q2, int dtype,
+                           long long n, double res, int incl, const long long* Np,
+                           long long N_start, long long N_max, uint8_t* out,
+                           const CallScratch& sc, const LaunchShape& ls, cudaStream_t st);
+
+cudaError_t arm_configs(const ArmDev& s, const void* q, int dtype, long long n, uint8_t* out,
+                        const CallScratch& sc, const LaunchShape& ls, cudaStream_t st);
+cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype, long long n,
+                      double res, int incl, const long long* Np, long long N_start,
+                      long long N_max, uint8_t* out, const CallScratch& sc,
+                      const LaunchShape& ls, cudaStream_t st);
+cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, float* c32,
+                        double* c64, cudaStream_t st);
+int arm_default_ctas_per_sm(const ArmDev& s, int warps);
+int arm_supported_spg(int idx);   // list of compiled SPG values, -1 at end
+int arm_gpl_for_spg(int spg);
+
+cudaError_t binary_indices(long long N, long long* out, cudaStream_t st);
+
+struct SliceTab {
+  int A, D, end_all;
+  int s[64], e[64];
+};
+cudaError_t dist_matrix(const double* qs, long long Q, const double* nodes, long long M, const SliceTab& t, int metric,
+                        double* out, int num_sms, cudaStream_t st);
+cudaError_t batch_cost(const double* a, const double* b, long long M, const SliceTab& t, int cmetric, int red, double w,
+                       int mode, double* out, int num_sms, cudaStream_t st);
+
+}  // namespace mrmg

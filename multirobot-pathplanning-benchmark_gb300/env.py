@@ -1,0 +1,180 @@
+"""Environment backends with the reference's plugin surface.
+
+``Gb300CollisionBackend`` implements the collision / cost methods of
+BaseProblem (problems/planning_env.py:1710-1982) on the device; a planner
+environment gets the GB300 backend by mixing it in before its mode logic,
+exactly where the reference's AbstractEnvironment / rai_env sit:
+
+    class my_env(SequenceMixin, Gb300CollisionBackend, BaseProblem): ...
+
+Two ready-made backends:
+
+* ``Gb300AbstractEnvironment`` -- AbstractEnvironment's scenes (spherical
+  point agents, Rectangle and Sphere obstacles, problems/abstract_env.py).
+* ``Gb300ArmEnvironment`` -- sphere-arm robots among boxes.
+
+Semantics (verdicts, N, index order, interpolation arithmetic, exceptions)
+follow abstract_env.py:255-354 and planning_env.py:1765-1881; the batched
+methods are additive.
+"""
+from __future__ import annotations
+
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from .collision import Gb300Scene
+from .configuration import Gb300Configuration, batch_config_cost as _batch_config_cost, config_cost as _config_cost
+from .scenes import AbstractScene, ArmScene
+
+
+def _state(q) -> np.ndarray:
+    if hasattr(q, "state"):
+        return np.asarray(q.state(), dtype=np.float64)
+    return np.asarray(q, dtype=np.float64)
+
+
+def _max_dist(q1: np.ndarray, q2: np.ndarray) -> float:
+    """config_dist(q1, q2, "max") (compute_abs_max_reduction, configuration.py:174-197)."""
+    d = q1 - q2
+    m = abs(d[0])
+    for v in np.abs(d[1:]):
+        if v > m:
+            m = v
+    return float(m)
+
+
+def _edge_N(q1: np.ndarray, q2: np.ndarray, resolution: float) -> int:
+    return max(2, int(_max_dist(q1, q2) / resolution) + 1)
+
+
+class Gb300CollisionBackend:
+    """Collision, edge, path and cost methods of BaseProblem on the GB300.
+
+    Subclasses set ``self._gb300`` (a Gb300Scene), ``collision_resolution``,
+    ``collision_tolerance``, ``cost_metric`` and ``cost_reduction``.
+    """
+
+    collision_resolution: float = 0.01
+    collision_tolerance: float = 0.01
+    cost_metric: str = "euclidean"
+    cost_reduction: str = "max"
+    _gb300: Gb300Scene
+
+    # --- single queries (planning_env.py:1724-1763) ------------------------
+    def is_collision_free(self, q, mode) -> bool:
+        if q is None:
+            raise ValueError
+        v = self._gb300.is_collision_free_batch(_state(q).reshape(1, -1))
+        return bool(v.item())
+
+    def is_edge_collision_free(self, q1, q2, mode, resolution: Optional[float] = None,
+                               tolerance: Optional[float] = None, include_endpoints: bool = False,
+                               N_start: int = 0, N_max: Optional[int] = None, N: Optional[int] = None) -> bool:
+        if resolution is None:
+            resolution = self.collision_resolution
+        a, b = _state(q1), _state(q2)
+        if N is not None and N_start > N:
+            raise AssertionError
+        v = self._gb300.is_edge_collision_free_batch(a.reshape(1, -1), b.reshape(1, -1), resolution,
+                                                     include_endpoints, None if N is None else [int(N)], N_start, N_max)
+        return bool(v.item())
+
+    def _batch_is_collision_free(self, qs: List, mode) -> bool:
+        """abstract_env.py:278-299: True iff every configuration is free."""
+        if len(qs) == 0:
+            return True
+        return bool(self.batch_is_collision_free(np.array([_state(q) for q in qs])).all())
+
+    # --- batched (additive) ------------------------------------------------
+    def batch_is_collision_free(self, qs, mode=None) -> np.ndarray:
+        """Per-configuration verdicts for an [n, D] array (or device tensor)."""
+        v = self._gb300.is_collision_free_batch(qs)
+        return v.bool().cpu().numpy() if not isinstance(qs, torch.Tensor) else v.bool()
+
+    def batch_is_edge_collision_free(self, q1s, q2s, mode=None, resolution: Optional[float] = None,
+                                     include_endpoints: bool = False, N=None) -> np.ndarray:
+        """Per-edge verdicts for [n, D] endpoint arrays (or device tensors)."""
+        if resolution is None:
+            resolution = self.collision_resolution
+        v = self._gb300.is_edge_collision_free_batch(q1s, q2s, resolution, include_endpoints, N)
+        return v.bool().cpu().numpy() if not isinstance(q1s, torch.Tensor) else v.bool()
+
+    # --- path check (planning_env.py:1765-1881), one batched pass ----------
+    def is_path_collision_free(self, path, binary_order: bool = True, resolution: Optional[float] = None,
+                               tolerance: Optional[float] = None, check_edges_in_order: bool = False,
+                               check_start_and_end: bool = True) -> bool:
+        """Same verdict as the reference: the vertices it checks (the first
+        only with check_start_and_end; the last always when checking edges in
+        order, else only with check_start_and_end) and the interior of every
+        edge.  The order of checks does not change a verdict, so all are
+        submitted at once."""
+        if resolution is None:
+            resolution = self.collision_resolution
+        P = len(path)
+        qs = np.array([_state(s.q) for s in path])
+        verts = list(range(1, P - 1))
+        if check_start_and_end and P >= 2:
+            verts = [0] + verts
+        if check_edges_in_order or check_start_and_end:
+            verts = verts + [P - 1]
+        if P == 1:
+            verts = [0] if (check_edges_in_order or check_start_and_end) else []
+        if verts and not self.batch_is_collision_free(qs[sorted(set(verts))]).all():
+            return False
+        if P >= 2 and not self.batch_is_edge_collision_free(qs[:-1], qs[1:], None, resolution, False).all():
+            return False
+        return True
+
+    # --- costs (abstract_env.py:238-253) -----------------------------------
+    def config_cost(self, start, end) -> float:
+        return _config_cost(start, end, self.cost_metric, self.cost_reduction)
+
+    def batch_config_cost(self, starts, ends, tmp_agent_slice=None) -> np.ndarray:
+        return _batch_config_cost(starts, ends, self.cost_metric, self.cost_reduction, tmp_agent_slice=tmp_agent_slice)
+
+    # --- sampling (planning_env.py:1697-1708) ------------------------------
+    def sample_config_uniform_in_limits(self):
+        q = np.random.uniform(low=self.limits[0, :], high=self.limits[1, :])
+        return self.start_pos.from_flat(q)
+
+
+class Gb300AbstractEnvironment(Gb300CollisionBackend):
+    """AbstractEnvironment (problems/abstract_env.py:112-131) on the GB300:
+    spherical agents among Rectangle and Sphere obstacles."""
+
+    def __init__(self, scene: AbstractScene, limits=None, start_pos=None, collision_resolution: float = 0.01,
+                 collision_tolerance: float = 0.01):
+        self.scene = scene
+        self.agent_radii = list(scene.agent_radii)
+        self.limits = limits if limits is not None else np.stack([np.full(scene.q_dim, -1.0), np.full(scene.q_dim, 1.0)])
+        sl = [tuple(map(int, s)) for s in scene.agent_slices]
+        self.start_pos = start_pos if start_pos is not None else Gb300Configuration(np.zeros(scene.q_dim), sl)
+        self.robots = [f"a{i + 1}" for i in range(len(sl))]
+        self.robot_dims = {r: e - s for r, (s, e) in zip(self.robots, sl)}
+        self.robot_idx = {r: list(range(s, e)) for r, (s, e) in zip(self.robots, sl)}
+        self.collision_resolution = collision_resolution
+        self.collision_tolerance = collision_tolerance
+        self.cost_metric = "euclidean"
+        self.cost_reduction = "max"
+        self._gb300 = Gb300Scene(scene)
+
+
+class Gb300ArmEnvironment(Gb300CollisionBackend):
+    """Sphere-arm robots (DH chains, optional planar bases) among boxes."""
+
+    def __init__(self, scene: ArmScene, collision_resolution: float = 0.05, collision_tolerance: float = 0.01,
+                 band: float = 0.0):
+        self.scene = scene
+        self.limits = scene.limits
+        sl = [tuple(map(int, s)) for s in scene.agent_slices()]
+        self.start_pos = Gb300Configuration(np.zeros(scene.q_dim), sl)
+        self.robots = [f"r{i}" for i in range(scene.n_robots)]
+        self.robot_dims = {r: e - s for r, (s, e) in zip(self.robots, sl)}
+        self.robot_idx = {r: list(range(s, e)) for r, (s, e) in zip(self.robots, sl)}
+        self.collision_resolution = collision_resolution
+        self.collision_tolerance = collision_tolerance
+        self.cost_metric = "euclidean"
+        self.cost_reduction = "max"
+        self._gb300 = Gb300Scene(scene, band=band)

@@ -1,0 +1,302 @@
+"""Generate the golden vectors in this folder by running the REFERENCE itself.
+
+Run in a container that has the reference checkout (it is not needed, and not
+read, anywhere else):
+
+    python tests/golden/make_golden.py /path/to/multirobot-pathplanning-benchmark
+
+The reference imports numba, matplotlib and robotic at module level; none is
+needed for the functions used here, so minimal stand-ins are put on sys.path:
+numba.jit/njit become identity decorators (the kernels then run in plain
+Python, i.e. in their written sequential IEEE order), matplotlib and robotic
+become empty modules.  The package parents are pre-seeded so that
+problems/__init__.py (which imports the rai scenes) is skipped.
+
+Outputs (numpy .npz, seeded, small):
+  binary_indices.npz     generate_binary_search_indices(N), N = 1..300 and a few large N
+  abstract_disc.npz      2 discs + 10 boxes: config / edge verdicts, edge call counts
+  abstract_test.npz      the reference's registered 'abstract.test' scene (sphere + box)
+  abstract_10d.npz       'abstract.center_rect_10d': 10-D agents
+  primitives3d.npz       Rectangle / Sphere collides_with_sphere in 3-D, incl. near-tangent
+  dist_cost.npz          batch_config_dist / batch_config_cost over several slicings
+  knn.npz                per-mode k nearest (argpartition + argsort, prm_graph.py:446-447)
+  known_answers.json     the reference tests' own known answers (tests/test.py)
+"""
+from __future__ import annotations
+
+import json
+import sys
+import tempfile
+import types
+from pathlib import Path
+
+import numpy as np
+
+OUT = Path(__file__).resolve().parent
+
+
+def import_reference(ref_root: Path):
+    src = ref_root / "src" / "multi_robot_multi_goal_planning"
+    stub_dir = Path(tempfile.mkdtemp(prefix="mrmg_stubs_"))
+    (stub_dir / "numba").mkdir()
+    (stub_dir / "numba" / "__init__.py").write_text(
+        "def jit(*a, **k):\n"
+        "    if a and callable(a[0]) and not k: return a[0]\n"
+        "    return lambda f: f\n"
+        "njit = jit\n"
+        "class _T:\n"
+        "    def __getitem__(self, k): return self\n"
+        "    def __call__(self, *a, **k): return self\n"
+        "float64 = _T(); int64 = _T(); boolean = _T(); prange = range\n"
+    )
+    (stub_dir / "matplotlib").mkdir()
+    (stub_dir / "matplotlib" / "__init__.py").write_text("")
+    (stub_dir / "matplotlib" / "pyplot.py").write_text("")
+    (stub_dir / "robotic").mkdir()
+    (stub_dir / "robotic" / "__init__.py").write_text("")
+    sys.path.insert(0, str(stub_dir))
+    for name, path in [
+        ("multi_robot_multi_goal_planning", src),
+        ("multi_robot_multi_goal_planning.problems", src / "problems"),
+        ("multi_robot_multi_goal_planning.problems.core", src / "problems" / "core"),
+    ]:
+        m = types.ModuleType(name)
+        m.__path__ = [str(path)]
+        sys.modules[name] = m
+    import importlib
+
+    pe = importlib.import_module("multi_robot_multi_goal_planning.problems.planning_env")
+    ae = importlib.import_module("multi_robot_multi_goal_planning.problems.abstract_env")
+    cf = importlib.import_module("multi_robot_multi_goal_planning.problems.core.configuration")
+    reg = importlib.import_module("multi_robot_multi_goal_planning.problems.core.registry")
+    return pe, ae, cf, reg
+
+
+class CallCounter:
+    def __init__(self, fn):
+        self.fn = fn
+        self.n = 0
+
+    def __call__(self, *a, **k):
+        self.n += 1
+        return self.fn(*a, **k)
+
+
+def disc_env(ae, reg, centers, half):
+    env = reg.get_env_by_name("abstract.test")
+    env.obstacles = [ae.Rectangle(centers[i], 2.0 * half[i]) for i in range(len(centers))]
+    env.agent_radii = [0.1, 0.1]
+    return env
+
+
+def near_tangent_disc_configs(rng, centers, half, n):
+    """Disc centres placed at distance 0.1 +- tiny from a box face or corner."""
+    out = []
+    for _ in range(n):
+        b = rng.integers(len(centers))
+        c, h = centers[b], half[b]
+        side = rng.integers(4)
+        eps = rng.choice([0.0, 1e-17, -1e-17, 1e-15, -1e-15, 1e-12, -1e-12, 1e-9, -1e-9])
+        t = rng.uniform(-1, 1)
+        if side == 0:
+            p = [c[0] + h[0] + 0.1 + eps, c[1] + t * h[1]]
+        elif side == 1:
+            p = [c[0] - h[0] - 0.1 - eps, c[1] + t * h[1]]
+        elif side == 2:
+            p = [c[0] + t * h[0], c[1] + h[1] + 0.1 + eps]
+        else:
+            p = [c[0] + t * h[0], c[1] - h[1] - 0.1 - eps]
+        other = rng.uniform(-1, 1, 2)
+        out.append(np.array(p + list(other)) if rng.random() < 0.5 else np.array(list(other) + p))
+    # agent - agent near 0.2 apart
+    for _ in range(n // 2):
+        a = rng.uniform(-0.5, 0.5, 2)
+        ang = rng.uniform(0, 2 * np.pi)
+        eps = rng.choice([0.0, 1e-16, -1e-16, 1e-12, -1e-12])
+        b = a + (0.2 + eps) * np.array([np.cos(ang), np.sin(ang)])
+        out.append(np.concatenate([a, b]))
+    return np.array(out)
+
+
+def main(ref_root: str):
+    pe, ae, cf, reg = import_reference(Path(ref_root))
+    Np = cf.NpConfiguration
+    rng = np.random.default_rng(20240601)
+
+    # --- binary search order -------------------------------------------------
+    Ns = list(range(1, 301)) + [511, 512, 513, 777, 1000, 1024, 2049]
+    flat = np.concatenate([np.array(pe.generate_binary_search_indices(N), dtype=np.int64) for N in Ns])
+    np.savez_compressed(OUT / "binary_indices.npz", Ns=np.array(Ns, dtype=np.int64), flat=flat)
+
+    # --- disc scene (2 discs r=0.1, 10 boxes) ----------------------------------
+    srng = np.random.default_rng(0)
+    centers = srng.uniform(-0.8, 0.8, (10, 2))
+    half = srng.uniform(0.05, 0.2, (10, 2))
+    env = disc_env(ae, reg, centers, half)
+    start = env.start_pos
+    configs = np.concatenate([rng.uniform(-1, 1, (3000, 4)), near_tangent_disc_configs(rng, centers, half, 1000)])
+    cfg_free = np.array([env.is_collision_free(start.from_flat(q), None) for q in configs], dtype=np.uint8)
+    q1 = rng.uniform(-1, 1, (400, 4))
+    q2 = rng.uniform(-1, 1, (400, 4))
+    # short edges too, so that some are free
+    q1s = rng.uniform(-1, 1, (400, 4))
+    q2s = q1s + rng.uniform(-0.05, 0.05, (400, 4))
+    Q1 = np.concatenate([q1, q1s])
+    Q2 = np.concatenate([q2, q2s])
+    variants = [dict(resolution=0.01), dict(resolution=0.01, include_endpoints=True),
+                dict(resolution=0.05, N_start=3, N_max=13), dict(resolution=0.02, N_start=10),
+                dict(resolution=0.1, include_endpoints=True, N_start=1, N_max=4)]
+    edge_out, edge_calls = [], []
+    counter = CallCounter(env.is_collision_free)
+    env.is_collision_free = counter
+    for v in variants:
+        outs, calls = [], []
+        for a, b in zip(Q1, Q2):
+            counter.n = 0
+            qa, qb = start.from_flat(a), start.from_flat(b)
+            N = int(cf.config_dist(qa, qb, "max") / v["resolution"]) + 1
+            N = max(2, N)
+            if v.get("N_start", 0) > N:
+                outs.append(255)
+                calls.append(-1)
+                continue
+            outs.append(int(env.is_edge_collision_free(qa, qb, None, **v)))
+            calls.append(counter.n)
+        edge_out.append(outs)
+        edge_calls.append(calls)
+    del env.is_collision_free
+    np.savez_compressed(
+        OUT / "abstract_disc.npz", centers=centers, half=half, configs=configs, config_free=cfg_free,
+        q1=Q1, q2=Q2, edge_free=np.array(edge_out, dtype=np.uint8), edge_calls=np.array(edge_calls, dtype=np.int64),
+        variants=json.dumps(variants),
+    )
+
+    # --- the reference's abstract.test scene (Sphere + Rectangle) -------------
+    env = reg.get_env_by_name("abstract.test")
+    start = env.start_pos
+    configs = rng.uniform(-2, 2, (3000, 4))
+    cfg_free = np.array([env.is_collision_free(start.from_flat(q), None) for q in configs], dtype=np.uint8)
+    q1 = rng.uniform(-2, 2, (300, 4))
+    q2 = q1 + rng.uniform(-0.4, 0.4, (300, 4))
+    e_free = np.array([env.is_edge_collision_free(start.from_flat(a), start.from_flat(b), None) for a, b in zip(q1, q2)],
+                      dtype=np.uint8)
+    obs = env.obstacles
+    np.savez_compressed(
+        OUT / "abstract_test.npz", configs=configs, config_free=cfg_free, q1=q1, q2=q2, edge_free=e_free,
+        sphere_pos=np.array([obs[0].pos]), sphere_radius=np.array([obs[0].radius]),
+        box_center=np.array([obs[1].center]), box_bounds=np.array([obs[1].bounds]),
+        resolution=env.collision_resolution,
+    )
+
+    # --- 10-D agents -----------------------------------------------------------
+    env = reg.get_env_by_name("abstract.center_rect_10d")
+    start = env.start_pos
+    configs = rng.uniform(-0.6, 0.6, (2000, 20))
+    cfg_free = np.array([env.is_collision_free(start.from_flat(q), None) for q in configs], dtype=np.uint8)
+    q1 = rng.uniform(-1, 1, (200, 20))
+    q2 = q1 + rng.uniform(-0.3, 0.3, (200, 20))
+    e_free = np.array([env.is_edge_collision_free(start.from_flat(a), start.from_flat(b), None, resolution=0.05)
+                       for a, b in zip(q1, q2)], dtype=np.uint8)
+    np.savez_compressed(OUT / "abstract_10d.npz", configs=configs, config_free=cfg_free, q1=q1, q2=q2,
+                        edge_free=e_free, box_center=env.obstacles[0].center, box_bounds=env.obstacles[0].bounds)
+
+    # --- 3-D primitives ------------------------------------------------------------
+    n = 8000
+    bc = rng.uniform(-1, 1, (n, 3))
+    bh = rng.uniform(0.02, 0.3, (n, 3))
+    sc = rng.uniform(-1.5, 1.5, (n, 3))
+    sr = rng.uniform(0.01, 0.2, n)
+    # half of them moved to within a hair of contact along one axis
+    for i in range(n // 2):
+        k = rng.integers(3)
+        sgn = rng.choice([-1.0, 1.0])
+        sc[i] = bc[i] + rng.uniform(-1, 1, 3) * bh[i]
+        sc[i, k] = bc[i, k] + sgn * (bh[i, k] + sr[i] + rng.choice([0.0, 1e-16, -1e-16, 1e-13, -1e-13]))
+    rect = np.array([ae.Rectangle(bc[i], 2.0 * bh[i]).collides_with_sphere(sc[i], float(sr[i])) for i in range(n)], dtype=np.uint8)
+    pa = rng.uniform(-1, 1, (n, 3))
+    ra = rng.uniform(0.01, 0.2, n)
+    rb = rng.uniform(0.01, 0.2, n)
+    dirs = rng.normal(size=(n, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    gap = rng.choice([0.0, 1e-16, -1e-16, 1e-13, -1e-13, 0.01, -0.01], n)
+    pb = pa + dirs * (ra + rb + gap)[:, None]
+    sph = np.array([ae.Sphere(pa[i], float(ra[i])).collides_with_sphere(pb[i], float(rb[i])) for i in range(n)], dtype=np.uint8)
+    np.savez_compressed(OUT / "primitives3d.npz", box_center=bc, box_half=bh, sphere_c=sc, sphere_r=sr, rect_hit=rect,
+                        pa=pa, ra=ra, pb=pb, rb=rb, sphere_hit=sph)
+
+    # --- distances / costs -----------------------------------------------------------
+    dd = {}
+    for tag, dims in [("2_2", [2, 2]), ("7_7", [7, 7]), ("3_3_3", [3, 3, 3]), ("2_5", [2, 5]), ("14", [14]), ("7x4", [7, 7, 7, 7])]:
+        D = sum(dims)
+        slices = [(sum(dims[:i]), sum(dims[:i + 1])) for i in range(len(dims))]
+        pt = rng.uniform(-np.pi, np.pi, D)
+        pts = rng.uniform(-np.pi, np.pi, (600, D))
+        q = Np(pt, slices)
+        dd[f"{tag}_pt"] = pt
+        dd[f"{tag}_pts"] = pts
+        dd[f"{tag}_slices"] = np.array(slices, dtype=np.int64)
+        for metric in ["euclidean", "sum_euclidean", "max_euclidean", "max"]:
+            dd[f"{tag}_dist_{metric}"] = cf.batch_config_dist(q, pts, metric)
+        for metric in ["euclidean", "max"]:
+            for red in ["max", "sum"]:
+                dd[f"{tag}_cost_{metric}_{red}"] = cf.batch_config_cost(q, pts, metric, red)
+                dd[f"{tag}_rowcost_{metric}_{red}"] = cf.batch_config_cost(pts[:300], pts[300:], metric, red,
+                                                                           tmp_agent_slice=np.array(slices))
+                dd[f"{tag}_pathcost_{metric}_{red}"] = cf.batch_config_cost(list(pts[:100]), None, metric, red,
+                                                                            tmp_agent_slice=np.array(slices))
+    np.savez_compressed(OUT / "dist_cost.npz", **dd)
+
+    # --- per-mode kNN (PRM selection) --------------------------------------------------
+    D = 28
+    slices = [(7 * i, 7 * i + 7) for i in range(4)]
+    sizes = [300, 120, 45, 9, 3]
+    nodes = np.concatenate([rng.normal(rng.uniform(-np.pi, np.pi, D), 0.3, (s, D)) for s in sizes])
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    Q = 64
+    qs = rng.uniform(-np.pi, np.pi, (Q, D))
+    qm = rng.integers(0, len(sizes), Q).astype(np.int32)
+    k = 10
+    res = {}
+    for metric in ["euclidean", "max_euclidean"]:
+        idx = np.full((Q, k), -1, dtype=np.int64)
+        for i in range(Q):
+            arr = nodes[off[qm[i]]:off[qm[i] + 1]]
+            dists = cf.batch_config_dist(Np(qs[i], slices), arr, metric)
+            kc = min(k, len(arr))
+            topk = np.argpartition(dists, kc - 1)[:kc]
+            topk = topk[np.argsort(dists[topk])]
+            idx[i, :kc] = topk
+        res[f"idx_{metric}"] = idx
+    np.savez_compressed(OUT / "knn.npz", nodes=nodes, mode_off=off, queries=qs, q_mode=qm, k=k,
+                        slices=np.array(slices, dtype=np.int64), **res)
+
+    # --- known answers from the reference's own tests (tests/test.py) -------------------
+    env = reg.get_env_by_name("abstract.test")
+    counter = CallCounter(env.is_collision_free)
+    a = env.start_pos.from_flat(np.array([-1, 0, 1, 1]))
+    b = env.start_pos.from_flat(np.array([-1, 1, 1, 0]))
+    c3 = env.start_pos.from_flat(np.array([-1, 2, 1, -1]))
+    ka = {"edge_free": bool(env.is_edge_collision_free(a, b, env.start_mode))}
+    env.is_collision_free = lambda q, m: (setattr(counter, "n", counter.n + 1) or True)
+    calls = []
+    for res_, inc in [(0.5, True), (0.5, False), (0.1, False), (0.1, True)]:
+        counter.n = 0
+        env.is_edge_collision_free(a, b, env.start_mode, resolution=res_, include_endpoints=inc)
+        calls.append(counter.n)
+    ka["edge_calls"] = calls
+    S = pe.State
+    path = [S(a, env.start_mode), S(b, env.start_mode), S(c3, env.start_mode)]
+    pcalls = []
+    for res_, order in [(0.5, True), (0.5, False), (0.1, True), (0.1, False)]:
+        counter.n = 0
+        env.is_path_collision_free(path, resolution=res_, check_edges_in_order=order)
+        pcalls.append(counter.n)
+    ka["path_calls"] = pcalls
+    del env.is_collision_free
+    ka["path_free"] = bool(env.is_path_collision_free(path, resolution=0.5))
+    (OUT / "known_answers.json").write_text(json.dumps(ka, indent=1))
+    print("golden vectors written to", OUT)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,45 @@
+"""The C ABI library loads (no GPU needed) and exports every symbol that
+include/mrmg_gb300.h declares, with a ctypes signature for each."""
+import re
+import subprocess
+from pathlib import Path
+
+from conftest import ROOT, pkg
+
+HEADER = ROOT / "include" / "mrmg_gb300.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mrmg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "mrmg_is_edge_collision_free_batch" in syms
+    assert len(syms) >= 15
+
+
+def test_library_exports_every_declared_symbol(cuda_lib):
+    lib_path = pkg("_lib").LIB_PATH
+    out = subprocess.run(["nm", "-D", "--defined-only", str(lib_path)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (mrmg_\w+)", out))
+    missing = [s for s in declared_symbols() if s not in exported]
+    assert not missing, missing
+    for s in declared_symbols():
+        assert hasattr(cuda_lib, s)
+
+
+def test_ctypes_signatures_cover_header():
+    assert sorted(pkg("_lib").SIGNATURES) == declared_symbols()
+
+
+def test_version_and_error_without_gpu(cuda_lib):
+    assert b"sm_103a" in cuda_lib.mrmg_version()
+    _lib = pkg("_lib")
+    # argument validation happens before any device call
+    assert cuda_lib.mrmg_scene_destroy(None) == 0
+    rc = cuda_lib.mrmg_is_collision_free_batch(None, None, 0, 1, None, None, 0)
+    assert rc == _lib.MRMG_ERR_ARG
+    assert b"NULL" in cuda_lib.mrmg_last_error() or b"scene" in cuda_lib.mrmg_last_error()

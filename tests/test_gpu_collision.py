@@ -1,0 +1,144 @@
+"""GPU parity: the CUDA collision path against the golden vectors of the
+reference and against the oracle.  Verdicts and indices must be bit-exact."""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import golden, pkg
+
+pytestmark = pytest.mark.gpu
+
+
+def _disc_scene(g):
+    return pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=g["centers"],
+        box_bounds=2.0 * g["half"], sphere_pos=np.zeros((0, 2)), sphere_radius=[], q_dim=4)
+
+
+def test_binary_order_on_device(gpu):
+    col = pkg("collision")
+    g = golden("binary_indices.npz")
+    off = 0
+    for N in g["Ns"]:
+        ref = tuple(int(x) for x in g["flat"][off:off + N])
+        off += N
+        assert col.binary_search_indices(int(N)) == ref, N
+
+
+def test_disc_configs_golden(gpu):
+    g = golden("abstract_disc.npz")
+    sc = pkg("collision").Gb300Scene(_disc_scene(g))
+    for dt in (np.float64,):
+        v = sc.is_collision_free_batch(g["configs"].astype(dt)).cpu().numpy()
+        assert np.array_equal(v, g["config_free"])
+
+
+def test_disc_edges_golden_all_variants(gpu):
+    g = golden("abstract_disc.npz")
+    sc = pkg("collision").Gb300Scene(_disc_scene(g))
+    variants = json.loads(str(g["variants"]))
+    for vi, v in enumerate(variants):
+        ref = g["edge_free"][vi]
+        ok = ref != 255
+        out = sc.is_edge_collision_free_batch(g["q1"][ok], g["q2"][ok], v["resolution"],
+                                              v.get("include_endpoints", False), None, v.get("N_start", 0),
+                                              v.get("N_max")).cpu().numpy()
+        assert np.array_equal(out, ref[ok]), vi
+        if (~ok).any():
+            with pytest.raises(AssertionError):
+                sc.is_edge_collision_free_batch(g["q1"][~ok], g["q2"][~ok], v["resolution"],
+                                                v.get("include_endpoints", False), None, v.get("N_start", 0),
+                                                v.get("N_max"))
+
+
+def test_disc_env_api_golden(gpu):
+    g = golden("abstract_disc.npz")
+    env = pkg("env").Gb300AbstractEnvironment(_disc_scene(g))
+    for i in range(0, 400, 37):
+        q = env.start_pos.from_flat(g["configs"][i])
+        assert env.is_collision_free(q, None) == bool(g["config_free"][i])
+    for e in range(0, 800, 53):
+        a, b = env.start_pos.from_flat(g["q1"][e]), env.start_pos.from_flat(g["q2"][e])
+        assert env.is_edge_collision_free(a, b, None) == bool(g["edge_free"][0, e])
+    with pytest.raises(ValueError):
+        env.is_collision_free(None, None)
+
+
+def test_abstract_test_scene_golden(gpu):
+    g = golden("abstract_test.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=g["box_center"],
+        box_bounds=g["box_bounds"], sphere_pos=g["sphere_pos"], sphere_radius=[float(g["sphere_radius"][0])], q_dim=4)
+    sc = pkg("collision").Gb300Scene(scene)
+    assert np.array_equal(sc.is_collision_free_batch(g["configs"]).cpu().numpy(), g["config_free"])
+    assert np.array_equal(sc.is_edge_collision_free_batch(g["q1"], g["q2"], float(g["resolution"])).cpu().numpy(),
+                          g["edge_free"])
+
+
+def test_known_answers_path(gpu):
+    """tests/test.py:50-58 and :93-105 of the reference: free edge and path."""
+    ka = golden("known_answers.json")
+    g = golden("abstract_test.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=g["box_center"],
+        box_bounds=g["box_bounds"], sphere_pos=g["sphere_pos"], sphere_radius=[float(g["sphere_radius"][0])], q_dim=4)
+    env = pkg("env").Gb300AbstractEnvironment(scene, limits=np.array([[-2.0] * 4, [2.0] * 4]))
+    q1 = env.start_pos.from_flat(np.array([-1.0, 0, 1, 1]))
+    q2 = env.start_pos.from_flat(np.array([-1.0, 1, 1, 0]))
+    q3 = env.start_pos.from_flat(np.array([-1.0, 2, 1, -1]))
+    assert env.is_edge_collision_free(q1, q2, None) == ka["edge_free"]
+
+    class S:
+        def __init__(self, q):
+            self.q, self.mode = q, None
+
+    assert env.is_path_collision_free([S(q1), S(q2), S(q3)], resolution=0.5) == ka["path_free"]
+
+
+def test_abstract_10d_golden(gpu):
+    g = golden("abstract_10d.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 10], [10, 20]]), agent_radii=[0.1, 0.1], box_center=g["box_center"][None],
+        box_bounds=g["box_bounds"][None], sphere_pos=np.zeros((0, 10)), sphere_radius=[], q_dim=20)
+    sc = pkg("collision").Gb300Scene(scene)
+    assert np.array_equal(sc.is_collision_free_batch(g["configs"]).cpu().numpy(), g["config_free"])
+    assert np.array_equal(sc.is_edge_collision_free_batch(g["q1"], g["q2"], 0.05).cpu().numpy(), g["edge_free"])
+
+
+def test_primitives_3d_golden(gpu):
+    g = golden("primitives3d.npz")
+    scenes, col = pkg("scenes"), pkg("collision")
+    for i in list(range(0, 200)) + list(range(4000, 4100)):
+        s = scenes.AbstractScene(np.array([[0, 3]]), [float(g["sphere_r"][i])], g["box_center"][i][None],
+                                 2.0 * g["box_half"][i][None], np.zeros((0, 3)), [], 3)
+        v = col.Gb300Scene(s).is_collision_free_batch(g["sphere_c"][i][None]).item()
+        assert v == (0 if g["rect_hit"][i] else 1), i
+        s2 = scenes.AbstractScene(np.array([[0, 3]]), [float(g["rb"][i])], np.zeros((0, 3)), np.zeros((0, 3)),
+                                  g["pa"][i][None], [float(g["ra"][i])], 3)
+        v2 = col.Gb300Scene(s2).is_collision_free_batch(g["pb"][i][None]).item()
+        assert v2 == (0 if g["sphere_hit"][i] else 1), i
+
+
+def test_disc_workload_vs_oracle(gpu, oracle):
+    scenes = pkg("scenes")
+    scene = scenes.make_disc_scene(0)
+    w = scenes.make_disc_workload(0)
+    sc = pkg("collision").Gb300Scene(scene)
+    o = oracle.OracleScene(scene)
+    assert np.array_equal(sc.is_collision_free_batch(w["configs"]).cpu().numpy(), o.configs_free(w["configs"]))
+    assert np.array_equal(sc.is_edge_collision_free_batch(w["q1"], w["q2"], 0.01).cpu().numpy(),
+                          o.edges_free(w["q1"], w["q2"], 0.01))
+
+
+def test_edge_errors(gpu):
+    g = golden("abstract_disc.npz")
+    sc = pkg("collision").Gb300Scene(_disc_scene(g))
+    q1 = np.array([[0.0, 0.0, 0.5, 0.5]])
+    q2 = np.array([[np.nan, 0.0, 0.5, 0.5]])
+    with pytest.raises(ValueError):          # int(nan) in the reference
+        sc.is_edge_collision_free_batch(q1, q2, 0.01)
+    with pytest.raises(AssertionError):      # N_start > N
+        sc.is_edge_collision_free_batch(q1, q1 + 0.001, 0.01, N_start=5)
+    # empty batch
+    assert sc.is_edge_collision_free_batch(np.zeros((0, 4)), np.zeros((0, 4)), 0.01).numel() == 0

@@ -1,0 +1,151 @@
+"""The oracle against the reference's own outputs (golden vectors generated by
+tests/golden/make_golden.py from the reference) -- the pin for every GPU parity
+test.  CPU only."""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import golden, pkg
+
+
+def test_binary_indices_known_answers(oracle):
+    # tests/test.py:36-47 of the reference
+    expect = {1: (0,), 2: (0, 1), 3: (1, 0, 2), 4: (1, 0, 2, 3), 5: (2, 0, 3, 1, 4)}
+    for n, e in expect.items():
+        assert oracle.binary_search_indices(n) == e
+        assert oracle.binary_search_indices_py(n) == e
+
+
+def test_binary_indices_golden(oracle):
+    g = golden("binary_indices.npz")
+    off = 0
+    for N in g["Ns"]:
+        ref = tuple(int(x) for x in g["flat"][off:off + N])
+        off += N
+        assert oracle.binary_search_indices(int(N)) == ref
+        if N <= 300:
+            assert oracle.binary_search_indices_py(int(N)) == ref
+
+
+def _disc_scene(g):
+    scenes = pkg("scenes")
+    return scenes.AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=g["centers"],
+        box_bounds=2.0 * g["half"], sphere_pos=np.zeros((0, 2)), sphere_radius=[], q_dim=4)
+
+
+def test_disc_scene_matches_generator():
+    g = golden("abstract_disc.npz")
+    s = pkg("scenes").make_disc_scene(0)
+    assert np.array_equal(s.box_center, g["centers"]) and np.array_equal(s.box_bounds, 2.0 * g["half"])
+
+
+def test_abstract_disc_configs(oracle):
+    g = golden("abstract_disc.npz")
+    o = oracle.OracleScene(_disc_scene(g))
+    assert np.array_equal(o.configs_free(g["configs"]), g["config_free"])
+
+
+def test_abstract_disc_edges_and_call_counts(oracle):
+    g = golden("abstract_disc.npz")
+    o = oracle.OracleScene(_disc_scene(g))
+    variants = json.loads(str(g["variants"]))
+    for vi, v in enumerate(variants):
+        for e in range(len(g["q1"])):
+            ref = int(g["edge_free"][vi, e])
+            if ref == 255:   # N_start > N: the reference asserts
+                with pytest.raises(ValueError):
+                    o.edge_free(g["q1"][e], g["q2"][e], count=True, **v)
+                continue
+            free, calls = o.edge_free(g["q1"][e], g["q2"][e], count=True, **v)
+            assert int(free) == ref, (vi, e)
+            assert calls == g["edge_calls"][vi, e], (vi, e)
+
+
+def test_abstract_test_scene(oracle):
+    g = golden("abstract_test.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=g["box_center"],
+        box_bounds=g["box_bounds"], sphere_pos=g["sphere_pos"], sphere_radius=[float(g["sphere_radius"][0])], q_dim=4)
+    o = oracle.OracleScene(scene)
+    assert np.array_equal(o.configs_free(g["configs"]), g["config_free"])
+    assert np.array_equal(o.edges_free(g["q1"], g["q2"], float(g["resolution"])), g["edge_free"])
+
+
+def test_abstract_10d(oracle):
+    g = golden("abstract_10d.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 10], [10, 20]]), agent_radii=[0.1, 0.1], box_center=g["box_center"][None],
+        box_bounds=g["box_bounds"][None], sphere_pos=np.zeros((0, 10)), sphere_radius=[], q_dim=20)
+    o = oracle.OracleScene(scene)
+    assert np.array_equal(o.configs_free(g["configs"]), g["config_free"])
+    assert np.array_equal(o.edges_free(g["q1"], g["q2"], 0.05), g["edge_free"])
+
+
+def test_primitives_3d(oracle):
+    g = golden("primitives3d.npz")
+    scenes = pkg("scenes")
+    n = len(g["rect_hit"])
+    for i in range(0, n, 7):
+        s = scenes.AbstractScene(np.array([[0, 3]]), [float(g["sphere_r"][i])], g["box_center"][i][None],
+                                 2.0 * g["box_half"][i][None], np.zeros((0, 3)), [], 3)
+        assert oracle.OracleScene(s).config_free(g["sphere_c"][i]) == (not g["rect_hit"][i]), i
+        s2 = scenes.AbstractScene(np.array([[0, 3]]), [float(g["rb"][i])], np.zeros((0, 3)), np.zeros((0, 3)),
+                                  g["pa"][i][None], [float(g["ra"][i])], 3)
+        assert oracle.OracleScene(s2).config_free(g["pb"][i]) == (not g["sphere_hit"][i]), i
+
+
+TAGS = ["2_2", "7_7", "3_3_3", "2_5", "14", "7x4"]
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_dist_cost(oracle, tag):
+    g = golden("dist_cost.npz")
+    pt, pts, sl = g[f"{tag}_pt"], g[f"{tag}_pts"], g[f"{tag}_slices"]
+    for metric in ["euclidean", "sum_euclidean", "max_euclidean", "max"]:
+        assert np.array_equal(oracle.batch_dist(pt, pts, sl, metric), g[f"{tag}_dist_{metric}"]), metric
+    for metric in ["euclidean", "max"]:
+        for red in ["max", "sum"]:
+            assert np.array_equal(oracle.batch_cost(pt, pts, sl, metric, red), g[f"{tag}_cost_{metric}_{red}"])
+            assert np.array_equal(oracle.batch_cost(pts[:300], pts[300:], sl, metric, red),
+                                  g[f"{tag}_rowcost_{metric}_{red}"])
+            assert np.array_equal(oracle.batch_cost(pts[:100], None, sl, metric, red),
+                                  g[f"{tag}_pathcost_{metric}_{red}"])
+
+
+def test_knn(oracle):
+    g = golden("knn.npz")
+    for metric in ["euclidean", "max_euclidean"]:
+        idx, _ = oracle.knn(g["queries"], g["q_mode"], g["nodes"], g["mode_off"], g["slices"], metric, int(g["k"]))
+        assert np.array_equal(idx, g[f"idx_{metric}"]), metric
+
+
+def test_known_answers_edge_calls(oracle):
+    """tests/test.py:61-90 of the reference: 3 / 1 / 9 / 11 calls."""
+    ka = golden("known_answers.json")
+    g = golden("abstract_test.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=g["box_center"],
+        box_bounds=g["box_bounds"], sphere_pos=g["sphere_pos"], sphere_radius=[float(g["sphere_radius"][0])], q_dim=4)
+    o = oracle.OracleScene(scene)
+    a, b = np.array([-1.0, 0, 1, 1]), np.array([-1.0, 1, 1, 0])
+    assert o.edge_free(a, b, 0.01) == ka["edge_free"]
+    # counting is_collision_free calls needs every check to pass: an empty scene
+    empty = pkg("scenes").AbstractScene(np.array([[0, 2], [2, 4]]), [0.0, 0.0], np.zeros((0, 2)), np.zeros((0, 2)),
+                                        np.zeros((0, 2)), [], 4)
+    oe = oracle.OracleScene(empty)
+    calls = [oe.edge_free(a, b, r, include_endpoints=inc, count=True)[1]
+             for r, inc in [(0.5, True), (0.5, False), (0.1, False), (0.1, True)]]
+    assert calls == ka["edge_calls"]
+
+
+def test_sincos_close_to_libm(oracle):
+    import math
+
+    xs = np.concatenate([np.linspace(-30, 30, 20001), [0.0, -0.0, math.pi, -math.pi, 1e6, 1e-300]])
+    for x in xs:
+        s, c = oracle.sincos(float(x))
+        assert abs(s - math.sin(x)) <= 4e-16 * max(1.0, abs(x) / 8) and abs(c - math.cos(x)) <= 4e-16 * max(1.0, abs(x) / 8)
+    assert all(math.isnan(v) for v in oracle.sincos(float("inf")))
+    assert all(math.isnan(v) for v in oracle.sincos(2.0 ** 31))
