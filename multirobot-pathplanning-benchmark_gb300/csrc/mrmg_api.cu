@@ -53,6 +53,9 @@ struct DevBlock {
 
 }  // namespace
 
+// work-queue counters are 32-bit: keep every batch well below 2^31
+constexpr long long kMaxBatch = (1ll << 31) - (1ll << 26);
+
 struct mrmg_scene {
   int kind = 0;   // 0 abstract, 1 arm
   int q_dim = 0;
@@ -429,6 +432,7 @@ int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype,
                                  void* stream, int32_t flags) {
   if (!sc) return fail(MRMG_ERR_ARG, "scene is NULL");
   if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
+  if (n > kMaxBatch) return fail(MRMG_ERR_ARG, "batch of %lld exceeds %lld items; split it", (long long)n, kMaxBatch);
   if (n == 0) return MRMG_OK;
   if (!d_q || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
   cudaStream_t st = (cudaStream_t)stream;
@@ -451,6 +455,7 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene* sc, const void* d_q1, const vo
   if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
   if (!d_N && !(resolution > 0.0)) return fail(MRMG_ERR_ARG, "resolution must be > 0");
   if (N_start < 0) return fail(MRMG_ERR_ARG, "N_start must be >= 0");
+  if (n > kMaxBatch) return fail(MRMG_ERR_ARG, "batch of %lld exceeds %lld items; split it", (long long)n, kMaxBatch);
   if (n == 0) return MRMG_OK;
   if (!d_q1 || !d_q2 || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
   cudaStream_t st = (cudaStream_t)stream;

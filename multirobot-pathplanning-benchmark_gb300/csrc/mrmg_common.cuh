@@ -135,6 +135,7 @@ struct BfsChunker {
   __device__ void init(long long n) { N = n; level = 0; slot = 0; emitted = 0; }
   __device__ bool next(int lane, long long* my_idx, unsigned* mask, long long* pos0) {
     while (emitted < N) {
+      if (level > 62) return false;   // unreachable for a correct midpoint tree; never loop forever
       long long lvl_slots = 1ll << level;
       if (slot >= lvl_slots) { level++; slot = 0; continue; }
       long long sl = slot + lane;
