@@ -55,8 +55,14 @@ enum {
 enum { MRMG_COST_EUCLIDEAN = 0, MRMG_COST_MAX = 1 };
 enum { MRMG_REDUCE_MAX = 0, MRMG_REDUCE_SUM = 1 };
 
-/* call flags */
-enum { MRMG_FLAG_ASYNC = 1 };
+/* call flags
+ *  MRMG_FLAG_ASYNC      return after enqueueing; the status of the device-side
+ *                       input checks is then not reported (graph capture)
+ *  MRMG_FLAG_FULL_EVAL  arm scenes: evaluate every interpolated configuration
+ *                       and every sphere pair without stopping at the first
+ *                       collision (same verdicts; used to measure the
+ *                       kernel's throughput against its roofline) */
+enum { MRMG_FLAG_ASYNC = 1, MRMG_FLAG_FULL_EVAL = 2 };
 
 const char *mrmg_version(void);
 const char *mrmg_last_error(void);
@@ -196,6 +202,15 @@ int mrmg_batch_config_cost(const double *d_starts, const double *d_ends, int64_t
                            const int64_t *h_slices, int32_t A, int32_t cost_metric,
                            int32_t reduction, double w, int32_t mode, double *d_out, void *stream,
                            int32_t flags);
+
+/* ------------------------------------------------------------------------ */
+/* Calibration                                                               */
+/* ------------------------------------------------------------------------ */
+
+/* Measured fused-multiply-add throughput of the device (precision 0 = FP32,
+ * 1 = FP64) in TFLOP/s: the roofline denominators of the collision (FP32
+ * pipe) and distance (FP64 pipe) kernels.  No counterpart in the reference. */
+int mrmg_microbench_fma(int32_t precision, int64_t iters, double *out_tflops, void *stream);
 
 #ifdef __cplusplus
 }

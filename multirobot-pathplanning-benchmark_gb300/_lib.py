@@ -22,6 +22,7 @@ MRMG_ERR_N_START = -5
 MRMG_F32 = 0
 MRMG_F64 = 1
 MRMG_FLAG_ASYNC = 1
+MRMG_FLAG_FULL_EVAL = 2
 
 METRICS = {"euclidean": 0, "sum_euclidean": 1, "max_euclidean": 2, "max": 3}
 COST_METRICS = {"euclidean": 0, "max": 1}
@@ -52,6 +53,7 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_binary_search_indices": (i32, [i64, vp, vp]),
     "mrmg_config_dist_matrix": (i32, [vp, i64, vp, i64, i32, vp, i32, i32, vp, vp, i32]),
     "mrmg_batch_config_cost": (i32, [vp, vp, i64, i32, vp, i32, i32, i32, f64, i32, vp, vp, i32]),
+    "mrmg_microbench_fma": (i32, [i32, i64, vp, vp]),
 }
 
 

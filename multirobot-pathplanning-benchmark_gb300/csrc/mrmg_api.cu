@@ -67,6 +67,7 @@ struct mrmg_scene {
   long long pend_cap = 0;
   int* h_ctr = nullptr;       // pinned mirror of the counters
   int ctas = 0, warps = 0;    // persistent launch shape (0 = automatic)
+  int occ_ctas_per_sm = 0;    // resident CTAs per SM of the first pass (8 warps)
   int num_sms = 0;
   int device = 0;
   double band = 0.0;
@@ -111,7 +112,7 @@ LaunchShape shape(mrmg_scene* sc) {
   ls.num_sms = sc->num_sms;
   ls.warps = sc->warps > 0 ? sc->warps : 8;
   if (sc->ctas > 0) ls.ctas = sc->ctas;
-  else if (sc->kind == 1) ls.ctas = sc->num_sms * arm_default_ctas_per_sm(sc->arm, ls.warps);
+  else if (sc->kind == 1) ls.ctas = sc->num_sms * std::max(1, sc->occ_ctas_per_sm * 8 / ls.warps);
   else ls.ctas = sc->num_sms * 8;
   return ls;
 }
@@ -384,6 +385,7 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   cudaError_t e = blk.upload(&sc->d_tables);
   if (e != cudaSuccess) { mrmg_scene_destroy(sc); return cuda_fail(e, "upload arm scene"); }
   sc->band = d.delta;
+  sc->occ_ctas_per_sm = arm_prepare(d, 8);
   sc->n_pairs_groups = (int64_t)pairs.size();
   sc->slot_to_sphere = slot_sphere;
   *out = sc;
@@ -443,7 +445,7 @@ int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype,
   CallScratch cs{sc->d_ctr, sc->d_pend, sc->pend_cap};
   LaunchShape ls = shape(sc);
   e = sc->kind == 0 ? abstract_configs(sc->ab, d_q, dtype, n, d_out, cs, ls, st)
-                    : arm_configs(sc->arm, d_q, dtype, n, d_out, cs, ls, st);
+                    : arm_configs(sc->arm, d_q, dtype, n, d_out, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
   if (e != cudaSuccess) return cuda_fail(e, "launch configs");
   return finish_call(sc, st, flags);
 }
@@ -469,7 +471,7 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene* sc, const void* d_q1, const vo
           ? abstract_edges(sc->ab, d_q1, d_q2, dtype, n, resolution, include_endpoints, (const long long*)d_N,
                            N_start, N_max, d_out, cs, ls, st)
           : arm_edges(sc->arm, d_q1, d_q2, dtype, n, resolution, include_endpoints, (const long long*)d_N, N_start,
-                      N_max, d_out, cs, ls, st);
+                      N_max, d_out, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
   if (e != cudaSuccess) return cuda_fail(e, "launch edges");
   return finish_call(sc, st, flags);
 }

@@ -236,8 +236,9 @@ __device__ bool exact_all_collide(const ArmDev& s, const double* wc64, int lane)
 // ---------------------------------------------------------------------------
 template <int GPL, int SPG, bool RESOLVE, class Theta>
 __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, float* wqv,
-                               float4* wsph, double* w64, int lane, Theta theta) {
+                               float4* wsph, double* w64, int lane, Theta theta, bool full) {
   __syncwarp();
+  bool hit_any = false;   // full evaluation: remember a collision instead of stopping
   // --- joint preprocessing (FP32 cos/sin of FP64-reduced angles)
   bool ok = true;
   for (int j = lane; j < s.D; j += 32) {
@@ -361,7 +362,10 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
             }
           }
       }
-      if (__any_sync(MRMG_FULL, coll)) return V_COLLIDE;
+      if (__any_sync(MRMG_FULL, coll)) {
+        if (!full) return V_COLLIDE;
+        hit_any = true;
+      }
     }
   }
 
@@ -414,9 +418,13 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
           }
         }
       }
-      if (__any_sync(MRMG_FULL, coll)) return V_COLLIDE;
+      if (__any_sync(MRMG_FULL, coll)) {
+        if (!full) return V_COLLIDE;
+        hit_any = true;
+      }
     }
   }
+  if (hit_any) return V_COLLIDE;
   if (RESOLVE) return V_FREE;
   return __any_sync(MRMG_FULL, unc) ? V_PENDING : V_FREE;
 }
@@ -440,7 +448,7 @@ constexpr int kCfgChunk = 4;
 
 template <int GPL, int SPG, bool RESOLVE>
 __global__ void __launch_bounds__(256) arm_configs_kernel(ArmDev s, const void* q, int dtype, long long n,
-                                                          uint8_t* out, int* ctr, long long* pend) {
+                                                          uint8_t* out, int* ctr, long long* pend, int full) {
   extern __shared__ __align__(16) unsigned char smem_arm[];
   ArmSmem t;
   stage_tables(s, smem_arm, &t);
@@ -459,7 +467,7 @@ __global__ void __launch_bounds__(256) arm_configs_kernel(ArmDev s, const void* 
     for (int c = 0; c < cnt; c++) {
       const long long i = RESOLVE ? pend[k0] : k0 + c;
       auto theta = [&](int j) { return ldq(q, dtype, i * D + j); };
-      uint8_t v = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, theta);
+      uint8_t v = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, theta, full != 0);
       if (lane == 0) {
         out[i] = v;
         if (!RESOLVE && v == V_PENDING) {
@@ -482,7 +490,7 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
                                                         long long n, double res, int incl,
                                                         const long long* Np, long long N_start,
                                                         long long N_max, uint8_t* out, int* ctr,
-                                                        long long* pend) {
+                                                        long long* pend, int full) {
   extern __shared__ __align__(16) unsigned char smem_arm[];
   ArmSmem t;
   stage_tables(s, smem_arm, &t);
@@ -552,7 +560,7 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
     unsigned m;
     long long pos0;
     bool coll = false, pending = false;
-    while (!coll && ch.next(lane, &v, &m, &pos0)) {
+    while (ch.next(lane, &v, &m, &pos0)) {
       if (pos0 >= nmax) break;
       const long long my_pos = pos0 + __popc(m & lt_mask);
       const bool active = v >= 0 && my_pos >= N_start && my_pos < nmax && (incl || (v != 0 && v != N - 1));
@@ -572,10 +580,14 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
           return __dadd_rn(a, __dmul_rn(d, di));
         };
         stat_cfg++;
-        const uint8_t code = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, theta);
-        if (code == V_COLLIDE) { coll = true; break; }
+        const uint8_t code = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, theta, full != 0);
+        if (code == V_COLLIDE) {
+          coll = true;
+          if (!full) break;
+        }
         if (code == V_PENDING) pending = true;
       }
+      if (coll && !full) break;
     }
     if (lane == 0) {
       const uint8_t r = coll ? V_COLLIDE : (pending ? V_PENDING : V_FREE);
@@ -653,12 +665,11 @@ __global__ void arm_centers_kernel(ArmDev s, const void* q, int dtype, long long
 // ---------------------------------------------------------------------------
 template <bool RESOLVE>
 cudaError_t launch_configs(const ArmDev& s, int gpl, const void* q, int dtype, long long n, uint8_t* out,
-                           const CallScratch& sc, int grid, int warps, size_t smem, cudaStream_t st) {
+                           const CallScratch& sc, int grid, int warps, size_t smem, int full, cudaStream_t st) {
 #define MRMG_ARM_CFG(G_, S_)                                                                       \
   if (gpl == G_ && s.SPG == S_) {                                                                  \
     auto k = arm_configs_kernel<G_, S_, RESOLVE>;                                                  \
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
-    k<<<grid, warps * 32, smem, st>>>(s, q, dtype, n, out, sc.ctr, sc.pend);                       \
+    k<<<grid, warps * 32, smem, st>>>(s, q, dtype, n, out, sc.ctr, sc.pend, full);                 \
     return cudaGetLastError();                                                                     \
   }
   MRMG_ARM_CFG(1, 6)
@@ -671,14 +682,13 @@ cudaError_t launch_configs(const ArmDev& s, int gpl, const void* q, int dtype, l
 template <bool RESOLVE>
 cudaError_t launch_edges(const ArmDev& s, int gpl, const void* q1, const void* q2, int dtype, long long n,
                          double res, int incl, const long long* Np, long long N_start, long long N_max,
-                         uint8_t* out, const CallScratch& sc, int grid, int warps, size_t smem,
+                         uint8_t* out, const CallScratch& sc, int grid, int warps, size_t smem, int full,
                          cudaStream_t st) {
 #define MRMG_ARM_EDGE(G_, S_)                                                                      \
   if (gpl == G_ && s.SPG == S_) {                                                                  \
     auto k = arm_edges_kernel<G_, S_, RESOLVE>;                                                    \
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
     k<<<grid, warps * 32, smem, st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out,     \
-                                      sc.ctr, sc.pend);                                            \
+                                      sc.ctr, sc.pend, full);                                      \
     return cudaGetLastError();                                                                     \
   }
   MRMG_ARM_EDGE(1, 6)
@@ -701,58 +711,65 @@ static size_t smem_pass(const ArmDev& s, int warps, bool with64) {
   return table_bytes(s) + (size_t)warps * (warp32_bytes(s) + (with64 ? warp64_bytes(s) : 0));
 }
 
-int arm_default_ctas_per_sm(const ArmDev& s, int warps) {
-  int gpl = arm_gpl_for_spg(s.SPG);
-  size_t smem = smem_pass(s, warps, false);
+// Sets the dynamic shared-memory limit of every kernel of the scene's variant
+// (once, at scene creation, so that later calls can be captured in a graph)
+// and returns the resident CTAs per SM of the first-pass edge kernel.
+int arm_prepare(const ArmDev& s, int warps) {
+  const int gpl = arm_gpl_for_spg(s.SPG);
+  const int s1 = (int)smem_pass(s, 8, false), s2 = (int)smem_pass(s, 2, true);
+  const int s3 = (int)smem_pass(s, 4, true);
   int blocks = 0;
   cudaError_t err = cudaErrorInvalidValue;
-#define MRMG_OCC(G_, S_)                                                                           \
+#define MRMG_PREP(G_, S_)                                                                          \
   if (gpl == G_ && s.SPG == S_) {                                                                  \
-    auto k = arm_edges_kernel<G_, S_, false>;                                                      \
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k, warps * 32, smem);             \
+    cudaFuncSetAttribute(arm_edges_kernel<G_, S_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1); \
+    cudaFuncSetAttribute(arm_edges_kernel<G_, S_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s2);  \
+    cudaFuncSetAttribute(arm_configs_kernel<G_, S_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1); \
+    cudaFuncSetAttribute(arm_configs_kernel<G_, S_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s2);  \
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, arm_edges_kernel<G_, S_, false>, warps * 32, \
+                                                        smem_pass(s, warps, false));              \
   }
-  MRMG_OCC(1, 6)
-  MRMG_OCC(2, 5)
-  MRMG_OCC(4, 8)
-#undef MRMG_OCC
+  MRMG_PREP(1, 6)
+  MRMG_PREP(2, 5)
+  MRMG_PREP(4, 8)
+#undef MRMG_PREP
+  cudaFuncSetAttribute(arm_centers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, s3);
   if (err != cudaSuccess || blocks < 1) return 1;
   return blocks;
 }
 
 cudaError_t arm_configs(const ArmDev& s, const void* q, int dtype, long long n, uint8_t* out,
-                        const CallScratch& sc, const LaunchShape& ls, cudaStream_t st) {
+                        const CallScratch& sc, const LaunchShape& ls, int full, cudaStream_t st) {
   const int gpl = arm_gpl_for_spg(s.SPG);
   const size_t smem1 = smem_pass(s, ls.warps, false);
   long long want = (n + (long long)ls.warps * kCfgChunk - 1) / ((long long)ls.warps * kCfgChunk);
   int grid = (int)std::max(1ll, std::min(want, (long long)ls.ctas));
-  cudaError_t e = launch_configs<false>(s, gpl, q, dtype, n, out, sc, grid, ls.warps, smem1, st);
+  cudaError_t e = launch_configs<false>(s, gpl, q, dtype, n, out, sc, grid, ls.warps, smem1, full, st);
   if (e != cudaSuccess) return e;
   const int w2 = 2;
-  return launch_configs<true>(s, gpl, q, dtype, n, out, sc, ls.num_sms, w2, smem_pass(s, w2, true), st);
+  return launch_configs<true>(s, gpl, q, dtype, n, out, sc, ls.num_sms, w2, smem_pass(s, w2, true), 0, st);
 }
 
 cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype, long long n,
                       double res, int incl, const long long* Np, long long N_start,
                       long long N_max, uint8_t* out, const CallScratch& sc,
-                      const LaunchShape& ls, cudaStream_t st) {
+                      const LaunchShape& ls, int full, cudaStream_t st) {
   const int gpl = arm_gpl_for_spg(s.SPG);
   const size_t smem1 = smem_pass(s, ls.warps, false);
   long long want = (n + ls.warps - 1) / ls.warps;
   int grid = (int)std::max(1ll, std::min(want, (long long)ls.ctas));
   cudaError_t e = launch_edges<false>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc,
-                                      grid, ls.warps, smem1, st);
+                                      grid, ls.warps, smem1, full, st);
   if (e != cudaSuccess) return e;
   const int w2 = 2;
   return launch_edges<true>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc, ls.num_sms,
-                            w2, smem_pass(s, w2, true), st);
+                            w2, smem_pass(s, w2, true), 0, st);
 }
 
 cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, float* c32, double* c64,
                         cudaStream_t st) {
   const int warps = 4;
   size_t smem = smem_pass(s, warps, true);
-  cudaFuncSetAttribute(arm_centers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   long long want = (n + warps - 1) / warps;
   int grid = (int)std::max(1ll, std::min(want, 4096ll));
   arm_centers_kernel<<<grid, warps * 32, smem, st>>>(s, q, dtype, n, c32, c64);

@@ -79,14 +79,14 @@ cudaError_t abstract_edges(const AbstractDev& s, const void* q1, const void* q2,
                            const CallScratch& sc, const LaunchShape& ls, cudaStream_t st);
 
 cudaError_t arm_configs(const ArmDev& s, const void* q, int dtype, long long n, uint8_t* out,
-                        const CallScratch& sc, const LaunchShape& ls, cudaStream_t st);
+                        const CallScratch& sc, const LaunchShape& ls, int full, cudaStream_t st);
 cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype, long long n,
                       double res, int incl, const long long* Np, long long N_start,
                       long long N_max, uint8_t* out, const CallScratch& sc,
-                      const LaunchShape& ls, cudaStream_t st);
+                      const LaunchShape& ls, int full, cudaStream_t st);
 cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, float* c32,
                         double* c64, cudaStream_t st);
-int arm_default_ctas_per_sm(const ArmDev& s, int warps);
+int arm_prepare(const ArmDev& s, int warps);
 int arm_supported_spg(int idx);   // list of compiled SPG values, -1 at end
 int arm_gpl_for_spg(int spg);
 

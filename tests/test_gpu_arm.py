@@ -130,21 +130,24 @@ def test_near_contact_sphere_box(gpu, oracle):
 
 
 def test_near_contact_sphere_sphere(gpu, oracle):
-    """Robot 1 translated so that one of its spheres touches a sphere of robot
-    0 at distance r0 + r1 + eps."""
+    """Robot 1 translated towards its closest sphere pair (a on another robot,
+    b on robot 1) until that pair is at distance r_a + r_b + eps; every other
+    pair involving robot 1 keeps a gap >= eps."""
     scenes, col = pkg("scenes"), pkg("collision")
     base = sparse_arm_scene(3, n_boxes=0)
     o0 = oracle.OracleScene(base)
     qs = _free_configs(o0, base, 24, 13)
-    rng = np.random.default_rng(6)
     eps_set = [-1e-5, -1e-9, -1e-14, 0.0, 1e-14, 1e-9, 1e-5]
-    ids0 = np.where(base.sphere_robot == 0)[0]
     ids1 = np.where(base.sphere_robot == 1)[0]
+    ids_o = np.where(base.sphere_robot != 1)[0]
+    rad = base.sphere_radius
     rechecked = 0
     for i, q in enumerate(qs):
         c = o0.sphere_centers(q)
-        a, b = rng.choice(ids0), rng.choice(ids1)
-        R = base.sphere_radius[a] + base.sphere_radius[b] + eps_set[i % len(eps_set)]
+        gaps = np.linalg.norm(c[ids_o][:, None] - c[ids1][None], axis=-1) - (rad[ids_o][:, None] + rad[ids1][None])
+        ia, ib = np.unravel_index(np.argmin(gaps), gaps.shape)
+        a, b = ids_o[ia], ids1[ib]
+        R = rad[a] + rad[b] + eps_set[i % len(eps_set)]
         d = c[b] - c[a]
         u = d / np.linalg.norm(d)
         shift = (c[a] + u * R) - c[b]
