@@ -381,15 +381,39 @@ def _profile_traffic():
     return None
 
 
+def run_profile(args):
+    """Short run for ncu: the first-pass edge kernel on the benchmark workload,
+    early-exit ('early') or full-evaluation ('full') mode, `--steps` launches."""
+    import torch
+
+    _lib, envm = pkg("_lib"), pkg("env")
+    scene, q1, q2, N = workload(0)
+    sc = envm.Gb300ArmEnvironment(scene, collision_resolution=RESOLUTION)._gb300
+    q1_d, q2_d = torch.from_numpy(q1).cuda(), torch.from_numpy(q2).cuda()
+    out = torch.empty(len(q1), dtype=torch.uint8, device="cuda")
+    flags = _lib.MRMG_FLAG_FULL_EVAL if args.profile == "full" else 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sc.is_edge_collision_free_batch(q1_d, q2_d, RESOLUTION, out=out, flags=flags)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "launches": args.steps, "s": time.perf_counter() - t0,
+                      "free": int(out.sum().item()), "stats": sc.last_call_stats()}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--plain-edges", type=int, default=2000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile", choices=["early", "full"], default=None,
+                    help="short run of the first-pass edge kernel for ncu captures")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -231,25 +231,84 @@ __device__ bool exact_all_collide(const ArmDev& s, const double* wc64, int lane)
 }
 
 // ---------------------------------------------------------------------------
-// Warp evaluation of one configuration.  `theta(j)` yields joint j in FP64.
+// Joint sources.  A source gives joint j of the configuration under test as a
+// double-float (pass 1, FP32 arithmetic only) and as the exact FP64 value the
+// reference computes (pass 2).  Every lane asks only for its own joints
+// j = lane + 32 u; their per-edge data live in that lane's registers.
+// ---------------------------------------------------------------------------
+constexpr int kJPL = (kMaxArmDof + 31) / 32;
+
+struct CfgSource {          // a stored configuration row
+  const void* q;
+  int dtype;
+  long long row;
+  int D;
+  __device__ void df(int j, float* h, float* l) const {
+    if (dtype == MRMG_F32) {
+      *h = ((const float*)q)[row * D + j];
+      *l = 0.f;
+    } else {
+      const double x = ((const double*)q)[row * D + j];
+      *h = (float)x;
+      *l = (float)__dsub_rn(x, (double)*h);
+    }
+  }
+  __device__ double f64(int j) const { return ldq(q, dtype, row * D + j); }
+};
+
+struct EdgeSourceDF {       // pass 1: q1 + (q2 - q1) * i / (N - 1) in double-float
+  float ah[kJPL], al[kJPL], dh[kJPL], dl[kJPL];
+  float fi, nm1, rn;
+  __device__ void df(int j, float* h, float* l) const {
+    const int u = j >> 5;
+    float a0 = 0.f, a1 = 0.f, d0 = 0.f, d1 = 0.f;
+#pragma unroll
+    for (int w = 0; w < kJPL; w++)
+      if (w == u) { a0 = ah[w]; a1 = al[w]; d0 = dh[w]; d1 = dl[w]; }
+    interp_df(a0, a1, d0, d1, fi, nm1, rn, h, l);
+  }
+  __device__ double f64(int) const { return 0.0; }
+};
+
+struct EdgeSource64 {       // pass 2: q1 + dir * i exactly as the reference (FP64)
+  double a1[kJPL], dir[kJPL];
+  double di;
+  __device__ double f64(int j) const {
+    const int u = j >> 5;
+    double a = 0.0, d = 0.0;
+#pragma unroll
+    for (int w = 0; w < kJPL; w++)
+      if (w == u) { a = a1[w]; d = dir[w]; }
+    return __dadd_rn(a, __dmul_rn(d, di));
+  }
+  __device__ void df(int j, float* h, float* l) const {
+    const double x = f64(j);
+    *h = (float)x;
+    *l = (float)__dsub_rn(x, (double)*h);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Warp evaluation of one configuration.
 // Returns V_COLLIDE, V_FREE, or (pass 1 only) V_PENDING; warp-uniform.
 // ---------------------------------------------------------------------------
-template <int GPL, int SPG, bool RESOLVE, class Theta>
+template <int GPL, int SPG, bool RESOLVE, class Src>
 __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, float* wqv,
-                               float4* wsph, double* w64, int lane, Theta theta, bool full) {
+                               float4* wsph, double* w64, int lane, const Src& src, bool full) {
   __syncwarp();
   bool hit_any = false;   // full evaluation: remember a collision instead of stopping
-  // --- joint preprocessing (FP32 cos/sin of FP64-reduced angles)
+  // --- joint preprocessing: FP32 cos/sin of angles reduced to [-pi, pi]
   bool ok = true;
   for (int j = lane; j < s.D; j += 32) {
-    const double th = theta(j);
+    float h, l;
+    src.df(j, &h, &l);
     if (is_prismatic(t, j)) {
-      wqv[j] = (float)th;
-      ok &= fabs(th) <= (double)s.xy_max;
+      wqv[j] = __fadd_rn(h, l);
+      ok &= fabsf(h) <= s.xy_max;
       wcs[j] = make_float2(1.f, 0.f);
     } else {
       float a;
-      ok &= reduce_angle_f32(th, &a);
+      ok &= reduce_df(h, l, &a);
       float sn, cs;
       sincosf(a, &sn, &cs);
       wcs[j] = make_float2(cs, sn);
@@ -260,9 +319,9 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
   double* wth64 = w64;
   double* wcs64 = w64 + ((s.D + 1) & ~1);
   double* wc64 = wcs64 + 2 * s.D;
-  if (RESOLVE) {
+  if constexpr (RESOLVE) {
     for (int j = lane; j < s.D; j += 32) {
-      const double th = theta(j);
+      const double th = src.f64(j);
       wth64[j] = th;
       double sn, cs;
       sincos_exact(th, &sn, &cs);
@@ -273,7 +332,7 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
   const bool all_ok = __all_sync(MRMG_FULL, ok);
   if (!RESOLVE && !all_ok) return V_PENDING;
   __syncwarp();
-  if (RESOLVE) {
+  if constexpr (RESOLVE) {
 #pragma unroll
     for (int u = 0; u < GPL; u++) {
       const int g = lane + 32 * u;
@@ -449,6 +508,7 @@ constexpr int kCfgChunk = 4;
 template <int GPL, int SPG, bool RESOLVE>
 __global__ void __launch_bounds__(256) arm_configs_kernel(ArmDev s, const void* q, int dtype, long long n,
                                                           uint8_t* out, int* ctr, long long* pend, int full) {
+  if (RESOLVE && ctr[kCtrPending] == 0) return;   // nothing was left undecided
   extern __shared__ __align__(16) unsigned char smem_arm[];
   ArmSmem t;
   stage_tables(s, smem_arm, &t);
@@ -466,8 +526,8 @@ __global__ void __launch_bounds__(256) arm_configs_kernel(ArmDev s, const void* 
     const int cnt = RESOLVE ? 1 : (int)min((long long)kCfgChunk, lim - k0);
     for (int c = 0; c < cnt; c++) {
       const long long i = RESOLVE ? pend[k0] : k0 + c;
-      auto theta = [&](int j) { return ldq(q, dtype, i * D + j); };
-      uint8_t v = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, theta, full != 0);
+      const CfgSource src{q, dtype, i, D};
+      uint8_t v = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, src, full != 0);
       if (lane == 0) {
         out[i] = v;
         if (!RESOLVE && v == V_PENDING) {
@@ -491,6 +551,7 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
                                                         const long long* Np, long long N_start,
                                                         long long N_max, uint8_t* out, int* ctr,
                                                         long long* pend, int full) {
+  if (RESOLVE && ctr[kCtrPending] == 0) return;   // nothing was left undecided
   extern __shared__ __align__(16) unsigned char smem_arm[];
   ArmSmem t;
   stage_tables(s, smem_arm, &t);
@@ -499,7 +560,6 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
   float2* wcs; float* wqv; float4* wsph; double* w64;
   warp_areas(s, smem_arm, table_bytes(s), wib, RESOLVE, &wcs, &wqv, &wsph, &w64);
   const int D = s.D;
-  constexpr int JPL = (kMaxArmDof + 31) / 32;
   const unsigned lt_mask = (1u << lane) - 1u;
   long long stat_cfg = 0;
 
@@ -515,72 +575,123 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
       if (k >= n) break;
       e = k;
     }
-    // endpoints in FP64 (lane l holds joints l, l+32, l+64)
-    double a1[JPL], dir[JPL];
-    double mloc = -1.0;
-    bool nan0 = false;
+    // endpoints of this lane's joints j = lane + 32 u
+    EdgeSourceDF sdf;
+    EdgeSource64 s64;
+    float mloc = 0.f;
+    bool nanf = false;
 #pragma unroll
-    for (int u = 0; u < JPL; u++) {
+    for (int u = 0; u < kJPL; u++) {
       const int j = lane + 32 * u;
-      a1[u] = 0.0; dir[u] = 0.0;
+      sdf.ah[u] = 0.f; sdf.al[u] = 0.f; sdf.dh[u] = 0.f; sdf.dl[u] = 0.f;
+      s64.a1[u] = 0.0; s64.dir[u] = 0.0;
       if (j < D) {
-        const double a = ldq(q1, dtype, e * D + j), b = ldq(q2, dtype, e * D + j);
-        a1[u] = a; dir[u] = b;
-        const double v = fabs(__dsub_rn(a, b));
-        if (j == 0) nan0 = (v != v);
-        mloc = fmax(mloc, v);
+        if (dtype == MRMG_F32) {
+          const float a = ((const float*)q1)[e * D + j], b = ((const float*)q2)[e * D + j];
+          sdf.ah[u] = a;
+          two_sum(b, -a, &sdf.dh[u], &sdf.dl[u]);           // q2 - q1 exactly
+        } else {
+          const double a = ((const double*)q1)[e * D + j], b = ((const double*)q2)[e * D + j];
+          const double d = __dsub_rn(b, a);
+          sdf.ah[u] = (float)a;
+          sdf.al[u] = (float)__dsub_rn(a, (double)sdf.ah[u]);
+          sdf.dh[u] = (float)d;
+          sdf.dl[u] = (float)__dsub_rn(d, (double)sdf.dh[u]);
+        }
+        nanf |= sdf.dh[u] != sdf.dh[u];
+        mloc = fmaxf(mloc, fabsf(sdf.dh[u]));
       }
     }
-    long long N;
-    bool bad = false;
+    long long N = 0;
+    bool bad = false, decided = false;
     if (Np) {
       N = Np[e];
       bad = N < 0;
-    } else {
-      const double m = warp_max_d(mloc);
+      decided = true;
+    } else if (!RESOLVE) {
+      // int(max|q1 - q2| / resolution) in FP32 with an integer-distance
+      // certificate; close to an integer (or non-finite) -> FP64 below
+      const float m32 = warp_max(mloc);
+      const bool anynan = __any_sync(MRMG_FULL, nanf);
+      const float t32 = __fdiv_rn(m32, (float)res);
+      if (!anynan && t32 < 4194304.f) {
+        const float fl = floorf(t32);
+        const float fr = t32 - fl;
+        const float tol = 4.8e-7f * fmaxf(t32, 1.f);
+        if (fr > tol && fr < 1.f - tol) {
+          N = (long long)fl + 1;
+          decided = true;
+        }
+      }
+    }
+    if (!decided) {
+      // config_dist(q1, q2, "max") / resolution in FP64 (abstract_env.py:321-323)
+      double mx = -1.0;
+      bool nan0 = false;
+#pragma unroll
+      for (int u = 0; u < kJPL; u++) {
+        const int j = lane + 32 * u;
+        if (j < D) {
+          const double v = fabs(__dsub_rn(ldq(q1, dtype, e * D + j), ldq(q2, dtype, e * D + j)));
+          if (j == 0) nan0 = (v != v);
+          mx = fmax(mx, v);
+        }
+      }
+      const double m = warp_max_d(mx);
       nan0 = __any_sync(MRMG_FULL, nan0);
       const double tq = __ddiv_rn(m, res);
       if (nan0 || !(tq < 9.0e15)) bad = true;
       N = bad ? 2 : (long long)tq + 1;
-      if (N < 2) N = 2;
     }
+    if (!Np && N < 2) N = 2;
     if (bad || N_start > N) {
       if (lane == 0) { atomicOr(&ctr[kCtrErr], bad ? E_BAD_INPUT : E_N_START); out[e] = 0; }
       __syncwarp();
       continue;
     }
     const long long nmax = (N_max < 0 || N_max > N) ? N : N_max;
-    const double denom = (double)(N - 1);
+    bool pending = false;
+    if constexpr (RESOLVE) {
+      const double denom = (double)(N - 1);
 #pragma unroll
-    for (int u = 0; u < JPL; u++) dir[u] = __ddiv_rn(__dsub_rn(dir[u], a1[u]), denom);
+      for (int u = 0; u < kJPL; u++) {
+        const int j = lane + 32 * u;
+        if (j < D) {
+          const double a = ldq(q1, dtype, e * D + j), b = ldq(q2, dtype, e * D + j);
+          s64.a1[u] = a;
+          s64.dir[u] = __ddiv_rn(__dsub_rn(b, a), denom);   // (q2 - q1) / (N - 1)
+        }
+      }
+    } else {
+      sdf.nm1 = (float)(N - 1);
+      sdf.rn = __frcp_rn(sdf.nm1);
+      if (N > (1ll << 24)) pending = true;    // indices beyond FP32 integers: exact pass
+    }
 
     BfsChunker ch;
-    ch.init(N);
+    ch.init(pending ? 0 : N);
     long long v;
     unsigned m;
     long long pos0;
-    bool coll = false, pending = false;
+    bool coll = false;
     while (ch.next(lane, &v, &m, &pos0)) {
       if (pos0 >= nmax) break;
       const long long my_pos = pos0 + __popc(m & lt_mask);
       const bool active = v >= 0 && my_pos >= N_start && my_pos < nmax && (incl || (v != 0 && v != N - 1));
       unsigned act = __ballot_sync(MRMG_FULL, active);
       while (act) {
-        const int src = __ffs(act) - 1;
+        const int srcl = __ffs(act) - 1;
         act &= act - 1;
-        const double di = (double)__shfl_sync(MRMG_FULL, v, src);
-        auto theta = [&](int j) {
-          // joint j lives in lane j % 32, slot j / 32 of that lane's registers;
-          // here every lane asks only for its own joints
-          const int u = j >> 5;
-          double a = 0.0, d = 0.0;
-#pragma unroll
-          for (int w = 0; w < JPL; w++)
-            if (w == u) { a = a1[w]; d = dir[w]; }
-          return __dadd_rn(a, __dmul_rn(d, di));
-        };
+        const long long iv = __shfl_sync(MRMG_FULL, v, srcl);
         stat_cfg++;
-        const uint8_t code = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, theta, full != 0);
+        uint8_t code;
+        if constexpr (RESOLVE) {
+          s64.di = (double)iv;
+          code = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, s64, false);
+        } else {
+          sdf.fi = (float)iv;
+          code = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
+        }
         if (code == V_COLLIDE) {
           coll = true;
           if (!full) break;

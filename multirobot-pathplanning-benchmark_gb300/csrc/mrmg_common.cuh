@@ -72,6 +72,48 @@ __device__ __forceinline__ bool reduce_angle_f32(double x, float* out) {
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Double-float (hi + lo FP32 pair) helpers for the FP32 bulk path.  The
+// intrinsics keep nvcc from fusing the error-free transforms.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float* s, float* e) {
+  const float t = __fadd_rn(a, b);
+  const float bb = __fsub_rn(t, a);
+  *e = __fadd_rn(__fsub_rn(a, __fsub_rn(t, bb)), __fsub_rn(b, bb));
+  *s = t;
+}
+
+// Angle h + l reduced to [-pi, pi] with one final rounding to FP32
+// (2*pi = C1 + C2, C1 = fl32(2*pi); k*C1 split exactly with an FMA, h - k*C1
+// exact by Sterbenz).  False when |h| >= 2^14 (the exact path decides).
+__device__ __forceinline__ bool reduce_df(float h, float l, float* out) {
+  if (h != h || l != l) { *out = __fadd_rn(h, l); return true; }   // NaN never collides
+  if (!(fabsf(h) < 16384.f)) { *out = 0.f; return false; }
+  const float C1 = 0x1.921fb6p+2f, C2 = -0x1.777a5cp-23f, INV = 0x1.45f306p-3f;
+  const float k = rintf(__fmul_rn(h, INV));
+  const float p1h = __fmul_rn(k, C1);
+  const float p1l = fmaf(k, C1, -p1h);
+  const float sh = __fsub_rn(h, p1h);
+  const float t = fmaf(-k, C2, __fsub_rn(l, p1l));
+  *out = __fadd_rn(sh, t);
+  return true;
+}
+
+// theta = a + d * (i / nm1) for double-float a = (ah, al), d = (dh, dl);
+// rn ~ 1 / nm1.  Result (h, l) carries ~44 significant bits.
+__device__ __forceinline__ void interp_df(float ah, float al, float dh, float dl, float fi, float nm1, float rn,
+                                          float* h, float* l) {
+  const float th = __fmul_rn(fi, rn);
+  const float tl = __fmul_rn(fmaf(-th, nm1, fi), rn);
+  const float ph = __fmul_rn(dh, th);
+  float pl = fmaf(dh, th, -ph);
+  pl = fmaf(dh, tl, fmaf(dl, th, pl));
+  float sh, sl;
+  two_sum(ah, ph, &sh, &sl);
+  *h = sh;
+  *l = __fadd_rn(__fadd_rn(sl, pl), al);
+}
+
 // np.sum of up to 15 float64 values in numpy's pairwise order.
 template <int N>
 __device__ __forceinline__ double np_sum_small(const double* a) {
@@ -156,6 +198,12 @@ struct BfsChunker {
 __device__ __forceinline__ float warp_min(float v) {
 #pragma unroll
   for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(MRMG_FULL, v, o));
+  return v;
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(MRMG_FULL, v, o));
   return v;
 }
 
