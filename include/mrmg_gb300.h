@@ -172,8 +172,10 @@ int mrmg_last_call_stats(const mrmg_scene *scene, int64_t *out4);
 int mrmg_arm_slot_map(const mrmg_scene *scene, int32_t *out, int64_t cap);
 
 /* Device-side generate_binary_search_indices(N) (planning_env.py:34-51),
- * written to d_out[N] (int64).  Exposes the edge kernels' index order. */
-int mrmg_binary_search_indices(int64_t N, int64_t *d_out, void *stream);
+ * written to d_out[N] (int64): chunked = 0 uses the closed-form position map
+ * the parallel edge phases use, 1 the level-by-level iterator of the
+ * sequential walks.  Exposes the edge kernels' index order. */
+int mrmg_binary_search_indices(int64_t N, int64_t *d_out, int32_t chunked, void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Distances and costs (FP64, bit-identical to the reference)                */

@@ -50,7 +50,7 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_arm_sphere_centers": (i32, [vp, vp, i32, i64, vp, vp, vp]),
     "mrmg_last_call_stats": (i32, [vp, vp]),
     "mrmg_arm_slot_map": (i32, [vp, vp, i64]),
-    "mrmg_binary_search_indices": (i32, [i64, vp, vp]),
+    "mrmg_binary_search_indices": (i32, [i64, vp, i32, vp]),
     "mrmg_config_dist_matrix": (i32, [vp, i64, vp, i64, i32, vp, i32, i32, vp, vp, i32]),
     "mrmg_batch_config_cost": (i32, [vp, vp, i64, i32, vp, i32, i32, i32, f64, i32, vp, vp, i32]),
     "mrmg_microbench_fma": (i32, [i32, i64, vp, vp]),

@@ -177,9 +177,10 @@ class Gb300Scene:
         return c32[:, idx], c64[:, idx]
 
 
-def binary_search_indices(N: int) -> tuple:
-    """generate_binary_search_indices(N) computed by the device iterator."""
+def binary_search_indices(N: int, chunked: bool = False) -> tuple:
+    """generate_binary_search_indices(N) computed on the device (closed-form
+    position map, or the chunked level iterator)."""
     lib = _lib.load()
     out = torch.zeros(max(int(N), 1), dtype=torch.int64, device="cuda")
-    _lib.check(lib.mrmg_binary_search_indices(int(N), out.data_ptr(), _lib.stream_handle(None)))
+    _lib.check(lib.mrmg_binary_search_indices(int(N), out.data_ptr(), int(chunked), _lib.stream_handle(None)))
     return tuple(out[: int(N)].cpu().tolist())

@@ -64,6 +64,7 @@ struct mrmg_scene {
   void* d_tables = nullptr;
   int* d_ctr = nullptr;
   long long* d_pend = nullptr;
+  SurvivorEdge* d_surv = nullptr;
   long long pend_cap = 0;
   int* h_ctr = nullptr;       // pinned mirror of the counters
   int ctas = 0, warps = 0;    // persistent launch shape (0 = automatic)
@@ -97,12 +98,19 @@ int ensure_pending(mrmg_scene* sc, long long n, cudaStream_t st) {
     return fail(MRMG_ERR_ARG, "scratch for %lld items must be reserved before stream capture", n);
   long long cap_new = std::max(n, 2 * sc->pend_cap);
   long long* p = nullptr;
+  SurvivorEdge* sv = nullptr;
   cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
   e = cudaMalloc(&p, sizeof(long long) * cap_new);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(pending)");
+  if (sc->kind == 1) {
+    e = cudaMalloc(&sv, sizeof(SurvivorEdge) * cap_new);
+    if (e != cudaSuccess) { cudaFree(p); return cuda_fail(e, "cudaMalloc(survivors)"); }
+  }
   if (sc->d_pend) cudaFree(sc->d_pend);
+  if (sc->d_surv) cudaFree(sc->d_surv);
   sc->d_pend = p;
+  sc->d_surv = sv;
   sc->pend_cap = cap_new;
   return MRMG_OK;
 }
@@ -397,6 +405,7 @@ int mrmg_scene_destroy(mrmg_scene* sc) {
   if (sc->d_tables) cudaFree(sc->d_tables);
   if (sc->d_ctr) cudaFree(sc->d_ctr);
   if (sc->d_pend) cudaFree(sc->d_pend);
+  if (sc->d_surv) cudaFree(sc->d_surv);
   if (sc->h_ctr) cudaFreeHost(sc->h_ctr);
   delete sc;
   return MRMG_OK;
@@ -442,7 +451,7 @@ int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype,
   if (rc) return rc;
   cudaError_t e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
-  CallScratch cs{sc->d_ctr, sc->d_pend, sc->pend_cap};
+  CallScratch cs{sc->d_ctr, sc->d_pend, sc->d_surv, sc->pend_cap};
   LaunchShape ls = shape(sc);
   e = sc->kind == 0 ? abstract_configs(sc->ab, d_q, dtype, n, d_out, cs, ls, st)
                     : arm_configs(sc->arm, d_q, dtype, n, d_out, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
@@ -465,7 +474,7 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene* sc, const void* d_q1, const vo
   if (rc) return rc;
   cudaError_t e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
-  CallScratch cs{sc->d_ctr, sc->d_pend, sc->pend_cap};
+  CallScratch cs{sc->d_ctr, sc->d_pend, sc->d_surv, sc->pend_cap};
   LaunchShape ls = shape(sc);
   e = sc->kind == 0
           ? abstract_edges(sc->ab, d_q1, d_q2, dtype, n, resolution, include_endpoints, (const long long*)d_N,
@@ -568,11 +577,11 @@ int mrmg_batch_config_cost(const double* d_starts, const double* d_ends, int64_t
   return sync_unless_async(st, flags, "cost");
 }
 
-int mrmg_binary_search_indices(int64_t N, int64_t* d_out, void* stream) {
+int mrmg_binary_search_indices(int64_t N, int64_t* d_out, int32_t chunked, void* stream) {
   if (N < 0 || (N > 0 && !d_out)) return fail(MRMG_ERR_ARG, "N / out");
   if (N == 0) return MRMG_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = binary_indices(N, (long long*)d_out, st);
+  cudaError_t e = binary_indices(N, (long long*)d_out, st, chunked);
   if (e != cudaSuccess) return cuda_fail(e, "launch binary indices");
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, "binary indices kernel");
@@ -584,7 +593,15 @@ int mrmg_binary_search_indices(int64_t N, int64_t* d_out, void* stream) {
 // ---------------------------------------------------------------------------
 namespace mrmg {
 namespace {
+// position-parallel form (bfs_at), the one the edge kernels use to deal
+// positions to warps
 __global__ void binary_indices_kernel(long long N, long long* out) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x)
+    out[p] = bfs_at(N, p);
+}
+
+// warp-chunked form (BfsChunker), the one the sequential edge walks use
+__global__ void binary_indices_chunked_kernel(long long N, long long* out) {
   const int lane = threadIdx.x & 31;
   BfsChunker ch;
   ch.init(N);
@@ -596,8 +613,9 @@ __global__ void binary_indices_kernel(long long N, long long* out) {
   }
 }
 }  // namespace
-cudaError_t binary_indices(long long N, long long* out, cudaStream_t st) {
-  binary_indices_kernel<<<1, 32, 0, st>>>(N, out);
+cudaError_t binary_indices(long long N, long long* out, cudaStream_t st, int chunked) {
+  if (chunked) binary_indices_chunked_kernel<<<1, 32, 0, st>>>(N, out);
+  else binary_indices_kernel<<<(int)std::min<long long>((N + 255) / 256, 1024), 256, 0, st>>>(N, out);
   return cudaGetLastError();
 }
 }  // namespace mrmg

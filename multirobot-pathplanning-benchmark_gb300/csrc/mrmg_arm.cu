@@ -541,16 +541,97 @@ __global__ void __launch_bounds__(256) arm_configs_kernel(ArmDev s, const void* 
 }
 
 // ---------------------------------------------------------------------------
-// Edges (warp per edge from a work queue; the warp walks the reference's
-// binary-search order one configuration at a time and stops at the first
-// certain collision).
+// Edges.
+//   phase A  warp per edge (work queue): N, then the first BFS position of
+//            generate_binary_search_indices(N) that is checked; most edges of a
+//            cluttered scene stop here.  Survivors are appended to a list with
+//            their remaining position range.
+//   phase B  the survivors' remaining positions, position-major (all
+//            survivors' next position, then the one after, ...), dealt to every
+//            warp in blocks of 32; a collision marks the edge dead and its
+//            remaining positions are skipped.  Long free edges no longer run on
+//            one warp.
+//   finalize survivors' verdicts; undecided ones join the FP64 pending list.
+//   pass 2   (RESOLVE) warp per pending edge, the reference's order, exact.
 // ---------------------------------------------------------------------------
+
+// this lane's joints of edge e as double-floats: a = q1, d = q2 - q1
+__device__ __forceinline__ void load_edge(const void* q1, const void* q2, int dtype, long long e, int D, int lane,
+                                          EdgeSourceDF* sdf, float* mloc, bool* nanf) {
+  *mloc = 0.f;
+  *nanf = false;
+#pragma unroll
+  for (int u = 0; u < kJPL; u++) {
+    const int j = lane + 32 * u;
+    sdf->ah[u] = 0.f; sdf->al[u] = 0.f; sdf->dh[u] = 0.f; sdf->dl[u] = 0.f;
+    if (j < D) {
+      if (dtype == MRMG_F32) {
+        const float a = ((const float*)q1)[e * D + j], b = ((const float*)q2)[e * D + j];
+        sdf->ah[u] = a;
+        two_sum(b, -a, &sdf->dh[u], &sdf->dl[u]);           // q2 - q1 exactly
+      } else {
+        const double a = ((const double*)q1)[e * D + j], b = ((const double*)q2)[e * D + j];
+        const double d = __dsub_rn(b, a);
+        sdf->ah[u] = (float)a;
+        sdf->al[u] = (float)__dsub_rn(a, (double)sdf->ah[u]);
+        sdf->dh[u] = (float)d;
+        sdf->dl[u] = (float)__dsub_rn(d, (double)sdf->dh[u]);
+      }
+      *nanf |= sdf->dh[u] != sdf->dh[u];
+      *mloc = fmaxf(*mloc, fabsf(sdf->dh[u]));
+    }
+  }
+}
+
+// N of edge e: given, or max(2, int(max|q1 - q2| / res) + 1) -- FP32 with an
+// integer-distance certificate, else FP64 (abstract_env.py:321-323).
+// Returns false on a non-finite edge length (int() of nan/inf raises).
+__device__ __forceinline__ bool edge_N(const void* q1, const void* q2, int dtype, long long e, int D, int lane,
+                                       double res, const long long* Np, float mloc, bool nanf, bool allow_fast,
+                                       long long* N_out) {
+  if (Np) {
+    *N_out = Np[e];
+    return *N_out >= 0;
+  }
+  if (allow_fast) {
+    const float m32 = warp_max(mloc);
+    const bool anynan = __any_sync(MRMG_FULL, nanf);
+    const float t32 = __fdiv_rn(m32, (float)res);
+    if (!anynan && t32 < 4194304.f) {
+      const float fl = floorf(t32);
+      const float fr = t32 - fl;
+      const float tol = 4.8e-7f * fmaxf(t32, 1.f);
+      if (fr > tol && fr < 1.f - tol) {
+        *N_out = max(2ll, (long long)fl + 1);
+        return true;
+      }
+    }
+  }
+  double mx = -1.0;
+  bool nan0 = false;
+#pragma unroll
+  for (int u = 0; u < kJPL; u++) {
+    const int j = lane + 32 * u;
+    if (j < D) {
+      const double v = fabs(__dsub_rn(ldq(q1, dtype, e * D + j), ldq(q2, dtype, e * D + j)));
+      if (j == 0) nan0 = (v != v);
+      mx = fmax(mx, v);
+    }
+  }
+  const double m = warp_max_d(mx);
+  nan0 = __any_sync(MRMG_FULL, nan0);
+  const double tq = __ddiv_rn(m, res);
+  if (nan0 || !(tq < 9.0e15)) return false;
+  *N_out = max(2ll, (long long)tq + 1);
+  return true;
+}
+
 template <int GPL, int SPG, bool RESOLVE>
 __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1, const void* q2, int dtype,
                                                         long long n, double res, int incl,
                                                         const long long* Np, long long N_start,
                                                         long long N_max, uint8_t* out, int* ctr,
-                                                        long long* pend, int full) {
+                                                        long long* pend, SurvivorEdge* surv, int full) {
   if (RESOLVE && ctr[kCtrPending] == 0) return;   // nothing was left undecided
   extern __shared__ __align__(16) unsigned char smem_arm[];
   ArmSmem t;
@@ -575,142 +656,179 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
       if (k >= n) break;
       e = k;
     }
-    // endpoints of this lane's joints j = lane + 32 u
     EdgeSourceDF sdf;
-    EdgeSource64 s64;
-    float mloc = 0.f;
-    bool nanf = false;
-#pragma unroll
-    for (int u = 0; u < kJPL; u++) {
-      const int j = lane + 32 * u;
-      sdf.ah[u] = 0.f; sdf.al[u] = 0.f; sdf.dh[u] = 0.f; sdf.dl[u] = 0.f;
-      s64.a1[u] = 0.0; s64.dir[u] = 0.0;
-      if (j < D) {
-        if (dtype == MRMG_F32) {
-          const float a = ((const float*)q1)[e * D + j], b = ((const float*)q2)[e * D + j];
-          sdf.ah[u] = a;
-          two_sum(b, -a, &sdf.dh[u], &sdf.dl[u]);           // q2 - q1 exactly
-        } else {
-          const double a = ((const double*)q1)[e * D + j], b = ((const double*)q2)[e * D + j];
-          const double d = __dsub_rn(b, a);
-          sdf.ah[u] = (float)a;
-          sdf.al[u] = (float)__dsub_rn(a, (double)sdf.ah[u]);
-          sdf.dh[u] = (float)d;
-          sdf.dl[u] = (float)__dsub_rn(d, (double)sdf.dh[u]);
-        }
-        nanf |= sdf.dh[u] != sdf.dh[u];
-        mloc = fmaxf(mloc, fabsf(sdf.dh[u]));
-      }
-    }
+    float mloc;
+    bool nanf;
+    load_edge(q1, q2, dtype, e, D, lane, &sdf, &mloc, &nanf);
     long long N = 0;
-    bool bad = false, decided = false;
-    if (Np) {
-      N = Np[e];
-      bad = N < 0;
-      decided = true;
-    } else if (!RESOLVE) {
-      // int(max|q1 - q2| / resolution) in FP32 with an integer-distance
-      // certificate; close to an integer (or non-finite) -> FP64 below
-      const float m32 = warp_max(mloc);
-      const bool anynan = __any_sync(MRMG_FULL, nanf);
-      const float t32 = __fdiv_rn(m32, (float)res);
-      if (!anynan && t32 < 4194304.f) {
-        const float fl = floorf(t32);
-        const float fr = t32 - fl;
-        const float tol = 4.8e-7f * fmaxf(t32, 1.f);
-        if (fr > tol && fr < 1.f - tol) {
-          N = (long long)fl + 1;
-          decided = true;
-        }
-      }
-    }
-    if (!decided) {
-      // config_dist(q1, q2, "max") / resolution in FP64 (abstract_env.py:321-323)
-      double mx = -1.0;
-      bool nan0 = false;
-#pragma unroll
-      for (int u = 0; u < kJPL; u++) {
-        const int j = lane + 32 * u;
-        if (j < D) {
-          const double v = fabs(__dsub_rn(ldq(q1, dtype, e * D + j), ldq(q2, dtype, e * D + j)));
-          if (j == 0) nan0 = (v != v);
-          mx = fmax(mx, v);
-        }
-      }
-      const double m = warp_max_d(mx);
-      nan0 = __any_sync(MRMG_FULL, nan0);
-      const double tq = __ddiv_rn(m, res);
-      if (nan0 || !(tq < 9.0e15)) bad = true;
-      N = bad ? 2 : (long long)tq + 1;
-    }
-    if (!Np && N < 2) N = 2;
-    if (bad || N_start > N) {
-      if (lane == 0) { atomicOr(&ctr[kCtrErr], bad ? E_BAD_INPUT : E_N_START); out[e] = 0; }
+    const bool good = edge_N(q1, q2, dtype, e, D, lane, res, Np, mloc, nanf, !RESOLVE, &N);
+    if (!good || N_start > N) {
+      if (lane == 0) { atomicOr(&ctr[kCtrErr], !good ? E_BAD_INPUT : E_N_START); out[e] = 0; }
       __syncwarp();
       continue;
     }
     const long long nmax = (N_max < 0 || N_max > N) ? N : N_max;
-    bool pending = false;
-    if constexpr (RESOLVE) {
+
+    if constexpr (!RESOLVE) {
+      // ---- phase A: the first checked position
+      uint8_t r = V_FREE;
+      if (N > (1ll << 24)) {
+        r = V_PENDING;                      // indices beyond exact FP32 integers: exact pass
+      } else {
+        long long p = N_start, iv = -1;
+        for (; p < nmax; p++) {
+          const long long c = bfs_at(N, p);
+          if (incl || (c != 0 && c != N - 1)) { iv = c; break; }
+        }
+        if (iv >= 0) {
+          sdf.nm1 = (float)(N - 1);
+          sdf.rn = __frcp_rn(sdf.nm1);
+          sdf.fi = (float)iv;
+          stat_cfg++;
+          const uint8_t code = eval_config<GPL, SPG, false>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
+          if (code == V_COLLIDE && !full) {
+            r = V_COLLIDE;
+          } else if (p + 1 < nmax) {
+            if (lane == 0) {
+              const int slot = atomicAdd(&ctr[kCtrL1], 1);
+              SurvivorEdge sv;
+              sv.e = e; sv.N = (int)N; sv.p_next = (int)(p + 1); sv.nmax = (int)nmax;
+              sv.dead = code == V_COLLIDE; sv.pend = code == V_PENDING; sv.pad = 0;
+              surv[slot] = sv;
+              atomicMax(&ctr[kCtrMaxJ], (int)(nmax - p - 1));
+            }
+            __syncwarp();
+            continue;                       // phase B and the finalize kernel decide
+          } else {
+            r = code;
+          }
+        }
+      }
+      if (lane == 0) {
+        out[e] = r;
+        if (r == V_PENDING) {
+          const int slot = atomicAdd(&ctr[kCtrPending], 1);
+          pend[slot] = e;
+        }
+      }
+      __syncwarp();
+    } else {
+      // ---- pass 2: the reference's order, one configuration at a time, FP64 where pending
+      EdgeSource64 s64;
       const double denom = (double)(N - 1);
 #pragma unroll
       for (int u = 0; u < kJPL; u++) {
         const int j = lane + 32 * u;
+        s64.a1[u] = 0.0; s64.dir[u] = 0.0;
         if (j < D) {
           const double a = ldq(q1, dtype, e * D + j), b = ldq(q2, dtype, e * D + j);
           s64.a1[u] = a;
           s64.dir[u] = __ddiv_rn(__dsub_rn(b, a), denom);   // (q2 - q1) / (N - 1)
         }
       }
-    } else {
-      sdf.nm1 = (float)(N - 1);
-      sdf.rn = __frcp_rn(sdf.nm1);
-      if (N > (1ll << 24)) pending = true;    // indices beyond FP32 integers: exact pass
-    }
-
-    BfsChunker ch;
-    ch.init(pending ? 0 : N);
-    long long v;
-    unsigned m;
-    long long pos0;
-    bool coll = false;
-    while (ch.next(lane, &v, &m, &pos0)) {
-      if (pos0 >= nmax) break;
-      const long long my_pos = pos0 + __popc(m & lt_mask);
-      const bool active = v >= 0 && my_pos >= N_start && my_pos < nmax && (incl || (v != 0 && v != N - 1));
-      unsigned act = __ballot_sync(MRMG_FULL, active);
-      while (act) {
-        const int srcl = __ffs(act) - 1;
-        act &= act - 1;
-        const long long iv = __shfl_sync(MRMG_FULL, v, srcl);
-        stat_cfg++;
-        uint8_t code;
-        if constexpr (RESOLVE) {
-          s64.di = (double)iv;
-          code = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, s64, false);
-        } else {
-          sdf.fi = (float)iv;
-          code = eval_config<GPL, SPG, RESOLVE>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
+      BfsChunker ch;
+      ch.init(N);
+      long long v;
+      unsigned m;
+      long long pos0;
+      bool coll = false;
+      while (!coll && ch.next(lane, &v, &m, &pos0)) {
+        if (pos0 >= nmax) break;
+        const long long my_pos = pos0 + __popc(m & lt_mask);
+        const bool active = v >= 0 && my_pos >= N_start && my_pos < nmax && (incl || (v != 0 && v != N - 1));
+        unsigned act = __ballot_sync(MRMG_FULL, active);
+        while (act) {
+          const int srcl = __ffs(act) - 1;
+          act &= act - 1;
+          s64.di = (double)__shfl_sync(MRMG_FULL, v, srcl);
+          if (eval_config<GPL, SPG, true>(s, t, wcs, wqv, wsph, w64, lane, s64, false) == V_COLLIDE) {
+            coll = true;
+            break;
+          }
         }
-        if (code == V_COLLIDE) {
-          coll = true;
-          if (!full) break;
-        }
-        if (code == V_PENDING) pending = true;
       }
-      if (coll && !full) break;
+      if (lane == 0) out[e] = coll ? V_COLLIDE : V_FREE;
+      __syncwarp();
     }
-    if (lane == 0) {
-      const uint8_t r = coll ? V_COLLIDE : (pending ? V_PENDING : V_FREE);
-      out[e] = r;
-      if (!RESOLVE && r == V_PENDING) {
-        const int slot = atomicAdd(&ctr[kCtrPending], 1);
-        pend[slot] = e;
-      }
-    }
-    __syncwarp();
   }
   if (lane == 0 && !RESOLVE) atomicAdd((unsigned long long*)&ctr[kCtrStat0], (unsigned long long)stat_cfg);
+}
+
+template <int GPL, int SPG>
+__global__ void __launch_bounds__(256) arm_edges_phase_b(ArmDev s, const void* q1, const void* q2, int dtype,
+                                                         int incl, int* ctr, SurvivorEdge* surv, int full) {
+  const int nsv = ctr[kCtrL1];
+  const long long maxj = ctr[kCtrMaxJ];
+  const long long total = (long long)nsv * maxj;
+  if (total == 0) return;
+  extern __shared__ __align__(16) unsigned char smem_arm[];
+  ArmSmem t;
+  stage_tables(s, smem_arm, &t);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float2* wcs; float* wqv; float4* wsph; double* w64;
+  warp_areas(s, smem_arm, table_bytes(s), wib, false, &wcs, &wqv, &wsph, &w64);
+  const int D = s.D;
+  long long stat_cfg = 0;
+  volatile SurvivorEdge* vsurv = surv;
+  while (true) {
+    unsigned long long b0 = 0;
+    if (lane == 0) b0 = atomicAdd((unsigned long long*)&ctr[kCtrQueueB], 32ull);
+    b0 = __shfl_sync(MRMG_FULL, b0, 0);
+    if ((long long)b0 >= total) break;
+    // item id -> (survivor l, offset j): position-major
+    const long long id = (long long)b0 + lane;
+    int l = 0;
+    long long iv = -1;
+    if (id < total) {
+      l = (int)(id % nsv);
+      const long long j = id / nsv;
+      const long long p = vsurv[l].p_next + j;
+      if (p < vsurv[l].nmax && (full || !vsurv[l].dead)) {
+        const long long N = vsurv[l].N;
+        const long long c = bfs_at(N, p);
+        if (incl || (c != 0 && c != N - 1)) iv = c;
+      }
+    }
+    unsigned act = __ballot_sync(MRMG_FULL, iv >= 0);
+    while (act) {
+      const int srcl = __ffs(act) - 1;
+      act &= act - 1;
+      const int ls = __shfl_sync(MRMG_FULL, l, srcl);
+      const long long is = __shfl_sync(MRMG_FULL, iv, srcl);
+      int dead = (lane == 0 && !full) ? vsurv[ls].dead : 0;   // read once, decide warp-uniformly
+      if (__shfl_sync(MRMG_FULL, dead, 0)) continue;          // another warp found its collision
+      const long long e = vsurv[ls].e;
+      const int N = vsurv[ls].N;
+      EdgeSourceDF sdf;
+      float mloc;
+      bool nanf;
+      load_edge(q1, q2, dtype, e, D, lane, &sdf, &mloc, &nanf);
+      sdf.nm1 = (float)(N - 1);
+      sdf.rn = __frcp_rn(sdf.nm1);
+      sdf.fi = (float)is;
+      stat_cfg++;
+      const uint8_t code = eval_config<GPL, SPG, false>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
+      if (lane == 0) {
+        if (code == V_COLLIDE) vsurv[ls].dead = 1;
+        else if (code == V_PENDING) vsurv[ls].pend = 1;
+      }
+    }
+  }
+  if (lane == 0) atomicAdd((unsigned long long*)&ctr[kCtrStat0], (unsigned long long)stat_cfg);
+}
+
+__global__ void arm_edges_finalize(int* ctr, const SurvivorEdge* surv, uint8_t* out, long long* pend) {
+  const int nsv = ctr[kCtrL1];
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nsv; l += gridDim.x * blockDim.x) {
+    const SurvivorEdge sv = surv[l];
+    const uint8_t r = sv.dead ? V_COLLIDE : (sv.pend ? V_PENDING : V_FREE);
+    out[sv.e] = r;
+    if (r == V_PENDING) {
+      const int slot = atomicAdd(&ctr[kCtrPending], 1);
+      pend[slot] = sv.e;
+    }
+  }
 }
 
 // sphere centres for the error-bound check: warp per configuration
@@ -799,13 +917,27 @@ cudaError_t launch_edges(const ArmDev& s, int gpl, const void* q1, const void* q
   if (gpl == G_ && s.SPG == S_) {                                                                  \
     auto k = arm_edges_kernel<G_, S_, RESOLVE>;                                                    \
     k<<<grid, warps * 32, smem, st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out,     \
-                                      sc.ctr, sc.pend, full);                                      \
+                                      sc.ctr, sc.pend, sc.surv, full);                             \
     return cudaGetLastError();                                                                     \
   }
   MRMG_ARM_EDGE(1, 6)
   MRMG_ARM_EDGE(2, 5)
   MRMG_ARM_EDGE(4, 8)
 #undef MRMG_ARM_EDGE
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_phase_b(const ArmDev& s, int gpl, const void* q1, const void* q2, int dtype, int incl,
+                           const CallScratch& sc, int grid, int warps, size_t smem, int full, cudaStream_t st) {
+#define MRMG_ARM_PB(G_, S_)                                                                        \
+  if (gpl == G_ && s.SPG == S_) {                                                                  \
+    arm_edges_phase_b<G_, S_><<<grid, warps * 32, smem, st>>>(s, q1, q2, dtype, incl, sc.ctr, sc.surv, full); \
+    return cudaGetLastError();                                                                     \
+  }
+  MRMG_ARM_PB(1, 6)
+  MRMG_ARM_PB(2, 5)
+  MRMG_ARM_PB(4, 8)
+#undef MRMG_ARM_PB
   return cudaErrorInvalidValue;
 }
 
@@ -837,6 +969,7 @@ int arm_prepare(const ArmDev& s, int warps) {
     cudaFuncSetAttribute(arm_edges_kernel<G_, S_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s2);  \
     cudaFuncSetAttribute(arm_configs_kernel<G_, S_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1); \
     cudaFuncSetAttribute(arm_configs_kernel<G_, S_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s2);  \
+    cudaFuncSetAttribute(arm_edges_phase_b<G_, S_>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1);        \
     err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, arm_edges_kernel<G_, S_, false>, warps * 32, \
                                                         smem_pass(s, warps, false));              \
   }
@@ -872,6 +1005,9 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
   cudaError_t e = launch_edges<false>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc,
                                       grid, ls.warps, smem1, full, st);
   if (e != cudaSuccess) return e;
+  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, st);
+  if (e != cudaSuccess) return e;
+  arm_edges_finalize<<<std::max(1, ls.num_sms), 256, 0, st>>>(sc.ctr, sc.surv, out, sc.pend);
   const int w2 = 2;
   return launch_edges<true>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc, ls.num_sms,
                             w2, smem_pass(s, w2, true), 0, st);

@@ -164,6 +164,29 @@ __device__ __forceinline__ long long bfs_node(long long N, int level, long long 
   return (s + e) >> 1;
 }
 
+// Position p of the BFS order directly.  Every level of the midpoint tree is
+// full except possibly the last (interval sizes on one level differ by at
+// most one), so positions below 2^L - 1 map to (level, slot) in closed form;
+// on the last level the r-th present node is found by descending the tree,
+// where a subtree rooted at depth d with interval size s has
+// s - (2^(L-d) - 1) nodes on level L.  O(log N), no table.
+__device__ __forceinline__ long long bfs_at(long long N, long long p) {
+  const int L = 63 - __clzll(N + 1);          // 2^L - 1 <= N
+  const long long full = (1ll << L) - 1;
+  if (p < full) {
+    const int lv = 63 - __clzll(p + 1);
+    return bfs_node(N, lv, p + 1 - (1ll << lv));
+  }
+  long long r = p - full, a = 0, b = N - 1;
+  for (int d = 0; d < L; d++) {
+    const long long m = (a + b) >> 1;
+    const long long cnt = (m - a) - ((1ll << (L - d - 1)) - 1);
+    if (r < cnt) b = m - 1;
+    else { r -= cnt; a = m + 1; }
+  }
+  return a;
+}
+
 // Warp-uniform iterator over the BFS order in chunks of up to 32 slots of one
 // level.  next() returns, per lane, the index held by that lane's slot (or -1
 // where the slot is empty), the ballot of non-empty slots and the BFS position

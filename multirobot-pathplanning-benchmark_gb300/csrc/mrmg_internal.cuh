@@ -54,13 +54,27 @@ struct ArmDev {
 };
 
 // per-call scratch counters (device): [0] work queue, [1] pending count,
-// [2] error bits, [3] pass-two queue, [4..7] statistics
+// [2] error bits, [3] pass-two queue, [4..5] configurations evaluated (64-bit),
+// [6] surviving edges, [7] longest remaining position range, [8..9] phase-B
+// queue (64-bit)
 constexpr int kCtrQueue = 0, kCtrPending = 1, kCtrErr = 2, kCtrQueue2 = 3, kCtrStat0 = 4;
-constexpr int kNumCtr = 8;
+constexpr int kCtrL1 = 6, kCtrMaxJ = 7, kCtrQueueB = 8;
+constexpr int kNumCtr = 16;
+
+// an edge that survived its first checked configuration: its remaining
+// BFS positions [p_next, nmax) are dealt to all warps
+struct SurvivorEdge {
+  long long e;
+  int N, p_next, nmax;
+  int dead;      // a remaining configuration collides
+  int pend;      // a configuration needs the exact FP64 pass
+  int pad;
+};
 
 struct CallScratch {
-  int* ctr;          // [kNumCtr]
-  long long* pend;   // pending item list
+  int* ctr;             // [kNumCtr]
+  long long* pend;      // pending item list
+  SurvivorEdge* surv;   // surviving edges (arm edge checks)
   long long pend_cap;
 };
 
@@ -90,7 +104,7 @@ int arm_prepare(const ArmDev& s, int warps);
 int arm_supported_spg(int idx);   // list of compiled SPG values, -1 at end
 int arm_gpl_for_spg(int spg);
 
-cudaError_t binary_indices(long long N, long long* out, cudaStream_t st);
+cudaError_t binary_indices(long long N, long long* out, cudaStream_t st, int chunked);
 
 struct SliceTab {
   int A, D, end_all;

@@ -24,6 +24,7 @@ def test_binary_order_on_device(gpu):
         ref = tuple(int(x) for x in g["flat"][off:off + N])
         off += N
         assert col.binary_search_indices(int(N)) == ref, N
+        assert col.binary_search_indices(int(N), chunked=True) == ref, N
 
 
 def test_disc_configs_golden(gpu):
