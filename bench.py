@@ -318,7 +318,7 @@ def run_gb300(args):
             batched_over_plain=value / plain,
             roofline={"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                       "frac": achieved / peak, "traffic": traffic,
-                      "kernel": "arm_edges_kernel<1,6,false> (first pass), full-evaluation mode",
+                      "kernel": "first pass (arm_edges_kernel phase A + arm_edges_phase_b), full-evaluation mode",
                       "algorithmic": f"{cfgs} configurations x {F1} flops per launch",
                       "ms_per_launch": full_ms,
                       "peak_source": "measured FP32 FFMA microbenchmark (mrmg_microbench_fma) in this run; "
@@ -340,13 +340,13 @@ def run_gb300(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": WORKLOAD_DESC, "edges_per_step": n, "edges_total": n * world,
                        "l2": "flushed between timed steps (256 MB write outside the timed events)",
-                       "form": "batched, CUDA-graph captured (counter reset, first pass, FP64 re-check pass, "
-                               "status copy)", "parallelism": f"replicas x{world}"},
+                       "form": "batched, CUDA-graph captured (counter reset, phase A, phase B, finalize, FP64 "
+                               "re-check pass, status copy)", "parallelism": f"replicas x{world}"},
             "verdict_mismatches": mism,
             "clocks": clk,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(q1.nbytes + q2.nbytes),
                     "d2h_bytes_per_step": int(n)},
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": 4 * args.steps,
             "wall_s_timed": t_wall,
         }
         line.update(extra)
@@ -404,7 +404,7 @@ def run_profile(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--plain-edges", type=int, default=2000)
