@@ -644,17 +644,23 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
   const unsigned lt_mask = (1u << lane) - 1u;
   long long stat_cfg = 0;
 
+  // phase A: static grid-stride over edges (one configuration each, uniform
+  // cost); pass 2: the pending list through a work queue (uneven cost)
+  const long long warp_g = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+  const long long warps_g = (long long)gridDim.x * (blockDim.x >> 5);
+  long long next_e = warp_g;
   while (true) {
-    long long k = 0;
-    if (lane == 0) k = atomicAdd(&ctr[RESOLVE ? kCtrQueue2 : kCtrQueue], 1);
-    k = __shfl_sync(MRMG_FULL, k, 0);
     long long e;
     if (RESOLVE) {
+      long long k = 0;
+      if (lane == 0) k = atomicAdd(&ctr[kCtrQueue2], 1);
+      k = __shfl_sync(MRMG_FULL, k, 0);
       if (k >= ctr[kCtrPending]) break;
       e = pend[k];
     } else {
-      if (k >= n) break;
-      e = k;
+      if (next_e >= n) break;
+      e = next_e;
+      next_e += warps_g;
     }
     EdgeSourceDF sdf;
     float mloc;
@@ -771,21 +777,27 @@ __global__ void __launch_bounds__(256) arm_edges_phase_b(ArmDev s, const void* q
   const int D = s.D;
   long long stat_cfg = 0;
   volatile SurvivorEdge* vsurv = surv;
+  constexpr int kGrab = 256;   // items per queue access: keeps the shared counter cold
+  unsigned long long b0 = 0;
+  int sub = kGrab / 32;
   while (true) {
-    unsigned long long b0 = 0;
-    if (lane == 0) b0 = atomicAdd((unsigned long long*)&ctr[kCtrQueueB], 32ull);
-    b0 = __shfl_sync(MRMG_FULL, b0, 0);
+    if (sub == kGrab / 32) {
+      if (lane == 0) b0 = atomicAdd((unsigned long long*)&ctr[kCtrQueueB], (unsigned long long)kGrab);
+      b0 = __shfl_sync(MRMG_FULL, b0, 0);
+      sub = 0;
+    }
     if ((long long)b0 >= total) break;
     // item id -> (survivor l, offset j): position-major
-    const long long id = (long long)b0 + lane;
+    const long long id = (long long)b0 + 32 * sub + lane;
+    sub++;
     int l = 0;
     long long iv = -1;
     if (id < total) {
       l = (int)(id % nsv);
       const long long j = id / nsv;
-      const long long p = vsurv[l].p_next + j;
-      if (p < vsurv[l].nmax && (full || !vsurv[l].dead)) {
-        const long long N = vsurv[l].N;
+      const long long p = __ldg(&surv[l].p_next) + j;
+      if (p < __ldg(&surv[l].nmax) && (full || !vsurv[l].dead)) {
+        const long long N = __ldg(&surv[l].N);
         const long long c = bfs_at(N, p);
         if (incl || (c != 0 && c != N - 1)) iv = c;
       }
@@ -798,8 +810,8 @@ __global__ void __launch_bounds__(256) arm_edges_phase_b(ArmDev s, const void* q
       const long long is = __shfl_sync(MRMG_FULL, iv, srcl);
       int dead = (lane == 0 && !full) ? vsurv[ls].dead : 0;   // read once, decide warp-uniformly
       if (__shfl_sync(MRMG_FULL, dead, 0)) continue;          // another warp found its collision
-      const long long e = vsurv[ls].e;
-      const int N = vsurv[ls].N;
+      const long long e = __ldg(&surv[ls].e);
+      const int N = __ldg(&surv[ls].N);
       EdgeSourceDF sdf;
       float mloc;
       bool nanf;
