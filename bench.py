@@ -340,13 +340,13 @@ def run_gb300(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": WORKLOAD_DESC, "edges_per_step": n, "edges_total": n * world,
                        "l2": "flushed between timed steps (256 MB write outside the timed events)",
-                       "form": "batched, CUDA-graph captured (counter reset, phase A, phase B, finalize, FP64 "
+                       "form": "batched, CUDA-graph captured (counter reset, phase A, phase B1, phase B2, finalize, FP64 "
                                "re-check pass, status copy)", "parallelism": f"replicas x{world}"},
             "verdict_mismatches": mism,
             "clocks": clk,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(q1.nbytes + q2.nbytes),
                     "d2h_bytes_per_step": int(n)},
-            "gpu_launches": 4 * args.steps,
+            "gpu_launches": 5 * args.steps,
             "wall_s_timed": t_wall,
         }
         line.update(extra)

@@ -504,6 +504,7 @@ __device__ __forceinline__ void warp_areas(const ArmDev& s, unsigned char* smem_
 // queue in chunks of kCfgChunk).
 // ---------------------------------------------------------------------------
 constexpr int kCfgChunk = 4;
+constexpr int kPhaseB1 = 3;   // positions per survivor in the first phase-B launch
 
 template <int GPL, int SPG, bool RESOLVE>
 __global__ void __launch_bounds__(256) arm_configs_kernel(ArmDev s, const void* q, int dtype, long long n,
@@ -644,23 +645,19 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
   const unsigned lt_mask = (1u << lane) - 1u;
   long long stat_cfg = 0;
 
-  // phase A: static grid-stride over edges (one configuration each, uniform
-  // cost); pass 2: the pending list through a work queue (uneven cost)
-  const long long warp_g = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
-  const long long warps_g = (long long)gridDim.x * (blockDim.x >> 5);
-  long long next_e = warp_g;
+  // edges (phase A) or pending edges (pass 2) through a work queue: the cost
+  // per edge is uneven (a free first configuration is a full evaluation)
   while (true) {
+    long long k = 0;
+    if (lane == 0) k = atomicAdd(&ctr[RESOLVE ? kCtrQueue2 : kCtrQueue], 1);
+    k = __shfl_sync(MRMG_FULL, k, 0);
     long long e;
     if (RESOLVE) {
-      long long k = 0;
-      if (lane == 0) k = atomicAdd(&ctr[kCtrQueue2], 1);
-      k = __shfl_sync(MRMG_FULL, k, 0);
       if (k >= ctr[kCtrPending]) break;
       e = pend[k];
     } else {
-      if (next_e >= n) break;
-      e = next_e;
-      next_e += warps_g;
+      if (k >= n) break;
+      e = k;
     }
     EdgeSourceDF sdf;
     float mloc;
@@ -760,13 +757,16 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
   if (lane == 0 && !RESOLVE) atomicAdd((unsigned long long*)&ctr[kCtrStat0], (unsigned long long)stat_cfg);
 }
 
+// positions p_next + j, j in [j_lo, j_hi), of every survivor (j_hi < 0: to the end)
 template <int GPL, int SPG>
 __global__ void __launch_bounds__(256) arm_edges_phase_b(ArmDev s, const void* q1, const void* q2, int dtype,
-                                                         int incl, int* ctr, SurvivorEdge* surv, int full) {
+                                                         int incl, int* ctr, SurvivorEdge* surv, int full,
+                                                         int j_lo, int j_hi) {
   const int nsv = ctr[kCtrL1];
-  const long long maxj = ctr[kCtrMaxJ];
+  const long long maxj = j_hi < 0 ? (long long)ctr[kCtrMaxJ] : min((long long)j_hi, (long long)ctr[kCtrMaxJ]);
+  const long long first = (long long)nsv * j_lo;
   const long long total = (long long)nsv * maxj;
-  if (total == 0) return;
+  if (total <= first) return;
   extern __shared__ __align__(16) unsigned char smem_arm[];
   ArmSmem t;
   stage_tables(s, smem_arm, &t);
@@ -777,19 +777,14 @@ __global__ void __launch_bounds__(256) arm_edges_phase_b(ArmDev s, const void* q
   const int D = s.D;
   long long stat_cfg = 0;
   volatile SurvivorEdge* vsurv = surv;
-  constexpr int kGrab = 256;   // items per queue access: keeps the shared counter cold
-  unsigned long long b0 = 0;
-  int sub = kGrab / 32;
-  while (true) {
-    if (sub == kGrab / 32) {
-      if (lane == 0) b0 = atomicAdd((unsigned long long*)&ctr[kCtrQueueB], (unsigned long long)kGrab);
-      b0 = __shfl_sync(MRMG_FULL, b0, 0);
-      sub = 0;
-    }
-    if ((long long)b0 >= total) break;
-    // item id -> (survivor l, offset j): position-major
-    const long long id = (long long)b0 + 32 * sub + lane;
-    sub++;
+  // static interleave, no shared counter: warp w takes items w, w + W, w + 2W,
+  // ... (32 per round, one per lane); items are position-major, so every
+  // warp walks its share in BFS-position order and the expensive items (the
+  // configurations of long free edges) spread over all warps
+  const long long W = (long long)gridDim.x * (blockDim.x >> 5);
+  const long long wg = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+  for (long long k0 = 0; first + wg + W * k0 < total; k0 += 32) {
+    const long long id = first + wg + W * (k0 + lane);
     int l = 0;
     long long iv = -1;
     if (id < total) {
@@ -940,10 +935,12 @@ cudaError_t launch_edges(const ArmDev& s, int gpl, const void* q1, const void* q
 }
 
 cudaError_t launch_phase_b(const ArmDev& s, int gpl, const void* q1, const void* q2, int dtype, int incl,
-                           const CallScratch& sc, int grid, int warps, size_t smem, int full, cudaStream_t st) {
+                           const CallScratch& sc, int grid, int warps, size_t smem, int full, int j_lo, int j_hi,
+                           cudaStream_t st) {
 #define MRMG_ARM_PB(G_, S_)                                                                        \
   if (gpl == G_ && s.SPG == S_) {                                                                  \
-    arm_edges_phase_b<G_, S_><<<grid, warps * 32, smem, st>>>(s, q1, q2, dtype, incl, sc.ctr, sc.surv, full); \
+    arm_edges_phase_b<G_, S_><<<grid, warps * 32, smem, st>>>(s, q1, q2, dtype, incl, sc.ctr, sc.surv, full, \
+                                                              j_lo, j_hi);                         \
     return cudaGetLastError();                                                                     \
   }
   MRMG_ARM_PB(1, 6)
@@ -1017,7 +1014,11 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
   cudaError_t e = launch_edges<false>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc,
                                       grid, ls.warps, smem1, full, st);
   if (e != cudaSuccess) return e;
-  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, st);
+  // B1: the next kPhaseB1 positions of every survivor (kills most colliding
+  // survivors); B2: everything left, spread over all warps
+  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, 0, kPhaseB1, st);
+  if (e != cudaSuccess) return e;
+  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, kPhaseB1, -1, st);
   if (e != cudaSuccess) return e;
   arm_edges_finalize<<<std::max(1, ls.num_sms), 256, 0, st>>>(sc.ctr, sc.surv, out, sc.pend);
   const int w2 = 2;
