@@ -130,6 +130,15 @@ int mrmg_scene_info(const mrmg_scene *scene, int64_t *out7, double *out_band);
  * autotuner; the verdicts never depend on it. */
 int mrmg_scene_set_launch(mrmg_scene *scene, int32_t ctas, int32_t warps_per_cta);
 
+/* Test-order autotuning for an arm scene: for the sample configurations
+ * d_q[n] (for example uniform in the joint limits) record which boxes each
+ * one touches, then order the boxes by greedy set cover so that a colliding
+ * configuration meets a touching box as early as possible.  Verdicts do not
+ * depend on the order.  h_order_out[B] (optional) receives the new order as
+ * indices into the current one.  Not capturable (it synchronises). */
+int mrmg_arm_scene_tune_order(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n,
+                              int32_t *h_order_out, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Collision checks                                                          */
 /* ------------------------------------------------------------------------ */

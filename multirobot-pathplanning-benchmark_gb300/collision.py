@@ -104,6 +104,17 @@ class Gb300Scene:
     def set_launch(self, ctas: int = 0, warps_per_cta: int = 0):
         _lib.check(self.lib.mrmg_scene_set_launch(self.h, int(ctas), int(warps_per_cta)))
 
+    def tune_test_order(self, samples, stream=None) -> np.ndarray:
+        """Order the boxes so that colliding configurations like `samples`
+        (e.g. uniform in the joint limits) stop early; returns the order."""
+        if self.kind != 1:
+            return np.zeros(0, dtype=np.int32)
+        qt = _dev_tensor(samples)
+        order = np.zeros(max(len(self.scene.box_lo), 1), dtype=np.int32)
+        _lib.check(self.lib.mrmg_arm_scene_tune_order(self.h, qt.data_ptr(), _dt_code(qt), qt.shape[0],
+                                                      order.ctypes.data, _lib.stream_handle(stream)))
+        return order[: len(self.scene.box_lo)]
+
     def last_call_stats(self) -> dict:
         out = np.zeros(4, dtype=np.int64)
         _lib.check(self.lib.mrmg_last_call_stats(self.h, out.ctypes.data))

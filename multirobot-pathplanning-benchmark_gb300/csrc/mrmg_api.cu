@@ -74,6 +74,8 @@ struct mrmg_scene {
   double band = 0.0;
   int64_t n_pairs_groups = 0;
   std::vector<int> slot_to_sphere;   // arm: slot -> input sphere index (-1 padding)
+  std::vector<float4> box32_host;    // arm: box tables in their current test order
+  std::vector<double> box64_host;
 };
 
 namespace {
@@ -393,6 +395,8 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   cudaError_t e = blk.upload(&sc->d_tables);
   if (e != cudaSuccess) { mrmg_scene_destroy(sc); return cuda_fail(e, "upload arm scene"); }
   sc->band = d.delta;
+  sc->box32_host = box32;
+  sc->box64_host = box64;
   sc->occ_ctas_per_sm = arm_prepare(d, 8);
   sc->n_pairs_groups = (int64_t)pairs.size();
   sc->slot_to_sphere = slot_sphere;
@@ -437,6 +441,63 @@ int mrmg_arm_slot_map(const mrmg_scene* sc, int32_t* out, int64_t cap) {
   if (cap < (int64_t)sc->slot_to_sphere.size()) return fail(MRMG_ERR_ARG, "capacity too small");
   for (size_t i = 0; i < sc->slot_to_sphere.size(); i++) out[i] = sc->slot_to_sphere[i];
   return (int)sc->slot_to_sphere.size();
+}
+
+int mrmg_arm_scene_tune_order(mrmg_scene* sc, const void* d_q, int32_t dtype, int64_t n, int32_t* h_order_out,
+                              void* stream) {
+  if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
+  if (n < 1 || (dtype != MRMG_F32 && dtype != MRMG_F64) || !d_q) return fail(MRMG_ERR_ARG, "samples / dtype");
+  const int B = sc->arm.B;
+  if (B < 2) return MRMG_OK;
+  const int words = (B + 31) / 32;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint32_t* d_hits = nullptr;
+  cudaError_t e = cudaMalloc(&d_hits, sizeof(uint32_t) * words * n);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(hits)");
+  e = arm_box_hits(sc->arm, d_q, dtype, n, d_hits, words, st);
+  std::vector<uint32_t> hits((size_t)words * n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hits.data(), d_hits, sizeof(uint32_t) * words * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_hits);
+  if (e != cudaSuccess) return cuda_fail(e, "box hit calibration");
+  // greedy cover: next the box that touches most samples not yet touched by
+  // the boxes before it; then the rest by how many samples they touch
+  std::vector<char> covered(n, 0), used(B, 0);
+  std::vector<int> order;
+  auto hit = [&](long long i, int b) { return (hits[i * words + b / 32] >> (b % 32)) & 1u; };
+  while ((int)order.size() < B) {
+    int best = -1;
+    long long best_cnt = -1, best_tot = -1;
+    for (int b = 0; b < B; b++) {
+      if (used[b]) continue;
+      long long cnt = 0, tot = 0;
+      for (long long i = 0; i < n; i++) {
+        const unsigned h = hit(i, b);
+        tot += h;
+        cnt += h && !covered[i];
+      }
+      if (cnt > best_cnt || (cnt == best_cnt && tot > best_tot)) { best = b; best_cnt = cnt; best_tot = tot; }
+    }
+    used[best] = 1;
+    order.push_back(best);
+    for (long long i = 0; i < n; i++)
+      if (hit(i, best)) covered[i] = 1;
+  }
+  std::vector<float4> b32(2 * B);
+  std::vector<double> b64(6 * (size_t)B);
+  for (int k = 0; k < B; k++) {
+    b32[2 * k] = sc->box32_host[2 * order[k]];
+    b32[2 * k + 1] = sc->box32_host[2 * order[k] + 1];
+    for (int c = 0; c < 6; c++) b64[6 * (size_t)k + c] = sc->box64_host[6 * (size_t)order[k] + c];
+  }
+  e = cudaMemcpy((void*)sc->arm.box32, b32.data(), sizeof(float4) * 2 * B, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy((void*)sc->arm.box64, b64.data(), sizeof(double) * 6 * B, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "upload box order");
+  sc->box32_host = b32;
+  sc->box64_host = b64;
+  if (h_order_out)
+    for (int k = 0; k < B; k++) h_order_out[k] = order[k];
+  return MRMG_OK;
 }
 
 int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype, int64_t n, uint8_t* d_out,

@@ -896,6 +896,65 @@ __global__ void arm_centers_kernel(ArmDev s, const void* q, int dtype, long long
   }
 }
 
+// Test-order calibration: for each sample configuration, the set of boxes
+// that any sphere touches (FP32, within the re-check band) as a bitmask
+// hits[i * words + b / 32].  Verdicts never depend on the order; the order
+// decides how soon a colliding configuration stops.
+__global__ void arm_box_hits_kernel(ArmDev s, const void* q, int dtype, long long n, uint32_t* hits, int words) {
+  extern __shared__ __align__(16) unsigned char smem_arm[];
+  ArmSmem t;
+  stage_tables(s, smem_arm, &t);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float2* wcs; float* wqv; float4* wsph; double* w64;
+  warp_areas(s, smem_arm, table_bytes(s), wib, false, &wcs, &wqv, &wsph, &w64);
+  const int D = s.D;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (long long i = blockIdx.x * (blockDim.x >> 5) + wib; i < n; i += nw) {
+    const CfgSource src{q, dtype, i, D};
+    for (int j = lane; j < D; j += 32) {
+      float h, l;
+      src.df(j, &h, &l);
+      if (is_prismatic(t, j)) { wqv[j] = __fadd_rn(h, l); wcs[j] = make_float2(1.f, 0.f); }
+      else {
+        float a;
+        reduce_df(h, l, &a);
+        float sn, cs;
+        sincosf(a, &sn, &cs);
+        wcs[j] = make_float2(cs, sn);
+      }
+    }
+    __syncwarp();
+    for (int w = 0; w < words; w++) {
+      uint32_t bits = 0;
+      for (int g = lane; g < s.G; g += 32) {
+        const int gi = t.grp[g];
+        float R[9], p[3];
+        chain32(s, t, wcs, wqv, gi & 0xff, gi >> 8, R, p);
+        for (int v = 0; v < s.SPG; v++) {
+          const float4 lf = t.sph[g * s.SPG + v];
+          const float4 bd = t.band[g * s.SPG + v];
+          if (bd.y < 0.f) continue;
+          const float x = p[0] + (R[0] * lf.x + R[1] * lf.y + R[2] * lf.z);
+          const float y = p[1] + (R[3] * lf.x + R[4] * lf.y + R[5] * lf.z);
+          const float z = p[2] + (R[6] * lf.x + R[7] * lf.y + R[8] * lf.z);
+          for (int b = 32 * w; b < min(s.B, 32 * w + 32); b++) {
+            const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
+            const float ex = fmaxf(fabsf(x - bc.x) - bh.x, 0.f);
+            const float ey = fmaxf(fabsf(y - bc.y) - bh.y, 0.f);
+            const float ez = fmaxf(fabsf(z - bc.z) - bh.z, 0.f);
+            if (fmaf(ez, ez, fmaf(ey, ey, ex * ex)) <= bd.y) bits |= 1u << (b - 32 * w);
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) bits |= __shfl_xor_sync(MRMG_FULL, bits, o);
+      if (lane == 0) hits[i * words + w] = bits;
+    }
+    __syncwarp();
+  }
+}
+
 // ---------------------------------------------------------------------------
 // dispatch over the compiled (groups per lane, spheres per group) variants
 // ---------------------------------------------------------------------------
@@ -1024,6 +1083,17 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
   const int w2 = 2;
   return launch_edges<true>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc, ls.num_sms,
                             w2, smem_pass(s, w2, true), 0, st);
+}
+
+cudaError_t arm_box_hits(const ArmDev& s, const void* q, int dtype, long long n, uint32_t* hits, int words,
+                         cudaStream_t st) {
+  const int warps = 4;
+  size_t smem = smem_pass(s, warps, false);
+  cudaFuncSetAttribute(arm_box_hits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  long long want = (n + warps - 1) / warps;
+  int grid = (int)std::max(1ll, std::min(want, 4096ll));
+  arm_box_hits_kernel<<<grid, warps * 32, smem, st>>>(s, q, dtype, n, hits, words);
+  return cudaGetLastError();
 }
 
 cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, float* c32, double* c64,

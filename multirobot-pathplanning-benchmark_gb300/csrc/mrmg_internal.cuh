@@ -98,6 +98,8 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
                       double res, int incl, const long long* Np, long long N_start,
                       long long N_max, uint8_t* out, const CallScratch& sc,
                       const LaunchShape& ls, int full, cudaStream_t st);
+cudaError_t arm_box_hits(const ArmDev& s, const void* q, int dtype, long long n, uint32_t* hits, int words,
+                         cudaStream_t st);
 cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, float* c32,
                         double* c64, cudaStream_t st);
 int arm_prepare(const ArmDev& s, int warps);

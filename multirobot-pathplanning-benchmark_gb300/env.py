@@ -165,7 +165,7 @@ class Gb300ArmEnvironment(Gb300CollisionBackend):
     """Sphere-arm robots (DH chains, optional planar bases) among boxes."""
 
     def __init__(self, scene: ArmScene, collision_resolution: float = 0.05, collision_tolerance: float = 0.01,
-                 band: float = 0.0):
+                 band: float = 0.0, tune_samples: int = 4096, seed: int = 0):
         self.scene = scene
         self.limits = scene.limits
         sl = [tuple(map(int, s)) for s in scene.agent_slices()]
@@ -178,3 +178,8 @@ class Gb300ArmEnvironment(Gb300CollisionBackend):
         self.cost_metric = "euclidean"
         self.cost_reduction = "max"
         self._gb300 = Gb300Scene(scene, band=band)
+        if tune_samples and self.limits is not None:
+            # test-order autotuning from configurations uniform in the joint limits
+            rng = np.random.default_rng(seed)
+            smp = rng.uniform(self.limits[0], self.limits[1], (tune_samples, scene.q_dim)).astype(np.float32)
+            self.box_order = self._gb300.tune_test_order(smp)

@@ -172,3 +172,16 @@ def test_arm_nan_and_huge_inputs(gpu, oracle):
     q[2, 0] = 3e9          # sine/cosine defined as NaN beyond 2^30
     q[3, 27] = np.inf
     assert np.array_equal(sc.is_collision_free_batch(q).cpu().numpy(), o.configs_free(q))
+
+
+def test_tuned_test_order_keeps_verdicts(gpu, oracle):
+    """The autotuned box order changes how soon a collision is found, never a verdict."""
+    scenes, envm = pkg("scenes"), pkg("env")
+    scene = scenes.make_arm_scene(0)
+    env = envm.Gb300ArmEnvironment(scene, tune_samples=2048, seed=3)
+    assert sorted(env.box_order.tolist()) == list(range(len(scene.box_lo)))
+    o = oracle.OracleScene(scene)
+    w = scenes.make_arm_workload(scene, seed=5, n_configs=20000, n_edges=5000)
+    assert np.array_equal(env.batch_is_collision_free(w["configs"]).astype(np.uint8), o.configs_free(w["configs"]))
+    assert np.array_equal(env.batch_is_edge_collision_free(w["q1"], w["q2"]).astype(np.uint8),
+                          o.edges_free(w["q1"], w["q2"], w["resolution"]))
