@@ -170,6 +170,17 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene *scene, const void *d_q1, const
 int mrmg_arm_sphere_centers(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n,
                             float *d_c32, double *d_c64, void *stream);
 
+/* Graph-capture support.  A call made with MRMG_FLAG_ASYNC inside a stream
+ * capture reports no status; its device-side error bits live in the word
+ * returned here (valid until the next call on the scene), which a captured
+ * graph can copy after each call.  mrmg_status_from_error_bits turns such
+ * bits into the status the synchronous call would have returned.
+ * mrmg_scene_reserve sizes the scene's scratch for batches of n items ahead
+ * of a capture (allocation is not capturable). */
+int mrmg_scene_error_word(mrmg_scene *scene, void **d_err);
+int mrmg_scene_reserve(mrmg_scene *scene, int64_t n, void *stream);
+int mrmg_status_from_error_bits(int32_t bits);
+
 /* Statistics of the scene's last completed call: [0] items re-checked in
  * FP64 (pass two), [1] device error bits, [2] configurations evaluated by the
  * edge kernel's first pass, [3] reserved. */

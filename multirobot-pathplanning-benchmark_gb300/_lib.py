@@ -50,6 +50,9 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_is_edge_collision_free_batch": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, vp, i32]),
     "mrmg_arm_sphere_centers": (i32, [vp, vp, i32, i64, vp, vp, vp]),
     "mrmg_last_call_stats": (i32, [vp, vp]),
+    "mrmg_scene_error_word": (i32, [vp, vp]),
+    "mrmg_scene_reserve": (i32, [vp, i64, vp]),
+    "mrmg_status_from_error_bits": (i32, [i32]),
     "mrmg_arm_slot_map": (i32, [vp, vp, i64]),
     "mrmg_binary_search_indices": (i32, [i64, vp, i32, vp]),
     "mrmg_config_dist_matrix": (i32, [vp, i64, vp, i64, i32, vp, i32, i32, vp, vp, i32]),

@@ -188,6 +188,93 @@ class Gb300Scene:
         return c32[:, idx], c64[:, idx]
 
 
+class EdgeCheckPlan:
+    """A batched edge check of fixed size captured as one CUDA graph.
+
+    The plan owns pinned host buffers for the endpoints and the verdicts and
+    device buffers for both.  One ``run()`` replays a graph that copies the
+    endpoints host->device in ``chunks`` pieces on a copy stream, checks each
+    piece on the compute stream as soon as it has arrived (copies overlap
+    checks), copies the verdicts back and records every piece's error bits.
+    Fill ``q1_host`` / ``q2_host`` (numpy views of the pinned buffers) and call
+    ``run()``; it returns the verdicts (1 = free) as a numpy view.
+    """
+
+    def __init__(self, scene: "Gb300Scene", n: int, resolution: float, include_endpoints: bool = False,
+                 dtype=torch.float32, chunks: int = 4):
+        self.scene = scene
+        self.n = int(n)
+        D = scene.q_dim
+        self.chunks = max(1, min(int(chunks), self.n)) if self.n else 1
+        self.q1_pin = torch.empty((self.n, D), dtype=dtype).pin_memory()
+        self.q2_pin = torch.empty((self.n, D), dtype=dtype).pin_memory()
+        self.out_pin = torch.empty(self.n, dtype=torch.uint8).pin_memory()
+        self.err_pin = torch.zeros(self.chunks, dtype=torch.int32).pin_memory()
+        self.q1_host = self.q1_pin.numpy()
+        self.q2_host = self.q2_pin.numpy()
+        self.q1 = torch.empty((self.n, D), dtype=dtype, device="cuda")
+        self.q2 = torch.empty((self.n, D), dtype=dtype, device="cuda")
+        self.out = torch.empty(self.n, dtype=torch.uint8, device="cuda")
+        self.err = torch.zeros(self.chunks, dtype=torch.int32, device="cuda")
+        self.compute = torch.cuda.Stream()
+        self.copy = torch.cuda.Stream()
+        bounds = np.linspace(0, self.n, self.chunks + 1).astype(np.int64)
+        self.bounds = [(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:])]
+        lib = scene.lib
+        _lib.check(lib.mrmg_scene_reserve(scene.h, max(b - a for a, b in self.bounds) if self.n else 0,
+                                          self.compute.cuda_stream))
+        ew = C.c_void_p()
+        _lib.check(lib.mrmg_scene_error_word(scene.h, C.byref(ew)))
+        self._err_view = torch.as_tensor(_DeviceWord(ew.value), device="cuda")
+        self.res, self.incl = float(resolution), bool(include_endpoints)
+        # warm-up outside the capture (first launches load modules)
+        with torch.cuda.stream(self.compute):
+            if self.n:
+                scene.is_edge_collision_free_batch(self.q1[:1], self.q2[:1], self.res, self.incl,
+                                                   out=self.out[:1], stream=self.compute)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, stream=self.compute):
+            self._enqueue()
+
+    def _enqueue(self):
+        sc, cs, cp = self.scene, self.compute, self.copy
+        cp.wait_stream(cs)
+        events = []
+        for a, b in self.bounds:
+            with torch.cuda.stream(cp):
+                self.q1[a:b].copy_(self.q1_pin[a:b], non_blocking=True)
+                self.q2[a:b].copy_(self.q2_pin[a:b], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(cp)
+            events.append(ev)
+        for k, ((a, b), ev) in enumerate(zip(self.bounds, events)):
+            cs.wait_event(ev)
+            if b > a:
+                sc.is_edge_collision_free_batch(self.q1[a:b], self.q2[a:b], self.res, self.incl, out=self.out[a:b],
+                                                stream=cs, flags=_lib.MRMG_FLAG_ASYNC)
+                with torch.cuda.stream(cs):
+                    self.err[k:k + 1].copy_(self._err_view)
+        with torch.cuda.stream(cs):
+            self.out_pin.copy_(self.out, non_blocking=True)
+            self.err_pin.copy_(self.err, non_blocking=True)
+
+    def run(self) -> np.ndarray:
+        self.graph.replay()
+        self.compute.synchronize()
+        bits = int(np.bitwise_or.reduce(self.err_pin.numpy())) if self.chunks else 0
+        if bits:
+            _lib.check(self.scene.lib.mrmg_status_from_error_bits(bits), "is_edge_collision_free")
+        return self.out_pin.numpy()
+
+
+class _DeviceWord:
+    """__cuda_array_interface__ view of one int32 at a device address."""
+
+    def __init__(self, addr: int):
+        self.__cuda_array_interface__ = {"shape": (1,), "typestr": "<i4", "data": (addr, False), "version": 3}
+
+
 def binary_search_indices(N: int, chunked: bool = False) -> tuple:
     """generate_binary_search_indices(N) computed on the device (closed-form
     position map, or the chunked level iterator)."""

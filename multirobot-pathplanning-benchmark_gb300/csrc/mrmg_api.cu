@@ -546,6 +546,24 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene* sc, const void* d_q1, const vo
   return finish_call(sc, st, flags);
 }
 
+int mrmg_scene_error_word(mrmg_scene* sc, void** d_err) {
+  if (!sc || !d_err) return fail(MRMG_ERR_ARG, "NULL argument");
+  *d_err = sc->d_ctr + kCtrErr;
+  return MRMG_OK;
+}
+
+int mrmg_scene_reserve(mrmg_scene* sc, int64_t n, void* stream) {
+  if (!sc || n < 0) return fail(MRMG_ERR_ARG, "scene / n");
+  return ensure_pending(sc, n, (cudaStream_t)stream);
+}
+
+int mrmg_status_from_error_bits(int32_t bits) {
+  if (bits & E_N_START) return fail(MRMG_ERR_N_START, "N_start > N for at least one edge");
+  if (bits & E_BAD_INPUT) return fail(MRMG_ERR_ARG, "non-finite or out-of-range edge length (int() of nan/inf)");
+  if (bits & E_TIMEOUT) return fail(MRMG_ERR_TIMEOUT, "a bounded device wait ran out");
+  return MRMG_OK;
+}
+
 int mrmg_last_call_stats(const mrmg_scene* sc, int64_t* out4) {
   if (!sc || !out4) return fail(MRMG_ERR_ARG, "NULL argument");
   out4[0] = sc->h_ctr[kCtrPending];

@@ -101,6 +101,17 @@ class Gb300CollisionBackend:
         v = self._gb300.is_edge_collision_free_batch(q1s, q2s, resolution, include_endpoints, N)
         return v.bool().cpu().numpy() if not isinstance(q1s, torch.Tensor) else v.bool()
 
+    def edge_check_plan(self, n: int, resolution: Optional[float] = None, include_endpoints: bool = False,
+                        chunks: int = 4, dtype=torch.float32):
+        """A reusable, graph-captured batched edge check for batches of `n`
+        edges: fill ``plan.q1_host`` / ``plan.q2_host`` (pinned) and call
+        ``plan.run()`` -> verdicts.  One graph launch per call; host->device
+        copies overlap the checks."""
+        from .collision import EdgeCheckPlan
+
+        return EdgeCheckPlan(self._gb300, n, self.collision_resolution if resolution is None else resolution,
+                             include_endpoints, dtype=dtype, chunks=chunks)
+
     # --- path check (planning_env.py:1765-1881), one batched pass ----------
     def is_path_collision_free(self, path, binary_order: bool = True, resolution: Optional[float] = None,
                                tolerance: Optional[float] = None, check_edges_in_order: bool = False,

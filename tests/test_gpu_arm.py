@@ -185,3 +185,23 @@ def test_tuned_test_order_keeps_verdicts(gpu, oracle):
     assert np.array_equal(env.batch_is_collision_free(w["configs"]).astype(np.uint8), o.configs_free(w["configs"]))
     assert np.array_equal(env.batch_is_edge_collision_free(w["q1"], w["q2"]).astype(np.uint8),
                           o.edges_free(w["q1"], w["q2"], w["resolution"]))
+
+
+def test_edge_check_plan_graph(gpu, oracle):
+    """The graph-captured plan (pipelined host->device chunks) gives the oracle's
+    verdicts, run after run, and reports bad edges as the plain call does."""
+    scenes, envm = pkg("scenes"), pkg("env")
+    scene = scenes.make_arm_scene(0)
+    env = envm.Gb300ArmEnvironment(scene, tune_samples=0)
+    o = oracle.OracleScene(scene)
+    w = scenes.make_arm_workload(scene, seed=2, n_configs=10, n_edges=6000)
+    ref = o.edges_free(w["q1"], w["q2"], w["resolution"])
+    plan = env.edge_check_plan(6000, chunks=3)
+    plan.q1_host[:] = w["q1"]
+    plan.q2_host[:] = w["q2"]
+    for _ in range(3):
+        assert np.array_equal(plan.run(), ref)
+    plan.q2_host[17, 0] = np.nan
+    plan.q1_host[17, 0] = np.nan
+    with pytest.raises(ValueError):
+        plan.run()
