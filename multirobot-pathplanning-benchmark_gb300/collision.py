@@ -260,7 +260,8 @@ class EdgeCheckPlan:
             self.err_pin.copy_(self.err, non_blocking=True)
 
     def run(self) -> np.ndarray:
-        self.graph.replay()
+        with torch.cuda.stream(self.compute):   # replay() launches on the current stream
+            self.graph.replay()
         self.compute.synchronize()
         bits = int(np.bitwise_or.reduce(self.err_pin.numpy())) if self.chunks else 0
         if bits:
