@@ -428,7 +428,7 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--plain-edges", type=int, default=2000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--chunks", type=int, default=4, help="pipelined chunks of the end-to-end plan")
+    ap.add_argument("--chunks", type=int, default=1, help="pipelined chunks of the end-to-end plan")
     ap.add_argument("--profile", choices=["early", "full"], default=None,
                     help="short run of the first-pass edge kernel for ncu captures")
     args = ap.parse_args()

@@ -102,7 +102,7 @@ class Gb300CollisionBackend:
         return v.bool().cpu().numpy() if not isinstance(q1s, torch.Tensor) else v.bool()
 
     def edge_check_plan(self, n: int, resolution: Optional[float] = None, include_endpoints: bool = False,
-                        chunks: int = 4, dtype=torch.float32):
+                        chunks: int = 1, dtype=torch.float32):
         """A reusable, graph-captured batched edge check for batches of `n`
         edges: fill ``plan.q1_host`` / ``plan.q2_host`` (pinned) and call
         ``plan.run()`` -> verdicts.  One graph launch per call; host->device
