@@ -164,6 +164,28 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene *scene, const void *d_q1, const
                                       int64_t N_start, int64_t N_max, uint8_t *d_out,
                                       void *stream, int32_t flags);
 
+/* Edge check that allocates nothing.  No counterpart in the reference.
+ * Same arguments, semantics and verdicts as mrmg_is_edge_collision_free_batch,
+ * for callers that cannot allocate device memory while they check edges:
+ * planner steps recorded into a CUDA graph (cudaMalloc is not a capturable
+ * operation), real-time loops that forbid allocation after start-up, and
+ * processes whose memory pool already owns the device.  The regular entry
+ * point may grow the scene's scratch with cudaMalloc; this one uses a fixed
+ * static device array instead and never allocates or frees.
+ *   Limit: at most MRMG_NOALLOC_MAX_EDGES edges per call; larger batches
+ *   return MRMG_ERR_ARG.  The array (256 B + 40 B per edge = 640 KiB) is
+ *   held by every GPU that loads the library until the process exits.
+ *   The first call on a device looks up the array's device address
+ *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   All calls share the array: calls that overlap on the GPU (other streams,
+ *   threads or scenes) race and must be serialised by the caller. */
+#define MRMG_NOALLOC_MAX_EDGES 16384
+int mrmg_is_edge_collision_free_batch_noalloc(mrmg_scene *scene, const void *d_q1, const void *d_q2,
+                                              int32_t dtype, int64_t n, double resolution,
+                                              int32_t include_endpoints, const int64_t *d_N,
+                                              int64_t N_start, int64_t N_max, uint8_t *d_out,
+                                              void *stream, int32_t flags);
+
 /* Sphere centres of an arm scene for d_q[n, q_dim]: d_c32[n, S, 3] from the
  * FP32 bulk path and d_c64[n, S, 3] from the exact FP64 path (either may be
  * NULL).  Used to verify the FP32 error bound against the re-check band. */

@@ -23,6 +23,7 @@ MRMG_F32 = 0
 MRMG_F64 = 1
 MRMG_FLAG_ASYNC = 1
 MRMG_FLAG_FULL_EVAL = 2
+MRMG_NOALLOC_MAX_EDGES = 16384
 
 METRICS = {"euclidean": 0, "sum_euclidean": 1, "max_euclidean": 2, "max": 3}
 COST_METRICS = {"euclidean": 0, "max": 1}
@@ -48,6 +49,7 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_arm_scene_tune_order": (i32, [vp, vp, i32, i64, vp, vp]),
     "mrmg_is_collision_free_batch": (i32, [vp, vp, i32, i64, vp, vp, i32]),
     "mrmg_is_edge_collision_free_batch": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, vp, i32]),
+    "mrmg_is_edge_collision_free_batch_noalloc": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, vp, i32]),
     "mrmg_arm_sphere_centers": (i32, [vp, vp, i32, i64, vp, vp, vp]),
     "mrmg_last_call_stats": (i32, [vp, vp]),
     "mrmg_scene_error_word": (i32, [vp, vp]),

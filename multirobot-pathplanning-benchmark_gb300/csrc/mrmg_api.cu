@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -562,6 +563,98 @@ int mrmg_status_from_error_bits(int32_t bits) {
   if (bits & E_BAD_INPUT) return fail(MRMG_ERR_ARG, "non-finite or out-of-range edge length (int() of nan/inf)");
   if (bits & E_TIMEOUT) return fail(MRMG_ERR_TIMEOUT, "a bounded device wait ran out");
   return MRMG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Edge checks without allocation.
+//
+// Some callers cannot call cudaMalloc at the moment they check edges: a
+// planner step being recorded into a CUDA graph (allocation is not a
+// capturable operation), a real-time control loop that forbids allocation
+// after start-up, or a process whose memory pool already owns the device.
+// The regular entry point grows the scene's scratch with cudaMalloc when a
+// larger batch arrives; this one takes its scratch from the fixed device
+// array below instead, so a call never allocates or frees.
+//
+// The array is sized for MRMG_NOALLOC_MAX_EDGES edges: 256 bytes of
+// counters, 8 bytes per edge for the FP64 pending list and 32 bytes per edge
+// for the survivor list (16,384 edges -> 640 KiB + 256 B).  Every GPU that
+// loads the library holds it until the process exits.  All calls share it
+// and it keeps the last call's contents; each call clears its counters
+// before use.  Calls that overlap on the GPU (other streams, threads or
+// scenes) race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocCtrBytes = 256;
+constexpr size_t kNoAllocPendBytes = sizeof(long long) * MRMG_NOALLOC_MAX_EDGES;
+constexpr size_t kNoAllocSurvBytes = sizeof(SurvivorEdge) * MRMG_NOALLOC_MAX_EDGES;
+static_assert(sizeof(int) * kNumCtr <= kNoAllocCtrBytes, "counters fit");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocCtrBytes + kNoAllocPendBytes + kNoAllocSurvBytes];
+
+// Host code only has a stand-in for g_noalloc_scratch; its device address is
+// looked up once per device (with that device current) and cached.
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {};
+
+int noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 256) return fail(MRMG_ERR_UNSUPPORTED, "device index %d", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = (unsigned char*)g_noalloc_addr[dev];
+  return MRMG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mrmg_is_edge_collision_free_batch_noalloc(mrmg_scene* sc, const void* d_q1, const void* d_q2, int32_t dtype,
+                                              int64_t n, double resolution, int32_t include_endpoints,
+                                              const int64_t* d_N, int64_t N_start, int64_t N_max, uint8_t* d_out,
+                                              void* stream, int32_t flags) {
+  if (!sc) return fail(MRMG_ERR_ARG, "scene is NULL");
+  if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
+  if (n > MRMG_NOALLOC_MAX_EDGES)
+    return fail(MRMG_ERR_ARG, "batch of %lld edges exceeds the no-allocation limit of %d edges per call",
+                (long long)n, (int)MRMG_NOALLOC_MAX_EDGES);
+  if (!d_N && !(resolution > 0.0)) return fail(MRMG_ERR_ARG, "resolution must be > 0");
+  if (N_start < 0) return fail(MRMG_ERR_ARG, "N_start must be >= 0");
+  if (n == 0) return MRMG_OK;
+  if (!d_q1 || !d_q2 || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
+  unsigned char* base = nullptr;
+  int rc = noalloc_scratch(&base);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  CallScratch cs{(int*)base, (long long*)(base + kNoAllocCtrBytes),
+                 (SurvivorEdge*)(base + kNoAllocCtrBytes + kNoAllocPendBytes), (long long)MRMG_NOALLOC_MAX_EDGES};
+  cudaError_t e = cudaMemsetAsync(cs.ctr, 0, sizeof(int) * kNumCtr, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  LaunchShape ls = shape(sc);
+  e = sc->kind == 0
+          ? abstract_edges(sc->ab, d_q1, d_q2, dtype, n, resolution, include_endpoints, (const long long*)d_N,
+                           N_start, N_max, d_out, cs, ls, st)
+          : arm_edges(sc->arm, d_q1, d_q2, dtype, n, resolution, include_endpoints, (const long long*)d_N, N_start,
+                      N_max, d_out, cs, ls, 0, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch edges");
+  // status: the counters go to the scene's pinned mirror (allocated with the scene)
+  e = cudaMemcpyAsync(sc->h_ctr, cs.ctr, sizeof(int) * kNumCtr, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(status)");
+  if (flags & MRMG_FLAG_ASYNC) return MRMG_OK;
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+  return mrmg_status_from_error_bits(sc->h_ctr[kCtrErr]);
 }
 
 int mrmg_last_call_stats(const mrmg_scene* sc, int64_t* out4) {
