@@ -248,6 +248,30 @@ int mrmg_batch_config_cost(const double *d_starts, const double *d_ends, int64_t
                            int32_t flags);
 
 /* ------------------------------------------------------------------------ */
+/* Per-mode nearest neighbours                                               */
+/* ------------------------------------------------------------------------ */
+
+/* Exact k nearest neighbours of every query within its mode: the k smallest
+ * batch_config_dist(query, nodes of the mode, metric) values
+ * (problems/core/configuration.py:303-349) in (distance, index) order --
+ * the selection of PRM get_neighbors (planners/prm/prm_graph.py:441-447,
+ * argpartition + argsort; ties, unspecified there, go to the lower index) and,
+ * with k = 1, RRT nearest (planners/rrtstar_base.py:1228-1254, argmin).
+ *   d_query_mode[Q]: mode of each query; d_mode_offsets[n_modes + 1]: the
+ *   node range of each mode in d_nodes[M, D]; indices are local to the mode.
+ *   Rows beyond the mode's size get index -1 and distance +inf.  k <= 64. */
+int mrmg_knn_exact(const double *d_queries, int64_t Q, const int32_t *d_query_mode,
+                   const double *d_nodes, const int64_t *d_mode_offsets, int32_t D,
+                   const int64_t *h_slices, int32_t A, int32_t metric, int32_t k, int64_t *d_idx,
+                   double *d_dist, void *stream, int32_t flags);
+
+/* Tensor-core self-test (no counterpart in the reference): C[128 x n] =
+ * A[128 x 64] * B[n x 64]^T for row-major BF16 A, B through the same shared-
+ * memory descriptors, instruction descriptor and tensor-memory path as the
+ * nearest-neighbour kernel; n in 32..256, multiple of 32. */
+int mrmg_selftest_umma(const void *d_a, const void *d_b, int32_t n, float *d_c, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Calibration                                                               */
 /* ------------------------------------------------------------------------ */
 

@@ -60,6 +60,8 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_config_dist_matrix": (i32, [vp, i64, vp, i64, i32, vp, i32, i32, vp, vp, i32]),
     "mrmg_batch_config_cost": (i32, [vp, vp, i64, i32, vp, i32, i32, i32, f64, i32, vp, vp, i32]),
     "mrmg_microbench_fma": (i32, [i32, i64, vp, vp]),
+    "mrmg_knn_exact": (i32, [vp, i64, vp, vp, vp, i32, vp, i32, i32, i32, vp, vp, vp, i32]),
+    "mrmg_selftest_umma": (i32, [vp, vp, i32, vp, vp]),
 }
 
 

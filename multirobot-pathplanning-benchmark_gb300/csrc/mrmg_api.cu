@@ -749,6 +749,39 @@ int mrmg_batch_config_cost(const double* d_starts, const double* d_ends, int64_t
   return sync_unless_async(st, flags, "cost");
 }
 
+int mrmg_knn_exact(const double* d_queries, int64_t Q, const int32_t* d_query_mode, const double* d_nodes,
+                   const int64_t* d_mode_offsets, int32_t D, const int64_t* h_slices, int32_t A, int32_t metric,
+                   int32_t k, int64_t* d_idx, double* d_dist, void* stream, int32_t flags) {
+  if (Q < 0 || metric < 0 || metric > 3 || k < 1 || k > 64) return fail(MRMG_ERR_ARG, "Q / metric / k (1..64)");
+  SliceTab t;
+  int rc = make_slices(h_slices, A, D, &t);
+  if (rc) return rc;
+  if (Q == 0) return MRMG_OK;
+  if (!d_queries || !d_query_mode || !d_nodes || !d_mode_offsets || !d_idx || !d_dist)
+    return fail(MRMG_ERR_ARG, "NULL device pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = knn_exact(d_queries, Q, d_query_mode, nullptr, 0, d_nodes, (const long long*)d_mode_offsets, t,
+                            metric, k, (long long*)d_idx, d_dist, device_sms(), st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch knn");
+  return sync_unless_async(st, flags, "knn");
+}
+
+int mrmg_selftest_umma(const void* d_a, const void* d_b, int32_t n, float* d_c, void* stream) {
+  if (n < 32 || n > 256 || n % 32) return fail(MRMG_ERR_ARG, "n must be 32..256, a multiple of 32");
+  cudaStream_t st = (cudaStream_t)stream;
+  int* d_err = nullptr;
+  cudaError_t e = cudaMalloc(&d_err, sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  cudaMemsetAsync(d_err, 0, sizeof(int), st);
+  e = umma_selftest(d_a, d_b, n, d_c, d_err, st);
+  int h_err = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_err);
+  if (e != cudaSuccess) return cuda_fail(e, "umma self-test");
+  return mrmg_status_from_error_bits(h_err);
+}
+
 int mrmg_binary_search_indices(int64_t N, int64_t* d_out, int32_t chunked, void* stream) {
   if (N < 0 || (N > 0 && !d_out)) return fail(MRMG_ERR_ARG, "N / out");
   if (N == 0) return MRMG_OK;

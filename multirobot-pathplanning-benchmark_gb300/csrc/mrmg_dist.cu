@@ -16,30 +16,6 @@ namespace {
 constexpr int kQTile = 16;        // queries per CTA (shared memory)
 constexpr int kMaxTileD = 128;    // coordinates staged per query
 
-// distance of one diff row: d(k) = a[k] - b[k]
-template <class Diff>
-__device__ __forceinline__ double dist_of(const SliceTab& t, int metric, Diff d) {
-  if (metric == MRMG_METRIC_EUCLIDEAN) {
-    double acc = 0.0;
-    for (int k = 0; k < t.end_all; k++) { double v = d(k); acc = __dadd_rn(acc, __dmul_rn(v, v)); }
-    return sqrt(acc);
-  }
-  if (metric == MRMG_METRIC_MAX) {
-    double m = fabs(d(0));
-    for (int k = 1; k < t.D; k++) { double v = fabs(d(k)); if (v > m) m = v; }
-    return m;
-  }
-  double red = 0.0;
-  for (int i = 0; i < t.A; i++) {
-    double acc = 0.0;
-    for (int k = t.s[i]; k < t.e[i]; k++) { double v = d(k); acc = __dadd_rn(acc, __dmul_rn(v, v)); }
-    const double r = sqrt(acc);
-    if (metric == MRMG_METRIC_SUM_EUCLIDEAN) red = __dadd_rn(red, r);
-    else if (i == 0 || r > red) red = r;
-  }
-  return red;
-}
-
 // out[q, m] = dist(queries[q] - nodes[m])
 __global__ void dist_matrix_kernel(const double* __restrict__ qs, long long Q, const double* __restrict__ nodes,
                                    long long M, SliceTab t, int metric, double* __restrict__ out) {

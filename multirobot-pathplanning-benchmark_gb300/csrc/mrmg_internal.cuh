@@ -83,6 +83,37 @@ struct LaunchShape {
   int num_sms;
 };
 
+struct SliceTab {
+  int A, D, end_all;
+  int s[64], e[64];
+};
+
+// FP64 distance of one difference row d(k) = a[k] - b[k] with the reference's
+// operation order (NpConfiguration._batch_dist, core/configuration.py:303-329:
+// sequential unfused sums of d*d, IEEE sqrt, strict '>' maxima)
+template <class Diff>
+__device__ __forceinline__ double dist_of(const SliceTab& t, int metric, Diff d) {
+  if (metric == MRMG_METRIC_EUCLIDEAN) {
+    double acc = 0.0;
+    for (int k = 0; k < t.end_all; k++) { double v = d(k); acc = __dadd_rn(acc, __dmul_rn(v, v)); }
+    return sqrt(acc);
+  }
+  if (metric == MRMG_METRIC_MAX) {
+    double m = fabs(d(0));
+    for (int k = 1; k < t.D; k++) { double v = fabs(d(k)); if (v > m) m = v; }
+    return m;
+  }
+  double red = 0.0;
+  for (int i = 0; i < t.A; i++) {
+    double acc = 0.0;
+    for (int k = t.s[i]; k < t.e[i]; k++) { double v = d(k); acc = __dadd_rn(acc, __dmul_rn(v, v)); }
+    const double r = sqrt(acc);
+    if (metric == MRMG_METRIC_SUM_EUCLIDEAN) red = __dadd_rn(red, r);
+    else if (i == 0 || r > red) red = r;
+  }
+  return red;
+}
+
 // host launchers ------------------------------------------------------------
 cudaError_t abstract_configs(const AbstractDev& s, const void* q, int dtype, long long n,
                              uint8_t* out, const CallScratch& sc, const LaunchShape& ls,
@@ -108,10 +139,12 @@ int arm_gpl_for_spg(int spg);
 
 cudaError_t binary_indices(long long N, long long* out, cudaStream_t st, int chunked);
 
-struct SliceTab {
-  int A, D, end_all;
-  int s[64], e[64];
-};
+
+cudaError_t knn_exact(const double* qs, long long Q, const int* q_mode, const long long* q_list, long long n_list,
+                      const double* nodes, const long long* mode_off, const SliceTab& t, int metric, int k,
+                      long long* out_idx, double* out_dist, int num_sms, cudaStream_t st);
+cudaError_t umma_selftest(const void* A, const void* B, int N, float* C, int* err, cudaStream_t st);
+
 cudaError_t dist_matrix(const double* qs, long long Q, const double* nodes, long long M, const SliceTab& t, int metric,
                         double* out, int num_sms, cudaStream_t st);
 cudaError_t batch_cost(const double* a, const double* b, long long M, const SliceTab& t, int cmetric, int red, double w,

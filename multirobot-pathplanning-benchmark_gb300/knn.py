@@ -1,0 +1,46 @@
+"""Per-mode k nearest neighbours on the GB300 (PRM get_neighbors,
+planners/prm/prm_graph.py:389-549; RRT nearest, planners/rrtstar_base.py:1228-1254).
+
+Indices are local to the query's mode and bit-identical to the reference's
+selection over its FP64 distances (ties, unspecified in the reference, go to
+the lower index)."""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .collision import _dev_tensor
+
+
+def _slices_arr(slices) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(slices, dtype=np.int64).reshape(-1, 2))
+
+
+def knn_exact(queries, query_mode, nodes, mode_offsets, slices, metric: str, k: int, stream=None):
+    """Exact FP64 k-NN (warp per query).  Returns (idx int64 [Q, k], dist float64 [Q, k]) on the device."""
+    lib = _lib.load()
+    qs = _dev_tensor(queries, dtype=torch.float64)
+    nd = _dev_tensor(nodes, dtype=torch.float64, device=qs.device)
+    qm = torch.as_tensor(np.asarray(query_mode, dtype=np.int32) if not isinstance(query_mode, torch.Tensor)
+                         else query_mode.to(torch.int32)).to(qs.device).contiguous()
+    mo = torch.as_tensor(np.asarray(mode_offsets, dtype=np.int64) if not isinstance(mode_offsets, torch.Tensor)
+                         else mode_offsets.to(torch.int64)).to(qs.device).contiguous()
+    sl = _slices_arr(slices)
+    Q, D = qs.shape
+    idx = torch.empty((Q, k), dtype=torch.int64, device=qs.device)
+    dist = torch.empty((Q, k), dtype=torch.float64, device=qs.device)
+    _lib.check(lib.mrmg_knn_exact(qs.data_ptr(), Q, qm.data_ptr(), nd.data_ptr(), mo.data_ptr(), D, sl.ctypes.data,
+                                  len(sl), _lib.METRICS[metric], int(k), idx.data_ptr(), dist.data_ptr(),
+                                  _lib.stream_handle(stream), 0), "knn")
+    return idx, dist
+
+
+def selftest_umma(a_bf16: torch.Tensor, b_bf16: torch.Tensor) -> torch.Tensor:
+    """C = A @ B^T through the tcgen05 path (A [128, 64], B [n, 64], BF16)."""
+    lib = _lib.load()
+    n = b_bf16.shape[0]
+    c = torch.zeros((128, n), dtype=torch.float32, device="cuda")
+    _lib.check(lib.mrmg_selftest_umma(a_bf16.contiguous().data_ptr(), b_bf16.contiguous().data_ptr(), n, c.data_ptr(),
+                                      _lib.stream_handle(None)), "umma self-test")
+    return c
