@@ -265,6 +265,28 @@ int mrmg_knn_exact(const double *d_queries, int64_t Q, const int32_t *d_query_mo
                    const int64_t *h_slices, int32_t A, int32_t metric, int32_t k, int64_t *d_idx,
                    double *d_dist, void *stream, int32_t flags);
 
+/* Per-mode node store for repeated k-NN queries (the planners' per-mode node
+ * arrays: PRM node_array_cache, prm_graph.py:399-402; RRT batch_subtree,
+ * rrtstar_base.py:254-306).  d_nodes[M, D] (FP64, caller-owned, must stay
+ * alive and unchanged while the store lives) is grouped by mode:
+ * h_mode_offsets[n_modes + 1].  For euclidean (D <= 29) and max_euclidean
+ * (<= 4 agents of <= 7 coordinates) the store packs split-BF16 tiles for the
+ * tensor-core candidate path; other metrics use the exact kernel. */
+typedef struct mrmg_node_store mrmg_node_store;
+int mrmg_node_store_create(const double *d_nodes, int64_t M, int32_t D, const int64_t *h_mode_offsets,
+                           int32_t n_modes, const int64_t *h_slices, int32_t A, int32_t metric,
+                           mrmg_node_store **out, void *stream);
+int mrmg_node_store_destroy(mrmg_node_store *store);
+
+/* k nearest neighbours of d_queries[Q, D] within their modes h_query_mode[Q]
+ * (host array): same result as mrmg_knn_exact -- on the tensor-core path the
+ * tcgen05 distance GEMM selects candidates, a certificate proves they contain
+ * the true k nearest (else the query reruns exactly) and FP64 re-ranks them.
+ * out_stats2 (optional): [0] tensor-core path used, [1] queries rerun exactly.
+ * Synchronises its stream. */
+int mrmg_knn(mrmg_node_store *store, const double *d_queries, int64_t Q, const int32_t *h_query_mode,
+             int32_t k, int64_t *d_idx, double *d_dist, int64_t *out_stats2, void *stream);
+
 /* Tensor-core self-test (no counterpart in the reference): C[128 x n] =
  * A[128 x 64] * B[n x 64]^T for row-major BF16 A, B through the same shared-
  * memory descriptors, instruction descriptor and tensor-memory path as the

@@ -62,6 +62,9 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_microbench_fma": (i32, [i32, i64, vp, vp]),
     "mrmg_knn_exact": (i32, [vp, i64, vp, vp, vp, i32, vp, i32, i32, i32, vp, vp, vp, i32]),
     "mrmg_selftest_umma": (i32, [vp, vp, i32, vp, vp]),
+    "mrmg_node_store_create": (i32, [vp, i64, i32, vp, i32, vp, i32, i32, C.POINTER(vp), vp]),
+    "mrmg_node_store_destroy": (i32, [vp]),
+    "mrmg_knn": (i32, [vp, vp, i64, vp, i32, vp, vp, vp, vp]),
 }
 
 

@@ -766,6 +766,103 @@ int mrmg_knn_exact(const double* d_queries, int64_t Q, const int32_t* d_query_mo
   return sync_unless_async(st, flags, "knn");
 }
 
+}  // extern "C"
+
+struct mrmg_node_store {
+  KnnStore* tc = nullptr;       // tensor-core candidate store (supported metric / shape)
+  KnnScratch* scratch = nullptr;
+  SliceTab t{};
+  int metric = 0;
+  int n_modes = 0;
+  long long M = 0;
+  const double* nodes = nullptr;
+  long long* d_mode_off = nullptr;   // exact path
+  int* d_qmode = nullptr;            // exact path: uploaded query modes
+  long long qmode_cap = 0;
+  long long last_fallback = 0;
+};
+
+extern "C" {
+
+int mrmg_node_store_create(const double* d_nodes, int64_t M, int32_t D, const int64_t* h_mode_offsets,
+                           int32_t n_modes, const int64_t* h_slices, int32_t A, int32_t metric,
+                           mrmg_node_store** out, void* stream) {
+  if (!out) return fail(MRMG_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (M < 0 || n_modes < 1 || metric < 0 || metric > 3 || !h_mode_offsets) return fail(MRMG_ERR_ARG, "M / modes / metric");
+  if (h_mode_offsets[0] != 0 || h_mode_offsets[n_modes] != M) return fail(MRMG_ERR_ARG, "mode offsets must span [0, M]");
+  for (int m = 0; m < n_modes; m++)
+    if (h_mode_offsets[m + 1] < h_mode_offsets[m]) return fail(MRMG_ERR_ARG, "mode offsets must not decrease");
+  if (M > 0 && !d_nodes) return fail(MRMG_ERR_ARG, "NULL nodes");
+  SliceTab t;
+  int rc = make_slices(h_slices, A, D, &t);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  mrmg_node_store* s = new mrmg_node_store();
+  s->t = t;
+  s->metric = metric;
+  s->n_modes = n_modes;
+  s->M = M;
+  s->nodes = d_nodes;
+  s->scratch = knn_scratch_new();
+  cudaError_t e = cudaMalloc(&s->d_mode_off, sizeof(long long) * (n_modes + 1));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->d_mode_off, h_mode_offsets, sizeof(long long) * (n_modes + 1), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && knn_tc_supported(t, metric)) {
+    s->tc = knn_store_new();
+    e = knn_store_build(s->tc, d_nodes, M, (const long long*)h_mode_offsets, n_modes, t, metric, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) { mrmg_node_store_destroy(s); return cuda_fail(e, "node store"); }
+  *out = s;
+  return MRMG_OK;
+}
+
+int mrmg_node_store_destroy(mrmg_node_store* s) {
+  if (!s) return MRMG_OK;
+  knn_store_delete(s->tc);
+  knn_scratch_delete(s->scratch);
+  if (s->d_mode_off) cudaFree(s->d_mode_off);
+  if (s->d_qmode) cudaFree(s->d_qmode);
+  delete s;
+  return MRMG_OK;
+}
+
+int mrmg_knn(mrmg_node_store* s, const double* d_queries, int64_t Q, const int32_t* h_query_mode, int32_t k,
+             int64_t* d_idx, double* d_dist, int64_t* out_stats2, void* stream) {
+  if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
+  if (Q < 0 || k < 1 || k > 64) return fail(MRMG_ERR_ARG, "Q / k (1..64)");
+  if (Q == 0) return MRMG_OK;
+  if (!d_queries || !h_query_mode || !d_idx || !d_dist) return fail(MRMG_ERR_ARG, "NULL pointer");
+  for (long long q = 0; q < Q; q++)
+    if (h_query_mode[q] < 0 || h_query_mode[q] >= s->n_modes) return fail(MRMG_ERR_ARG, "query %lld: mode out of range", q);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaSuccess;
+  int nfb = 0;
+  bool tc = s->tc && k <= 16;
+  if (tc) {
+    e = knn_query(s->tc, d_queries, Q, h_query_mode, k, (long long*)d_idx, d_dist, s->scratch, device_sms(), &nfb, st);
+    if (e == cudaErrorLaunchTimeout) return fail(MRMG_ERR_TIMEOUT, "a bounded tensor-core pipeline wait ran out");
+  } else {
+    if (s->qmode_cap < Q) {
+      if (s->d_qmode) cudaFree(s->d_qmode);
+      s->d_qmode = nullptr;
+      e = cudaMalloc(&s->d_qmode, sizeof(int) * Q);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+      s->qmode_cap = Q;
+    }
+    e = cudaMemcpyAsync(s->d_qmode, h_query_mode, sizeof(int) * Q, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = knn_exact(d_queries, Q, s->d_qmode, nullptr, 0, s->nodes, s->d_mode_off, s->t, s->metric, k,
+                    (long long*)d_idx, d_dist, device_sms(), st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "knn");
+  s->last_fallback = nfb;
+  if (out_stats2) { out_stats2[0] = tc ? 1 : 0; out_stats2[1] = nfb; }
+  return MRMG_OK;
+}
+
 int mrmg_selftest_umma(const void* d_a, const void* d_b, int32_t n, float* d_c, void* stream) {
   if (n < 32 || n > 256 || n % 32) return fail(MRMG_ERR_ARG, "n must be 32..256, a multiple of 32");
   cudaStream_t st = (cudaStream_t)stream;

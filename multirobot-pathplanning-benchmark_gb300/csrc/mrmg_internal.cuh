@@ -143,6 +143,18 @@ cudaError_t binary_indices(long long N, long long* out, cudaStream_t st, int chu
 cudaError_t knn_exact(const double* qs, long long Q, const int* q_mode, const long long* q_list, long long n_list,
                       const double* nodes, const long long* mode_off, const SliceTab& t, int metric, int k,
                       long long* out_idx, double* out_dist, int num_sms, cudaStream_t st);
+struct KnnStore;
+struct KnnScratch;
+bool knn_tc_supported(const SliceTab& t, int metric);
+cudaError_t knn_store_build(KnnStore* s, const double* d_nodes, long long M, const long long* h_mode_off, int n_modes,
+                            const SliceTab& t, int metric, cudaStream_t st);
+void knn_store_free(KnnStore* s);
+cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h_q_mode, int k, long long* d_idx,
+                      double* d_dist, KnnScratch* scr, int num_sms, int* n_fallback_out, cudaStream_t st);
+KnnStore* knn_store_new();
+void knn_store_delete(KnnStore* s);
+KnnScratch* knn_scratch_new();
+void knn_scratch_delete(KnnScratch* s);
 cudaError_t umma_selftest(const void* A, const void* B, int N, float* C, int* err, cudaStream_t st);
 
 cudaError_t dist_matrix(const double* qs, long long Q, const double* nodes, long long M, const SliceTab& t, int metric,

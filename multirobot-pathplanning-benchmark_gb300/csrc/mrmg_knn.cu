@@ -294,3 +294,585 @@ cudaError_t umma_selftest(const void* A, const void* B, int N, float* C, int* er
 }
 
 }  // namespace mrmg
+
+// ===========================================================================
+// Tensor-core candidate path
+// ===========================================================================
+namespace mrmg {
+
+// node-store formats
+enum : int { KNN_FMT_EUCL = 0, KNN_FMT_AGENT = 1 };
+constexpr int kNtEucl = 256, kNtAgent = 64;
+
+struct KnnItem {          // one CTA: a query tile of one mode against a chunk of its node tiles
+  int mode, q0, qn;       // queries qorder[q0 .. q0+qn)
+  int tile0, tile1;       // node tiles [tile0, tile1) of the mode (mode-local tile index)
+  int chunk;              // chunk slot of this item in the candidate lists
+  int pad;
+};
+
+struct KnnStoreDev {
+  int fmt, NT, D, A;
+  int agent_s[4], agent_e[4];
+  const unsigned char* tiles;     // packed SW128 tiles
+  const long long* mode_off;      // node ranges (device)
+  const int* mode_tile0;          // first global tile of each mode
+  const float* mode_xmax;         // max |x| of each mode (for the error bound)
+};
+
+namespace {
+
+__device__ __forceinline__ void put_bf16(unsigned char* row_base_tile, int row, int col, float v) {
+  *(__nv_bfloat16*)(row_base_tile + sw128_off(row, col)) = __float2bfloat16_rn(v);
+}
+
+// split x into bf16 hi + lo (both as floats)
+__device__ __forceinline__ void split2(double x, float* hi, float* lo) {
+  const float xf = (float)x;
+  const float h = __bfloat162float(__float2bfloat16_rn(xf));
+  *hi = h;
+  *lo = __bfloat162float(__float2bfloat16_rn((float)(x - (double)h)));
+}
+
+__global__ void knn_pack_kernel(const double* __restrict__ nodes, KnnStoreDev st, int n_modes, long long total_rows,
+                                unsigned char* __restrict__ tiles, float* __restrict__ xmax_out) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total_rows;
+       g += (long long)gridDim.x * blockDim.x) {
+    const long long tile = g / st.NT;
+    const int row = (int)(g % st.NT);
+    // find the mode of this tile (few modes: linear scan)
+    int m = 0;
+    while (m + 1 < n_modes && st.mode_tile0[m + 1] <= tile) m++;
+    const long long local = (tile - st.mode_tile0[m]) * st.NT + row;
+    const long long node = st.mode_off[m] + local;
+    unsigned char* t = tiles + tile * (long long)st.NT * kRowBytes;
+    for (int c = 0; c < 64; c++) put_bf16(t, row, c, 0.f);
+    if (node >= st.mode_off[m + 1]) {     // padding row: a huge |x|^2 term, never selected
+      if (st.fmt == KNN_FMT_EUCL) put_bf16(t, row, st.D, 1.0e30f);
+      else for (int a = 0; a < st.A; a++) put_bf16(t, row, 16 * a + 2 * (st.agent_e[a] - st.agent_s[a]), 1.0e30f);
+      continue;
+    }
+    const double* x = nodes + node * st.D;
+    double n2 = 0.0;
+    if (st.fmt == KNN_FMT_EUCL) {
+      for (int j = 0; j < st.D; j++) {
+        float h, l;
+        split2(x[j], &h, &l);
+        put_bf16(t, row, j, h);
+        put_bf16(t, row, st.D + 3 + j, l);
+        n2 += x[j] * x[j];
+      }
+      const float a1 = __bfloat162float(__float2bfloat16_rn((float)n2));
+      const double r1 = n2 - (double)a1;
+      const float a2 = __bfloat162float(__float2bfloat16_rn((float)r1));
+      const float a3 = (float)(r1 - (double)a2);
+      put_bf16(t, row, st.D, a1);
+      put_bf16(t, row, st.D + 1, a2);
+      put_bf16(t, row, st.D + 2, a3);
+    } else {
+      for (int a = 0; a < st.A; a++) {
+        const int s = st.agent_s[a], d = st.agent_e[a] - s;
+        double na = 0.0;
+        for (int j = 0; j < d; j++) {
+          float h, l;
+          split2(x[s + j], &h, &l);
+          put_bf16(t, row, 16 * a + j, h);
+          put_bf16(t, row, 16 * a + d + j, l);
+          na += x[s + j] * x[s + j];
+        }
+        const float a1 = __bfloat162float(__float2bfloat16_rn((float)na));
+        put_bf16(t, row, 16 * a + 2 * d, a1);
+        put_bf16(t, row, 16 * a + 2 * d + 1, (float)(na - (double)a1));
+        n2 += na;
+      }
+    }
+    atomicMax((int*)&xmax_out[m], __float_as_int((float)sqrt(n2) * 1.000001f));   // non-negative floats order as ints
+  }
+}
+
+// per-thread sorted candidate list (approximate squared distance, local index)
+__device__ __forceinline__ void keep_insert(float (&kd)[kKeep], int (&ki)[kKeep], float d, int id) {
+  if (!(d < kd[kKeep - 1])) return;
+#pragma unroll
+  for (int i = kKeep - 1; i > 0; i--) {
+    if (d < kd[i - 1]) { kd[i] = kd[i - 1]; ki[i] = ki[i - 1]; }
+    else if (d < kd[i]) { kd[i] = d; ki[i] = id; }
+  }
+  if (d < kd[0]) { kd[0] = d; ki[0] = id; }
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(128, 1) knn_tc_kernel(KnnStoreDev st, const double* __restrict__ qs,
+                                                        const int* __restrict__ qorder, const KnnItem* __restrict__ items,
+                                                        int chunks_max, float* __restrict__ cand_d,
+                                                        int* __restrict__ cand_i, float* __restrict__ q_eps,
+                                                        int* __restrict__ err) {
+  constexpr int NT = FMT == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
+  constexpr uint32_t BT = NT * kRowBytes;   // bytes per node tile
+  extern __shared__ __align__(1024) unsigned char sm_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)sm_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sA1 = base;
+  unsigned char* sA2 = base + kTileM * kRowBytes;
+  unsigned char* sB0 = base + 2 * kTileM * kRowBytes;
+  __shared__ uint64_t bar_load[2], bar_mma[2];
+  __shared__ uint32_t tbase;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const KnnItem it = items[blockIdx.x];
+  const int D = st.D;
+
+  if (tid == 0) {
+    mbar_init(&bar_load[0], 1); mbar_init(&bar_load[1], 1);
+    mbar_init(&bar_mma[0], 1); mbar_init(&bar_mma[1], 1);
+    s_fail = 0;
+    fence_barrier_init();
+  }
+  if (warp == 0) tmem_alloc(&tbase, 512);
+
+  // ---- the query tile: A1 = [q_hi | -1/2 ... | q_hi], A2 = [q_lo]; one thread per row
+  float qn = 0.f, qna[4] = {0.f, 0.f, 0.f, 0.f};
+  long long qid = -1;
+  {
+    const int r = tid;
+    for (int c = 0; c < 64; c++) {
+      *(__nv_bfloat16*)(sA1 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
+      *(__nv_bfloat16*)(sA2 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
+    }
+    if (r < it.qn) {
+      qid = qorder[it.q0 + r];
+      const double* q = qs + qid * D;
+      if (FMT == KNN_FMT_EUCL) {
+        double n2 = 0.0;
+        for (int j = 0; j < D; j++) {
+          float h, l;
+          split2(q[j], &h, &l);
+          *(__nv_bfloat16*)(sA1 + sw128_off(r, j)) = __float2bfloat16_rn(h);
+          *(__nv_bfloat16*)(sA1 + sw128_off(r, D + 3 + j)) = __float2bfloat16_rn(h);
+          *(__nv_bfloat16*)(sA2 + sw128_off(r, j)) = __float2bfloat16_rn(l);
+          n2 += q[j] * q[j];
+        }
+        for (int c = 0; c < 3; c++) *(__nv_bfloat16*)(sA1 + sw128_off(r, D + c)) = __float2bfloat16_rn(-0.5f);
+        qn = (float)n2;
+      } else {
+        for (int a = 0; a < st.A; a++) {
+          const int s = st.agent_s[a], d = st.agent_e[a] - s;
+          double na = 0.0;
+          for (int j = 0; j < d; j++) {
+            float h, l;
+            split2(q[s + j], &h, &l);
+            *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(h);
+            *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + d + j)) = __float2bfloat16_rn(h);
+            *(__nv_bfloat16*)(sA2 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(l);
+            na += q[s + j] * q[s + j];
+          }
+          *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + 2 * d)) = __float2bfloat16_rn(-0.5f);
+          *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + 2 * d + 1)) = __float2bfloat16_rn(-0.5f);
+          qna[a] = (float)na;
+          qn += (float)na;
+        }
+      }
+      // error bound of the approximate squared distance (split-BF16 operands,
+      // FP32 accumulation), per query; stored once per query
+      if (it.chunk == 0) {
+        const float s = sqrtf(qn) + st.mode_xmax[it.mode];
+        q_eps[qid] = 1.2e-4f * s * s + 1e-30f;
+      }
+    }
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = tbase;
+  const int T = it.tile1 - it.tile0;
+  const unsigned char* gtiles = st.tiles + (long long)(st.mode_tile0[it.mode] + it.tile0) * BT;
+  const uint32_t idesc = idesc_bf16(kTileM, NT);
+
+  auto issue_load = [&](int t) {
+    unsigned char* dst = sB0 + (t & 1) * BT;
+    mbar_expect_tx(&bar_load[t & 1], BT);
+    bulk_g2s(dst, gtiles + (long long)t * BT, BT, &bar_load[t & 1]);
+  };
+  auto issue_mma = [&](int t) {
+    const uint32_t a1 = su32(sA1), a2 = su32(sA2), b = su32(sB0 + (t & 1) * BT);
+    const uint32_t dcol = tm + (uint32_t)((t & 1) * 256);
+    if (FMT == KNN_FMT_EUCL) {
+      for (int s = 0; s < 4; s++) umma_bf16(dcol, sw128_desc(a1 + 32 * s), sw128_desc(b + 32 * s), idesc, s > 0);
+      const int s2 = (D + 15) / 16;
+      for (int s = 0; s < s2; s++) umma_bf16(dcol, sw128_desc(a2 + 32 * s), sw128_desc(b + 32 * s), idesc, 1);
+    } else {
+      for (int a = 0; a < st.A; a++) {
+        umma_bf16(dcol + 64 * a, sw128_desc(a1 + 32 * a), sw128_desc(b + 32 * a), idesc, 0);
+        umma_bf16(dcol + 64 * a, sw128_desc(a2 + 32 * a), sw128_desc(b + 32 * a), idesc, 1);
+      }
+    }
+    umma_commit(&bar_mma[t & 1]);
+  };
+
+  if (tid == 0 && T > 0) {
+    issue_load(0);
+    if (T > 1) issue_load(1);
+    if (mbar_wait(&bar_load[0], 0)) issue_mma(0);
+    else s_fail = 1;
+  }
+
+  float kd[kKeep];
+  int ki[kKeep];
+#pragma unroll
+  for (int i = 0; i < kKeep; i++) { kd[i] = __int_as_float(0x7f800000); ki[i] = -1; }
+
+  for (int t = 0; t < T; t++) {
+    if (tid == 0 && t + 1 < T && !s_fail) {
+      if (mbar_wait(&bar_load[(t + 1) & 1], ((t + 1) >> 1) & 1)) issue_mma(t + 1);
+      else s_fail = 1;
+    }
+    const bool done = mbar_wait(&bar_mma[t & 1], (t >> 1) & 1);
+    if (!done) s_fail = 1;
+    tc_fence_after();
+    if (tid == 0 && t + 2 < T && done) issue_load(t + 2);   // tile t's MMAs have read its buffer
+    if (done) {
+      const int col_node0 = (it.tile0 + t) * NT;
+      const uint32_t lane_base = tm + ((uint32_t)(32 * warp) << 16) + (uint32_t)((t & 1) * 256);
+      if (FMT == KNN_FMT_EUCL) {
+        for (int c0 = 0; c0 < NT; c0 += 32) {
+          float v[32];
+          tmem_ld32(lane_base + c0, v);
+#pragma unroll
+          for (int i = 0; i < 32; i++) keep_insert(kd, ki, fmaf(-2.f, v[i], qn), col_node0 + c0 + i);
+        }
+      } else {
+        for (int c0 = 0; c0 < NT; c0 += 32) {
+          float m[32];
+#pragma unroll
+          for (int i = 0; i < 32; i++) m[i] = -__int_as_float(0x7f800000);
+          for (int a = 0; a < st.A; a++) {
+            float v[32];
+            tmem_ld32(lane_base + 64 * a + c0, v);
+            const float qa = qna[a];
+#pragma unroll
+            for (int i = 0; i < 32; i++) m[i] = fmaxf(m[i], fmaf(-2.f, v[i], qa));
+          }
+#pragma unroll
+          for (int i = 0; i < 32; i++) keep_insert(kd, ki, m[i], col_node0 + c0 + i);
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (s_fail) break;
+  }
+  if (s_fail && tid == 0) atomicOr(err, E_TIMEOUT);
+  (void)lane;
+  if (qid >= 0) {
+    float* od = cand_d + ((size_t)qid * chunks_max + it.chunk) * kKeep;
+    int* oi = cand_i + ((size_t)qid * chunks_max + it.chunk) * kKeep;
+#pragma unroll
+    for (int i = 0; i < kKeep; i++) { od[i] = kd[i]; oi[i] = ki[i]; }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tm, 512);
+}
+
+// ---------------------------------------------------------------------------
+// merge: certify the kept candidates and re-rank them in exact FP64
+// ---------------------------------------------------------------------------
+__global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
+                                 const double* __restrict__ nodes, const long long* __restrict__ mode_off,
+                                 const int* __restrict__ mode_chunks, int chunks_max, const float* __restrict__ cand_d,
+                                 const int* __restrict__ cand_i, const float* __restrict__ q_eps, SliceTab t,
+                                 int metric, int k, long long* __restrict__ out_idx, double* __restrict__ out_dist,
+                                 long long* __restrict__ fallback, int* __restrict__ n_fallback) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  const float INF = __int_as_float(0x7f800000);
+  const double DINF = __longlong_as_double(0x7ff0000000000000ll);
+  for (long long q = warp; q < Q; q += nwarps) {
+    const int m = q_mode[q];
+    const long long M = mode_off[m + 1] - mode_off[m];
+    const int C = mode_chunks[m];
+    if (M == 0 || C == 0) {
+      for (int r = lane; r < k; r += 32) { out_idx[q * k + r] = -1; out_dist[q * k + r] = DINF; }
+      continue;
+    }
+    // lane l holds chunks l and l + 32 (C <= 64)
+    const float* cd = cand_d + (size_t)q * chunks_max * kKeep;
+    const int* ci = cand_i + (size_t)q * chunks_max * kKeep;
+    int h0 = 0, h1 = 0;
+    const int c0 = lane, c1 = lane + 32;
+    // approximate k-th smallest value by k rounds of a warp argmin over list heads
+    float kth = INF;
+    for (int r = 0; r < k; r++) {
+      const float v0 = (c0 < C && h0 < kKeep) ? cd[c0 * kKeep + h0] : INF;
+      const float v1 = (c1 < C && h1 < kKeep) ? cd[c1 * kKeep + h1] : INF;
+      float v = fminf(v0, v1);
+      float b = v;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) b = fminf(b, __shfl_xor_sync(MRMG_FULL, b, o));
+      kth = b;
+      const unsigned who = __ballot_sync(MRMG_FULL, v == b);
+      if (b == INF) break;
+      if (lane == __ffs(who) - 1) { if (v0 <= v1) h0++; else h1++; }
+    }
+    const float tau = kth == INF ? INF : kth + 2.f * q_eps[q];
+    // certified when every full list ends above tau
+    bool unsafe = false;
+    if (c0 < C) unsafe |= ci[c0 * kKeep + kKeep - 1] >= 0 && !(cd[c0 * kKeep + kKeep - 1] > tau);
+    if (c1 < C) unsafe |= ci[c1 * kKeep + kKeep - 1] >= 0 && !(cd[c1 * kKeep + kKeep - 1] > tau);
+    if (__any_sync(MRMG_FULL, unsafe)) {
+      if (lane == 0) { const int s = atomicAdd(n_fallback, 1); fallback[s] = q; }
+      continue;
+    }
+    // exact FP64 re-rank of every candidate within tau
+    double td[kKnnMaxK > 16 ? 16 : kKnnMaxK];
+    long long tix[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) { td[i] = DINF; tix[i] = -1; }
+    const double* qq = qs + q * t.D;
+    for (int cc = lane; cc < C; cc += 32)
+      for (int j = 0; j < kKeep; j++) {
+        const int id = ci[cc * kKeep + j];
+        if (id < 0 || id >= M || !(cd[cc * kKeep + j] <= tau)) continue;
+        const double* xx = nodes + (mode_off[m] + id) * t.D;
+        auto dfun = [&](int jj) { return __dsub_rn(qq[jj], xx[jj]); };
+        topk_insert<16>(td, tix, k < 16 ? k : 16, dist_of(t, metric, dfun), id);
+      }
+    int head = 0;
+    for (int r = 0; r < k; r++) {
+      double hd = DINF;
+      long long hi = 0x7fffffffffffffffll;
+#pragma unroll
+      for (int i = 0; i < 16; i++)
+        if (i == head) { hd = td[i]; hi = tix[i] < 0 ? 0x7fffffffffffffffll : tix[i]; }
+      const int win = warp_argmin(hd, hi);
+      const double wd = __shfl_sync(MRMG_FULL, hd, win);
+      const long long wi = __shfl_sync(MRMG_FULL, hi, win);
+      if (lane == 0) {
+        out_idx[q * k + r] = wi == 0x7fffffffffffffffll ? -1 : wi;
+        out_dist[q * k + r] = wi == 0x7fffffffffffffffll ? DINF : wd;
+      }
+      if (lane == win) head++;
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side: node store and query launch
+// ---------------------------------------------------------------------------
+struct KnnStore {
+  KnnStoreDev dev;
+  SliceTab slices;
+  int metric = 0;
+  int n_modes = 0;
+  std::vector<long long> mode_off;       // host copy
+  std::vector<int> mode_tiles;           // tiles per mode
+  const double* nodes = nullptr;         // caller-owned FP64 nodes
+  void* block = nullptr;                 // device allocation: tiles, offsets, per-mode data
+  long long total_tiles = 0;
+};
+
+bool knn_tc_supported(const SliceTab& t, int metric) {
+  if (metric == MRMG_METRIC_EUCLIDEAN) return t.end_all == t.D && t.D >= 1 && 2 * t.D + 3 <= 64;
+  if (metric == MRMG_METRIC_MAX_EUCLIDEAN) {
+    if (t.A < 1 || t.A > 4) return false;
+    for (int i = 0; i < t.A; i++)
+      if (t.e[i] - t.s[i] < 1 || 2 * (t.e[i] - t.s[i]) + 2 > 16) return false;
+    return true;
+  }
+  return false;
+}
+
+cudaError_t knn_store_build(KnnStore* s, const double* d_nodes, long long M, const long long* h_mode_off, int n_modes,
+                            const SliceTab& t, int metric, cudaStream_t st) {
+  s->slices = t;
+  s->metric = metric;
+  s->n_modes = n_modes;
+  s->nodes = d_nodes;
+  s->mode_off.assign(h_mode_off, h_mode_off + n_modes + 1);
+  const int fmt = metric == MRMG_METRIC_EUCLIDEAN ? KNN_FMT_EUCL : KNN_FMT_AGENT;
+  const int NT = fmt == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
+  std::vector<int> tile0(n_modes + 1, 0);
+  s->mode_tiles.assign(n_modes, 0);
+  for (int m = 0; m < n_modes; m++) {
+    const long long cnt = h_mode_off[m + 1] - h_mode_off[m];
+    s->mode_tiles[m] = (int)((cnt + NT - 1) / NT);
+    tile0[m + 1] = tile0[m] + s->mode_tiles[m];
+  }
+  s->total_tiles = tile0[n_modes];
+  const size_t tiles_bytes = (size_t)std::max<long long>(s->total_tiles, 1) * NT * kRowBytes;
+  const size_t off_bytes = sizeof(long long) * (n_modes + 1);
+  const size_t t0_bytes = sizeof(int) * (n_modes + 1);
+  const size_t xm_bytes = sizeof(float) * n_modes;
+  auto al = [](size_t x) { return (x + 1023) & ~(size_t)1023; };
+  const size_t total = al(tiles_bytes) + al(off_bytes) + al(t0_bytes) + al(xm_bytes);
+  cudaError_t e = cudaMalloc(&s->block, total);
+  if (e != cudaSuccess) return e;
+  unsigned char* b = (unsigned char*)s->block;
+  unsigned char* tiles = b;
+  long long* d_off = (long long*)(b + al(tiles_bytes));
+  int* d_t0 = (int*)((unsigned char*)d_off + al(off_bytes));
+  float* d_xm = (float*)((unsigned char*)d_t0 + al(t0_bytes));
+  e = cudaMemcpyAsync(d_off, h_mode_off, off_bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_t0, tile0.data(), t0_bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_xm, 0, xm_bytes, st);
+  if (e != cudaSuccess) return e;
+  KnnStoreDev& d = s->dev;
+  d.fmt = fmt;
+  d.NT = NT;
+  d.D = t.D;
+  d.A = t.A;
+  for (int i = 0; i < 4; i++) { d.agent_s[i] = i < t.A ? t.s[i] : 0; d.agent_e[i] = i < t.A ? t.e[i] : 0; }
+  d.tiles = tiles;
+  d.mode_off = d_off;
+  d.mode_tile0 = d_t0;
+  d.mode_xmax = d_xm;
+  const long long rows = s->total_tiles * NT;
+  if (rows > 0) {
+    const int grid = (int)std::min<long long>((rows + 255) / 256, 4096);
+    knn_pack_kernel<<<grid, 256, 0, st>>>(d_nodes, d, n_modes, rows, tiles, d_xm);
+  }
+  return cudaGetLastError();
+}
+
+void knn_store_free(KnnStore* s) {
+  if (s->block) cudaFree(s->block);
+  s->block = nullptr;
+}
+
+// scratch for one query launch, owned by the caller (the ABI layer)
+struct KnnScratch {
+  void* block = nullptr;
+  size_t bytes = 0;
+};
+
+cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h_q_mode, int k, long long* d_idx,
+                      double* d_dist, KnnScratch* scr, int num_sms, int* n_fallback_out, cudaStream_t st) {
+  const int n_modes = s->n_modes;
+  // group queries by mode
+  std::vector<int> order(Q), qcount(n_modes, 0), qstart(n_modes + 1, 0);
+  for (long long q = 0; q < Q; q++) qcount[h_q_mode[q]]++;
+  for (int m = 0; m < n_modes; m++) qstart[m + 1] = qstart[m] + qcount[m];
+  {
+    std::vector<int> fill(qstart.begin(), qstart.end() - 1);
+    for (long long q = 0; q < Q; q++) order[fill[h_q_mode[q]]++] = (int)q;
+  }
+  // work items: query tiles x node-tile chunks, about three waves of CTAs
+  long long units = 0;
+  for (int m = 0; m < n_modes; m++) units += (long long)((qcount[m] + kTileM - 1) / kTileM) * s->mode_tiles[m];
+  const long long target = std::max(1, 3 * num_sms);
+  int tpc = (int)std::max<long long>(1, (units + target - 1) / target);
+  int chunks_max = 1;
+  for (int m = 0; m < n_modes; m++) chunks_max = std::max(chunks_max, (s->mode_tiles[m] + tpc - 1) / tpc);
+  while (chunks_max > 64) {   // at most 64 candidate lists per query
+    tpc *= 2;
+    chunks_max = 1;
+    for (int m = 0; m < n_modes; m++) chunks_max = std::max(chunks_max, (s->mode_tiles[m] + tpc - 1) / tpc);
+  }
+  std::vector<KnnItem> items;
+  std::vector<int> mode_chunks(n_modes, 0);
+  for (int m = 0; m < n_modes; m++) {
+    if (qcount[m] == 0 || s->mode_tiles[m] == 0) continue;
+    const int nch = (s->mode_tiles[m] + tpc - 1) / tpc;
+    mode_chunks[m] = nch;
+    for (int q0 = 0; q0 < qcount[m]; q0 += kTileM)
+      for (int c = 0; c < nch; c++) {
+        KnnItem it;
+        it.mode = m;
+        it.q0 = qstart[m] + q0;
+        it.qn = std::min(kTileM, qcount[m] - q0);
+        it.tile0 = c * tpc;
+        it.tile1 = std::min(s->mode_tiles[m], (c + 1) * tpc);
+        it.chunk = c;
+        it.pad = 0;
+        items.push_back(it);
+      }
+  }
+  // scratch: order, q_mode, items, mode_chunks, cand lists, eps, fallback list, counters
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b_order = al(sizeof(int) * std::max<long long>(Q, 1));
+  const size_t b_qmode = b_order;
+  const size_t b_items = al(sizeof(KnnItem) * std::max<size_t>(items.size(), 1));
+  const size_t b_mch = al(sizeof(int) * std::max(n_modes, 1));
+  const size_t b_cd = al(sizeof(float) * std::max<long long>(Q, 1) * chunks_max * kKeep);
+  const size_t b_ci = b_cd;
+  const size_t b_eps = al(sizeof(float) * std::max<long long>(Q, 1));
+  const size_t b_fb = al(sizeof(long long) * std::max<long long>(Q, 1));
+  const size_t b_ctr = 256;
+  const size_t need = b_order + b_qmode + b_items + b_mch + b_cd + b_ci + b_eps + b_fb + b_ctr;
+  if (scr->bytes < need) {
+    if (scr->block) cudaFree(scr->block);
+    scr->block = nullptr;
+    cudaError_t e = cudaMalloc(&scr->block, need);
+    if (e != cudaSuccess) { scr->bytes = 0; return e; }
+    scr->bytes = need;
+  }
+  unsigned char* p = (unsigned char*)scr->block;
+  int* d_order = (int*)p; p += b_order;
+  int* d_qmode = (int*)p; p += b_qmode;
+  KnnItem* d_items = (KnnItem*)p; p += b_items;
+  int* d_mch = (int*)p; p += b_mch;
+  float* d_cd = (float*)p; p += b_cd;
+  int* d_ci = (int*)p; p += b_ci;
+  float* d_eps = (float*)p; p += b_eps;
+  long long* d_fb = (long long*)p; p += b_fb;
+  int* d_ctr = (int*)p;   // [0] fallback count, [1] error bits
+  std::vector<int> qm(h_q_mode, h_q_mode + Q);
+  cudaError_t e = cudaMemcpyAsync(d_order, order.data(), sizeof(int) * Q, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_qmode, qm.data(), sizeof(int) * Q, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !items.empty())
+    e = cudaMemcpyAsync(d_items, items.data(), sizeof(KnnItem) * items.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_mch, mode_chunks.data(), sizeof(int) * n_modes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, 256, st);
+  if (e != cudaSuccess) return e;
+  const int NT = s->dev.NT;
+  // at least 120 KB of shared memory: one CTA per SM, so two CTAs never wait
+  // on each other for the 512 tensor-memory columns each allocates
+  const size_t smem = std::max<size_t>(1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes, 120 * 1024);
+  if (!items.empty()) {
+    if (s->dev.fmt == KNN_FMT_EUCL) {
+      cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_EUCL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      knn_tc_kernel<KNN_FMT_EUCL><<<(int)items.size(), 128, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
+                                                                         d_cd, d_ci, d_eps, d_ctr + 1);
+    } else {
+      cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_AGENT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      knn_tc_kernel<KNN_FMT_AGENT><<<(int)items.size(), 128, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
+                                                                          d_cd, d_ci, d_eps, d_ctr + 1);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  const int mgrid = (int)std::min<long long>((Q + 3) / 4, (long long)num_sms * 16);
+  knn_merge_kernel<<<std::max(mgrid, 1), 128, 0, st>>>(d_qs, Q, d_qmode, s->nodes, s->dev.mode_off, d_mch, chunks_max,
+                                                       d_cd, d_ci, d_eps, s->slices, s->metric, k, d_idx, d_dist, d_fb,
+                                                       d_ctr);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  int h_ctr[2] = {0, 0};
+  e = cudaMemcpyAsync(h_ctr, d_ctr, sizeof(int) * 2, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  *n_fallback_out = h_ctr[0];
+  if (h_ctr[1]) return cudaErrorLaunchTimeout;
+  if (h_ctr[0] > 0) {
+    e = knn_exact(d_qs, Q, d_qmode, d_fb, h_ctr[0], s->nodes, s->dev.mode_off, s->slices, s->metric, k, d_idx, d_dist,
+                  num_sms, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+KnnStore* knn_store_new() { return new KnnStore(); }
+void knn_store_delete(KnnStore* s) {
+  if (s) { knn_store_free(s); delete s; }
+}
+KnnScratch* knn_scratch_new() { return new KnnScratch(); }
+void knn_scratch_delete(KnnScratch* s) {
+  if (s) { if (s->block) cudaFree(s->block); delete s; }
+}
+
+}  // namespace mrmg

@@ -44,3 +44,51 @@ def selftest_umma(a_bf16: torch.Tensor, b_bf16: torch.Tensor) -> torch.Tensor:
     _lib.check(lib.mrmg_selftest_umma(a_bf16.contiguous().data_ptr(), b_bf16.contiguous().data_ptr(), n, c.data_ptr(),
                                       _lib.stream_handle(None)), "umma self-test")
     return c
+
+
+class NodeStore:
+    """Per-mode node arrays resident on the device for repeated k-NN queries
+    (the planners' node_array_cache / batch_subtree).  Euclidean and
+    max_euclidean queries use the tensor-core candidate path (tcgen05 split-
+    BF16 distance GEMM, certified, FP64 re-rank); other metrics the exact one."""
+
+    def __init__(self, nodes, mode_offsets, slices, metric: str = "euclidean", stream=None):
+        import ctypes as C
+
+        self.lib = _lib.load()
+        self.nodes = _dev_tensor(nodes, dtype=torch.float64)
+        self.mode_offsets = np.ascontiguousarray(np.asarray(mode_offsets, dtype=np.int64))
+        self.slices = _slices_arr(slices)
+        self.metric = metric
+        self.D = self.nodes.shape[1]
+        h = C.c_void_p()
+        _lib.check(self.lib.mrmg_node_store_create(self.nodes.data_ptr(), self.nodes.shape[0], self.D,
+                                                   self.mode_offsets.ctypes.data, len(self.mode_offsets) - 1,
+                                                   self.slices.ctypes.data, len(self.slices), _lib.METRICS[metric],
+                                                   C.byref(h), _lib.stream_handle(stream)), "node store")
+        self.h = h
+        self.last_stats = {}
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.mrmg_node_store_destroy(self.h)
+            self.h.value = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def knn(self, queries, query_mode, k: int, stream=None):
+        """(idx [Q, k] int64, dist [Q, k] float64) on the device; idx local to the mode."""
+        qs = _dev_tensor(queries, dtype=torch.float64)
+        qm = np.ascontiguousarray(np.asarray(query_mode, dtype=np.int32))
+        Q = qs.shape[0]
+        idx = torch.empty((Q, k), dtype=torch.int64, device=qs.device)
+        dist = torch.empty((Q, k), dtype=torch.float64, device=qs.device)
+        st = np.zeros(2, dtype=np.int64)
+        _lib.check(self.lib.mrmg_knn(self.h, qs.data_ptr(), Q, qm.ctypes.data, int(k), idx.data_ptr(),
+                                     dist.data_ptr(), st.ctypes.data, _lib.stream_handle(stream)), "knn")
+        self.last_stats = {"tensor_core": bool(st[0]), "rerun_exact": int(st[1])}
+        return idx, dist

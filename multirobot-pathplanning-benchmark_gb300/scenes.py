@@ -298,3 +298,27 @@ def make_arm_workload(scene: ArmScene, seed: int = 0, n_configs: int = 1_000_000
     N = lognormal_steps(n_edges, seed + 7)
     q1, q2 = edges_with_steps(scene, N, resolution, seed + 11)
     return dict(configs=uniform_configs(scene, n_configs, seed + 3), q1=q1, q2=q2, N=N, resolution=resolution)
+
+
+def make_knn_workload(seed: int = 0, n_nodes: int = 200_000, n_modes: int = 16, n_centers: int = 64,
+                      n_queries: int = 4096, dim: int = 28, agents: int = 4, zipf: float = 1.1, sigma: float = 0.3):
+    """Per-mode nearest-neighbour workload on the four-arm configuration space:
+    `n_nodes` nodes in `dim`-D as Gaussian clusters (sigma rad) around
+    `n_centers` centres uniform in [-pi, pi]^dim, split over `n_modes` modes
+    with Zipf(`zipf`) sizes; `n_queries` queries uniform in [-pi, pi]^dim,
+    each in a mode drawn with the same Zipf probabilities.  Agent slices are
+    `agents` equal blocks (max_euclidean = max over the blocks)."""
+    rng = np.random.default_rng(seed)
+    p = 1.0 / np.arange(1, n_modes + 1) ** zipf
+    p /= p.sum()
+    sizes = np.floor(p * n_nodes).astype(np.int64)
+    sizes[0] += n_nodes - sizes.sum()
+    centers = rng.uniform(-np.pi, np.pi, (n_centers, dim))
+    which = rng.integers(0, n_centers, n_nodes)
+    nodes = centers[which] + rng.normal(0.0, sigma, (n_nodes, dim))
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    queries = rng.uniform(-np.pi, np.pi, (n_queries, dim))
+    q_mode = rng.choice(n_modes, n_queries, p=p).astype(np.int32)
+    blk = dim // agents
+    slices = np.array([[a * blk, (a + 1) * blk] for a in range(agents)], dtype=np.int64)
+    return dict(nodes=nodes, mode_offsets=offsets, queries=queries, q_mode=q_mode, slices=slices, k=10)

@@ -47,3 +47,47 @@ def test_knn_exact_all_metrics_vs_oracle(gpu, oracle):
             oi, od = oracle.knn(qs, qm, nodes, off, sl, metric, k)
             assert np.array_equal(idx.cpu().numpy(), oi), (metric, k)
             assert np.array_equal(dist.cpu().numpy(), od), (metric, k)
+
+
+def test_knn_tensor_core_golden(gpu):
+    knn = pkg("knn")
+    g = golden("knn.npz")
+    for metric in ["euclidean", "max_euclidean"]:
+        store = knn.NodeStore(g["nodes"], g["mode_off"], g["slices"], metric)
+        idx, dist = store.knn(g["queries"], g["q_mode"], int(g["k"]))
+        assert store.last_stats["tensor_core"]
+        assert np.array_equal(idx.cpu().numpy(), g[f"idx_{metric}"]), metric
+
+
+@pytest.mark.parametrize("metric", ["euclidean", "max_euclidean"])
+def test_knn_tensor_core_workload_vs_oracle(gpu, oracle, metric):
+    """The per-mode workload (Zipf modes, clustered nodes) at reduced size:
+    indices and FP64 distances identical to the oracle's exact selection."""
+    knn, scenes = pkg("knn"), pkg("scenes")
+    w = scenes.make_knn_workload(seed=3, n_nodes=40_000, n_queries=1024)
+    store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], metric)
+    for k in (1, 10, 16):
+        idx, dist = store.knn(w["queries"], w["q_mode"], k)
+        oi, od = oracle.knn(w["queries"], w["q_mode"], w["nodes"], w["mode_offsets"], w["slices"], metric, k)
+        assert np.array_equal(idx.cpu().numpy(), oi), (metric, k)
+        assert np.array_equal(dist.cpu().numpy(), od), (metric, k)
+        assert store.last_stats["tensor_core"]
+        assert store.last_stats["rerun_exact"] < 0.05 * len(w["queries"])
+
+
+def test_knn_store_other_metrics_and_edge_modes(gpu, oracle):
+    """Metrics outside the tensor-core shapes and k > 16 use the exact kernel;
+    empty and tiny modes pad with index -1 / +inf like the oracle."""
+    knn = pkg("knn")
+    rng = np.random.default_rng(9)
+    nodes = rng.uniform(-2, 2, (2000, 14))
+    off = np.array([0, 0, 5, 1990, 2000])
+    qs = rng.uniform(-2, 2, (100, 14))
+    qm = rng.integers(0, 4, 100).astype(np.int32)
+    sl = [[0, 7], [7, 14]]
+    for metric, k in [("sum_euclidean", 10), ("max", 10), ("euclidean", 20), ("euclidean", 10), ("max_euclidean", 12)]:
+        store = knn.NodeStore(nodes, off, sl, metric)
+        idx, dist = store.knn(qs, qm, k)
+        oi, od = oracle.knn(qs, qm, nodes, off, sl, metric, k)
+        assert np.array_equal(idx.cpu().numpy(), oi), (metric, k)
+        assert np.array_equal(dist.cpu().numpy(), od), (metric, k)
