@@ -346,6 +346,8 @@ def run_gb300(args):
         )
         if world == 1:
             extra["cpu_baseline"] = cpu_baseline(orc, scene, q1, q2, budget_s=args.cpu_seconds)
+            if not args.skip_extra:
+                extra["knn"] = bench_knn(orc)
 
     mism = int(reduce_max(float(mism), world))
     if rank == 0:
@@ -375,6 +377,45 @@ def run_gb300(args):
 
         dist.destroy_process_group()
     return 0 if mism == 0 else 3
+
+
+def bench_knn(orc, steps: int = 20) -> dict:
+    """Per-mode k-NN on the 200k-node / 16-mode / 4,096-query workload, k = 10,
+    euclidean and max_euclidean: device time of the full query batch (inputs
+    resident), indices checked against the oracle, CPU oracle on a sample."""
+    import torch
+
+    knn, scenes = pkg("knn"), pkg("scenes")
+    w = scenes.make_knn_workload(seed=0)
+    sizes = np.diff(w["mode_offsets"])
+    pairs = int(sizes[w["q_mode"]].sum())
+    qs = torch.from_numpy(w["queries"]).cuda()
+    out = {"workload": "200,000 nodes in 28-D (64 Gaussian clusters, sigma 0.3), 16 modes with Zipf(1.1) sizes, "
+                       "4,096 uniform queries, k = 10", "pairs_per_batch": pairs}
+    for metric in ["euclidean", "max_euclidean"]:
+        store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], metric)
+        idx, dist = store.knn(qs, w["q_mode"], w["k"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            idx, dist = store.knn(qs, w["q_mode"], w["k"])
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / steps
+        oi, od = orc.knn(w["queries"], w["q_mode"], w["nodes"], w["mode_offsets"], w["slices"], metric, w["k"])
+        mism = int((idx.cpu().numpy() != oi).sum())
+        # CPU: the oracle on a 256-query sample, scaled
+        sub = slice(0, 256)
+        t1 = time.perf_counter()
+        orc.knn(w["queries"][sub], w["q_mode"][sub], w["nodes"], w["mode_offsets"], w["slices"], metric, w["k"])
+        cpu_s = (time.perf_counter() - t1) * len(w["queries"]) / 256
+        issued = 2 * (96 if metric == "euclidean" else 128) * pairs
+        out[metric] = {"queries_per_s": len(w["queries"]) / dt, "ms_per_batch": 1e3 * dt, "index_mismatches": mism,
+                       "tensor_core": store.last_stats.get("tensor_core"),
+                       "rerun_exact": store.last_stats.get("rerun_exact"),
+                       "gemm_tflops_issued": issued / dt / 1e12,
+                       "cpu_queries_per_s": len(w["queries"]) / cpu_s, "cpu_cores": orc.num_threads()}
+        store.close()
+    return out
 
 
 def _measure_fp32_peak(_lib) -> float:
@@ -429,6 +470,7 @@ def main():
     ap.add_argument("--plain-edges", type=int, default=2000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--chunks", type=int, default=1, help="pipelined chunks of the end-to-end plan")
+    ap.add_argument("--skip-extra", action="store_true", help="only the headline edge-check workload")
     ap.add_argument("--profile", choices=["early", "full"], default=None,
                     help="short run of the first-pass edge kernel for ncu captures")
     args = ap.parse_args()
