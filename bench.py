@@ -443,8 +443,22 @@ def _profile_traffic():
 
 def run_profile(args):
     """Short run for ncu: the first-pass edge kernel on the benchmark workload,
-    early-exit ('early') or full-evaluation ('full') mode, `--steps` launches."""
+    early-exit ('early') or full-evaluation ('full') mode, or the per-mode k-NN
+    batch ('knn', euclidean), `--steps` launches."""
     import torch
+
+    if args.profile == "knn":
+        knn, scenes = pkg("knn"), pkg("scenes")
+        w = scenes.make_knn_workload(seed=0)
+        store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], "euclidean")
+        qs = torch.from_numpy(w["queries"]).cuda()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            idx, _ = store.knn(qs, w["q_mode"], w["k"])
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "knn", "launches": args.steps, "s": time.perf_counter() - t0,
+                          "stats": store.last_stats}), flush=True)
+        return 0
 
     _lib, envm = pkg("_lib"), pkg("env")
     scene, q1, q2, N = workload(0)
@@ -471,7 +485,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--chunks", type=int, default=1, help="pipelined chunks of the end-to-end plan")
     ap.add_argument("--skip-extra", action="store_true", help="only the headline edge-check workload")
-    ap.add_argument("--profile", choices=["early", "full"], default=None,
+    ap.add_argument("--profile", choices=["early", "full", "knn"], default=None,
                     help="short run of the first-pass edge kernel for ncu captures")
     args = ap.parse_args()
     if args.profile:
