@@ -28,7 +28,8 @@ namespace mrmg {
 
 constexpr int kKnnMaxK = 64;
 constexpr int kKeep = 16;          // candidates kept per query per node chunk
-constexpr int kTileM = 128;        // queries per tile (TMEM lanes)
+constexpr int kTileM = 128;        // rows of the self-test tile
+constexpr int kNodeTile = 128;     // nodes per tile (TMEM lanes of the candidate kernel)
 constexpr int kRowBytes = 128;     // one SW128 row: 64 bf16
 constexpr long long kWaitSpins = 1ll << 22;
 
@@ -37,9 +38,14 @@ constexpr long long kWaitSpins = 1ll << 22;
 // ---------------------------------------------------------------------------
 namespace {
 
+// Distances are >= 0 (or +inf), so their IEEE bit patterns order like the
+// values: lists compare int64 keys on the integer pipe instead of FP64
+// comparisons (GB300 runs FP64 at a small fraction of its FP32/INT rate).
+__device__ __forceinline__ long long dkey(double d) { return __double_as_longlong(d); }
+
 template <int KM>
-__device__ __forceinline__ void topk_insert(double (&td)[KM], long long (&ti)[KM], int k, double d, long long id) {
-  // lists hold (distance, index) ascending; equal distances keep the lower index
+__device__ __forceinline__ void topk_insert(long long (&td)[KM], long long (&ti)[KM], int k, long long d, long long id) {
+  // lists hold (distance key, index) ascending; equal distances keep the lower index
   if (!(d < td[k - 1])) return;
 #pragma unroll
   for (int i = KM - 1; i > 0; i--) {
@@ -51,15 +57,15 @@ __device__ __forceinline__ void topk_insert(double (&td)[KM], long long (&ti)[KM
   if (d < td[0]) { td[0] = d; ti[0] = id; }
 }
 
-// lexicographic warp argmin over (d, id); returns the winning lane
-__device__ __forceinline__ int warp_argmin(double d, long long id) {
+// lexicographic warp argmin over (distance key, id); returns the winning lane
+__device__ __forceinline__ int warp_argmin(long long d, long long id) {
   int lane = threadIdx.x & 31;
-  double bd = d;
+  long long bd = d;
   long long bi = id;
   int bl = lane;
 #pragma unroll
   for (int o = 16; o; o >>= 1) {
-    const double od = __shfl_xor_sync(MRMG_FULL, bd, o);
+    const long long od = __shfl_xor_sync(MRMG_FULL, bd, o);
     const long long oi = __shfl_xor_sync(MRMG_FULL, bi, o);
     const int ol = __shfl_xor_sync(MRMG_FULL, bl, o);
     if (od < bd || (od == bd && oi < bi) || (od == bd && oi == bi && ol < bl)) { bd = od; bi = oi; bl = ol; }
@@ -81,31 +87,32 @@ __global__ void knn_exact_kernel(const double* __restrict__ qs, long long Q, con
     const long long q = q_list ? q_list[w] : w;
     const int m = q_mode[q];
     const long long s = mode_off[m], e = mode_off[m + 1];
-    double td[KM];
+    long long td[KM];
     long long ti[KM];
 #pragma unroll
-    for (int i = 0; i < KM; i++) { td[i] = __longlong_as_double(0x7ff0000000000000ll); ti[i] = -1; }
+    for (int i = 0; i < KM; i++) { td[i] = 0x7ff0000000000000ll; ti[i] = -1; }
     const double* qq = qs + q * D;
     for (long long x = s + lane; x < e; x += 32) {
       const double* xx = nodes + x * D;
       auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
-      topk_insert<KM>(td, ti, k, dist_of(t, metric, dfun), x - s);
+      topk_insert<KM>(td, ti, k, dkey(dist_of(t, metric, dfun)), x - s);
     }
     // merge the 32 sorted lane lists
     int head = 0;
     for (int r = 0; r < k; r++) {
-      double hd = __longlong_as_double(0x7ff0000000000000ll);
+      long long hd = 0x7ff0000000000000ll;
       long long hi = 0x7fffffffffffffffll;
 #pragma unroll
       for (int i = 0; i < KM; i++)
         if (i == head && i < k) { hd = td[i]; hi = ti[i]; }
       if (hi < 0) hi = 0x7fffffffffffffffll;
       const int win = warp_argmin(hd, hi);
-      const double wd = __shfl_sync(MRMG_FULL, hd, win);
+      const long long wd = __shfl_sync(MRMG_FULL, hd, win);
       const long long wi = __shfl_sync(MRMG_FULL, hi, win);
       if (lane == 0) {
         out_idx[q * k + r] = wi == 0x7fffffffffffffffll ? -1 : wi;
-        out_dist[q * k + r] = wi == 0x7fffffffffffffffll ? __longlong_as_double(0x7ff0000000000000ll) : wd;
+        out_dist[q * k + r] = wi == 0x7fffffffffffffffll ? __longlong_as_double(0x7ff0000000000000ll)
+                                                         : __longlong_as_double(wd);
       }
       if (lane == win) head++;
     }
@@ -302,7 +309,6 @@ namespace mrmg {
 
 // node-store formats
 enum : int { KNN_FMT_EUCL = 0, KNN_FMT_AGENT = 1 };
-constexpr int kNtEucl = 256, kNtAgent = 64;
 
 struct KnnItem {          // one CTA: a query tile of one mode against a chunk of its node tiles
   int mode, q0, qn;       // queries qorder[q0 .. q0+qn)
@@ -390,34 +396,65 @@ __global__ void knn_pack_kernel(const double* __restrict__ nodes, KnnStoreDev st
   }
 }
 
-// per-thread sorted candidate list (approximate squared distance, local index)
-__device__ __forceinline__ void keep_insert(float (&kd)[kKeep], int (&ki)[kKeep], float d, int id) {
-  if (!(d < kd[kKeep - 1])) return;
-#pragma unroll
-  for (int i = kKeep - 1; i > 0; i--) {
-    if (d < kd[i - 1]) { kd[i] = kd[i - 1]; ki[i] = ki[i - 1]; }
-    else if (d < kd[i]) { kd[i] = d; ki[i] = id; }
+// Transposed tile: node tile (128 nodes) x query tile (NQ queries).  TMEM lane
+// = node, column = query.  Warp w reads lane quarter w % 4 and column half
+// w / 4; for each query column the warp compares its 32 nodes' values with the
+// query's current threshold (the 16th kept value of that quarter's list) and
+// inserts the rare survivors with a warp-parallel shift.
+template <int FMT>
+struct TcShape {
+  static constexpr int NQ = FMT == KNN_FMT_EUCL ? 128 : 64;         // queries per tile
+  static constexpr int ACC = FMT == KNN_FMT_EUCL ? NQ : 4 * NQ;     // accumulator columns per buffer
+  static constexpr int TMEM_COLS = 2 * ACC;                         // double buffer
+  static constexpr uint32_t AT = kNodeTile * kRowBytes;             // node tile bytes
+  static constexpr uint32_t BQ = NQ * kRowBytes;                    // query tile bytes
+  static constexpr size_t LISTS = (size_t)4 * NQ * kKeep * 8;       // per-quarter candidate lists
+  static constexpr size_t SMEM = 1024 + 2 * BQ + 2 * AT + LISTS + NQ * 4 * sizeof(float);
+};
+
+__device__ __noinline__ void warp_insert(float* ld, int* li, unsigned m, float d2, int myid, int lane) {
+  float e = lane < kKeep ? ld[lane] : __int_as_float(0x7f800000);
+  int ei = lane < kKeep ? li[lane] : -1;
+  while (m) {
+    const int b = __ffs(m) - 1;
+    m &= m - 1;
+    const float d = __shfl_sync(MRMG_FULL, d2, b);
+    const int id = __shfl_sync(MRMG_FULL, myid, b);
+    const int pos = __popc(__ballot_sync(MRMG_FULL, lane < kKeep && e <= d));   // equal values keep the earlier node
+    if (pos < kKeep) {
+      const float pe = __shfl_up_sync(MRMG_FULL, e, 1);
+      const int pi = __shfl_up_sync(MRMG_FULL, ei, 1);
+      if (lane < kKeep) {
+        if (lane == pos) { e = d; ei = id; }
+        else if (lane > pos) { e = pe; ei = pi; }
+      }
+    }
   }
-  if (d < kd[0]) { kd[0] = d; ki[0] = id; }
+  if (lane < kKeep) { ld[lane] = e; li[lane] = ei; }
+  __syncwarp();
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(128, 1) knn_tc_kernel(KnnStoreDev st, const double* __restrict__ qs,
+__global__ void __launch_bounds__(256, 1) knn_tc_kernel(KnnStoreDev st, const double* __restrict__ qs,
                                                         const int* __restrict__ qorder, const KnnItem* __restrict__ items,
                                                         int chunks_max, float* __restrict__ cand_d,
                                                         int* __restrict__ cand_i, float* __restrict__ q_eps,
                                                         int* __restrict__ err) {
-  constexpr int NT = FMT == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
-  constexpr uint32_t BT = NT * kRowBytes;   // bytes per node tile
+  using SH = TcShape<FMT>;
+  constexpr int NQ = SH::NQ;
   extern __shared__ __align__(1024) unsigned char sm_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)sm_raw + 1023) & ~(uintptr_t)1023);
-  unsigned char* sA1 = base;
-  unsigned char* sA2 = base + kTileM * kRowBytes;
-  unsigned char* sB0 = base + 2 * kTileM * kRowBytes;
+  unsigned char* sB1 = base;
+  unsigned char* sB2 = base + SH::BQ;
+  unsigned char* sA0 = base + 2 * SH::BQ;
+  float* lst_d = (float*)(sA0 + 2 * SH::AT);                  // [4][NQ][kKeep]
+  int* lst_i = (int*)(lst_d + 4 * NQ * kKeep);
+  float* qn_s = (float*)(lst_i + 4 * NQ * kKeep);             // [NQ][4]: |q|^2 (or per agent)
   __shared__ uint64_t bar_load[2], bar_mma[2];
   __shared__ uint32_t tbase;
   __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3, half = warp >> 2;
   const KnnItem it = items[blockIdx.x];
   const int D = st.D;
 
@@ -427,55 +464,57 @@ __global__ void __launch_bounds__(128, 1) knn_tc_kernel(KnnStoreDev st, const do
     s_fail = 0;
     fence_barrier_init();
   }
-  if (warp == 0) tmem_alloc(&tbase, 512);
+  if (warp == 0) tmem_alloc(&tbase, SH::TMEM_COLS);
+  for (int i = tid; i < 4 * NQ * kKeep; i += blockDim.x) { lst_d[i] = __int_as_float(0x7f800000); lst_i[i] = -1; }
 
-  // ---- the query tile: A1 = [q_hi | -1/2 ... | q_hi], A2 = [q_lo]; one thread per row
-  float qn = 0.f, qna[4] = {0.f, 0.f, 0.f, 0.f};
-  long long qid = -1;
-  {
+  // ---- the query tile: B1 = [q_hi | -1/2 ... | q_hi], B2 = [q_lo]; one thread per query row
+  if (tid < NQ) {
     const int r = tid;
     for (int c = 0; c < 64; c++) {
-      *(__nv_bfloat16*)(sA1 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
-      *(__nv_bfloat16*)(sA2 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
+      *(__nv_bfloat16*)(sB1 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
+      *(__nv_bfloat16*)(sB2 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
     }
+    float qn = 0.f;
+    for (int a = 0; a < 4; a++) qn_s[r * 4 + a] = 0.f;
     if (r < it.qn) {
-      qid = qorder[it.q0 + r];
+      const long long qid = qorder[it.q0 + r];
       const double* q = qs + qid * D;
       if (FMT == KNN_FMT_EUCL) {
         double n2 = 0.0;
         for (int j = 0; j < D; j++) {
           float h, l;
           split2(q[j], &h, &l);
-          *(__nv_bfloat16*)(sA1 + sw128_off(r, j)) = __float2bfloat16_rn(h);
-          *(__nv_bfloat16*)(sA1 + sw128_off(r, D + 3 + j)) = __float2bfloat16_rn(h);
-          *(__nv_bfloat16*)(sA2 + sw128_off(r, j)) = __float2bfloat16_rn(l);
+          *(__nv_bfloat16*)(sB1 + sw128_off(r, j)) = __float2bfloat16_rn(h);
+          *(__nv_bfloat16*)(sB1 + sw128_off(r, D + 3 + j)) = __float2bfloat16_rn(h);
+          *(__nv_bfloat16*)(sB2 + sw128_off(r, j)) = __float2bfloat16_rn(l);
           n2 += q[j] * q[j];
         }
-        for (int c = 0; c < 3; c++) *(__nv_bfloat16*)(sA1 + sw128_off(r, D + c)) = __float2bfloat16_rn(-0.5f);
+        for (int c = 0; c < 3; c++) *(__nv_bfloat16*)(sB1 + sw128_off(r, D + c)) = __float2bfloat16_rn(-0.5f);
         qn = (float)n2;
+        qn_s[r * 4] = qn;
       } else {
         for (int a = 0; a < st.A; a++) {
-          const int s = st.agent_s[a], d = st.agent_e[a] - s;
+          const int s0 = st.agent_s[a], d = st.agent_e[a] - s0;
           double na = 0.0;
           for (int j = 0; j < d; j++) {
             float h, l;
-            split2(q[s + j], &h, &l);
-            *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(h);
-            *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + d + j)) = __float2bfloat16_rn(h);
-            *(__nv_bfloat16*)(sA2 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(l);
-            na += q[s + j] * q[s + j];
+            split2(q[s0 + j], &h, &l);
+            *(__nv_bfloat16*)(sB1 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(h);
+            *(__nv_bfloat16*)(sB1 + sw128_off(r, 16 * a + d + j)) = __float2bfloat16_rn(h);
+            *(__nv_bfloat16*)(sB2 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(l);
+            na += q[s0 + j] * q[s0 + j];
           }
-          *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + 2 * d)) = __float2bfloat16_rn(-0.5f);
-          *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + 2 * d + 1)) = __float2bfloat16_rn(-0.5f);
-          qna[a] = (float)na;
+          *(__nv_bfloat16*)(sB1 + sw128_off(r, 16 * a + 2 * d)) = __float2bfloat16_rn(-0.5f);
+          *(__nv_bfloat16*)(sB1 + sw128_off(r, 16 * a + 2 * d + 1)) = __float2bfloat16_rn(-0.5f);
+          qn_s[r * 4 + a] = (float)na;
           qn += (float)na;
         }
       }
       // error bound of the approximate squared distance (split-BF16 operands,
       // FP32 accumulation), per query; stored once per query
       if (it.chunk == 0) {
-        const float s = sqrtf(qn) + st.mode_xmax[it.mode];
-        q_eps[qid] = 1.2e-4f * s * s + 1e-30f;
+        const float sq = sqrtf(qn) + st.mode_xmax[it.mode];
+        q_eps[qid] = 1.2e-4f * sq * sq + 1e-30f;
       }
     }
   }
@@ -485,25 +524,24 @@ __global__ void __launch_bounds__(128, 1) knn_tc_kernel(KnnStoreDev st, const do
   tc_fence_after();
   const uint32_t tm = tbase;
   const int T = it.tile1 - it.tile0;
-  const unsigned char* gtiles = st.tiles + (long long)(st.mode_tile0[it.mode] + it.tile0) * BT;
-  const uint32_t idesc = idesc_bf16(kTileM, NT);
+  const unsigned char* gtiles = st.tiles + (long long)(st.mode_tile0[it.mode] + it.tile0) * SH::AT;
+  const uint32_t idesc = idesc_bf16(kNodeTile, NQ);
 
   auto issue_load = [&](int t) {
-    unsigned char* dst = sB0 + (t & 1) * BT;
-    mbar_expect_tx(&bar_load[t & 1], BT);
-    bulk_g2s(dst, gtiles + (long long)t * BT, BT, &bar_load[t & 1]);
+    mbar_expect_tx(&bar_load[t & 1], SH::AT);
+    bulk_g2s(sA0 + (t & 1) * SH::AT, gtiles + (long long)t * SH::AT, SH::AT, &bar_load[t & 1]);
   };
   auto issue_mma = [&](int t) {
-    const uint32_t a1 = su32(sA1), a2 = su32(sA2), b = su32(sB0 + (t & 1) * BT);
-    const uint32_t dcol = tm + (uint32_t)((t & 1) * 256);
+    const uint32_t a = su32(sA0 + (t & 1) * SH::AT), b1 = su32(sB1), b2 = su32(sB2);
+    const uint32_t dcol = tm + (uint32_t)((t & 1) * SH::ACC);
     if (FMT == KNN_FMT_EUCL) {
-      for (int s = 0; s < 4; s++) umma_bf16(dcol, sw128_desc(a1 + 32 * s), sw128_desc(b + 32 * s), idesc, s > 0);
+      for (int s = 0; s < 4; s++) umma_bf16(dcol, sw128_desc(a + 32 * s), sw128_desc(b1 + 32 * s), idesc, s > 0);
       const int s2 = (D + 15) / 16;
-      for (int s = 0; s < s2; s++) umma_bf16(dcol, sw128_desc(a2 + 32 * s), sw128_desc(b + 32 * s), idesc, 1);
+      for (int s = 0; s < s2; s++) umma_bf16(dcol, sw128_desc(a + 32 * s), sw128_desc(b2 + 32 * s), idesc, 1);
     } else {
-      for (int a = 0; a < st.A; a++) {
-        umma_bf16(dcol + 64 * a, sw128_desc(a1 + 32 * a), sw128_desc(b + 32 * a), idesc, 0);
-        umma_bf16(dcol + 64 * a, sw128_desc(a2 + 32 * a), sw128_desc(b + 32 * a), idesc, 1);
+      for (int g = 0; g < st.A; g++) {
+        umma_bf16(dcol + NQ * g, sw128_desc(a + 32 * g), sw128_desc(b1 + 32 * g), idesc, 0);
+        umma_bf16(dcol + NQ * g, sw128_desc(a + 32 * g), sw128_desc(b2 + 32 * g), idesc, 1);
       }
     }
     umma_commit(&bar_mma[t & 1]);
@@ -516,11 +554,7 @@ __global__ void __launch_bounds__(128, 1) knn_tc_kernel(KnnStoreDev st, const do
     else s_fail = 1;
   }
 
-  float kd[kKeep];
-  int ki[kKeep];
-#pragma unroll
-  for (int i = 0; i < kKeep; i++) { kd[i] = __int_as_float(0x7f800000); ki[i] = -1; }
-
+  constexpr int HALF = NQ / 2;     // query columns per warp
   for (int t = 0; t < T; t++) {
     if (tid == 0 && t + 1 < T && !s_fail) {
       if (mbar_wait(&bar_load[(t + 1) & 1], ((t + 1) >> 1) & 1)) issue_mma(t + 1);
@@ -531,29 +565,32 @@ __global__ void __launch_bounds__(128, 1) knn_tc_kernel(KnnStoreDev st, const do
     tc_fence_after();
     if (tid == 0 && t + 2 < T && done) issue_load(t + 2);   // tile t's MMAs have read its buffer
     if (done) {
-      const int col_node0 = (it.tile0 + t) * NT;
-      const uint32_t lane_base = tm + ((uint32_t)(32 * warp) << 16) + (uint32_t)((t & 1) * 256);
-      if (FMT == KNN_FMT_EUCL) {
-        for (int c0 = 0; c0 < NT; c0 += 32) {
-          float v[32];
+      const int my_node = (it.tile0 + t) * kNodeTile + 32 * quarter + lane;
+      const uint32_t lane_base = tm + ((uint32_t)(32 * quarter) << 16) + (uint32_t)((t & 1) * SH::ACC);
+      for (int c0 = half * HALF; c0 < half * HALF + HALF; c0 += 32) {
+        float v[32];
+        float qn_l[4];
+        if (FMT == KNN_FMT_EUCL) {
           tmem_ld32(lane_base + c0, v);
+          qn_l[0] = qn_s[(c0 + lane) * 4];
+        } else {
+          for (int g = 0; g < 4; g++) qn_l[g] = qn_s[(c0 + lane) * 4 + g];
 #pragma unroll
-          for (int i = 0; i < 32; i++) keep_insert(kd, ki, fmaf(-2.f, v[i], qn), col_node0 + c0 + i);
-        }
-      } else {
-        for (int c0 = 0; c0 < NT; c0 += 32) {
-          float m[32];
+          for (int i = 0; i < 32; i++) v[i] = -__int_as_float(0x7f800000);
+          for (int g = 0; g < st.A; g++) {
+            float w[32];
+            tmem_ld32(lane_base + NQ * g + c0, w);
+            const float qg = g == 0 ? qn_l[0] : g == 1 ? qn_l[1] : g == 2 ? qn_l[2] : qn_l[3];
 #pragma unroll
-          for (int i = 0; i < 32; i++) m[i] = -__int_as_float(0x7f800000);
-          for (int a = 0; a < st.A; a++) {
-            float v[32];
-            tmem_ld32(lane_base + 64 * a + c0, v);
-            const float qa = qna[a];
-#pragma unroll
-            for (int i = 0; i < 32; i++) m[i] = fmaxf(m[i], fmaf(-2.f, v[i], qa));
+            for (int i = 0; i < 32; i++) v[i] = fmaxf(v[i], fmaf(-2.f, w[i], __shfl_sync(MRMG_FULL, qg, i)));
           }
+        }
 #pragma unroll
-          for (int i = 0; i < 32; i++) keep_insert(kd, ki, m[i], col_node0 + c0 + i);
+        for (int j = 0; j < 32; j++) {
+          const float d2 = FMT == KNN_FMT_EUCL ? fmaf(-2.f, v[j], __shfl_sync(MRMG_FULL, qn_l[0], j)) : v[j];
+          float* ld = lst_d + ((size_t)quarter * NQ + c0 + j) * kKeep;
+          const unsigned m = __ballot_sync(MRMG_FULL, d2 < ld[kKeep - 1]);
+          if (m) warp_insert(ld, lst_i + ((size_t)quarter * NQ + c0 + j) * kKeep, m, d2, my_node, lane);
         }
       }
     }
@@ -563,17 +600,34 @@ __global__ void __launch_bounds__(128, 1) knn_tc_kernel(KnnStoreDev st, const do
     if (s_fail) break;
   }
   if (s_fail && tid == 0) atomicOr(err, E_TIMEOUT);
-  (void)lane;
-  if (qid >= 0) {
+
+  // merge the four quarter lists of each query into its candidate list
+  if (tid < it.qn) {
+    const long long qid = qorder[it.q0 + tid];
+    int h[4] = {0, 0, 0, 0};
     float* od = cand_d + ((size_t)qid * chunks_max + it.chunk) * kKeep;
     int* oi = cand_i + ((size_t)qid * chunks_max + it.chunk) * kKeep;
-#pragma unroll
-    for (int i = 0; i < kKeep; i++) { od[i] = kd[i]; oi[i] = ki[i]; }
+    for (int r = 0; r < kKeep; r++) {
+      int bq = 0;
+      float bd = __int_as_float(0x7f800000);
+      int bi = 0x7fffffff;
+      for (int g = 0; g < 4; g++) {
+        if (h[g] >= kKeep) continue;
+        const float d = lst_d[((size_t)g * NQ + tid) * kKeep + h[g]];
+        const int i = lst_i[((size_t)g * NQ + tid) * kKeep + h[g]];
+        if (i < 0) continue;
+        if (d < bd || (d == bd && i < bi)) { bd = d; bi = i; bq = g; }
+      }
+      if (bi == 0x7fffffff) { od[r] = __int_as_float(0x7f800000); oi[r] = -1; continue; }
+      od[r] = bd;
+      oi[r] = bi;
+      h[bq]++;
+    }
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) tmem_dealloc(tm, 512);
+  if (warp == 0) tmem_dealloc(tm, SH::TMEM_COLS);
 }
 
 // ---------------------------------------------------------------------------
@@ -627,10 +681,10 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
       continue;
     }
     // exact FP64 re-rank of every candidate within tau
-    double td[kKnnMaxK > 16 ? 16 : kKnnMaxK];
+    long long td[16];
     long long tix[16];
 #pragma unroll
-    for (int i = 0; i < 16; i++) { td[i] = DINF; tix[i] = -1; }
+    for (int i = 0; i < 16; i++) { td[i] = 0x7ff0000000000000ll; tix[i] = -1; }
     const double* qq = qs + q * t.D;
     for (int cc = lane; cc < C; cc += 32)
       for (int j = 0; j < kKeep; j++) {
@@ -638,21 +692,21 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
         if (id < 0 || id >= M || !(cd[cc * kKeep + j] <= tau)) continue;
         const double* xx = nodes + (mode_off[m] + id) * t.D;
         auto dfun = [&](int jj) { return __dsub_rn(qq[jj], xx[jj]); };
-        topk_insert<16>(td, tix, k < 16 ? k : 16, dist_of(t, metric, dfun), id);
+        topk_insert<16>(td, tix, k < 16 ? k : 16, dkey(dist_of(t, metric, dfun)), id);
       }
     int head = 0;
     for (int r = 0; r < k; r++) {
-      double hd = DINF;
+      long long hd = 0x7ff0000000000000ll;
       long long hi = 0x7fffffffffffffffll;
 #pragma unroll
       for (int i = 0; i < 16; i++)
         if (i == head) { hd = td[i]; hi = tix[i] < 0 ? 0x7fffffffffffffffll : tix[i]; }
       const int win = warp_argmin(hd, hi);
-      const double wd = __shfl_sync(MRMG_FULL, hd, win);
+      const long long wd = __shfl_sync(MRMG_FULL, hd, win);
       const long long wi = __shfl_sync(MRMG_FULL, hi, win);
       if (lane == 0) {
         out_idx[q * k + r] = wi == 0x7fffffffffffffffll ? -1 : wi;
-        out_dist[q * k + r] = wi == 0x7fffffffffffffffll ? DINF : wd;
+        out_dist[q * k + r] = wi == 0x7fffffffffffffffll ? DINF : __longlong_as_double(wd);
       }
       if (lane == win) head++;
     }
@@ -695,7 +749,7 @@ cudaError_t knn_store_build(KnnStore* s, const double* d_nodes, long long M, con
   s->nodes = d_nodes;
   s->mode_off.assign(h_mode_off, h_mode_off + n_modes + 1);
   const int fmt = metric == MRMG_METRIC_EUCLIDEAN ? KNN_FMT_EUCL : KNN_FMT_AGENT;
-  const int NT = fmt == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
+  const int NT = kNodeTile;
   std::vector<int> tile0(n_modes + 1, 0);
   s->mode_tiles.assign(n_modes, 0);
   for (int m = 0; m < n_modes; m++) {
@@ -762,8 +816,9 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
     for (long long q = 0; q < Q; q++) order[fill[h_q_mode[q]]++] = (int)q;
   }
   // work items: query tiles x node-tile chunks, about three waves of CTAs
+  const int NQ = s->dev.fmt == KNN_FMT_EUCL ? TcShape<KNN_FMT_EUCL>::NQ : TcShape<KNN_FMT_AGENT>::NQ;
   long long units = 0;
-  for (int m = 0; m < n_modes; m++) units += (long long)((qcount[m] + kTileM - 1) / kTileM) * s->mode_tiles[m];
+  for (int m = 0; m < n_modes; m++) units += (long long)((qcount[m] + NQ - 1) / NQ) * s->mode_tiles[m];
   const long long target = std::max(1, 3 * num_sms);
   int tpc = (int)std::max<long long>(1, (units + target - 1) / target);
   int chunks_max = 1;
@@ -779,12 +834,12 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
     if (qcount[m] == 0 || s->mode_tiles[m] == 0) continue;
     const int nch = (s->mode_tiles[m] + tpc - 1) / tpc;
     mode_chunks[m] = nch;
-    for (int q0 = 0; q0 < qcount[m]; q0 += kTileM)
+    for (int q0 = 0; q0 < qcount[m]; q0 += NQ)
       for (int c = 0; c < nch; c++) {
         KnnItem it;
         it.mode = m;
         it.q0 = qstart[m] + q0;
-        it.qn = std::min(kTileM, qcount[m] - q0);
+        it.qn = std::min(NQ, qcount[m] - q0);
         it.tile0 = c * tpc;
         it.tile1 = std::min(s->mode_tiles[m], (c + 1) * tpc);
         it.chunk = c;
@@ -829,18 +884,18 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_mch, mode_chunks.data(), sizeof(int) * n_modes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, 256, st);
   if (e != cudaSuccess) return e;
-  const int NT = s->dev.NT;
-  // at least 120 KB of shared memory: one CTA per SM, so two CTAs never wait
-  // on each other for the 512 tensor-memory columns each allocates
-  const size_t smem = std::max<size_t>(1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes, 120 * 1024);
   if (!items.empty()) {
+    // at least 120 KB of shared memory: one CTA per SM, so two CTAs never wait
+    // on each other for tensor-memory columns
     if (s->dev.fmt == KNN_FMT_EUCL) {
+      const size_t smem = std::max<size_t>(TcShape<KNN_FMT_EUCL>::SMEM, 120 * 1024);
       cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_EUCL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      knn_tc_kernel<KNN_FMT_EUCL><<<(int)items.size(), 128, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
+      knn_tc_kernel<KNN_FMT_EUCL><<<(int)items.size(), 256, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
                                                                          d_cd, d_ci, d_eps, d_ctr + 1);
     } else {
+      const size_t smem = std::max<size_t>(TcShape<KNN_FMT_AGENT>::SMEM, 120 * 1024);
       cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_AGENT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      knn_tc_kernel<KNN_FMT_AGENT><<<(int)items.size(), 128, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
+      knn_tc_kernel<KNN_FMT_AGENT><<<(int)items.size(), 256, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
                                                                           d_cd, d_ci, d_eps, d_ctr + 1);
     }
     e = cudaGetLastError();
