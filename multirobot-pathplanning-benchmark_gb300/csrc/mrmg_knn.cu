@@ -28,8 +28,7 @@ namespace mrmg {
 
 constexpr int kKnnMaxK = 64;
 constexpr int kKeep = 16;          // candidates kept per query per node chunk
-constexpr int kTileM = 128;        // rows of the self-test tile
-constexpr int kNodeTile = 128;     // nodes per tile (TMEM lanes of the candidate kernel)
+constexpr int kTileM = 128;        // queries per tile (TMEM lanes)
 constexpr int kRowBytes = 128;     // one SW128 row: 64 bf16
 constexpr long long kWaitSpins = 1ll << 22;
 
@@ -309,6 +308,7 @@ namespace mrmg {
 
 // node-store formats
 enum : int { KNN_FMT_EUCL = 0, KNN_FMT_AGENT = 1 };
+constexpr int kNtEucl = 256, kNtAgent = 64;
 
 struct KnnItem {          // one CTA: a query tile of one mode against a chunk of its node tiles
   int mode, q0, qn;       // queries qorder[q0 .. q0+qn)
@@ -396,65 +396,44 @@ __global__ void knn_pack_kernel(const double* __restrict__ nodes, KnnStoreDev st
   }
 }
 
-// Transposed tile: node tile (128 nodes) x query tile (NQ queries).  TMEM lane
-// = node, column = query.  Warp w reads lane quarter w % 4 and column half
-// w / 4; for each query column the warp compares its 32 nodes' values with the
-// query's current threshold (the 16th kept value of that quarter's list) and
-// inserts the rare survivors with a warp-parallel shift.
-template <int FMT>
-struct TcShape {
-  static constexpr int NQ = FMT == KNN_FMT_EUCL ? 128 : 64;         // queries per tile
-  static constexpr int ACC = FMT == KNN_FMT_EUCL ? NQ : 4 * NQ;     // accumulator columns per buffer
-  static constexpr int TMEM_COLS = 2 * ACC;                         // double buffer
-  static constexpr uint32_t AT = kNodeTile * kRowBytes;             // node tile bytes
-  static constexpr uint32_t BQ = NQ * kRowBytes;                    // query tile bytes
-  static constexpr size_t LISTS = (size_t)4 * NQ * kKeep * 8;       // per-quarter candidate lists
-  static constexpr size_t SMEM = 1024 + 2 * BQ + 2 * AT + LISTS + NQ * 4 * sizeof(float);
-};
-
-__device__ __noinline__ void warp_insert(float* ld, int* li, unsigned m, float d2, int myid, int lane) {
-  float e = lane < kKeep ? ld[lane] : __int_as_float(0x7f800000);
-  int ei = lane < kKeep ? li[lane] : -1;
-  while (m) {
-    const int b = __ffs(m) - 1;
-    m &= m - 1;
-    const float d = __shfl_sync(MRMG_FULL, d2, b);
-    const int id = __shfl_sync(MRMG_FULL, myid, b);
-    const int pos = __popc(__ballot_sync(MRMG_FULL, lane < kKeep && e <= d));   // equal values keep the earlier node
-    if (pos < kKeep) {
-      const float pe = __shfl_up_sync(MRMG_FULL, e, 1);
-      const int pi = __shfl_up_sync(MRMG_FULL, ei, 1);
-      if (lane < kKeep) {
-        if (lane == pos) { e = d; ei = id; }
-        else if (lane > pos) { e = pe; ei = pi; }
-      }
-    }
+// per-thread sorted candidate list (approximate squared distance, local index)
+__device__ __forceinline__ void keep_insert(float (&kd)[kKeep], int (&ki)[kKeep], float d, int id) {
+  if (!(d < kd[kKeep - 1])) return;
+#pragma unroll
+  for (int i = kKeep - 1; i > 0; i--) {
+    if (d < kd[i - 1]) { kd[i] = kd[i - 1]; ki[i] = ki[i - 1]; }
+    else if (d < kd[i]) { kd[i] = d; ki[i] = id; }
   }
-  if (lane < kKeep) { ld[lane] = e; li[lane] = ei; }
-  __syncwarp();
+  if (d < kd[0]) { kd[0] = d; ki[0] = id; }
 }
 
+// Column groups of the epilogue: warp w reads TMEM lanes 32*(w%4) (the lane
+// quadrant its warp rank allows) and the w/4-th slice of each tile's columns,
+// so every query row is scanned by kSplit threads with their own kept lists,
+// merged through shared memory at the end.
+template <int FMT> struct TcSplit { static constexpr int S = FMT == KNN_FMT_EUCL ? 4 : 2; };
+
 template <int FMT>
-__global__ void __launch_bounds__(256, 1) knn_tc_kernel(KnnStoreDev st, const double* __restrict__ qs,
+__global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnStoreDev st, const double* __restrict__ qs,
                                                         const int* __restrict__ qorder, const KnnItem* __restrict__ items,
                                                         int chunks_max, float* __restrict__ cand_d,
                                                         int* __restrict__ cand_i, float* __restrict__ q_eps,
                                                         int* __restrict__ err) {
-  using SH = TcShape<FMT>;
-  constexpr int NQ = SH::NQ;
+  constexpr int NT = FMT == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
+  constexpr uint32_t BT = NT * kRowBytes;   // bytes per node tile
+  constexpr int S = TcSplit<FMT>::S, NCOL = NT / S;
+  static_assert(NCOL % 32 == 0, "column slice is whole 32-column loads");
   extern __shared__ __align__(1024) unsigned char sm_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)sm_raw + 1023) & ~(uintptr_t)1023);
-  unsigned char* sB1 = base;
-  unsigned char* sB2 = base + SH::BQ;
-  unsigned char* sA0 = base + 2 * SH::BQ;
-  float* lst_d = (float*)(sA0 + 2 * SH::AT);                  // [4][NQ][kKeep]
-  int* lst_i = (int*)(lst_d + 4 * NQ * kKeep);
-  float* qn_s = (float*)(lst_i + 4 * NQ * kKeep);             // [NQ][4]: |q|^2 (or per agent)
+  unsigned char* sA1 = base;
+  unsigned char* sA2 = base + kTileM * kRowBytes;
+  unsigned char* sB0 = base + 2 * kTileM * kRowBytes;
   __shared__ uint64_t bar_load[2], bar_mma[2];
   __shared__ uint32_t tbase;
   __shared__ int s_fail;
+  __shared__ float s_qn[kTileM], s_qna[4][kTileM];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, half = warp >> 2;
+  const int row = tid & (kTileM - 1), slice = tid / kTileM;
   const KnnItem it = items[blockIdx.x];
   const int D = st.D;
 
@@ -464,59 +443,59 @@ __global__ void __launch_bounds__(256, 1) knn_tc_kernel(KnnStoreDev st, const do
     s_fail = 0;
     fence_barrier_init();
   }
-  if (warp == 0) tmem_alloc(&tbase, SH::TMEM_COLS);
-  for (int i = tid; i < 4 * NQ * kKeep; i += blockDim.x) { lst_d[i] = __int_as_float(0x7f800000); lst_i[i] = -1; }
+  if (warp == 0) tmem_alloc(&tbase, 512);
 
-  // ---- the query tile: B1 = [q_hi | -1/2 ... | q_hi], B2 = [q_lo]; one thread per query row
-  if (tid < NQ) {
+  // ---- the query tile: A1 = [q_hi | -1/2 ... | q_hi], A2 = [q_lo]; one thread per row
+  float qn = 0.f, qna[4] = {0.f, 0.f, 0.f, 0.f};
+  long long qid = -1;
+  if (tid < kTileM) {
     const int r = tid;
     for (int c = 0; c < 64; c++) {
-      *(__nv_bfloat16*)(sB1 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
-      *(__nv_bfloat16*)(sB2 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
+      *(__nv_bfloat16*)(sA1 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
+      *(__nv_bfloat16*)(sA2 + sw128_off(r, c)) = __float2bfloat16_rn(0.f);
     }
-    float qn = 0.f;
-    for (int a = 0; a < 4; a++) qn_s[r * 4 + a] = 0.f;
     if (r < it.qn) {
-      const long long qid = qorder[it.q0 + r];
+      qid = qorder[it.q0 + r];
       const double* q = qs + qid * D;
       if (FMT == KNN_FMT_EUCL) {
         double n2 = 0.0;
         for (int j = 0; j < D; j++) {
           float h, l;
           split2(q[j], &h, &l);
-          *(__nv_bfloat16*)(sB1 + sw128_off(r, j)) = __float2bfloat16_rn(h);
-          *(__nv_bfloat16*)(sB1 + sw128_off(r, D + 3 + j)) = __float2bfloat16_rn(h);
-          *(__nv_bfloat16*)(sB2 + sw128_off(r, j)) = __float2bfloat16_rn(l);
+          *(__nv_bfloat16*)(sA1 + sw128_off(r, j)) = __float2bfloat16_rn(h);
+          *(__nv_bfloat16*)(sA1 + sw128_off(r, D + 3 + j)) = __float2bfloat16_rn(h);
+          *(__nv_bfloat16*)(sA2 + sw128_off(r, j)) = __float2bfloat16_rn(l);
           n2 += q[j] * q[j];
         }
-        for (int c = 0; c < 3; c++) *(__nv_bfloat16*)(sB1 + sw128_off(r, D + c)) = __float2bfloat16_rn(-0.5f);
+        for (int c = 0; c < 3; c++) *(__nv_bfloat16*)(sA1 + sw128_off(r, D + c)) = __float2bfloat16_rn(-0.5f);
         qn = (float)n2;
-        qn_s[r * 4] = qn;
       } else {
         for (int a = 0; a < st.A; a++) {
-          const int s0 = st.agent_s[a], d = st.agent_e[a] - s0;
+          const int s = st.agent_s[a], d = st.agent_e[a] - s;
           double na = 0.0;
           for (int j = 0; j < d; j++) {
             float h, l;
-            split2(q[s0 + j], &h, &l);
-            *(__nv_bfloat16*)(sB1 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(h);
-            *(__nv_bfloat16*)(sB1 + sw128_off(r, 16 * a + d + j)) = __float2bfloat16_rn(h);
-            *(__nv_bfloat16*)(sB2 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(l);
-            na += q[s0 + j] * q[s0 + j];
+            split2(q[s + j], &h, &l);
+            *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(h);
+            *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + d + j)) = __float2bfloat16_rn(h);
+            *(__nv_bfloat16*)(sA2 + sw128_off(r, 16 * a + j)) = __float2bfloat16_rn(l);
+            na += q[s + j] * q[s + j];
           }
-          *(__nv_bfloat16*)(sB1 + sw128_off(r, 16 * a + 2 * d)) = __float2bfloat16_rn(-0.5f);
-          *(__nv_bfloat16*)(sB1 + sw128_off(r, 16 * a + 2 * d + 1)) = __float2bfloat16_rn(-0.5f);
-          qn_s[r * 4 + a] = (float)na;
+          *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + 2 * d)) = __float2bfloat16_rn(-0.5f);
+          *(__nv_bfloat16*)(sA1 + sw128_off(r, 16 * a + 2 * d + 1)) = __float2bfloat16_rn(-0.5f);
+          qna[a] = (float)na;
           qn += (float)na;
         }
       }
       // error bound of the approximate squared distance (split-BF16 operands,
       // FP32 accumulation), per query; stored once per query
       if (it.chunk == 0) {
-        const float sq = sqrtf(qn) + st.mode_xmax[it.mode];
-        q_eps[qid] = 1.2e-4f * sq * sq + 1e-30f;
+        const float s = sqrtf(qn) + st.mode_xmax[it.mode];
+        q_eps[qid] = 1.2e-4f * s * s + 1e-30f;
       }
     }
+    s_qn[r] = qn;
+    for (int a = 0; a < 4; a++) s_qna[a][r] = qna[a];
   }
   fence_async_smem();
   tc_fence_before();
@@ -524,24 +503,26 @@ __global__ void __launch_bounds__(256, 1) knn_tc_kernel(KnnStoreDev st, const do
   tc_fence_after();
   const uint32_t tm = tbase;
   const int T = it.tile1 - it.tile0;
-  const unsigned char* gtiles = st.tiles + (long long)(st.mode_tile0[it.mode] + it.tile0) * SH::AT;
-  const uint32_t idesc = idesc_bf16(kNodeTile, NQ);
+  qn = s_qn[row];
+  const unsigned char* gtiles = st.tiles + (long long)(st.mode_tile0[it.mode] + it.tile0) * BT;
+  const uint32_t idesc = idesc_bf16(kTileM, NT);
 
   auto issue_load = [&](int t) {
-    mbar_expect_tx(&bar_load[t & 1], SH::AT);
-    bulk_g2s(sA0 + (t & 1) * SH::AT, gtiles + (long long)t * SH::AT, SH::AT, &bar_load[t & 1]);
+    unsigned char* dst = sB0 + (t & 1) * BT;
+    mbar_expect_tx(&bar_load[t & 1], BT);
+    bulk_g2s(dst, gtiles + (long long)t * BT, BT, &bar_load[t & 1]);
   };
   auto issue_mma = [&](int t) {
-    const uint32_t a = su32(sA0 + (t & 1) * SH::AT), b1 = su32(sB1), b2 = su32(sB2);
-    const uint32_t dcol = tm + (uint32_t)((t & 1) * SH::ACC);
+    const uint32_t a1 = su32(sA1), a2 = su32(sA2), b = su32(sB0 + (t & 1) * BT);
+    const uint32_t dcol = tm + (uint32_t)((t & 1) * 256);
     if (FMT == KNN_FMT_EUCL) {
-      for (int s = 0; s < 4; s++) umma_bf16(dcol, sw128_desc(a + 32 * s), sw128_desc(b1 + 32 * s), idesc, s > 0);
+      for (int s = 0; s < 4; s++) umma_bf16(dcol, sw128_desc(a1 + 32 * s), sw128_desc(b + 32 * s), idesc, s > 0);
       const int s2 = (D + 15) / 16;
-      for (int s = 0; s < s2; s++) umma_bf16(dcol, sw128_desc(a + 32 * s), sw128_desc(b2 + 32 * s), idesc, 1);
+      for (int s = 0; s < s2; s++) umma_bf16(dcol, sw128_desc(a2 + 32 * s), sw128_desc(b + 32 * s), idesc, 1);
     } else {
-      for (int g = 0; g < st.A; g++) {
-        umma_bf16(dcol + NQ * g, sw128_desc(a + 32 * g), sw128_desc(b1 + 32 * g), idesc, 0);
-        umma_bf16(dcol + NQ * g, sw128_desc(a + 32 * g), sw128_desc(b2 + 32 * g), idesc, 1);
+      for (int a = 0; a < st.A; a++) {
+        umma_bf16(dcol + 64 * a, sw128_desc(a1 + 32 * a), sw128_desc(b + 32 * a), idesc, 0);
+        umma_bf16(dcol + 64 * a, sw128_desc(a2 + 32 * a), sw128_desc(b + 32 * a), idesc, 1);
       }
     }
     umma_commit(&bar_mma[t & 1]);
@@ -554,7 +535,11 @@ __global__ void __launch_bounds__(256, 1) knn_tc_kernel(KnnStoreDev st, const do
     else s_fail = 1;
   }
 
-  constexpr int HALF = NQ / 2;     // query columns per warp
+  float kd[kKeep];
+  int ki[kKeep];
+#pragma unroll
+  for (int i = 0; i < kKeep; i++) { kd[i] = __int_as_float(0x7f800000); ki[i] = -1; }
+
   for (int t = 0; t < T; t++) {
     if (tid == 0 && t + 1 < T && !s_fail) {
       if (mbar_wait(&bar_load[(t + 1) & 1], ((t + 1) >> 1) & 1)) issue_mma(t + 1);
@@ -565,32 +550,31 @@ __global__ void __launch_bounds__(256, 1) knn_tc_kernel(KnnStoreDev st, const do
     tc_fence_after();
     if (tid == 0 && t + 2 < T && done) issue_load(t + 2);   // tile t's MMAs have read its buffer
     if (done) {
-      const int my_node = (it.tile0 + t) * kNodeTile + 32 * quarter + lane;
-      const uint32_t lane_base = tm + ((uint32_t)(32 * quarter) << 16) + (uint32_t)((t & 1) * SH::ACC);
-      for (int c0 = half * HALF; c0 < half * HALF + HALF; c0 += 32) {
-        float v[32];
-        float qn_l[4];
-        if (FMT == KNN_FMT_EUCL) {
+      const int col_node0 = (it.tile0 + t) * NT;
+      const uint32_t lane_base = tm + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((t & 1) * 256);
+      if (FMT == KNN_FMT_EUCL) {
+#pragma unroll 1
+        for (int c0 = slice * NCOL; c0 < slice * NCOL + NCOL; c0 += 32) {
+          float v[32];
           tmem_ld32(lane_base + c0, v);
-          qn_l[0] = qn_s[(c0 + lane) * 4];
-        } else {
-          for (int g = 0; g < 4; g++) qn_l[g] = qn_s[(c0 + lane) * 4 + g];
 #pragma unroll
-          for (int i = 0; i < 32; i++) v[i] = -__int_as_float(0x7f800000);
-          for (int g = 0; g < st.A; g++) {
-            float w[32];
-            tmem_ld32(lane_base + NQ * g + c0, w);
-            const float qg = g == 0 ? qn_l[0] : g == 1 ? qn_l[1] : g == 2 ? qn_l[2] : qn_l[3];
-#pragma unroll
-            for (int i = 0; i < 32; i++) v[i] = fmaxf(v[i], fmaf(-2.f, w[i], __shfl_sync(MRMG_FULL, qg, i)));
-          }
+          for (int i = 0; i < 32; i++) keep_insert(kd, ki, fmaf(-2.f, v[i], qn), col_node0 + c0 + i);
         }
+      } else {
+#pragma unroll 1
+        for (int c0 = slice * NCOL; c0 < slice * NCOL + NCOL; c0 += 32) {
+          float m[32];
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-          const float d2 = FMT == KNN_FMT_EUCL ? fmaf(-2.f, v[j], __shfl_sync(MRMG_FULL, qn_l[0], j)) : v[j];
-          float* ld = lst_d + ((size_t)quarter * NQ + c0 + j) * kKeep;
-          const unsigned m = __ballot_sync(MRMG_FULL, d2 < ld[kKeep - 1]);
-          if (m) warp_insert(ld, lst_i + ((size_t)quarter * NQ + c0 + j) * kKeep, m, d2, my_node, lane);
+          for (int i = 0; i < 32; i++) m[i] = -__int_as_float(0x7f800000);
+          for (int a = 0; a < st.A; a++) {
+            float v[32];
+            tmem_ld32(lane_base + 64 * a + c0, v);
+            const float qa = s_qna[a][row];
+#pragma unroll
+            for (int i = 0; i < 32; i++) m[i] = fmaxf(m[i], fmaf(-2.f, v[i], qa));
+          }
+#pragma unroll
+          for (int i = 0; i < 32; i++) keep_insert(kd, ki, m[i], col_node0 + c0 + i);
         }
       }
     }
@@ -600,34 +584,39 @@ __global__ void __launch_bounds__(256, 1) knn_tc_kernel(KnnStoreDev st, const do
     if (s_fail) break;
   }
   if (s_fail && tid == 0) atomicOr(err, E_TIMEOUT);
-
-  // merge the four quarter lists of each query into its candidate list
-  if (tid < it.qn) {
-    const long long qid = qorder[it.q0 + tid];
-    int h[4] = {0, 0, 0, 0};
+  (void)lane;
+  // merge the slices' lists into slice 0's; every MMA has completed, so the
+  // operand buffers are free (skipped after a timeout: copies may be in flight)
+  if (!s_fail) {
+    float* md = (float*)base;
+    int* mi = (int*)(base + (size_t)(S - 1) * kTileM * kKeep * sizeof(float));
+    if (slice > 0) {
+#pragma unroll
+      for (int i = 0; i < kKeep; i++) {
+        md[((size_t)(slice - 1) * kKeep + i) * kTileM + row] = kd[i];
+        mi[((size_t)(slice - 1) * kKeep + i) * kTileM + row] = ki[i];
+      }
+    }
+    __syncthreads();
+    if (slice == 0) {
+      for (int o = 0; o < S - 1; o++)
+        for (int i = 0; i < kKeep; i++) {
+          const float d = md[((size_t)o * kKeep + i) * kTileM + row];
+          if (!(d < kd[kKeep - 1])) break;   // each list is sorted
+          keep_insert(kd, ki, d, mi[((size_t)o * kKeep + i) * kTileM + row]);
+        }
+    }
+  }
+  if (qid >= 0) {
     float* od = cand_d + ((size_t)qid * chunks_max + it.chunk) * kKeep;
     int* oi = cand_i + ((size_t)qid * chunks_max + it.chunk) * kKeep;
-    for (int r = 0; r < kKeep; r++) {
-      int bq = 0;
-      float bd = __int_as_float(0x7f800000);
-      int bi = 0x7fffffff;
-      for (int g = 0; g < 4; g++) {
-        if (h[g] >= kKeep) continue;
-        const float d = lst_d[((size_t)g * NQ + tid) * kKeep + h[g]];
-        const int i = lst_i[((size_t)g * NQ + tid) * kKeep + h[g]];
-        if (i < 0) continue;
-        if (d < bd || (d == bd && i < bi)) { bd = d; bi = i; bq = g; }
-      }
-      if (bi == 0x7fffffff) { od[r] = __int_as_float(0x7f800000); oi[r] = -1; continue; }
-      od[r] = bd;
-      oi[r] = bi;
-      h[bq]++;
-    }
+#pragma unroll
+    for (int i = 0; i < kKeep; i++) { od[i] = kd[i]; oi[i] = ki[i]; }
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) tmem_dealloc(tm, SH::TMEM_COLS);
+  if (warp == 0) tmem_dealloc(tm, 512);
 }
 
 // ---------------------------------------------------------------------------
@@ -749,7 +738,7 @@ cudaError_t knn_store_build(KnnStore* s, const double* d_nodes, long long M, con
   s->nodes = d_nodes;
   s->mode_off.assign(h_mode_off, h_mode_off + n_modes + 1);
   const int fmt = metric == MRMG_METRIC_EUCLIDEAN ? KNN_FMT_EUCL : KNN_FMT_AGENT;
-  const int NT = kNodeTile;
+  const int NT = fmt == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
   std::vector<int> tile0(n_modes + 1, 0);
   s->mode_tiles.assign(n_modes, 0);
   for (int m = 0; m < n_modes; m++) {
@@ -816,9 +805,8 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
     for (long long q = 0; q < Q; q++) order[fill[h_q_mode[q]]++] = (int)q;
   }
   // work items: query tiles x node-tile chunks, about three waves of CTAs
-  const int NQ = s->dev.fmt == KNN_FMT_EUCL ? TcShape<KNN_FMT_EUCL>::NQ : TcShape<KNN_FMT_AGENT>::NQ;
   long long units = 0;
-  for (int m = 0; m < n_modes; m++) units += (long long)((qcount[m] + NQ - 1) / NQ) * s->mode_tiles[m];
+  for (int m = 0; m < n_modes; m++) units += (long long)((qcount[m] + kTileM - 1) / kTileM) * s->mode_tiles[m];
   const long long target = std::max(1, 3 * num_sms);
   int tpc = (int)std::max<long long>(1, (units + target - 1) / target);
   int chunks_max = 1;
@@ -834,12 +822,12 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
     if (qcount[m] == 0 || s->mode_tiles[m] == 0) continue;
     const int nch = (s->mode_tiles[m] + tpc - 1) / tpc;
     mode_chunks[m] = nch;
-    for (int q0 = 0; q0 < qcount[m]; q0 += NQ)
+    for (int q0 = 0; q0 < qcount[m]; q0 += kTileM)
       for (int c = 0; c < nch; c++) {
         KnnItem it;
         it.mode = m;
         it.q0 = qstart[m] + q0;
-        it.qn = std::min(NQ, qcount[m] - q0);
+        it.qn = std::min(kTileM, qcount[m] - q0);
         it.tile0 = c * tpc;
         it.tile1 = std::min(s->mode_tiles[m], (c + 1) * tpc);
         it.chunk = c;
@@ -884,18 +872,18 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_mch, mode_chunks.data(), sizeof(int) * n_modes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, 256, st);
   if (e != cudaSuccess) return e;
+  const int NT = s->dev.NT;
+  // at least 120 KB of shared memory: one CTA per SM, so two CTAs never wait
+  // on each other for the 512 tensor-memory columns each allocates
+  const size_t smem = std::max<size_t>(1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes, 120 * 1024);
   if (!items.empty()) {
-    // at least 120 KB of shared memory: one CTA per SM, so two CTAs never wait
-    // on each other for tensor-memory columns
     if (s->dev.fmt == KNN_FMT_EUCL) {
-      const size_t smem = std::max<size_t>(TcShape<KNN_FMT_EUCL>::SMEM, 120 * 1024);
       cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_EUCL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      knn_tc_kernel<KNN_FMT_EUCL><<<(int)items.size(), 256, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
+      knn_tc_kernel<KNN_FMT_EUCL><<<(int)items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
                                                                          d_cd, d_ci, d_eps, d_ctr + 1);
     } else {
-      const size_t smem = std::max<size_t>(TcShape<KNN_FMT_AGENT>::SMEM, 120 * 1024);
       cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_AGENT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      knn_tc_kernel<KNN_FMT_AGENT><<<(int)items.size(), 256, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
+      knn_tc_kernel<KNN_FMT_AGENT><<<(int)items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
                                                                           d_cd, d_ci, d_eps, d_ctr + 1);
     }
     e = cudaGetLastError();
