@@ -348,6 +348,7 @@ def run_gb300(args):
             extra["cpu_baseline"] = cpu_baseline(orc, scene, q1, q2, budget_s=args.cpu_seconds)
             if not args.skip_extra:
                 extra["knn"] = bench_knn(orc)
+                extra["penetration"] = bench_penetration()
 
     mism = int(reduce_max(float(mism), world))
     if rank == 0:
@@ -418,6 +419,82 @@ def bench_knn(orc, steps: int = 20) -> dict:
     return out
 
 
+def bench_penetration(steps: int = 10) -> dict:
+    """Path-penetration cost and gradient on 512 paths x 256 waypoints x 28
+    joints (four-arm scene; straight lines between collision-free endpoints
+    plus N(0, 0.05^2) noise): device time of the cost, the gradient and both
+    in one launch (inputs resident), accuracy against the float64 oracle on
+    two sampled paths, the MUFU roofline, and the float64 torch-autograd CPU
+    path on a sample."""
+    import torch
+
+    pen, col, scenes, _lib = pkg("penetration"), pkg("collision"), pkg("scenes"), pkg("_lib")
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import penetration_f64 as orc_pen
+
+    sc = scenes.make_arm_scene(0)
+    s = col.Gb300Scene(sc)
+    paths = scenes.make_path_workload(sc, seed=0, is_free=lambda q: s.is_collision_free_batch(q).cpu().numpy())
+    w = torch.from_numpy(paths).cuda()
+    P, T, D = w.shape
+    S, B = len(sc.sphere_radius), len(sc.box_lo)
+    counts = np.bincount(sc.sphere_robot, minlength=sc.n_robots)
+    n_pairs = S * B + int((counts.sum() ** 2 - (counts ** 2).sum()) // 2)
+    out = {"workload": f"{P} paths x {T} waypoints x {D} joints, four-arm scene ({S} spheres, {B} boxes, "
+                       f"{n_pairs} pairs per waypoint); margin 0.02, scale 0.02, beta 1, smoothness 0.1",
+           "pairs_per_waypoint": n_pairs}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(**kw):
+        for _ in range(3):
+            pen.path_penetration(s, w, **kw)
+        torch.cuda.synchronize()
+        ev0.record()
+        for _ in range(steps):
+            pen.path_penetration(s, w, **kw)
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / steps
+
+    ms_cost = timed(cost=True)
+    ms_grad = timed(cost=False, grad=True)
+    ms_both = timed(cost=True, grad=True)
+    res = pen.path_penetration(s, w, cost=True, grad=True)
+    errs = []
+    for p in (0, P // 2):
+        c_ref, g_ref = orc_pen.penetration_grad(sc.arrays(), paths[p:p + 1])
+        g = res["grad"][p].cpu().numpy().astype(np.float64)
+        errs.append({"path": p, "cost_rel_err": float(abs(res["cost"][p].item() - c_ref[0]) / abs(c_ref[0])),
+                     "grad_rel_err": float(np.linalg.norm(g - g_ref[0]) / np.linalg.norm(g_ref[0]))})
+    # MUFU operations per pair of the cost kernel: sqrt, 2^x and log2
+    import ctypes as C
+
+    mufu = C.c_double(0)
+    _lib.check(_lib.load().mrmg_microbench_fma(2, 20000, C.byref(mufu), None))
+    wpts = P * T
+    ach = 3.0 * n_pairs * wpts / (ms_cost * 1e-3) / 1e12
+    out.update({
+        "ms_cost": ms_cost, "ms_grad": ms_grad, "ms_cost_and_grad": ms_both,
+        "waypoints_per_s_cost_and_grad": wpts / (ms_both * 1e-3),
+        "paths_per_s_cost_and_grad": P / (ms_both * 1e-3),
+        "accuracy": errs,
+        "roofline_cost_kernel": {"bound": "mufu", "achieved": ach, "peak": mufu.value, "unit": "Tops/s",
+                                 "frac": ach / mufu.value,
+                                 "algorithmic": f"{wpts} waypoints x {n_pairs} pairs x 3 MUFU ops per launch",
+                                 "peak_source": "measured ex2.approx microbenchmark (mrmg_microbench_fma precision 2)"},
+    })
+    # CPU: float64 torch autograd (cost + gradient), all threads, on 2 paths
+    n_cpu = 2
+    t0 = time.perf_counter()
+    orc_pen.penetration_grad(sc.arrays(), paths[:n_cpu])
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": n_cpu * T / cpu_s, "unit": "waypoints/s (cost + gradient)",
+                           "cores": torch.get_num_threads(), "kind": "port",
+                           "sample": f"{n_cpu} paths x {T} waypoints, float64 torch autograd on the host"}
+    s.close()
+    return out
+
+
 def _measure_fp32_peak(_lib) -> float:
     import ctypes as C
 
@@ -460,6 +537,20 @@ def run_profile(args):
                           "stats": store.last_stats}), flush=True)
         return 0
 
+    if args.profile == "pen":
+        pen, col, scenes = pkg("penetration"), pkg("collision"), pkg("scenes")
+        sc = scenes.make_arm_scene(0)
+        s = col.Gb300Scene(sc)
+        paths = scenes.make_path_workload(sc, seed=0, n_paths=128)
+        w = torch.from_numpy(paths).cuda()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            pen.path_penetration(s, w, cost=True)
+            pen.path_penetration(s, w, cost=False, grad=True)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "pen", "launches": 2 * args.steps, "s": time.perf_counter() - t0}), flush=True)
+        return 0
+
     _lib, envm = pkg("_lib"), pkg("env")
     scene, q1, q2, N = workload(0)
     sc = envm.Gb300ArmEnvironment(scene, collision_resolution=RESOLUTION)._gb300
@@ -485,7 +576,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--chunks", type=int, default=1, help="pipelined chunks of the end-to-end plan")
     ap.add_argument("--skip-extra", action="store_true", help="only the headline edge-check workload")
-    ap.add_argument("--profile", choices=["early", "full", "knn"], default=None,
+    ap.add_argument("--profile", choices=["early", "full", "knn", "pen"], default=None,
                     help="short run of the first-pass edge kernel for ncu captures")
     args = ap.parse_args()
     if args.profile:

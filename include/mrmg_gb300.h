@@ -192,6 +192,29 @@ int mrmg_is_edge_collision_free_batch_noalloc(mrmg_scene *scene, const void *d_q
 int mrmg_arm_sphere_centers(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n,
                             float *d_c32, double *d_c64, void *stream);
 
+/* Smoothed path-penetration cost of an arm scene and its gradient through
+ * forward kinematics.  No counterpart in the reference: it feeds gradient
+ * path repair and shortcutting (robot_mode_shortcut,
+ * planners/shortcutting.py:87-244).  d_paths is [n_paths, n_waypoints,
+ * q_dim] FP32.  h_params = {margin, scale, beta, smooth_weight}; per path
+ *   cost = sum_t sum_pairs softplus(beta (margin - d)) / (beta scale)
+ *        + smooth_weight * sum_t |w[t+1] - w[t]|^2
+ * over every sphere-box pair (d = signed box distance of the centre minus the
+ * radius) and every pair of spheres on different robots (d = centre distance
+ * minus both radii).  Outputs (each may be NULL, not all): d_cost[n_paths]
+ * (FP64), d_wp_cost[n_paths, n_waypoints] (the pair terms of waypoint t plus
+ * its smoothness term towards t+1), d_grad[n_paths, n_waypoints, q_dim] =
+ * d_grad_cost[p] * dcost_p/dw (d_grad_cost NULL means 1).  warps_per_cta 0 =
+ * automatic (16).  Synchronises unless MRMG_FLAG_ASYNC. */
+int mrmg_path_penetration(mrmg_scene *scene, const float *d_paths, int64_t n_paths,
+                          int32_t n_waypoints, const double *h_params, const float *d_grad_cost,
+                          double *d_cost, float *d_wp_cost, float *d_grad, int32_t warps_per_cta,
+                          void *stream, int32_t flags);
+
+/* Penetration-kernel facts: [0] spheres, [1] boxes, [2] shared memory per CTA
+ * of the cost-only kernel, [3] of the gradient kernel (bytes, 16 warps). */
+int mrmg_penetration_info(const mrmg_scene *scene, int64_t *out4);
+
 /* Graph-capture support.  A call made with MRMG_FLAG_ASYNC inside a stream
  * capture reports no status; its device-side error bits live in the word
  * returned here (valid until the next call on the scene), which a captured
@@ -298,8 +321,10 @@ int mrmg_selftest_umma(const void *d_a, const void *d_b, int32_t n, float *d_c, 
 /* ------------------------------------------------------------------------ */
 
 /* Measured fused-multiply-add throughput of the device (precision 0 = FP32,
- * 1 = FP64) in TFLOP/s: the roofline denominators of the collision (FP32
- * pipe) and distance (FP64 pipe) kernels.  No counterpart in the reference. */
+ * 1 = FP64) in TFLOP/s, or (precision 2) the special-function-unit rate of
+ * ex2.approx in T operations/s: the roofline denominators of the collision
+ * (FP32 pipe), distance (FP64 pipe) and penetration-cost (MUFU) kernels.  No
+ * counterpart in the reference. */
 int mrmg_microbench_fma(int32_t precision, int64_t iters, double *out_tflops, void *stream);
 
 #ifdef __cplusplus

@@ -51,6 +51,8 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_is_edge_collision_free_batch": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, vp, i32]),
     "mrmg_is_edge_collision_free_batch_noalloc": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, vp, i32]),
     "mrmg_arm_sphere_centers": (i32, [vp, vp, i32, i64, vp, vp, vp]),
+    "mrmg_path_penetration": (i32, [vp, vp, i64, i32, vp, vp, vp, vp, vp, i32, vp, i32]),
+    "mrmg_penetration_info": (i32, [vp, vp]),
     "mrmg_last_call_stats": (i32, [vp, vp]),
     "mrmg_scene_error_word": (i32, [vp, vp]),
     "mrmg_scene_reserve": (i32, [vp, i64, vp]),

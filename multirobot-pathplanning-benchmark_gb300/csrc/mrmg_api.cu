@@ -75,6 +75,9 @@ struct mrmg_scene {
   double band = 0.0;
   int64_t n_pairs_groups = 0;
   std::vector<int> slot_to_sphere;   // arm: slot -> input sphere index (-1 padding)
+  PenDev pen{};                      // arm: path-penetration cost tables
+  double* d_pen_seg = nullptr;       // per-segment cost scratch
+  long long pen_seg_cap = 0;
   std::vector<float4> box32_host;    // arm: box tables in their current test order
   std::vector<double> box64_host;
 };
@@ -393,6 +396,46 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   blk.add(box32.data(), box32.size(), &d.box32);
   blk.add(grp.data(), grp.size(), &d.grp);
   blk.add(pairs.data(), pairs.size(), &d.pairs);
+  // penetration-cost tables: real spheres in slot order (robot, then frame)
+  std::vector<float4> pen_sph, pen_box(2 * B);
+  std::vector<int4> pen_task;
+  PenDev& pd = sc->pen;
+  {
+    // slots are ordered by robot, then frame: lk is the prefix count of
+    // spheres over (robot, frame) in that order
+    int cnt[kMaxRobots][kMaxLinks + 1] = {};
+    for (int sl = 0; sl < G * SPG; sl++) {
+      const int i = slot_sphere[sl];
+      if (i < 0) continue;
+      const int r = grp[sl / SPG] & 0xff, k = grp[sl / SPG] >> 8;
+      cnt[r][k]++;
+      const double* l = h_sphere_local + 3 * i;
+      pen_sph.push_back(make_float4((float)l[0], (float)l[1], (float)l[2], (float)h_sphere_radius[i]));
+    }
+    int acc = 0;
+    for (int r = 0; r < kMaxRobots; r++) {
+      for (int k = 0; k <= kMaxLinks; k++) { pd.lk[r][k] = acc; acc += cnt[r][k]; }
+      pd.lk[r][kMaxLinks + 1] = acc;
+    }
+    const int Sn = (int)pen_sph.size();
+    // tasks: consecutive sphere pairs of one robot
+    for (int r = 0; r < R; r++) {
+      const int s0 = pd.lk[r][0], s1 = pd.lk[r][kMaxLinks + 1];
+      for (int i = s0; i < s1; i += 2) pen_task.push_back(make_int4(i, i + 1 < s1 ? i + 1 : -1, s0, s1));
+    }
+    pd.S = Sn;
+    pd.B = B;
+    pd.NTK = (int)pen_task.size();
+  }
+  for (int b = 0; b < B; b++) {
+    const double* lo = h_box_lo + 3 * b;
+    const double* hi = h_box_hi + 3 * b;
+    pen_box[2 * b] = make_float4((float)(0.5 * (lo[0] + hi[0])), (float)(0.5 * (lo[1] + hi[1])), (float)(0.5 * (lo[2] + hi[2])), 0.f);
+    pen_box[2 * b + 1] = make_float4((float)(0.5 * (hi[0] - lo[0])), (float)(0.5 * (hi[1] - lo[1])), (float)(0.5 * (hi[2] - lo[2])), 0.f);
+  }
+  blk.add(pen_sph.data(), pen_sph.size(), &pd.sph);
+  blk.add(pen_task.data(), pen_task.size(), &pd.task);
+  blk.add(pen_box.data(), pen_box.size(), &pd.box);
   cudaError_t e = blk.upload(&sc->d_tables);
   if (e != cudaSuccess) { mrmg_scene_destroy(sc); return cuda_fail(e, "upload arm scene"); }
   sc->band = d.delta;
@@ -411,6 +454,7 @@ int mrmg_scene_destroy(mrmg_scene* sc) {
   if (sc->d_ctr) cudaFree(sc->d_ctr);
   if (sc->d_pend) cudaFree(sc->d_pend);
   if (sc->d_surv) cudaFree(sc->d_surv);
+  if (sc->d_pen_seg) cudaFree(sc->d_pen_seg);
   if (sc->h_ctr) cudaFreeHost(sc->h_ctr);
   delete sc;
   return MRMG_OK;
@@ -678,6 +722,67 @@ int mrmg_arm_sphere_centers(mrmg_scene* sc, const void* d_q, int32_t dtype, int6
   if (e != cudaSuccess) return cuda_fail(e, "launch centers");
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, "centers kernel");
+  return MRMG_OK;
+}
+
+int mrmg_path_penetration(mrmg_scene* sc, const float* d_paths, int64_t P, int32_t T, const double* h_params,
+                          const float* d_grad_cost, double* d_cost, float* d_wp_cost, float* d_grad,
+                          int32_t warps_per_cta, void* stream, int32_t flags) {
+  if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
+  if (!h_params) return fail(MRMG_ERR_ARG, "params is NULL");
+  if (P < 0 || T < 1) return fail(MRMG_ERR_ARG, "need n_paths >= 0 and n_waypoints >= 1");
+  if (!d_cost && !d_wp_cost && !d_grad) return fail(MRMG_ERR_ARG, "no output requested");
+  if (P > 0 && !d_paths) return fail(MRMG_ERR_ARG, "paths is NULL");
+  const double margin = h_params[0], scale = h_params[1], beta = h_params[2], smooth = h_params[3];
+  if (!std::isfinite(margin) || !(scale > 0.0) || !std::isfinite(scale) || !(beta > 0.0) || !std::isfinite(beta) ||
+      !(smooth >= 0.0) || !std::isfinite(smooth))
+    return fail(MRMG_ERR_ARG, "params: finite margin, scale > 0, beta > 0, smooth weight >= 0");
+  const long long nseg = (T + 31) / 32;
+  if (P * nseg >= (1ll << 31)) return fail(MRMG_ERR_ARG, "too many path segments for one call");
+  int warps = warps_per_cta > 0 ? warps_per_cta : 16;
+  if (warps < sc->arm.R) warps = sc->arm.R;
+  if (warps > 16) return fail(MRMG_ERR_UNSUPPORTED, "warps per CTA must be <= 16 (and >= robots)");
+  int smem_max = 0;
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, sc->device);
+  const size_t smem = pen_smem_bytes(sc->pen.S, sc->pen.B, sc->arm.R, sc->arm.D, d_grad != nullptr, warps);
+  if (smem > (size_t)smem_max)
+    return fail(MRMG_ERR_UNSUPPORTED, "scene too large for the penetration kernel (%zu B shared memory > %d)", smem,
+                smem_max);
+  if (P == 0) return MRMG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (d_cost && P * nseg > sc->pen_seg_cap) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cap);
+    if (cap != cudaStreamCaptureStatusNone)
+      return fail(MRMG_ERR_ARG, "penetration scratch must be sized by an uncaptured call of at least this size first");
+    if (sc->d_pen_seg) cudaFree(sc->d_pen_seg);
+    sc->d_pen_seg = nullptr;
+    sc->pen_seg_cap = 0;
+    cudaError_t e = cudaMalloc(&sc->d_pen_seg, sizeof(double) * P * nseg);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(penetration scratch)");
+    sc->pen_seg_cap = P * nseg;
+  }
+  PenParams pp;
+  pp.margin = (float)margin;
+  pp.inv_scale = (float)(1.0 / scale);
+  pp.beta = (float)beta;
+  pp.inv_beta = (float)(1.0 / beta);
+  pp.smooth_w = (float)smooth;
+  cudaError_t e = pen_launch(sc->arm, sc->pen, pp, d_paths, P, T, d_grad_cost, sc->d_pen_seg, d_cost, d_wp_cost,
+                             d_grad, warps, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch penetration cost");
+  if (flags & MRMG_FLAG_ASYNC) return MRMG_OK;
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "penetration kernel");
+  return MRMG_OK;
+}
+
+int mrmg_penetration_info(const mrmg_scene* sc, int64_t* out4) {
+  if (!sc || sc->kind != 1 || !out4) return fail(MRMG_ERR_ARG, "arm scene and out4 required");
+  out4[0] = sc->pen.S;
+  out4[1] = sc->pen.B;
+  out4[2] = (int64_t)pen_smem_bytes(sc->pen.S, sc->pen.B, sc->arm.R, sc->arm.D, 0, 16);
+  out4[3] = (int64_t)pen_smem_bytes(sc->pen.S, sc->pen.B, sc->arm.R, sc->arm.D, 1, 16);
   return MRMG_OK;
 }
 

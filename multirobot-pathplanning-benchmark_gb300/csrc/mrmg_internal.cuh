@@ -53,6 +53,25 @@ struct ArmDev {
   const uint32_t* pairs;   // [NP]     group a | group b << 16 (different robots)
 };
 
+// ---------------------------------------------------------------------------
+// Path-penetration cost tables of an arm scene: the real spheres (padding
+// dropped) grouped by robot, then by frame, so the spheres of other robots
+// are [0, first of robot) and [first of next robot, S); boxes in input order.
+// ---------------------------------------------------------------------------
+struct PenDev {
+  int S, B, NTK;
+  const float4* sph;     // [S]  local xyz, radius
+  const int4* task;      // [NTK] sphere, second sphere of the same robot (-1: none),
+                         //       the robot's first sphere, the next robot's first sphere
+  const float4* box;     // [2B] centre xyz, half extents xyz
+  int lk[kMaxRobots][kMaxLinks + 2];   // spheres of (robot r, frame k): [lk[r][k], lk[r][k+1])
+};
+
+// cost of one pair with signed distance d: softplus(beta (margin - d)) / (beta scale)
+struct PenParams {
+  float margin, inv_scale, beta, inv_beta, smooth_w;
+};
+
 // per-call scratch counters (device): [0] work queue, [1] pending count,
 // [2] error bits, [3] pass-two queue, [4..5] configurations evaluated (64-bit),
 // [6] surviving edges, [7] longest remaining position range, [8..9] phase-B
@@ -136,6 +155,11 @@ cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, 
 int arm_prepare(const ArmDev& s, int warps);
 int arm_supported_spg(int idx);   // list of compiled SPG values, -1 at end
 int arm_gpl_for_spg(int spg);
+
+size_t pen_smem_bytes(int S, int B, int R, int D, int grad, int warps);
+cudaError_t pen_launch(const ArmDev& a, const PenDev& pd, const PenParams& pp, const float* paths, long long P, int T,
+                       const float* gout, double* seg, double* cost, float* wp_cost, float* grad, int warps,
+                       cudaStream_t st);
 
 cudaError_t binary_indices(long long N, long long* out, cudaStream_t st, int chunked);
 

@@ -322,3 +322,34 @@ def make_knn_workload(seed: int = 0, n_nodes: int = 200_000, n_modes: int = 16, 
     blk = dim // agents
     slices = np.array([[a * blk, (a + 1) * blk] for a in range(agents)], dtype=np.int64)
     return dict(nodes=nodes, mode_offsets=offsets, queries=queries, q_mode=q_mode, slices=slices, k=10)
+
+
+def make_path_workload(scene: ArmScene, seed: int = 0, n_paths: int = 512, n_waypoints: int = 256,
+                       noise: float = 0.05, is_free=None) -> np.ndarray:
+    """Paths for the penetration cost: straight lines between endpoints drawn
+    uniform in the joint limits (only collision-free ones when ``is_free``,
+    a callable on [n, D] float32 arrays returning per-row verdicts, is given),
+    interior waypoints perturbed by N(0, noise^2) per joint.  FP32 [P, T, D]."""
+    rng = np.random.default_rng(seed)
+    lim = scene.limits
+    D = lim.shape[1]
+    need = 2 * n_paths
+    ends = []
+    got = 0
+    for _ in range(10_000):
+        if got >= need:
+            break
+        cand = rng.uniform(lim[0], lim[1], (max(4 * need, 1024), D)).astype(np.float32)
+        if is_free is not None:
+            cand = cand[np.asarray(is_free(cand)).astype(bool)]
+        ends.append(cand)
+        got += len(cand)
+    if got < need:
+        raise RuntimeError("could not draw enough collision-free endpoints")
+    e = np.concatenate(ends)[:need]
+    q1, q2 = e[:n_paths].astype(np.float64), e[n_paths:].astype(np.float64)
+    s = np.linspace(0.0, 1.0, n_waypoints)
+    paths = q1[:, None, :] + s[None, :, None] * (q2 - q1)[:, None, :]
+    if n_waypoints > 2:
+        paths[:, 1:-1] += rng.normal(0.0, noise, (n_paths, n_waypoints - 2, D))
+    return paths.astype(np.float32)
