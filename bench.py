@@ -349,6 +349,7 @@ def run_gb300(args):
             if not args.skip_extra:
                 extra["knn"] = bench_knn(orc)
                 extra["penetration"] = bench_penetration()
+                extra["serving"] = bench_serving(orc)
 
     mism = int(reduce_max(float(mism), world))
     if rank == 0:
@@ -493,6 +494,64 @@ def bench_penetration(steps: int = 10) -> dict:
                            "sample": f"{n_cpu} paths x {T} waypoints, float64 torch autograd on the host"}
     s.close()
     return out
+
+
+def bench_serving(orc, steps: int = 24, warmup: int = 3) -> dict:
+    """Serving-shaped load on eight mobile manipulators (72-D, 304 spheres,
+    200 boxes): each step 64 planner instances submit 100-20,000 uniform
+    configurations and 10-5,000 edges (N uniform in 5..800) each; one graph
+    launch per step after the launch shape is autotuned.  Reports host
+    latency p50/p99 (packing + copies + checks + split), device time, items/s,
+    verdicts of two instances against the oracle, and the oracle's CPU rate."""
+    import torch
+
+    scenes, envm, srv = pkg("scenes"), pkg("env"), pkg("serving")
+    sc = scenes.make_mobile_scene(0)
+    env = envm.Gb300ArmEnvironment(sc)              # tunes the box test order
+    s = env._gb300
+    pool = [scenes.make_serving_requests(sc, seed=100 + i) for i in range(3)]
+    # autotune the persistent grid on a quarter of the first step
+    r0 = pool[0]
+    cfg = np.concatenate([r["configs"] for r in r0[:16]])
+    q1 = np.concatenate([cfg] + [r["q1"] for r in r0[:16]])
+    q2 = np.concatenate([cfg] + [r["q2"] for r in r0[:16]])
+    N = np.concatenate([np.full(len(cfg), 3, np.int64)] + [r["N"] for r in r0[:16]])
+    tune = srv.autotune_launch(s, q1, q2, N, ctas_per_sm=(1, 2, 3, 4), warps=(4, 8), repeats=3)
+    b = srv.ServingBatcher(s)
+    for i in range(warmup):
+        b.step(pool[i % len(pool)])
+    b.latencies.clear()
+    b.device_ms.clear()
+    items = cfgs = edges = 0
+    t0 = time.perf_counter()
+    for i in range(steps):
+        res = b.step(pool[i % len(pool)])
+        cfgs += res.n_configs
+        edges += res.n_edges
+    wall = time.perf_counter() - t0
+    lat = b.latency_percentiles()
+    # verdicts of two instances of the first step against the oracle
+    res = b.step(pool[0])
+    o = orc.OracleScene(sc)
+    mism = 0
+    t1 = time.perf_counter()
+    for k in (0, 1):
+        r = pool[0][k]
+        mism += int((res.config_free[k] != o.configs_free(r["configs"])).sum())
+        mism += int((res.edge_free[k] != o.edges_free(r["q1"], r["q2"], 0.05, N=r["N"])).sum())
+    cpu_s = time.perf_counter() - t1
+    cpu_items = sum(len(pool[0][k]["configs"]) + len(pool[0][k]["q1"]) for k in (0, 1))
+    items = cfgs + edges
+    return {
+        "workload": "8 mobile manipulators (planar base + 6-DoF arm, 72-D, 304 spheres), 200 boxes in a 6x6x2 m room; "
+                    "64 instances/step, each 100-20,000 configs and 10-5,000 edges (N 5..800)",
+        "steps": steps, "configs_per_step": cfgs / steps, "edges_per_step": edges / steps,
+        "latency": lat, "items_per_s": items / wall, "configs_per_s": cfgs / wall, "edges_per_s": edges / wall,
+        "graph_launches_per_step": 1, "buckets": [list(k) for k in b.graphs],
+        "autotune": tune, "verdict_mismatches_sampled": mism,
+        "cpu_baseline": {"value": cpu_items / cpu_s, "unit": "items/s (configs + edges)", "cores": orc.num_threads(),
+                         "kind": "port", "sample": "instances 0 and 1 of one step, oracle/oracle.c FP64, OpenMP"},
+    }
 
 
 def _measure_fp32_peak(_lib) -> float:

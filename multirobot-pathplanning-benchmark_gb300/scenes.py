@@ -353,3 +353,26 @@ def make_path_workload(scene: ArmScene, seed: int = 0, n_paths: int = 512, n_way
     if n_waypoints > 2:
         paths[:, 1:-1] += rng.normal(0.0, noise, (n_paths, n_waypoints - 2, D))
     return paths.astype(np.float32)
+
+
+def make_serving_requests(scene: ArmScene, seed: int = 0, n_instances: int = 64, configs=(100, 20_000),
+                          edges=(10, 5_000), steps=(5, 800)) -> list:
+    """One planner step of a serving load: each instance submits a uniform
+    number of configurations (``configs`` range, inclusive) uniform in the
+    joint limits and a uniform number of edges (``edges`` range) between
+    endpoints uniform in the limits, each with an explicit interpolation count
+    N uniform in ``steps``.  FP32 endpoints."""
+    rng = np.random.default_rng(seed)
+    lim = scene.limits
+    D = lim.shape[1]
+    out = []
+    for _ in range(n_instances):
+        nc = int(rng.integers(configs[0], configs[1] + 1))
+        ne = int(rng.integers(edges[0], edges[1] + 1))
+        out.append(dict(
+            configs=rng.uniform(lim[0], lim[1], (nc, D)).astype(np.float32),
+            q1=rng.uniform(lim[0], lim[1], (ne, D)).astype(np.float32),
+            q2=rng.uniform(lim[0], lim[1], (ne, D)).astype(np.float32),
+            N=rng.integers(steps[0], steps[1] + 1, ne).astype(np.int64),
+        ))
+    return out
