@@ -279,6 +279,28 @@ def run_gb300(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         vh = plan.run()
+    e2e_serial_s = reduce_max(time.perf_counter() - t0, world)
+    e2e_serial = world * n * args.steps / e2e_serial_s
+    mism += int((vh != ref).sum())
+
+    # the same with two plans in flight: step k+1's endpoints cross to the
+    # device while step k's checks run (every step still copies its inputs
+    # and reads its verdicts back inside the timed region)
+    pipe = env.edge_check_pipeline(n, depth=2)
+    for p in pipe.plans:
+        p.q1_host[:] = q1
+        p.q2_host[:] = q2
+    for _ in range(args.warmup):
+        pipe.result(pipe.submit())
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    prev = pipe.submit()
+    for _ in range(args.steps - 1):
+        cur = pipe.submit()
+        vh = pipe.result(prev)
+        prev = cur
+    vh = pipe.result(prev)
     e2e_s = reduce_max(time.perf_counter() - t0, world)
     e2e = world * n * args.steps / e2e_s
     mism += int((vh != ref).sum())
@@ -365,8 +387,11 @@ def run_gb300(args):
             "clocks": clk,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(q1.nbytes + q2.nbytes),
                     "d2h_bytes_per_step": int(n),
-                    "api": f"Gb300ArmEnvironment.edge_check_plan(n).run(): one CUDA graph per step, "
-                           f"{args.chunks} pipelined chunks"},
+                    "api": "Gb300ArmEnvironment.edge_check_pipeline(n, depth=2): one CUDA graph per step "
+                           "(endpoints host->device, checks, verdicts device->host), two steps in flight"},
+            "e2e_serial": {"value": e2e_serial, "unit": UNIT,
+                           "api": f"Gb300ArmEnvironment.edge_check_plan(n).run(): one step at a time, "
+                                  f"{args.chunks} pipelined chunks"},
             "e2e_batch_call": {"value": call_e2e, "unit": UNIT,
                                "api": "Gb300ArmEnvironment.batch_is_edge_collision_free(pinned tensors)"},
             "gpu_launches": 5 * args.steps,

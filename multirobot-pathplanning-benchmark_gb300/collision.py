@@ -259,14 +259,53 @@ class EdgeCheckPlan:
             self.out_pin.copy_(self.out, non_blocking=True)
             self.err_pin.copy_(self.err, non_blocking=True)
 
-    def run(self) -> np.ndarray:
+    def launch(self):
+        """Replay the graph on the plan's stream without waiting."""
         with torch.cuda.stream(self.compute):   # replay() launches on the current stream
             self.graph.replay()
+
+    def wait(self) -> np.ndarray:
+        """Wait for the last launch; its verdicts (1 = free) as a numpy view of
+        the pinned output buffer."""
         self.compute.synchronize()
         bits = int(np.bitwise_or.reduce(self.err_pin.numpy())) if self.chunks else 0
         if bits:
             _lib.check(self.scene.lib.mrmg_status_from_error_bits(bits), "is_edge_collision_free")
         return self.out_pin.numpy()
+
+    def run(self) -> np.ndarray:
+        self.launch()
+        return self.wait()
+
+
+class EdgeCheckPipeline:
+    """Several ``EdgeCheckPlan`` slots, each on its own scene handle (own
+    per-call scratch) and stream, so consecutive batches overlap: while one
+    slot's checks run, the next slot's endpoints are already crossing to the
+    device.  ``submit()`` launches the next slot and returns its index;
+    ``result(slot)`` waits for that slot and returns its verdicts.  Fill a
+    slot's ``q1_host`` / ``q2_host`` only after its previous result was taken.
+    Every batch still copies its endpoints host->device and its verdicts back.
+    """
+
+    def __init__(self, plans: list):
+        if not plans:
+            raise ValueError("a pipeline needs at least one plan")
+        self.plans = plans
+        self.next = 0
+
+    @property
+    def depth(self) -> int:
+        return len(self.plans)
+
+    def submit(self) -> int:
+        slot = self.next
+        self.plans[slot].launch()
+        self.next = (slot + 1) % len(self.plans)
+        return slot
+
+    def result(self, slot: int) -> np.ndarray:
+        return self.plans[slot].wait()
 
 
 class _DeviceWord:

@@ -588,8 +588,8 @@ __device__ __forceinline__ void load_edge(const void* q1, const void* q2, int dt
 // integer-distance certificate, else FP64 (abstract_env.py:321-323).
 // Returns false on a non-finite edge length (int() of nan/inf raises).
 __device__ __forceinline__ bool edge_N(const void* q1, const void* q2, int dtype, long long e, int D, int lane,
-                                       double res, const long long* Np, float mloc, bool nanf, bool allow_fast,
-                                       long long* N_out) {
+                                       double res, float res32, const long long* Np, float mloc, bool nanf,
+                                       bool allow_fast, long long* N_out) {
   if (Np) {
     *N_out = Np[e];
     return *N_out >= 0;
@@ -597,13 +597,13 @@ __device__ __forceinline__ bool edge_N(const void* q1, const void* q2, int dtype
   if (allow_fast) {
     const float m32 = warp_max(mloc);
     const bool anynan = __any_sync(MRMG_FULL, nanf);
-    const float t32 = __fdiv_rn(m32, (float)res);
+    const float t32 = __fdiv_rn(m32, res32);
     if (!anynan && t32 < 4194304.f) {
       const float fl = floorf(t32);
       const float fr = t32 - fl;
       const float tol = 4.8e-7f * fmaxf(t32, 1.f);
       if (fr > tol && fr < 1.f - tol) {
-        *N_out = max(2ll, (long long)fl + 1);
+        *N_out = max(2, (int)fl + 1);   // through int32: fl < 2^22
         return true;
       }
     }
@@ -642,6 +642,7 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
   float2* wcs; float* wqv; float4* wsph; double* w64;
   warp_areas(s, smem_arm, table_bytes(s), wib, RESOLVE, &wcs, &wqv, &wsph, &w64);
   const int D = s.D;
+  const float res32 = (float)res;
   const unsigned lt_mask = (1u << lane) - 1u;
   long long stat_cfg = 0;
 
@@ -664,7 +665,7 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
     bool nanf;
     load_edge(q1, q2, dtype, e, D, lane, &sdf, &mloc, &nanf);
     long long N = 0;
-    const bool good = edge_N(q1, q2, dtype, e, D, lane, res, Np, mloc, nanf, !RESOLVE, &N);
+    const bool good = edge_N(q1, q2, dtype, e, D, lane, res, res32, Np, mloc, nanf, !RESOLVE, &N);
     if (!good || N_start > N) {
       if (lane == 0) { atomicOr(&ctr[kCtrErr], !good ? E_BAD_INPUT : E_N_START); out[e] = 0; }
       __syncwarp();
@@ -684,9 +685,11 @@ __global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1
           if (incl || (c != 0 && c != N - 1)) { iv = c; break; }
         }
         if (iv >= 0) {
-          sdf.nm1 = (float)(N - 1);
+          // N <= 2^24 here: int32 -> FP32 conversions (the 64-bit ones issue
+          // on the FP64 pipe, which is narrow on this part)
+          sdf.nm1 = (float)(int)(N - 1);
           sdf.rn = __frcp_rn(sdf.nm1);
-          sdf.fi = (float)iv;
+          sdf.fi = (float)(int)iv;
           stat_cfg++;
           const uint8_t code = eval_config<GPL, SPG, false>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
           if (code == V_COLLIDE && !full) {
@@ -813,7 +816,7 @@ __global__ void __launch_bounds__(256) arm_edges_phase_b(ArmDev s, const void* q
       load_edge(q1, q2, dtype, e, D, lane, &sdf, &mloc, &nanf);
       sdf.nm1 = (float)(N - 1);
       sdf.rn = __frcp_rn(sdf.nm1);
-      sdf.fi = (float)is;
+      sdf.fi = (float)(int)is;   // survivors have N <= 2^24
       stat_cfg++;
       const uint8_t code = eval_config<GPL, SPG, false>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
       if (lane == 0) {

@@ -112,6 +112,31 @@ class Gb300CollisionBackend:
         return EdgeCheckPlan(self._gb300, n, self.collision_resolution if resolution is None else resolution,
                              include_endpoints, dtype=dtype, chunks=chunks)
 
+    def edge_check_pipeline(self, n: int, depth: int = 2, resolution: Optional[float] = None,
+                            include_endpoints: bool = False, dtype=torch.float32):
+        """``depth`` plans of ``n`` edges on separate scene handles and streams
+        (see ``collision.EdgeCheckPipeline``): batch k+1's copies overlap
+        batch k's checks."""
+        from .collision import EdgeCheckPipeline
+
+        scenes = [self._gb300] + [self._clone_scene() for _ in range(max(1, int(depth)) - 1)]
+        res = self.collision_resolution if resolution is None else resolution
+        from .collision import EdgeCheckPlan
+
+        return EdgeCheckPipeline([EdgeCheckPlan(sc, n, res, include_endpoints, dtype=dtype, chunks=1)
+                                  for sc in scenes])
+
+    def _clone_scene(self):
+        """Another handle on the same scene (own scratch), with the same box
+        test order as this env's handle."""
+        from .collision import Gb300Scene
+
+        sc = Gb300Scene(self.scene)
+        smp = getattr(self, "_tune_samples", None)
+        if smp is not None:
+            sc.tune_test_order(smp)
+        return sc
+
     # --- path check (planning_env.py:1765-1881), one batched pass ----------
     def is_path_collision_free(self, path, binary_order: bool = True, resolution: Optional[float] = None,
                                tolerance: Optional[float] = None, check_edges_in_order: bool = False,
@@ -193,4 +218,5 @@ class Gb300ArmEnvironment(Gb300CollisionBackend):
             # test-order autotuning from configurations uniform in the joint limits
             rng = np.random.default_rng(seed)
             smp = rng.uniform(self.limits[0], self.limits[1], (tune_samples, scene.q_dim)).astype(np.float32)
+            self._tune_samples = smp
             self.box_order = self._gb300.tune_test_order(smp)

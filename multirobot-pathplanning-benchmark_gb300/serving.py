@@ -218,7 +218,7 @@ class ServingBatcher:
 
 
 def autotune_launch(scene: Gb300Scene, q1, q2, N, resolution: float = 0.0, include_endpoints: bool = False,
-                    ctas_per_sm=(1, 2, 3, 4), warps=(4, 8, 16), repeats: int = 3) -> dict:
+                    ctas_per_sm=(1, 2, 3, 4), warps=(4, 8), repeats: int = 3) -> dict:
     """Time the edge pipeline on a sample (q1, q2, N) for every launch shape
     (CTAs per SM x warps per CTA), keep the fastest on the scene and return
     the table.  Shapes the scene's shared memory does not allow are skipped."""
@@ -230,26 +230,26 @@ def autotune_launch(scene: Gb300Scene, q1, q2, N, resolution: float = 0.0, inclu
     table = []
     ref = None
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for cps in ctas_per_sm:
-        for w in warps:
-            try:
-                scene.set_launch(cps * sms, w)
-                scene.is_edge_collision_free_batch(a, b, resolution, include_endpoints, N=Nt, out=out)
-            except (ValueError, NotImplementedError, RuntimeError):
-                continue
-            got = out.cpu().numpy()
-            if ref is None:
-                ref = got.copy()
-            elif not np.array_equal(ref, got):
-                raise AssertionError("verdicts changed with the launch shape")
-            ts = []
-            for _ in range(repeats):
-                ev0.record()
-                scene.is_edge_collision_free_batch(a, b, resolution, include_endpoints, N=Nt, out=out)
-                ev1.record()
-                torch.cuda.synchronize()
-                ts.append(ev0.elapsed_time(ev1))
-            table.append({"ctas_per_sm": cps, "warps": w, "ms": float(np.median(ts))})
+    shapes = [(cps, w) for cps in ctas_per_sm for w in warps]
+    for cps, w in shapes:
+        try:
+            scene.set_launch(cps * sms, w)
+            scene.is_edge_collision_free_batch(a, b, resolution, include_endpoints, N=Nt, out=out)
+        except (ValueError, NotImplementedError, RuntimeError):
+            continue
+        got = out.cpu().numpy()
+        if ref is None:
+            ref = got.copy()
+        elif not np.array_equal(ref, got):
+            raise AssertionError("verdicts changed with the launch shape")
+        ts = []
+        for _ in range(repeats):
+            ev0.record()
+            scene.is_edge_collision_free_batch(a, b, resolution, include_endpoints, N=Nt, out=out)
+            ev1.record()
+            torch.cuda.synchronize()
+            ts.append(ev0.elapsed_time(ev1))
+        table.append({"ctas_per_sm": cps, "warps": w, "ms": float(np.median(ts))})
     if not table:
         scene.set_launch(0, 0)
         return {"best": None, "table": table}

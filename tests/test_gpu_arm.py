@@ -205,3 +205,32 @@ def test_edge_check_plan_graph(gpu, oracle):
     plan.q1_host[17, 0] = np.nan
     with pytest.raises(ValueError):
         plan.run()
+
+
+def test_edge_check_pipeline(gpu, oracle):
+    """Two plans in flight on separate scene handles: every batch gets the
+    oracle's verdicts, also when the slots hold different batches."""
+    scenes, envm = pkg("scenes"), pkg("env")
+    scene = scenes.make_arm_scene(0)
+    env = envm.Gb300ArmEnvironment(scene, collision_resolution=0.05, tune_samples=512)
+    o = oracle.OracleScene(scene)
+    w = [scenes.make_arm_workload(scene, seed=s, n_configs=10, n_edges=700) for s in (1, 2, 3)]
+    want = [o.edges_free(x["q1"], x["q2"], 0.05) for x in w]
+    pipe = env.edge_check_pipeline(700, depth=2)
+    assert pipe.depth == 2
+    got = []
+    order = [0, 1, 2, 1, 0, 2]
+    tickets = []
+    for k, i in enumerate(order):
+        slot = pipe.next
+        if len(tickets) >= pipe.depth:
+            t, j = tickets.pop(0)
+            got.append((j, pipe.result(t).copy()))
+        pipe.plans[slot].q1_host[:] = w[i]["q1"]
+        pipe.plans[slot].q2_host[:] = w[i]["q2"]
+        tickets.append((pipe.submit(), i))
+    for t, j in tickets:
+        got.append((j, pipe.result(t).copy()))
+    assert len(got) == len(order)
+    for j, v in got:
+        assert np.array_equal(v, want[j]), j
