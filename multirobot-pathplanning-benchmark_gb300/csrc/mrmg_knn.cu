@@ -411,6 +411,33 @@ __device__ __forceinline__ void keep_insert(float (&kd)[kKeep], int (&ki)[kKeep]
 // quadrant its warp rank allows) and the w/4-th slice of each tile's columns,
 // so every query row is scanned by kSplit threads with their own kept lists,
 // merged through shared memory at the end.
+// One 32-column chunk of a query row: the approximate squared distances go
+// to this thread's column of `cand` (column-major over the CTA's threads, so
+// stores and dynamically indexed reloads are bank-conflict free), a bitmask
+// marks those under the current 16th kept distance, and only the marked ones
+// are inserted: the warp runs as many insert steps as its busiest lane needs,
+// instead of one per column whenever any lane inserts.
+template <bool FROM_DOT>
+__device__ __forceinline__ void keep_chunk(float (&kd)[kKeep], int (&ki)[kKeep], const float (&v)[32], float qn,
+                                           float* cand, int col0) {
+  const float thr = kd[kKeep - 1];
+  const int nth = blockDim.x;
+  unsigned m = 0;
+#pragma unroll
+  for (int i = 0; i < 32; i++) {
+    const float d = FROM_DOT ? fmaf(-2.f, v[i], qn) : v[i];
+    if (d < thr) {
+      cand[i * nth] = d;
+      m |= 1u << i;
+    }
+  }
+  while (m) {
+    const int i = __ffs(m) - 1;
+    m &= m - 1;
+    keep_insert(kd, ki, cand[i * nth], col0 + i);
+  }
+}
+
 template <int FMT> struct TcSplit { static constexpr int S = FMT == KNN_FMT_EUCL ? 4 : 2; };
 
 template <int FMT>
@@ -428,6 +455,8 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   unsigned char* sA1 = base;
   unsigned char* sA2 = base + kTileM * kRowBytes;
   unsigned char* sB0 = base + 2 * kTileM * kRowBytes;
+  // per-thread candidate column: [32][blockDim] floats after the operand buffers
+  float* cand = (float*)(sB0 + 2 * (size_t)BT) + threadIdx.x;
   __shared__ uint64_t bar_load[2], bar_mma[2];
   __shared__ uint32_t tbase;
   __shared__ int s_fail;
@@ -557,8 +586,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
         for (int c0 = slice * NCOL; c0 < slice * NCOL + NCOL; c0 += 32) {
           float v[32];
           tmem_ld32(lane_base + c0, v);
-#pragma unroll
-          for (int i = 0; i < 32; i++) keep_insert(kd, ki, fmaf(-2.f, v[i], qn), col_node0 + c0 + i);
+          keep_chunk<true>(kd, ki, v, qn, cand, col_node0 + c0);
         }
       } else {
 #pragma unroll 1
@@ -573,8 +601,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
 #pragma unroll
             for (int i = 0; i < 32; i++) m[i] = fmaxf(m[i], fmaf(-2.f, v[i], qa));
           }
-#pragma unroll
-          for (int i = 0; i < 32; i++) keep_insert(kd, ki, m[i], col_node0 + c0 + i);
+          keep_chunk<false>(kd, ki, m, 0.f, cand, col_node0 + c0);
         }
       }
     }
@@ -619,6 +646,8 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   if (warp == 0) tmem_dealloc(tm, 512);
 }
 
+constexpr int kMergeWarps = 4;   // warps per merge CTA
+
 // ---------------------------------------------------------------------------
 // merge: certify the kept candidates and re-rank them in exact FP64
 // ---------------------------------------------------------------------------
@@ -628,11 +657,17 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
                                  const int* __restrict__ cand_i, const float* __restrict__ q_eps, SliceTab t,
                                  int metric, int k, long long* __restrict__ out_idx, double* __restrict__ out_dist,
                                  long long* __restrict__ fallback, int* __restrict__ n_fallback) {
-  const int lane = threadIdx.x & 31;
-  const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
   const float INF = __int_as_float(0x7f800000);
   const double DINF = __longlong_as_double(0x7ff0000000000000ll);
+  // per warp: the query's candidate lists (<= 64 x 16 approximate distances)
+  // and the gathered ids within tau
+  __shared__ float s_cd[kMergeWarps][64 * kKeep];
+  __shared__ int s_id[kMergeWarps][64 * kKeep];
+  float* sv = s_cd[wib];
+  int* sid = s_id[wib];
   for (long long q = warp; q < Q; q += nwarps) {
     const int m = q_mode[q];
     const long long M = mode_off[m + 1] - mode_off[m];
@@ -641,16 +676,21 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
       for (int r = lane; r < k; r += 32) { out_idx[q * k + r] = -1; out_dist[q * k + r] = DINF; }
       continue;
     }
-    // lane l holds chunks l and l + 32 (C <= 64)
+    // lane l holds chunks l and l + 32 (C <= 64); the lists are staged in
+    // shared memory with coalesced loads, so the rounds below do not wait on
+    // global memory
     const float* cd = cand_d + (size_t)q * chunks_max * kKeep;
     const int* ci = cand_i + (size_t)q * chunks_max * kKeep;
+    __syncwarp();
+    for (int x = lane; x < C * kKeep; x += 32) sv[x] = cd[x];
+    __syncwarp();
     int h0 = 0, h1 = 0;
     const int c0 = lane, c1 = lane + 32;
     // approximate k-th smallest value by k rounds of a warp argmin over list heads
     float kth = INF;
     for (int r = 0; r < k; r++) {
-      const float v0 = (c0 < C && h0 < kKeep) ? cd[c0 * kKeep + h0] : INF;
-      const float v1 = (c1 < C && h1 < kKeep) ? cd[c1 * kKeep + h1] : INF;
+      const float v0 = (c0 < C && h0 < kKeep) ? sv[c0 * kKeep + h0] : INF;
+      const float v1 = (c1 < C && h1 < kKeep) ? sv[c1 * kKeep + h1] : INF;
       float v = fminf(v0, v1);
       float b = v;
 #pragma unroll
@@ -663,8 +703,8 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
     const float tau = kth == INF ? INF : kth + 2.f * q_eps[q];
     // certified when every full list ends above tau
     bool unsafe = false;
-    if (c0 < C) unsafe |= ci[c0 * kKeep + kKeep - 1] >= 0 && !(cd[c0 * kKeep + kKeep - 1] > tau);
-    if (c1 < C) unsafe |= ci[c1 * kKeep + kKeep - 1] >= 0 && !(cd[c1 * kKeep + kKeep - 1] > tau);
+    if (c0 < C) unsafe |= ci[c0 * kKeep + kKeep - 1] >= 0 && !(sv[c0 * kKeep + kKeep - 1] > tau);
+    if (c1 < C) unsafe |= ci[c1 * kKeep + kKeep - 1] >= 0 && !(sv[c1 * kKeep + kKeep - 1] > tau);
     if (__any_sync(MRMG_FULL, unsafe)) {
       if (lane == 0) { const int s = atomicAdd(n_fallback, 1); fallback[s] = q; }
       continue;
@@ -675,14 +715,29 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
 #pragma unroll
     for (int i = 0; i < 16; i++) { td[i] = 0x7ff0000000000000ll; tix[i] = -1; }
     const double* qq = qs + q * t.D;
-    for (int cc = lane; cc < C; cc += 32)
-      for (int j = 0; j < kKeep; j++) {
-        const int id = ci[cc * kKeep + j];
-        if (id < 0 || id >= M || !(cd[cc * kKeep + j] <= tau)) continue;
-        const double* xx = nodes + (mode_off[m] + id) * t.D;
-        auto dfun = [&](int jj) { return __dsub_rn(qq[jj], xx[jj]); };
-        topk_insert<16>(td, tix, k < 16 ? k : 16, dkey(dist_of(t, metric, dfun)), id);
-      }
+    // gather the candidates within tau (a sorted prefix of each list) into
+    // one warp-wide list, then compute their FP64 distances one per lane
+    int n0 = 0, n1 = 0;
+    if (c0 < C) while (n0 < kKeep && sv[c0 * kKeep + n0] <= tau) n0++;
+    if (c1 < C) while (n1 < kKeep && sv[c1 * kKeep + n1] <= tau) n1++;
+    int mine = n0 + n1, incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(MRMG_FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int ncand = __shfl_sync(MRMG_FULL, incl, 31);
+    int w = incl - mine;
+    for (int j = 0; j < n0; j++) sid[w++] = ci[c0 * kKeep + j];
+    for (int j = 0; j < n1; j++) sid[w++] = ci[c1 * kKeep + j];
+    __syncwarp();
+    for (int x = lane; x < ncand; x += 32) {
+      const int id = sid[x];
+      if (id < 0 || id >= M) continue;
+      const double* xx = nodes + (mode_off[m] + id) * t.D;
+      auto dfun = [&](int jj) { return __dsub_rn(qq[jj], xx[jj]); };
+      topk_insert<16>(td, tix, k < 16 ? k : 16, dkey(dist_of(t, metric, dfun)), id);
+    }
     int head = 0;
     for (int r = 0; r < k; r++) {
       long long hd = 0x7ff0000000000000ll;
@@ -875,7 +930,10 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   const int NT = s->dev.NT;
   // at least 120 KB of shared memory: one CTA per SM, so two CTAs never wait
   // on each other for the 512 tensor-memory columns each allocates
-  const size_t smem = std::max<size_t>(1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes, 120 * 1024);
+  const int nthreads = 128 * (s->dev.fmt == KNN_FMT_EUCL ? TcSplit<KNN_FMT_EUCL>::S : TcSplit<KNN_FMT_AGENT>::S);
+  const size_t smem = std::max<size_t>(1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes +
+                                           32 * sizeof(float) * (size_t)nthreads,
+                                       120 * 1024);
   if (!items.empty()) {
     if (s->dev.fmt == KNN_FMT_EUCL) {
       cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_EUCL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -890,7 +948,7 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
     if (e != cudaSuccess) return e;
   }
   const int mgrid = (int)std::min<long long>((Q + 3) / 4, (long long)num_sms * 16);
-  knn_merge_kernel<<<std::max(mgrid, 1), 128, 0, st>>>(d_qs, Q, d_qmode, s->nodes, s->dev.mode_off, d_mch, chunks_max,
+  knn_merge_kernel<<<std::max(mgrid, 1), 32 * kMergeWarps, 0, st>>>(d_qs, Q, d_qmode, s->nodes, s->dev.mode_off, d_mch, chunks_max,
                                                        d_cd, d_ci, d_eps, s->slices, s->metric, k, d_idx, d_dist, d_fb,
                                                        d_ctr);
   e = cudaGetLastError();
