@@ -64,66 +64,89 @@ __device__ __forceinline__ float rcpa(float x) { float y; asm("rcp.approx.ftz.f3
 // e = 2^-|x2|:  softplus(beta (margin - d)) = ln 2 * (max(x2, 0) + log2(1 + e))
 // and sigmoid(beta (margin - d)) = 1 / (1 + e) for x2 >= 0, e / (1 + e) else.
 // K folds the constant part: x2 = K - beta log2(e) * (distance).
-struct PairAcc {
-  float ps;            // sum of max(x2, 0) + log2(1 + e)
-  float gx, gy, gz;    // dcost / dcentre
+//
+// A task's two spheres are evaluated together in packed FP32x2 arithmetic
+// (.x = first sphere, .y = second): one add / multiply / FMA instruction does
+// both; min/max, abs and the special functions stay per component.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+
+struct PairAcc2 {
+  float2 ps;           // sums of max(x2, 0) + log2(1 + e)
+  float2 gx, gy, gz;   // dcost / dcentre
 };
 
+// softplus (base 2) of x2 into ps; sigmoid-based dterm/d(distance) into w
 template <bool COST, bool GRAD>
-__device__ __forceinline__ void box_pair(float cx, float cy, float cz, const float4& bc, const float4& bh, float bl,
-                                         float K, float inv_scale, PairAcc& acc) {
-  const float dx = cx - bc.x, dy = cy - bc.y, dz = cz - bc.z;
-  const float ax = fabsf(dx) - bh.x, ay = fabsf(dy) - bh.y, az = fabsf(dz) - bh.z;
-  const float ux = fmaxf(ax, 0.f), uy = fmaxf(ay, 0.f), uz = fmaxf(az, 0.f);
-  const float u2 = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
-  const float mx = fmaxf(ax, fmaxf(ay, az));
-  if (!GRAD) {
-    // signed distance of the box: |max(q, 0)| + min(max_k q_k, 0)
-    const float x2 = fmaf(-bl, sqrta(u2) + fminf(mx, 0.f), K);
-    const float e = ex2a(-fabsf(x2));
-    acc.ps += fmaxf(x2, 0.f) + lg2a(1.f + e);
-  } else {
-    const float inv = rsqa(fmaxf(u2, 1e-30f));
-    const bool outside = mx > 0.f;
-    const float x2 = fmaf(-bl, outside ? u2 * inv : mx, K);
-    const float e = ex2a(-fabsf(x2));
-    if (COST) acc.ps += fmaxf(x2, 0.f) + lg2a(1.f + e);
-    const float r = rcpa(1.f + e);
-    const float w = -(x2 >= 0.f ? r : e * r) * inv_scale;   // dterm / d(distance)
-    // d(distance)/dc: the unit vector of max(q, 0) outside, the axis of the
-    // largest q inside; both with the signs of c - centre
-    float sx, sy, sz;
-    if (outside) {
-      sx = ux * inv; sy = uy * inv; sz = uz * inv;
-    } else {
-      const bool bx = ax >= ay && ax >= az, by = !bx && ay >= az;
-      sx = bx ? 1.f : 0.f; sy = by ? 1.f : 0.f; sz = (!bx && !by) ? 1.f : 0.f;
-    }
-    acc.gx = fmaf(w, copysignf(sx, dx), acc.gx);
-    acc.gy = fmaf(w, copysignf(sy, dy), acc.gy);
-    acc.gz = fmaf(w, copysignf(sz, dz), acc.gz);
+__device__ __forceinline__ void term2(float2 x2, float inv_scale, float2& ps, float2& w) {
+  const float2 e = make_float2(ex2a(-fabsf(x2.x)), ex2a(-fabsf(x2.y)));
+  const float2 ope = add2(e, bc2(1.f));
+  if (COST)
+    ps = add2(ps, add2(make_float2(fmaxf(x2.x, 0.f), fmaxf(x2.y, 0.f)), make_float2(lg2a(ope.x), lg2a(ope.y))));
+  if (GRAD) {
+    const float2 r = make_float2(rcpa(ope.x), rcpa(ope.y));
+    const float2 er = mul2(e, r);
+    w = mul2(make_float2(x2.x >= 0.f ? r.x : er.x, x2.y >= 0.f ? r.y : er.y), bc2(-inv_scale));
   }
 }
 
 template <bool COST, bool GRAD>
-__device__ __forceinline__ void sphere_pair(float cx, float cy, float cz, float jx, float jy, float jz, float bl, float K,
-                                            float inv_scale, PairAcc& acc) {
-  const float vx = cx - jx, vy = cy - jy, vz = cz - jz;
-  const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+__device__ __forceinline__ void box_pair2(float2 cx, float2 cy, float2 cz, const float4& bc, const float4& bh,
+                                          float2 nbl, float2 K, float inv_scale, PairAcc2& acc) {
+  const float2 dx = add2(cx, bc2(-bc.x)), dy = add2(cy, bc2(-bc.y)), dz = add2(cz, bc2(-bc.z));
+  const float2 ax = make_float2(fabsf(dx.x) - bh.x, fabsf(dx.y) - bh.x);
+  const float2 ay = make_float2(fabsf(dy.x) - bh.y, fabsf(dy.y) - bh.y);
+  const float2 az = make_float2(fabsf(dz.x) - bh.z, fabsf(dz.y) - bh.z);
+  const float2 ux = make_float2(fmaxf(ax.x, 0.f), fmaxf(ax.y, 0.f));
+  const float2 uy = make_float2(fmaxf(ay.x, 0.f), fmaxf(ay.y, 0.f));
+  const float2 uz = make_float2(fmaxf(az.x, 0.f), fmaxf(az.y, 0.f));
+  const float2 u2 = fma2(ux, ux, fma2(uy, uy, mul2(uz, uz)));
+  const float2 mx = make_float2(fmaxf(ax.x, fmaxf(ay.x, az.x)), fmaxf(ax.y, fmaxf(ay.y, az.y)));
+  float2 w;
   if (!GRAD) {
-    const float x2 = fmaf(-bl, sqrta(d2), K);
-    const float e = ex2a(-fabsf(x2));
-    acc.ps += fmaxf(x2, 0.f) + lg2a(1.f + e);
+    // signed distance of the box: |max(q, 0)| + min(max_k q_k, 0)
+    const float2 sdf = add2(make_float2(sqrta(u2.x), sqrta(u2.y)), make_float2(fminf(mx.x, 0.f), fminf(mx.y, 0.f)));
+    term2<COST, false>(fma2(nbl, sdf, K), inv_scale, acc.ps, w);
   } else {
-    const float inv = rsqa(fmaxf(d2, 1e-30f));
-    const float x2 = fmaf(-bl, d2 * inv, K);
-    const float e = ex2a(-fabsf(x2));
-    if (COST) acc.ps += fmaxf(x2, 0.f) + lg2a(1.f + e);
-    const float r = rcpa(1.f + e);
-    const float f = -(x2 >= 0.f ? r : e * r) * inv_scale * inv;
-    acc.gx = fmaf(f, vx, acc.gx);
-    acc.gy = fmaf(f, vy, acc.gy);
-    acc.gz = fmaf(f, vz, acc.gz);
+    const float2 inv = make_float2(rsqa(fmaxf(u2.x, 1e-30f)), rsqa(fmaxf(u2.y, 1e-30f)));
+    const float2 ui = mul2(u2, inv);
+    const bool ox = mx.x > 0.f, oy = mx.y > 0.f;
+    const float2 sdf = make_float2(ox ? ui.x : mx.x, oy ? ui.y : mx.y);
+    term2<COST, true>(fma2(nbl, sdf, K), inv_scale, acc.ps, w);
+    // d(distance)/dc: the unit vector of max(q, 0) outside, the axis of the
+    // largest q inside; both with the signs of c - centre
+    float2 sx = mul2(ux, inv), sy = mul2(uy, inv), sz = mul2(uz, inv);
+    if (!ox) {
+      const bool bx = ax.x >= ay.x && ax.x >= az.x, by = !bx && ay.x >= az.x;
+      sx.x = bx ? 1.f : 0.f; sy.x = by ? 1.f : 0.f; sz.x = (!bx && !by) ? 1.f : 0.f;
+    }
+    if (!oy) {
+      const bool bx = ax.y >= ay.y && ax.y >= az.y, by = !bx && ay.y >= az.y;
+      sx.y = bx ? 1.f : 0.f; sy.y = by ? 1.f : 0.f; sz.y = (!bx && !by) ? 1.f : 0.f;
+    }
+    acc.gx = fma2(w, make_float2(copysignf(sx.x, dx.x), copysignf(sx.y, dx.y)), acc.gx);
+    acc.gy = fma2(w, make_float2(copysignf(sy.x, dy.x), copysignf(sy.y, dy.y)), acc.gy);
+    acc.gz = fma2(w, make_float2(copysignf(sz.x, dz.x), copysignf(sz.y, dz.y)), acc.gz);
+  }
+}
+
+template <bool COST, bool GRAD>
+__device__ __forceinline__ void sphere_pair2(float2 cx, float2 cy, float2 cz, float jx, float jy, float jz, float2 nbl,
+                                             float2 K, float inv_scale, PairAcc2& acc) {
+  const float2 vx = add2(cx, bc2(-jx)), vy = add2(cy, bc2(-jy)), vz = add2(cz, bc2(-jz));
+  const float2 d2 = fma2(vx, vx, fma2(vy, vy, mul2(vz, vz)));
+  float2 w;
+  if (!GRAD) {
+    term2<COST, false>(fma2(nbl, make_float2(sqrta(d2.x), sqrta(d2.y)), K), inv_scale, acc.ps, w);
+  } else {
+    const float2 inv = make_float2(rsqa(fmaxf(d2.x, 1e-30f)), rsqa(fmaxf(d2.y, 1e-30f)));
+    term2<COST, true>(fma2(nbl, mul2(d2, inv), K), inv_scale, acc.ps, w);
+    const float2 f = mul2(w, inv);
+    acc.gx = fma2(f, vx, acc.gx);
+    acc.gy = fma2(f, vy, acc.gy);
+    acc.gz = fma2(f, vz, acc.gz);
   }
 }
 
@@ -248,41 +271,34 @@ __global__ void __launch_bounds__(512, 1)
     const int4 task = tasks[tk];   // sphere, second sphere (-1: none), robot's first sphere, next robot's first
     const bool two = task.y >= 0;
     const int i0 = task.x, i1 = two ? task.y : task.x;
-    const float c0x = C[(3 * i0) * kSeg + lane], c0y = C[(3 * i0 + 1) * kSeg + lane], c0z = C[(3 * i0 + 2) * kSeg + lane];
-    const float c1x = C[(3 * i1) * kSeg + lane], c1y = C[(3 * i1 + 1) * kSeg + lane], c1z = C[(3 * i1 + 2) * kSeg + lane];
-    const float K0 = fmaf(bl, sph[i0].w, blm), K1 = fmaf(bl, sph[i1].w, blm);
-    PairAcc a0{0.f, 0.f, 0.f, 0.f}, a1{0.f, 0.f, 0.f, 0.f};
+    const float2 cx = make_float2(C[(3 * i0) * kSeg + lane], C[(3 * i1) * kSeg + lane]);
+    const float2 cy = make_float2(C[(3 * i0 + 1) * kSeg + lane], C[(3 * i1 + 1) * kSeg + lane]);
+    const float2 cz = make_float2(C[(3 * i0 + 2) * kSeg + lane], C[(3 * i1 + 2) * kSeg + lane]);
+    const float2 K = make_float2(fmaf(bl, sph[i0].w, blm), fmaf(bl, sph[i1].w, blm));
+    const float2 nbl = bc2(-bl);
+    PairAcc2 a{bc2(0.f), bc2(0.f), bc2(0.f), bc2(0.f)};
 #pragma unroll 2
-    for (int b = 0; b < B; b++) {
-      const float4 bc = box[2 * b], bh = box[2 * b + 1];
-      box_pair<COST, GRAD>(c0x, c0y, c0z, bc, bh, bl, K0, pp.inv_scale, a0);
-      box_pair<COST, GRAD>(c1x, c1y, c1z, bc, bh, bl, K1, pp.inv_scale, a1);
-    }
+    for (int b = 0; b < B; b++)
+      box_pair2<COST, GRAD>(cx, cy, cz, box[2 * b], box[2 * b + 1], nbl, K, pp.inv_scale, a);
 #pragma unroll 2
-    for (int j = task.w; j < S; j++) {
-      const float jx = C[(3 * j) * kSeg + lane], jy = C[(3 * j + 1) * kSeg + lane], jz = C[(3 * j + 2) * kSeg + lane];
-      const float bj = br[j];
-      sphere_pair<COST, GRAD>(c0x, c0y, c0z, jx, jy, jz, bl, K0 + bj, pp.inv_scale, a0);
-      sphere_pair<COST, GRAD>(c1x, c1y, c1z, jx, jy, jz, bl, K1 + bj, pp.inv_scale, a1);
-    }
+    for (int j = task.w; j < S; j++)
+      sphere_pair2<COST, GRAD>(cx, cy, cz, C[(3 * j) * kSeg + lane], C[(3 * j + 1) * kSeg + lane],
+                               C[(3 * j + 2) * kSeg + lane], nbl, add2(K, bc2(br[j])), pp.inv_scale, a);
     if (GRAD) {
 #pragma unroll 2
-      for (int j = 0; j < task.z; j++) {
-        const float jx = C[(3 * j) * kSeg + lane], jy = C[(3 * j + 1) * kSeg + lane], jz = C[(3 * j + 2) * kSeg + lane];
-        const float bj = br[j];
-        sphere_pair<false, true>(c0x, c0y, c0z, jx, jy, jz, bl, K0 + bj, pp.inv_scale, a0);
-        sphere_pair<false, true>(c1x, c1y, c1z, jx, jy, jz, bl, K1 + bj, pp.inv_scale, a1);
-      }
-      Gs[(3 * i0) * kSeg + lane] = a0.gx;
-      Gs[(3 * i0 + 1) * kSeg + lane] = a0.gy;
-      Gs[(3 * i0 + 2) * kSeg + lane] = a0.gz;
+      for (int j = 0; j < task.z; j++)
+        sphere_pair2<false, true>(cx, cy, cz, C[(3 * j) * kSeg + lane], C[(3 * j + 1) * kSeg + lane],
+                                  C[(3 * j + 2) * kSeg + lane], nbl, add2(K, bc2(br[j])), pp.inv_scale, a);
+      Gs[(3 * i0) * kSeg + lane] = a.gx.x;
+      Gs[(3 * i0 + 1) * kSeg + lane] = a.gy.x;
+      Gs[(3 * i0 + 2) * kSeg + lane] = a.gz.x;
       if (two) {
-        Gs[(3 * i1) * kSeg + lane] = a1.gx;
-        Gs[(3 * i1 + 1) * kSeg + lane] = a1.gy;
-        Gs[(3 * i1 + 2) * kSeg + lane] = a1.gz;
+        Gs[(3 * i1) * kSeg + lane] = a.gx.y;
+        Gs[(3 * i1 + 1) * kSeg + lane] = a.gy.y;
+        Gs[(3 * i1 + 2) * kSeg + lane] = a.gz.y;
       }
     }
-    if (COST) acc2(acc_h, acc_l, two ? a0.ps + a1.ps : a0.ps);
+    if (COST) acc2(acc_h, acc_l, two ? a.ps.x + a.ps.y : a.ps.x);
   }
   if (COST) {
     part[warp * kSeg + lane] = acc_h;
