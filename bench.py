@@ -555,6 +555,21 @@ def bench_serving(orc, steps: int = 24, warmup: int = 3) -> dict:
         edges += res.n_edges
     wall = time.perf_counter() - t0
     lat = b.latency_percentiles()
+    # zero-copy submission: the instances write their requests straight into
+    # the pinned staging views (untimed: that is request production); the
+    # latency runs from submit to verdicts on the host
+    b.latencies.clear()
+    b.device_ms.clear()
+    for i in range(steps):
+        reqs = pool[i % len(pool)]
+        slots = b.prepare([(len(r["configs"]), len(r["q1"])) for r in reqs])
+        for k, r in enumerate(reqs):
+            slots.configs[k][:] = r["configs"]
+            slots.q1[k][:] = r["q1"]
+            slots.q2[k][:] = r["q2"]
+            slots.N[k][:] = r["N"]
+        b.submit(slots, t0=time.perf_counter())
+    lat_zc = b.latency_percentiles()
     # verdicts of two instances of the first step against the oracle
     res = b.step(pool[0])
     o = orc.OracleScene(sc)
@@ -571,7 +586,7 @@ def bench_serving(orc, steps: int = 24, warmup: int = 3) -> dict:
         "workload": "8 mobile manipulators (planar base + 6-DoF arm, 72-D, 304 spheres), 200 boxes in a 6x6x2 m room; "
                     "64 instances/step, each 100-20,000 configs and 10-5,000 edges (N 5..800)",
         "steps": steps, "configs_per_step": cfgs / steps, "edges_per_step": edges / steps,
-        "latency": lat, "items_per_s": items / wall, "configs_per_s": cfgs / wall, "edges_per_s": edges / wall,
+        "latency": lat, "latency_zero_copy": lat_zc, "items_per_s": items / wall, "configs_per_s": cfgs / wall, "edges_per_s": edges / wall,
         "graph_launches_per_step": 1, "buckets": [list(k) for k in b.graphs],
         "autotune": tune, "verdict_mismatches_sampled": mism,
         "cpu_baseline": {"value": cpu_items / cpu_s, "unit": "items/s (configs + edges)", "cores": orc.num_threads(),

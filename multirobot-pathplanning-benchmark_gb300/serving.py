@@ -109,6 +109,21 @@ class _StepGraph:
 
 
 @dataclass
+class StepSlots:
+    """Per-instance views into one bucket's pinned staging buffers: an
+    instance writes its configurations into ``configs[k]`` and its edges into
+    ``q1[k]`` / ``q2[k]`` / ``N[k]`` (no further host copy)."""
+    graph: object
+    configs: list
+    q1: list
+    q2: list
+    N: list
+    n_configs: int
+    n_edges: int
+    t0: float = 0.0
+
+
+@dataclass
 class StepResult:
     config_free: list          # per instance: uint8 verdicts of its configurations
     edge_free: list            # per instance: uint8 verdicts of its edges
@@ -147,6 +162,50 @@ class ServingBatcher:
             g = _StepGraph(self.scene, key[0], key[1], self.incl)
             self.graphs[key] = g
         return g
+
+    def prepare(self, sizes: list) -> StepSlots:
+        """Staging views for one step: ``sizes`` holds (configurations, edges)
+        per instance.  Fill the views (explicit N for every edge), then call
+        ``submit``; the views stay valid until the next ``prepare`` of the
+        same capacity bucket."""
+        nc = int(sum(int(a) for a, _ in sizes))
+        ne = int(sum(int(b) for _, b in sizes))
+        g = self._graph(nc, ne)
+        cfg_h, e1_h, e2_h, N_h = g.cfg_pin.numpy(), g.e1_pin.numpy(), g.e2_pin.numpy(), g.N_pin.numpy()
+        cv, q1v, q2v, nv = [], [], [], []
+        oc = oe = 0
+        for a, b in sizes:
+            a, b = int(a), int(b)
+            cv.append(cfg_h[oc:oc + a])
+            q1v.append(e1_h[oe:oe + b])
+            q2v.append(e2_h[oe:oe + b])
+            nv.append(N_h[g.ccap + oe:g.ccap + oe + b])
+            oc += a
+            oe += b
+        return StepSlots(g, cv, q1v, q2v, nv, nc, ne, time.perf_counter())
+
+    def submit(self, slots: StepSlots, t0=None) -> StepResult:
+        """Launch a prepared step and split its verdicts per instance; the
+        latency is counted from ``t0`` (default: the time of ``prepare``)."""
+        g, nc, ne = slots.graph, slots.n_configs, slots.n_edges
+        N_h = g.N_pin.numpy()
+        N_h[:nc] = 3
+        N_h[nc:g.ccap] = 2
+        N_h[g.ccap + ne:] = 2
+        out = g.run()
+        self.device_ms.append(g.device_ms)
+        cf, ef = [], []
+        o = 0
+        for c in slots.configs:
+            cf.append(out[o:o + len(c)].copy())
+            o += len(c)
+        o = g.ccap
+        for a in slots.q1:
+            ef.append(out[o:o + len(a)].copy())
+            o += len(a)
+        lat = time.perf_counter() - (slots.t0 if t0 is None else t0)
+        self.latencies.append(lat)
+        return StepResult(cf, ef, lat, g.device_ms, nc, ne, (g.ccap, g.ecap))
 
     def step(self, requests: list) -> StepResult:
         t0 = time.perf_counter()

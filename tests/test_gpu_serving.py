@@ -90,3 +90,25 @@ def test_mismatched_edges_rejected(gpu):
         b.step([dict(q1=np.zeros((3, 28), np.float32), q2=np.zeros((2, 28), np.float32))])
     with pytest.raises(ValueError):
         b.step([dict(q1=np.zeros((3, 28), np.float32), q2=np.zeros((3, 28), np.float32), N=[5, 5])])
+
+
+def test_zero_copy_prepare_submit(gpu, oracle):
+    """Requests written straight into the staging views give the same
+    verdicts as the copying path."""
+    scenes, col, srv = pkg("scenes"), pkg("collision"), pkg("serving")
+    sc = scenes.make_mobile_scene(0)
+    s = col.Gb300Scene(sc)
+    orc = oracle.OracleScene(sc)
+    b = srv.ServingBatcher(s, config_quantum=1024, edge_quantum=256)
+    reqs = _requests(sc, 5, n=4)
+    slots = b.prepare([(len(r["configs"]), len(r["q1"])) for r in reqs])
+    for k, r in enumerate(reqs):
+        slots.configs[k][:] = r["configs"]
+        slots.q1[k][:] = r["q1"]
+        slots.q2[k][:] = r["q2"]
+        slots.N[k][:] = r["N"]
+    res = b.submit(slots)
+    _check(orc, reqs, res)
+    res2 = b.step(reqs)
+    for a, c in zip(res.config_free + res.edge_free, res2.config_free + res2.edge_free):
+        assert np.array_equal(a, c)
