@@ -342,6 +342,19 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   d.R = R; d.D = D; d.G = G; d.SPG = SPG; d.B = B; d.NP = (int)pairs.size();
   d.delta = f32_up(delta);
   d.xy_max = (float)xy_max;
+  {
+    // |centre| <= cmax for every configuration the FP32 path accepts (planar
+    // bases are limited to |x|, |y| <= xy_max); the pair filter's FP32 value
+    // s_a + s_b - 2 a.b (s = |c|^2 - 2 r^2) and the direct FP32
+    // |a - b|^2 - (r_a + r_b)^2 each lie within 24 * 2^-24 * (2 cmax^2 +
+    // 4 rmax^2) / 2 of their exact values (a generous multiple of the
+    // rounding of their products and sums)
+    double rmax = 0.0;
+    for (int i = 0; i < S; i++) rmax = std::max(rmax, h_sphere_radius[i]);
+    rmax += delta;
+    const double cmax = reach_max + rmax;
+    d.pair_eps = f32_up(24.0 * std::ldexp(1.0, -24) * (2.0 * cmax * cmax + 4.0 * rmax * rmax));
+  }
   for (int r = 0; r < R; r++) { d.q_off[r] = h_q_offset[r]; d.base_kind[r] = h_base_kind[r]; d.nl[r] = h_n_links[r]; }
   d.prismatic[0] = prism[0]; d.prismatic[1] = prism[1]; d.prismatic[2] = prism[2];
 

@@ -59,7 +59,7 @@ __host__ __device__ inline size_t table_bytes(const ArmDev& s) {
 // per-warp FP32 work area: joint cos/sin, planar translations, sphere table
 __host__ __device__ inline size_t warp32_bytes(const ArmDev& s) {
   return align16(sizeof(float2) * s.D) + align16(sizeof(float) * s.D) +
-         align16(sizeof(float4) * s.G * s.SPG);
+         align16(sizeof(float4) * s.G * s.SPG) + align16(sizeof(float) * s.G * s.SPG);
 }
 
 // per-warp FP64 work area for pass 2: joint values, cos/sin, sphere centres
@@ -288,6 +288,11 @@ struct EdgeSource64 {       // pass 2: q1 + dir * i exactly as the reference (FP
   }
 };
 
+// the warp's pair-filter norms s = |c|^2 - r'^2, stored right after its sphere table
+__device__ __forceinline__ float* wss_of(const ArmDev& s, float4* wsph) {
+  return (float*)((unsigned char*)wsph + align16(sizeof(float4) * s.G * s.SPG));
+}
+
 // ---------------------------------------------------------------------------
 // Warp evaluation of one configuration.
 // Returns V_COLLIDE, V_FREE, or (pass 1 only) V_PENDING; warp-uniform.
@@ -428,31 +433,47 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
     }
   }
 
-  // --- spheres of different robots
+  // --- spheres of different robots.  Filter: since (r_a + r_b)^2 <= 2 r_a^2 +
+  // 2 r_b^2 (equal for equal radii), |a - b|^2 - (r_a + r_b)^2 >= s_a + s_b - 2 a.b
+  // with s = |c|^2 - 2 r^2 per sphere (r = radius + delta): three products
+  // per pair.  Pairs with a filter value within its FP32 error bound go to the
+  // direct test below, which decides exactly as before.
   const float d4 = 4.f * s.delta;
+  float* wss = wss_of(s, wsph);
+#pragma unroll
+  for (int u = 0; u < GPL; u++) {
+    const int g = lane + 32 * u;
+    if (g < s.G)
+#pragma unroll
+      for (int v = 0; v < SPG; v++) {
+        const float4 c = wsph[g * SPG + v];
+        wss[g * SPG + v] = fmaf(c.x, c.x, fmaf(c.y, c.y, fmaf(c.z, c.z, -2.f * c.w * c.w)));
+      }
+  }
+  __syncwarp();
   for (int base = 0; base < s.NP; base += 32) {
     const int pi = base + lane;
     float umin = 3.0e38f;
     uint32_t pr = 0;
     if (pi < s.NP) {
       pr = t.pairs[pi];
-      const float4* A = wsph + (pr & 0xffff) * SPG;
-      const float4* Bq = wsph + (pr >> 16) * SPG;
-      float4 a[SPG];
+      const int sa0 = (pr & 0xffff) * SPG, sb0 = (pr >> 16) * SPG;
+      float4 a[SPG];   // (-2 x, -2 y, -2 z, s)
 #pragma unroll
-      for (int v = 0; v < SPG; v++) a[v] = A[v];
+      for (int v = 0; v < SPG; v++) {
+        const float4 c = wsph[sa0 + v];
+        a[v] = make_float4(-2.f * c.x, -2.f * c.y, -2.f * c.z, wss[sa0 + v]);
+      }
 #pragma unroll
       for (int w = 0; w < SPG; w++) {
-        const float4 bq = Bq[w];
+        const float4 bq = wsph[sb0 + w];
+        const float sb = wss[sb0 + w];
 #pragma unroll
-        for (int v = 0; v < SPG; v++) {
-          const float dx = a[v].x - bq.x, dy = a[v].y - bq.y, dz = a[v].z - bq.z;
-          const float W = a[v].w + bq.w;
-          umin = fminf(umin, fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -W * W))));
-        }
+        for (int v = 0; v < SPG; v++)
+          umin = fminf(umin, fmaf(a[v].x, bq.x, fmaf(a[v].y, bq.y, fmaf(a[v].z, bq.z, a[v].w + sb))));
       }
     }
-    if (__any_sync(MRMG_FULL, umin <= 0.f)) {
+    if (__any_sync(MRMG_FULL, umin <= s.pair_eps)) {
       bool coll = false;
       if (umin <= 0.f) {
         const int ga = pr & 0xffff, gb = pr >> 16;
@@ -496,6 +517,7 @@ __device__ __forceinline__ void warp_areas(const ArmDev& s, unsigned char* smem_
   *wcs = (float2*)p; p += align16(sizeof(float2) * s.D);
   *wqv = (float*)p; p += align16(sizeof(float) * s.D);
   *wsph = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
+  p += align16(sizeof(float) * s.G * s.SPG);   // pair-filter norms (after wsph, see wss_of)
   *w64 = (double*)p;
 }
 
@@ -628,7 +650,7 @@ __device__ __forceinline__ bool edge_N(const void* q1, const void* q2, int dtype
 }
 
 template <int GPL, int SPG, bool RESOLVE>
-__global__ void __launch_bounds__(256) arm_edges_kernel(ArmDev s, const void* q1, const void* q2, int dtype,
+__global__ void __launch_bounds__(256, RESOLVE ? 1 : 4) arm_edges_kernel(ArmDev s, const void* q1, const void* q2, int dtype,
                                                         long long n, double res, int incl,
                                                         const long long* Np, long long N_start,
                                                         long long N_max, uint8_t* out, int* ctr,

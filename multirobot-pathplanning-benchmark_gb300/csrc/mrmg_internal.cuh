@@ -36,6 +36,7 @@ struct ArmDev {
   int R, D, G, SPG, B, NP;
   float delta;      // FP32 re-check band (metres)
   float xy_max;     // planar base |x|,|y| beyond this -> exact path
+  float pair_eps;   // FP32 error bound (m^2) of the pair filter s_a + s_b - 2 a.b
   int q_off[kMaxRobots], base_kind[kMaxRobots], nl[kMaxRobots];
   uint32_t prismatic[3];   // bit j: joint j is a planar-base translation
   // exact FP64 tables (global memory)
