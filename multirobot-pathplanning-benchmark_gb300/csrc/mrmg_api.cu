@@ -408,6 +408,36 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   blk.add(band32.data(), band32.size(), &d.band32);
   blk.add(box32.data(), box32.size(), &d.box32);
   blk.add(grp.data(), grp.size(), &d.grp);
+  // group bounds: the centre of the group's local sphere offsets and a radius
+  // over |offset - centre| + r, widened by 4 delta (FP32 error of the group
+  // centre and of each sphere centre, plus rounding of the bound test)
+  std::vector<float4> gbs(G);
+  for (int g = 0; g < G; g++) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    int cnt = 0;
+    for (int v = 0; v < SPG; v++) {
+      const int i = slot_sphere[g * SPG + v];
+      if (i < 0) continue;
+      cnt++;
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::min(lo[k], h_sphere_local[3 * i + k]);
+        hi[k] = std::max(hi[k], h_sphere_local[3 * i + k]);
+      }
+    }
+    if (!cnt) { gbs[g] = make_float4(0.f, 0.f, 0.f, -1.f); continue; }
+    double c[3], rad = 0.0;
+    for (int k = 0; k < 3; k++) c[k] = 0.5 * (lo[k] + hi[k]);
+    for (int v = 0; v < SPG; v++) {
+      const int i = slot_sphere[g * SPG + v];
+      if (i < 0) continue;
+      double d2 = 0.0;
+      for (int k = 0; k < 3; k++) d2 += (h_sphere_local[3 * i + k] - c[k]) * (h_sphere_local[3 * i + k] - c[k]);
+      rad = std::max(rad, std::sqrt(d2) + h_sphere_radius[i]);
+    }
+    rad += 4.0 * delta;
+    gbs[g] = make_float4((float)c[0], (float)c[1], (float)c[2], f32_up(rad * rad * (1.0 + 1e-6)));
+  }
+  blk.add(gbs.data(), gbs.size(), &d.gbs32);
   blk.add(pairs.data(), pairs.size(), &d.pairs);
   // penetration-cost tables: real spheres in slot order (robot, then frame)
   std::vector<float4> pen_sph, pen_box(2 * B);

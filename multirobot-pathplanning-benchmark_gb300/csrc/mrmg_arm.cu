@@ -39,6 +39,7 @@ struct ArmSmem {
   float4* sph;      // [G*SPG]
   float4* band;     // [G*SPG]
   int* grp;         // [G]
+  float4* gbs;      // [G] group bounds
   uint32_t* pairs;  // [NP]
   uint32_t prismatic[3];
 };
@@ -52,6 +53,7 @@ __host__ __device__ inline size_t table_bytes(const ArmDev& s) {
   b += align16(sizeof(float4) * s.R * kMaxLinks);
   b += align16(sizeof(float4) * s.G * s.SPG) * 2;
   b += align16(sizeof(int) * s.G);
+  b += align16(sizeof(float4) * s.G);
   b += align16(sizeof(uint32_t) * s.NP);
   return b;
 }
@@ -76,6 +78,7 @@ __device__ void stage_tables(const ArmDev& s, unsigned char* base, ArmSmem* t) {
   t->sph = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
   t->band = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
   t->grp = (int*)p; p += align16(sizeof(int) * s.G);
+  t->gbs = (float4*)p; p += align16(sizeof(float4) * s.G);
   t->pairs = (uint32_t*)p;
   for (int i = threadIdx.x; i < s.B * 2; i += blockDim.x) t->box[i] = s.box32[i];
   for (int i = threadIdx.x; i < s.R * 3; i += blockDim.x) t->base[i] = s.base32[i];
@@ -84,7 +87,10 @@ __device__ void stage_tables(const ArmDev& s, unsigned char* base, ArmSmem* t) {
     t->sph[i] = s.sph32[i];
     t->band[i] = s.band32[i];
   }
-  for (int i = threadIdx.x; i < s.G; i += blockDim.x) t->grp[i] = s.grp[i];
+  for (int i = threadIdx.x; i < s.G; i += blockDim.x) {
+    t->grp[i] = s.grp[i];
+    t->gbs[i] = s.gbs32[i];
+  }
   for (int i = threadIdx.x; i < s.NP; i += blockDim.x) t->pairs[i] = s.pairs[i];
   t->prismatic[0] = s.prismatic[0];
   t->prismatic[1] = s.prismatic[1];
@@ -359,8 +365,9 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
     if (!all_ok) return exact_all_collide(s, wc64, lane) ? V_COLLIDE : V_FREE;
   }
 
-  // --- FP32 chain + sphere centres of the owned groups
+  // --- FP32 chain + sphere centres (and group bound centres) of the owned groups
   float cx[GPL][SPG], cy[GPL][SPG], cz[GPL][SPG], rh[GPL][SPG];
+  float gb[GPL][4];
 #pragma unroll
   for (int u = 0; u < GPL; u++) {
     const int g = lane + 32 * u;
@@ -368,6 +375,11 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
       const int gi = t.grp[g];
       float R[9], p[3];
       chain32(s, t, wcs, wqv, gi & 0xff, gi >> 8, R, p);
+      const float4 lb = t.gbs[g];
+      gb[u][0] = p[0] + (R[0] * lb.x + R[1] * lb.y + R[2] * lb.z);
+      gb[u][1] = p[1] + (R[3] * lb.x + R[4] * lb.y + R[5] * lb.z);
+      gb[u][2] = p[2] + (R[6] * lb.x + R[7] * lb.y + R[8] * lb.z);
+      gb[u][3] = lb.w;
 #pragma unroll
       for (int v = 0; v < SPG; v++) {
         const float4 l = t.sph[g * SPG + v];
@@ -384,6 +396,7 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
       for (int v = 0; v < SPG; v++) {
         cx[u][v] = kFar * (float)(200 + lane); cy[u][v] = cx[u][v]; cz[u][v] = 0.f; rh[u][v] = -1.f;
       }
+      gb[u][0] = kFar * (float)(200 + lane); gb[u][1] = gb[u][0]; gb[u][2] = 0.f; gb[u][3] = -1.f;
     }
   }
   __syncwarp();
@@ -394,14 +407,21 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
     const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
     float umin = 3.0e38f;
 #pragma unroll
-    for (int u = 0; u < GPL; u++)
+    for (int u = 0; u < GPL; u++) {
+      // the group's bound first: its spheres are tested only if it reaches the box
+      const float gx = fmaxf(fabsf(gb[u][0] - bc.x) - bh.x, 0.f);
+      const float gy = fmaxf(fabsf(gb[u][1] - bc.y) - bh.y, 0.f);
+      const float gz = fmaxf(fabsf(gb[u][2] - bc.z) - bh.z, 0.f);
+      if (fmaf(gz, gz, fmaf(gy, gy, fmaf(gx, gx, -gb[u][3]))) <= 0.f) {
 #pragma unroll
-      for (int v = 0; v < SPG; v++) {
-        const float ex = fmaxf(fabsf(cx[u][v] - bc.x) - bh.x, 0.f);
-        const float ey = fmaxf(fabsf(cy[u][v] - bc.y) - bh.y, 0.f);
-        const float ez = fmaxf(fabsf(cz[u][v] - bc.z) - bh.z, 0.f);
-        umin = fminf(umin, fmaf(ez, ez, fmaf(ey, ey, fmaf(ex, ex, -rh[u][v]))));
+        for (int v = 0; v < SPG; v++) {
+          const float ex = fmaxf(fabsf(cx[u][v] - bc.x) - bh.x, 0.f);
+          const float ey = fmaxf(fabsf(cy[u][v] - bc.y) - bh.y, 0.f);
+          const float ez = fmaxf(fabsf(cz[u][v] - bc.z) - bh.z, 0.f);
+          umin = fminf(umin, fmaf(ez, ez, fmaf(ey, ey, fmaf(ex, ex, -rh[u][v]))));
+        }
       }
+    }
     if (__any_sync(MRMG_FULL, umin <= 0.f)) {
       bool coll = false;
       if (umin <= 0.f) {
@@ -650,7 +670,7 @@ __device__ __forceinline__ bool edge_N(const void* q1, const void* q2, int dtype
 }
 
 template <int GPL, int SPG, bool RESOLVE>
-__global__ void __launch_bounds__(256, RESOLVE ? 1 : 4) arm_edges_kernel(ArmDev s, const void* q1, const void* q2, int dtype,
+__global__ void __launch_bounds__(256, (RESOLVE || GPL > 1) ? 1 : 4) arm_edges_kernel(ArmDev s, const void* q1, const void* q2, int dtype,
                                                         long long n, double res, int incl,
                                                         const long long* Np, long long N_start,
                                                         long long N_max, uint8_t* out, int* ctr,
@@ -784,7 +804,7 @@ __global__ void __launch_bounds__(256, RESOLVE ? 1 : 4) arm_edges_kernel(ArmDev 
 
 // positions p_next + j, j in [j_lo, j_hi), of every survivor (j_hi < 0: to the end)
 template <int GPL, int SPG>
-__global__ void __launch_bounds__(256) arm_edges_phase_b(ArmDev s, const void* q1, const void* q2, int dtype,
+__global__ void __launch_bounds__(256, GPL > 1 ? 1 : 4) arm_edges_phase_b(ArmDev s, const void* q1, const void* q2, int dtype,
                                                          int incl, int* ctr, SurvivorEdge* surv, int full,
                                                          int j_lo, int j_hi) {
   const int nsv = ctr[kCtrL1];

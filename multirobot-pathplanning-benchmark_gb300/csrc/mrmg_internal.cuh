@@ -51,6 +51,8 @@ struct ArmDev {
   const float4* band32;    // [G*SPG]  rlo^2, rhi^2, r + delta, r - delta  (padding: -1,-1,0,0)
   const float4* box32;     // [B*2]    centre xyz, half extents xyz
   const int* grp;          // [G]      robot | link << 8
+  const float4* gbs32;     // [G]      group bound: local centre xyz, radius^2 (radius covers every
+                           //          sphere of the group plus 4 delta; padding groups: -1)
   const uint32_t* pairs;   // [NP]     group a | group b << 16 (different robots)
 };
 
