@@ -61,7 +61,8 @@ __host__ __device__ inline size_t table_bytes(const ArmDev& s) {
 // per-warp FP32 work area: joint cos/sin, planar translations, sphere table
 __host__ __device__ inline size_t warp32_bytes(const ArmDev& s) {
   return align16(sizeof(float2) * s.D) + align16(sizeof(float) * s.D) +
-         align16(sizeof(float4) * s.G * s.SPG) + align16(sizeof(float) * s.G * s.SPG);
+         align16(sizeof(float4) * s.G * s.SPG) + align16(sizeof(float) * s.G * s.SPG) +
+         align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * s.NP);
 }
 
 // per-warp FP64 work area for pass 2: joint values, cos/sin, sphere centres
@@ -294,9 +295,16 @@ struct EdgeSource64 {       // pass 2: q1 + dir * i exactly as the reference (FP
   }
 };
 
-// the warp's pair-filter norms s = |c|^2 - r'^2, stored right after its sphere table
+// the warp's pair-filter norms s = |c|^2 - 2 r'^2, group bounds (world centre,
+// radius) and near group-pair list, stored right after its sphere table
 __device__ __forceinline__ float* wss_of(const ArmDev& s, float4* wsph) {
   return (float*)((unsigned char*)wsph + align16(sizeof(float4) * s.G * s.SPG));
+}
+__device__ __forceinline__ float4* wgb_of(const ArmDev& s, float4* wsph) {
+  return (float4*)((unsigned char*)wss_of(s, wsph) + align16(sizeof(float) * s.G * s.SPG));
+}
+__device__ __forceinline__ uint32_t* wnear_of(const ArmDev& s, float4* wsph) {
+  return (uint32_t*)((unsigned char*)wgb_of(s, wsph) + align16(sizeof(float4) * s.G));
 }
 
 // ---------------------------------------------------------------------------
@@ -458,25 +466,51 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
   // with s = |c|^2 - 2 r^2 per sphere (r = radius + delta): three products
   // per pair.  Pairs with a filter value within its FP32 error bound go to the
   // direct test below, which decides exactly as before.
+  // Group pairs whose bounds are apart (|g_a - g_b| > R_a + R_b; each R holds
+  // 4 delta, 2 delta more than the band needs) cannot hold a flagged sphere
+  // pair: they are dropped first and the rest are compacted, so the sphere
+  // pairs run in dense rounds.
   const float d4 = 4.f * s.delta;
   float* wss = wss_of(s, wsph);
+  float4* wgb = wgb_of(s, wsph);
+  uint32_t* wnear = wnear_of(s, wsph);
 #pragma unroll
   for (int u = 0; u < GPL; u++) {
     const int g = lane + 32 * u;
-    if (g < s.G)
+    if (g < s.G) {
 #pragma unroll
       for (int v = 0; v < SPG; v++) {
         const float4 c = wsph[g * SPG + v];
         wss[g * SPG + v] = fmaf(c.x, c.x, fmaf(c.y, c.y, fmaf(c.z, c.z, -2.f * c.w * c.w)));
       }
+      wgb[g] = make_float4(gb[u][0], gb[u][1], gb[u][2], gb[u][3] >= 0.f ? sqrtf(gb[u][3]) : -1.0e30f);
+    }
   }
   __syncwarp();
+  int nnear = 0;
+  const unsigned lt = (1u << lane) - 1u;
   for (int base = 0; base < s.NP; base += 32) {
     const int pi = base + lane;
-    float umin = 3.0e38f;
+    bool near = false;
     uint32_t pr = 0;
     if (pi < s.NP) {
       pr = t.pairs[pi];
+      const float4 ga = wgb[pr & 0xffff], gq = wgb[pr >> 16];
+      const float dx = ga.x - gq.x, dy = ga.y - gq.y, dz = ga.z - gq.z;
+      const float rr = ga.w + gq.w;
+      near = rr > 0.f && fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= rr * rr;
+    }
+    const unsigned m = __ballot_sync(MRMG_FULL, near);
+    if (near) wnear[nnear + __popc(m & lt)] = pr;
+    nnear += __popc(m);
+  }
+  __syncwarp();
+  for (int base = 0; base < nnear; base += 32) {
+    const int pi = base + lane;
+    float umin = 3.0e38f;
+    uint32_t pr = 0;
+    if (pi < nnear) {
+      pr = wnear[pi];
       const int sa0 = (pr & 0xffff) * SPG, sb0 = (pr >> 16) * SPG;
       float4 a[SPG];   // (-2 x, -2 y, -2 z, s)
 #pragma unroll
@@ -537,7 +571,8 @@ __device__ __forceinline__ void warp_areas(const ArmDev& s, unsigned char* smem_
   *wcs = (float2*)p; p += align16(sizeof(float2) * s.D);
   *wqv = (float*)p; p += align16(sizeof(float) * s.D);
   *wsph = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
-  p += align16(sizeof(float) * s.G * s.SPG);   // pair-filter norms (after wsph, see wss_of)
+  // pair-filter norms, group bounds, near group pairs (after wsph, see wss_of)
+  p += align16(sizeof(float) * s.G * s.SPG) + align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * s.NP);
   *w64 = (double*)p;
 }
 
