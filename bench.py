@@ -381,7 +381,7 @@ def run_gb300(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": WORKLOAD_DESC, "edges_per_step": n, "edges_total": n * world,
                        "l2": "flushed between timed steps (256 MB write outside the timed events)",
-                       "form": "batched, CUDA-graph captured (counter reset, phase A, phase B1, phase B2, finalize, FP64 "
+                       "form": "batched, CUDA-graph captured (counter reset, phase A, phase B1, phase B2 + finalize, FP64 "
                                "re-check pass, status copy)", "parallelism": f"replicas x{world}"},
             "verdict_mismatches": mism,
             "clocks": clk,
@@ -394,7 +394,7 @@ def run_gb300(args):
                                   f"{args.chunks} pipelined chunks"},
             "e2e_batch_call": {"value": call_e2e, "unit": UNIT,
                                "api": "Gb300ArmEnvironment.batch_is_edge_collision_free(pinned tensors)"},
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": 4 * args.steps,
             "wall_s_timed": t_wall,
         }
         line.update(extra)

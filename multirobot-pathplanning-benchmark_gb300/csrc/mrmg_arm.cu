@@ -629,7 +629,8 @@ __global__ void __launch_bounds__(256) arm_configs_kernel(ArmDev s, const void* 
 //            warp in blocks of 32; a collision marks the edge dead and its
 //            remaining positions are skipped.  Long free edges no longer run on
 //            one warp.
-//   finalize survivors' verdicts; undecided ones join the FP64 pending list.
+//   finalize survivors' verdicts (last CTA of the last phase-B launch);
+//            undecided ones join the FP64 pending list.
 //   pass 2   (RESOLVE) warp per pending edge, the reference's order, exact.
 // ---------------------------------------------------------------------------
 
@@ -781,7 +782,7 @@ __global__ void __launch_bounds__(256, (RESOLVE || GPL > 1) ? 1 : 4) arm_edges_k
               atomicMax(&ctr[kCtrMaxJ], (int)(nmax - p - 1));
             }
             __syncwarp();
-            continue;                       // phase B and the finalize kernel decide
+            continue;                       // phase B decides (its last launch finalizes)
           } else {
             r = code;
           }
@@ -837,16 +838,38 @@ __global__ void __launch_bounds__(256, (RESOLVE || GPL > 1) ? 1 : 4) arm_edges_k
   if (lane == 0 && !RESOLVE) atomicAdd((unsigned long long*)&ctr[kCtrStat0], (unsigned long long)stat_cfg);
 }
 
+// survivors' verdicts; undecided ones join the FP64 pending list.  Run by
+// one CTA (thread stride) after every phase-B configuration has finished.
+__device__ void finalize_survivors(int* ctr, const SurvivorEdge* surv, uint8_t* out, long long* pend) {
+  const int nsv = *(volatile int*)&ctr[kCtrL1];
+  const volatile SurvivorEdge* vs = surv;
+  for (int l = threadIdx.x; l < nsv; l += blockDim.x) {
+    const long long e = vs[l].e;
+    const uint8_t r = vs[l].dead ? V_COLLIDE : (vs[l].pend ? V_PENDING : V_FREE);
+    out[e] = r;
+    if (r == V_PENDING) {
+      const int slot = atomicAdd(&ctr[kCtrPending], 1);
+      pend[slot] = e;
+    }
+  }
+}
+
 // positions p_next + j, j in [j_lo, j_hi), of every survivor (j_hi < 0: to the end)
 template <int GPL, int SPG>
 __global__ void __launch_bounds__(256, GPL > 1 ? 1 : 4) arm_edges_phase_b(ArmDev s, const void* q1, const void* q2, int dtype,
                                                          int incl, int* ctr, SurvivorEdge* surv, int full,
-                                                         int j_lo, int j_hi) {
+                                                         int j_lo, int j_hi, uint8_t* out, long long* pend) {
+  // the last launch (j_hi < 0) also finalizes: its last CTA to finish sets the
+  // survivors' verdicts (or CTA 0, when the launch has no positions left)
+  const bool fin = j_hi < 0;
   const int nsv = ctr[kCtrL1];
   const long long maxj = j_hi < 0 ? (long long)ctr[kCtrMaxJ] : min((long long)j_hi, (long long)ctr[kCtrMaxJ]);
   const long long first = (long long)nsv * j_lo;
   const long long total = (long long)nsv * maxj;
-  if (total <= first) return;
+  if (total <= first) {
+    if (fin && blockIdx.x == 0) finalize_survivors(ctr, surv, out, pend);
+    return;
+  }
   extern __shared__ __align__(16) unsigned char smem_arm[];
   ArmSmem t;
   stage_tables(s, smem_arm, &t);
@@ -903,20 +926,22 @@ __global__ void __launch_bounds__(256, GPL > 1 ? 1 : 4) arm_edges_phase_b(ArmDev
     }
   }
   if (lane == 0) atomicAdd((unsigned long long*)&ctr[kCtrStat0], (unsigned long long)stat_cfg);
-}
-
-__global__ void arm_edges_finalize(int* ctr, const SurvivorEdge* surv, uint8_t* out, long long* pend) {
-  const int nsv = ctr[kCtrL1];
-  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nsv; l += gridDim.x * blockDim.x) {
-    const SurvivorEdge sv = surv[l];
-    const uint8_t r = sv.dead ? V_COLLIDE : (sv.pend ? V_PENDING : V_FREE);
-    out[sv.e] = r;
-    if (r == V_PENDING) {
-      const int slot = atomicAdd(&ctr[kCtrPending], 1);
-      pend[slot] = sv.e;
+  if (fin) {
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      s_last = atomicAdd(&ctr[kCtrDoneB], 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      finalize_survivors(ctr, surv, out, pend);
     }
   }
 }
+
+
 
 // sphere centres for the error-bound check: warp per configuration
 __global__ void arm_centers_kernel(ArmDev s, const void* q, int dtype, long long n, float* c32, double* c64) {
@@ -1075,11 +1100,11 @@ cudaError_t launch_edges(const ArmDev& s, int gpl, const void* q1, const void* q
 
 cudaError_t launch_phase_b(const ArmDev& s, int gpl, const void* q1, const void* q2, int dtype, int incl,
                            const CallScratch& sc, int grid, int warps, size_t smem, int full, int j_lo, int j_hi,
-                           cudaStream_t st) {
+                           uint8_t* out, cudaStream_t st) {
 #define MRMG_ARM_PB(G_, S_)                                                                        \
   if (gpl == G_ && s.SPG == S_) {                                                                  \
     arm_edges_phase_b<G_, S_><<<grid, warps * 32, smem, st>>>(s, q1, q2, dtype, incl, sc.ctr, sc.surv, full, \
-                                                              j_lo, j_hi);                         \
+                                                              j_lo, j_hi, out, sc.pend);           \
     return cudaGetLastError();                                                                     \
   }
   MRMG_ARM_PB(1, 6)
@@ -1155,11 +1180,11 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
   if (e != cudaSuccess) return e;
   // B1: the next kPhaseB1 positions of every survivor (kills most colliding
   // survivors); B2: everything left, spread over all warps
-  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, 0, kPhaseB1, st);
+  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, 0, kPhaseB1, out, st);
   if (e != cudaSuccess) return e;
-  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, kPhaseB1, -1, st);
+  // B2 finalizes the survivors' verdicts in its last CTA
+  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, kPhaseB1, -1, out, st);
   if (e != cudaSuccess) return e;
-  arm_edges_finalize<<<std::max(1, ls.num_sms), 256, 0, st>>>(sc.ctr, sc.surv, out, sc.pend);
   const int w2 = 2;
   return launch_edges<true>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc, ls.num_sms,
                             w2, smem_pass(s, w2, true), 0, st);

@@ -78,9 +78,10 @@ struct PenParams {
 // per-call scratch counters (device): [0] work queue, [1] pending count,
 // [2] error bits, [3] pass-two queue, [4..5] configurations evaluated (64-bit),
 // [6] surviving edges, [7] longest remaining position range, [8..9] phase-B
-// queue (64-bit)
+// queue (64-bit), [10] finished CTAs of the last phase-B launch
 constexpr int kCtrQueue = 0, kCtrPending = 1, kCtrErr = 2, kCtrQueue2 = 3, kCtrStat0 = 4;
 constexpr int kCtrL1 = 6, kCtrMaxJ = 7, kCtrQueueB = 8;
+constexpr int kCtrDoneB = 10;   // CTAs of the last phase-B launch that have finished
 constexpr int kNumCtr = 16;
 
 // an edge that survived its first checked configuration: its remaining
