@@ -844,8 +844,10 @@ void knn_store_free(KnnStore* s) {
 
 // scratch for one query launch, owned by the caller (the ABI layer)
 struct KnnScratch {
-  void* block = nullptr;
+  void* block = nullptr;    // device scratch
   size_t bytes = 0;
+  void* host = nullptr;     // pinned staging: the per-call tables go up in one copy
+  size_t host_bytes = 0;
 };
 
 cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h_q_mode, int k, long long* d_idx,
@@ -919,12 +921,24 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   float* d_eps = (float*)p; p += b_eps;
   long long* d_fb = (long long*)p; p += b_fb;
   int* d_ctr = (int*)p;   // [0] fallback count, [1] error bits
-  std::vector<int> qm(h_q_mode, h_q_mode + Q);
-  cudaError_t e = cudaMemcpyAsync(d_order, order.data(), sizeof(int) * Q, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_qmode, qm.data(), sizeof(int) * Q, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess && !items.empty())
-    e = cudaMemcpyAsync(d_items, items.data(), sizeof(KnnItem) * items.size(), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_mch, mode_chunks.data(), sizeof(int) * n_modes, cudaMemcpyHostToDevice, st);
+  // order, query modes, items and chunk counts sit back to back in the device
+  // block: stage them in pinned memory with the same layout, one copy
+  const size_t b_up = b_order + b_qmode + b_items + b_mch;
+  if (scr->host_bytes < b_up + 256) {
+    if (scr->host) cudaFreeHost(scr->host);
+    scr->host = nullptr;
+    scr->host_bytes = 0;
+    cudaError_t e = cudaMallocHost(&scr->host, b_up + 256);
+    if (e != cudaSuccess) return e;
+    scr->host_bytes = b_up + 256;
+  }
+  unsigned char* hp = (unsigned char*)scr->host;
+  std::memcpy(hp, order.data(), sizeof(int) * Q);
+  std::memcpy(hp + b_order, h_q_mode, sizeof(int) * Q);
+  if (!items.empty()) std::memcpy(hp + b_order + b_qmode, items.data(), sizeof(KnnItem) * items.size());
+  std::memcpy(hp + b_order + b_qmode + b_items, mode_chunks.data(), sizeof(int) * n_modes);
+  int* h_ctr = (int*)(hp + b_up);
+  cudaError_t e = cudaMemcpyAsync(d_order, hp, b_up, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, 256, st);
   if (e != cudaSuccess) return e;
   const int NT = s->dev.NT;
@@ -934,13 +948,28 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   const size_t smem = std::max<size_t>(1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes +
                                            32 * sizeof(float) * (size_t)nthreads,
                                        120 * 1024);
+  // the attribute is per function: raise it once, to the opt-in limit less
+  // the kernel's static shared memory
+  static bool attr_set = false;
+  if (!attr_set) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, knn_tc_kernel<KNN_FMT_EUCL>) == cudaSuccess)
+      cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_EUCL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           optin - (int)fa.sharedSizeBytes);
+    if (cudaFuncGetAttributes(&fa, knn_tc_kernel<KNN_FMT_AGENT>) == cudaSuccess)
+      cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_AGENT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           optin - (int)fa.sharedSizeBytes);
+    cudaGetLastError();
+    attr_set = true;
+  }
   if (!items.empty()) {
     if (s->dev.fmt == KNN_FMT_EUCL) {
-      cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_EUCL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       knn_tc_kernel<KNN_FMT_EUCL><<<(int)items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
                                                                          d_cd, d_ci, d_eps, d_ctr + 1);
     } else {
-      cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_AGENT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       knn_tc_kernel<KNN_FMT_AGENT><<<(int)items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
                                                                           d_cd, d_ci, d_eps, d_ctr + 1);
     }
@@ -953,7 +982,6 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
                                                        d_ctr);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  int h_ctr[2] = {0, 0};
   e = cudaMemcpyAsync(h_ctr, d_ctr, sizeof(int) * 2, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
@@ -973,7 +1001,11 @@ void knn_store_delete(KnnStore* s) {
 }
 KnnScratch* knn_scratch_new() { return new KnnScratch(); }
 void knn_scratch_delete(KnnScratch* s) {
-  if (s) { if (s->block) cudaFree(s->block); delete s; }
+  if (s) {
+    if (s->block) cudaFree(s->block);
+    if (s->host) cudaFreeHost(s->host);
+    delete s;
+  }
 }
 
 }  // namespace mrmg
