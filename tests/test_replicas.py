@@ -1,0 +1,65 @@
+"""The multi-GPU path is replicas only: each rank checks its own seeded
+shard of edges, the job's time is the max over ranks, rank 0 reports.  These
+tests run that host logic as world-size-2 gloo ranks on the CPU."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch.multiprocessing as mp
+
+from conftest import ROOT
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out_dir):
+    import sys
+
+    sys.path.insert(0, str(ROOT))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import torch.distributed as dist
+
+    import bench
+
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    w, r, local = bench.dist_env()
+    assert (w, r, local) == (world, rank, rank)
+    bench.barrier(world)
+    # the slowest replica sets the job time
+    t = bench.reduce_max(1.0 + rank, world)
+    scene, q1, q2, N = bench.workload(rank)
+    np.savez(os.path.join(out_dir, f"rank{rank}.npz"), t=t, q1=q1[:64], N=N[:64])
+    bench.barrier(world)
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_shard_and_max(tmp_path):
+    world, port = 2, _free_port()
+    mp.spawn(_rank_main, args=(world, port, str(tmp_path)), nprocs=world, join=True)
+    r0, r1 = np.load(tmp_path / "rank0.npz"), np.load(tmp_path / "rank1.npz")
+    assert float(r0["t"]) == float(r1["t"]) == 2.0
+    # every rank gets its own seeded shard (weak scaling, no data exchange)
+    assert not np.array_equal(r0["q1"], r1["q1"])
+    assert r0["q1"].shape == r1["q1"].shape
+
+
+def test_reference_arm_other_ranks_do_nothing(monkeypatch):
+    import sys
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    monkeypatch.setenv("RANK", "1")
+
+    class A:
+        steps, warmup = 3, 3
+
+    # rank 1 of the reference arm exits 0 without work (rank 0 alone runs it)
+    assert bench.run_reference(A()) == 0
