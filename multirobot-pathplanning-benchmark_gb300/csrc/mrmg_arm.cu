@@ -59,10 +59,14 @@ __host__ __device__ inline size_t table_bytes(const ArmDev& s) {
 }
 
 // per-warp FP32 work area: joint cos/sin, planar translations, sphere table
+constexpr int kNearBlock = 512;   // at most this many group pairs compacted per block of the pair rounds
+
+__host__ __device__ inline int near_block(const ArmDev& s) { return s.NP < kNearBlock ? (s.NP > 0 ? s.NP : 1) : kNearBlock; }
+
 __host__ __device__ inline size_t warp32_bytes(const ArmDev& s) {
   return align16(sizeof(float2) * s.D) + align16(sizeof(float) * s.D) +
          align16(sizeof(float4) * s.G * s.SPG) + align16(sizeof(float) * s.G * s.SPG) +
-         align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * s.NP);
+         align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * near_block(s));
 }
 
 // per-warp FP64 work area for pass 2: joint values, cos/sin, sphere centres
@@ -487,13 +491,16 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
     }
   }
   __syncwarp();
-  int nnear = 0;
   const unsigned lt = (1u << lane) - 1u;
-  for (int base = 0; base < s.NP; base += 32) {
+  const int nblk = near_block(s);
+  for (int blk = 0; blk < s.NP; blk += nblk) {
+  const int blk_end = min(s.NP, blk + nblk);
+  int nnear = 0;
+  for (int base = blk; base < blk_end; base += 32) {
     const int pi = base + lane;
     bool near = false;
     uint32_t pr = 0;
-    if (pi < s.NP) {
+    if (pi < blk_end) {
       pr = t.pairs[pi];
       const float4 ga = wgb[pr & 0xffff], gq = wgb[pr >> 16];
       const float dx = ga.x - gq.x, dy = ga.y - gq.y, dz = ga.z - gq.z;
@@ -558,6 +565,8 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
       }
     }
   }
+  __syncwarp();   // the next block rewrites the near list
+  }
   if (hit_any) return V_COLLIDE;
   if (RESOLVE) return V_FREE;
   return __any_sync(MRMG_FULL, unc) ? V_PENDING : V_FREE;
@@ -572,7 +581,7 @@ __device__ __forceinline__ void warp_areas(const ArmDev& s, unsigned char* smem_
   *wqv = (float*)p; p += align16(sizeof(float) * s.D);
   *wsph = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
   // pair-filter norms, group bounds, near group pairs (after wsph, see wss_of)
-  p += align16(sizeof(float) * s.G * s.SPG) + align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * s.NP);
+  p += align16(sizeof(float) * s.G * s.SPG) + align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * near_block(s));
   *w64 = (double*)p;
 }
 
@@ -584,7 +593,7 @@ constexpr int kCfgChunk = 4;
 constexpr int kPhaseB1 = 3;   // positions per survivor in the first phase-B launch
 
 template <int GPL, int SPG, bool RESOLVE>
-__global__ void __launch_bounds__(256) arm_configs_kernel(ArmDev s, const void* q, int dtype, long long n,
+__global__ void __launch_bounds__(256, RESOLVE ? 1 : (GPL == 1 ? 4 : (GPL == 2 ? 2 : 1))) arm_configs_kernel(ArmDev s, const void* q, int dtype, long long n,
                                                           uint8_t* out, int* ctr, long long* pend, int full) {
   if (RESOLVE && ctr[kCtrPending] == 0) return;   // nothing was left undecided
   extern __shared__ __align__(16) unsigned char smem_arm[];
@@ -706,7 +715,7 @@ __device__ __forceinline__ bool edge_N(const void* q1, const void* q2, int dtype
 }
 
 template <int GPL, int SPG, bool RESOLVE>
-__global__ void __launch_bounds__(256, (RESOLVE || GPL > 1) ? 1 : 4) arm_edges_kernel(ArmDev s, const void* q1, const void* q2, int dtype,
+__global__ void __launch_bounds__(256, RESOLVE ? 1 : (GPL == 1 ? 4 : (GPL == 2 ? 2 : 1))) arm_edges_kernel(ArmDev s, const void* q1, const void* q2, int dtype,
                                                         long long n, double res, int incl,
                                                         const long long* Np, long long N_start,
                                                         long long N_max, uint8_t* out, int* ctr,
@@ -856,7 +865,7 @@ __device__ void finalize_survivors(int* ctr, const SurvivorEdge* surv, uint8_t* 
 
 // positions p_next + j, j in [j_lo, j_hi), of every survivor (j_hi < 0: to the end)
 template <int GPL, int SPG>
-__global__ void __launch_bounds__(256, GPL > 1 ? 1 : 4) arm_edges_phase_b(ArmDev s, const void* q1, const void* q2, int dtype,
+__global__ void __launch_bounds__(256, GPL == 1 ? 4 : (GPL == 2 ? 2 : 1)) arm_edges_phase_b(ArmDev s, const void* q1, const void* q2, int dtype,
                                                          int incl, int* ctr, SurvivorEdge* surv, int full,
                                                          int j_lo, int j_hi, uint8_t* out, long long* pend) {
   // the last launch (j_hi < 0) also finalizes: its last CTA to finish sets the

@@ -157,8 +157,10 @@ __device__ __forceinline__ void acc2(float& h, float& l, float v) {
   l += e;
 }
 
+// the cost kernel fits two 16-warp CTAs per SM (shared memory allows it when
+// the registers stay at 64); the gradient kernel holds twice the tables
 template <bool COST, bool GRAD>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(512, GRAD ? 1 : 2)
     pen_kernel(ArmDev a, PenDev pd, PenParams pp, const float* __restrict__ paths, int T, int nseg,
                const float* __restrict__ gout, double* __restrict__ seg_cost, float* __restrict__ wp_cost,
                float* __restrict__ grad) {
