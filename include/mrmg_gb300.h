@@ -150,6 +150,18 @@ int mrmg_arm_scene_tune_order(mrmg_scene *scene, const void *d_q, int32_t dtype,
 int mrmg_is_collision_free_batch(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n,
                                  uint8_t *d_out, void *stream, int32_t flags);
 
+/* is_collision_free_for_robot (rai_base_env.py:515-615, pinocchio_env.py:
+ * 502-, called by the per-robot rejection sampler,
+ * planners/collision_free_sampler.py:115-135) for a set of robots of an arm
+ * scene, per configuration: a configuration is free for the set unless a
+ * sphere of a robot in the set touches a box or a sphere of another robot in
+ * the set (collisions with robots outside the set are ignored, as the
+ * reference ignores collisions that involve another robot).  Bit r of
+ * robot_mask selects robot r.  Exact, like is_collision_free: the engines'
+ * summed-penetration tolerance is not modelled. */
+int mrmg_is_collision_free_batch_robots(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n,
+                                        uint32_t robot_mask, uint8_t *d_out, void *stream, int32_t flags);
+
 /* Per-edge verdicts for the linear edges d_q1[n] -> d_q2[n], interpolated at
  * `resolution` exactly as BaseProblem.is_edge_collision_free
  * (planning_env.py:1746-1763; abstract_env.py:301-354):

@@ -48,6 +48,7 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_scene_set_launch": (i32, [vp, i32, i32]),
     "mrmg_arm_scene_tune_order": (i32, [vp, vp, i32, i64, vp, vp]),
     "mrmg_is_collision_free_batch": (i32, [vp, vp, i32, i64, vp, vp, i32]),
+    "mrmg_is_collision_free_batch_robots": (i32, [vp, vp, i32, i64, C.c_uint32, vp, vp, i32]),
     "mrmg_is_edge_collision_free_batch": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, vp, i32]),
     "mrmg_is_edge_collision_free_batch_noalloc": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, vp, i32]),
     "mrmg_arm_sphere_centers": (i32, [vp, vp, i32, i64, vp, vp, vp]),

@@ -135,6 +135,26 @@ class Gb300Scene:
                                                          _lib.stream_handle(stream), flags), "is_collision_free")
         return out
 
+    def is_collision_free_batch_robots(self, q, robot_mask: int, out=None, stream=None, flags: int = 0) -> torch.Tensor:
+        """Per-configuration verdicts for the robots in ``robot_mask`` (bit r =
+        robot r): collisions of those robots with boxes and with each other;
+        robots outside the mask are ignored (arm scenes)."""
+        if self.kind != 1:
+            raise NotImplementedError("per-robot checks exist for arm scenes")
+        qt = _dev_tensor(q)
+        if qt.dim() == 1:
+            qt = qt.reshape(1, -1)
+        if qt.shape[-1] != self.q_dim:
+            raise ValueError(f"configurations must have {self.q_dim} coordinates")
+        n = qt.shape[0]
+        if out is None:
+            out = torch.empty(n, dtype=torch.uint8, device=qt.device)
+        _lib.check(self.lib.mrmg_is_collision_free_batch_robots(self.h, qt.data_ptr(), _dt_code(qt), n,
+                                                                int(robot_mask), out.data_ptr(),
+                                                                _lib.stream_handle(stream), flags),
+                   "is_collision_free_for_robot")
+        return out
+
     def is_edge_collision_free_batch(self, q1, q2, resolution: float, include_endpoints: bool = False, N=None,
                                      N_start: int = 0, N_max=None, out=None, stream=None, flags: int = 0) -> torch.Tensor:
         """Per-edge verdicts (1 = free) for the linear edges q1[n] -> q2[n]."""

@@ -357,6 +357,7 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   }
   for (int r = 0; r < R; r++) { d.q_off[r] = h_q_offset[r]; d.base_kind[r] = h_base_kind[r]; d.nl[r] = h_n_links[r]; }
   d.prismatic[0] = prism[0]; d.prismatic[1] = prism[1]; d.prismatic[2] = prism[2];
+  d.robot_mask = R >= 32 ? 0xffffffffu : ((1u << R) - 1u);
 
   std::vector<float4> base32(R * 3), dh32(R * kMaxLinks), sph32(G * SPG), band32(G * SPG), box32(2 * B);
   std::vector<double> sph64((size_t)G * SPG * 5), box64((size_t)B * 6);
@@ -604,6 +605,28 @@ int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype,
   LaunchShape ls = shape(sc);
   e = sc->kind == 0 ? abstract_configs(sc->ab, d_q, dtype, n, d_out, cs, ls, st)
                     : arm_configs(sc->arm, d_q, dtype, n, d_out, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch configs");
+  return finish_call(sc, st, flags);
+}
+
+int mrmg_is_collision_free_batch_robots(mrmg_scene* sc, const void* d_q, int32_t dtype, int64_t n,
+                                        uint32_t robot_mask, uint8_t* d_out, void* stream, int32_t flags) {
+  if (!sc || sc->kind != 1) return fail(MRMG_ERR_UNSUPPORTED, "per-robot checks need an arm scene");
+  const uint32_t all = sc->arm.R >= 32 ? 0xffffffffu : ((1u << sc->arm.R) - 1u);
+  if (!(robot_mask & all) || (robot_mask & ~all)) return fail(MRMG_ERR_ARG, "robot mask must select robots of the scene");
+  if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
+  if (n > kMaxBatch) return fail(MRMG_ERR_ARG, "batch of %lld exceeds %lld items; split it", (long long)n, kMaxBatch);
+  if (n == 0) return MRMG_OK;
+  if (!d_q || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = ensure_pending(sc, n, st);
+  if (rc) return rc;
+  cudaError_t e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  CallScratch cs{sc->d_ctr, sc->d_pend, sc->d_surv, sc->pend_cap};
+  ArmDev a = sc->arm;
+  a.robot_mask = robot_mask;
+  e = arm_configs(a, d_q, dtype, n, d_out, cs, shape(sc), (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
   if (e != cudaSuccess) return cuda_fail(e, "launch configs");
   return finish_call(sc, st, flags);
 }

@@ -216,17 +216,22 @@ __device__ __forceinline__ bool exact_pair_hit(const double* a, const double* b,
 
 // every test of the configuration in FP64 (pass 2, when an angle or a planar
 // translation is outside the FP32 path's range)
+__device__ __forceinline__ bool group_in_mask(const ArmDev& s, int g) {
+  return (s.robot_mask >> (s.grp[g] & 0xff)) & 1u;
+}
+
 __device__ bool exact_all_collide(const ArmDev& s, const double* wc64, int lane) {
   bool hit = false;
   const int slots = s.G * s.SPG;
   for (int sl = lane; sl < slots && !hit; sl += 32) {
-    if (s.sph64[(size_t)sl * 5 + 3] < 0.0) continue;
+    if (s.sph64[(size_t)sl * 5 + 3] < 0.0 || !group_in_mask(s, sl / s.SPG)) continue;
     for (int b = 0; b < s.B && !hit; b++)
       hit |= exact_box_hit(wc64 + (size_t)sl * 3, s.box64 + (size_t)b * 6, s.sph64[(size_t)sl * 5 + 4]);
   }
   for (int pi = lane; pi < s.NP && !hit; pi += 32) {
     const uint32_t pr = s.pairs[pi];
     const int ga = pr & 0xffff, gb = pr >> 16;
+    if (!group_in_mask(s, ga) || !group_in_mask(s, gb)) continue;
     for (int v = 0; v < s.SPG && !hit; v++) {
       const int sa = ga * s.SPG + v;
       if (s.sph64[(size_t)sa * 5 + 3] < 0.0) continue;
@@ -391,7 +396,9 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
       gb[u][0] = p[0] + (R[0] * lb.x + R[1] * lb.y + R[2] * lb.z);
       gb[u][1] = p[1] + (R[3] * lb.x + R[4] * lb.y + R[5] * lb.z);
       gb[u][2] = p[2] + (R[6] * lb.x + R[7] * lb.y + R[8] * lb.z);
-      gb[u][3] = lb.w;
+      // a robot outside the call's mask: its bound never reaches a box or
+      // another group, so none of its spheres is tested
+      gb[u][3] = ((s.robot_mask >> (gi & 0xff)) & 1u) ? lb.w : -1.f;
 #pragma unroll
       for (int v = 0; v < SPG; v++) {
         const float4 l = t.sph[g * SPG + v];

@@ -39,6 +39,7 @@ struct ArmDev {
   float pair_eps;   // FP32 error bound (m^2) of the pair filter s_a + s_b - 2 a.b
   int q_off[kMaxRobots], base_kind[kMaxRobots], nl[kMaxRobots];
   uint32_t prismatic[3];   // bit j: joint j is a planar-base translation
+  uint32_t robot_mask;     // bit r: robot r's spheres take part (per call; all robots by default)
   // exact FP64 tables (global memory)
   const double* base64;    // [R*12]
   const double* dh64;      // [R*8*4]  a, d, cos(alpha), sin(alpha)

@@ -81,6 +81,33 @@ class Gb300CollisionBackend:
                                                      include_endpoints, None if N is None else [int(N)], N_start, N_max)
         return bool(v.item())
 
+    def is_collision_free_for_robot(self, r, q, m=None, collision_tolerance: Optional[float] = None,
+                                    set_mode: bool = True) -> bool:
+        """rai_base_env.py:515-615 for arm scenes: free unless a robot of ``r``
+        (a name or a list of names) touches a box or another robot of ``r``;
+        collisions with robots outside ``r`` are ignored.  The check is
+        exact, like is_collision_free (``collision_tolerance`` is accepted
+        for the signature; the engines' summed-penetration allowance is not
+        modelled)."""
+        v = self._gb300.is_collision_free_batch_robots(_state(q).reshape(1, -1), self._robot_mask(r))
+        return bool(v.item())
+
+    def batch_is_collision_free_for_robot(self, r, qs, mode=None) -> np.ndarray:
+        """Per-configuration verdicts of is_collision_free_for_robot."""
+        v = self._gb300.is_collision_free_batch_robots(qs, self._robot_mask(r))
+        return v.bool().cpu().numpy() if not isinstance(qs, torch.Tensor) else v.bool()
+
+    def _robot_mask(self, r) -> int:
+        names = [r] if isinstance(r, str) else list(r)
+        mask = 0
+        for name in names:
+            if name not in self.robots:
+                raise ValueError(f"unknown robot {name!r}")
+            mask |= 1 << self.robots.index(name)
+        if not mask:
+            raise ValueError("no robot given")
+        return mask
+
     def _batch_is_collision_free(self, qs: List, mode) -> bool:
         """abstract_env.py:278-299: True iff every configuration is free."""
         if len(qs) == 0:

@@ -319,9 +319,13 @@ int orc_arm_fk(const void *p, const double *q, double *centers) {
   return ORC_OK;
 }
 
-static int arm_config_free_centers(const orc_arm *a, const double *c) {
+/* mask: bit r selects robot r (is_collision_free_for_robot: collisions of the
+ * selected robots with boxes and with each other; pairs with an unselected
+ * robot are ignored, rai_base_env.py:515-615); all bits: is_collision_free */
+static int arm_config_free_centers_mask(const orc_arm *a, const double *c, uint32_t mask) {
   /* sphere - box: clip, squared distance summed in numpy order, <= r**2 */
   for (int s = 0; s < a->S; s++) {
+    if (!((mask >> a->s_robot[s]) & 1u)) continue;
     const double *cc = c + 3 * s;
     for (int b = 0; b < a->B; b++)
       if (rect_hits(a->lo + 3 * b, a->hi + 3 * b, cc, 3, a->s_r2[s])) return 0;
@@ -330,19 +334,28 @@ static int arm_config_free_centers(const orc_arm *a, const double *c) {
   for (int i = 0; i < a->S; i++)
     for (int j = i + 1; j < a->S; j++) {
       if (a->s_robot[i] == a->s_robot[j]) continue;
+      if (!((mask >> a->s_robot[i]) & 1u) || !((mask >> a->s_robot[j]) & 1u)) continue;
       double d[3] = {c[3 * i] - c[3 * j], c[3 * i + 1] - c[3 * j + 1], c[3 * i + 2] - c[3 * j + 2]};
       if (sqrt(np_norm_sq(d, 3)) < a->s_r[i] + a->s_r[j]) return 0;
     }
   return 1;
 }
 
-int orc_arm_config_free(const void *p, const double *q) {
+int orc_arm_config_free_mask(const void *p, const double *q, uint32_t mask) {
   const orc_arm *a = (const orc_arm *)p;
   double *c = (double *)malloc(sizeof(double) * 3 * a->S);
   orc_arm_fk(a, q, c);
-  int r = arm_config_free_centers(a, c);
+  int r = arm_config_free_centers_mask(a, c, mask);
   free(c);
   return r;
+}
+
+int orc_arm_config_free(const void *p, const double *q) { return orc_arm_config_free_mask(p, q, 0xffffffffu); }
+
+int orc_arm_configs_free_mask(const void *scene, const double *q, int64_t n, int32_t D, uint32_t mask, uint8_t *out) {
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < n; i++) out[i] = (uint8_t)orc_arm_config_free_mask(scene, q + (size_t)i * D, mask);
+  return ORC_OK;
 }
 
 /* ------------------------------------------------------------------------ */

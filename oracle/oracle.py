@@ -66,6 +66,7 @@ def lib() -> C.CDLL:
         L.orc_arm_fk.argtypes = [vp, vp, vp]
         L.orc_edge_free.argtypes = [i32, vp, vp, vp, i32, f64, i32, i64, i64, i64, vp, vp]
         L.orc_configs_free.argtypes = [i32, vp, vp, i64, i32, vp]
+        L.orc_arm_configs_free_mask.argtypes = [vp, vp, i64, i32, C.c_uint32, vp]
         L.orc_edges_free.argtypes = [i32, vp, vp, vp, i64, i32, f64, i32, vp, i64, i64, vp, vp]
         L.orc_binary_indices.argtypes = [i64, vp]
         L.orc_sincos.argtypes = [f64, vp, vp]
@@ -136,6 +137,13 @@ class OracleScene:
         qs = _c(qs, np.float64).reshape(-1, self.D)
         out = np.zeros(len(qs), dtype=np.uint8)
         lib().orc_configs_free(self.kind, self.h, _p(qs), len(qs), self.D, _p(out))
+        return out
+
+    def configs_free_for_robots(self, qs, robot_mask: int) -> np.ndarray:
+        """is_collision_free_for_robot for the robots in robot_mask (arm scenes)."""
+        qs = _c(qs, np.float64).reshape(-1, self.D)
+        out = np.zeros(len(qs), dtype=np.uint8)
+        lib().orc_arm_configs_free_mask(self.h, _p(qs), len(qs), self.D, int(robot_mask), _p(out))
         return out
 
     def edge_free(self, q1, q2, resolution, include_endpoints=False, N_start=0, N_max=None, N=None, count=False):

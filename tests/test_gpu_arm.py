@@ -234,3 +234,25 @@ def test_edge_check_pipeline(gpu, oracle):
     assert len(got) == len(order)
     for j, v in got:
         assert np.array_equal(v, want[j]), j
+
+
+@pytest.mark.parametrize("kind", ["arm", "mobile"])
+def test_collision_free_for_robot(gpu, oracle, kind):
+    """is_collision_free_for_robot: every robot subset tried gives the
+    oracle's verdicts; the full set equals is_collision_free."""
+    scenes, envm = pkg("scenes"), pkg("env")
+    scene = scenes.make_arm_scene(0) if kind == "arm" else scenes.make_mobile_scene(0)
+    env = envm.Gb300ArmEnvironment(scene, tune_samples=256)
+    o = oracle.OracleScene(scene)
+    q = scenes.uniform_configs(scene, 3000, seed=17)
+    R = scene.n_robots
+    masks = [1 << r for r in range(R)] + [0b11, (1 << R) - 1, 0b101]
+    for m in masks:
+        names = [env.robots[r] for r in range(R) if (m >> r) & 1]
+        got = env.batch_is_collision_free_for_robot(names, q)
+        want = o.configs_free_for_robots(q, m)
+        assert np.array_equal(got.astype(np.uint8), want), m
+    assert np.array_equal(env.batch_is_collision_free_for_robot(env.robots, q), env.batch_is_collision_free(q))
+    assert env.is_collision_free_for_robot(env.robots[0], q[0]) == bool(o.configs_free_for_robots(q[:1], 1)[0])
+    with pytest.raises(ValueError):
+        env.is_collision_free_for_robot("no-such-robot", q[0])

@@ -149,3 +149,19 @@ def test_sincos_close_to_libm(oracle):
         assert abs(s - math.sin(x)) <= 4e-16 * max(1.0, abs(x) / 8) and abs(c - math.cos(x)) <= 4e-16 * max(1.0, abs(x) / 8)
     assert all(math.isnan(v) for v in oracle.sincos(float("inf")))
     assert all(math.isnan(v) for v in oracle.sincos(2.0 ** 31))
+
+
+def test_oracle_robot_mask_semantics(oracle):
+    """The masked check: all robots = is_collision_free; a robot's verdict
+    ignores the other robots (their spheres and pairs with them)."""
+    from conftest import pkg
+
+    scenes = pkg("scenes")
+    sc = scenes.make_arm_scene(0)
+    o = oracle.OracleScene(sc)
+    q = scenes.uniform_configs(sc, 500, seed=2, dtype=np.float64)
+    assert np.array_equal(o.configs_free_for_robots(q, 0b1111), o.configs_free(q))
+    single = [o.configs_free_for_robots(q, 1 << r) for r in range(4)]
+    both = o.configs_free_for_robots(q, 0b0011)
+    # a pair of robots is free only if each robot alone is free
+    assert np.all(both <= single[0] & single[1])
