@@ -322,6 +322,25 @@ int mrmg_node_store_destroy(mrmg_node_store *store);
 int mrmg_knn(mrmg_node_store *store, const double *d_queries, int64_t Q, const int32_t *h_query_mode,
              int32_t k, int64_t *d_idx, double *d_dist, int64_t *out_stats2, void *stream);
 
+/* Radius neighbours (RRT* near, planners/rrtstar_base.py:1296-1337, with
+ * find_nearest_indices, rrtstar_base.py:439-453): for each query q, every
+ * node j of its mode h_query_mode[q] whose batch_config_dist value satisfies
+ * dist <= h_radius[q] + add_eps (the sum in FP64: the reference adds 1e-10),
+ * in ascending j (np.nonzero order).  Result in CSR form: d_offsets[Q + 1]
+ * (always written), mode-local d_idx[] and FP64 d_dist[] at positions
+ * offsets[q] .. offsets[q+1]; positions >= cap are not written.
+ * *out_total = offsets[Q].  When it exceeds cap, mrmg_near_fetch writes the
+ * whole result into larger buffers without recomputing it (the store keeps
+ * it until its next radius query; d_queries must stay unchanged until then).
+ * On the tensor-core store the candidate bitmap comes from the tcgen05
+ * distance tiles with the error bound added to the radius, then every
+ * candidate is re-checked in FP64; other metrics check every node in FP64.
+ * Synchronises its stream. */
+int mrmg_near(mrmg_node_store *store, const double *d_queries, int64_t Q, const int32_t *h_query_mode,
+              const double *h_radius, double add_eps, int64_t *d_offsets, int64_t *d_idx, double *d_dist,
+              int64_t cap, int64_t *out_total, void *stream);
+int mrmg_near_fetch(mrmg_node_store *store, int64_t *d_idx, double *d_dist, int64_t cap, void *stream);
+
 /* Tensor-core self-test (no counterpart in the reference): C[128 x n] =
  * A[128 x 64] * B[n x 64]^T for row-major BF16 A, B through the same shared-
  * memory descriptors, instruction descriptor and tensor-memory path as the

@@ -68,6 +68,8 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_node_store_create": (i32, [vp, i64, i32, vp, i32, vp, i32, i32, C.POINTER(vp), vp]),
     "mrmg_node_store_destroy": (i32, [vp]),
     "mrmg_knn": (i32, [vp, vp, i64, vp, i32, vp, vp, vp, vp]),
+    "mrmg_near": (i32, [vp, vp, i64, vp, vp, f64, vp, vp, vp, i64, vp, vp]),
+    "mrmg_near_fetch": (i32, [vp, vp, vp, i64, vp]),
 }
 
 

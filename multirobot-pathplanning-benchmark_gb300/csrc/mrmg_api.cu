@@ -951,6 +951,9 @@ struct mrmg_node_store {
   int* d_qmode = nullptr;            // exact path: uploaded query modes
   long long qmode_cap = 0;
   long long last_fallback = 0;
+  std::vector<long long> h_mode_off;
+  NearState* near = nullptr;         // radius queries: scratch and the last result
+  bool near_valid = false;
 };
 
 extern "C" {
@@ -976,6 +979,8 @@ int mrmg_node_store_create(const double* d_nodes, int64_t M, int32_t D, const in
   s->M = M;
   s->nodes = d_nodes;
   s->scratch = knn_scratch_new();
+  s->near = near_state_new();
+  s->h_mode_off.assign(h_mode_offsets, h_mode_offsets + n_modes + 1);
   cudaError_t e = cudaMalloc(&s->d_mode_off, sizeof(long long) * (n_modes + 1));
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(s->d_mode_off, h_mode_offsets, sizeof(long long) * (n_modes + 1), cudaMemcpyHostToDevice, st);
@@ -993,6 +998,7 @@ int mrmg_node_store_destroy(mrmg_node_store* s) {
   if (!s) return MRMG_OK;
   knn_store_delete(s->tc);
   knn_scratch_delete(s->scratch);
+  near_state_delete(s->near);
   if (s->d_mode_off) cudaFree(s->d_mode_off);
   if (s->d_qmode) cudaFree(s->d_qmode);
   delete s;
@@ -1032,6 +1038,46 @@ int mrmg_knn(mrmg_node_store* s, const double* d_queries, int64_t Q, const int32
   s->last_fallback = nfb;
   if (out_stats2) { out_stats2[0] = tc ? 1 : 0; out_stats2[1] = nfb; }
   return MRMG_OK;
+}
+
+int mrmg_near(mrmg_node_store* s, const double* d_queries, int64_t Q, const int32_t* h_query_mode,
+              const double* h_radius, double add_eps, int64_t* d_offsets, int64_t* d_idx, double* d_dist, int64_t cap,
+              int64_t* out_total, void* stream) {
+  if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
+  if (Q < 0 || cap < 0) return fail(MRMG_ERR_ARG, "Q / cap must be >= 0");
+  if (!d_offsets || !out_total) return fail(MRMG_ERR_ARG, "NULL offsets / total");
+  if (Q > 0 && (!d_queries || !h_query_mode || !h_radius)) return fail(MRMG_ERR_ARG, "NULL pointer");
+  if (cap > 0 && (!d_idx || !d_dist)) return fail(MRMG_ERR_ARG, "NULL output with cap > 0");
+  if (!(add_eps >= 0.0)) return fail(MRMG_ERR_ARG, "add_eps must be >= 0");
+  for (long long q = 0; q < Q; q++)
+    if (h_query_mode[q] < 0 || h_query_mode[q] >= s->n_modes) return fail(MRMG_ERR_ARG, "query %lld: mode out of range", q);
+  cudaStream_t st = (cudaStream_t)stream;
+  s->near_valid = false;
+  *out_total = 0;
+  if (Q == 0) {
+    cudaError_t e = cudaMemsetAsync(d_offsets, 0, sizeof(int64_t), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "near");
+  }
+  long long total = 0;
+  cudaError_t e = near_query(s->near, s->tc, s->nodes, s->d_mode_off, s->h_mode_off.data(), s->n_modes, s->t,
+                             s->metric, d_queries, Q, h_query_mode, h_radius, add_eps, (long long*)d_offsets,
+                             (long long*)d_idx, d_dist, cap, device_sms(), &total, st);
+  if (e == cudaErrorLaunchTimeout) return fail(MRMG_ERR_TIMEOUT, "a bounded tensor-core pipeline wait ran out");
+  if (e != cudaSuccess) return cuda_fail(e, "near");
+  s->near_valid = true;
+  *out_total = total;
+  return MRMG_OK;
+}
+
+int mrmg_near_fetch(mrmg_node_store* s, int64_t* d_idx, double* d_dist, int64_t cap, void* stream) {
+  if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
+  if (!s->near_valid) return fail(MRMG_ERR_ARG, "no radius query to fetch");
+  if (cap < near_last_total(s->near)) return fail(MRMG_ERR_ARG, "cap %lld < total %lld", (long long)cap,
+                                                    near_last_total(s->near));
+  if (cap > 0 && (!d_idx || !d_dist)) return fail(MRMG_ERR_ARG, "NULL output");
+  cudaError_t e = near_fetch(s->near, (long long*)d_idx, d_dist, cap, device_sms(), (cudaStream_t)stream);
+  return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "near fetch");
 }
 
 int mrmg_selftest_umma(const void* d_a, const void* d_b, int32_t n, float* d_c, void* stream) {

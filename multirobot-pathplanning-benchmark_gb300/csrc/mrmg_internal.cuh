@@ -184,6 +184,16 @@ KnnStore* knn_store_new();
 void knn_store_delete(KnnStore* s);
 KnnScratch* knn_scratch_new();
 void knn_scratch_delete(KnnScratch* s);
+struct NearState;
+NearState* near_state_new();
+void near_state_delete(NearState* ns);
+cudaError_t near_query(NearState* ns, KnnStore* tc, const double* nodes, const long long* d_mode_off,
+                       const long long* h_mode_off, int n_modes, const SliceTab& t, int metric, const double* d_qs,
+                       long long Q, const int* h_q_mode, const double* h_radius, double add_eps,
+                       long long* d_offsets, long long* d_idx, double* d_dist, long long cap, int num_sms,
+                       long long* total_out, cudaStream_t st);
+cudaError_t near_fetch(NearState* ns, long long* d_idx, double* d_dist, long long cap, int num_sms, cudaStream_t st);
+long long near_last_total(const NearState* ns);
 cudaError_t umma_selftest(const void* A, const void* B, int N, float* C, int* err, cudaStream_t st);
 
 cudaError_t dist_matrix(const double* qs, long long Q, const double* nodes, long long M, const SliceTab& t, int metric,

@@ -438,14 +438,37 @@ __device__ __forceinline__ void keep_chunk(float (&kd)[kKeep], int (&ki)[kKeep],
   }
 }
 
+// Radius mode: each thread's 32 columns of a chunk are 32 consecutive
+// mode-local nodes starting on a multiple of 32, so the chunk's verdicts are
+// one whole word of the query's candidate bitmap, written by exactly this
+// thread (no atomics, no list capacity).
+struct RadOut {
+  unsigned* bits;                   // word w of query q at bits[woff[q] + w]
+  const long long* woff;            // [Q + 1]
+  const float* rad2;                // per query: (radius + eps)^2 rounded up (or -1)
+};
+
+template <bool FROM_DOT>
+__device__ __forceinline__ void rad_chunk(const float (&v)[32], float qn, float tau, long long qid, int col0,
+                                          const RadOut& ro) {
+  if (qid < 0) return;
+  unsigned m = 0;
+#pragma unroll
+  for (int i = 0; i < 32; i++) {
+    const float d = FROM_DOT ? fmaf(-2.f, v[i], qn) : v[i];
+    if (d <= tau) m |= 1u << i;
+  }
+  ro.bits[ro.woff[qid] + (col0 >> 5)] = m;
+}
+
 template <int FMT> struct TcSplit { static constexpr int S = FMT == KNN_FMT_EUCL ? 4 : 2; };
 
-template <int FMT>
+template <int FMT, bool RAD>
 __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnStoreDev st, const double* __restrict__ qs,
                                                         const int* __restrict__ qorder, const KnnItem* __restrict__ items,
                                                         int chunks_max, float* __restrict__ cand_d,
                                                         int* __restrict__ cand_i, float* __restrict__ q_eps,
-                                                        int* __restrict__ err) {
+                                                        int* __restrict__ err, RadOut ro) {
   constexpr int NT = FMT == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
   constexpr uint32_t BT = NT * kRowBytes;   // bytes per node tile
   constexpr int S = TcSplit<FMT>::S, NCOL = NT / S;
@@ -461,6 +484,8 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   __shared__ uint32_t tbase;
   __shared__ int s_fail;
   __shared__ float s_qn[kTileM], s_qna[4][kTileM];
+  __shared__ float s_tau[RAD ? kTileM : 1];
+  __shared__ long long s_qid[RAD ? kTileM : 1];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row = tid & (kTileM - 1), slice = tid / kTileM;
   const KnnItem it = items[blockIdx.x];
@@ -518,11 +543,12 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
       }
       // error bound of the approximate squared distance (split-BF16 operands,
       // FP32 accumulation), per query; stored once per query
-      if (it.chunk == 0) {
-        const float s = sqrtf(qn) + st.mode_xmax[it.mode];
-        q_eps[qid] = 1.2e-4f * s * s + 1e-30f;
-      }
+      const float es = sqrtf(qn) + st.mode_xmax[it.mode];
+      const float eps = 1.2e-4f * es * es + 1e-30f;
+      if (!RAD && it.chunk == 0) q_eps[qid] = eps;
+      if (RAD) s_tau[r] = ro.rad2[qid] < 0.f ? -__int_as_float(0x7f800000) : ro.rad2[qid] + 1.0001f * eps;
     }
+    if (RAD) s_qid[r] = qid;
     s_qn[r] = qn;
     for (int a = 0; a < 4; a++) s_qna[a][r] = qna[a];
   }
@@ -586,7 +612,8 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
         for (int c0 = slice * NCOL; c0 < slice * NCOL + NCOL; c0 += 32) {
           float v[32];
           tmem_ld32(lane_base + c0, v);
-          keep_chunk<true>(kd, ki, v, qn, cand, col_node0 + c0);
+          if (RAD) rad_chunk<true>(v, qn, s_tau[row], s_qid[row], col_node0 + c0, ro);
+          else keep_chunk<true>(kd, ki, v, qn, cand, col_node0 + c0);
         }
       } else {
 #pragma unroll 1
@@ -601,7 +628,8 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
 #pragma unroll
             for (int i = 0; i < 32; i++) m[i] = fmaxf(m[i], fmaf(-2.f, v[i], qa));
           }
-          keep_chunk<false>(kd, ki, m, 0.f, cand, col_node0 + c0);
+          if (RAD) rad_chunk<false>(m, 0.f, s_tau[row], s_qid[row], col_node0 + c0, ro);
+          else keep_chunk<false>(kd, ki, m, 0.f, cand, col_node0 + c0);
         }
       }
     }
@@ -614,7 +642,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   (void)lane;
   // merge the slices' lists into slice 0's; every MMA has completed, so the
   // operand buffers are free (skipped after a timeout: copies may be in flight)
-  if (!s_fail) {
+  if (!RAD && !s_fail) {
     float* md = (float*)base;
     int* mi = (int*)(base + (size_t)(S - 1) * kTileM * kKeep * sizeof(float));
     if (slice > 0) {
@@ -634,7 +662,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
         }
     }
   }
-  if (qid >= 0) {
+  if (!RAD && qid >= 0) {
     float* od = cand_d + ((size_t)qid * chunks_max + it.chunk) * kKeep;
     int* oi = cand_i + ((size_t)qid * chunks_max + it.chunk) * kKeep;
 #pragma unroll
@@ -757,6 +785,159 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
   }
 }
 
+// ---------------------------------------------------------------------------
+// radius queries: exact re-check of the candidate bitmap, scan, ordered emit
+// ---------------------------------------------------------------------------
+constexpr int kNearWarps = 4;
+
+// Each warp takes a query and walks its bitmap 32 words (1024 nodes) at a
+// time: the set bits are listed in shared memory and spread over the lanes for
+// the FP64 distance, so a dense word does not serialise one lane.  Bits whose
+// exact distance exceeds the query's r' (or past the mode's nodes) are cleared.
+__global__ void near_exact_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
+                                  const double* __restrict__ nodes, const long long* __restrict__ mode_off, SliceTab t,
+                                  int metric, const double* __restrict__ rp, const long long* __restrict__ woff,
+                                  unsigned* __restrict__ bits, long long* __restrict__ counts) {
+  __shared__ int s_list[kNearWarps][1024];
+  __shared__ unsigned s_res[kNearWarps][32];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long warp = (long long)blockIdx.x * kNearWarps + wib;
+  const long long nwarps = (long long)gridDim.x * kNearWarps;
+  int* list = s_list[wib];
+  for (long long q = warp; q < Q; q += nwarps) {
+    const int m = q_mode[q];
+    const long long M = mode_off[m + 1] - mode_off[m];
+    const double* xb = nodes + mode_off[m] * t.D;
+    const double* qq = qs + q * t.D;
+    const long long w0 = woff[q], W = woff[q + 1] - w0;
+    const double r = rp[q];
+    long long cnt = 0;
+    for (long long base = 0; base < W; base += 32) {
+      const long long w = base + lane;
+      const unsigned mk = w < W ? bits[w0 + w] : 0u;
+      const int c = __popc(mk);
+      int incl = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(MRMG_FULL, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int n = __shfl_sync(MRMG_FULL, incl, 31);
+      if (n == 0) continue;
+      int pos = incl - c;
+      unsigned mm = mk;
+      while (mm) {
+        const int b = __ffs(mm) - 1;
+        mm &= mm - 1;
+        list[pos++] = lane * 32 + b;
+      }
+      s_res[wib][lane] = 0u;
+      __syncwarp();
+      for (int x = lane; x < n; x += 32) {
+        const int loc = list[x];
+        const long long id = base * 32 + loc;
+        if (id >= M) continue;
+        const double* xx = xb + id * t.D;
+        auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
+        if (dist_of(t, metric, dfun) <= r) atomicOr(&s_res[wib][loc >> 5], 1u << (loc & 31));
+      }
+      __syncwarp();
+      const unsigned res = s_res[wib][lane];
+      if (w < W) bits[w0 + w] = res;
+      cnt += __popc(res);
+      __syncwarp();
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(MRMG_FULL, cnt, o);
+    if (lane == 0) counts[q] = cnt;
+  }
+}
+
+// exclusive scan of the per-query counts into offsets[Q + 1] (one block; the
+// query counts of a planner batch are thousands, not millions)
+__global__ void near_scan_kernel(const long long* __restrict__ counts, long long Q, long long* __restrict__ offs_user,
+                                 long long* __restrict__ offs, long long* __restrict__ total) {
+  __shared__ long long s[1024];
+  const int tid = threadIdx.x;
+  const long long per = (Q + 1023) / 1024;
+  const long long lo = tid * per < Q ? tid * per : Q, hi = lo + per < Q ? lo + per : Q;
+  long long sum = 0;
+  for (long long i = lo; i < hi; i++) sum += counts[i];
+  s[tid] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const long long y = tid >= o ? s[tid - o] : 0;
+    __syncthreads();
+    s[tid] += y;
+    __syncthreads();
+  }
+  long long run = s[tid] - sum;
+  for (long long i = lo; i < hi; i++) {
+    offs[i] = run;
+    if (offs_user) offs_user[i] = run;
+    run += counts[i];
+  }
+  if (tid == 1023) {
+    offs[Q] = s[1023];
+    if (offs_user) offs_user[Q] = s[1023];
+    *total = s[1023];
+  }
+}
+
+// ascending mode-local indices and their FP64 distances, written from
+// offsets[q]; positions at or past `cap` are skipped
+__global__ void near_emit_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
+                                 const double* __restrict__ nodes, const long long* __restrict__ mode_off, SliceTab t,
+                                 int metric, const long long* __restrict__ woff, const unsigned* __restrict__ bits,
+                                 const long long* __restrict__ offs, long long cap, long long* __restrict__ out_idx,
+                                 double* __restrict__ out_dist) {
+  __shared__ int s_list[kNearWarps][1024];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long warp = (long long)blockIdx.x * kNearWarps + wib;
+  const long long nwarps = (long long)gridDim.x * kNearWarps;
+  int* list = s_list[wib];
+  for (long long q = warp; q < Q; q += nwarps) {
+    long long o = offs[q];
+    if (o >= cap || offs[q + 1] == o) continue;
+    const int m = q_mode[q];
+    const double* xb = nodes + mode_off[m] * t.D;
+    const double* qq = qs + q * t.D;
+    const long long w0 = woff[q], W = woff[q + 1] - w0;
+    for (long long base = 0; base < W && o < cap; base += 32) {
+      const long long w = base + lane;
+      const unsigned mk = w < W ? bits[w0 + w] : 0u;
+      const int c = __popc(mk);
+      int incl = c;
+#pragma unroll
+      for (int sh = 1; sh < 32; sh <<= 1) {
+        const int y = __shfl_up_sync(MRMG_FULL, incl, sh);
+        if (lane >= sh) incl += y;
+      }
+      const int n = __shfl_sync(MRMG_FULL, incl, 31);
+      if (n == 0) continue;
+      int pos = incl - c;
+      unsigned mm = mk;
+      while (mm) {
+        const int b = __ffs(mm) - 1;
+        mm &= mm - 1;
+        list[pos++] = lane * 32 + b;
+      }
+      __syncwarp();
+      for (int x = lane; x < n; x += 32) {
+        const long long p = o + x;
+        if (p >= cap) break;
+        const long long id = base * 32 + list[x];
+        const double* xx = xb + id * t.D;
+        auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
+        out_idx[p] = id;
+        out_dist[p] = dist_of(t, metric, dfun);
+      }
+      o += n;
+      __syncwarp();
+    }
+  }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -850,20 +1031,27 @@ struct KnnScratch {
   size_t host_bytes = 0;
 };
 
-cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h_q_mode, int k, long long* d_idx,
-                      double* d_dist, KnnScratch* scr, int num_sms, int* n_fallback_out, cudaStream_t st) {
+// queries grouped by mode (order), and work items: query tiles x node-tile
+// chunks, about three waves of CTAs, at most 64 chunks per mode
+struct ItemPlan {
+  std::vector<int> order, qcount, qstart, mode_chunks;
+  std::vector<KnnItem> items;
+  int chunks_max = 1;
+};
+
+static void plan_items(const KnnStore* s, const int* h_q_mode, long long Q, int num_sms, ItemPlan* pl) {
   const int n_modes = s->n_modes;
-  // group queries by mode
-  std::vector<int> order(Q), qcount(n_modes, 0), qstart(n_modes + 1, 0);
-  for (long long q = 0; q < Q; q++) qcount[h_q_mode[q]]++;
-  for (int m = 0; m < n_modes; m++) qstart[m + 1] = qstart[m] + qcount[m];
+  pl->order.assign(Q, 0);
+  pl->qcount.assign(n_modes, 0);
+  pl->qstart.assign(n_modes + 1, 0);
+  for (long long q = 0; q < Q; q++) pl->qcount[h_q_mode[q]]++;
+  for (int m = 0; m < n_modes; m++) pl->qstart[m + 1] = pl->qstart[m] + pl->qcount[m];
   {
-    std::vector<int> fill(qstart.begin(), qstart.end() - 1);
-    for (long long q = 0; q < Q; q++) order[fill[h_q_mode[q]]++] = (int)q;
+    std::vector<int> fill(pl->qstart.begin(), pl->qstart.end() - 1);
+    for (long long q = 0; q < Q; q++) pl->order[fill[h_q_mode[q]]++] = (int)q;
   }
-  // work items: query tiles x node-tile chunks, about three waves of CTAs
   long long units = 0;
-  for (int m = 0; m < n_modes; m++) units += (long long)((qcount[m] + kTileM - 1) / kTileM) * s->mode_tiles[m];
+  for (int m = 0; m < n_modes; m++) units += (long long)((pl->qcount[m] + kTileM - 1) / kTileM) * s->mode_tiles[m];
   const long long target = std::max(1, 3 * num_sms);
   int tpc = (int)std::max<long long>(1, (units + target - 1) / target);
   int chunks_max = 1;
@@ -873,25 +1061,62 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
     chunks_max = 1;
     for (int m = 0; m < n_modes; m++) chunks_max = std::max(chunks_max, (s->mode_tiles[m] + tpc - 1) / tpc);
   }
-  std::vector<KnnItem> items;
-  std::vector<int> mode_chunks(n_modes, 0);
+  pl->chunks_max = chunks_max;
+  pl->items.clear();
+  pl->mode_chunks.assign(n_modes, 0);
   for (int m = 0; m < n_modes; m++) {
-    if (qcount[m] == 0 || s->mode_tiles[m] == 0) continue;
+    if (pl->qcount[m] == 0 || s->mode_tiles[m] == 0) continue;
     const int nch = (s->mode_tiles[m] + tpc - 1) / tpc;
-    mode_chunks[m] = nch;
-    for (int q0 = 0; q0 < qcount[m]; q0 += kTileM)
+    pl->mode_chunks[m] = nch;
+    for (int q0 = 0; q0 < pl->qcount[m]; q0 += kTileM)
       for (int c = 0; c < nch; c++) {
         KnnItem it;
         it.mode = m;
-        it.q0 = qstart[m] + q0;
-        it.qn = std::min(kTileM, qcount[m] - q0);
+        it.q0 = pl->qstart[m] + q0;
+        it.qn = std::min(kTileM, pl->qcount[m] - q0);
         it.tile0 = c * tpc;
         it.tile1 = std::min(s->mode_tiles[m], (c + 1) * tpc);
         it.chunk = c;
         it.pad = 0;
-        items.push_back(it);
+        pl->items.push_back(it);
       }
   }
+}
+
+static size_t tc_smem_bytes(const KnnStore* s) {
+  const int NT = s->dev.NT;
+  const int nthreads = 128 * (s->dev.fmt == KNN_FMT_EUCL ? TcSplit<KNN_FMT_EUCL>::S : TcSplit<KNN_FMT_AGENT>::S);
+  return std::max<size_t>(1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes +
+                              32 * sizeof(float) * (size_t)nthreads,
+                          120 * 1024);
+}
+
+// the attribute is per function: raise it once, to the opt-in limit less the
+// kernel's static shared memory
+template <int FMT, bool RAD>
+static void raise_smem_limit() {
+  static bool done = false;
+  if (done) return;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, knn_tc_kernel<FMT, RAD>) == cudaSuccess)
+    cudaFuncSetAttribute(knn_tc_kernel<FMT, RAD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         optin - (int)fa.sharedSizeBytes);
+  cudaGetLastError();
+  done = true;
+}
+
+cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h_q_mode, int k, long long* d_idx,
+                      double* d_dist, KnnScratch* scr, int num_sms, int* n_fallback_out, cudaStream_t st) {
+  const int n_modes = s->n_modes;
+  ItemPlan pl;
+  plan_items(s, h_q_mode, Q, num_sms, &pl);
+  const std::vector<int>& order = pl.order;
+  const std::vector<KnnItem>& items = pl.items;
+  const std::vector<int>& mode_chunks = pl.mode_chunks;
+  const int chunks_max = pl.chunks_max;
   // scratch: order, q_mode, items, mode_chunks, cand lists, eps, fallback list, counters
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t b_order = al(sizeof(int) * std::max<long long>(Q, 1));
@@ -941,37 +1166,18 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   cudaError_t e = cudaMemcpyAsync(d_order, hp, b_up, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, 256, st);
   if (e != cudaSuccess) return e;
-  const int NT = s->dev.NT;
   // at least 120 KB of shared memory: one CTA per SM, so two CTAs never wait
   // on each other for the 512 tensor-memory columns each allocates
-  const int nthreads = 128 * (s->dev.fmt == KNN_FMT_EUCL ? TcSplit<KNN_FMT_EUCL>::S : TcSplit<KNN_FMT_AGENT>::S);
-  const size_t smem = std::max<size_t>(1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes +
-                                           32 * sizeof(float) * (size_t)nthreads,
-                                       120 * 1024);
-  // the attribute is per function: raise it once, to the opt-in limit less
-  // the kernel's static shared memory
-  static bool attr_set = false;
-  if (!attr_set) {
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, knn_tc_kernel<KNN_FMT_EUCL>) == cudaSuccess)
-      cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_EUCL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           optin - (int)fa.sharedSizeBytes);
-    if (cudaFuncGetAttributes(&fa, knn_tc_kernel<KNN_FMT_AGENT>) == cudaSuccess)
-      cudaFuncSetAttribute(knn_tc_kernel<KNN_FMT_AGENT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           optin - (int)fa.sharedSizeBytes);
-    cudaGetLastError();
-    attr_set = true;
-  }
+  const size_t smem = tc_smem_bytes(s);
+  raise_smem_limit<KNN_FMT_EUCL, false>();
+  raise_smem_limit<KNN_FMT_AGENT, false>();
   if (!items.empty()) {
     if (s->dev.fmt == KNN_FMT_EUCL) {
-      knn_tc_kernel<KNN_FMT_EUCL><<<(int)items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
-                                                                         d_cd, d_ci, d_eps, d_ctr + 1);
+      knn_tc_kernel<KNN_FMT_EUCL, false><<<(int)items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
+                                                                         d_cd, d_ci, d_eps, d_ctr + 1, RadOut{});
     } else {
-      knn_tc_kernel<KNN_FMT_AGENT><<<(int)items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
-                                                                          d_cd, d_ci, d_eps, d_ctr + 1);
+      knn_tc_kernel<KNN_FMT_AGENT, false><<<(int)items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
+                                                                          d_cd, d_ci, d_eps, d_ctr + 1, RadOut{});
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -994,6 +1200,175 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   }
   return cudaSuccess;
 }
+
+// ---------------------------------------------------------------------------
+// radius queries (host)
+// ---------------------------------------------------------------------------
+struct NearState {
+  KnnScratch scr;
+  // the last query, kept for near_fetch
+  const double* qs = nullptr;
+  long long Q = 0;
+  const double* nodes = nullptr;
+  const long long* mode_off = nullptr;
+  SliceTab t{};
+  int metric = 0;
+  const int* qmode = nullptr;
+  const long long* woff = nullptr;
+  const unsigned* bits = nullptr;
+  const long long* offs = nullptr;
+  long long total = 0;
+};
+
+NearState* near_state_new() { return new NearState(); }
+void near_state_delete(NearState* ns) {
+  if (!ns) return;
+  if (ns->scr.block) cudaFree(ns->scr.block);
+  if (ns->scr.host) cudaFreeHost(ns->scr.host);
+  delete ns;
+}
+
+static int near_grid(long long Q, int num_sms) {
+  return (int)std::max<long long>(1, std::min<long long>((Q + kNearWarps - 1) / kNearWarps, (long long)num_sms * 16));
+}
+
+// f32 value >= x^2 (x >= 0 finite), +inf for +inf, -1 for x < 0 or NaN (nothing within)
+static float rad2_up(double x) {
+  if (!(x >= 0.0)) return -1.f;
+  const double x2 = x * x;
+  if (x2 > 3.0e38) return __builtin_huge_valf();
+  const float f = (float)x2;
+  return (double)f >= x2 ? f : std::nextafter(f, __builtin_huge_valf());
+}
+
+cudaError_t near_query(NearState* ns, KnnStore* tc, const double* nodes, const long long* d_mode_off,
+                       const long long* h_mode_off, int n_modes, const SliceTab& t, int metric, const double* d_qs,
+                       long long Q, const int* h_q_mode, const double* h_radius, double add_eps,
+                       long long* d_offsets, long long* d_idx, double* d_dist, long long cap, int num_sms,
+                       long long* total_out, cudaStream_t st) {
+  // words of each query's bitmap: whole node tiles on the tensor-core path
+  // (every word is written by the candidate kernel), else ceil(M / 32)
+  std::vector<long long> words(n_modes);
+  for (int m = 0; m < n_modes; m++) {
+    const long long M = h_mode_off[m + 1] - h_mode_off[m];
+    words[m] = tc ? (long long)tc->mode_tiles[m] * tc->dev.NT / 32 : (M + 31) / 32;
+  }
+  ItemPlan pl;
+  if (tc) plan_items(tc, h_q_mode, Q, num_sms, &pl);
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b_order = al(sizeof(int) * std::max<long long>(Q, 1));
+  const size_t b_qmode = b_order;
+  const size_t b_items = al(sizeof(KnnItem) * std::max<size_t>(pl.items.size(), 1));
+  const size_t b_woff = al(sizeof(long long) * (Q + 1));
+  const size_t b_rp = al(sizeof(double) * std::max<long long>(Q, 1));
+  const size_t b_rad2 = al(sizeof(float) * std::max<long long>(Q, 1));
+  const size_t b_up = b_order + b_qmode + b_items + b_woff + b_rp + b_rad2;
+  // host tables
+  if (ns->scr.host_bytes < b_up + 256) {
+    if (ns->scr.host) cudaFreeHost(ns->scr.host);
+    ns->scr.host = nullptr;
+    ns->scr.host_bytes = 0;
+    cudaError_t e = cudaMallocHost(&ns->scr.host, b_up + 256);
+    if (e != cudaSuccess) return e;
+    ns->scr.host_bytes = b_up + 256;
+  }
+  unsigned char* hp = (unsigned char*)ns->scr.host;
+  long long* h_woff = (long long*)(hp + b_order + b_qmode + b_items);
+  double* h_rp = (double*)(hp + b_order + b_qmode + b_items + b_woff);
+  float* h_rad2 = (float*)(hp + b_order + b_qmode + b_items + b_woff + b_rp);
+  h_woff[0] = 0;
+  for (long long q = 0; q < Q; q++) {
+    h_woff[q + 1] = h_woff[q] + words[h_q_mode[q]];
+    h_rp[q] = h_radius[q] + add_eps;     // the reference's r += eps, in FP64
+    h_rad2[q] = rad2_up(h_rp[q]);
+  }
+  const long long Wtot = h_woff[Q];
+  if (tc) std::memcpy(hp, pl.order.data(), sizeof(int) * Q);
+  std::memcpy(hp + b_order, h_q_mode, sizeof(int) * Q);
+  if (!pl.items.empty()) std::memcpy(hp + b_order + b_qmode, pl.items.data(), sizeof(KnnItem) * pl.items.size());
+  long long* h_ctr = (long long*)(hp + b_up);
+  // device: the uploaded tables, then bitmap, counts, offsets, counters
+  const size_t b_bits = al(sizeof(unsigned) * std::max<long long>(Wtot, 1));
+  const size_t b_cnt = al(sizeof(long long) * std::max<long long>(Q, 1));
+  const size_t b_offs = al(sizeof(long long) * (Q + 1));
+  const size_t need = b_up + b_bits + b_cnt + b_offs + 256;
+  if (ns->scr.bytes < need) {
+    if (ns->scr.block) cudaFree(ns->scr.block);
+    ns->scr.block = nullptr;
+    ns->scr.bytes = 0;
+    cudaError_t e = cudaMalloc(&ns->scr.block, need);
+    if (e != cudaSuccess) return e;
+    ns->scr.bytes = need;
+  }
+  unsigned char* p = (unsigned char*)ns->scr.block;
+  int* d_order = (int*)p;
+  int* d_qmode = (int*)(p + b_order);
+  KnnItem* d_items = (KnnItem*)(p + b_order + b_qmode);
+  long long* d_woff = (long long*)(p + b_order + b_qmode + b_items);
+  double* d_rp = (double*)(p + b_order + b_qmode + b_items + b_woff);
+  float* d_rad2 = (float*)(p + b_order + b_qmode + b_items + b_woff + b_rp);
+  unsigned* d_bits = (unsigned*)(p + b_up);
+  long long* d_cnt = (long long*)(p + b_up + b_bits);
+  long long* d_offs = (long long*)(p + b_up + b_bits + b_cnt);
+  long long* d_ctr = (long long*)(p + b_up + b_bits + b_cnt + b_offs);   // [0] total, [1] error bits
+  cudaError_t e = cudaMemcpyAsync(p, hp, b_up, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, 256, st);
+  if (e != cudaSuccess) return e;
+  if (tc && !pl.items.empty()) {
+    const size_t smem = tc_smem_bytes(tc);
+    const RadOut ro{d_bits, d_woff, d_rad2};
+    if (tc->dev.fmt == KNN_FMT_EUCL) {
+      raise_smem_limit<KNN_FMT_EUCL, true>();
+      knn_tc_kernel<KNN_FMT_EUCL, true><<<(int)pl.items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(
+          tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, (int*)(d_ctr + 1), ro);
+    } else {
+      raise_smem_limit<KNN_FMT_AGENT, true>();
+      knn_tc_kernel<KNN_FMT_AGENT, true><<<(int)pl.items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(
+          tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, (int*)(d_ctr + 1), ro);
+    }
+  } else if (!tc && Wtot > 0) {
+    e = cudaMemsetAsync(d_bits, 0xff, sizeof(unsigned) * Wtot, st);   // every node is a candidate
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int grid = near_grid(Q, num_sms);
+  near_exact_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, d_mode_off, t, metric, d_rp, d_woff,
+                                                      d_bits, d_cnt);
+  near_scan_kernel<<<1, 1024, 0, st>>>(d_cnt, Q, d_offsets, d_offs, d_ctr);
+  if (cap > 0)
+    near_emit_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, d_mode_off, t, metric, d_woff, d_bits,
+                                                       d_offs, cap, d_idx, d_dist);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_ctr, d_ctr, 2 * sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  if (h_ctr[1]) return cudaErrorLaunchTimeout;
+  ns->qs = d_qs;
+  ns->Q = Q;
+  ns->nodes = nodes;
+  ns->mode_off = d_mode_off;
+  ns->t = t;
+  ns->metric = metric;
+  ns->qmode = d_qmode;
+  ns->woff = d_woff;
+  ns->bits = d_bits;
+  ns->offs = d_offs;
+  ns->total = h_ctr[0];
+  *total_out = h_ctr[0];
+  return cudaSuccess;
+}
+
+cudaError_t near_fetch(NearState* ns, long long* d_idx, double* d_dist, long long cap, int num_sms, cudaStream_t st) {
+  if (ns->Q == 0 || cap <= 0) return cudaSuccess;
+  near_emit_kernel<<<near_grid(ns->Q, num_sms), 32 * kNearWarps, 0, st>>>(
+      ns->qs, ns->Q, ns->qmode, ns->nodes, ns->mode_off, ns->t, ns->metric, ns->woff, ns->bits, ns->offs, cap, d_idx,
+      d_dist);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
+}
+
+long long near_last_total(const NearState* ns) { return ns->total; }
 
 KnnStore* knn_store_new() { return new KnnStore(); }
 void knn_store_delete(KnnStore* s) {

@@ -92,3 +92,32 @@ class NodeStore:
                                      dist.data_ptr(), st.ctypes.data, _lib.stream_handle(stream)), "knn")
         self.last_stats = {"tensor_core": bool(st[0]), "rerun_exact": int(st[1])}
         return idx, dist
+
+    def near(self, queries, query_mode, radius, add_eps: float = 1e-10, cap: int | None = None, stream=None):
+        """Radius neighbours, as RRT* near / find_nearest_indices
+        (planners/rrtstar_base.py:439-453, 1296-1337): per query every node of
+        its mode with distance <= radius + add_eps, ascending mode-local index.
+        ``radius`` is a scalar or one value per query.  Returns CSR device
+        tensors (offsets [Q + 1], idx [total], dist [total] float64)."""
+        qs = _dev_tensor(queries, dtype=torch.float64)
+        qm = np.ascontiguousarray(np.asarray(query_mode, dtype=np.int32).reshape(-1))
+        Q = qs.shape[0]
+        if qm.shape[0] != Q:
+            raise ValueError("one mode per query")
+        r = np.ascontiguousarray(np.broadcast_to(np.asarray(radius, dtype=np.float64), (Q,)))
+        if cap is None:
+            cap = max(1024, 64 * Q)
+        offs = torch.empty(Q + 1, dtype=torch.int64, device=qs.device)
+        idx = torch.empty(max(cap, 1), dtype=torch.int64, device=qs.device)
+        dist = torch.empty(max(cap, 1), dtype=torch.float64, device=qs.device)
+        tot = np.zeros(1, dtype=np.int64)
+        _lib.check(self.lib.mrmg_near(self.h, qs.data_ptr(), Q, qm.ctypes.data, r.ctypes.data, float(add_eps),
+                                      offs.data_ptr(), idx.data_ptr(), dist.data_ptr(), int(cap), tot.ctypes.data,
+                                      _lib.stream_handle(stream)), "near")
+        total = int(tot[0])
+        if total > cap:
+            idx = torch.empty(total, dtype=torch.int64, device=qs.device)
+            dist = torch.empty(total, dtype=torch.float64, device=qs.device)
+            _lib.check(self.lib.mrmg_near_fetch(self.h, idx.data_ptr(), dist.data_ptr(), total,
+                                                _lib.stream_handle(stream)), "near fetch")
+        return offs, idx[:total], dist[:total]

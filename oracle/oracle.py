@@ -277,5 +277,28 @@ def knn(qs, q_mode, nodes, mode_off, slices, metric, k):
     return idx, dist
 
 
+def near(qs, q_mode, nodes, mode_off, slices, metric, radius, add_eps=1e-10):
+    """Radius neighbours per mode as RRT* near (planners/rrtstar_base.py:1296-1337)
+    selects them: batch_config_dist of the query against its mode's nodes, then
+    find_nearest_indices (rrtstar_base.py:439-453): r += 1e-10 in FP64 and
+    np.nonzero(dists <= r), ascending.  CSR result (offsets, idx, dist)."""
+    qs = _c(qs, np.float64)
+    q_mode = np.asarray(q_mode).reshape(-1)
+    nodes = _c(nodes, np.float64)
+    mode_off = np.asarray(mode_off, dtype=np.int64)
+    radius = np.broadcast_to(np.asarray(radius, dtype=np.float64), (len(qs),))
+    offs, idx, dist = [0], [], []
+    for i in range(len(qs)):
+        lo, hi = mode_off[q_mode[i]], mode_off[q_mode[i] + 1]
+        d = batch_dist(qs[i], nodes[lo:hi], slices, metric) if hi > lo else np.zeros(0)
+        r = radius[i] + add_eps
+        sel = np.nonzero(d <= r)[0]
+        idx.append(sel.astype(np.int64))
+        dist.append(d[sel])
+        offs.append(offs[-1] + len(sel))
+    cat = lambda xs, dt: np.concatenate(xs).astype(dt) if xs else np.zeros(0, dt)
+    return np.array(offs, dtype=np.int64), cat(idx, np.int64), cat(dist, np.float64)
+
+
 def num_threads() -> int:
     return int(lib().orc_num_threads())

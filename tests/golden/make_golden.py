@@ -20,6 +20,8 @@ Outputs (numpy .npz, seeded, small):
   primitives3d.npz       Rectangle / Sphere collides_with_sphere in 3-D, incl. near-tangent
   dist_cost.npz          batch_config_dist / batch_config_cost over several slicings
   knn.npz                per-mode k nearest (argpartition + argsort, prm_graph.py:446-447)
+  near.npz               per-mode radius neighbours (find_nearest_indices, rrtstar_base.py:439-453),
+                         radii on and around node distances so that the added 1e-10 decides
   known_answers.json     the reference tests' own known answers (tests/test.py)
 """
 from __future__ import annotations
@@ -295,8 +297,73 @@ def main(ref_root: str):
     del env.is_collision_free
     ka["path_free"] = bool(env.is_path_collision_free(path, resolution=0.5))
     (OUT / "known_answers.json").write_text(json.dumps(ka, indent=1))
+    make_near(cf)
     print("golden vectors written to", OUT)
 
 
+def make_near(cf):
+    """Radius neighbours per mode by the reference's own find_nearest_indices
+    over batch_config_dist (RRT* near, rrtstar_base.py:1296-1337)."""
+    src_mod = "multi_robot_multi_goal_planning.planners"
+    if src_mod not in sys.modules:
+        m = types.ModuleType(src_mod)
+        m.__path__ = [str(Path(cf.__file__).resolve().parents[2] / "planners")]
+        sys.modules[src_mod] = m
+    import importlib
+
+    rb = importlib.import_module(src_mod + ".rrtstar_base")
+    rng = np.random.default_rng(20)
+    D = 28
+    slices = [(7 * i, 7 * i + 7) for i in range(4)]
+    sizes = [400, 150, 33, 1, 0, 64]
+    nodes = np.concatenate([rng.normal(rng.uniform(-np.pi, np.pi, D), 0.3, (s, D)) for s in sizes])
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    Q = 96
+    qm = rng.integers(0, len(sizes), Q).astype(np.int32)
+    qs = np.empty((Q, D))
+    for i in range(Q):
+        lo, hi = off[qm[i]], off[qm[i] + 1]
+        if hi > lo and i % 4 != 3:     # near the mode's nodes, one query exactly on a node
+            base = nodes[rng.integers(lo, hi)]
+            qs[i] = base if i % 16 == 0 else base + rng.normal(0, 0.2, D)
+        else:
+            qs[i] = rng.uniform(-np.pi, np.pi, D)
+    res = {}
+    for metric in ["euclidean", "max_euclidean"]:
+        radius = np.empty(Q)
+        idx, offs = [], [0]
+        for i in range(Q):
+            arr = nodes[off[qm[i]]:off[qm[i] + 1]]
+            q = cf.NpConfiguration(qs[i], slices)
+            dists = cf.batch_config_dist(q, arr, metric) if len(arr) else np.zeros(0)
+            kind = i % 6
+            if len(dists) == 0:
+                r = 0.7
+            elif kind == 0:
+                r = float(np.quantile(dists, 0.1))
+            elif kind == 1:
+                r = float(dists[rng.integers(len(dists))])             # a node exactly on the radius
+            elif kind == 2:
+                r = float(dists[rng.integers(len(dists))]) - 0.5e-10   # inside only by the added 1e-10
+            elif kind == 3:
+                r = float(dists[rng.integers(len(dists))]) - 2e-10     # just outside
+            elif kind == 4:
+                r = 0.0
+            else:
+                r = float(dists.max()) * 1.01                          # the whole mode
+            radius[i] = r
+            sel = rb.find_nearest_indices(dists, r) if len(dists) else np.zeros(0, dtype=np.int64)
+            idx.append(np.asarray(sel, dtype=np.int64))
+            offs.append(offs[-1] + len(sel))
+        res[f"radius_{metric}"] = radius
+        res[f"offsets_{metric}"] = np.array(offs, dtype=np.int64)
+        res[f"idx_{metric}"] = np.concatenate(idx) if idx else np.zeros(0, dtype=np.int64)
+    np.savez_compressed(OUT / "near.npz", nodes=nodes, mode_off=off, queries=qs, q_mode=qm,
+                        slices=np.array(slices, dtype=np.int64), **res)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 2 and sys.argv[2] == "near":
+        make_near(import_reference(Path(sys.argv[1]))[2])
+    else:
+        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -91,3 +91,65 @@ def test_knn_store_other_metrics_and_edge_modes(gpu, oracle):
         oi, od = oracle.knn(qs, qm, nodes, off, sl, metric, k)
         assert np.array_equal(idx.cpu().numpy(), oi), (metric, k)
         assert np.array_equal(dist.cpu().numpy(), od), (metric, k)
+
+
+def _csr_equal(got, want):
+    offs, idx, dist = (x.cpu().numpy() for x in got)
+    wo, wi, wd = want
+    return np.array_equal(offs, wo) and np.array_equal(idx, wi) and np.array_equal(dist, wd)
+
+
+def test_near_golden(gpu, oracle):
+    """Radius neighbours on the tensor-core store against the reference's
+    find_nearest_indices (radii on, just inside and just outside node
+    distances by less than the added 1e-10; an empty and a one-node mode)."""
+    knn = pkg("knn")
+    g = golden("near.npz")
+    for metric in ["euclidean", "max_euclidean"]:
+        store = knn.NodeStore(g["nodes"], g["mode_off"], g["slices"], metric)
+        offs, idx, dist = store.near(g["queries"], g["q_mode"], g[f"radius_{metric}"])
+        assert np.array_equal(offs.cpu().numpy(), g[f"offsets_{metric}"]), metric
+        assert np.array_equal(idx.cpu().numpy(), g[f"idx_{metric}"]), metric
+        want = oracle.near(g["queries"], g["q_mode"], g["nodes"], g["mode_off"], g["slices"], metric,
+                           g[f"radius_{metric}"])
+        assert _csr_equal((offs, idx, dist), want), metric
+
+
+@pytest.mark.parametrize("metric", ["euclidean", "max_euclidean"])
+def test_near_workload_vs_oracle(gpu, oracle, metric):
+    """The per-mode workload at reduced size, radii at the 24th-nearest
+    distance (some lowered by 0.5e-10, so that only the added epsilon keeps the
+    node), a tiny output capacity (the fetch path) and r = 0."""
+    knn, scenes = pkg("knn"), pkg("scenes")
+    w = scenes.make_knn_workload(seed=4, n_nodes=40_000, n_queries=512)
+    _, od = oracle.knn(w["queries"], w["q_mode"], w["nodes"], w["mode_offsets"], w["slices"], metric, 24)
+    r = od[:, -1].copy()
+    r[::3] -= 0.5e-10
+    r[~np.isfinite(r)] = 1.0
+    store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], metric)
+    want = oracle.near(w["queries"], w["q_mode"], w["nodes"], w["mode_offsets"], w["slices"], metric, r)
+    assert want[0][-1] > 0
+    assert _csr_equal(store.near(w["queries"], w["q_mode"], r), want)
+    assert _csr_equal(store.near(w["queries"], w["q_mode"], r, cap=7), want)
+    z = oracle.near(w["queries"], w["q_mode"], w["nodes"], w["mode_offsets"], w["slices"], metric, 0.0)
+    assert _csr_equal(store.near(w["queries"], w["q_mode"], 0.0), z)
+
+
+def test_near_other_metrics_and_edge_modes(gpu, oracle):
+    """Metrics outside the tensor-core shapes check every node in FP64; empty
+    and tiny modes, negative and infinite radii, and no queries at all."""
+    knn = pkg("knn")
+    rng = np.random.default_rng(10)
+    nodes = rng.uniform(-2, 2, (2000, 14))
+    off = np.array([0, 0, 5, 1990, 2000])
+    qs = rng.uniform(-2, 2, (100, 14))
+    qm = rng.integers(0, 4, 100).astype(np.int32)
+    sl = [[0, 7], [7, 14]]
+    r = rng.uniform(0.5, 4.0, 100)
+    r[5], r[6] = -1.0, np.inf
+    for metric in ["sum_euclidean", "max", "euclidean", "max_euclidean"]:
+        store = knn.NodeStore(nodes, off, sl, metric)
+        want = oracle.near(qs, qm, nodes, off, sl, metric, r)
+        assert _csr_equal(store.near(qs, qm, r), want), metric
+        offs, idx, dist = store.near(qs[:0], qm[:0], 1.0)
+        assert offs.cpu().tolist() == [0] and idx.numel() == 0

@@ -121,6 +121,23 @@ def test_knn(oracle):
         assert np.array_equal(idx, g[f"idx_{metric}"]), metric
 
 
+def test_near(oracle):
+    """Radius neighbours against the reference's find_nearest_indices, with
+    radii on, just inside (by less than the added 1e-10) and just outside
+    node distances, r = 0 and whole modes; an empty and a one-node mode."""
+    g = golden("near.npz")
+    for metric in ["euclidean", "max_euclidean"]:
+        offs, idx, dist = oracle.near(g["queries"], g["q_mode"], g["nodes"], g["mode_off"], g["slices"], metric,
+                                      g[f"radius_{metric}"])
+        assert np.array_equal(offs, g[f"offsets_{metric}"]), metric
+        assert np.array_equal(idx, g[f"idx_{metric}"]), metric
+        assert np.all(dist <= g[f"radius_{metric}"][np.repeat(np.arange(len(offs) - 1), np.diff(offs))] + 1e-10)
+        # the boundary cases are present: the added 1e-10 changes some selection
+        o0, _, _ = oracle.near(g["queries"], g["q_mode"], g["nodes"], g["mode_off"], g["slices"], metric,
+                               g[f"radius_{metric}"], add_eps=0.0)
+        assert o0[-1] < offs[-1], metric
+
+
 def test_known_answers_edge_calls(oracle):
     """tests/test.py:61-90 of the reference: 3 / 1 / 9 / 11 calls."""
     ka = golden("known_answers.json")
