@@ -300,18 +300,34 @@ int mrmg_knn_exact(const double *d_queries, int64_t Q, const int32_t *d_query_mo
                    const int64_t *h_slices, int32_t A, int32_t metric, int32_t k, int64_t *d_idx,
                    double *d_dist, void *stream, int32_t flags);
 
-/* Per-mode node store for repeated k-NN queries (the planners' per-mode node
- * arrays: PRM node_array_cache, prm_graph.py:399-402; RRT batch_subtree,
- * rrtstar_base.py:254-306).  d_nodes[M, D] (FP64, caller-owned, must stay
- * alive and unchanged while the store lives) is grouped by mode:
- * h_mode_offsets[n_modes + 1].  For euclidean (D <= 29) and max_euclidean
- * (<= 4 agents of <= 7 coordinates) the store packs split-BF16 tiles for the
- * tensor-core candidate path; other metrics use the exact kernel. */
+/* Per-mode node store for repeated k-NN and radius queries (the planners'
+ * per-mode node arrays: PRM node_array_cache, prm_graph.py:399-402; RRT
+ * batch_subtree, rrtstar_base.py:254-306).  The store copies d_nodes[M, D]
+ * (FP64, grouped by mode: h_mode_offsets[n_modes + 1]) into device memory it
+ * owns; the caller's array may be freed afterwards.  For euclidean (D <= 29)
+ * and max_euclidean (<= 4 agents of <= 7 coordinates) it also packs
+ * split-BF16 tiles for the tensor-core candidate path; other metrics use the
+ * exact kernel.  M may be 0 (every mode empty). */
 typedef struct mrmg_node_store mrmg_node_store;
 int mrmg_node_store_create(const double *d_nodes, int64_t M, int32_t D, const int64_t *h_mode_offsets,
                            int32_t n_modes, const int64_t *h_slices, int32_t A, int32_t metric,
                            mrmg_node_store **out, void *stream);
 int mrmg_node_store_destroy(mrmg_node_store *store);
+
+/* Incremental insertion (SingleTree.add_node, rrtstar_base.py:270-276, and
+ * MultimodalGraph.add_nodes, prm_graph.py:289-291): appends rows[n, D] (FP64,
+ * host or device memory) to `mode`, after its existing nodes, so that the
+ * mode-local index of a node is its insertion order.  A mode index past the
+ * last creates the modes in between, empty.  Only the tiles the new rows touch
+ * are packed; a full mode segment doubles its capacity.  Synchronises. */
+int mrmg_node_store_append(mrmg_node_store *store, int32_t mode, const double *rows, int64_t n, void *stream);
+
+/* Removal as SingleTree.remove_node (rrtstar_base.py:278-289): the mode's
+ * last node moves into slot idx and the mode shrinks by one.  Synchronises. */
+int mrmg_node_store_remove(mrmg_node_store *store, int32_t mode, int64_t idx, void *stream);
+
+/* out3: [0] number of modes, [1] nodes in `mode`, [2] tensor-core path. */
+int mrmg_node_store_info(const mrmg_node_store *store, int32_t mode, int64_t *out3);
 
 /* k nearest neighbours of d_queries[Q, D] within their modes h_query_mode[Q]
  * (host array): same result as mrmg_knn_exact -- on the tensor-core path the

@@ -70,6 +70,9 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_knn": (i32, [vp, vp, i64, vp, i32, vp, vp, vp, vp]),
     "mrmg_near": (i32, [vp, vp, i64, vp, vp, f64, vp, vp, vp, i64, vp, vp]),
     "mrmg_near_fetch": (i32, [vp, vp, vp, i64, vp]),
+    "mrmg_node_store_append": (i32, [vp, i32, vp, i64, vp]),
+    "mrmg_node_store_info": (i32, [vp, i32, vp]),
+    "mrmg_node_store_remove": (i32, [vp, i32, i64, vp]),
 }
 
 

@@ -931,8 +931,9 @@ int mrmg_knn_exact(const double* d_queries, int64_t Q, const int32_t* d_query_mo
   if (!d_queries || !d_query_mode || !d_nodes || !d_mode_offsets || !d_idx || !d_dist)
     return fail(MRMG_ERR_ARG, "NULL device pointer");
   cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = knn_exact(d_queries, Q, d_query_mode, nullptr, 0, d_nodes, (const long long*)d_mode_offsets, t,
-                            metric, k, (long long*)d_idx, d_dist, device_sms(), st);
+  cudaError_t e = knn_exact(d_queries, Q, d_query_mode, nullptr, 0, d_nodes, (const long long*)d_mode_offsets,
+                            (const long long*)d_mode_offsets + 1, t, metric, k, (long long*)d_idx, d_dist,
+                            device_sms(), st);
   if (e != cudaSuccess) return cuda_fail(e, "launch knn");
   return sync_unless_async(st, flags, "knn");
 }
@@ -940,20 +941,12 @@ int mrmg_knn_exact(const double* d_queries, int64_t Q, const int32_t* d_query_mo
 }  // extern "C"
 
 struct mrmg_node_store {
-  KnnStore* tc = nullptr;       // tensor-core candidate store (supported metric / shape)
+  KnnStore* store = nullptr;         // owned nodes (+ tensor-core tiles)
   KnnScratch* scratch = nullptr;
-  SliceTab t{};
-  int metric = 0;
-  int n_modes = 0;
-  long long M = 0;
-  const double* nodes = nullptr;
-  long long* d_mode_off = nullptr;   // exact path
-  int* d_qmode = nullptr;            // exact path: uploaded query modes
-  long long qmode_cap = 0;
-  long long last_fallback = 0;
-  std::vector<long long> h_mode_off;
   NearState* near = nullptr;         // radius queries: scratch and the last result
   bool near_valid = false;
+  int D = 0;
+  long long last_fallback = 0;
 };
 
 extern "C" {
@@ -973,21 +966,11 @@ int mrmg_node_store_create(const double* d_nodes, int64_t M, int32_t D, const in
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   mrmg_node_store* s = new mrmg_node_store();
-  s->t = t;
-  s->metric = metric;
-  s->n_modes = n_modes;
-  s->M = M;
-  s->nodes = d_nodes;
+  s->D = D;
   s->scratch = knn_scratch_new();
   s->near = near_state_new();
-  s->h_mode_off.assign(h_mode_offsets, h_mode_offsets + n_modes + 1);
-  cudaError_t e = cudaMalloc(&s->d_mode_off, sizeof(long long) * (n_modes + 1));
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(s->d_mode_off, h_mode_offsets, sizeof(long long) * (n_modes + 1), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess && knn_tc_supported(t, metric)) {
-    s->tc = knn_store_new();
-    e = knn_store_build(s->tc, d_nodes, M, (const long long*)h_mode_offsets, n_modes, t, metric, st);
-  }
+  s->store = knn_store_new();
+  cudaError_t e = knn_store_build(s->store, d_nodes, M, (const long long*)h_mode_offsets, n_modes, t, metric, D, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) { mrmg_node_store_destroy(s); return cuda_fail(e, "node store"); }
   *out = s;
@@ -996,12 +979,48 @@ int mrmg_node_store_create(const double* d_nodes, int64_t M, int32_t D, const in
 
 int mrmg_node_store_destroy(mrmg_node_store* s) {
   if (!s) return MRMG_OK;
-  knn_store_delete(s->tc);
+  knn_store_delete(s->store);
   knn_scratch_delete(s->scratch);
   near_state_delete(s->near);
-  if (s->d_mode_off) cudaFree(s->d_mode_off);
-  if (s->d_qmode) cudaFree(s->d_qmode);
   delete s;
+  return MRMG_OK;
+}
+
+int mrmg_node_store_append(mrmg_node_store* s, int32_t mode, const double* rows, int64_t n, void* stream) {
+  if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
+  if (mode < 0 || n < 0) return fail(MRMG_ERR_ARG, "mode / n must be >= 0");
+  if (n > 0 && !rows) return fail(MRMG_ERR_ARG, "NULL rows");
+  if (knn_store_count(s->store, mode) + n > (1ll << 31) - 1) return fail(MRMG_ERR_ARG, "a mode holds < 2^31 nodes");
+  cudaStream_t st = (cudaStream_t)stream;
+  s->near_valid = false;
+  cudaError_t e = knn_store_append(s->store, mode, rows, n, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "node store append");
+}
+
+int mrmg_node_store_remove(mrmg_node_store* s, int32_t mode, int64_t idx, void* stream) {
+  if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
+  if (mode < 0 || mode >= knn_store_modes(s->store)) return fail(MRMG_ERR_ARG, "mode out of range");
+  if (idx < 0 || idx >= knn_store_count(s->store, mode)) return fail(MRMG_ERR_ARG, "index out of range");
+  cudaStream_t st = (cudaStream_t)stream;
+  s->near_valid = false;
+  cudaError_t e = knn_store_remove(s->store, mode, idx, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "node store remove");
+}
+
+int mrmg_node_store_info(const mrmg_node_store* s, int32_t mode, int64_t* out3) {
+  if (!s || !out3) return fail(MRMG_ERR_ARG, "NULL pointer");
+  out3[0] = knn_store_modes(s->store);
+  out3[1] = mode >= 0 ? knn_store_count(s->store, mode) : 0;
+  out3[2] = knn_store_tc(s->store) ? 1 : 0;
+  return MRMG_OK;
+}
+
+static int check_query_modes(const mrmg_node_store* s, const int32_t* h_query_mode, long long Q) {
+  const int n = knn_store_modes(s->store);
+  for (long long q = 0; q < Q; q++)
+    if (h_query_mode[q] < 0 || h_query_mode[q] >= n) return fail(MRMG_ERR_ARG, "query %lld: mode out of range", q);
   return MRMG_OK;
 }
 
@@ -1011,32 +1030,15 @@ int mrmg_knn(mrmg_node_store* s, const double* d_queries, int64_t Q, const int32
   if (Q < 0 || k < 1 || k > 64) return fail(MRMG_ERR_ARG, "Q / k (1..64)");
   if (Q == 0) return MRMG_OK;
   if (!d_queries || !h_query_mode || !d_idx || !d_dist) return fail(MRMG_ERR_ARG, "NULL pointer");
-  for (long long q = 0; q < Q; q++)
-    if (h_query_mode[q] < 0 || h_query_mode[q] >= s->n_modes) return fail(MRMG_ERR_ARG, "query %lld: mode out of range", q);
-  cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = cudaSuccess;
-  int nfb = 0;
-  bool tc = s->tc && k <= 16;
-  if (tc) {
-    e = knn_query(s->tc, d_queries, Q, h_query_mode, k, (long long*)d_idx, d_dist, s->scratch, device_sms(), &nfb, st);
-    if (e == cudaErrorLaunchTimeout) return fail(MRMG_ERR_TIMEOUT, "a bounded tensor-core pipeline wait ran out");
-  } else {
-    if (s->qmode_cap < Q) {
-      if (s->d_qmode) cudaFree(s->d_qmode);
-      s->d_qmode = nullptr;
-      e = cudaMalloc(&s->d_qmode, sizeof(int) * Q);
-      if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
-      s->qmode_cap = Q;
-    }
-    e = cudaMemcpyAsync(s->d_qmode, h_query_mode, sizeof(int) * Q, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-      e = knn_exact(d_queries, Q, s->d_qmode, nullptr, 0, s->nodes, s->d_mode_off, s->t, s->metric, k,
-                    (long long*)d_idx, d_dist, device_sms(), st);
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  int rc = check_query_modes(s, h_query_mode, Q);
+  if (rc) return rc;
+  int used_tc = 0, nfb = 0;
+  cudaError_t e = knn_store_query(s->store, s->scratch, d_queries, Q, h_query_mode, k, (long long*)d_idx, d_dist,
+                                  device_sms(), &used_tc, &nfb, (cudaStream_t)stream);
+  if (e == cudaErrorLaunchTimeout) return fail(MRMG_ERR_TIMEOUT, "a bounded tensor-core pipeline wait ran out");
   if (e != cudaSuccess) return cuda_fail(e, "knn");
   s->last_fallback = nfb;
-  if (out_stats2) { out_stats2[0] = tc ? 1 : 0; out_stats2[1] = nfb; }
+  if (out_stats2) { out_stats2[0] = used_tc; out_stats2[1] = nfb; }
   return MRMG_OK;
 }
 
@@ -1049,8 +1051,8 @@ int mrmg_near(mrmg_node_store* s, const double* d_queries, int64_t Q, const int3
   if (Q > 0 && (!d_queries || !h_query_mode || !h_radius)) return fail(MRMG_ERR_ARG, "NULL pointer");
   if (cap > 0 && (!d_idx || !d_dist)) return fail(MRMG_ERR_ARG, "NULL output with cap > 0");
   if (!(add_eps >= 0.0)) return fail(MRMG_ERR_ARG, "add_eps must be >= 0");
-  for (long long q = 0; q < Q; q++)
-    if (h_query_mode[q] < 0 || h_query_mode[q] >= s->n_modes) return fail(MRMG_ERR_ARG, "query %lld: mode out of range", q);
+  int rc = check_query_modes(s, h_query_mode, Q);
+  if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   s->near_valid = false;
   *out_total = 0;
@@ -1060,8 +1062,7 @@ int mrmg_near(mrmg_node_store* s, const double* d_queries, int64_t Q, const int3
     return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "near");
   }
   long long total = 0;
-  cudaError_t e = near_query(s->near, s->tc, s->nodes, s->d_mode_off, s->h_mode_off.data(), s->n_modes, s->t,
-                             s->metric, d_queries, Q, h_query_mode, h_radius, add_eps, (long long*)d_offsets,
+  cudaError_t e = near_query(s->near, s->store, d_queries, Q, h_query_mode, h_radius, add_eps, (long long*)d_offsets,
                              (long long*)d_idx, d_dist, cap, device_sms(), &total, st);
   if (e == cudaErrorLaunchTimeout) return fail(MRMG_ERR_TIMEOUT, "a bounded tensor-core pipeline wait ran out");
   if (e != cudaSuccess) return cuda_fail(e, "near");

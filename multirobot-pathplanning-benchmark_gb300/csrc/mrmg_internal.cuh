@@ -170,16 +170,22 @@ cudaError_t binary_indices(long long N, long long* out, cudaStream_t st, int chu
 
 
 cudaError_t knn_exact(const double* qs, long long Q, const int* q_mode, const long long* q_list, long long n_list,
-                      const double* nodes, const long long* mode_off, const SliceTab& t, int metric, int k,
-                      long long* out_idx, double* out_dist, int num_sms, cudaStream_t st);
+                      const double* nodes, const long long* mode_beg, const long long* mode_end, const SliceTab& t,
+                      int metric, int k, long long* out_idx, double* out_dist, int num_sms, cudaStream_t st);
 struct KnnStore;
 struct KnnScratch;
 bool knn_tc_supported(const SliceTab& t, int metric);
 cudaError_t knn_store_build(KnnStore* s, const double* d_nodes, long long M, const long long* h_mode_off, int n_modes,
-                            const SliceTab& t, int metric, cudaStream_t st);
+                            const SliceTab& t, int metric, int D, cudaStream_t st);
+cudaError_t knn_store_append(KnnStore* s, int mode, const double* rows, long long n, cudaStream_t st);
+cudaError_t knn_store_remove(KnnStore* s, int mode, long long idx, cudaStream_t st);
+long long knn_store_count(const KnnStore* s, int mode);
+int knn_store_modes(const KnnStore* s);
+bool knn_store_tc(const KnnStore* s);
 void knn_store_free(KnnStore* s);
-cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h_q_mode, int k, long long* d_idx,
-                      double* d_dist, KnnScratch* scr, int num_sms, int* n_fallback_out, cudaStream_t st);
+cudaError_t knn_store_query(KnnStore* s, KnnScratch* scr, const double* d_qs, long long Q, const int* h_q_mode, int k,
+                            long long* d_idx, double* d_dist, int num_sms, int* used_tc, int* n_fallback,
+                            cudaStream_t st);
 KnnStore* knn_store_new();
 void knn_store_delete(KnnStore* s);
 KnnScratch* knn_scratch_new();
@@ -187,11 +193,9 @@ void knn_scratch_delete(KnnScratch* s);
 struct NearState;
 NearState* near_state_new();
 void near_state_delete(NearState* ns);
-cudaError_t near_query(NearState* ns, KnnStore* tc, const double* nodes, const long long* d_mode_off,
-                       const long long* h_mode_off, int n_modes, const SliceTab& t, int metric, const double* d_qs,
-                       long long Q, const int* h_q_mode, const double* h_radius, double add_eps,
-                       long long* d_offsets, long long* d_idx, double* d_dist, long long cap, int num_sms,
-                       long long* total_out, cudaStream_t st);
+cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long Q, const int* h_q_mode,
+                       const double* h_radius, double add_eps, long long* d_offsets, long long* d_idx, double* d_dist,
+                       long long cap, int num_sms, long long* total_out, cudaStream_t st);
 cudaError_t near_fetch(NearState* ns, long long* d_idx, double* d_dist, long long cap, int num_sms, cudaStream_t st);
 long long near_last_total(const NearState* ns);
 cudaError_t umma_selftest(const void* A, const void* B, int N, float* C, int* err, cudaStream_t st);

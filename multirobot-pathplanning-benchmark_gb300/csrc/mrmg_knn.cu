@@ -75,8 +75,9 @@ __device__ __forceinline__ int warp_argmin(long long d, long long id) {
 template <int KM>
 __global__ void knn_exact_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
                                  const long long* __restrict__ q_list, long long n_list,
-                                 const double* __restrict__ nodes, const long long* __restrict__ mode_off, SliceTab t,
-                                 int metric, int k, long long* __restrict__ out_idx, double* __restrict__ out_dist) {
+                                 const double* __restrict__ nodes, const long long* __restrict__ mode_beg,
+                                 const long long* __restrict__ mode_end, SliceTab t, int metric, int k,
+                                 long long* __restrict__ out_idx, double* __restrict__ out_dist) {
   const int lane = threadIdx.x & 31;
   const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
@@ -85,7 +86,7 @@ __global__ void knn_exact_kernel(const double* __restrict__ qs, long long Q, con
   for (long long w = warp; w < total; w += nwarps) {
     const long long q = q_list ? q_list[w] : w;
     const int m = q_mode[q];
-    const long long s = mode_off[m], e = mode_off[m + 1];
+    const long long s = mode_beg[m], e = mode_end[m];
     long long td[KM];
     long long ti[KM];
 #pragma unroll
@@ -121,18 +122,18 @@ __global__ void knn_exact_kernel(const double* __restrict__ qs, long long Q, con
 }  // namespace
 
 cudaError_t knn_exact(const double* qs, long long Q, const int* q_mode, const long long* q_list, long long n_list,
-                      const double* nodes, const long long* mode_off, const SliceTab& t, int metric, int k,
-                      long long* out_idx, double* out_dist, int num_sms, cudaStream_t st) {
+                      const double* nodes, const long long* mode_beg, const long long* mode_end, const SliceTab& t,
+                      int metric, int k, long long* out_idx, double* out_dist, int num_sms, cudaStream_t st) {
   const long long total = q_list ? n_list : Q;
   if (total <= 0) return cudaSuccess;
   const int warps = 4;
   const int grid = (int)std::min<long long>((total + warps - 1) / warps, (long long)num_sms * 16);
   if (k <= 16)
-    knn_exact_kernel<16><<<grid, warps * 32, 0, st>>>(qs, Q, q_mode, q_list, n_list, nodes, mode_off, t, metric, k,
-                                                      out_idx, out_dist);
+    knn_exact_kernel<16><<<grid, warps * 32, 0, st>>>(qs, Q, q_mode, q_list, n_list, nodes, mode_beg, mode_end, t,
+                                                      metric, k, out_idx, out_dist);
   else
-    knn_exact_kernel<kKnnMaxK><<<grid, warps * 32, 0, st>>>(qs, Q, q_mode, q_list, n_list, nodes, mode_off, t, metric,
-                                                            k, out_idx, out_dist);
+    knn_exact_kernel<kKnnMaxK><<<grid, warps * 32, 0, st>>>(qs, Q, q_mode, q_list, n_list, nodes, mode_beg, mode_end,
+                                                            t, metric, k, out_idx, out_dist);
   return cudaGetLastError();
 }
 
@@ -321,8 +322,9 @@ struct KnnStoreDev {
   int fmt, NT, D, A;
   int agent_s[4], agent_e[4];
   const unsigned char* tiles;     // packed SW128 tiles
-  const long long* mode_off;      // node ranges (device)
-  const int* mode_tile0;          // first global tile of each mode
+  const long long* mode_beg;      // first row of each mode in the node buffer (device)
+  const long long* mode_end;      // one past its last row
+  const int* mode_tile0;          // first global tile of each mode (mode_beg / NT)
   const float* mode_xmax;         // max |x| of each mode (for the error bound)
 };
 
@@ -340,20 +342,27 @@ __device__ __forceinline__ void split2(double x, float* hi, float* lo) {
   *lo = __bfloat162float(__float2bfloat16_rn((float)(x - (double)h)));
 }
 
-__global__ void knn_pack_kernel(const double* __restrict__ nodes, KnnStoreDev st, int n_modes, long long total_rows,
-                                unsigned char* __restrict__ tiles, float* __restrict__ xmax_out) {
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total_rows;
+// packs the rows of global tiles [tile_lo, tile_hi): a row past its mode's
+// last node is padding.  `mode` >= 0 names the tiles' mode, else each tile's
+// mode is found from the (ascending) first tiles.
+__global__ void knn_pack_kernel(const double* __restrict__ nodes, KnnStoreDev st, int n_modes, int mode,
+                                long long tile_lo, long long tile_hi, unsigned char* __restrict__ tiles,
+                                float* __restrict__ xmax_out) {
+  const long long rows = (tile_hi - tile_lo) * st.NT;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < rows;
        g += (long long)gridDim.x * blockDim.x) {
-    const long long tile = g / st.NT;
+    const long long tile = tile_lo + g / st.NT;
     const int row = (int)(g % st.NT);
-    // find the mode of this tile (few modes: linear scan)
-    int m = 0;
-    while (m + 1 < n_modes && st.mode_tile0[m + 1] <= tile) m++;
+    int m = mode;
+    if (m < 0) {
+      m = 0;
+      while (m + 1 < n_modes && st.mode_tile0[m + 1] <= tile) m++;
+    }
     const long long local = (tile - st.mode_tile0[m]) * st.NT + row;
-    const long long node = st.mode_off[m] + local;
+    const long long node = st.mode_beg[m] + local;
     unsigned char* t = tiles + tile * (long long)st.NT * kRowBytes;
     for (int c = 0; c < 64; c++) put_bf16(t, row, c, 0.f);
-    if (node >= st.mode_off[m + 1]) {     // padding row: a huge |x|^2 term, never selected
+    if (node >= st.mode_end[m]) {     // padding row: a huge |x|^2 term, never selected
       if (st.fmt == KNN_FMT_EUCL) put_bf16(t, row, st.D, 1.0e30f);
       else for (int a = 0; a < st.A; a++) put_bf16(t, row, 16 * a + 2 * (st.agent_e[a] - st.agent_s[a]), 1.0e30f);
       continue;
@@ -680,8 +689,8 @@ constexpr int kMergeWarps = 4;   // warps per merge CTA
 // merge: certify the kept candidates and re-rank them in exact FP64
 // ---------------------------------------------------------------------------
 __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
-                                 const double* __restrict__ nodes, const long long* __restrict__ mode_off,
-                                 const int* __restrict__ mode_chunks, int chunks_max, const float* __restrict__ cand_d,
+                                 const double* __restrict__ nodes, const long long* __restrict__ mode_beg,
+                                 const long long* __restrict__ mode_end, const int* __restrict__ mode_chunks, int chunks_max, const float* __restrict__ cand_d,
                                  const int* __restrict__ cand_i, const float* __restrict__ q_eps, SliceTab t,
                                  int metric, int k, long long* __restrict__ out_idx, double* __restrict__ out_dist,
                                  long long* __restrict__ fallback, int* __restrict__ n_fallback) {
@@ -698,7 +707,7 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
   int* sid = s_id[wib];
   for (long long q = warp; q < Q; q += nwarps) {
     const int m = q_mode[q];
-    const long long M = mode_off[m + 1] - mode_off[m];
+    const long long M = mode_end[m] - mode_beg[m];
     const int C = mode_chunks[m];
     if (M == 0 || C == 0) {
       for (int r = lane; r < k; r += 32) { out_idx[q * k + r] = -1; out_dist[q * k + r] = DINF; }
@@ -762,7 +771,7 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
     for (int x = lane; x < ncand; x += 32) {
       const int id = sid[x];
       if (id < 0 || id >= M) continue;
-      const double* xx = nodes + (mode_off[m] + id) * t.D;
+      const double* xx = nodes + (mode_beg[m] + id) * t.D;
       auto dfun = [&](int jj) { return __dsub_rn(qq[jj], xx[jj]); };
       topk_insert<16>(td, tix, k < 16 ? k : 16, dkey(dist_of(t, metric, dfun)), id);
     }
@@ -795,7 +804,8 @@ constexpr int kNearWarps = 4;
 // the FP64 distance, so a dense word does not serialise one lane.  Bits whose
 // exact distance exceeds the query's r' (or past the mode's nodes) are cleared.
 __global__ void near_exact_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
-                                  const double* __restrict__ nodes, const long long* __restrict__ mode_off, SliceTab t,
+                                  const double* __restrict__ nodes, const long long* __restrict__ mode_beg,
+                                  const long long* __restrict__ mode_end, SliceTab t,
                                   int metric, const double* __restrict__ rp, const long long* __restrict__ woff,
                                   unsigned* __restrict__ bits, long long* __restrict__ counts) {
   __shared__ int s_list[kNearWarps][1024];
@@ -806,8 +816,8 @@ __global__ void near_exact_kernel(const double* __restrict__ qs, long long Q, co
   int* list = s_list[wib];
   for (long long q = warp; q < Q; q += nwarps) {
     const int m = q_mode[q];
-    const long long M = mode_off[m + 1] - mode_off[m];
-    const double* xb = nodes + mode_off[m] * t.D;
+    const long long M = mode_end[m] - mode_beg[m];
+    const double* xb = nodes + mode_beg[m] * t.D;
     const double* qq = qs + q * t.D;
     const long long w0 = woff[q], W = woff[q + 1] - w0;
     const double r = rp[q];
@@ -887,7 +897,7 @@ __global__ void near_scan_kernel(const long long* __restrict__ counts, long long
 // ascending mode-local indices and their FP64 distances, written from
 // offsets[q]; positions at or past `cap` are skipped
 __global__ void near_emit_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
-                                 const double* __restrict__ nodes, const long long* __restrict__ mode_off, SliceTab t,
+                                 const double* __restrict__ nodes, const long long* __restrict__ mode_beg, SliceTab t,
                                  int metric, const long long* __restrict__ woff, const unsigned* __restrict__ bits,
                                  const long long* __restrict__ offs, long long cap, long long* __restrict__ out_idx,
                                  double* __restrict__ out_dist) {
@@ -900,7 +910,7 @@ __global__ void near_emit_kernel(const double* __restrict__ qs, long long Q, con
     long long o = offs[q];
     if (o >= cap || offs[q + 1] == o) continue;
     const int m = q_mode[q];
-    const double* xb = nodes + mode_off[m] * t.D;
+    const double* xb = nodes + mode_beg[m] * t.D;
     const double* qq = qs + q * t.D;
     const long long w0 = woff[q], W = woff[q + 1] - w0;
     for (long long base = 0; base < W && o < cap; base += 32) {
@@ -943,16 +953,33 @@ __global__ void near_emit_kernel(const double* __restrict__ qs, long long Q, con
 // ---------------------------------------------------------------------------
 // host side: node store and query launch
 // ---------------------------------------------------------------------------
+// The store owns its nodes: FP64 rows grouped by mode, each mode in a
+// segment with room to grow (a multiple of the tile height), and on the
+// tensor-core path the split-BF16 tiles of the same rows at the same
+// positions.  Appending copies the new rows and packs only the tiles they
+// touch; a full segment doubles (every segment is moved once to a new layout).
 struct KnnStore {
-  KnnStoreDev dev;
-  SliceTab slices;
+  KnnStoreDev dev{};                      // tile-kernel view (tensor-core path)
+  bool tc = false;
+  SliceTab slices{};
   int metric = 0;
   int n_modes = 0;
-  std::vector<long long> mode_off;       // host copy
-  std::vector<int> mode_tiles;           // tiles per mode
-  const double* nodes = nullptr;         // caller-owned FP64 nodes
-  void* block = nullptr;                 // device allocation: tiles, offsets, per-mode data
-  long long total_tiles = 0;
+  int D = 0;
+  int NT = 64;                            // rows per tile = capacity granule
+  std::vector<long long> beg, cnt, cap;   // per mode: first row, rows, capacity
+  std::vector<int> mode_tiles;            // per mode: tiles holding its rows
+  double* nodes = nullptr;                // [cap_total, D]
+  unsigned char* tiles = nullptr;         // [cap_total / NT] tiles (tensor-core path)
+  void* meta = nullptr;                   // device: beg, end, tile0, xmax per mode
+  long long* d_beg = nullptr;
+  long long* d_end = nullptr;
+  int* d_tile0 = nullptr;
+  float* d_xmax = nullptr;
+  long long cap_total = 0;
+  std::vector<long long> h_meta;          // staging for the beg / end upload
+  std::vector<int> h_tile0;
+  int* d_qmode = nullptr;                 // exact path: uploaded query modes
+  long long qmode_cap = 0;
 };
 
 bool knn_tc_supported(const SliceTab& t, int metric) {
@@ -966,61 +993,201 @@ bool knn_tc_supported(const SliceTab& t, int metric) {
   return false;
 }
 
-cudaError_t knn_store_build(KnnStore* s, const double* d_nodes, long long M, const long long* h_mode_off, int n_modes,
-                            const SliceTab& t, int metric, cudaStream_t st) {
-  s->slices = t;
-  s->metric = metric;
-  s->n_modes = n_modes;
-  s->nodes = d_nodes;
-  s->mode_off.assign(h_mode_off, h_mode_off + n_modes + 1);
-  const int fmt = metric == MRMG_METRIC_EUCLIDEAN ? KNN_FMT_EUCL : KNN_FMT_AGENT;
-  const int NT = fmt == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
-  std::vector<int> tile0(n_modes + 1, 0);
-  s->mode_tiles.assign(n_modes, 0);
-  for (int m = 0; m < n_modes; m++) {
-    const long long cnt = h_mode_off[m + 1] - h_mode_off[m];
-    s->mode_tiles[m] = (int)((cnt + NT - 1) / NT);
-    tile0[m + 1] = tile0[m] + s->mode_tiles[m];
-  }
-  s->total_tiles = tile0[n_modes];
-  const size_t tiles_bytes = (size_t)std::max<long long>(s->total_tiles, 1) * NT * kRowBytes;
-  const size_t off_bytes = sizeof(long long) * (n_modes + 1);
-  const size_t t0_bytes = sizeof(int) * (n_modes + 1);
-  const size_t xm_bytes = sizeof(float) * n_modes;
-  auto al = [](size_t x) { return (x + 1023) & ~(size_t)1023; };
-  const size_t total = al(tiles_bytes) + al(off_bytes) + al(t0_bytes) + al(xm_bytes);
-  cudaError_t e = cudaMalloc(&s->block, total);
-  if (e != cudaSuccess) return e;
-  unsigned char* b = (unsigned char*)s->block;
-  unsigned char* tiles = b;
-  long long* d_off = (long long*)(b + al(tiles_bytes));
-  int* d_t0 = (int*)((unsigned char*)d_off + al(off_bytes));
-  float* d_xm = (float*)((unsigned char*)d_t0 + al(t0_bytes));
-  e = cudaMemcpyAsync(d_off, h_mode_off, off_bytes, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_t0, tile0.data(), t0_bytes, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_xm, 0, xm_bytes, st);
-  if (e != cudaSuccess) return e;
+static size_t al1k(size_t x) { return (x + 1023) & ~(size_t)1023; }
+
+static void set_dev_view(KnnStore* s) {
   KnnStoreDev& d = s->dev;
-  d.fmt = fmt;
-  d.NT = NT;
-  d.D = t.D;
-  d.A = t.A;
-  for (int i = 0; i < 4; i++) { d.agent_s[i] = i < t.A ? t.s[i] : 0; d.agent_e[i] = i < t.A ? t.e[i] : 0; }
-  d.tiles = tiles;
-  d.mode_off = d_off;
-  d.mode_tile0 = d_t0;
-  d.mode_xmax = d_xm;
-  const long long rows = s->total_tiles * NT;
-  if (rows > 0) {
-    const int grid = (int)std::min<long long>((rows + 255) / 256, 4096);
-    knn_pack_kernel<<<grid, 256, 0, st>>>(d_nodes, d, n_modes, rows, tiles, d_xm);
+  d.NT = s->NT;
+  d.D = s->D;
+  d.A = s->slices.A;
+  for (int i = 0; i < 4; i++) {
+    d.agent_s[i] = i < s->slices.A ? s->slices.s[i] : 0;
+    d.agent_e[i] = i < s->slices.A ? s->slices.e[i] : 0;
   }
+  d.tiles = s->tiles;
+  d.mode_beg = s->d_beg;
+  d.mode_end = s->d_end;
+  d.mode_tile0 = s->d_tile0;
+  d.mode_xmax = s->d_xmax;
+}
+
+static cudaError_t upload_meta(KnnStore* s, cudaStream_t st) {
+  const int n = s->n_modes;
+  s->h_meta.resize(2 * (size_t)std::max(n, 1));
+  s->h_tile0.resize(std::max(n, 1));
+  for (int m = 0; m < n; m++) {
+    s->h_meta[m] = s->beg[m];
+    s->h_meta[n + m] = s->beg[m] + s->cnt[m];
+    s->h_tile0[m] = (int)(s->beg[m] / s->NT);
+  }
+  if (n == 0) return cudaSuccess;
+  // beg and end sit back to back on the device
+  cudaError_t e = cudaMemcpyAsync(s->d_beg, s->h_meta.data(), sizeof(long long) * 2 * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_tile0, s->h_tile0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+  return e;
+}
+
+// new buffers for `n_new` modes with capacities `cap_new` (rows, multiples of
+// NT); the old modes' rows, tiles and norm bounds move over
+static cudaError_t relayout(KnnStore* s, int n_new, const std::vector<long long>& cap_new, cudaStream_t st) {
+  std::vector<long long> beg_new(n_new, 0);
+  long long total = 0;
+  for (int m = 0; m < n_new; m++) { beg_new[m] = total; total += cap_new[m]; }
+  double* nodes = nullptr;
+  unsigned char* tiles = nullptr;
+  void* meta = nullptr;
+  const size_t b_l = al1k(sizeof(long long) * std::max(n_new, 1));
+  const size_t b_i = al1k(sizeof(int) * std::max(n_new, 1));
+  cudaError_t e = cudaMalloc(&nodes, sizeof(double) * std::max<long long>(total, 1) * std::max(s->D, 1));
+  if (e == cudaSuccess && s->tc) e = cudaMalloc(&tiles, (size_t)std::max<long long>(total, s->NT) * kRowBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&meta, 2 * b_l + 2 * b_i);
+  if (e != cudaSuccess) {
+    if (nodes) cudaFree(nodes);
+    if (tiles) cudaFree(tiles);
+    return e;
+  }
+  long long* d_beg = (long long*)meta;
+  long long* d_end = d_beg + (n_new > 0 ? n_new : 1);    // beg and end back to back
+  int* d_tile0 = (int*)((unsigned char*)meta + 2 * b_l);
+  float* d_xmax = (float*)((unsigned char*)meta + 2 * b_l + b_i);
+  e = cudaMemsetAsync(d_xmax, 0, sizeof(float) * std::max(n_new, 1), st);
+  for (int m = 0; m < s->n_modes && e == cudaSuccess; m++) {
+    if (s->cnt[m] == 0) continue;
+    e = cudaMemcpyAsync(nodes + beg_new[m] * s->D, s->nodes + s->beg[m] * s->D, sizeof(double) * s->cnt[m] * s->D,
+                        cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess && s->tc)
+      e = cudaMemcpyAsync(tiles + beg_new[m] * kRowBytes, s->tiles + s->beg[m] * kRowBytes,
+                          (size_t)s->mode_tiles[m] * s->NT * kRowBytes, cudaMemcpyDeviceToDevice, st);
+  }
+  if (e == cudaSuccess && s->n_modes > 0 && s->d_xmax)
+    e = cudaMemcpyAsync(d_xmax, s->d_xmax, sizeof(float) * std::min(s->n_modes, n_new), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // the old buffers are read until here
+  if (e != cudaSuccess) {
+    cudaFree(nodes);
+    if (tiles) cudaFree(tiles);
+    cudaFree(meta);
+    return e;
+  }
+  if (s->nodes) cudaFree(s->nodes);
+  if (s->tiles) cudaFree(s->tiles);
+  if (s->meta) cudaFree(s->meta);
+  s->nodes = nodes;
+  s->tiles = tiles;
+  s->meta = meta;
+  s->d_beg = d_beg;
+  s->d_end = d_end;
+  s->d_tile0 = d_tile0;
+  s->d_xmax = d_xmax;
+  s->cnt.resize(n_new, 0);
+  s->mode_tiles.resize(n_new, 0);
+  s->beg = beg_new;
+  s->cap = cap_new;
+  s->n_modes = n_new;
+  s->cap_total = total;
+  set_dev_view(s);
+  return upload_meta(s, st);
+}
+
+static long long round_up(long long x, long long g) { return (x + g - 1) / g * g; }
+
+static cudaError_t pack_tiles(KnnStore* s, int mode, long long tile_lo, long long tile_hi, cudaStream_t st) {
+  if (!s->tc || tile_hi <= tile_lo) return cudaSuccess;
+  const long long rows = (tile_hi - tile_lo) * s->NT;
+  const int grid = (int)std::min<long long>((rows + 255) / 256, 4096);
+  knn_pack_kernel<<<grid, 256, 0, st>>>(s->nodes, s->dev, s->n_modes, mode, tile_lo, tile_hi, s->tiles, s->d_xmax);
   return cudaGetLastError();
 }
 
+cudaError_t knn_store_build(KnnStore* s, const double* d_nodes, long long M, const long long* h_mode_off, int n_modes,
+                            const SliceTab& t, int metric, int D, cudaStream_t st) {
+  s->slices = t;
+  s->metric = metric;
+  s->D = D;
+  s->tc = knn_tc_supported(t, metric);
+  const int fmt = metric == MRMG_METRIC_EUCLIDEAN ? KNN_FMT_EUCL : KNN_FMT_AGENT;
+  s->NT = s->tc ? (fmt == KNN_FMT_EUCL ? kNtEucl : kNtAgent) : 64;
+  s->dev.fmt = fmt;
+  std::vector<long long> cap(n_modes, 0);
+  for (int m = 0; m < n_modes; m++) {
+    const long long c = h_mode_off[m + 1] - h_mode_off[m];
+    cap[m] = c > 0 ? round_up(c + c / 4, s->NT) : 0;   // a quarter to grow into
+  }
+  cudaError_t e = relayout(s, n_modes, cap, st);
+  if (e != cudaSuccess) return e;
+  for (int m = 0; m < n_modes && e == cudaSuccess; m++) {
+    const long long c = h_mode_off[m + 1] - h_mode_off[m];
+    s->cnt[m] = c;
+    s->mode_tiles[m] = (int)((c + s->NT - 1) / s->NT);
+    if (c > 0)
+      e = cudaMemcpyAsync(s->nodes + s->beg[m] * D, d_nodes + h_mode_off[m] * D, sizeof(double) * c * D,
+                          cudaMemcpyDeviceToDevice, st);
+  }
+  if (e == cudaSuccess) e = upload_meta(s, st);
+  if (e == cudaSuccess) e = pack_tiles(s, -1, 0, s->cap_total / s->NT, st);
+  return e;
+}
+
+cudaError_t knn_store_append(KnnStore* s, int mode, const double* rows, long long n, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (mode >= s->n_modes || s->cnt[mode] + n > s->cap[mode]) {
+    std::vector<long long> cap = s->cap;
+    cap.resize(std::max(s->n_modes, mode + 1), 0);
+    const long long need = (mode < s->n_modes ? s->cnt[mode] : 0) + n;
+    if (need > cap[mode]) cap[mode] = round_up(std::max(need, 2 * cap[mode]), s->NT);
+    e = relayout(s, (int)cap.size(), cap, st);
+    if (e != cudaSuccess) return e;
+  }
+  if (n == 0) return cudaSuccess;
+  const long long old = s->cnt[mode];
+  // rows may be host or device memory
+  e = cudaMemcpyAsync(s->nodes + (s->beg[mode] + old) * s->D, rows, sizeof(double) * n * s->D, cudaMemcpyDefault, st);
+  if (e != cudaSuccess) return e;
+  s->cnt[mode] = old + n;
+  s->mode_tiles[mode] = (int)((old + n + s->NT - 1) / s->NT);
+  s->h_meta[s->n_modes + mode] = s->beg[mode] + old + n;
+  e = cudaMemcpyAsync(s->d_end + mode, &s->h_meta[s->n_modes + mode], sizeof(long long), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  const long long t0 = s->beg[mode] / s->NT;
+  return pack_tiles(s, mode, t0 + old / s->NT, t0 + s->mode_tiles[mode], st);
+}
+
+// removal by moving the mode's last node into the freed slot (the order
+// SingleTree.remove_node leaves, rrtstar_base.py:278-289); repacks the two
+// tiles involved
+cudaError_t knn_store_remove(KnnStore* s, int mode, long long idx, cudaStream_t st) {
+  const long long last = s->cnt[mode] - 1;
+  cudaError_t e = cudaSuccess;
+  if (idx != last)
+    e = cudaMemcpyAsync(s->nodes + (s->beg[mode] + idx) * s->D, s->nodes + (s->beg[mode] + last) * s->D,
+                        sizeof(double) * s->D, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  s->cnt[mode] = last;
+  s->mode_tiles[mode] = (int)((last + s->NT - 1) / s->NT);
+  s->h_meta[s->n_modes + mode] = s->beg[mode] + last;
+  e = cudaMemcpyAsync(s->d_end + mode, &s->h_meta[s->n_modes + mode], sizeof(long long), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  // the tile of the old last row (that row becomes padding) unless the mode
+  // no longer uses it, and the tile of idx when it is another one
+  const long long t0 = s->beg[mode] / s->NT;
+  const long long t_last = last / s->NT, t_idx = idx / s->NT;
+  if (t_last < s->mode_tiles[mode]) e = pack_tiles(s, mode, t0 + t_last, t0 + t_last + 1, st);
+  if (e == cudaSuccess && idx != last && t_idx != t_last) e = pack_tiles(s, mode, t0 + t_idx, t0 + t_idx + 1, st);
+  return e;
+}
+
+long long knn_store_count(const KnnStore* s, int mode) { return mode < s->n_modes ? s->cnt[mode] : 0; }
+int knn_store_modes(const KnnStore* s) { return s->n_modes; }
+bool knn_store_tc(const KnnStore* s) { return s->tc; }
+
 void knn_store_free(KnnStore* s) {
-  if (s->block) cudaFree(s->block);
-  s->block = nullptr;
+  if (s->nodes) cudaFree(s->nodes);
+  if (s->tiles) cudaFree(s->tiles);
+  if (s->meta) cudaFree(s->meta);
+  if (s->d_qmode) cudaFree(s->d_qmode);
+  s->nodes = nullptr;
+  s->tiles = nullptr;
+  s->meta = nullptr;
+  s->d_qmode = nullptr;
 }
 
 // scratch for one query launch, owned by the caller (the ABI layer)
@@ -1183,7 +1350,7 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
     if (e != cudaSuccess) return e;
   }
   const int mgrid = (int)std::min<long long>((Q + 3) / 4, (long long)num_sms * 16);
-  knn_merge_kernel<<<std::max(mgrid, 1), 32 * kMergeWarps, 0, st>>>(d_qs, Q, d_qmode, s->nodes, s->dev.mode_off, d_mch, chunks_max,
+  knn_merge_kernel<<<std::max(mgrid, 1), 32 * kMergeWarps, 0, st>>>(d_qs, Q, d_qmode, s->nodes, s->d_beg, s->d_end, d_mch, chunks_max,
                                                        d_cd, d_ci, d_eps, s->slices, s->metric, k, d_idx, d_dist, d_fb,
                                                        d_ctr);
   e = cudaGetLastError();
@@ -1194,11 +1361,39 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   *n_fallback_out = h_ctr[0];
   if (h_ctr[1]) return cudaErrorLaunchTimeout;
   if (h_ctr[0] > 0) {
-    e = knn_exact(d_qs, Q, d_qmode, d_fb, h_ctr[0], s->nodes, s->dev.mode_off, s->slices, s->metric, k, d_idx, d_dist,
-                  num_sms, st);
+    e = knn_exact(d_qs, Q, d_qmode, d_fb, h_ctr[0], s->nodes, s->d_beg, s->d_end, s->slices, s->metric, k, d_idx,
+                  d_dist, num_sms, st);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+// k nearest on the store: the tensor-core path for its formats and k <= 16,
+// else the exact kernel over the store's nodes
+cudaError_t knn_store_query(KnnStore* s, KnnScratch* scr, const double* d_qs, long long Q, const int* h_q_mode, int k,
+                            long long* d_idx, double* d_dist, int num_sms, int* used_tc, int* n_fallback,
+                            cudaStream_t st) {
+  *used_tc = 0;
+  *n_fallback = 0;
+  if (s->tc && k <= 16) {
+    *used_tc = 1;
+    cudaError_t e = knn_query(s, d_qs, Q, h_q_mode, k, d_idx, d_dist, scr, num_sms, n_fallback, st);
+    return e;
+  }
+  if (s->qmode_cap < Q) {
+    if (s->d_qmode) cudaFree(s->d_qmode);
+    s->d_qmode = nullptr;
+    s->qmode_cap = 0;
+    cudaError_t e = cudaMalloc(&s->d_qmode, sizeof(int) * Q);
+    if (e != cudaSuccess) return e;
+    s->qmode_cap = Q;
+  }
+  cudaError_t e = cudaMemcpyAsync(s->d_qmode, h_q_mode, sizeof(int) * Q, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = knn_exact(d_qs, Q, s->d_qmode, nullptr, 0, s->nodes, s->d_beg, s->d_end, s->slices, s->metric, k, d_idx, d_dist,
+                  num_sms, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
 }
 
 // ---------------------------------------------------------------------------
@@ -1210,7 +1405,7 @@ struct NearState {
   const double* qs = nullptr;
   long long Q = 0;
   const double* nodes = nullptr;
-  const long long* mode_off = nullptr;
+  const long long* mode_beg = nullptr;
   SliceTab t{};
   int metric = 0;
   const int* qmode = nullptr;
@@ -1241,18 +1436,19 @@ static float rad2_up(double x) {
   return (double)f >= x2 ? f : std::nextafter(f, __builtin_huge_valf());
 }
 
-cudaError_t near_query(NearState* ns, KnnStore* tc, const double* nodes, const long long* d_mode_off,
-                       const long long* h_mode_off, int n_modes, const SliceTab& t, int metric, const double* d_qs,
-                       long long Q, const int* h_q_mode, const double* h_radius, double add_eps,
-                       long long* d_offsets, long long* d_idx, double* d_dist, long long cap, int num_sms,
-                       long long* total_out, cudaStream_t st) {
+cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long Q, const int* h_q_mode,
+                       const double* h_radius, double add_eps, long long* d_offsets, long long* d_idx, double* d_dist,
+                       long long cap, int num_sms, long long* total_out, cudaStream_t st) {
+  const int n_modes = s->n_modes;
+  KnnStore* tc = s->tc ? s : nullptr;
+  const double* nodes = s->nodes;
+  const SliceTab& t = s->slices;
+  const int metric = s->metric;
   // words of each query's bitmap: whole node tiles on the tensor-core path
   // (every word is written by the candidate kernel), else ceil(M / 32)
   std::vector<long long> words(n_modes);
-  for (int m = 0; m < n_modes; m++) {
-    const long long M = h_mode_off[m + 1] - h_mode_off[m];
-    words[m] = tc ? (long long)tc->mode_tiles[m] * tc->dev.NT / 32 : (M + 31) / 32;
-  }
+  for (int m = 0; m < n_modes; m++)
+    words[m] = tc ? (long long)s->mode_tiles[m] * s->NT / 32 : (s->cnt[m] + 31) / 32;
   ItemPlan pl;
   if (tc) plan_items(tc, h_q_mode, Q, num_sms, &pl);
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -1317,7 +1513,7 @@ cudaError_t near_query(NearState* ns, KnnStore* tc, const double* nodes, const l
   if (tc && !pl.items.empty()) {
     const size_t smem = tc_smem_bytes(tc);
     const RadOut ro{d_bits, d_woff, d_rad2};
-    if (tc->dev.fmt == KNN_FMT_EUCL) {
+    if (s->dev.fmt == KNN_FMT_EUCL) {
       raise_smem_limit<KNN_FMT_EUCL, true>();
       knn_tc_kernel<KNN_FMT_EUCL, true><<<(int)pl.items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(
           tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, (int*)(d_ctr + 1), ro);
@@ -1332,11 +1528,11 @@ cudaError_t near_query(NearState* ns, KnnStore* tc, const double* nodes, const l
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int grid = near_grid(Q, num_sms);
-  near_exact_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, d_mode_off, t, metric, d_rp, d_woff,
-                                                      d_bits, d_cnt);
+  near_exact_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, s->d_end, t, metric, d_rp,
+                                                      d_woff, d_bits, d_cnt);
   near_scan_kernel<<<1, 1024, 0, st>>>(d_cnt, Q, d_offsets, d_offs, d_ctr);
   if (cap > 0)
-    near_emit_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, d_mode_off, t, metric, d_woff, d_bits,
+    near_emit_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, t, metric, d_woff, d_bits,
                                                        d_offs, cap, d_idx, d_dist);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(h_ctr, d_ctr, 2 * sizeof(long long), cudaMemcpyDeviceToHost, st);
@@ -1346,7 +1542,7 @@ cudaError_t near_query(NearState* ns, KnnStore* tc, const double* nodes, const l
   ns->qs = d_qs;
   ns->Q = Q;
   ns->nodes = nodes;
-  ns->mode_off = d_mode_off;
+  ns->mode_beg = s->d_beg;
   ns->t = t;
   ns->metric = metric;
   ns->qmode = d_qmode;
@@ -1361,7 +1557,7 @@ cudaError_t near_query(NearState* ns, KnnStore* tc, const double* nodes, const l
 cudaError_t near_fetch(NearState* ns, long long* d_idx, double* d_dist, long long cap, int num_sms, cudaStream_t st) {
   if (ns->Q == 0 || cap <= 0) return cudaSuccess;
   near_emit_kernel<<<near_grid(ns->Q, num_sms), 32 * kNearWarps, 0, st>>>(
-      ns->qs, ns->Q, ns->qmode, ns->nodes, ns->mode_off, ns->t, ns->metric, ns->woff, ns->bits, ns->offs, cap, d_idx,
+      ns->qs, ns->Q, ns->qmode, ns->nodes, ns->mode_beg, ns->t, ns->metric, ns->woff, ns->bits, ns->offs, cap, d_idx,
       d_dist);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

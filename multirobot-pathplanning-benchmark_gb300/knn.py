@@ -47,8 +47,10 @@ def selftest_umma(a_bf16: torch.Tensor, b_bf16: torch.Tensor) -> torch.Tensor:
 
 
 class NodeStore:
-    """Per-mode node arrays resident on the device for repeated k-NN queries
-    (the planners' node_array_cache / batch_subtree).  Euclidean and
+    """Per-mode node arrays resident on the device for repeated k-NN and
+    radius queries (the planners' node_array_cache / batch_subtree).  The
+    store owns a copy of the nodes and grows by ``append`` / shrinks by
+    ``remove`` as SingleTree does (rrtstar_base.py:270-289).  Euclidean and
     max_euclidean queries use the tensor-core candidate path (tcgen05 split-
     BF16 distance GEMM, certified, FP64 re-rank); other metrics the exact one."""
 
@@ -67,7 +69,50 @@ class NodeStore:
                                                    self.slices.ctypes.data, len(self.slices), _lib.METRICS[metric],
                                                    C.byref(h), _lib.stream_handle(stream)), "node store")
         self.h = h
+        self.nodes = None          # the store holds its own copy
         self.last_stats = {}
+
+    @classmethod
+    def empty(cls, dim: int, n_modes: int, slices, metric: str = "euclidean", stream=None):
+        """A store with ``n_modes`` empty modes, filled by ``append``."""
+        return cls(np.zeros((0, dim)), np.zeros(n_modes + 1, dtype=np.int64), slices, metric, stream)
+
+    def append(self, mode: int, rows, stream=None):
+        """Appends rows [n, D] (host or device) to ``mode``; their mode-local
+        indices continue the mode's insertion order."""
+        if isinstance(rows, torch.Tensor):
+            t = rows.detach().to(torch.float64).contiguous()
+            if t.dim() == 1:
+                t = t.unsqueeze(0)
+            ptr, n, keep = t.data_ptr(), t.shape[0], t
+            if t.shape[-1] != self.D:
+                raise ValueError(f"rows must have {self.D} columns")
+        else:
+            a = np.ascontiguousarray(np.asarray(rows, dtype=np.float64).reshape(-1, self.D))
+            ptr, n, keep = a.ctypes.data, a.shape[0], a
+        _lib.check(self.lib.mrmg_node_store_append(self.h, int(mode), ptr, int(n), _lib.stream_handle(stream)),
+                   "append")
+        del keep
+
+    def remove(self, mode: int, idx: int, stream=None):
+        """Removes node ``idx`` of ``mode``: the mode's last node takes its index."""
+        _lib.check(self.lib.mrmg_node_store_remove(self.h, int(mode), int(idx), _lib.stream_handle(stream)), "remove")
+
+    def _info(self, mode: int = -1):
+        o = np.zeros(3, dtype=np.int64)
+        _lib.check(self.lib.mrmg_node_store_info(self.h, int(mode), o.ctypes.data))
+        return o
+
+    @property
+    def n_modes(self) -> int:
+        return int(self._info()[0])
+
+    def size(self, mode: int) -> int:
+        return int(self._info(mode)[1])
+
+    @property
+    def tensor_core(self) -> bool:
+        return bool(self._info()[2])
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:

@@ -153,3 +153,96 @@ def test_near_other_metrics_and_edge_modes(gpu, oracle):
         assert _csr_equal(store.near(qs, qm, r), want), metric
         offs, idx, dist = store.near(qs[:0], qm[:0], 1.0)
         assert offs.cpu().tolist() == [0] and idx.numel() == 0
+
+
+class _HostModes:
+    """Host mirror of a growing per-mode node store (insertion order, removal
+    by moving the last node into the freed slot, as SingleTree does)."""
+
+    def __init__(self, dim):
+        self.dim = dim
+        self.modes = []
+
+    def append(self, m, rows):
+        while len(self.modes) <= m:
+            self.modes.append(np.zeros((0, self.dim)))
+        self.modes[m] = np.concatenate([self.modes[m], np.asarray(rows).reshape(-1, self.dim)])
+
+    def remove(self, m, i):
+        a = self.modes[m]
+        a[i] = a[-1]
+        self.modes[m] = a[:-1]
+
+    def arrays(self):
+        off = np.concatenate([[0], np.cumsum([len(a) for a in self.modes])]).astype(np.int64)
+        return np.concatenate(self.modes), off
+
+
+@pytest.mark.parametrize("metric", ["euclidean", "max_euclidean", "sum_euclidean"])
+def test_node_store_incremental(gpu, oracle, metric):
+    """A store grown by appends (single rows across tile boundaries and
+    capacity doublings, batches, modes created past the last) and shrunk by
+    removals answers k-NN and radius queries like the oracle over the same
+    per-mode arrays."""
+    knn, scenes = pkg("knn"), pkg("scenes")
+    w = scenes.make_knn_workload(seed=6, n_nodes=12_000, n_modes=4, n_queries=256)
+    nodes, off, sl = w["nodes"], w["mode_offsets"], w["slices"]
+    rng = np.random.default_rng(11)
+    host = _HostModes(nodes.shape[1])
+    half = [off[m] + (off[m + 1] - off[m]) // 2 for m in range(4)]
+    first = np.concatenate([nodes[off[m]:half[m]] for m in range(4)])
+    first_off = np.concatenate([[0], np.cumsum([half[m] - off[m] for m in range(4)])])
+    store = knn.NodeStore(first, first_off, sl, metric)
+    for m in range(4):
+        host.append(m, nodes[off[m]:half[m]])
+    # RRT-style single rows into mode 1, PRM-style batches elsewhere, a new mode 6
+    for r in nodes[half[1]:half[1] + 700]:
+        store.append(1, r)
+        host.append(1, r)
+    for m in (0, 2, 3):
+        rows = nodes[half[m]:off[m + 1]]
+        for chunk in np.array_split(rows, 3):
+            store.append(m, torch.from_numpy(chunk).cuda())
+            host.append(m, chunk)
+    extra = rng.normal(0, 1.0, (300, nodes.shape[1]))
+    store.append(6, extra)
+    host.append(6, extra)
+    for m, i in [(1, 0), (1, 5), (0, 17), (6, 299), (2, 3)]:
+        store.remove(m, i)
+        host.remove(m, i)
+    assert store.n_modes == 7 and store.size(5) == 0
+    assert [store.size(m) for m in range(7)] == [len(a) for a in host.modes]
+    allnodes, alloff = host.arrays()
+    qm = rng.integers(0, 7, 256).astype(np.int32)
+    qs = w["queries"][:256]
+    for k in (1, 10):
+        idx, dist = store.knn(qs, qm, k)
+        oi, od = oracle.knn(qs, qm, allnodes, alloff, sl, metric, k)
+        assert np.array_equal(idx.cpu().numpy(), oi), (metric, k)
+        assert np.array_equal(dist.cpu().numpy(), od), (metric, k)
+    _, od = oracle.knn(qs, qm, allnodes, alloff, sl, metric, 12)
+    r = np.where(np.isfinite(od[:, -1]), od[:, -1], 1.0)
+    assert _csr_equal(store.near(qs, qm, r), oracle.near(qs, qm, allnodes, alloff, sl, metric, r))
+
+
+def test_node_store_grow_from_empty(gpu, oracle):
+    """An empty store filled one node at a time, queried as it grows (the RRT
+    loop: nearest, near, add)."""
+    knn = pkg("knn")
+    rng = np.random.default_rng(12)
+    D, sl = 8, [[0, 4], [4, 8]]
+    store = knn.NodeStore.empty(D, 2, sl, "euclidean")
+    host = _HostModes(D)
+    for step in range(300):
+        m = int(rng.integers(0, 2))
+        q = rng.uniform(-1, 1, (1, D))
+        if store.size(m) > 0:
+            allnodes, alloff = host.arrays()
+            idx, dist = store.knn(q, [m], 1)
+            oi, od = oracle.knn(q, [m], allnodes, alloff, sl, "euclidean", 1)
+            assert np.array_equal(idx.cpu().numpy(), oi) and np.array_equal(dist.cpu().numpy(), od), step
+            got = store.near(q, [m], 0.6)
+            assert _csr_equal(got, oracle.near(q, [m], allnodes, alloff, sl, "euclidean", 0.6)), step
+        store.append(m, q)
+        host.append(m, q)
+    assert store.size(0) + store.size(1) == 300
