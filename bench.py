@@ -447,8 +447,57 @@ def bench_knn(orc, steps: int = 20) -> dict:
                        "rerun_exact": store.last_stats.get("rerun_exact"),
                        "gemm_tflops_issued": issued / dt / 1e12,
                        "cpu_queries_per_s": len(w["queries"]) / cpu_s, "cpu_cores": orc.num_threads()}
+        # radius queries: each query's radius is its 16th-nearest distance
+        _, d16 = store.knn(qs, w["q_mode"], 16)
+        r = d16[:, -1].cpu().numpy()
+        r = np.where(np.isfinite(r), r, 0.0)
+        offs, nidx, ndist = store.near(qs, w["q_mode"], r)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            offs, nidx, ndist = store.near(qs, w["q_mode"], r)
+        torch.cuda.synchronize()
+        dtn = (time.perf_counter() - t0) / steps
+        so = orc.near(w["queries"][sub], w["q_mode"][sub], w["nodes"], w["mode_offsets"], w["slices"], metric, r[sub])
+        o = offs.cpu().numpy()
+        ok = np.array_equal(o[:257] - o[0], so[0]) and np.array_equal(nidx[:int(o[256])].cpu().numpy(), so[1])
+        out[metric]["near"] = {"queries_per_s": len(w["queries"]) / dtn, "ms_per_batch": 1e3 * dtn,
+                               "neighbours": int(o[-1]), "sample_256_identical": bool(ok)}
         store.close()
+    out["rrt_loop"] = bench_rrt_loop(w)
     return out
+
+
+def bench_rrt_loop(w, iters: int = 2000) -> dict:
+    """The RRT* inner loop on a node store that already holds the 200k-node
+    workload: per iteration one nearest query (k = 1), one radius query and
+    one single-row append, each a synchronous library call from host arrays."""
+    knn = pkg("knn")
+    store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], "euclidean")
+    rng = np.random.default_rng(1)
+    qs = rng.uniform(-np.pi, np.pi, (iters, w["nodes"].shape[1]))
+    modes = rng.integers(0, len(w["mode_offsets"]) - 1, iters).astype(np.int32)
+    for i in range(20):
+        store.knn(qs[i:i + 1], modes[i:i + 1], 1)
+        store.near(qs[i:i + 1], modes[i:i + 1], 0.5)
+    t = {"nearest": 0.0, "near": 0.0, "append": 0.0}
+    n0 = sum(store.size(m) for m in range(store.n_modes))
+    for i in range(iters):
+        q, m = qs[i:i + 1], modes[i:i + 1]
+        t0 = time.perf_counter()
+        idx, dist = store.knn(q, m, 1)
+        t1 = time.perf_counter()
+        store.near(q, m, 0.5)
+        t2 = time.perf_counter()
+        store.append(int(m[0]), q)
+        t3 = time.perf_counter()
+        t["nearest"] += t1 - t0
+        t["near"] += t2 - t1
+        t["append"] += t3 - t2
+    grown = sum(store.size(m) for m in range(store.n_modes)) - n0
+    store.close()
+    return {"iterations": iters, "nodes_appended": grown,
+            **{f"{k}_us": 1e6 * v / iters for k, v in t.items()}}
 
 
 def bench_penetration(steps: int = 10) -> dict:
@@ -642,6 +691,21 @@ def run_profile(args):
                           "stats": store.last_stats}), flush=True)
         return 0
 
+    if args.profile == "near":
+        knn, scenes = pkg("knn"), pkg("scenes")
+        w = scenes.make_knn_workload(seed=0)
+        store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], "euclidean")
+        qs = torch.from_numpy(w["queries"]).cuda()
+        _, d16 = store.knn(qs, w["q_mode"], 16)
+        r = np.nan_to_num(d16[:, -1].cpu().numpy(), posinf=0.0)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            offs, _, _ = store.near(qs, w["q_mode"], r)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "near", "launches": args.steps, "s": time.perf_counter() - t0,
+                          "neighbours": int(offs[-1].item())}), flush=True)
+        return 0
+
     if args.profile == "pen":
         pen, col, scenes = pkg("penetration"), pkg("collision"), pkg("scenes")
         sc = scenes.make_arm_scene(0)
@@ -681,7 +745,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--chunks", type=int, default=1, help="pipelined chunks of the end-to-end plan")
     ap.add_argument("--skip-extra", action="store_true", help="only the headline edge-check workload")
-    ap.add_argument("--profile", choices=["early", "full", "knn", "pen"], default=None,
+    ap.add_argument("--profile", choices=["early", "full", "knn", "near", "pen"], default=None,
                     help="short run of the first-pass edge kernel for ncu captures")
     args = ap.parse_args()
     if args.profile:

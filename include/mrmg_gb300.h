@@ -326,6 +326,14 @@ int mrmg_node_store_append(mrmg_node_store *store, int32_t mode, const double *r
  * last node moves into slot idx and the mode shrinks by one.  Synchronises. */
 int mrmg_node_store_remove(mrmg_node_store *store, int32_t mode, int64_t idx, void *stream);
 
+/* Query path of the store (all give identical results): 0 = automatic (the
+ * node-parallel exact path for batches of less than about 4M node-row x
+ * coordinate FP64 work, else the tensor-core path where the metric and shape
+ * allow it), 1 = the tensor-core path wherever it applies, 2 = the
+ * node-parallel exact path (FP64 distance of every node; work items are
+ * (query, 256-node chunk) pairs). */
+int mrmg_node_store_set_path(mrmg_node_store *store, int32_t path);
+
 /* out3: [0] number of modes, [1] nodes in `mode`, [2] tensor-core path. */
 int mrmg_node_store_info(const mrmg_node_store *store, int32_t mode, int64_t *out3);
 

@@ -72,6 +72,7 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_near_fetch": (i32, [vp, vp, vp, i64, vp]),
     "mrmg_node_store_append": (i32, [vp, i32, vp, i64, vp]),
     "mrmg_node_store_info": (i32, [vp, i32, vp]),
+    "mrmg_node_store_set_path": (i32, [vp, i32]),
     "mrmg_node_store_remove": (i32, [vp, i32, i64, vp]),
 }
 

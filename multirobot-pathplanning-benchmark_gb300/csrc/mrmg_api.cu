@@ -1009,6 +1009,13 @@ int mrmg_node_store_remove(mrmg_node_store* s, int32_t mode, int64_t idx, void* 
   return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "node store remove");
 }
 
+int mrmg_node_store_set_path(mrmg_node_store* s, int32_t path) {
+  if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
+  if (path < 0 || path > 2) return fail(MRMG_ERR_ARG, "path: 0 auto, 1 tensor core, 2 exact");
+  knn_store_set_path(s->store, path);
+  return MRMG_OK;
+}
+
 int mrmg_node_store_info(const mrmg_node_store* s, int32_t mode, int64_t* out3) {
   if (!s || !out3) return fail(MRMG_ERR_ARG, "NULL pointer");
   out3[0] = knn_store_modes(s->store);

@@ -182,6 +182,7 @@ cudaError_t knn_store_remove(KnnStore* s, int mode, long long idx, cudaStream_t 
 long long knn_store_count(const KnnStore* s, int mode);
 int knn_store_modes(const KnnStore* s);
 bool knn_store_tc(const KnnStore* s);
+void knn_store_set_path(KnnStore* s, int path);
 void knn_store_free(KnnStore* s);
 cudaError_t knn_store_query(KnnStore* s, KnnScratch* scr, const double* d_qs, long long Q, const int* h_q_mode, int k,
                             long long* d_idx, double* d_dist, int num_sms, int* used_tc, int* n_fallback,

@@ -119,6 +119,142 @@ __global__ void knn_exact_kernel(const double* __restrict__ qs, long long Q, con
   }
 }
 
+// ---------------------------------------------------------------------------
+// Node-parallel exact FP64 paths for small query batches: work items are
+// (query, chunk of kSplitNodes nodes) pairs, so one query spreads over the
+// whole GPU instead of one warp.
+// ---------------------------------------------------------------------------
+constexpr int kSplitNodes = 256;
+
+// index q of the range [off[q], off[q + 1]) holding f (off ascending, off[0] = 0 <= f < off[Q])
+__device__ __forceinline__ long long owner_of(const long long* __restrict__ off, long long Q, long long f) {
+  long long lo = 0, hi = Q;
+  while (hi - lo > 1) {
+    const long long mid = (lo + hi) >> 1;
+    if (off[mid] <= f) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// warp per item: the chunk's k best (distance key, mode-local index), ascending
+template <int KM>
+__global__ void knn_split_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
+                                 const long long* __restrict__ ioff, const double* __restrict__ nodes,
+                                 const long long* __restrict__ mode_beg, const long long* __restrict__ mode_end,
+                                 SliceTab t, int metric, int k, long long* __restrict__ cand_key,
+                                 long long* __restrict__ cand_idx) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  const long long n_items = ioff[Q];
+  for (long long it = warp; it < n_items; it += nwarps) {
+    const long long q = owner_of(ioff, Q, it);
+    const int m = q_mode[q];
+    const long long b = mode_beg[m];
+    const long long s = b + (it - ioff[q]) * kSplitNodes;
+    const long long e = s + kSplitNodes < mode_end[m] ? s + kSplitNodes : mode_end[m];
+    long long td[KM];
+    long long ti[KM];
+#pragma unroll
+    for (int i = 0; i < KM; i++) { td[i] = 0x7ff0000000000000ll; ti[i] = -1; }
+    const double* qq = qs + q * t.D;
+    for (long long x = s + lane; x < e; x += 32) {
+      const double* xx = nodes + x * t.D;
+      auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
+      topk_insert<KM>(td, ti, k, dkey(dist_of(t, metric, dfun)), x - b);
+    }
+    int head = 0;
+    for (int r = 0; r < k; r++) {
+      long long hd = 0x7ff0000000000000ll;
+      long long hi = 0x7fffffffffffffffll;
+#pragma unroll
+      for (int i = 0; i < KM; i++)
+        if (i == head && i < k) { hd = td[i]; hi = ti[i]; }
+      if (hi < 0) hi = 0x7fffffffffffffffll;
+      const int win = warp_argmin(hd, hi);
+      const long long wd = __shfl_sync(MRMG_FULL, hd, win);
+      const long long wi = __shfl_sync(MRMG_FULL, hi, win);
+      if (lane == 0) {
+        cand_key[it * k + r] = wd;
+        cand_idx[it * k + r] = wi == 0x7fffffffffffffffll ? -1 : wi;
+      }
+      if (lane == win) head++;
+    }
+  }
+}
+
+// warp per query: lane l takes the query's items l, l + 32, ... whole and in
+// order (each item's list is sorted and later items hold higher indices, so
+// equal distances still arrive in index order), then the lanes merge
+template <int KM>
+__global__ void knn_split_merge_kernel(long long Q, const long long* __restrict__ ioff, int k,
+                                       const long long* __restrict__ cand_key, const long long* __restrict__ cand_idx,
+                                       long long* __restrict__ out_idx, double* __restrict__ out_dist) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long q = warp; q < Q; q += nwarps) {
+    long long td[KM];
+    long long ti[KM];
+#pragma unroll
+    for (int i = 0; i < KM; i++) { td[i] = 0x7ff0000000000000ll; ti[i] = -1; }
+    for (long long it = ioff[q] + lane; it < ioff[q + 1]; it += 32)
+      for (int r = 0; r < k; r++) {
+        const long long id = cand_idx[it * k + r];
+        const long long d = cand_key[it * k + r];
+        if (id < 0 || !(d < td[k - 1])) break;   // sorted: nothing further enters
+        topk_insert<KM>(td, ti, k, d, id);
+      }
+    int head = 0;
+    for (int r = 0; r < k; r++) {
+      long long hd = 0x7ff0000000000000ll;
+      long long hi = 0x7fffffffffffffffll;
+#pragma unroll
+      for (int i = 0; i < KM; i++)
+        if (i == head && i < k) { hd = td[i]; hi = ti[i]; }
+      if (hi < 0) hi = 0x7fffffffffffffffll;
+      const int win = warp_argmin(hd, hi);
+      const long long wd = __shfl_sync(MRMG_FULL, hd, win);
+      const long long wi = __shfl_sync(MRMG_FULL, hi, win);
+      if (lane == 0) {
+        out_idx[q * k + r] = wi == 0x7fffffffffffffffll ? -1 : wi;
+        out_dist[q * k + r] = wi == 0x7fffffffffffffffll ? __longlong_as_double(0x7ff0000000000000ll)
+                                                         : __longlong_as_double(wd);
+      }
+      if (lane == win) head++;
+    }
+  }
+}
+
+// radius, exact: warp per (query, bitmap word), lane = node of the word
+__global__ void near_split_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
+                                  const double* __restrict__ nodes, const long long* __restrict__ mode_beg,
+                                  const long long* __restrict__ mode_end, SliceTab t, int metric,
+                                  const double* __restrict__ rp, const long long* __restrict__ woff,
+                                  unsigned* __restrict__ bits, unsigned long long* __restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  const long long total = woff[Q];
+  for (long long f = warp; f < total; f += nwarps) {
+    const long long q = owner_of(woff, Q, f);
+    const int m = q_mode[q];
+    const long long id = (f - woff[q]) * 32 + lane;
+    bool in = false;
+    if (id < mode_end[m] - mode_beg[m]) {
+      const double* qq = qs + q * t.D;
+      const double* xx = nodes + (mode_beg[m] + id) * t.D;
+      auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
+      in = dist_of(t, metric, dfun) <= rp[q];
+    }
+    const unsigned mk = __ballot_sync(MRMG_FULL, in);
+    if (lane == 0) {
+      bits[f] = mk;
+      if (mk) atomicAdd(counts + q, (unsigned long long)__popc(mk));
+    }
+  }
+}
+
 }  // namespace
 
 cudaError_t knn_exact(const double* qs, long long Q, const int* q_mode, const long long* q_list, long long n_list,
@@ -980,6 +1116,7 @@ struct KnnStore {
   std::vector<int> h_tile0;
   int* d_qmode = nullptr;                 // exact path: uploaded query modes
   long long qmode_cap = 0;
+  int path = 0;                           // 0 auto, 1 tensor core where supported, 2 node-parallel exact
 };
 
 bool knn_tc_supported(const SliceTab& t, int metric) {
@@ -1178,6 +1315,7 @@ cudaError_t knn_store_remove(KnnStore* s, int mode, long long idx, cudaStream_t 
 long long knn_store_count(const KnnStore* s, int mode) { return mode < s->n_modes ? s->cnt[mode] : 0; }
 int knn_store_modes(const KnnStore* s) { return s->n_modes; }
 bool knn_store_tc(const KnnStore* s) { return s->tc; }
+void knn_store_set_path(KnnStore* s, int path) { s->path = path; }
 
 void knn_store_free(KnnStore* s) {
   if (s->nodes) cudaFree(s->nodes);
@@ -1368,13 +1506,95 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   return cudaSuccess;
 }
 
-// k nearest on the store: the tensor-core path for its formats and k <= 16,
-// else the exact kernel over the store's nodes
+// FP64 work (node rows x coordinates) below which a batch takes the
+// node-parallel exact path even where the tensor-core path applies: about
+// 150,000 distances in 28-D, some 10 us of the GPU's FP64 rate, less than the
+// tensor-core path's per-tile setup for a handful of queries
+constexpr long long kSmallWork = 1ll << 22;
+
+static long long batch_work(const KnnStore* s, const int* h_q_mode, long long Q) {
+  if (s->path == 1) return kSmallWork + 1;
+  if (s->path == 2) return 0;
+  long long w = 0;
+  for (long long q = 0; q < Q; q++) w += s->cnt[h_q_mode[q]];
+  return w * std::max(s->D, 1);
+}
+
+// pinned + device scratch of at least the given sizes
+static cudaError_t scratch_reserve(KnnScratch* scr, size_t dev_bytes, size_t host_bytes) {
+  if (scr->bytes < dev_bytes) {
+    if (scr->block) cudaFree(scr->block);
+    scr->block = nullptr;
+    scr->bytes = 0;
+    cudaError_t e = cudaMalloc(&scr->block, dev_bytes);
+    if (e != cudaSuccess) return e;
+    scr->bytes = dev_bytes;
+  }
+  if (scr->host_bytes < host_bytes) {
+    if (scr->host) cudaFreeHost(scr->host);
+    scr->host = nullptr;
+    scr->host_bytes = 0;
+    cudaError_t e = cudaMallocHost(&scr->host, host_bytes);
+    if (e != cudaSuccess) return e;
+    scr->host_bytes = host_bytes;
+  }
+  return cudaSuccess;
+}
+
+// node-parallel exact k nearest: items (query, 256-node chunk), then a merge
+static cudaError_t knn_split_query(KnnStore* s, KnnScratch* scr, const double* d_qs, long long Q, const int* h_q_mode,
+                                   int k, long long* d_idx, double* d_dist, int num_sms, cudaStream_t st) {
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b_qm = al(sizeof(int) * Q), b_off = al(sizeof(long long) * (Q + 1));
+  const size_t b_up = b_qm + b_off;
+  cudaError_t e = scratch_reserve(scr, 0, b_up);
+  if (e != cudaSuccess) return e;
+  unsigned char* hp = (unsigned char*)scr->host;
+  std::memcpy(hp, h_q_mode, sizeof(int) * Q);
+  long long* ioff = (long long*)(hp + b_qm);
+  ioff[0] = 0;
+  for (long long q = 0; q < Q; q++) ioff[q + 1] = ioff[q] + (s->cnt[h_q_mode[q]] + kSplitNodes - 1) / kSplitNodes;
+  const long long n_items = ioff[Q];
+  const size_t b_cand = al(sizeof(long long) * std::max<long long>(n_items, 1) * k);
+  e = scratch_reserve(scr, b_up + 2 * b_cand, 0);
+  if (e != cudaSuccess) return e;
+  unsigned char* p = (unsigned char*)scr->block;
+  const int* d_qm = (const int*)p;
+  const long long* d_ioff = (const long long*)(p + b_qm);
+  long long* d_ck = (long long*)(p + b_up);
+  long long* d_ci = (long long*)(p + b_up + b_cand);
+  e = cudaMemcpyAsync(p, hp, b_up, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  if (n_items > 0) {
+    const int grid = (int)std::min<long long>((n_items + 3) / 4, (long long)num_sms * 16);
+    if (k <= 16)
+      knn_split_kernel<16><<<grid, 128, 0, st>>>(d_qs, Q, d_qm, d_ioff, s->nodes, s->d_beg, s->d_end, s->slices,
+                                                 s->metric, k, d_ck, d_ci);
+    else
+      knn_split_kernel<kKnnMaxK><<<grid, 128, 0, st>>>(d_qs, Q, d_qm, d_ioff, s->nodes, s->d_beg, s->d_end, s->slices,
+                                                       s->metric, k, d_ck, d_ci);
+  }
+  const int mgrid = (int)std::max<long long>(1, std::min<long long>((Q + 3) / 4, (long long)num_sms * 16));
+  if (k <= 16)
+    knn_split_merge_kernel<16><<<mgrid, 128, 0, st>>>(Q, d_ioff, k, d_ck, d_ci, d_idx, d_dist);
+  else
+    knn_split_merge_kernel<kKnnMaxK><<<mgrid, 128, 0, st>>>(Q, d_ioff, k, d_ck, d_ci, d_idx, d_dist);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // the pinned tables are reused by the next call
+  return e;
+}
+
+// k nearest on the store: the node-parallel exact path for small batches,
+// the tensor-core path for its formats and k <= 16, else the exact
+// warp-per-query kernel
 cudaError_t knn_store_query(KnnStore* s, KnnScratch* scr, const double* d_qs, long long Q, const int* h_q_mode, int k,
                             long long* d_idx, double* d_dist, int num_sms, int* used_tc, int* n_fallback,
                             cudaStream_t st) {
   *used_tc = 0;
   *n_fallback = 0;
+  const bool small = batch_work(s, h_q_mode, Q) <= kSmallWork;
+  if (small || (!(s->tc && k <= 16) && Q < 2048))
+    return knn_split_query(s, scr, d_qs, Q, h_q_mode, k, d_idx, d_dist, num_sms, st);
   if (s->tc && k <= 16) {
     *used_tc = 1;
     cudaError_t e = knn_query(s, d_qs, Q, h_q_mode, k, d_idx, d_dist, scr, num_sms, n_fallback, st);
@@ -1440,7 +1660,8 @@ cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long
                        const double* h_radius, double add_eps, long long* d_offsets, long long* d_idx, double* d_dist,
                        long long cap, int num_sms, long long* total_out, cudaStream_t st) {
   const int n_modes = s->n_modes;
-  KnnStore* tc = s->tc ? s : nullptr;
+  const bool small = batch_work(s, h_q_mode, Q) <= kSmallWork;
+  KnnStore* tc = s->tc && !small ? s : nullptr;   // else every node is checked in FP64, node-parallel
   const double* nodes = s->nodes;
   const SliceTab& t = s->slices;
   const int metric = s->metric;
@@ -1522,14 +1743,22 @@ cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long
       knn_tc_kernel<KNN_FMT_AGENT, true><<<(int)pl.items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(
           tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, (int*)(d_ctr + 1), ro);
     }
-  } else if (!tc && Wtot > 0) {
-    e = cudaMemsetAsync(d_bits, 0xff, sizeof(unsigned) * Wtot, st);   // every node is a candidate
   }
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int grid = near_grid(Q, num_sms);
-  near_exact_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, s->d_end, t, metric, d_rp,
-                                                      d_woff, d_bits, d_cnt);
+  if (tc) {
+    near_exact_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, s->d_end, t, metric, d_rp,
+                                                        d_woff, d_bits, d_cnt);
+  } else {
+    e = cudaMemsetAsync(d_cnt, 0, sizeof(long long) * Q, st);
+    if (e != cudaSuccess) return e;
+    if (Wtot > 0) {
+      const int g2 = (int)std::min<long long>((Wtot + 3) / 4, (long long)num_sms * 16);
+      near_split_kernel<<<g2, 128, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, s->d_end, t, metric, d_rp, d_woff,
+                                            d_bits, (unsigned long long*)d_cnt);
+    }
+  }
   near_scan_kernel<<<1, 1024, 0, st>>>(d_cnt, Q, d_offsets, d_offs, d_ctr);
   if (cap > 0)
     near_emit_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, t, metric, d_woff, d_bits,

@@ -54,7 +54,9 @@ class NodeStore:
     max_euclidean queries use the tensor-core candidate path (tcgen05 split-
     BF16 distance GEMM, certified, FP64 re-rank); other metrics the exact one."""
 
-    def __init__(self, nodes, mode_offsets, slices, metric: str = "euclidean", stream=None):
+    PATHS = {"auto": 0, "tensor_core": 1, "exact": 2}
+
+    def __init__(self, nodes, mode_offsets, slices, metric: str = "euclidean", stream=None, path: str = "auto"):
         import ctypes as C
 
         self.lib = _lib.load()
@@ -70,12 +72,19 @@ class NodeStore:
                                                    C.byref(h), _lib.stream_handle(stream)), "node store")
         self.h = h
         self.nodes = None          # the store holds its own copy
+        self.set_path(path)
         self.last_stats = {}
 
+    def set_path(self, path: str):
+        """'auto', 'tensor_core' (wherever the metric allows) or 'exact'
+        (node-parallel FP64); the results are identical."""
+        _lib.check(self.lib.mrmg_node_store_set_path(self.h, self.PATHS[path]), "set_path")
+        self.path = path
+
     @classmethod
-    def empty(cls, dim: int, n_modes: int, slices, metric: str = "euclidean", stream=None):
+    def empty(cls, dim: int, n_modes: int, slices, metric: str = "euclidean", stream=None, path: str = "auto"):
         """A store with ``n_modes`` empty modes, filled by ``append``."""
-        return cls(np.zeros((0, dim)), np.zeros(n_modes + 1, dtype=np.int64), slices, metric, stream)
+        return cls(np.zeros((0, dim)), np.zeros(n_modes + 1, dtype=np.int64), slices, metric, stream, path)
 
     def append(self, mode: int, rows, stream=None):
         """Appends rows [n, D] (host or device) to ``mode``; their mode-local

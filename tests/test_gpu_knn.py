@@ -49,34 +49,38 @@ def test_knn_exact_all_metrics_vs_oracle(gpu, oracle):
             assert np.array_equal(dist.cpu().numpy(), od), (metric, k)
 
 
-def test_knn_tensor_core_golden(gpu):
+@pytest.mark.parametrize("path", ["tensor_core", "exact", "auto"])
+def test_knn_store_golden(gpu, path):
     knn = pkg("knn")
     g = golden("knn.npz")
     for metric in ["euclidean", "max_euclidean"]:
-        store = knn.NodeStore(g["nodes"], g["mode_off"], g["slices"], metric)
+        store = knn.NodeStore(g["nodes"], g["mode_off"], g["slices"], metric, path=path)
         idx, dist = store.knn(g["queries"], g["q_mode"], int(g["k"]))
-        assert store.last_stats["tensor_core"]
+        assert store.last_stats["tensor_core"] == (path == "tensor_core")
         assert np.array_equal(idx.cpu().numpy(), g[f"idx_{metric}"]), metric
 
 
+@pytest.mark.parametrize("path", ["auto", "exact"])
 @pytest.mark.parametrize("metric", ["euclidean", "max_euclidean"])
-def test_knn_tensor_core_workload_vs_oracle(gpu, oracle, metric):
+def test_knn_workload_vs_oracle(gpu, oracle, metric, path):
     """The per-mode workload (Zipf modes, clustered nodes) at reduced size:
-    indices and FP64 distances identical to the oracle's exact selection."""
+    indices and FP64 distances identical to the oracle's exact selection
+    (the automatic path takes the tensor cores at this size)."""
     knn, scenes = pkg("knn"), pkg("scenes")
     w = scenes.make_knn_workload(seed=3, n_nodes=40_000, n_queries=1024)
-    store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], metric)
+    store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], metric, path=path)
     for k in (1, 10, 16):
         idx, dist = store.knn(w["queries"], w["q_mode"], k)
         oi, od = oracle.knn(w["queries"], w["q_mode"], w["nodes"], w["mode_offsets"], w["slices"], metric, k)
         assert np.array_equal(idx.cpu().numpy(), oi), (metric, k)
         assert np.array_equal(dist.cpu().numpy(), od), (metric, k)
-        assert store.last_stats["tensor_core"]
+        assert store.last_stats["tensor_core"] == (path == "auto")
         assert store.last_stats["rerun_exact"] < 0.05 * len(w["queries"])
 
 
-def test_knn_store_other_metrics_and_edge_modes(gpu, oracle):
-    """Metrics outside the tensor-core shapes and k > 16 use the exact kernel;
+@pytest.mark.parametrize("path", ["auto", "tensor_core", "exact"])
+def test_knn_store_other_metrics_and_edge_modes(gpu, oracle, path):
+    """Metrics outside the tensor-core shapes and k > 16 use the exact kernels;
     empty and tiny modes pad with index -1 / +inf like the oracle."""
     knn = pkg("knn")
     rng = np.random.default_rng(9)
@@ -85,8 +89,9 @@ def test_knn_store_other_metrics_and_edge_modes(gpu, oracle):
     qs = rng.uniform(-2, 2, (100, 14))
     qm = rng.integers(0, 4, 100).astype(np.int32)
     sl = [[0, 7], [7, 14]]
-    for metric, k in [("sum_euclidean", 10), ("max", 10), ("euclidean", 20), ("euclidean", 10), ("max_euclidean", 12)]:
-        store = knn.NodeStore(nodes, off, sl, metric)
+    for metric, k in [("sum_euclidean", 10), ("max", 10), ("euclidean", 20), ("euclidean", 10), ("max_euclidean", 12),
+                      ("max", 40)]:
+        store = knn.NodeStore(nodes, off, sl, metric, path=path)
         idx, dist = store.knn(qs, qm, k)
         oi, od = oracle.knn(qs, qm, nodes, off, sl, metric, k)
         assert np.array_equal(idx.cpu().numpy(), oi), (metric, k)
@@ -99,14 +104,15 @@ def _csr_equal(got, want):
     return np.array_equal(offs, wo) and np.array_equal(idx, wi) and np.array_equal(dist, wd)
 
 
-def test_near_golden(gpu, oracle):
-    """Radius neighbours on the tensor-core store against the reference's
-    find_nearest_indices (radii on, just inside and just outside node
-    distances by less than the added 1e-10; an empty and a one-node mode)."""
+@pytest.mark.parametrize("path", ["tensor_core", "exact"])
+def test_near_golden(gpu, oracle, path):
+    """Radius neighbours against the reference's find_nearest_indices (radii
+    on, just inside and just outside node distances by less than the added
+    1e-10; an empty and a one-node mode)."""
     knn = pkg("knn")
     g = golden("near.npz")
     for metric in ["euclidean", "max_euclidean"]:
-        store = knn.NodeStore(g["nodes"], g["mode_off"], g["slices"], metric)
+        store = knn.NodeStore(g["nodes"], g["mode_off"], g["slices"], metric, path=path)
         offs, idx, dist = store.near(g["queries"], g["q_mode"], g[f"radius_{metric}"])
         assert np.array_equal(offs.cpu().numpy(), g[f"offsets_{metric}"]), metric
         assert np.array_equal(idx.cpu().numpy(), g[f"idx_{metric}"]), metric
@@ -115,8 +121,9 @@ def test_near_golden(gpu, oracle):
         assert _csr_equal((offs, idx, dist), want), metric
 
 
+@pytest.mark.parametrize("path", ["auto", "exact"])
 @pytest.mark.parametrize("metric", ["euclidean", "max_euclidean"])
-def test_near_workload_vs_oracle(gpu, oracle, metric):
+def test_near_workload_vs_oracle(gpu, oracle, metric, path):
     """The per-mode workload at reduced size, radii at the 24th-nearest
     distance (some lowered by 0.5e-10, so that only the added epsilon keeps the
     node), a tiny output capacity (the fetch path) and r = 0."""
@@ -126,7 +133,7 @@ def test_near_workload_vs_oracle(gpu, oracle, metric):
     r = od[:, -1].copy()
     r[::3] -= 0.5e-10
     r[~np.isfinite(r)] = 1.0
-    store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], metric)
+    store = knn.NodeStore(w["nodes"], w["mode_offsets"], w["slices"], metric, path=path)
     want = oracle.near(w["queries"], w["q_mode"], w["nodes"], w["mode_offsets"], w["slices"], metric, r)
     assert want[0][-1] > 0
     assert _csr_equal(store.near(w["queries"], w["q_mode"], r), want)
@@ -135,7 +142,8 @@ def test_near_workload_vs_oracle(gpu, oracle, metric):
     assert _csr_equal(store.near(w["queries"], w["q_mode"], 0.0), z)
 
 
-def test_near_other_metrics_and_edge_modes(gpu, oracle):
+@pytest.mark.parametrize("path", ["auto", "tensor_core", "exact"])
+def test_near_other_metrics_and_edge_modes(gpu, oracle, path):
     """Metrics outside the tensor-core shapes check every node in FP64; empty
     and tiny modes, negative and infinite radii, and no queries at all."""
     knn = pkg("knn")
@@ -148,7 +156,7 @@ def test_near_other_metrics_and_edge_modes(gpu, oracle):
     r = rng.uniform(0.5, 4.0, 100)
     r[5], r[6] = -1.0, np.inf
     for metric in ["sum_euclidean", "max", "euclidean", "max_euclidean"]:
-        store = knn.NodeStore(nodes, off, sl, metric)
+        store = knn.NodeStore(nodes, off, sl, metric, path=path)
         want = oracle.near(qs, qm, nodes, off, sl, metric, r)
         assert _csr_equal(store.near(qs, qm, r), want), metric
         offs, idx, dist = store.near(qs[:0], qm[:0], 1.0)
@@ -178,8 +186,9 @@ class _HostModes:
         return np.concatenate(self.modes), off
 
 
-@pytest.mark.parametrize("metric", ["euclidean", "max_euclidean", "sum_euclidean"])
-def test_node_store_incremental(gpu, oracle, metric):
+@pytest.mark.parametrize("metric,path", [("euclidean", "tensor_core"), ("max_euclidean", "tensor_core"),
+                                         ("sum_euclidean", "auto"), ("euclidean", "exact")])
+def test_node_store_incremental(gpu, oracle, metric, path):
     """A store grown by appends (single rows across tile boundaries and
     capacity doublings, batches, modes created past the last) and shrunk by
     removals answers k-NN and radius queries like the oracle over the same
@@ -192,7 +201,7 @@ def test_node_store_incremental(gpu, oracle, metric):
     half = [off[m] + (off[m + 1] - off[m]) // 2 for m in range(4)]
     first = np.concatenate([nodes[off[m]:half[m]] for m in range(4)])
     first_off = np.concatenate([[0], np.cumsum([half[m] - off[m] for m in range(4)])])
-    store = knn.NodeStore(first, first_off, sl, metric)
+    store = knn.NodeStore(first, first_off, sl, metric, path=path)
     for m in range(4):
         host.append(m, nodes[off[m]:half[m]])
     # RRT-style single rows into mode 1, PRM-style batches elsewhere, a new mode 6
