@@ -119,6 +119,24 @@ int mrmg_arm_scene_create(int32_t n_robots, int32_t q_dim, const int32_t *h_q_of
                           int32_t n_boxes, const double *h_box_lo, const double *h_box_hi,
                           double band, mrmg_scene **out);
 
+/* Per-mode scene tables (objects placed or attached by mode: the rai scenes'
+ * set_to_mode, rai_base_env.py:704-840, and VAMP's
+ * attached objects, mr_vamp_env.py:506-650).  The box pool is the scene's
+ * boxes; mode m keeps boxes h_mode_boxes[h_mode_box_off[m] ..
+ * h_mode_box_off[m+1]).  h_sphere_attach[S] (may be NULL) tags spheres that
+ * belong to an attached object (id >= 0; -1 = part of the robot, always
+ * present): mode m keeps the tagged spheres whose id is listed in
+ * h_mode_attach[h_mode_attach_off[m] .. h_mode_attach_off[m+1]).  Each mode
+ * gets its own device tables; set once per scene. */
+int mrmg_arm_scene_set_modes(mrmg_scene *sc, int32_t n_modes, const int32_t *h_sphere_attach,
+                             const int64_t *h_mode_box_off, const int32_t *h_mode_boxes,
+                             const int64_t *h_mode_attach_off, const int32_t *h_mode_attach);
+
+/* Selects the tables later calls on this scene use: mode m, or -1 for the
+ * scene as created (every box and sphere).  A host-side switch; launches
+ * already captured in a CUDA graph keep the tables of their capture. */
+int mrmg_scene_set_mode(mrmg_scene *sc, int32_t mode);
+
 int mrmg_scene_destroy(mrmg_scene *scene);
 
 /* Scene facts: [0] kind (0 abstract, 1 arm), [1] q_dim, [2] spheres per group,

@@ -70,6 +70,8 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_knn": (i32, [vp, vp, i64, vp, i32, vp, vp, vp, vp]),
     "mrmg_near": (i32, [vp, vp, i64, vp, vp, f64, vp, vp, vp, i64, vp, vp]),
     "mrmg_near_fetch": (i32, [vp, vp, vp, i64, vp]),
+    "mrmg_arm_scene_set_modes": (i32, [vp, i32, vp, vp, vp, vp, vp]),
+    "mrmg_scene_set_mode": (i32, [vp, i32]),
     "mrmg_node_store_append": (i32, [vp, i32, vp, i64, vp]),
     "mrmg_node_store_info": (i32, [vp, i32, vp]),
     "mrmg_node_store_set_path": (i32, [vp, i32]),

@@ -79,6 +79,23 @@ class Gb300Scene:
         self.h = h
         self.q_dim = scene.q_dim
         self._slot_map = None
+        self.mode = -1
+        if self.kind == 1 and scene.n_modes:
+            t = scene.mode_tables()
+            _lib.check(self.lib.mrmg_arm_scene_set_modes(
+                self.h, scene.n_modes, P(t["sphere_attach"]), P(t["box_off"]), P(t["boxes"]), P(t["attach_off"]),
+                P(t["attach"])), "scene modes")
+
+    def set_mode(self, mode: int):
+        """Tables of mode ``mode`` for later calls (-1: the scene as created,
+        every box and sphere).  Graphs captured earlier keep their tables."""
+        _lib.check(self.lib.mrmg_scene_set_mode(self.h, int(mode)), "set_mode")
+        self.mode = int(mode)
+
+    def _n_boxes(self) -> int:
+        if self.mode >= 0:
+            return len(self.scene.mode_boxes[self.mode])
+        return len(self.scene.box_lo)
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:
@@ -110,10 +127,11 @@ class Gb300Scene:
         if self.kind != 1:
             return np.zeros(0, dtype=np.int32)
         qt = _dev_tensor(samples)
-        order = np.zeros(max(len(self.scene.box_lo), 1), dtype=np.int32)
+        nb = self._n_boxes()
+        order = np.zeros(max(nb, 1), dtype=np.int32)
         _lib.check(self.lib.mrmg_arm_scene_tune_order(self.h, qt.data_ptr(), _dt_code(qt), qt.shape[0],
                                                       order.ctypes.data, _lib.stream_handle(stream)))
-        return order[: len(self.scene.box_lo)]
+        return order[:nb]
 
     def last_call_stats(self) -> dict:
         out = np.zeros(4, dtype=np.int64)

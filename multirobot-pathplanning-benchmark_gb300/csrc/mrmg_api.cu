@@ -54,6 +54,27 @@ struct DevBlock {
 
 }  // namespace
 
+// creation inputs of an arm scene that per-mode tables are built from
+struct ArmSrc {
+  int S = 0, B = 0, SPG = 0, G = 0;
+  double delta = 0.0;
+  std::vector<double> local, radius, box_lo, box_hi;
+  std::vector<int> slot_sphere, grp;
+};
+
+// one complete set of sphere- and box-dependent tables: the device views in
+// `d` / `pd` and host copies of the box tables (their test order can be tuned)
+struct ArmTables {
+  ArmDev d{};
+  PenDev pd{};
+  std::vector<float4> box32_host;
+  std::vector<double> box64_host;
+  // host data kept until the upload
+  std::vector<float4> sph32, band32, gbs, pen_sph, pen_box;
+  std::vector<double> sph64;
+  std::vector<int4> pen_task;
+};
+
 // work-queue counters are 32-bit: keep every batch well below 2^31
 constexpr long long kMaxBatch = (1ll << 31) - (1ll << 26);
 
@@ -78,8 +99,14 @@ struct mrmg_scene {
   PenDev pen{};                      // arm: path-penetration cost tables
   double* d_pen_seg = nullptr;       // per-segment cost scratch
   long long pen_seg_cap = 0;
-  std::vector<float4> box32_host;    // arm: box tables in their current test order
-  std::vector<double> box64_host;
+  // arm: the table sets -- the scene as created, and one per mode when modes
+  // are declared; `arm` / `pen` are copies of the current set's views
+  ArmTables base;
+  std::vector<ArmTables> modes;
+  int cur_mode = -1;
+  void* d_mode_tables = nullptr;
+  ArmSrc src;
+  ArmTables& tabs() { return cur_mode < 0 ? base : modes[cur_mode]; }
 };
 
 namespace {
@@ -153,6 +180,141 @@ float f32_down(double x) {
   float f = (float)x;
   if ((double)f > x) f = nextafterf(f, -INFINITY);
   return f;
+}
+
+// Slot tables of one sphere set: slots whose sphere is off (or absent) are
+// padding, and each group bound covers the group's spheres that are on: the
+// centre of their local offsets and a radius over |offset - centre| + r,
+// widened by 4 delta (FP32 error of the group centre and of each sphere
+// centre, plus rounding of the bound test); a group with none is never near.
+void sphere_tables(const ArmSrc& a, const std::vector<char>& on, ArmTables* t) {
+  const int NS = a.G * a.SPG;
+  t->sph32.assign(NS, make_float4(0.f, 0.f, 0.f, 0.f));
+  t->band32.assign(NS, make_float4(-1.f, -1.f, 0.f, 0.f));
+  t->sph64.assign((size_t)NS * 5, 0.0);
+  t->gbs.assign(a.G, make_float4(0.f, 0.f, 0.f, -1.f));
+  auto live = [&](int sl) { const int i = a.slot_sphere[sl]; return i >= 0 && on[i] ? i : -1; };
+  for (int sl = 0; sl < NS; sl++) {
+    const int i = live(sl);
+    if (i < 0) { t->sph64[(size_t)sl * 5 + 3] = -1.0; continue; }
+    const double* l = &a.local[3 * i];
+    const double r = a.radius[i];
+    t->sph32[sl] = make_float4((float)l[0], (float)l[1], (float)l[2], (float)r);
+    const double rhi = r + a.delta, rlo = r - a.delta;
+    t->band32[sl] = make_float4(rlo > 0 ? f32_down(rlo * rlo * (1.0 - 1e-6)) : -1.f, f32_up(rhi * rhi * (1.0 + 1e-6)),
+                                f32_up(r + a.delta), f32_down(r - a.delta));
+    for (int k = 0; k < 3; k++) t->sph64[(size_t)sl * 5 + k] = l[k];
+    t->sph64[(size_t)sl * 5 + 3] = r;
+    t->sph64[(size_t)sl * 5 + 4] = r * r;
+  }
+  for (int g = 0; g < a.G; g++) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    int cnt = 0;
+    for (int v = 0; v < a.SPG; v++) {
+      const int i = live(g * a.SPG + v);
+      if (i < 0) continue;
+      cnt++;
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::min(lo[k], a.local[3 * i + k]);
+        hi[k] = std::max(hi[k], a.local[3 * i + k]);
+      }
+    }
+    if (!cnt) continue;
+    double c[3], rad = 0.0;
+    for (int k = 0; k < 3; k++) c[k] = 0.5 * (lo[k] + hi[k]);
+    for (int v = 0; v < a.SPG; v++) {
+      const int i = live(g * a.SPG + v);
+      if (i < 0) continue;
+      double d2 = 0.0;
+      for (int k = 0; k < 3; k++) d2 += (a.local[3 * i + k] - c[k]) * (a.local[3 * i + k] - c[k]);
+      rad = std::max(rad, std::sqrt(d2) + a.radius[i]);
+    }
+    rad += 4.0 * a.delta;
+    t->gbs[g] = make_float4((float)c[0], (float)c[1], (float)c[2], f32_up(rad * rad * (1.0 + 1e-6)));
+  }
+}
+
+// box tables of a box set, larger boxes first (earlier certain collisions;
+// verdicts do not depend on the order): FP32 centre / half extent (the band
+// absorbs their rounding, |box| < 1e6 m) and FP64 lo / hi
+void box_tables(const ArmSrc& a, std::vector<int> boxes, ArmTables* t) {
+  auto vol = [&](int b) {
+    double v = 1.0;
+    for (int k = 0; k < 3; k++) v *= std::max(0.0, a.box_hi[3 * b + k] - a.box_lo[3 * b + k]);
+    return v;
+  };
+  std::stable_sort(boxes.begin(), boxes.end(), [&](int x, int y) { return vol(x) > vol(y); });
+  const int B = (int)boxes.size();
+  t->box32_host.assign(2 * (size_t)B, make_float4(0.f, 0.f, 0.f, 0.f));
+  t->box64_host.assign(6 * (size_t)B, 0.0);
+  for (int bi = 0; bi < B; bi++) {
+    const double* lo = &a.box_lo[3 * boxes[bi]];
+    const double* hi = &a.box_hi[3 * boxes[bi]];
+    t->box32_host[2 * bi] = make_float4((float)(0.5 * (lo[0] + hi[0])), (float)(0.5 * (lo[1] + hi[1])),
+                                        (float)(0.5 * (lo[2] + hi[2])), 0.f);
+    t->box32_host[2 * bi + 1] = make_float4((float)(0.5 * (hi[0] - lo[0])), (float)(0.5 * (hi[1] - lo[1])),
+                                            (float)(0.5 * (hi[2] - lo[2])), 0.f);
+    for (int k = 0; k < 3; k++) { t->box64_host[6 * (size_t)bi + k] = lo[k]; t->box64_host[6 * (size_t)bi + 3 + k] = hi[k]; }
+  }
+  t->d.B = B;
+}
+
+// penetration-cost tables: the set's spheres in slot order (robot, then
+// frame), tasks of two consecutive spheres of one robot, boxes in the given order
+void pen_tables(const ArmSrc& a, int R, const std::vector<char>& on, const std::vector<int>& boxes, ArmTables* t) {
+  PenDev& pd = t->pd;
+  int cnt[kMaxRobots][kMaxLinks + 1] = {};
+  t->pen_sph.clear();
+  t->pen_task.clear();
+  for (int sl = 0; sl < a.G * a.SPG; sl++) {
+    const int i = a.slot_sphere[sl];
+    if (i < 0 || !on[i]) continue;
+    const int r = a.grp[sl / a.SPG] & 0xff, k = a.grp[sl / a.SPG] >> 8;
+    cnt[r][k]++;
+    t->pen_sph.push_back(make_float4((float)a.local[3 * i], (float)a.local[3 * i + 1], (float)a.local[3 * i + 2],
+                                     (float)a.radius[i]));
+  }
+  int acc = 0;
+  for (int r = 0; r < kMaxRobots; r++) {
+    for (int k = 0; k <= kMaxLinks; k++) { pd.lk[r][k] = acc; acc += cnt[r][k]; }
+    pd.lk[r][kMaxLinks + 1] = acc;
+  }
+  for (int r = 0; r < R; r++) {
+    const int s0 = pd.lk[r][0], s1 = pd.lk[r][kMaxLinks + 1];
+    for (int i = s0; i < s1; i += 2) t->pen_task.push_back(make_int4(i, i + 1 < s1 ? i + 1 : -1, s0, s1));
+  }
+  t->pen_box.assign(2 * boxes.size(), make_float4(0.f, 0.f, 0.f, 0.f));
+  for (size_t j = 0; j < boxes.size(); j++) {
+    const double* lo = &a.box_lo[3 * boxes[j]];
+    const double* hi = &a.box_hi[3 * boxes[j]];
+    t->pen_box[2 * j] = make_float4((float)(0.5 * (lo[0] + hi[0])), (float)(0.5 * (lo[1] + hi[1])),
+                                    (float)(0.5 * (lo[2] + hi[2])), 0.f);
+    t->pen_box[2 * j + 1] = make_float4((float)(0.5 * (hi[0] - lo[0])), (float)(0.5 * (hi[1] - lo[1])),
+                                        (float)(0.5 * (hi[2] - lo[2])), 0.f);
+  }
+  pd.S = (int)t->pen_sph.size();
+  pd.B = (int)boxes.size();
+  pd.NTK = (int)t->pen_task.size();
+}
+
+// registers a table set's arrays with the upload block
+void add_tables(DevBlock& blk, ArmTables* t) {
+  blk.add(t->sph64.data(), t->sph64.size(), &t->d.sph64);
+  blk.add(t->box64_host.data(), t->box64_host.size(), &t->d.box64);
+  blk.add(t->sph32.data(), t->sph32.size(), &t->d.sph32);
+  blk.add(t->band32.data(), t->band32.size(), &t->d.band32);
+  blk.add(t->box32_host.data(), t->box32_host.size(), &t->d.box32);
+  blk.add(t->gbs.data(), t->gbs.size(), &t->d.gbs32);
+  blk.add(t->pen_sph.data(), t->pen_sph.size(), &t->pd.sph);
+  blk.add(t->pen_task.data(), t->pen_task.size(), &t->pd.task);
+  blk.add(t->pen_box.data(), t->pen_box.size(), &t->pd.box);
+}
+
+// drops the host copies needed only for the upload
+void trim_tables(ArmTables* t) {
+  for (auto* v : {&t->sph32, &t->band32, &t->gbs, &t->pen_sph, &t->pen_box}) std::vector<float4>().swap(*v);
+  std::vector<double>().swap(t->sph64);
+  std::vector<int4>().swap(t->pen_task);
 }
 
 }  // namespace
@@ -323,16 +485,6 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   if (band > delta) delta = band;
   if (!(delta < 1.0)) return fail(MRMG_ERR_ARG, "kinematic reach too large for the FP32 path");
 
-  // box order: larger boxes first (earlier certain collisions; verdicts do not depend on order)
-  std::vector<int> border(B);
-  std::iota(border.begin(), border.end(), 0);
-  auto vol = [&](int b) {
-    double v = 1.0;
-    for (int k = 0; k < 3; k++) v *= std::max(0.0, h_box_hi[3 * b + k] - h_box_lo[3 * b + k]);
-    return v;
-  };
-  std::stable_sort(border.begin(), border.end(), [&](int a, int b) { return vol(a) > vol(b); });
-
   mrmg_scene* sc = new mrmg_scene();
   sc->kind = 1;
   sc->q_dim = D;
@@ -359,8 +511,7 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   d.prismatic[0] = prism[0]; d.prismatic[1] = prism[1]; d.prismatic[2] = prism[2];
   d.robot_mask = R >= 32 ? 0xffffffffu : ((1u << R) - 1u);
 
-  std::vector<float4> base32(R * 3), dh32(R * kMaxLinks), sph32(G * SPG), band32(G * SPG), box32(2 * B);
-  std::vector<double> sph64((size_t)G * SPG * 5), box64((size_t)B * 6);
+  std::vector<float4> base32(R * 3), dh32(R * kMaxLinks);
   for (int r = 0; r < R; r++) {
     const double* bp = h_base_pose + r * 12;
     for (int i = 0; i < 3; i++) base32[r * 3 + i] = make_float4((float)bp[3 * i], (float)bp[3 * i + 1], (float)bp[3 * i + 2], (float)bp[9 + i]);
@@ -369,122 +520,43 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
       dh32[r * kMaxLinks + k] = make_float4((float)h[0], (float)h[1], (float)h[2], (float)h[3]);
     }
   }
-  for (int sl = 0; sl < G * SPG; sl++) {
-    int i = slot_sphere[sl];
-    if (i < 0) {
-      sph32[sl] = make_float4(0.f, 0.f, 0.f, 0.f);
-      band32[sl] = make_float4(-1.f, -1.f, 0.f, 0.f);
-      for (int k = 0; k < 5; k++) sph64[(size_t)sl * 5 + k] = k == 3 ? -1.0 : 0.0;
-      continue;
-    }
-    const double* l = h_sphere_local + 3 * i;
-    const double r = h_sphere_radius[i];
-    sph32[sl] = make_float4((float)l[0], (float)l[1], (float)l[2], (float)r);
-    const double rhi = r + delta, rlo = r - delta;
-    band32[sl] = make_float4(rlo > 0 ? f32_down(rlo * rlo * (1.0 - 1e-6)) : -1.f, f32_up(rhi * rhi * (1.0 + 1e-6)),
-                             f32_up(r + delta), f32_down(r - delta));
-    sph64[(size_t)sl * 5 + 0] = l[0];
-    sph64[(size_t)sl * 5 + 1] = l[1];
-    sph64[(size_t)sl * 5 + 2] = l[2];
-    sph64[(size_t)sl * 5 + 3] = r;
-    sph64[(size_t)sl * 5 + 4] = r * r;
-  }
-  for (int bi = 0; bi < B; bi++) {
-    const int b = border[bi];
-    const double* lo = h_box_lo + 3 * b;
-    const double* hi = h_box_hi + 3 * b;
-    // FP32 centre / half extent; the band absorbs their rounding (|box| < 1e6 m)
-    box32[2 * bi] = make_float4((float)(0.5 * (lo[0] + hi[0])), (float)(0.5 * (lo[1] + hi[1])), (float)(0.5 * (lo[2] + hi[2])), 0.f);
-    box32[2 * bi + 1] = make_float4((float)(0.5 * (hi[0] - lo[0])), (float)(0.5 * (hi[1] - lo[1])), (float)(0.5 * (hi[2] - lo[2])), 0.f);
-    for (int k = 0; k < 3; k++) { box64[(size_t)bi * 6 + k] = lo[k]; box64[(size_t)bi * 6 + 3 + k] = hi[k]; }
-  }
+  // the creation inputs the sphere / box tables (and later per-mode tables) come from
+  ArmSrc& a = sc->src;
+  a.S = S; a.B = B; a.SPG = SPG; a.G = G; a.delta = delta;
+  a.local.assign(h_sphere_local, h_sphere_local + 3 * (size_t)S);
+  a.radius.assign(h_sphere_radius, h_sphere_radius + S);
+  a.box_lo.assign(h_box_lo, h_box_lo + 3 * (size_t)B);
+  a.box_hi.assign(h_box_hi, h_box_hi + 3 * (size_t)B);
+  a.slot_sphere = slot_sphere;
+  a.grp = grp;
+  std::vector<char> all_on(S, 1);
+  std::vector<int> all_boxes(B);
+  std::iota(all_boxes.begin(), all_boxes.end(), 0);
+  ArmTables& t = sc->base;
+  sphere_tables(a, all_on, &t);
+  box_tables(a, all_boxes, &t);
+  pen_tables(a, R, all_on, all_boxes, &t);
   DevBlock blk;
   blk.add(h_base_pose, (size_t)R * 12, &d.base64);
   blk.add(h_dh, (size_t)R * kMaxLinks * 4, &d.dh64);
-  blk.add(sph64.data(), sph64.size(), &d.sph64);
-  blk.add(box64.data(), box64.size(), &d.box64);
   blk.add(base32.data(), base32.size(), &d.base32);
   blk.add(dh32.data(), dh32.size(), &d.dh32);
-  blk.add(sph32.data(), sph32.size(), &d.sph32);
-  blk.add(band32.data(), band32.size(), &d.band32);
-  blk.add(box32.data(), box32.size(), &d.box32);
   blk.add(grp.data(), grp.size(), &d.grp);
-  // group bounds: the centre of the group's local sphere offsets and a radius
-  // over |offset - centre| + r, widened by 4 delta (FP32 error of the group
-  // centre and of each sphere centre, plus rounding of the bound test)
-  std::vector<float4> gbs(G);
-  for (int g = 0; g < G; g++) {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    int cnt = 0;
-    for (int v = 0; v < SPG; v++) {
-      const int i = slot_sphere[g * SPG + v];
-      if (i < 0) continue;
-      cnt++;
-      for (int k = 0; k < 3; k++) {
-        lo[k] = std::min(lo[k], h_sphere_local[3 * i + k]);
-        hi[k] = std::max(hi[k], h_sphere_local[3 * i + k]);
-      }
-    }
-    if (!cnt) { gbs[g] = make_float4(0.f, 0.f, 0.f, -1.f); continue; }
-    double c[3], rad = 0.0;
-    for (int k = 0; k < 3; k++) c[k] = 0.5 * (lo[k] + hi[k]);
-    for (int v = 0; v < SPG; v++) {
-      const int i = slot_sphere[g * SPG + v];
-      if (i < 0) continue;
-      double d2 = 0.0;
-      for (int k = 0; k < 3; k++) d2 += (h_sphere_local[3 * i + k] - c[k]) * (h_sphere_local[3 * i + k] - c[k]);
-      rad = std::max(rad, std::sqrt(d2) + h_sphere_radius[i]);
-    }
-    rad += 4.0 * delta;
-    gbs[g] = make_float4((float)c[0], (float)c[1], (float)c[2], f32_up(rad * rad * (1.0 + 1e-6)));
-  }
-  blk.add(gbs.data(), gbs.size(), &d.gbs32);
   blk.add(pairs.data(), pairs.size(), &d.pairs);
-  // penetration-cost tables: real spheres in slot order (robot, then frame)
-  std::vector<float4> pen_sph, pen_box(2 * B);
-  std::vector<int4> pen_task;
-  PenDev& pd = sc->pen;
-  {
-    // slots are ordered by robot, then frame: lk is the prefix count of
-    // spheres over (robot, frame) in that order
-    int cnt[kMaxRobots][kMaxLinks + 1] = {};
-    for (int sl = 0; sl < G * SPG; sl++) {
-      const int i = slot_sphere[sl];
-      if (i < 0) continue;
-      const int r = grp[sl / SPG] & 0xff, k = grp[sl / SPG] >> 8;
-      cnt[r][k]++;
-      const double* l = h_sphere_local + 3 * i;
-      pen_sph.push_back(make_float4((float)l[0], (float)l[1], (float)l[2], (float)h_sphere_radius[i]));
-    }
-    int acc = 0;
-    for (int r = 0; r < kMaxRobots; r++) {
-      for (int k = 0; k <= kMaxLinks; k++) { pd.lk[r][k] = acc; acc += cnt[r][k]; }
-      pd.lk[r][kMaxLinks + 1] = acc;
-    }
-    const int Sn = (int)pen_sph.size();
-    // tasks: consecutive sphere pairs of one robot
-    for (int r = 0; r < R; r++) {
-      const int s0 = pd.lk[r][0], s1 = pd.lk[r][kMaxLinks + 1];
-      for (int i = s0; i < s1; i += 2) pen_task.push_back(make_int4(i, i + 1 < s1 ? i + 1 : -1, s0, s1));
-    }
-    pd.S = Sn;
-    pd.B = B;
-    pd.NTK = (int)pen_task.size();
-  }
-  for (int b = 0; b < B; b++) {
-    const double* lo = h_box_lo + 3 * b;
-    const double* hi = h_box_hi + 3 * b;
-    pen_box[2 * b] = make_float4((float)(0.5 * (lo[0] + hi[0])), (float)(0.5 * (lo[1] + hi[1])), (float)(0.5 * (lo[2] + hi[2])), 0.f);
-    pen_box[2 * b + 1] = make_float4((float)(0.5 * (hi[0] - lo[0])), (float)(0.5 * (hi[1] - lo[1])), (float)(0.5 * (hi[2] - lo[2])), 0.f);
-  }
-  blk.add(pen_sph.data(), pen_sph.size(), &pd.sph);
-  blk.add(pen_task.data(), pen_task.size(), &pd.task);
-  blk.add(pen_box.data(), pen_box.size(), &pd.box);
+  add_tables(blk, &t);
   cudaError_t e = blk.upload(&sc->d_tables);
   if (e != cudaSuccess) { mrmg_scene_destroy(sc); return cuda_fail(e, "upload arm scene"); }
+  // the base set's view: the shared tables plus its own
+  {
+    ArmDev v = d;
+    v.sph64 = t.d.sph64; v.box64 = t.d.box64; v.sph32 = t.d.sph32; v.band32 = t.d.band32;
+    v.box32 = t.d.box32; v.gbs32 = t.d.gbs32; v.B = t.d.B;
+    t.d = v;
+    sc->arm = v;
+    sc->pen = t.pd;
+  }
+  trim_tables(&t);
   sc->band = d.delta;
-  sc->box32_host = box32;
-  sc->box64_host = box64;
   sc->occ_ctas_per_sm = arm_prepare(d, 8);
   sc->n_pairs_groups = (int64_t)pairs.size();
   sc->slot_to_sphere = slot_sphere;
@@ -492,9 +564,75 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   return MRMG_OK;
 }
 
+int mrmg_arm_scene_set_modes(mrmg_scene* sc, int32_t n_modes, const int32_t* h_sphere_attach,
+                             const int64_t* h_mode_box_off, const int32_t* h_mode_boxes,
+                             const int64_t* h_mode_attach_off, const int32_t* h_mode_attach) {
+  if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
+  if (!sc->modes.empty()) return fail(MRMG_ERR_ARG, "the scene's modes are already set");
+  if (n_modes < 1 || n_modes > (1 << 16)) return fail(MRMG_ERR_ARG, "modes must be 1..65536");
+  if (!h_mode_box_off || !h_mode_attach_off) return fail(MRMG_ERR_ARG, "NULL offsets");
+  const ArmSrc& a = sc->src;
+  if (h_sphere_attach)
+    for (int i = 0; i < a.S; i++)
+      if (h_sphere_attach[i] < -1) return fail(MRMG_ERR_ARG, "sphere %d: attachment id must be >= -1", i);
+  for (const int64_t* off : {h_mode_box_off, h_mode_attach_off}) {
+    if (off[0] != 0) return fail(MRMG_ERR_ARG, "mode offsets must start at 0");
+    for (int m = 0; m < n_modes; m++)
+      if (off[m + 1] < off[m]) return fail(MRMG_ERR_ARG, "mode offsets must not decrease");
+  }
+  if ((h_mode_box_off[n_modes] > 0 && !h_mode_boxes) || (h_mode_attach_off[n_modes] > 0 && !h_mode_attach))
+    return fail(MRMG_ERR_ARG, "NULL mode lists");
+  sc->modes.assign(n_modes, ArmTables());
+  DevBlock blk;
+  for (int m = 0; m < n_modes; m++) {
+    std::vector<int> boxes;
+    std::vector<char> seen(a.B, 0);
+    for (int64_t j = h_mode_box_off[m]; j < h_mode_box_off[m + 1]; j++) {
+      const int b = h_mode_boxes[j];
+      if (b < 0 || b >= a.B || seen[b]) { sc->modes.clear(); return fail(MRMG_ERR_ARG, "mode %d: bad or repeated box %d", m, b); }
+      seen[b] = 1;
+      boxes.push_back(b);
+    }
+    std::vector<char> on(a.S, 1);
+    if (h_sphere_attach)
+      for (int i = 0; i < a.S; i++) {
+        if (h_sphere_attach[i] < 0) continue;
+        on[i] = 0;
+        for (int64_t j = h_mode_attach_off[m]; j < h_mode_attach_off[m + 1]; j++)
+          if (h_mode_attach[j] == h_sphere_attach[i]) on[i] = 1;
+      }
+    ArmTables* t = &sc->modes[m];
+    sphere_tables(a, on, t);
+    box_tables(a, boxes, t);
+    pen_tables(a, sc->arm.R, on, boxes, t);
+    add_tables(blk, t);
+  }
+  cudaError_t e = blk.upload(&sc->d_mode_tables);
+  if (e != cudaSuccess) { sc->modes.clear(); return cuda_fail(e, "upload mode tables"); }
+  for (int m = 0; m < n_modes; m++) {
+    ArmTables& t = sc->modes[m];
+    ArmDev v = sc->base.d;
+    v.sph64 = t.d.sph64; v.box64 = t.d.box64; v.sph32 = t.d.sph32; v.band32 = t.d.band32;
+    v.box32 = t.d.box32; v.gbs32 = t.d.gbs32; v.B = t.d.B;
+    t.d = v;
+    trim_tables(&t);
+  }
+  return MRMG_OK;
+}
+
+int mrmg_scene_set_mode(mrmg_scene* sc, int32_t mode) {
+  if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
+  if (mode < -1 || mode >= (int)sc->modes.size()) return fail(MRMG_ERR_ARG, "mode %d out of range", mode);
+  sc->cur_mode = mode;
+  sc->arm = sc->tabs().d;
+  sc->pen = sc->tabs().pd;
+  return MRMG_OK;
+}
+
 int mrmg_scene_destroy(mrmg_scene* sc) {
   if (!sc) return MRMG_OK;
   if (sc->d_tables) cudaFree(sc->d_tables);
+  if (sc->d_mode_tables) cudaFree(sc->d_mode_tables);
   if (sc->d_ctr) cudaFree(sc->d_ctr);
   if (sc->d_pend) cudaFree(sc->d_pend);
   if (sc->d_surv) cudaFree(sc->d_surv);
@@ -575,15 +713,15 @@ int mrmg_arm_scene_tune_order(mrmg_scene* sc, const void* d_q, int32_t dtype, in
   std::vector<float4> b32(2 * B);
   std::vector<double> b64(6 * (size_t)B);
   for (int k = 0; k < B; k++) {
-    b32[2 * k] = sc->box32_host[2 * order[k]];
-    b32[2 * k + 1] = sc->box32_host[2 * order[k] + 1];
-    for (int c = 0; c < 6; c++) b64[6 * (size_t)k + c] = sc->box64_host[6 * (size_t)order[k] + c];
+    b32[2 * k] = sc->tabs().box32_host[2 * order[k]];
+    b32[2 * k + 1] = sc->tabs().box32_host[2 * order[k] + 1];
+    for (int c = 0; c < 6; c++) b64[6 * (size_t)k + c] = sc->tabs().box64_host[6 * (size_t)order[k] + c];
   }
   e = cudaMemcpy((void*)sc->arm.box32, b32.data(), sizeof(float4) * 2 * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy((void*)sc->arm.box64, b64.data(), sizeof(double) * 6 * B, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "upload box order");
-  sc->box32_host = b32;
-  sc->box64_host = b64;
+  sc->tabs().box32_host = b32;
+  sc->tabs().box64_host = b64;
   if (h_order_out)
     for (int k = 0; k < B; k++) h_order_out[k] = order[k];
   return MRMG_OK;

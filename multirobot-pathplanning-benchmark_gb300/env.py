@@ -29,6 +29,21 @@ from .configuration import Gb300Configuration, batch_config_cost as _batch_confi
 from .scenes import AbstractScene, ArmScene
 
 
+def _tune_all(sc: Gb300Scene, smp) -> np.ndarray:
+    """Tunes the box test order of every table set of the scene (the scene as
+    created and each mode's); returns the order of the scene as created."""
+    if sc.kind != 1 or not sc.scene.n_modes:
+        return sc.tune_test_order(smp)
+    cur = sc.mode
+    for m in range(sc.scene.n_modes):
+        sc.set_mode(m)
+        sc.tune_test_order(smp)
+    sc.set_mode(-1)
+    order = sc.tune_test_order(smp)
+    sc.set_mode(cur)
+    return order
+
+
 def _state(q) -> np.ndarray:
     if hasattr(q, "state"):
         return np.asarray(q.state(), dtype=np.float64)
@@ -62,10 +77,23 @@ class Gb300CollisionBackend:
     cost_reduction: str = "max"
     _gb300: Gb300Scene
 
+    _mode_index = None
+
+    def _use_mode(self, mode):
+        """Per-mode scenes: select the tables of the planner's ``mode``
+        (``mode_index(mode)`` gives the table index; None leaves the current
+        tables), as the reference envs call set_to_mode before a check."""
+        if self._mode_index is None or mode is None:
+            return
+        idx = int(self._mode_index(mode))
+        if idx != self._gb300.mode:
+            self._gb300.set_mode(idx)
+
     # --- single queries (planning_env.py:1724-1763) ------------------------
     def is_collision_free(self, q, mode) -> bool:
         if q is None:
             raise ValueError
+        self._use_mode(mode)
         v = self._gb300.is_collision_free_batch(_state(q).reshape(1, -1))
         return bool(v.item())
 
@@ -77,6 +105,7 @@ class Gb300CollisionBackend:
         a, b = _state(q1), _state(q2)
         if N is not None and N_start > N:
             raise AssertionError
+        self._use_mode(mode)
         v = self._gb300.is_edge_collision_free_batch(a.reshape(1, -1), b.reshape(1, -1), resolution,
                                                      include_endpoints, None if N is None else [int(N)], N_start, N_max)
         return bool(v.item())
@@ -89,11 +118,13 @@ class Gb300CollisionBackend:
         exact, like is_collision_free (``collision_tolerance`` is accepted
         for the signature; the engines' summed-penetration allowance is not
         modelled)."""
+        self._use_mode(m)
         v = self._gb300.is_collision_free_batch_robots(_state(q).reshape(1, -1), self._robot_mask(r))
         return bool(v.item())
 
     def batch_is_collision_free_for_robot(self, r, qs, mode=None) -> np.ndarray:
         """Per-configuration verdicts of is_collision_free_for_robot."""
+        self._use_mode(mode)
         v = self._gb300.is_collision_free_batch_robots(qs, self._robot_mask(r))
         return v.bool().cpu().numpy() if not isinstance(qs, torch.Tensor) else v.bool()
 
@@ -112,11 +143,12 @@ class Gb300CollisionBackend:
         """abstract_env.py:278-299: True iff every configuration is free."""
         if len(qs) == 0:
             return True
-        return bool(self.batch_is_collision_free(np.array([_state(q) for q in qs])).all())
+        return bool(self.batch_is_collision_free(np.array([_state(q) for q in qs]), mode).all())
 
     # --- batched (additive) ------------------------------------------------
     def batch_is_collision_free(self, qs, mode=None) -> np.ndarray:
         """Per-configuration verdicts for an [n, D] array (or device tensor)."""
+        self._use_mode(mode)
         v = self._gb300.is_collision_free_batch(qs)
         return v.bool().cpu().numpy() if not isinstance(qs, torch.Tensor) else v.bool()
 
@@ -125,6 +157,7 @@ class Gb300CollisionBackend:
         """Per-edge verdicts for [n, D] endpoint arrays (or device tensors)."""
         if resolution is None:
             resolution = self.collision_resolution
+        self._use_mode(mode)
         v = self._gb300.is_edge_collision_free_batch(q1s, q2s, resolution, include_endpoints, N)
         return v.bool().cpu().numpy() if not isinstance(q1s, torch.Tensor) else v.bool()
 
@@ -161,7 +194,9 @@ class Gb300CollisionBackend:
         sc = Gb300Scene(self.scene)
         smp = getattr(self, "_tune_samples", None)
         if smp is not None:
-            sc.tune_test_order(smp)
+            _tune_all(sc, smp)
+        if sc.kind == 1 and self._gb300.mode >= 0:
+            sc.set_mode(self._gb300.mode)
         return sc
 
     # --- path check (planning_env.py:1765-1881), one batched pass ----------
@@ -177,6 +212,8 @@ class Gb300CollisionBackend:
             resolution = self.collision_resolution
         P = len(path)
         qs = np.array([_state(s.q) for s in path])
+        if self._mode_index is not None and P >= 1 and getattr(path[0], "mode", None) is not None:
+            return self._path_free_by_mode(path, qs, resolution, check_edges_in_order, check_start_and_end)
         verts = list(range(1, P - 1))
         if check_start_and_end and P >= 2:
             verts = [0] + verts
@@ -188,6 +225,29 @@ class Gb300CollisionBackend:
             return False
         if P >= 2 and not self.batch_is_edge_collision_free(qs[:-1], qs[1:], None, resolution, False).all():
             return False
+        return True
+
+    def _path_free_by_mode(self, path, qs, resolution, check_edges_in_order, check_start_and_end) -> bool:
+        """is_path_collision_free on a per-mode scene: each vertex in its
+        state's mode, each edge in the mode of its first state
+        (planning_env.py:1805-1816), one batch per mode."""
+        P = len(path)
+        verts = set(range(1, P - 1))
+        if check_start_and_end:
+            verts.add(0)
+        if check_edges_in_order or check_start_and_end:
+            verts.add(P - 1)
+        idx = [int(self._mode_index(s.mode)) for s in path]
+        for m in sorted(set(idx)):
+            vs = [i for i in sorted(verts) if idx[i] == m]
+            es = [i for i in range(P - 1) if idx[i] == m]
+            if self._gb300.mode != m:
+                self._gb300.set_mode(m)
+            if vs and not self._gb300.is_collision_free_batch(qs[vs]).bool().all():
+                return False
+            if es and not self._gb300.is_edge_collision_free_batch(qs[es], qs[[i + 1 for i in es]], resolution,
+                                                                    False).bool().all():
+                return False
         return True
 
     # --- costs (abstract_env.py:238-253) -----------------------------------
@@ -228,8 +288,13 @@ class Gb300ArmEnvironment(Gb300CollisionBackend):
     """Sphere-arm robots (DH chains, optional planar bases) among boxes."""
 
     def __init__(self, scene: ArmScene, collision_resolution: float = 0.05, collision_tolerance: float = 0.01,
-                 band: float = 0.0, tune_samples: int = 4096, seed: int = 0):
+                 band: float = 0.0, tune_samples: int = 4096, seed: int = 0, mode_index=None):
+        """``mode_index`` (per-mode scenes): maps a planner mode to the
+        scene's table index; by default an int is its own index and a mode
+        object uses its ``id``."""
         self.scene = scene
+        if scene.n_modes:
+            self._mode_index = mode_index or (lambda m: m if isinstance(m, (int, np.integer)) else m.id)
         self.limits = scene.limits
         sl = [tuple(map(int, s)) for s in scene.agent_slices()]
         self.start_pos = Gb300Configuration(np.zeros(scene.q_dim), sl)
@@ -246,4 +311,4 @@ class Gb300ArmEnvironment(Gb300CollisionBackend):
             rng = np.random.default_rng(seed)
             smp = rng.uniform(self.limits[0], self.limits[1], (tune_samples, scene.q_dim)).astype(np.float32)
             self._tune_samples = smp
-            self.box_order = self._gb300.tune_test_order(smp)
+            self.box_order = _tune_all(self._gb300, smp)

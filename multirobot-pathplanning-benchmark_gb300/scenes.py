@@ -119,10 +119,43 @@ class ArmScene:
     box_hi: np.ndarray          # [B, 3]
     q_dim: int
     limits: np.ndarray = field(default=None)   # [2, q_dim]
+    # per-mode scene tables (optional): the boxes above are the pool; mode m
+    # keeps boxes mode_boxes[m] and the attached-object spheres whose
+    # sphere_attach id is in mode_attach[m] (sphere_attach -1: robot sphere)
+    sphere_attach: np.ndarray = field(default=None)   # [S] int32
+    mode_boxes: list = field(default=None)
+    mode_attach: list = field(default=None)
 
     @property
     def n_robots(self) -> int:
         return len(self.q_offset)
+
+    @property
+    def n_modes(self) -> int:
+        return 0 if self.mode_boxes is None else len(self.mode_boxes)
+
+    def for_mode(self, m: int) -> "ArmScene":
+        """The scene as mode ``m`` sees it: its boxes and the spheres present."""
+        att = np.full(len(self.sphere_radius), -1) if self.sphere_attach is None else np.asarray(self.sphere_attach)
+        on = (att < 0) | np.isin(att, np.asarray(self.mode_attach[m], dtype=np.int64))
+        bx = np.asarray(self.mode_boxes[m], dtype=np.int64)
+        return ArmScene(
+            q_offset=self.q_offset, base_kind=self.base_kind, base_pose=self.base_pose, n_links=self.n_links,
+            dh=self.dh, sphere_robot=np.asarray(self.sphere_robot)[on], sphere_link=np.asarray(self.sphere_link)[on],
+            sphere_local=np.asarray(self.sphere_local)[on], sphere_radius=np.asarray(self.sphere_radius)[on],
+            box_lo=np.asarray(self.box_lo).reshape(-1, 3)[bx], box_hi=np.asarray(self.box_hi).reshape(-1, 3)[bx],
+            q_dim=self.q_dim, limits=self.limits)
+
+    def mode_tables(self) -> dict:
+        """Flat arrays for the library: attachment ids and per-mode lists."""
+        S = len(self.sphere_radius)
+        att = np.full(S, -1, dtype=np.int32) if self.sphere_attach is None else np.asarray(self.sphere_attach, np.int32)
+        bl = [np.asarray(b, dtype=np.int32).reshape(-1) for b in self.mode_boxes]
+        al = [np.asarray(a, dtype=np.int32).reshape(-1) for a in self.mode_attach]
+        off = lambda ls: np.concatenate([[0], np.cumsum([len(x) for x in ls])]).astype(np.int64)
+        cat = lambda ls: np.ascontiguousarray(np.concatenate(ls) if ls else np.zeros(0), dtype=np.int32)
+        return dict(sphere_attach=np.ascontiguousarray(att), box_off=off(bl), boxes=cat(bl), attach_off=off(al),
+                    attach=cat(al))
 
     def robot_dofs(self) -> list:
         return [int(self.n_links[r] + (3 if self.base_kind[r] == 1 else 0)) for r in range(self.n_robots)]
@@ -207,6 +240,51 @@ def make_arm_scene(seed: int = 0, n_boxes: int = 50, n_links: int = 7, spheres_p
         q_dim=D,
         limits=lim,
     )
+
+
+def make_arm_mode_scene(seed: int = 0, n_objects: int = 6, n_modes: int = 12, n_static: int = 40):
+    """The four-arm table scene with movable objects, for per-mode tables.
+    Each object j is a box (half extents U[0.03, 0.06] m) with two resting
+    poses on the table (centres uniform in [-0.7, 0.7]^2, resting on z = 0)
+    and a grasp by robot j % 4: held, it is three spheres of radius 0.04 m
+    along the z axis of that robot's last link frame (offsets 0.05, 0.10,
+    0.15 m).  Mode m draws, per object, resting pose A, pose B or held (at
+    most one object per robot); the box pool is the static boxes then the
+    objects' pose-A and pose-B boxes."""
+    rng = np.random.default_rng(seed)
+    sc = make_arm_scene(seed, n_boxes=n_static)
+    R, L = sc.n_robots, int(sc.n_links[0])
+    half = rng.uniform(0.03, 0.06, (n_objects, 3))
+    lo, hi = [sc.box_lo], [sc.box_hi]
+    for p in range(2):
+        c = np.stack([rng.uniform(-0.7, 0.7, n_objects), rng.uniform(-0.7, 0.7, n_objects), half[:, 2]], -1)
+        lo.append(c - half)
+        hi.append(c + half)
+    s_robot, s_link, s_loc, s_rad, s_att = [sc.sphere_robot], [sc.sphere_link], [sc.sphere_local], [sc.sphere_radius], \
+        [np.full(len(sc.sphere_radius), -1, dtype=np.int32)]
+    for j in range(n_objects):
+        s_robot.append(np.full(3, j % R, dtype=np.int32))
+        s_link.append(np.full(3, L, dtype=np.int32))
+        s_loc.append(np.array([[0.0, 0.0, 0.05], [0.0, 0.0, 0.10], [0.0, 0.0, 0.15]]))
+        s_rad.append(np.full(3, 0.04))
+        s_att.append(np.full(3, j, dtype=np.int32))
+    mode_boxes, mode_attach = [], []
+    for m in range(n_modes):
+        boxes, att, busy = list(range(n_static)), [], set()
+        for j in range(n_objects):
+            st = int(rng.integers(0, 3))
+            if st == 2 and (j % R) not in busy:
+                att.append(j)
+                busy.add(j % R)
+            else:
+                boxes.append(n_static + (st % 2) * n_objects + j)
+        mode_boxes.append(boxes)
+        mode_attach.append(att)
+    sc.box_lo, sc.box_hi = np.concatenate(lo), np.concatenate(hi)
+    sc.sphere_robot, sc.sphere_link = np.concatenate(s_robot), np.concatenate(s_link)
+    sc.sphere_local, sc.sphere_radius = np.concatenate(s_loc), np.concatenate(s_rad)
+    sc.sphere_attach, sc.mode_boxes, sc.mode_attach = np.concatenate(s_att), mode_boxes, mode_attach
+    return sc
 
 
 def make_mobile_scene(seed: int = 0, n_robots: int = 8, n_boxes: int = 200):
