@@ -377,6 +377,7 @@ def run_gb300(args):
                 extra["knn"] = bench_knn(orc)
                 extra["penetration"] = bench_penetration()
                 extra["serving"] = bench_serving(orc)
+                extra["prm_lazy"] = bench_prm_lazy()
 
     mism = int(reduce_max(float(mism), world))
     if rank == 0:
@@ -573,6 +574,68 @@ def bench_penetration(steps: int = 10) -> dict:
                            "cores": torch.get_num_threads(), "kind": "port",
                            "sample": f"{n_cpu} paths x {T} waypoints, float64 torch autograd on the host"}
     s.close()
+    return out
+
+
+class _PrmNode:
+    def __init__(self, i, q):
+        self.id = i
+        self.state = type("State", (), {"q": q, "mode": None})()
+        self.whitelist, self.blacklist = set(), set()
+
+
+def bench_prm_lazy(n_nodes: int = 3000, k: int = 10, window: int = 256) -> dict:
+    """The composite PRM's lazy A* (prm_graph.py:552-746) on a roadmap of
+    about 3,000 collision-free configurations of the four-arm scene with 5
+    boxes (k = 10 nearest, node-store k-NN), edges checked at 0.05 rad: one
+    device call per popped edge (the reference's call pattern) against
+    speculative batches of up to 256 upcoming edges.  Edge costs and the
+    heuristic (cost to the goal) are precomputed in one batched call each, so
+    the timings isolate the edge checks; both searches give the same path."""
+    lazy, scenes, envm, knn = pkg("lazy"), pkg("scenes"), pkg("env"), pkg("knn")
+    scene = scenes.make_arm_scene(1, n_boxes=5)
+    env = envm.Gb300ArmEnvironment(scene, collision_resolution=0.05, tune_samples=1024)
+    q = scenes.uniform_configs(scene, 4 * n_nodes, seed=7, dtype=np.float64)
+    q = q[env.batch_is_collision_free(q)][:n_nodes]
+    q = q[:1] + 0.35 * (q - q[:1])            # a compact roadmap around the first configuration
+    q = np.ascontiguousarray(q[env.batch_is_collision_free(q)])
+    n = len(q)
+    sl = scene.agent_slices()
+    store = knn.NodeStore(q, [0, n], sl, "euclidean")
+    nbr = store.knn(q, np.zeros(n, dtype=np.int32), k + 1)[0].cpu().numpy()[:, 1:]
+    store.close()
+    ecost = env.batch_config_cost(np.repeat(q, k, 0), q[nbr.reshape(-1)], sl).reshape(n, k)
+    cost_tab = {(i, int(j)): float(ecost[i, c]) for i in range(n) for c, j in enumerate(nbr[i])}
+    rows = [q[i].copy() for i in range(n)]
+    row_of = {id(r): i for i, r in enumerate(rows)}
+
+    def search(goal, w):
+        hc = env.batch_config_cost(np.repeat(q[goal][None], n, 0), q, sl)
+        nodes = [_PrmNode(i, rows[i]) for i in range(n)]
+        checker = lazy.SpeculativeEdgeChecker(env, resolution=0.05, window=w)
+        t0 = time.perf_counter()
+        r = lazy.lazy_astar(nodes[0], [nodes[goal]], lambda nd: ([nodes[j] for j in nbr[nd.id]], nbr[nd.id]),
+                            lambda a, b: cost_tab[(row_of[id(a)], row_of[id(b)])],
+                            lambda a, ids: ecost[row_of[id(a)]], lambda nd: float(hc[nd.id]), checker)
+        r["seconds"] = time.perf_counter() - t0
+        return r
+
+    goal = None
+    for cand in np.argsort(-np.abs(q - q[0]).max(1))[:40]:
+        r = search(int(cand), window)
+        if len(r["path"]) >= 6:
+            goal = int(cand)
+            break
+    out = {"roadmap_nodes": n, "k": k, "resolution": 0.05, "window": window, "goal_found": goal is not None}
+    if goal is None:
+        return out
+    seq, bat = search(goal, 1), search(goal, window)
+    for tag, r in (("per_edge_calls", seq), ("batched", bat)):
+        out[tag] = {"seconds": r["seconds"], "device_calls": r["calls"], "edges_checked": r["edges_checked"],
+                    "edge_lookups": r["lookups"], "processed_edges": r["processed_edges"]}
+    out["same_path"] = [nd.id for nd in seq["path"]] == [nd.id for nd in bat["path"]]
+    out["path_nodes"] = len(bat["path"])
+    out["speedup"] = seq["seconds"] / max(bat["seconds"], 1e-12)
     return out
 
 

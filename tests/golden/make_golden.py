@@ -22,6 +22,8 @@ Outputs (numpy .npz, seeded, small):
   knn.npz                per-mode k nearest (argpartition + argsort, prm_graph.py:446-447)
   near.npz               per-mode radius neighbours (find_nearest_indices, rrtstar_base.py:439-453),
                          radii on and around node distances so that the added 1e-10 decides
+  prm_search.npz         the composite PRM's lazy A* (MultimodalGraph.search, prm_graph.py:552-746)
+                         on the disc scene over a fixed k-NN graph: path and printed counters
   known_answers.json     the reference tests' own known answers (tests/test.py)
 """
 from __future__ import annotations
@@ -298,6 +300,7 @@ def main(ref_root: str):
     ka["path_free"] = bool(env.is_path_collision_free(path, resolution=0.5))
     (OUT / "known_answers.json").write_text(json.dumps(ka, indent=1))
     make_near(cf)
+    make_prm_search(pe, ae, cf, reg)
     print("golden vectors written to", OUT)
 
 
@@ -362,8 +365,93 @@ def make_near(cf):
                         slices=np.array(slices, dtype=np.int64), **res)
 
 
+def _seed_planners(cf):
+    import importlib
+
+    base = "multi_robot_multi_goal_planning.planners"
+    root = Path(cf.__file__).resolve().parents[2] / "planners"
+    for name, path in [(base, root), (base + ".prm", root / "prm")]:
+        if name not in sys.modules:
+            m = types.ModuleType(name)
+            m.__path__ = [str(path)]
+            sys.modules[name] = m
+    return importlib
+
+
+def make_prm_search(pe, ae, cf, reg):
+    """The reference's own MultimodalGraph.search (prm_graph.py:552-746) on
+    the disc scene (the one of abstract_disc.npz) over a fixed graph: 250
+    collision-free configurations, each joined to its 10 nearest (euclidean
+    batch_config_dist, stable order), start = configuration 0, the goal the
+    mode's only transition node (lower bound 0, so h is the cost to the
+    goal), resolution 0.1.  Saved: the graph, the path as
+    configuration indices and the counters the search prints, for a goal it
+    reaches and one it cannot."""
+    import contextlib
+    import io
+
+    importlib = _seed_planners(cf)
+    pg = importlib.import_module("multi_robot_multi_goal_planning.planners.prm.prm_graph")
+    srng = np.random.default_rng(0)
+    centers = srng.uniform(-0.8, 0.8, (10, 2))
+    half = srng.uniform(0.05, 0.2, (10, 2))
+    env = disc_env(ae, reg, centers, half)
+    mode = env.start_mode
+    rng = np.random.default_rng(31)
+    qs = []
+    while len(qs) < 250:
+        q = rng.uniform(-1, 1, 4)
+        if env.is_collision_free(env.start_pos.from_flat(q), mode):
+            qs.append(q)
+    qs = np.array(qs)
+    nodes = [pg.Node(pe.State(env.start_pos.from_flat(q), mode)) for q in qs]
+    pos = {n.id: i for i, n in enumerate(nodes)}
+    k = 10
+    nbr = np.zeros((len(qs), k), dtype=np.int64)
+    for i, n in enumerate(nodes):
+        d = cf.batch_config_dist(n.state.q, qs, "euclidean")
+        nbr[i] = np.argsort(d, kind="stable")[1:k + 1]
+    def run(gi):
+        for n in nodes:
+            n.whitelist, n.blacklist = set(), set()
+        goal = nodes[gi]
+        goal.lb_cost_to_goal = 0.0
+        graph = types.SimpleNamespace(
+            get_neighbors=lambda n, space_extent=None: ([nodes[j] for j in nbr[pos[n.id]]], qs[nbr[pos[n.id]]]),
+            transition_nodes={mode: [goal]}, transition_node_array_cache={}, transition_node_lb_cache={})
+        out = io.StringIO()
+        with contextlib.redirect_stdout(out):
+            path = pg.MultimodalGraph.search(graph, nodes[0], [goal], env, best_cost=None, resolution=0.1)
+        txt = out.getvalue()
+        return ([pos[n.id] for n in path], int(txt.split("Wasted pops")[1].split()[0]),
+                int(txt.split("Processed edges")[1].split()[0]))
+
+    # goals: the first configuration (after 0) the search reaches over at
+    # least five edges, and the first it cannot reach
+    found = missing = None
+    for gi in range(1, len(qs)):
+        r = run(gi)
+        if found is None and len(r[0]) >= 6:
+            found = (gi,) + r
+        if missing is None and not r[0]:
+            missing = (gi,) + r
+        if found and missing:
+            break
+    res = {}
+    for tag, (gi, path, wasted, processed) in [("found", found), ("missing", missing)]:
+        res[f"goal_{tag}"] = gi
+        res[f"path_{tag}"] = np.array(path, dtype=np.int64)
+        res[f"wasted_pops_{tag}"] = wasted
+        res[f"processed_edges_{tag}"] = processed
+    np.savez_compressed(OUT / "prm_search.npz", centers=centers, half=half, configs=qs, neighbors=nbr, start=0,
+                        resolution=0.1, **res)
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "near":
+    if len(sys.argv) > 2 and sys.argv[2] == "prm_search":
+        pe_, ae_, cf_, reg_ = import_reference(Path(sys.argv[1]))
+        make_prm_search(pe_, ae_, cf_, reg_)
+    elif len(sys.argv) > 2 and sys.argv[2] == "near":
         make_near(import_reference(Path(sys.argv[1]))[2])
     else:
         main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -138,6 +138,49 @@ def test_near(oracle):
         assert o0[-1] < offs[-1], metric
 
 
+class _Node:
+    """A graph node as the PRM search uses it (prm_graph.py:29-67)."""
+
+    def __init__(self, i, q, mode=0):
+        self.id = i
+        self.state = type("State", (), {"q": q, "mode": mode})()
+        self.whitelist, self.blacklist = set(), set()
+
+
+def prm_search_case(g, tag):
+    """Nodes, neighbour function, costs and heuristic of the stored search."""
+    qs, nbr = g["configs"], g["neighbors"]
+    nodes = [_Node(i, q) for i, q in enumerate(qs)]
+    goal = nodes[int(g[f"goal_{tag}"])]
+    return nodes, goal, (lambda n: ([nodes[j] for j in nbr[n.id]], qs[nbr[n.id]]))
+
+
+@pytest.mark.parametrize("window", [1, 16])
+def test_prm_lazy_search_golden(oracle, window):
+    """The lazy A* restatement, with oracle edge checks and speculative
+    windows of 1 and 16 edges, reproduces the reference's own search: the
+    path (start twice, as its reconstruction writes it) and both counters,
+    for a reachable and an unreachable goal."""
+    lazy = pkg("lazy")
+    g = golden("prm_search.npz")
+    o = oracle.OracleScene(pkg("scenes").make_disc_scene(0))
+    sl = [[0, 2], [2, 4]]
+    bcost = lambda a, B: oracle.batch_cost(a, np.asarray(B), sl, "euclidean", "max", 0.01)
+    cost = lambda a, b: float(bcost(a, np.asarray(b)[None])[0])
+    res = float(g["resolution"])
+    for tag in ("found", "missing"):
+        nodes, goal, nb = prm_search_case(g, tag)
+        h = lambda n: float(np.min(0.0 + bcost(n.state.q, goal.state.q[None])))
+        checker = lazy.SpeculativeEdgeChecker(check=lambda q0, q1, m: o.edges_free(q0, q1, res).astype(bool),
+                                              window=window)
+        r = lazy.lazy_astar(nodes[0], [goal], nb, cost, bcost, h, checker)
+        assert [n.id for n in r["path"]] == g[f"path_{tag}"].tolist(), tag
+        assert r["processed_edges"] == int(g[f"processed_edges_{tag}"]), tag
+        assert r["wasted_pops"] == int(g[f"wasted_pops_{tag}"]), tag
+        if window > 1:
+            assert r["calls"] < r["lookups"]
+
+
 def test_known_answers_edge_calls(oracle):
     """tests/test.py:61-90 of the reference: 3 / 1 / 9 / 11 calls."""
     ka = golden("known_answers.json")
