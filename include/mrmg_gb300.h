@@ -369,8 +369,9 @@ int mrmg_knn(mrmg_node_store *store, const double *d_queries, int64_t Q, const i
  * node j of its mode h_query_mode[q] whose batch_config_dist value satisfies
  * dist <= h_radius[q] + add_eps (the sum in FP64: the reference adds 1e-10),
  * in ascending j (np.nonzero order).  Result in CSR form: d_offsets[Q + 1]
- * (always written), mode-local d_idx[] and FP64 d_dist[] at positions
- * offsets[q] .. offsets[q+1]; positions >= cap are not written.
+ * (always written), mode-local d_idx[] and FP64 d_dist[] (may be NULL: no
+ * distances) at positions offsets[q] .. offsets[q+1]; positions >= cap are
+ * not written.
  * *out_total = offsets[Q].  When it exceeds cap, mrmg_near_fetch writes the
  * whole result into larger buffers without recomputing it (the store keeps
  * it until its next radius query; d_queries must stay unchanged until then).

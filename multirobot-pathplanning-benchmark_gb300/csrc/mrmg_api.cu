@@ -1194,7 +1194,7 @@ int mrmg_near(mrmg_node_store* s, const double* d_queries, int64_t Q, const int3
   if (Q < 0 || cap < 0) return fail(MRMG_ERR_ARG, "Q / cap must be >= 0");
   if (!d_offsets || !out_total) return fail(MRMG_ERR_ARG, "NULL offsets / total");
   if (Q > 0 && (!d_queries || !h_query_mode || !h_radius)) return fail(MRMG_ERR_ARG, "NULL pointer");
-  if (cap > 0 && (!d_idx || !d_dist)) return fail(MRMG_ERR_ARG, "NULL output with cap > 0");
+  if (cap > 0 && !d_idx) return fail(MRMG_ERR_ARG, "NULL index output with cap > 0");
   if (!(add_eps >= 0.0)) return fail(MRMG_ERR_ARG, "add_eps must be >= 0");
   int rc = check_query_modes(s, h_query_mode, Q);
   if (rc) return rc;
@@ -1221,7 +1221,7 @@ int mrmg_near_fetch(mrmg_node_store* s, int64_t* d_idx, double* d_dist, int64_t 
   if (!s->near_valid) return fail(MRMG_ERR_ARG, "no radius query to fetch");
   if (cap < near_last_total(s->near)) return fail(MRMG_ERR_ARG, "cap %lld < total %lld", (long long)cap,
                                                     near_last_total(s->near));
-  if (cap > 0 && (!d_idx || !d_dist)) return fail(MRMG_ERR_ARG, "NULL output");
+  if (cap > 0 && !d_idx) return fail(MRMG_ERR_ARG, "NULL index output");
   cudaError_t e = near_fetch(s->near, (long long*)d_idx, d_dist, cap, device_sms(), (cudaStream_t)stream);
   return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "near fetch");
 }

@@ -120,6 +120,74 @@ __global__ void knn_exact_kernel(const double* __restrict__ qs, long long Q, con
 }
 
 // ---------------------------------------------------------------------------
+// Radius decision (d <= r' as the reference's FP64 distance decides it) with
+// an FP32 pre-test for the euclidean and max-over-agents metrics: the FP32
+// sum of squared coordinate differences (per agent, then the maximum) lies
+// within 2.4e-6 (|q| + |x|)^2 of the exact squared distance (each FP32
+// coordinate difference within 2^-23 (|q_j| + |x_j|) of the exact one, the
+// sum of 28 squares within 28 * 2^-24 of its value), so a node more than
+// 7.7e-6 (|q| + |x|)^2 (three times that) plus 2^-20 r'^2 (the rounding of
+// r'^2 and of these sums) inside or outside r'^2 is decided without FP64;
+// the rest, and every other metric, take the FP64 distance.  GB300 issues
+// FP64 at a small fraction of its FP32 rate, and a warp instruction costs the
+// same with one active lane as with 32, so this keeps the sparse re-checks
+// of radius queries off the FP64 pipe.
+// ---------------------------------------------------------------------------
+struct RadiusTest {
+  double rp;     // r' = radius + eps (FP64)
+  float lo, hi;  // (r')^2 (1 -+ 2^-20) in FP32
+};
+
+__device__ __forceinline__ RadiusTest radius_test(double rp) {
+  RadiusTest r;
+  r.rp = rp;
+  const float r2 = (float)(rp * rp);
+  r.lo = r2 * (1.f - 9.5367431640625e-7f);
+  r.hi = r2 * (1.f + 9.5367431640625e-7f);
+  return r;
+}
+
+// q32 / x32: FP32 copies (rounded to nearest) of the FP64 rows qq / xx
+__device__ __forceinline__ bool within_radius(const float* __restrict__ q32, const float* __restrict__ x32,
+                                              const double* __restrict__ qq, const double* __restrict__ xx,
+                                              const SliceTab& t, int metric, const RadiusTest& r) {
+  if (!(r.rp >= 0.0)) return false;   // distances are >= 0; NaN selects nothing
+  if (metric == MRMG_METRIC_EUCLIDEAN || metric == MRMG_METRIC_MAX_EUCLIDEAN) {
+    float qn = 0.f, xn = 0.f, m = 0.f;
+    if (metric == MRMG_METRIC_EUCLIDEAN) {
+      for (int k = 0; k < t.end_all; k++) {
+        const float qf = q32[k], xf = x32[k], d = qf - xf;
+        m = fmaf(d, d, m);
+        qn = fmaf(qf, qf, qn);
+        xn = fmaf(xf, xf, xn);
+      }
+    } else {
+      for (int a = 0; a < t.A; a++) {
+        float sa = 0.f;
+        for (int k = t.s[a]; k < t.e[a]; k++) {
+          const float qf = q32[k], xf = x32[k], d = qf - xf;
+          sa = fmaf(d, d, sa);
+          qn = fmaf(qf, qf, qn);
+          xn = fmaf(xf, xf, xn);
+        }
+        m = fmaxf(m, sa);
+      }
+    }
+    const float e = sqrtf(qn) + sqrtf(xn);
+    const float bnd = 7.7e-6f * e * e;
+    if (m < r.lo - bnd) return true;
+    if (m > r.hi + bnd) return false;
+  }
+  auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
+  return dist_of(t, metric, dfun) <= r.rp;
+}
+
+__global__ void f64_to_f32_kernel(const double* __restrict__ src, float* __restrict__ dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+// ---------------------------------------------------------------------------
 // Node-parallel exact FP64 paths for small query batches: work items are
 // (query, chunk of kSplitNodes nodes) pairs, so one query spreads over the
 // whole GPU instead of one warp.
@@ -137,9 +205,12 @@ __device__ __forceinline__ long long owner_of(const long long* __restrict__ off,
 }
 
 // warp per item: the chunk's k best (distance key, mode-local index), ascending
+// (queries are listed entries: query qmap[l] for list entry l, or l itself
+// when qmap is NULL; q_mode is per list entry)
 template <int KM>
-__global__ void knn_split_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
-                                 const long long* __restrict__ ioff, const double* __restrict__ nodes,
+__global__ void knn_split_kernel(const double* __restrict__ qs, const long long* __restrict__ qmap, long long Q,
+                                 const int* __restrict__ q_mode, const long long* __restrict__ ioff,
+                                 const double* __restrict__ nodes,
                                  const long long* __restrict__ mode_beg, const long long* __restrict__ mode_end,
                                  SliceTab t, int metric, int k, long long* __restrict__ cand_key,
                                  long long* __restrict__ cand_idx) {
@@ -148,16 +219,16 @@ __global__ void knn_split_kernel(const double* __restrict__ qs, long long Q, con
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
   const long long n_items = ioff[Q];
   for (long long it = warp; it < n_items; it += nwarps) {
-    const long long q = owner_of(ioff, Q, it);
-    const int m = q_mode[q];
+    const long long l = owner_of(ioff, Q, it);
+    const int m = q_mode[l];
     const long long b = mode_beg[m];
-    const long long s = b + (it - ioff[q]) * kSplitNodes;
+    const long long s = b + (it - ioff[l]) * kSplitNodes;
     const long long e = s + kSplitNodes < mode_end[m] ? s + kSplitNodes : mode_end[m];
     long long td[KM];
     long long ti[KM];
 #pragma unroll
     for (int i = 0; i < KM; i++) { td[i] = 0x7ff0000000000000ll; ti[i] = -1; }
-    const double* qq = qs + q * t.D;
+    const double* qq = qs + (qmap ? qmap[l] : l) * t.D;
     for (long long x = s + lane; x < e; x += 32) {
       const double* xx = nodes + x * t.D;
       auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
@@ -187,18 +258,20 @@ __global__ void knn_split_kernel(const double* __restrict__ qs, long long Q, con
 // order (each item's list is sorted and later items hold higher indices, so
 // equal distances still arrive in index order), then the lanes merge
 template <int KM>
-__global__ void knn_split_merge_kernel(long long Q, const long long* __restrict__ ioff, int k,
+__global__ void knn_split_merge_kernel(const long long* __restrict__ qmap, long long Q,
+                                       const long long* __restrict__ ioff, int k,
                                        const long long* __restrict__ cand_key, const long long* __restrict__ cand_idx,
                                        long long* __restrict__ out_idx, double* __restrict__ out_dist) {
   const int lane = threadIdx.x & 31;
   const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long q = warp; q < Q; q += nwarps) {
+  for (long long l = warp; l < Q; l += nwarps) {
+    const long long q = qmap ? qmap[l] : l;
     long long td[KM];
     long long ti[KM];
 #pragma unroll
     for (int i = 0; i < KM; i++) { td[i] = 0x7ff0000000000000ll; ti[i] = -1; }
-    for (long long it = ioff[q] + lane; it < ioff[q + 1]; it += 32)
+    for (long long it = ioff[l] + lane; it < ioff[l + 1]; it += 32)
       for (int r = 0; r < k; r++) {
         const long long id = cand_idx[it * k + r];
         const long long d = cand_key[it * k + r];
@@ -227,8 +300,9 @@ __global__ void knn_split_merge_kernel(long long Q, const long long* __restrict_
 }
 
 // radius, exact: warp per (query, bitmap word), lane = node of the word
-__global__ void near_split_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
-                                  const double* __restrict__ nodes, const long long* __restrict__ mode_beg,
+__global__ void near_split_kernel(const double* __restrict__ qs, const float* __restrict__ qs32, long long Q,
+                                  const int* __restrict__ q_mode, const double* __restrict__ nodes,
+                                  const float* __restrict__ nodes32, const long long* __restrict__ mode_beg,
                                   const long long* __restrict__ mode_end, SliceTab t, int metric,
                                   const double* __restrict__ rp, const long long* __restrict__ woff,
                                   unsigned* __restrict__ bits, unsigned long long* __restrict__ counts) {
@@ -242,10 +316,9 @@ __global__ void near_split_kernel(const double* __restrict__ qs, long long Q, co
     const long long id = (f - woff[q]) * 32 + lane;
     bool in = false;
     if (id < mode_end[m] - mode_beg[m]) {
-      const double* qq = qs + q * t.D;
-      const double* xx = nodes + (mode_beg[m] + id) * t.D;
-      auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
-      in = dist_of(t, metric, dfun) <= rp[q];
+      const long long x = mode_beg[m] + id;
+      in = within_radius(qs32 + q * t.D, nodes32 + x * t.D, qs + q * t.D, nodes + x * t.D, t, metric,
+                         radius_test(rp[q]));
     }
     const unsigned mk = __ballot_sync(MRMG_FULL, in);
     if (lane == 0) {
@@ -939,11 +1012,15 @@ constexpr int kNearWarps = 4;
 // time: the set bits are listed in shared memory and spread over the lanes for
 // the FP64 distance, so a dense word does not serialise one lane.  Bits whose
 // exact distance exceeds the query's r' (or past the mode's nodes) are cleared.
-__global__ void near_exact_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
-                                  const double* __restrict__ nodes, const long long* __restrict__ mode_beg,
+constexpr int kNearStage = 48;   // results per query staged in order by the exact pass
+
+__global__ void near_exact_kernel(const double* __restrict__ qs, const float* __restrict__ qs32, long long Q,
+                                  const int* __restrict__ q_mode, const double* __restrict__ nodes,
+                                  const float* __restrict__ nodes32, const long long* __restrict__ mode_beg,
                                   const long long* __restrict__ mode_end, SliceTab t,
                                   int metric, const double* __restrict__ rp, const long long* __restrict__ woff,
-                                  unsigned* __restrict__ bits, long long* __restrict__ counts) {
+                                  unsigned* __restrict__ bits, long long* __restrict__ counts,
+                                  int* __restrict__ stage) {
   __shared__ int s_list[kNearWarps][1024];
   __shared__ unsigned s_res[kNearWarps][32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -954,9 +1031,11 @@ __global__ void near_exact_kernel(const double* __restrict__ qs, long long Q, co
     const int m = q_mode[q];
     const long long M = mode_end[m] - mode_beg[m];
     const double* xb = nodes + mode_beg[m] * t.D;
+    const float* xb32 = nodes32 + mode_beg[m] * t.D;
     const double* qq = qs + q * t.D;
+    const float* qq32 = qs32 + q * t.D;
     const long long w0 = woff[q], W = woff[q + 1] - w0;
-    const double r = rp[q];
+    const RadiusTest rt = radius_test(rp[q]);
     long long cnt = 0;
     for (long long base = 0; base < W; base += 32) {
       const long long w = base + lane;
@@ -983,19 +1062,31 @@ __global__ void near_exact_kernel(const double* __restrict__ qs, long long Q, co
         const int loc = list[x];
         const long long id = base * 32 + loc;
         if (id >= M) continue;
-        const double* xx = xb + id * t.D;
-        auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
-        if (dist_of(t, metric, dfun) <= r) atomicOr(&s_res[wib][loc >> 5], 1u << (loc & 31));
+        if (within_radius(qq32, xb32 + id * t.D, qq, xb + id * t.D, t, metric, rt))
+          atomicOr(&s_res[wib][loc >> 5], 1u << (loc & 31));
       }
       __syncwarp();
       const unsigned res = s_res[wib][lane];
       if (w < W) bits[w0 + w] = res;
-      cnt += __popc(res);
+      // stage the first kNearStage results of the query in ascending order
+      const int rc = __popc(res);
+      int ri = rc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(MRMG_FULL, ri, o);
+        if (lane >= o) ri += y;
+      }
+      long long sp = cnt + ri - rc;
+      unsigned rm = res;
+      while (rm && sp < kNearStage) {
+        const int b = __ffs(rm) - 1;
+        rm &= rm - 1;
+        stage[q * kNearStage + sp++] = (int)((base + lane) * 32 + b);
+      }
+      cnt += __shfl_sync(MRMG_FULL, ri, 31);
       __syncwarp();
     }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(MRMG_FULL, cnt, o);
-    if (lane == 0) counts[q] = cnt;
+    if (lane == 0) counts[q] = cnt;   // the same in every lane
   }
 }
 
@@ -1030,13 +1121,11 @@ __global__ void near_scan_kernel(const long long* __restrict__ counts, long long
   }
 }
 
-// ascending mode-local indices and their FP64 distances, written from
-// offsets[q]; positions at or past `cap` are skipped
-__global__ void near_emit_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
-                                 const double* __restrict__ nodes, const long long* __restrict__ mode_beg, SliceTab t,
-                                 int metric, const long long* __restrict__ woff, const unsigned* __restrict__ bits,
-                                 const long long* __restrict__ offs, long long cap, long long* __restrict__ out_idx,
-                                 double* __restrict__ out_dist) {
+// ascending mode-local indices, written from offsets[q]; positions at or
+// past `cap` are skipped (their distances follow in near_dist_kernel)
+__global__ void near_emit_kernel(long long Q, const long long* __restrict__ woff, const unsigned* __restrict__ bits,
+                                 const int* __restrict__ stage, const long long* __restrict__ offs, long long cap,
+                                 long long* __restrict__ out_idx) {
   __shared__ int s_list[kNearWarps][1024];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const long long warp = (long long)blockIdx.x * kNearWarps + wib;
@@ -1044,10 +1133,12 @@ __global__ void near_emit_kernel(const double* __restrict__ qs, long long Q, con
   int* list = s_list[wib];
   for (long long q = warp; q < Q; q += nwarps) {
     long long o = offs[q];
-    if (o >= cap || offs[q + 1] == o) continue;
-    const int m = q_mode[q];
-    const double* xb = nodes + mode_beg[m] * t.D;
-    const double* qq = qs + q * t.D;
+    const long long nq = offs[q + 1] - o;
+    if (o >= cap || nq == 0) continue;
+    if (stage && nq <= kNearStage) {   // staged by the exact pass
+      for (int x = lane; x < nq && o + x < cap; x += 32) out_idx[o + x] = stage[q * kNearStage + x];
+      continue;
+    }
     const long long w0 = woff[q], W = woff[q + 1] - w0;
     for (long long base = 0; base < W && o < cap; base += 32) {
       const long long w = base + lane;
@@ -1072,15 +1163,28 @@ __global__ void near_emit_kernel(const double* __restrict__ qs, long long Q, con
       for (int x = lane; x < n; x += 32) {
         const long long p = o + x;
         if (p >= cap) break;
-        const long long id = base * 32 + list[x];
-        const double* xx = xb + id * t.D;
-        auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
-        out_idx[p] = id;
-        out_dist[p] = dist_of(t, metric, dfun);
+        out_idx[p] = base * 32 + list[x];
       }
       o += n;
       __syncwarp();
     }
+  }
+}
+
+// FP64 distance of every written neighbour, a thread per output position (all
+// lanes busy on the FP64 pipe); the total comes from the scan on the device
+__global__ void near_dist_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
+                                 const double* __restrict__ nodes, const long long* __restrict__ mode_beg, SliceTab t,
+                                 int metric, const long long* __restrict__ offs, long long cap,
+                                 const long long* __restrict__ out_idx, double* __restrict__ out_dist) {
+  const long long total = offs[Q] < cap ? offs[Q] : cap;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long q = owner_of(offs, Q, p);
+    const double* qq = qs + q * t.D;
+    const double* xx = nodes + (mode_beg[q_mode[q]] + out_idx[p]) * t.D;
+    auto dfun = [&](int j) { return __dsub_rn(qq[j], xx[j]); };
+    out_dist[p] = dist_of(t, metric, dfun);
   }
 }
 
@@ -1105,6 +1209,7 @@ struct KnnStore {
   std::vector<long long> beg, cnt, cap;   // per mode: first row, rows, capacity
   std::vector<int> mode_tiles;            // per mode: tiles holding its rows
   double* nodes = nullptr;                // [cap_total, D]
+  float* nodes32 = nullptr;               // [cap_total, D] FP32 copy (radius pre-tests)
   unsigned char* tiles = nullptr;         // [cap_total / NT] tiles (tensor-core path)
   void* meta = nullptr;                   // device: beg, end, tile0, xmax per mode
   long long* d_beg = nullptr;
@@ -1171,15 +1276,18 @@ static cudaError_t relayout(KnnStore* s, int n_new, const std::vector<long long>
   long long total = 0;
   for (int m = 0; m < n_new; m++) { beg_new[m] = total; total += cap_new[m]; }
   double* nodes = nullptr;
+  float* nodes32 = nullptr;
   unsigned char* tiles = nullptr;
   void* meta = nullptr;
   const size_t b_l = al1k(sizeof(long long) * std::max(n_new, 1));
   const size_t b_i = al1k(sizeof(int) * std::max(n_new, 1));
   cudaError_t e = cudaMalloc(&nodes, sizeof(double) * std::max<long long>(total, 1) * std::max(s->D, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&nodes32, sizeof(float) * std::max<long long>(total, 1) * std::max(s->D, 1));
   if (e == cudaSuccess && s->tc) e = cudaMalloc(&tiles, (size_t)std::max<long long>(total, s->NT) * kRowBytes);
   if (e == cudaSuccess) e = cudaMalloc(&meta, 2 * b_l + 2 * b_i);
   if (e != cudaSuccess) {
     if (nodes) cudaFree(nodes);
+    if (nodes32) cudaFree(nodes32);
     if (tiles) cudaFree(tiles);
     return e;
   }
@@ -1192,6 +1300,9 @@ static cudaError_t relayout(KnnStore* s, int n_new, const std::vector<long long>
     if (s->cnt[m] == 0) continue;
     e = cudaMemcpyAsync(nodes + beg_new[m] * s->D, s->nodes + s->beg[m] * s->D, sizeof(double) * s->cnt[m] * s->D,
                         cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(nodes32 + beg_new[m] * s->D, s->nodes32 + s->beg[m] * s->D,
+                          sizeof(float) * s->cnt[m] * s->D, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess && s->tc)
       e = cudaMemcpyAsync(tiles + beg_new[m] * kRowBytes, s->tiles + s->beg[m] * kRowBytes,
                           (size_t)s->mode_tiles[m] * s->NT * kRowBytes, cudaMemcpyDeviceToDevice, st);
@@ -1201,14 +1312,17 @@ static cudaError_t relayout(KnnStore* s, int n_new, const std::vector<long long>
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // the old buffers are read until here
   if (e != cudaSuccess) {
     cudaFree(nodes);
+    cudaFree(nodes32);
     if (tiles) cudaFree(tiles);
     cudaFree(meta);
     return e;
   }
   if (s->nodes) cudaFree(s->nodes);
+  if (s->nodes32) cudaFree(s->nodes32);
   if (s->tiles) cudaFree(s->tiles);
   if (s->meta) cudaFree(s->meta);
   s->nodes = nodes;
+  s->nodes32 = nodes32;
   s->tiles = tiles;
   s->meta = meta;
   s->d_beg = d_beg;
@@ -1226,6 +1340,14 @@ static cudaError_t relayout(KnnStore* s, int n_new, const std::vector<long long>
 }
 
 static long long round_up(long long x, long long g) { return (x + g - 1) / g * g; }
+
+// FP32 copy of n values (rounded to nearest)
+static cudaError_t to_f32(const double* src, float* dst, long long n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (int)std::min<long long>((n + 255) / 256, 4096);
+  f64_to_f32_kernel<<<grid, 256, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
+}
 
 static cudaError_t pack_tiles(KnnStore* s, int mode, long long tile_lo, long long tile_hi, cudaStream_t st) {
   if (!s->tc || tile_hi <= tile_lo) return cudaSuccess;
@@ -1258,6 +1380,7 @@ cudaError_t knn_store_build(KnnStore* s, const double* d_nodes, long long M, con
     if (c > 0)
       e = cudaMemcpyAsync(s->nodes + s->beg[m] * D, d_nodes + h_mode_off[m] * D, sizeof(double) * c * D,
                           cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = to_f32(s->nodes + s->beg[m] * D, s->nodes32 + s->beg[m] * D, c * D, st);
   }
   if (e == cudaSuccess) e = upload_meta(s, st);
   if (e == cudaSuccess) e = pack_tiles(s, -1, 0, s->cap_total / s->NT, st);
@@ -1278,6 +1401,8 @@ cudaError_t knn_store_append(KnnStore* s, int mode, const double* rows, long lon
   const long long old = s->cnt[mode];
   // rows may be host or device memory
   e = cudaMemcpyAsync(s->nodes + (s->beg[mode] + old) * s->D, rows, sizeof(double) * n * s->D, cudaMemcpyDefault, st);
+  if (e == cudaSuccess)
+    e = to_f32(s->nodes + (s->beg[mode] + old) * s->D, s->nodes32 + (s->beg[mode] + old) * s->D, n * s->D, st);
   if (e != cudaSuccess) return e;
   s->cnt[mode] = old + n;
   s->mode_tiles[mode] = (int)((old + n + s->NT - 1) / s->NT);
@@ -1294,9 +1419,13 @@ cudaError_t knn_store_append(KnnStore* s, int mode, const double* rows, long lon
 cudaError_t knn_store_remove(KnnStore* s, int mode, long long idx, cudaStream_t st) {
   const long long last = s->cnt[mode] - 1;
   cudaError_t e = cudaSuccess;
-  if (idx != last)
+  if (idx != last) {
     e = cudaMemcpyAsync(s->nodes + (s->beg[mode] + idx) * s->D, s->nodes + (s->beg[mode] + last) * s->D,
                         sizeof(double) * s->D, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s->nodes32 + (s->beg[mode] + idx) * s->D, s->nodes32 + (s->beg[mode] + last) * s->D,
+                          sizeof(float) * s->D, cudaMemcpyDeviceToDevice, st);
+  }
   if (e != cudaSuccess) return e;
   s->cnt[mode] = last;
   s->mode_tiles[mode] = (int)((last + s->NT - 1) / s->NT);
@@ -1319,6 +1448,8 @@ void knn_store_set_path(KnnStore* s, int path) { s->path = path; }
 
 void knn_store_free(KnnStore* s) {
   if (s->nodes) cudaFree(s->nodes);
+  if (s->nodes32) cudaFree(s->nodes32);
+  s->nodes32 = nullptr;
   if (s->tiles) cudaFree(s->tiles);
   if (s->meta) cudaFree(s->meta);
   if (s->d_qmode) cudaFree(s->d_qmode);
@@ -1413,6 +1544,10 @@ static void raise_smem_limit() {
   done = true;
 }
 
+static cudaError_t knn_split_query(KnnStore* s, KnnScratch* scr, const double* d_qs, long long Q, const int* h_q_mode,
+                                   int k, long long* d_idx, double* d_dist, int num_sms, cudaStream_t st,
+                                   const long long* h_list = nullptr, long long n_list = 0);
+
 cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h_q_mode, int k, long long* d_idx,
                       double* d_dist, KnnScratch* scr, int num_sms, int* n_fallback_out, cudaStream_t st) {
   const int n_modes = s->n_modes;
@@ -1498,9 +1633,12 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   if (e != cudaSuccess) return e;
   *n_fallback_out = h_ctr[0];
   if (h_ctr[1]) return cudaErrorLaunchTimeout;
-  if (h_ctr[0] > 0) {
-    e = knn_exact(d_qs, Q, d_qmode, d_fb, h_ctr[0], s->nodes, s->d_beg, s->d_end, s->slices, s->metric, k, d_idx,
-                  d_dist, num_sms, st);
+  if (h_ctr[0] > 0) {   // uncertified queries: node-parallel exact (the list leaves the scratch first)
+    std::vector<long long> fb(h_ctr[0]);
+    e = cudaMemcpyAsync(fb.data(), d_fb, sizeof(long long) * fb.size(), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess)
+      e = knn_split_query(s, scr, d_qs, Q, h_q_mode, k, d_idx, d_dist, num_sms, st, fb.data(), (long long)fb.size());
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -1541,26 +1679,33 @@ static cudaError_t scratch_reserve(KnnScratch* scr, size_t dev_bytes, size_t hos
   return cudaSuccess;
 }
 
-// node-parallel exact k nearest: items (query, 256-node chunk), then a merge
+// node-parallel exact k nearest: items (query, 256-node chunk), then a merge;
+// with `h_list` only the listed queries (n_list of them) are answered
 static cudaError_t knn_split_query(KnnStore* s, KnnScratch* scr, const double* d_qs, long long Q, const int* h_q_mode,
-                                   int k, long long* d_idx, double* d_dist, int num_sms, cudaStream_t st) {
+                                   int k, long long* d_idx, double* d_dist, int num_sms, cudaStream_t st,
+                                   const long long* h_list, long long n_list) {
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  const size_t b_qm = al(sizeof(int) * Q), b_off = al(sizeof(long long) * (Q + 1));
-  const size_t b_up = b_qm + b_off;
+  const long long L = h_list ? n_list : Q;
+  const size_t b_qm = al(sizeof(int) * std::max<long long>(L, 1)), b_off = al(sizeof(long long) * (L + 1));
+  const size_t b_map = h_list ? al(sizeof(long long) * std::max<long long>(L, 1)) : 0;
+  const size_t b_up = b_qm + b_off + b_map;
   cudaError_t e = scratch_reserve(scr, 0, b_up);
   if (e != cudaSuccess) return e;
   unsigned char* hp = (unsigned char*)scr->host;
-  std::memcpy(hp, h_q_mode, sizeof(int) * Q);
+  int* hqm = (int*)hp;
+  for (long long l = 0; l < L; l++) hqm[l] = h_q_mode[h_list ? h_list[l] : l];
   long long* ioff = (long long*)(hp + b_qm);
   ioff[0] = 0;
-  for (long long q = 0; q < Q; q++) ioff[q + 1] = ioff[q] + (s->cnt[h_q_mode[q]] + kSplitNodes - 1) / kSplitNodes;
-  const long long n_items = ioff[Q];
+  for (long long l = 0; l < L; l++) ioff[l + 1] = ioff[l] + (s->cnt[hqm[l]] + kSplitNodes - 1) / kSplitNodes;
+  if (h_list) std::memcpy(hp + b_qm + b_off, h_list, sizeof(long long) * L);
+  const long long n_items = ioff[L];
   const size_t b_cand = al(sizeof(long long) * std::max<long long>(n_items, 1) * k);
   e = scratch_reserve(scr, b_up + 2 * b_cand, 0);
   if (e != cudaSuccess) return e;
   unsigned char* p = (unsigned char*)scr->block;
   const int* d_qm = (const int*)p;
   const long long* d_ioff = (const long long*)(p + b_qm);
+  const long long* d_map = h_list ? (const long long*)(p + b_qm + b_off) : nullptr;
   long long* d_ck = (long long*)(p + b_up);
   long long* d_ci = (long long*)(p + b_up + b_cand);
   e = cudaMemcpyAsync(p, hp, b_up, cudaMemcpyHostToDevice, st);
@@ -1568,17 +1713,17 @@ static cudaError_t knn_split_query(KnnStore* s, KnnScratch* scr, const double* d
   if (n_items > 0) {
     const int grid = (int)std::min<long long>((n_items + 3) / 4, (long long)num_sms * 16);
     if (k <= 16)
-      knn_split_kernel<16><<<grid, 128, 0, st>>>(d_qs, Q, d_qm, d_ioff, s->nodes, s->d_beg, s->d_end, s->slices,
-                                                 s->metric, k, d_ck, d_ci);
+      knn_split_kernel<16><<<grid, 128, 0, st>>>(d_qs, d_map, L, d_qm, d_ioff, s->nodes, s->d_beg, s->d_end,
+                                                 s->slices, s->metric, k, d_ck, d_ci);
     else
-      knn_split_kernel<kKnnMaxK><<<grid, 128, 0, st>>>(d_qs, Q, d_qm, d_ioff, s->nodes, s->d_beg, s->d_end, s->slices,
-                                                       s->metric, k, d_ck, d_ci);
+      knn_split_kernel<kKnnMaxK><<<grid, 128, 0, st>>>(d_qs, d_map, L, d_qm, d_ioff, s->nodes, s->d_beg, s->d_end,
+                                                       s->slices, s->metric, k, d_ck, d_ci);
   }
-  const int mgrid = (int)std::max<long long>(1, std::min<long long>((Q + 3) / 4, (long long)num_sms * 16));
+  const int mgrid = (int)std::max<long long>(1, std::min<long long>((L + 3) / 4, (long long)num_sms * 16));
   if (k <= 16)
-    knn_split_merge_kernel<16><<<mgrid, 128, 0, st>>>(Q, d_ioff, k, d_ck, d_ci, d_idx, d_dist);
+    knn_split_merge_kernel<16><<<mgrid, 128, 0, st>>>(d_map, L, d_ioff, k, d_ck, d_ci, d_idx, d_dist);
   else
-    knn_split_merge_kernel<kKnnMaxK><<<mgrid, 128, 0, st>>>(Q, d_ioff, k, d_ck, d_ci, d_idx, d_dist);
+    knn_split_merge_kernel<kKnnMaxK><<<mgrid, 128, 0, st>>>(d_map, L, d_ioff, k, d_ck, d_ci, d_idx, d_dist);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // the pinned tables are reused by the next call
   return e;
@@ -1631,6 +1776,7 @@ struct NearState {
   const int* qmode = nullptr;
   const long long* woff = nullptr;
   const unsigned* bits = nullptr;
+  const int* stage = nullptr;
   const long long* offs = nullptr;
   long long total = 0;
 };
@@ -1708,7 +1854,9 @@ cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long
   const size_t b_bits = al(sizeof(unsigned) * std::max<long long>(Wtot, 1));
   const size_t b_cnt = al(sizeof(long long) * std::max<long long>(Q, 1));
   const size_t b_offs = al(sizeof(long long) * (Q + 1));
-  const size_t need = b_up + b_bits + b_cnt + b_offs + 256;
+  const size_t b_q32 = al(sizeof(float) * std::max<long long>(Q, 1) * std::max(s->D, 1));
+  const size_t b_stage = al(sizeof(int) * std::max<long long>(Q, 1) * kNearStage);
+  const size_t need = b_up + b_bits + b_cnt + b_offs + 256 + b_q32 + b_stage;
   if (ns->scr.bytes < need) {
     if (ns->scr.block) cudaFree(ns->scr.block);
     ns->scr.block = nullptr;
@@ -1728,8 +1876,11 @@ cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long
   long long* d_cnt = (long long*)(p + b_up + b_bits);
   long long* d_offs = (long long*)(p + b_up + b_bits + b_cnt);
   long long* d_ctr = (long long*)(p + b_up + b_bits + b_cnt + b_offs);   // [0] total, [1] error bits
+  float* d_q32 = (float*)(p + b_up + b_bits + b_cnt + b_offs + 256);
+  int* d_stage = (int*)(p + b_up + b_bits + b_cnt + b_offs + 256 + b_q32);
   cudaError_t e = cudaMemcpyAsync(p, hp, b_up, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, 256, st);
+  if (e == cudaSuccess) e = to_f32(d_qs, d_q32, Q * s->D, st);
   if (e != cudaSuccess) return e;
   if (tc && !pl.items.empty()) {
     const size_t smem = tc_smem_bytes(tc);
@@ -1748,21 +1899,24 @@ cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long
   if (e != cudaSuccess) return e;
   const int grid = near_grid(Q, num_sms);
   if (tc) {
-    near_exact_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, s->d_end, t, metric, d_rp,
-                                                        d_woff, d_bits, d_cnt);
+    near_exact_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, d_q32, Q, d_qmode, nodes, s->nodes32, s->d_beg,
+                                                        s->d_end, t, metric, d_rp, d_woff, d_bits, d_cnt, d_stage);
   } else {
     e = cudaMemsetAsync(d_cnt, 0, sizeof(long long) * Q, st);
     if (e != cudaSuccess) return e;
     if (Wtot > 0) {
       const int g2 = (int)std::min<long long>((Wtot + 3) / 4, (long long)num_sms * 16);
-      near_split_kernel<<<g2, 128, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, s->d_end, t, metric, d_rp, d_woff,
-                                            d_bits, (unsigned long long*)d_cnt);
+      near_split_kernel<<<g2, 128, 0, st>>>(d_qs, d_q32, Q, d_qmode, nodes, s->nodes32, s->d_beg, s->d_end, t, metric,
+                                            d_rp, d_woff, d_bits, (unsigned long long*)d_cnt);
     }
   }
   near_scan_kernel<<<1, 1024, 0, st>>>(d_cnt, Q, d_offsets, d_offs, d_ctr);
-  if (cap > 0)
-    near_emit_kernel<<<grid, 32 * kNearWarps, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, t, metric, d_woff, d_bits,
-                                                       d_offs, cap, d_idx, d_dist);
+  if (cap > 0) {
+    near_emit_kernel<<<grid, 32 * kNearWarps, 0, st>>>(Q, d_woff, d_bits, tc ? d_stage : nullptr, d_offs, cap, d_idx);
+    if (d_dist)
+      near_dist_kernel<<<num_sms * 4, 256, 0, st>>>(d_qs, Q, d_qmode, nodes, s->d_beg, t, metric, d_offs, cap, d_idx,
+                                                    d_dist);
+  }
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(h_ctr, d_ctr, 2 * sizeof(long long), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1777,6 +1931,7 @@ cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long
   ns->qmode = d_qmode;
   ns->woff = d_woff;
   ns->bits = d_bits;
+  ns->stage = tc ? d_stage : nullptr;
   ns->offs = d_offs;
   ns->total = h_ctr[0];
   *total_out = h_ctr[0];
@@ -1785,9 +1940,11 @@ cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long
 
 cudaError_t near_fetch(NearState* ns, long long* d_idx, double* d_dist, long long cap, int num_sms, cudaStream_t st) {
   if (ns->Q == 0 || cap <= 0) return cudaSuccess;
-  near_emit_kernel<<<near_grid(ns->Q, num_sms), 32 * kNearWarps, 0, st>>>(
-      ns->qs, ns->Q, ns->qmode, ns->nodes, ns->mode_beg, ns->t, ns->metric, ns->woff, ns->bits, ns->offs, cap, d_idx,
-      d_dist);
+  near_emit_kernel<<<near_grid(ns->Q, num_sms), 32 * kNearWarps, 0, st>>>(ns->Q, ns->woff, ns->bits, ns->stage,
+                                                                            ns->offs, cap, d_idx);
+  if (d_dist)
+    near_dist_kernel<<<num_sms * 4, 256, 0, st>>>(ns->qs, ns->Q, ns->qmode, ns->nodes, ns->mode_beg, ns->t,
+                                                  ns->metric, ns->offs, cap, d_idx, d_dist);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return e;

@@ -147,12 +147,14 @@ class NodeStore:
         self.last_stats = {"tensor_core": bool(st[0]), "rerun_exact": int(st[1])}
         return idx, dist
 
-    def near(self, queries, query_mode, radius, add_eps: float = 1e-10, cap: int | None = None, stream=None):
+    def near(self, queries, query_mode, radius, add_eps: float = 1e-10, cap: int | None = None,
+             distances: bool = True, stream=None):
         """Radius neighbours, as RRT* near / find_nearest_indices
         (planners/rrtstar_base.py:439-453, 1296-1337): per query every node of
         its mode with distance <= radius + add_eps, ascending mode-local index.
         ``radius`` is a scalar or one value per query.  Returns CSR device
-        tensors (offsets [Q + 1], idx [total], dist [total] float64)."""
+        tensors (offsets [Q + 1], idx [total], dist [total] float64; dist is
+        None when ``distances`` is False)."""
         qs = _dev_tensor(queries, dtype=torch.float64)
         qm = np.ascontiguousarray(np.asarray(query_mode, dtype=np.int32).reshape(-1))
         Q = qs.shape[0]
@@ -163,15 +165,15 @@ class NodeStore:
             cap = max(1024, 64 * Q)
         offs = torch.empty(Q + 1, dtype=torch.int64, device=qs.device)
         idx = torch.empty(max(cap, 1), dtype=torch.int64, device=qs.device)
-        dist = torch.empty(max(cap, 1), dtype=torch.float64, device=qs.device)
+        dist = torch.empty(max(cap, 1), dtype=torch.float64, device=qs.device) if distances else None
         tot = np.zeros(1, dtype=np.int64)
         _lib.check(self.lib.mrmg_near(self.h, qs.data_ptr(), Q, qm.ctypes.data, r.ctypes.data, float(add_eps),
-                                      offs.data_ptr(), idx.data_ptr(), dist.data_ptr(), int(cap), tot.ctypes.data,
-                                      _lib.stream_handle(stream)), "near")
+                                      offs.data_ptr(), idx.data_ptr(), None if dist is None else dist.data_ptr(),
+                                      int(cap), tot.ctypes.data, _lib.stream_handle(stream)), "near")
         total = int(tot[0])
         if total > cap:
             idx = torch.empty(total, dtype=torch.int64, device=qs.device)
-            dist = torch.empty(total, dtype=torch.float64, device=qs.device)
-            _lib.check(self.lib.mrmg_near_fetch(self.h, idx.data_ptr(), dist.data_ptr(), total,
-                                                _lib.stream_handle(stream)), "near fetch")
-        return offs, idx[:total], dist[:total]
+            dist = torch.empty(total, dtype=torch.float64, device=qs.device) if distances else None
+            _lib.check(self.lib.mrmg_near_fetch(self.h, idx.data_ptr(), None if dist is None else dist.data_ptr(),
+                                                total, _lib.stream_handle(stream)), "near fetch")
+        return offs, idx[:total], (dist[:total] if dist is not None else None)

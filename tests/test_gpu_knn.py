@@ -138,6 +138,8 @@ def test_near_workload_vs_oracle(gpu, oracle, metric, path):
     assert want[0][-1] > 0
     assert _csr_equal(store.near(w["queries"], w["q_mode"], r), want)
     assert _csr_equal(store.near(w["queries"], w["q_mode"], r, cap=7), want)
+    offs, idx, dist = store.near(w["queries"], w["q_mode"], r, distances=False)
+    assert dist is None and np.array_equal(offs.cpu().numpy(), want[0]) and np.array_equal(idx.cpu().numpy(), want[1])
     z = oracle.near(w["queries"], w["q_mode"], w["nodes"], w["mode_offsets"], w["slices"], metric, 0.0)
     assert _csr_equal(store.near(w["queries"], w["q_mode"], 0.0), z)
 
@@ -255,3 +257,24 @@ def test_node_store_grow_from_empty(gpu, oracle):
         store.append(m, q)
         host.append(m, q)
     assert store.size(0) + store.size(1) == 300
+
+
+def test_knn_uncertified_queries_rerun(gpu, oracle):
+    """Nodes repeated many times fill the kept candidate lists with ties, so
+    the certificate fails and those queries are answered by the node-parallel
+    exact kernels; the result is still the oracle's (ties to the lower index)."""
+    knn = pkg("knn")
+    rng = np.random.default_rng(13)
+    base = rng.uniform(-1, 1, (40, 28))
+    nodes = np.concatenate([np.repeat(base, 150, axis=0), rng.uniform(-1, 1, (3000, 28))])
+    off = np.array([0, 6000, len(nodes)])
+    qs = np.concatenate([base[:20] + 1e-3, rng.uniform(-1, 1, (200, 28))])
+    qm = np.concatenate([np.zeros(20, np.int32), rng.integers(0, 2, 200).astype(np.int32)])
+    sl = [[0, 7], [7, 14], [14, 21], [21, 28]]
+    store = knn.NodeStore(nodes, off, sl, "euclidean", path="tensor_core")
+    for k in (10, 16):
+        idx, dist = store.knn(qs, qm, k)
+        oi, od = oracle.knn(qs, qm, nodes, off, sl, "euclidean", k)
+        assert np.array_equal(idx.cpu().numpy(), oi), k
+        assert np.array_equal(dist.cpu().numpy(), od), k
+        assert store.last_stats["rerun_exact"] >= 20

@@ -58,3 +58,29 @@ def test_penetration_params_record():
 def test_new_entry_points_exported(cuda_lib):
     for name in ("mrmg_path_penetration", "mrmg_penetration_info", "mrmg_microbench_fma"):
         assert hasattr(cuda_lib, name)
+
+
+def test_radius_fp32_band():
+    """The FP32 pre-test of radius queries assumes the FP32 sum of squared
+    coordinate differences lies within 2.4e-6 (|q| + |x|)^2 of the exact
+    squared distance (the kernel decides outside 7.7e-6 of that).  Checked
+    with numpy FP32 arithmetic (separate multiply and add: more rounding than
+    the kernel's fused chain) on 28-D inputs from 1e-3 to 1e4 in scale,
+    including near-duplicate pairs and mixed signs."""
+    rng = np.random.default_rng(0)
+    worst = 0.0
+    for scale in (1e-3, 1.0, 3.14, 1e2, 1e4):
+        q = rng.uniform(-scale, scale, (4000, 28))
+        x = np.where(rng.random((4000, 1)) < 0.3, q + rng.normal(0, 1e-5 * scale, q.shape),
+                     rng.uniform(-scale, scale, q.shape))
+        qf, xf = q.astype(np.float32), x.astype(np.float32)
+        m = np.zeros(len(q), dtype=np.float32)
+        for k in range(28):
+            d = qf[:, k] - xf[:, k]
+            m = (m + d * d).astype(np.float32)
+        exact = np.array([float(sum((a - b) ** 2 for a, b in zip(map(np.longdouble, qi), map(np.longdouble, xi))))
+                          for qi, xi in zip(q[:400], x[:400])])
+        e = np.linalg.norm(q[:400], axis=1) + np.linalg.norm(x[:400], axis=1)
+        ratio = np.abs(m[:400].astype(np.float64) - exact) / (e * e)
+        worst = max(worst, float(ratio.max()))
+    assert worst <= 2.4e-6, worst
