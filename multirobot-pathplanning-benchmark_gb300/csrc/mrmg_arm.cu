@@ -63,10 +63,18 @@ constexpr int kNearBlock = 512;   // at most this many group pairs compacted per
 
 __host__ __device__ inline int near_block(const ArmDev& s) { return s.NP < kNearBlock ? (s.NP > 0 ? s.NP : 1) : kNearBlock; }
 
+constexpr int kBoxBlock = 8;   // boxes whose near (group, box) items are compacted together
+
+// the per-warp list holds the near (group, box) items of one box block, then
+// the near group pairs of one pair block
+__host__ __device__ inline int list_cap(const ArmDev& s) {
+  return near_block(s) > s.G * kBoxBlock ? near_block(s) : s.G * kBoxBlock;
+}
+
 __host__ __device__ inline size_t warp32_bytes(const ArmDev& s) {
   return align16(sizeof(float2) * s.D) + align16(sizeof(float) * s.D) +
          align16(sizeof(float4) * s.G * s.SPG) + align16(sizeof(float) * s.G * s.SPG) +
-         align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * near_block(s));
+         align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * list_cap(s));
 }
 
 // per-warp FP64 work area for pass 2: joint values, cos/sin, sphere centres
@@ -320,7 +328,11 @@ __device__ __forceinline__ uint32_t* wnear_of(const ArmDev& s, float4* wsph) {
 // Warp evaluation of one configuration.
 // Returns V_COLLIDE, V_FREE, or (pass 1 only) V_PENDING; warp-uniform.
 // ---------------------------------------------------------------------------
-template <int GPL, int SPG, bool RESOLVE, class Src>
+// COMPACT selects the box phase: per box with an early exit at the first
+// colliding box (configurations that mostly collide: the first position of
+// each edge, stored configurations), or compacted (group, box) items in
+// blocks (positions of surviving edges, mostly free: every box is scanned).
+template <int GPL, int SPG, bool RESOLVE, bool COMPACT = false, class Src>
 __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, float* wqv,
                                float4* wsph, double* w64, int lane, const Src& src, bool full) {
   __syncwarp();
@@ -383,7 +395,7 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
   }
 
   // --- FP32 chain + sphere centres (and group bound centres) of the owned groups
-  float cx[GPL][SPG], cy[GPL][SPG], cz[GPL][SPG], rh[GPL][SPG];
+  float cx[GPL][SPG], cy[GPL][SPG], cz[GPL][SPG], rh[GPL][SPG];   // per-box phase only
   float gb[GPL][4];
 #pragma unroll
   for (int u = 0; u < GPL; u++) {
@@ -407,13 +419,15 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
         float y = p[1] + (R[3] * l.x + R[4] * l.y + R[5] * l.z);
         float z = p[2] + (R[6] * l.x + R[7] * l.y + R[8] * l.z);
         if (bd.y < 0.f) { x = kFar * (float)(g + 1); y = x; z = 0.f; }   // padding slot
-        cx[u][v] = x; cy[u][v] = y; cz[u][v] = z; rh[u][v] = bd.y;
+        if constexpr (!COMPACT) { cx[u][v] = x; cy[u][v] = y; cz[u][v] = z; rh[u][v] = bd.y; }
         wsph[g * SPG + v] = make_float4(x, y, z, bd.z);
       }
     } else {
+      if constexpr (!COMPACT) {
 #pragma unroll
-      for (int v = 0; v < SPG; v++) {
-        cx[u][v] = kFar * (float)(200 + lane); cy[u][v] = cx[u][v]; cz[u][v] = 0.f; rh[u][v] = -1.f;
+        for (int v = 0; v < SPG; v++) {
+          cx[u][v] = kFar * (float)(200 + lane); cy[u][v] = cx[u][v]; cz[u][v] = 0.f; rh[u][v] = -1.f;
+        }
       }
       gb[u][0] = kFar * (float)(200 + lane); gb[u][1] = gb[u][0]; gb[u][2] = 0.f; gb[u][3] = -1.f;
     }
@@ -421,40 +435,50 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
   __syncwarp();
 
   bool unc = false;
-  // --- spheres against boxes
-  for (int b = 0; b < s.B; b++) {
-    const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
-    float umin = 3.0e38f;
+  // --- spheres against boxes.  Per block of boxes, every lane tests its
+  // groups' bounds against each box and the (group, box) pairs whose bound
+  // reaches the box are compacted into the warp's list; then each lane takes
+  // one listed pair and tests the group's spheres (centres from the warp's
+  // sphere table), so the sphere tests run with the lanes full.  A collision
+  // ends the configuration after its block (early exit); the blocks grow
+  // 1, 1, 2, 4, then kBoxBlock boxes, so the boxes tested first (the
+  // tuned order puts the likeliest hits there) still exit early.
+  if constexpr (COMPACT) {
+    uint32_t* witem = wnear_of(s, wsph);
+    const unsigned ltb = (1u << lane) - 1u;
+    int bs = 1;
+    for (int b0 = 0; b0 < s.B; b0 += bs, bs = b0 <= 1 ? 1 : min(2 * bs, kBoxBlock)) {
+      const int b1 = min(s.B, b0 + bs);
+      int nit = 0;
+      for (int b = b0; b < b1; b++) {
+        const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
 #pragma unroll
-    for (int u = 0; u < GPL; u++) {
-      // the group's bound first: its spheres are tested only if it reaches the box
-      const float gx = fmaxf(fabsf(gb[u][0] - bc.x) - bh.x, 0.f);
-      const float gy = fmaxf(fabsf(gb[u][1] - bc.y) - bh.y, 0.f);
-      const float gz = fmaxf(fabsf(gb[u][2] - bc.z) - bh.z, 0.f);
-      if (fmaf(gz, gz, fmaf(gy, gy, fmaf(gx, gx, -gb[u][3]))) <= 0.f) {
-#pragma unroll
-        for (int v = 0; v < SPG; v++) {
-          const float ex = fmaxf(fabsf(cx[u][v] - bc.x) - bh.x, 0.f);
-          const float ey = fmaxf(fabsf(cy[u][v] - bc.y) - bh.y, 0.f);
-          const float ez = fmaxf(fabsf(cz[u][v] - bc.z) - bh.z, 0.f);
-          umin = fminf(umin, fmaf(ez, ez, fmaf(ey, ey, fmaf(ex, ex, -rh[u][v]))));
+        for (int u = 0; u < GPL; u++) {
+          const float gx = fmaxf(fabsf(gb[u][0] - bc.x) - bh.x, 0.f);
+          const float gy = fmaxf(fabsf(gb[u][1] - bc.y) - bh.y, 0.f);
+          const float gz = fmaxf(fabsf(gb[u][2] - bc.z) - bh.z, 0.f);
+          const bool nr = fmaf(gz, gz, fmaf(gy, gy, fmaf(gx, gx, -gb[u][3]))) <= 0.f;
+          const unsigned m = __ballot_sync(MRMG_FULL, nr);
+          if (nr) witem[nit + __popc(m & ltb)] = (uint32_t)(lane + 32 * u) | ((uint32_t)b << 16);
+          nit += __popc(m);
         }
       }
-    }
-    if (__any_sync(MRMG_FULL, umin <= 0.f)) {
-      bool coll = false;
-      if (umin <= 0.f) {
-#pragma unroll
-        for (int u = 0; u < GPL; u++)
+      __syncwarp();
+      for (int base = 0; base < nit; base += 32) {
+        bool coll = false;
+        if (base + lane < nit) {
+          const uint32_t it = witem[base + lane];
+          const int g = it & 0xffff, b = it >> 16;
+          const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
 #pragma unroll
           for (int v = 0; v < SPG; v++) {
-            const int g = lane + 32 * u;
-            const float ex = fmaxf(fabsf(cx[u][v] - bc.x) - bh.x, 0.f);
-            const float ey = fmaxf(fabsf(cy[u][v] - bc.y) - bh.y, 0.f);
-            const float ez = fmaxf(fabsf(cz[u][v] - bc.z) - bh.z, 0.f);
+            const float4 c = wsph[g * SPG + v];
+            const float4 bd = t.band[g * SPG + v];
+            const float ex = fmaxf(fabsf(c.x - bc.x) - bh.x, 0.f);
+            const float ey = fmaxf(fabsf(c.y - bc.y) - bh.y, 0.f);
+            const float ez = fmaxf(fabsf(c.z - bc.z) - bh.z, 0.f);
             const float ss = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-            if (ss <= rh[u][v]) {
-              const float4 bd = t.band[g * SPG + v];
+            if (ss <= bd.y) {
               if (ss < bd.x) coll = true;
               else if (RESOLVE) {
                 const int slot = g * SPG + v;
@@ -464,10 +488,64 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
               }
             }
           }
+        }
+        if (__any_sync(MRMG_FULL, coll)) {
+          if (!full) return V_COLLIDE;
+          hit_any = true;
+        }
       }
-      if (__any_sync(MRMG_FULL, coll)) {
-        if (!full) return V_COLLIDE;
-        hit_any = true;
+      __syncwarp();   // the next block rewrites the list
+    }
+  }
+  if constexpr (!COMPACT) {
+    // --- spheres against boxes, box by box
+    for (int b = 0; b < s.B; b++) {
+      const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
+      float umin = 3.0e38f;
+#pragma unroll
+      for (int u = 0; u < GPL; u++) {
+        // the group's bound first: its spheres are tested only if it reaches the box
+        const float gx = fmaxf(fabsf(gb[u][0] - bc.x) - bh.x, 0.f);
+        const float gy = fmaxf(fabsf(gb[u][1] - bc.y) - bh.y, 0.f);
+        const float gz = fmaxf(fabsf(gb[u][2] - bc.z) - bh.z, 0.f);
+        if (fmaf(gz, gz, fmaf(gy, gy, fmaf(gx, gx, -gb[u][3]))) <= 0.f) {
+#pragma unroll
+          for (int v = 0; v < SPG; v++) {
+            const float ex = fmaxf(fabsf(cx[u][v] - bc.x) - bh.x, 0.f);
+            const float ey = fmaxf(fabsf(cy[u][v] - bc.y) - bh.y, 0.f);
+            const float ez = fmaxf(fabsf(cz[u][v] - bc.z) - bh.z, 0.f);
+            umin = fminf(umin, fmaf(ez, ez, fmaf(ey, ey, fmaf(ex, ex, -rh[u][v]))));
+          }
+        }
+      }
+      if (__any_sync(MRMG_FULL, umin <= 0.f)) {
+        bool coll = false;
+        if (umin <= 0.f) {
+#pragma unroll
+          for (int u = 0; u < GPL; u++)
+#pragma unroll
+            for (int v = 0; v < SPG; v++) {
+              const int g = lane + 32 * u;
+              const float ex = fmaxf(fabsf(cx[u][v] - bc.x) - bh.x, 0.f);
+              const float ey = fmaxf(fabsf(cy[u][v] - bc.y) - bh.y, 0.f);
+              const float ez = fmaxf(fabsf(cz[u][v] - bc.z) - bh.z, 0.f);
+              const float ss = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+              if (ss <= rh[u][v]) {
+                const float4 bd = t.band[g * SPG + v];
+                if (ss < bd.x) coll = true;
+                else if (RESOLVE) {
+                  const int slot = g * SPG + v;
+                  coll |= exact_box_hit(wc64 + (size_t)slot * 3, s.box64 + (size_t)b * 6, s.sph64[(size_t)slot * 5 + 4]);
+                } else {
+                  unc = true;
+                }
+              }
+            }
+        }
+        if (__any_sync(MRMG_FULL, coll)) {
+          if (!full) return V_COLLIDE;
+          hit_any = true;
+        }
       }
     }
   }
@@ -588,7 +666,7 @@ __device__ __forceinline__ void warp_areas(const ArmDev& s, unsigned char* smem_
   *wqv = (float*)p; p += align16(sizeof(float) * s.D);
   *wsph = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
   // pair-filter norms, group bounds, near group pairs (after wsph, see wss_of)
-  p += align16(sizeof(float) * s.G * s.SPG) + align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * near_block(s));
+  p += align16(sizeof(float) * s.G * s.SPG) + align16(sizeof(float4) * s.G) + align16(sizeof(uint32_t) * list_cap(s));
   *w64 = (double*)p;
 }
 
@@ -934,7 +1012,7 @@ __global__ void __launch_bounds__(256, GPL == 1 ? 4 : (GPL == 2 ? 2 : 1)) arm_ed
       sdf.rn = __frcp_rn(sdf.nm1);
       sdf.fi = (float)(int)is;   // survivors have N <= 2^24
       stat_cfg++;
-      const uint8_t code = eval_config<GPL, SPG, false>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
+      const uint8_t code = eval_config<GPL, SPG, false, true>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
       if (lane == 0) {
         if (code == V_COLLIDE) vsurv[ls].dead = 1;
         else if (code == V_PENDING) vsurv[ls].pend = 1;
