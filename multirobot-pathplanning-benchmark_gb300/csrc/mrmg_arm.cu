@@ -328,11 +328,16 @@ __device__ __forceinline__ uint32_t* wnear_of(const ArmDev& s, float4* wsph) {
 // Warp evaluation of one configuration.
 // Returns V_COLLIDE, V_FREE, or (pass 1 only) V_PENDING; warp-uniform.
 // ---------------------------------------------------------------------------
-// COMPACT selects the box phase: per box with an early exit at the first
-// colliding box (configurations that mostly collide: the first position of
-// each edge, stored configurations), or compacted (group, box) items in
-// blocks (positions of surviving edges, mostly free: every box is scanned).
-template <int GPL, int SPG, bool RESOLVE, bool COMPACT = false, class Src>
+// BOXES selects the box phase: BOX_EACH tests box by box with an early exit
+// at the first colliding box (stored configurations); BOX_BLOCKS compacts
+// the near (group, box) items of blocks of boxes (positions of surviving
+// edges, mostly free: every box is scanned); BOX_HEAD_BLOCKS tests the
+// first kBoxBlock boxes (the tuned order puts the likeliest hits first) box
+// by box and the rest in blocks (first positions of edges: most collide early,
+// the survivors scan everything).
+enum : int { BOX_EACH = 0, BOX_BLOCKS = 1, BOX_HEAD_BLOCKS = 2 };
+
+template <int GPL, int SPG, bool RESOLVE, int BOXES = BOX_EACH, class Src>
 __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, float* wqv,
                                float4* wsph, double* w64, int lane, const Src& src, bool full) {
   __syncwarp();
@@ -419,11 +424,11 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
         float y = p[1] + (R[3] * l.x + R[4] * l.y + R[5] * l.z);
         float z = p[2] + (R[6] * l.x + R[7] * l.y + R[8] * l.z);
         if (bd.y < 0.f) { x = kFar * (float)(g + 1); y = x; z = 0.f; }   // padding slot
-        if constexpr (!COMPACT) { cx[u][v] = x; cy[u][v] = y; cz[u][v] = z; rh[u][v] = bd.y; }
+        if constexpr (BOXES != BOX_BLOCKS) { cx[u][v] = x; cy[u][v] = y; cz[u][v] = z; rh[u][v] = bd.y; }
         wsph[g * SPG + v] = make_float4(x, y, z, bd.z);
       }
     } else {
-      if constexpr (!COMPACT) {
+      if constexpr (BOXES != BOX_BLOCKS) {
 #pragma unroll
         for (int v = 0; v < SPG; v++) {
           cx[u][v] = kFar * (float)(200 + lane); cy[u][v] = cx[u][v]; cz[u][v] = 0.f; rh[u][v] = -1.f;
@@ -435,71 +440,10 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
   __syncwarp();
 
   bool unc = false;
-  // --- spheres against boxes.  Per block of boxes, every lane tests its
-  // groups' bounds against each box and the (group, box) pairs whose bound
-  // reaches the box are compacted into the warp's list; then each lane takes
-  // one listed pair and tests the group's spheres (centres from the warp's
-  // sphere table), so the sphere tests run with the lanes full.  A collision
-  // ends the configuration after its block (early exit); the blocks grow
-  // 1, 1, 2, 4, then kBoxBlock boxes, so the boxes tested first (the
-  // tuned order puts the likeliest hits there) still exit early.
-  if constexpr (COMPACT) {
-    uint32_t* witem = wnear_of(s, wsph);
-    const unsigned ltb = (1u << lane) - 1u;
-    int bs = 1;
-    for (int b0 = 0; b0 < s.B; b0 += bs, bs = b0 <= 1 ? 1 : min(2 * bs, kBoxBlock)) {
-      const int b1 = min(s.B, b0 + bs);
-      int nit = 0;
-      for (int b = b0; b < b1; b++) {
-        const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
-#pragma unroll
-        for (int u = 0; u < GPL; u++) {
-          const float gx = fmaxf(fabsf(gb[u][0] - bc.x) - bh.x, 0.f);
-          const float gy = fmaxf(fabsf(gb[u][1] - bc.y) - bh.y, 0.f);
-          const float gz = fmaxf(fabsf(gb[u][2] - bc.z) - bh.z, 0.f);
-          const bool nr = fmaf(gz, gz, fmaf(gy, gy, fmaf(gx, gx, -gb[u][3]))) <= 0.f;
-          const unsigned m = __ballot_sync(MRMG_FULL, nr);
-          if (nr) witem[nit + __popc(m & ltb)] = (uint32_t)(lane + 32 * u) | ((uint32_t)b << 16);
-          nit += __popc(m);
-        }
-      }
-      __syncwarp();
-      for (int base = 0; base < nit; base += 32) {
-        bool coll = false;
-        if (base + lane < nit) {
-          const uint32_t it = witem[base + lane];
-          const int g = it & 0xffff, b = it >> 16;
-          const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
-#pragma unroll
-          for (int v = 0; v < SPG; v++) {
-            const float4 c = wsph[g * SPG + v];
-            const float4 bd = t.band[g * SPG + v];
-            const float ex = fmaxf(fabsf(c.x - bc.x) - bh.x, 0.f);
-            const float ey = fmaxf(fabsf(c.y - bc.y) - bh.y, 0.f);
-            const float ez = fmaxf(fabsf(c.z - bc.z) - bh.z, 0.f);
-            const float ss = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-            if (ss <= bd.y) {
-              if (ss < bd.x) coll = true;
-              else if (RESOLVE) {
-                const int slot = g * SPG + v;
-                coll |= exact_box_hit(wc64 + (size_t)slot * 3, s.box64 + (size_t)b * 6, s.sph64[(size_t)slot * 5 + 4]);
-              } else {
-                unc = true;
-              }
-            }
-          }
-        }
-        if (__any_sync(MRMG_FULL, coll)) {
-          if (!full) return V_COLLIDE;
-          hit_any = true;
-        }
-      }
-      __syncwarp();   // the next block rewrites the list
-    }
-  }
-  if constexpr (!COMPACT) {
-    // --- spheres against boxes, box by box
-    for (int b = 0; b < s.B; b++) {
+  const int b_each = BOXES == BOX_EACH ? s.B : (BOXES == BOX_HEAD_BLOCKS ? min(s.B, kBoxBlock) : 0);
+  {
+    // --- spheres against boxes, box by box: all of them, or the head
+    for (int b = 0; b < b_each; b++) {
       const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
       float umin = 3.0e38f;
 #pragma unroll
@@ -547,6 +491,69 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
           hit_any = true;
         }
       }
+    }
+  }
+
+  // --- spheres against boxes in blocks.  Per block, every lane tests its
+  // groups' bounds against each box and the (group, box) pairs whose bound
+  // reaches the box are compacted into the warp's list; then each lane takes
+  // one listed pair and tests the group's spheres (centres from the warp's
+  // sphere table), so the sphere tests run with the lanes full.  A collision
+  // ends the configuration after its block (early exit).
+  if constexpr (BOXES != BOX_EACH) {
+    uint32_t* witem = wnear_of(s, wsph);
+    const unsigned ltb = (1u << lane) - 1u;
+    // BOX_BLOCKS: blocks of 1, 1, 2, 4, then kBoxBlock boxes from the first
+    // box; BOX_HEAD_BLOCKS: blocks of kBoxBlock after the per-box head
+    int bs = BOXES == BOX_BLOCKS ? 1 : kBoxBlock;
+    for (int b0 = b_each; b0 < s.B; b0 += bs, bs = (BOXES == BOX_BLOCKS && b0 <= 1) ? 1 : min(2 * bs, kBoxBlock)) {
+      const int b1 = min(s.B, b0 + bs);
+      int nit = 0;
+      for (int b = b0; b < b1; b++) {
+        const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
+#pragma unroll
+        for (int u = 0; u < GPL; u++) {
+          const float gx = fmaxf(fabsf(gb[u][0] - bc.x) - bh.x, 0.f);
+          const float gy = fmaxf(fabsf(gb[u][1] - bc.y) - bh.y, 0.f);
+          const float gz = fmaxf(fabsf(gb[u][2] - bc.z) - bh.z, 0.f);
+          const bool nr = fmaf(gz, gz, fmaf(gy, gy, fmaf(gx, gx, -gb[u][3]))) <= 0.f;
+          const unsigned m = __ballot_sync(MRMG_FULL, nr);
+          if (nr) witem[nit + __popc(m & ltb)] = (uint32_t)(lane + 32 * u) | ((uint32_t)b << 16);
+          nit += __popc(m);
+        }
+      }
+      __syncwarp();
+      for (int base = 0; base < nit; base += 32) {
+        bool coll = false;
+        if (base + lane < nit) {
+          const uint32_t it = witem[base + lane];
+          const int g = it & 0xffff, b = it >> 16;
+          const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
+#pragma unroll
+          for (int v = 0; v < SPG; v++) {
+            const float4 c = wsph[g * SPG + v];
+            const float4 bd = t.band[g * SPG + v];
+            const float ex = fmaxf(fabsf(c.x - bc.x) - bh.x, 0.f);
+            const float ey = fmaxf(fabsf(c.y - bc.y) - bh.y, 0.f);
+            const float ez = fmaxf(fabsf(c.z - bc.z) - bh.z, 0.f);
+            const float ss = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+            if (ss <= bd.y) {
+              if (ss < bd.x) coll = true;
+              else if (RESOLVE) {
+                const int slot = g * SPG + v;
+                coll |= exact_box_hit(wc64 + (size_t)slot * 3, s.box64 + (size_t)b * 6, s.sph64[(size_t)slot * 5 + 4]);
+              } else {
+                unc = true;
+              }
+            }
+          }
+        }
+        if (__any_sync(MRMG_FULL, coll)) {
+          if (!full) return V_COLLIDE;
+          hit_any = true;
+        }
+      }
+      __syncwarp();   // the next block rewrites the list
     }
   }
 
@@ -863,7 +870,8 @@ __global__ void __launch_bounds__(256, RESOLVE ? 1 : (GPL == 1 ? 4 : (GPL == 2 ?
           sdf.rn = __frcp_rn(sdf.nm1);
           sdf.fi = (float)(int)iv;
           stat_cfg++;
-          const uint8_t code = eval_config<GPL, SPG, false>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
+          const uint8_t code = eval_config<GPL, SPG, false, BOX_HEAD_BLOCKS>(s, t, wcs, wqv, wsph, w64, lane, sdf,
+                                                                          full != 0);
           if (code == V_COLLIDE && !full) {
             r = V_COLLIDE;
           } else if (p + 1 < nmax) {
@@ -1012,7 +1020,7 @@ __global__ void __launch_bounds__(256, GPL == 1 ? 4 : (GPL == 2 ? 2 : 1)) arm_ed
       sdf.rn = __frcp_rn(sdf.nm1);
       sdf.fi = (float)(int)is;   // survivors have N <= 2^24
       stat_cfg++;
-      const uint8_t code = eval_config<GPL, SPG, false, true>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
+      const uint8_t code = eval_config<GPL, SPG, false, BOX_BLOCKS>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
       if (lane == 0) {
         if (code == V_COLLIDE) vsurv[ls].dead = 1;
         else if (code == V_PENDING) vsurv[ls].pend = 1;
