@@ -611,18 +611,39 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
     if (pi < nnear) {
       pr = wnear[pi];
       const int sa0 = (pr & 0xffff) * SPG, sb0 = (pr >> 16) * SPG;
-      float4 a[SPG];   // (-2 x, -2 y, -2 z, s)
+      // phase B: group a's spheres two at a time in packed FP32x2 registers
+      // (each packed FMA / add rounds its two elements exactly as the scalar
+      // instruction would, so the filter values are the scalar ones); the
+      // first positions keep scalar code, which fits their register budget
+      constexpr int P2 = BOXES == BOX_BLOCKS ? SPG / 2 : 0;
+      float2 ax[P2 > 0 ? P2 : 1], ay[P2 > 0 ? P2 : 1], az[P2 > 0 ? P2 : 1], aw[P2 > 0 ? P2 : 1];
 #pragma unroll
-      for (int v = 0; v < SPG; v++) {
+      for (int v = 0; v < P2; v++) {
+        const float4 c0 = wsph[sa0 + 2 * v], c1 = wsph[sa0 + 2 * v + 1];
+        ax[v] = make_float2(-2.f * c0.x, -2.f * c1.x);
+        ay[v] = make_float2(-2.f * c0.y, -2.f * c1.y);
+        az[v] = make_float2(-2.f * c0.z, -2.f * c1.z);
+        aw[v] = make_float2(wss[sa0 + 2 * v], wss[sa0 + 2 * v + 1]);
+      }
+      float4 a[SPG - 2 * P2 > 0 ? SPG - 2 * P2 : 1];   // the spheres not packed: (-2 x, -2 y, -2 z, s)
+#pragma unroll
+      for (int v = 2 * P2; v < SPG; v++) {
         const float4 c = wsph[sa0 + v];
-        a[v] = make_float4(-2.f * c.x, -2.f * c.y, -2.f * c.z, wss[sa0 + v]);
+        a[v - 2 * P2] = make_float4(-2.f * c.x, -2.f * c.y, -2.f * c.z, wss[sa0 + v]);
       }
 #pragma unroll
       for (int w = 0; w < SPG; w++) {
         const float4 bq = wsph[sb0 + w];
         const float sb = wss[sb0 + w];
+        const float2 bx = make_float2(bq.x, bq.x), by = make_float2(bq.y, bq.y), bz = make_float2(bq.z, bq.z);
+        const float2 sb2 = make_float2(sb, sb);
 #pragma unroll
-        for (int v = 0; v < SPG; v++)
+        for (int v = 0; v < P2; v++) {
+          const float2 f = __ffma2_rn(ax[v], bx, __ffma2_rn(ay[v], by, __ffma2_rn(az[v], bz, __fadd2_rn(aw[v], sb2))));
+          umin = fminf(umin, fminf(f.x, f.y));
+        }
+#pragma unroll
+        for (int v = 0; v < SPG - 2 * P2; v++)
           umin = fminf(umin, fmaf(a[v].x, bq.x, fmaf(a[v].y, bq.y, fmaf(a[v].z, bq.z, a[v].w + sb))));
       }
     }
