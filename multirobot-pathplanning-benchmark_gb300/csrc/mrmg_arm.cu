@@ -979,7 +979,7 @@ __device__ void finalize_survivors(int* ctr, const SurvivorEdge* surv, uint8_t* 
 
 // positions p_next + j, j in [j_lo, j_hi), of every survivor (j_hi < 0: to the end)
 template <int GPL, int SPG>
-__global__ void __launch_bounds__(256, GPL == 1 ? 4 : (GPL == 2 ? 2 : 1)) arm_edges_phase_b(ArmDev s, const void* q1, const void* q2, int dtype,
+__global__ void __launch_bounds__(256, GPL == 1 ? 3 : (GPL == 2 ? 2 : 1)) arm_edges_phase_b(ArmDev s, const void* q1, const void* q2, int dtype,
                                                          int incl, int* ctr, SurvivorEdge* surv, int full,
                                                          int j_lo, int j_hi, uint8_t* out, long long* pend) {
   // the last launch (j_hi < 0) also finalizes: its last CTA to finish sets the
@@ -1221,11 +1221,31 @@ cudaError_t launch_edges(const ArmDev& s, int gpl, const void* q1, const void* q
   return cudaErrorInvalidValue;
 }
 
+// resident CTAs per SM of the phase-B kernel (its register budget differs
+// from phase A's), cached per variant and shape
+template <int G_, int S_>
+int phase_b_occupancy(int warps, size_t smem) {
+  static int cached[9] = {0};
+  static size_t cached_smem[9] = {0};
+  if (warps < 1 || warps > 8) return 1;
+  if (cached[warps] == 0 || cached_smem[warps] != smem) {
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, arm_edges_phase_b<G_, S_>, warps * 32, smem) !=
+            cudaSuccess || blocks < 1)
+      blocks = 1;
+    cudaGetLastError();
+    cached[warps] = blocks;
+    cached_smem[warps] = smem;
+  }
+  return cached[warps];
+}
+
 cudaError_t launch_phase_b(const ArmDev& s, int gpl, const void* q1, const void* q2, int dtype, int incl,
                            const CallScratch& sc, int grid, int warps, size_t smem, int full, int j_lo, int j_hi,
-                           uint8_t* out, cudaStream_t st) {
+                           uint8_t* out, int num_sms, cudaStream_t st) {
 #define MRMG_ARM_PB(G_, S_)                                                                        \
   if (gpl == G_ && s.SPG == S_) {                                                                  \
+    grid = std::min(grid, num_sms * phase_b_occupancy<G_, S_>(warps, smem));                       \
     arm_edges_phase_b<G_, S_><<<grid, warps * 32, smem, st>>>(s, q1, q2, dtype, incl, sc.ctr, sc.surv, full, \
                                                               j_lo, j_hi, out, sc.pend);           \
     return cudaGetLastError();                                                                     \
@@ -1303,10 +1323,12 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
   if (e != cudaSuccess) return e;
   // B1: the next kPhaseB1 positions of every survivor (kills most colliding
   // survivors); B2: everything left, spread over all warps
-  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, 0, kPhaseB1, out, st);
+  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, 0, kPhaseB1, out, ls.num_sms,
+                     st);
   if (e != cudaSuccess) return e;
   // B2 finalizes the survivors' verdicts in its last CTA
-  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, kPhaseB1, -1, out, st);
+  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, kPhaseB1, -1, out, ls.num_sms,
+                     st);
   if (e != cudaSuccess) return e;
   const int w2 = 2;
   return launch_edges<true>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc, ls.num_sms,
