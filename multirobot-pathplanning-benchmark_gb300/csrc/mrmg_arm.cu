@@ -529,14 +529,39 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
           const uint32_t it = witem[base + lane];
           const int g = it & 0xffff, b = it >> 16;
           const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
+          // phase B: two spheres per packed FP32x2 instruction (each element
+          // rounds as the scalar instruction would: the same ss values)
+          constexpr int Q2 = BOXES == BOX_BLOCKS ? SPG / 2 : 0;
+          float ssp[2 * Q2 > 0 ? 2 * Q2 : 1];
+#pragma unroll
+          for (int v2 = 0; v2 < Q2; v2++) {
+            const float4 c0 = wsph[g * SPG + 2 * v2], c1 = wsph[g * SPG + 2 * v2 + 1];
+            const float2 dx = __fadd2_rn(make_float2(c0.x, c1.x), make_float2(-bc.x, -bc.x));
+            const float2 dy = __fadd2_rn(make_float2(c0.y, c1.y), make_float2(-bc.y, -bc.y));
+            const float2 dz = __fadd2_rn(make_float2(c0.z, c1.z), make_float2(-bc.z, -bc.z));
+            const float2 ox = __fadd2_rn(make_float2(fabsf(dx.x), fabsf(dx.y)), make_float2(-bh.x, -bh.x));
+            const float2 oy = __fadd2_rn(make_float2(fabsf(dy.x), fabsf(dy.y)), make_float2(-bh.y, -bh.y));
+            const float2 oz = __fadd2_rn(make_float2(fabsf(dz.x), fabsf(dz.y)), make_float2(-bh.z, -bh.z));
+            const float2 ex = make_float2(fmaxf(ox.x, 0.f), fmaxf(ox.y, 0.f));
+            const float2 ey = make_float2(fmaxf(oy.x, 0.f), fmaxf(oy.y, 0.f));
+            const float2 ez = make_float2(fmaxf(oz.x, 0.f), fmaxf(oz.y, 0.f));
+            const float2 s2 = __ffma2_rn(ez, ez, __ffma2_rn(ey, ey, __fmul2_rn(ex, ex)));
+            ssp[2 * v2] = s2.x;
+            ssp[2 * v2 + 1] = s2.y;
+          }
 #pragma unroll
           for (int v = 0; v < SPG; v++) {
             const float4 c = wsph[g * SPG + v];
             const float4 bd = t.band[g * SPG + v];
-            const float ex = fmaxf(fabsf(c.x - bc.x) - bh.x, 0.f);
-            const float ey = fmaxf(fabsf(c.y - bc.y) - bh.y, 0.f);
-            const float ez = fmaxf(fabsf(c.z - bc.z) - bh.z, 0.f);
-            const float ss = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+            float ss;
+            if (v < 2 * Q2) {
+              ss = ssp[v];
+            } else {
+              const float ex = fmaxf(fabsf(c.x - bc.x) - bh.x, 0.f);
+              const float ey = fmaxf(fabsf(c.y - bc.y) - bh.y, 0.f);
+              const float ez = fmaxf(fabsf(c.z - bc.z) - bh.z, 0.f);
+              ss = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+            }
             if (ss <= bd.y) {
               if (ss < bd.x) coll = true;
               else if (RESOLVE) {
