@@ -509,7 +509,36 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
     for (int b0 = b_each; b0 < s.B; b0 += bs, bs = (BOXES == BOX_BLOCKS && b0 <= 1) ? 1 : min(2 * bs, kBoxBlock)) {
       const int b1 = min(s.B, b0 + bs);
       int nit = 0;
-      for (int b = b0; b < b1; b++) {
+      int b = b0;
+      if constexpr (BOXES == BOX_BLOCKS) {
+        // phase B: two boxes per packed FP32x2 instruction (same values as
+        // the scalar test below)
+        for (; b + 1 < b1; b += 2) {
+          const float4 c0 = t.box[2 * b], h0 = t.box[2 * b + 1], c1 = t.box[2 * b + 2], h1 = t.box[2 * b + 3];
+#pragma unroll
+          for (int u = 0; u < GPL; u++) {
+            const float2 dx = __fadd2_rn(make_float2(gb[u][0], gb[u][0]), make_float2(-c0.x, -c1.x));
+            const float2 dy = __fadd2_rn(make_float2(gb[u][1], gb[u][1]), make_float2(-c0.y, -c1.y));
+            const float2 dz = __fadd2_rn(make_float2(gb[u][2], gb[u][2]), make_float2(-c0.z, -c1.z));
+            const float2 ox = __fadd2_rn(make_float2(fabsf(dx.x), fabsf(dx.y)), make_float2(-h0.x, -h1.x));
+            const float2 oy = __fadd2_rn(make_float2(fabsf(dy.x), fabsf(dy.y)), make_float2(-h0.y, -h1.y));
+            const float2 oz = __fadd2_rn(make_float2(fabsf(dz.x), fabsf(dz.y)), make_float2(-h0.z, -h1.z));
+            const float2 gx = make_float2(fmaxf(ox.x, 0.f), fmaxf(ox.y, 0.f));
+            const float2 gy = make_float2(fmaxf(oy.x, 0.f), fmaxf(oy.y, 0.f));
+            const float2 gz = make_float2(fmaxf(oz.x, 0.f), fmaxf(oz.y, 0.f));
+            const float nr2 = -gb[u][3];
+            const float2 q2 = __ffma2_rn(gz, gz, __ffma2_rn(gy, gy, __ffma2_rn(gx, gx, make_float2(nr2, nr2))));
+            const bool n0 = q2.x <= 0.f, n1 = q2.y <= 0.f;
+            const unsigned m0 = __ballot_sync(MRMG_FULL, n0);
+            if (n0) witem[nit + __popc(m0 & ltb)] = (uint32_t)(lane + 32 * u) | ((uint32_t)b << 16);
+            nit += __popc(m0);
+            const unsigned m1 = __ballot_sync(MRMG_FULL, n1);
+            if (n1) witem[nit + __popc(m1 & ltb)] = (uint32_t)(lane + 32 * u) | ((uint32_t)(b + 1) << 16);
+            nit += __popc(m1);
+          }
+        }
+      }
+      for (; b < b1; b++) {
         const float4 bc = t.box[2 * b], bh = t.box[2 * b + 1];
 #pragma unroll
         for (int u = 0; u < GPL; u++) {
