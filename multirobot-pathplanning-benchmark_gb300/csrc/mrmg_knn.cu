@@ -518,7 +518,7 @@ namespace mrmg {
 
 // node-store formats
 enum : int { KNN_FMT_EUCL = 0, KNN_FMT_AGENT = 1 };
-constexpr int kNtEucl = 256, kNtAgent = 64;
+constexpr int kNtEucl = 128, kNtAgent = 64;
 
 struct KnnItem {          // one CTA: a query tile of one mode against a chunk of its node tiles
   int mode, q0, qn;       // queries qorder[q0 .. q0+qn)
@@ -679,7 +679,7 @@ __device__ __forceinline__ void rad_chunk(const float (&v)[32], float qn, float 
   ro.bits[ro.woff[qid] + (col0 >> 5)] = m;
 }
 
-template <int FMT> struct TcSplit { static constexpr int S = FMT == KNN_FMT_EUCL ? 4 : 2; };
+template <int FMT> struct TcSplit { static constexpr int S = FMT == KNN_FMT_EUCL ? 1 : 2; };
 
 template <int FMT, bool RAD>
 __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnStoreDev st, const double* __restrict__ qs,
@@ -691,6 +691,10 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   constexpr uint32_t BT = NT * kRowBytes;   // bytes per node tile
   constexpr int S = TcSplit<FMT>::S, NCOL = NT / S;
   static_assert(NCOL % 32 == 0, "column slice is whole 32-column loads");
+  // tensor-memory columns: two accumulator buffers of one node tile each
+  // (euclidean: 2 x 128 = 256, so two CTAs share an SM's 512 columns;
+  // per-agent blocks: 2 x 4 x 64 = 512, one CTA per SM)
+  constexpr uint32_t kTm = FMT == KNN_FMT_EUCL ? 2 * NT : 512;
   extern __shared__ __align__(1024) unsigned char sm_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)sm_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sA1 = base;
@@ -715,7 +719,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
     s_fail = 0;
     fence_barrier_init();
   }
-  if (warp == 0) tmem_alloc(&tbase, 512);
+  if (warp == 0) tmem_alloc(&tbase, kTm);
 
   // ---- the query tile: A1 = [q_hi | -1/2 ... | q_hi], A2 = [q_lo]; one thread per row
   float qn = 0.f, qna[4] = {0.f, 0.f, 0.f, 0.f};
@@ -787,7 +791,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   };
   auto issue_mma = [&](int t) {
     const uint32_t a1 = su32(sA1), a2 = su32(sA2), b = su32(sB0 + (t & 1) * BT);
-    const uint32_t dcol = tm + (uint32_t)((t & 1) * 256);
+    const uint32_t dcol = tm + (uint32_t)((t & 1) * (kTm / 2));
     if (FMT == KNN_FMT_EUCL) {
       for (int s = 0; s < 4; s++) umma_bf16(dcol, sw128_desc(a1 + 32 * s), sw128_desc(b + 32 * s), idesc, s > 0);
       const int s2 = (D + 15) / 16;
@@ -824,7 +828,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
     if (tid == 0 && t + 2 < T && done) issue_load(t + 2);   // tile t's MMAs have read its buffer
     if (done) {
       const int col_node0 = (it.tile0 + t) * NT;
-      const uint32_t lane_base = tm + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((t & 1) * 256);
+      const uint32_t lane_base = tm + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((t & 1) * (kTm / 2));
       if (FMT == KNN_FMT_EUCL) {
 #pragma unroll 1
         for (int c0 = slice * NCOL; c0 < slice * NCOL + NCOL; c0 += 32) {
@@ -889,7 +893,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) tmem_dealloc(tm, 512);
+  if (warp == 0) tmem_dealloc(tm, kTm);
 }
 
 constexpr int kMergeWarps = 4;   // warps per merge CTA
@@ -1519,12 +1523,18 @@ static void plan_items(const KnnStore* s, const int* h_q_mode, long long Q, int 
   }
 }
 
+// Shared memory of a candidate CTA.  The euclidean kernel takes 256 tensor-
+// memory columns and about 81 KB, so two CTAs share an SM (a third does not
+// fit in shared memory, so no CTA waits for columns); the per-agent kernel
+// takes all 512 columns and is held to one CTA per SM by asking for at least
+// 120 KB, so two CTAs never wait on each other for the columns.
 static size_t tc_smem_bytes(const KnnStore* s) {
   const int NT = s->dev.NT;
-  const int nthreads = 128 * (s->dev.fmt == KNN_FMT_EUCL ? TcSplit<KNN_FMT_EUCL>::S : TcSplit<KNN_FMT_AGENT>::S);
-  return std::max<size_t>(1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes +
-                              32 * sizeof(float) * (size_t)nthreads,
-                          120 * 1024);
+  const bool eucl = s->dev.fmt == KNN_FMT_EUCL;
+  const int nthreads = 128 * (eucl ? TcSplit<KNN_FMT_EUCL>::S : TcSplit<KNN_FMT_AGENT>::S);
+  const size_t need = 1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes +
+                      32 * sizeof(float) * (size_t)nthreads;
+  return eucl ? need : std::max<size_t>(need, 120 * 1024);
 }
 
 // the attribute is per function: raise it once, to the opt-in limit less the
@@ -1606,8 +1616,6 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   cudaError_t e = cudaMemcpyAsync(d_order, hp, b_up, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, 256, st);
   if (e != cudaSuccess) return e;
-  // at least 120 KB of shared memory: one CTA per SM, so two CTAs never wait
-  // on each other for the 512 tensor-memory columns each allocates
   const size_t smem = tc_smem_bytes(s);
   raise_smem_limit<KNN_FMT_EUCL, false>();
   raise_smem_limit<KNN_FMT_AGENT, false>();

@@ -118,3 +118,35 @@ def test_mode_penetration_cost(gpu):
         assert np.all(np.abs(c - ref) <= 1e-5 * np.abs(ref)), m
         costs[m] = c
     assert not np.allclose(costs[1], costs[7])
+
+
+def test_mode_edge_cases(gpu, oracle):
+    """A mode with no boxes and no attached objects (only robot-robot
+    contacts remain), a mode with every object held, and the argument
+    checks: repeated or out-of-range boxes and a second set of modes are
+    refused."""
+    import copy
+
+    scenes, col = pkg("scenes"), pkg("collision")
+    base = scenes.make_arm_mode_scene(2, n_objects=4, n_modes=3)
+    scene = copy.deepcopy(base)
+    scene.mode_boxes = [[], list(range(len(scene.box_lo))), [0, 3]]
+    scene.mode_attach = [[], [0, 1, 2, 3], [2]]
+    sc = col.Gb300Scene(scene)
+    q = scenes.uniform_configs(scene, 3000, seed=4, dtype=np.float32)
+    for m in range(3):
+        sc.set_mode(m)
+        o = oracle.OracleScene(scene.for_mode(m))
+        assert np.array_equal(sc.is_collision_free_batch(q).cpu().numpy(), o.configs_free(q)), m
+    sc.set_mode(0)
+    assert sc.is_collision_free_batch(q).cpu().numpy().mean() > 0.5   # no boxes: most configurations free
+    for boxes in ([[0, 0]], [[len(scene.box_lo)]]):
+        bad = copy.deepcopy(base)
+        bad.mode_boxes, bad.mode_attach = boxes, [[]]
+        with pytest.raises(ValueError):
+            col.Gb300Scene(bad)
+    t = scene.mode_tables()
+    with pytest.raises(ValueError):
+        pkg("_lib").check(sc.lib.mrmg_arm_scene_set_modes(
+            sc.h, scene.n_modes, t["sphere_attach"].ctypes.data, t["box_off"].ctypes.data, t["boxes"].ctypes.data,
+            t["attach_off"].ctypes.data, t["attach"].ctypes.data))
