@@ -1,0 +1,134 @@
+"""CPU checks of the MJCF planar-scene importer: the parsed geometry and
+limits, exactness of the cylinder-to-sphere mapping against a direct 2-D
+restatement of the planar problem (disc against rectangle, disc against
+disc), the conservative cover of box robots (never free where the rotated
+box touches an obstacle), and the refused forms."""
+import numpy as np
+import pytest
+
+from conftest import pkg
+
+SCENE = """
+<mujoco>
+  <worldbody>
+    <geom name="floor" type="plane" size="0 0 0.05" pos="0 0 -0.05"/>
+    <body name="walls" pos="0 0 0.1">
+      <geom type="box" pos="0 1.8 0" size="1.7 0.1 0.1"/>
+      <geom type="box" pos="0 -1.8 0" size="1.7 0.1 0.1"/>
+      <geom type="box" pos="1.8 0 0" size="0.1 1.7 0.1"/>
+      <geom type="box" pos="-1.8 0 0" size="0.1 1.7 0.1"/>
+      <geom type="box" pos="0.3 -0.2 0" size="0.4 0.3 0.1"/>
+    </body>
+    <body name="r_disc" pos="0 0 0.1">
+      <joint name="d_x" type="slide" axis="1 0 0" range="-1.6 1.6"/>
+      <joint name="d_y" type="slide" axis="0 1 0" range="-1.6 1.6"/>
+      <joint name="d_t" type="hinge" axis="0 0 1" range="-180 180"/>
+      <geom type="cylinder" size="0.12 0.05"/>
+    </body>
+    <body name="r_bar" pos="0 0 0.1">
+      <joint name="b_x" type="slide" axis="1 0 0" range="-1.6 1.6"/>
+      <joint name="b_y" type="slide" axis="0 1 0" range="-1.6 1.6"/>
+      <joint name="b_t" type="hinge" axis="0 0 1" range="-90 90"/>
+      <geom type="box" size="0.06 0.3 0.1"/>
+    </body>
+    <body name="crate" pos="-0.9 0.9 0.1">
+      <freejoint/>
+      <geom type="box" size="0.15 0.15 0.1"/>
+    </body>
+  </worldbody>
+</mujoco>
+"""
+
+
+def _load(text=SCENE, robots=None):
+    return pkg("importers").load_mjcf_planar(text, robots)
+
+
+def test_mjcf_geometry_and_limits():
+    sc = _load()
+    assert sc.n_robots == 2 and sc.q_dim == 6
+    assert len(sc.box_lo) == 6 and sc.movable_boxes == {"crate": [5]}
+    np.testing.assert_allclose(sc.box_lo[4], [-0.1, -0.5, 0.0])
+    np.testing.assert_allclose(sc.box_hi[5], [-0.75, 1.05, 0.2])
+    np.testing.assert_allclose(sc.limits[:, 2], [-np.pi, np.pi])          # degrees -> radians
+    np.testing.assert_allclose(sc.limits[:, 5], [-np.pi / 2, np.pi / 2])
+    r0 = sc.sphere_radius[sc.sphere_robot == 0]
+    r1 = sc.sphere_radius[sc.sphere_robot == 1]
+    assert r0.tolist() == [0.12]
+    assert np.allclose(r1, np.sqrt(2) * 0.06) and len(r1) == 5
+    loc = sc.sphere_local[sc.sphere_robot == 1]
+    assert np.all(loc[:, 0] == 0) and np.isclose(loc[:, 1].min(), -0.24) and np.isclose(loc[:, 1].max(), 0.24)
+    assert np.diff(np.sort(loc[:, 1])).max() <= 2 * 0.06 + 1e-12   # a cover: centres at most 2 w apart
+    assert _load(robots=["r_bar"]).n_robots == 1
+
+
+def _rect_dist2(p, lo, hi):
+    c = np.clip(p, lo, hi)
+    return ((c - p) ** 2).sum(-1)
+
+
+def test_cylinder_robots_are_exact(oracle):
+    """Two cylinder robots: the oracle's verdicts on the imported scene equal
+    the planar problem written directly (discs among rectangles)."""
+    text = SCENE.replace('<geom type="box" size="0.06 0.3 0.1"/>', '<geom type="cylinder" size="0.2 0.05"/>')
+    sc = _load(text)
+    o = oracle.OracleScene(sc)
+    rng = np.random.default_rng(0)
+    q = rng.uniform(sc.limits[0], sc.limits[1], (4000, 6))
+    got = o.configs_free(q).astype(bool)
+    lo, hi = sc.box_lo[:, :2], sc.box_hi[:, :2]
+    want = np.ones(len(q), dtype=bool)
+    for k, (off, r) in enumerate([(0, 0.12), (3, 0.2)]):
+        d2 = _rect_dist2(q[:, None, off:off + 2], lo[None], hi[None])
+        want &= ~(d2 <= r * r).any(1)
+    want &= ~(np.sqrt(((q[:, 0:2] - q[:, 3:5]) ** 2).sum(1)) < 0.32)
+    assert np.array_equal(got, want)
+    assert 0.1 < want.mean() < 0.9
+
+
+def _box_touches_rect(c, th, half, lo, hi):
+    """Separating-axis test of a rotated rectangle against axis-aligned ones."""
+    u = np.array([np.cos(th), np.sin(th)])
+    v = np.array([-np.sin(th), np.cos(th)])
+    corners = [c + sx * half[0] * u + sy * half[1] * v for sx in (-1, 1) for sy in (-1, 1)]
+    P = np.array(corners)
+    for l, h in zip(lo, hi):
+        Q = np.array([[l[0], l[1]], [h[0], l[1]], [h[0], h[1]], [l[0], h[1]]])
+        sep = False
+        for ax in (np.array([1.0, 0.0]), np.array([0.0, 1.0]), u, v):
+            a, b = P @ ax, Q @ ax
+            if a.max() < b.min() or b.max() < a.min():
+                sep = True
+                break
+        if not sep:
+            return True
+    return False
+
+
+def test_box_robot_cover_is_conservative(oracle):
+    """A configuration the covered model calls free never has the bar robot's
+    true rectangle touching an obstacle."""
+    sc = _load()
+    keep = sc.sphere_robot == 1
+    sc1 = pkg("importers").load_mjcf_planar(SCENE, ["r_bar"])
+    o = oracle.OracleScene(sc1)
+    rng = np.random.default_rng(1)
+    q = rng.uniform(sc1.limits[0], sc1.limits[1], (1500, 3))
+    free = o.configs_free(q).astype(bool)
+    lo, hi = sc1.box_lo[:, :2], sc1.box_hi[:, :2]
+    for i in np.nonzero(free)[0]:
+        assert not _box_touches_rect(q[i, :2], q[i, 2], (0.06, 0.3), lo, hi), i
+    assert keep.sum() == 5 and 0.05 < free.mean() < 0.95
+
+
+@pytest.mark.parametrize("bad, err", [
+    ('<geom type="box" pos="0.3 -0.2 0" size="0.4 0.3 0.1"/>',
+     '<geom type="box" pos="0.3 -0.2 0" size="0.4 0.3 0.1" euler="0 0 30"/>'),
+    ('<geom type="cylinder" size="0.12 0.05"/>', '<geom type="mesh" mesh="m"/>'),
+    ('<body name="r_disc" pos="0 0 0.1">', '<body name="r_disc" pos="0.5 0 0.1">'),
+    ('<joint name="d_t" type="hinge" axis="0 0 1" range="-180 180"/>',
+     '<joint name="d_t" type="hinge" axis="0 1 0" range="-180 180"/>'),
+])
+def test_refused_forms(bad, err):
+    with pytest.raises(NotImplementedError):
+        _load(SCENE.replace(bad, err))
