@@ -64,6 +64,7 @@ constexpr int kNearBlock = 512;   // at most this many group pairs compacted per
 __host__ __device__ inline int near_block(const ArmDev& s) { return s.NP < kNearBlock ? (s.NP > 0 ? s.NP : 1) : kNearBlock; }
 
 constexpr int kBoxBlock = 8;   // boxes whose near (group, box) items are compacted together
+constexpr int kBoxHead = 8;    // first positions: boxes tested one by one before the blocks
 
 // the per-warp list holds the near (group, box) items of one box block, then
 // the near group pairs of one pair block
@@ -440,7 +441,7 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
   __syncwarp();
 
   bool unc = false;
-  const int b_each = BOXES == BOX_EACH ? s.B : (BOXES == BOX_HEAD_BLOCKS ? min(s.B, kBoxBlock) : 0);
+  const int b_each = BOXES == BOX_EACH ? s.B : (BOXES == BOX_HEAD_BLOCKS ? min(s.B, kBoxHead) : 0);
   {
     // --- spheres against boxes, box by box: all of them, or the head
     for (int b = 0; b < b_each; b++) {
