@@ -299,6 +299,263 @@ __global__ void knn_split_merge_kernel(const long long* __restrict__ qmap, long 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Node-parallel k-NN with an FP32 candidate pass (euclidean, max over
+// agents): per (query, 256-node chunk) item the k smallest FP32 squared
+// distances of the FP32 node copy (direct coordinate differences; per agent,
+// then the maximum), the item's (k+1)-th smallest value (the first node left
+// out) and the band 7.7e-6 (|q| + max |x|)^2 that bounds the FP32 values'
+// error (the radius pre-test's bound).  The merge re-ranks in FP64 only the
+// candidates within tau = (k-th FP32 value + 2 band)(1 + 2^-20) and
+// certifies that every left-out node lies above tau (then its FP64 distance
+// exceeds the k-th); a query that fails is rerun on the FP64 kernels.
+// ---------------------------------------------------------------------------
+constexpr int kSplitWarps = 4;
+
+template <int KM>
+__global__ void knn_split32_kernel(const double* __restrict__ qs, const long long* __restrict__ qmap, long long Q,
+                                   const int* __restrict__ q_mode, const long long* __restrict__ ioff,
+                                   const float* __restrict__ nodes32, const long long* __restrict__ mode_beg,
+                                   const long long* __restrict__ mode_end, SliceTab t, int metric, int k,
+                                   float* __restrict__ cand_key, int* __restrict__ cand_idx,
+                                   float* __restrict__ item_next, float* __restrict__ item_band) {
+  __shared__ float s_q[kSplitWarps][64];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long warp = (long long)blockIdx.x * kSplitWarps + wib;
+  const long long nwarps = (long long)gridDim.x * kSplitWarps;
+  const long long n_items = ioff[Q];
+  const float INF = __int_as_float(0x7f800000);
+  float* q32 = s_q[wib];
+  long long cur = -1;
+  float qn = 0.f;
+  for (long long it = warp; it < n_items; it += nwarps) {
+    const long long l = owner_of(ioff, Q, it);
+    const long long q = qmap ? qmap[l] : l;
+    if (q != cur) {   // the query in FP32 (and |q|^2), once per query in this warp
+      __syncwarp();
+      for (int j = lane; j < t.D; j += 32) q32[j] = (float)qs[q * t.D + j];
+      __syncwarp();
+      float a = 0.f;
+      for (int j = 0; j < t.D; j++) a = fmaf(q32[j], q32[j], a);
+      qn = a;
+      cur = q;
+    }
+    const int m = q_mode[l];
+    const long long b = mode_beg[m];
+    const long long s = b + (it - ioff[l]) * kSplitNodes;
+    const long long e = s + kSplitNodes < mode_end[m] ? s + kSplitNodes : mode_end[m];
+    float td[KM];
+    int ti[KM];
+#pragma unroll
+    for (int i = 0; i < KM; i++) { td[i] = INF; ti[i] = 0x7fffffff; }
+    float xmax = 0.f;
+    for (long long x = s + lane; x < e; x += 32) {
+      const float* xx = nodes32 + x * t.D;
+      float v = 0.f, xn = 0.f;
+      if (metric == MRMG_METRIC_EUCLIDEAN) {
+        for (int j = 0; j < t.end_all; j++) {
+          const float d = q32[j] - xx[j];
+          v = fmaf(d, d, v);
+          xn = fmaf(xx[j], xx[j], xn);
+        }
+      } else {
+        for (int a = 0; a < t.A; a++) {
+          float sa = 0.f;
+          for (int j = t.s[a]; j < t.e[a]; j++) {
+            const float d = q32[j] - xx[j];
+            sa = fmaf(d, d, sa);
+            xn = fmaf(xx[j], xx[j], xn);
+          }
+          v = fmaxf(v, sa);
+        }
+      }
+      xmax = fmaxf(xmax, xn);
+      if (v != v) v = INF;   // NaN coordinates: never a candidate here, the FP64 check decides
+      const int id = (int)(x - b);
+      if (v < td[KM - 1]) {   // nodes arrive in index order: equal values keep the lower index first
+#pragma unroll
+        for (int i = KM - 1; i > 0; i--) {
+          if (v < td[i - 1]) { td[i] = td[i - 1]; ti[i] = ti[i - 1]; }
+          else if (v < td[i]) { td[i] = v; ti[i] = id; }
+        }
+        if (v < td[0]) { td[0] = v; ti[0] = id; }
+      }
+    }
+    // the item's k smallest (value, index), then the (k+1)-th value
+    int head = 0;
+    for (int r = 0; r <= k; r++) {
+      float hv = INF;
+      int hi = 0x7fffffff;
+#pragma unroll
+      for (int i = 0; i < KM; i++)
+        if (i == head) { hv = td[i]; hi = ti[i]; }
+      float bv = hv;
+      int bi = hi, bl = lane;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        const float ov = __shfl_xor_sync(MRMG_FULL, bv, o);
+        const int oi = __shfl_xor_sync(MRMG_FULL, bi, o);
+        const int ol = __shfl_xor_sync(MRMG_FULL, bl, o);
+        if (ov < bv || (ov == bv && (oi < bi || (oi == bi && ol < bl)))) { bv = ov; bi = oi; bl = ol; }
+      }
+      if (r < k) {
+        if (lane == 0) {
+          cand_key[it * k + r] = bv;
+          cand_idx[it * k + r] = bv == INF ? -1 : bi;
+        }
+        if (lane == bl) head++;
+      } else if (lane == 0) {
+        item_next[it] = bv;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) xmax = fmaxf(xmax, __shfl_xor_sync(MRMG_FULL, xmax, o));
+    if (lane == 0) {
+      const float ee = sqrtf(qn) + sqrtf(xmax);
+      item_band[it] = 7.7e-6f * ee * ee;
+    }
+  }
+}
+
+// merge of the FP32 candidates: warp per query
+constexpr int kSplitGather = 512;   // candidates within tau re-ranked per query (more: rerun)
+
+template <int KM>
+__global__ void knn_split32_merge_kernel(const double* __restrict__ qs, const long long* __restrict__ qmap,
+                                         long long Q, const int* __restrict__ q_mode,
+                                         const long long* __restrict__ ioff, const double* __restrict__ nodes,
+                                         const long long* __restrict__ mode_beg,
+                                         const long long* __restrict__ mode_end, SliceTab t, int metric, int k,
+                                         const float* __restrict__ cand_key, const int* __restrict__ cand_idx,
+                                         const float* __restrict__ item_next, const float* __restrict__ item_band,
+                                         long long* __restrict__ out_idx, double* __restrict__ out_dist,
+                                         long long* __restrict__ fallback, int* __restrict__ n_fallback) {
+  __shared__ int s_id[kSplitWarps][kSplitGather];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long warp = (long long)blockIdx.x * kSplitWarps + wib;
+  const long long nwarps = (long long)gridDim.x * kSplitWarps;
+  const float INF = __int_as_float(0x7f800000);
+  int* sid = s_id[wib];
+  for (long long l = warp; l < Q; l += nwarps) {
+    const long long q = qmap ? qmap[l] : l;
+    const int m = q_mode[l];
+    const long long M = mode_end[m] - mode_beg[m];
+    const long long i0 = ioff[l], i1 = ioff[l + 1];
+    // the k-th smallest FP32 value over the items' sorted lists, and the band
+    float band = 0.f;
+    for (long long it = i0 + lane; it < i1; it += 32) band = fmaxf(band, item_band[it]);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) band = fmaxf(band, __shfl_xor_sync(MRMG_FULL, band, o));
+    float kth = INF;
+    {
+      // lane l owns items l, l + 32, ..., (up to 16 each: 512 items, modes
+      // of up to 131,072 nodes; larger ones rerun) with a head position per item
+      int heads[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++) heads[j] = 0;
+      const long long n_it = i1 - i0;
+      bool ok = n_it <= 512;
+      if (__any_sync(MRMG_FULL, !ok)) {
+        if (lane == 0) { const int slot = atomicAdd(n_fallback, 1); fallback[slot] = l; }
+        continue;
+      }
+      for (int r = 0; r < k; r++) {
+        float bv = INF;
+        int bj = -1;
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const long long it = i0 + lane + 32 * j;
+          if (it < i1 && heads[j] < k) {
+            const float v = cand_key[it * k + heads[j]];
+            if (v < bv) { bv = v; bj = j; }
+          }
+        }
+        float wv = bv;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) wv = fminf(wv, __shfl_xor_sync(MRMG_FULL, wv, o));
+        kth = wv;
+        if (wv == INF) break;
+        const unsigned who = __ballot_sync(MRMG_FULL, bv == wv);
+        if (lane == __ffs(who) - 1) {
+#pragma unroll
+          for (int j = 0; j < 16; j++)
+            if (j == bj) heads[j]++;
+        }
+      }
+    }
+    const float tau = kth == INF ? INF : (kth + 2.f * band) * (1.f + 9.5367431640625e-7f);
+    // certificate: every left-out node of every item lies above tau (with
+    // fewer than k finite values: every node of the mode is a candidate)
+    bool unsafe = false;
+    if (kth != INF)
+      for (long long it = i0 + lane; it < i1; it += 32) unsafe |= !(item_next[it] > tau);
+    // gather the finite candidates within tau, in item order
+    int mine = 0;
+    for (long long it = i0 + lane; it < i1; it += 32)
+      for (int r = 0; r < k && cand_key[it * k + r] <= tau && cand_key[it * k + r] < INF; r++) mine++;
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(MRMG_FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int ncand = __shfl_sync(MRMG_FULL, incl, 31);
+    unsafe |= ncand > kSplitGather || (kth == INF && ncand != M);
+    if (__any_sync(MRMG_FULL, unsafe)) {
+      if (lane == 0) { const int slot = atomicAdd(n_fallback, 1); fallback[slot] = l; }
+      continue;
+    }
+    int w = incl - mine;
+    for (long long it = i0 + lane; it < i1; it += 32)
+      for (int r = 0; r < k && cand_key[it * k + r] <= tau && cand_key[it * k + r] < INF; r++)
+        sid[w++] = cand_idx[it * k + r];
+    __syncwarp();
+    // FP64 re-rank, one candidate per lane; (distance, index) order
+    long long td[KM];
+    long long ti[KM];
+#pragma unroll
+    for (int i = 0; i < KM; i++) { td[i] = 0x7ff0000000000000ll; ti[i] = 0x7fffffffffffffffll; }
+    const double* qq = qs + q * t.D;
+    const double* xb = nodes + mode_beg[m] * t.D;
+    for (int x = lane; x < ncand; x += 32) {
+      const long long id = sid[x];
+      const double* xx = xb + id * t.D;
+      auto dfun = [&](int jj) { return __dsub_rn(qq[jj], xx[jj]); };
+      const long long d = dkey(dist_of(t, metric, dfun));
+      if (d < td[k - 1] || (d == td[k - 1] && id < ti[k - 1])) {
+#pragma unroll
+        for (int i = KM - 1; i > 0; i--) {
+          if (i < k) {
+            const bool before = d < td[i - 1] || (d == td[i - 1] && id < ti[i - 1]);
+            const bool here = d < td[i] || (d == td[i] && id < ti[i]);
+            if (before) { td[i] = td[i - 1]; ti[i] = ti[i - 1]; }
+            else if (here) { td[i] = d; ti[i] = id; }
+          }
+        }
+        if (d < td[0] || (d == td[0] && id < ti[0])) { td[0] = d; ti[0] = id; }
+      }
+    }
+    int head = 0;
+    for (int r = 0; r < k; r++) {
+      long long hd = 0x7ff0000000000000ll;
+      long long hi = 0x7fffffffffffffffll;
+#pragma unroll
+      for (int i = 0; i < KM; i++)
+        if (i == head) { hd = td[i]; hi = ti[i]; }
+      const int win = warp_argmin(hd, hi);
+      const long long wd = __shfl_sync(MRMG_FULL, hd, win);
+      const long long wi = __shfl_sync(MRMG_FULL, hi, win);
+      if (lane == 0) {
+        out_idx[q * k + r] = wi == 0x7fffffffffffffffll ? -1 : wi;
+        out_dist[q * k + r] = wi == 0x7fffffffffffffffll ? __longlong_as_double(0x7ff0000000000000ll)
+                                                         : __longlong_as_double(wd);
+      }
+      if (lane == win) head++;
+    }
+    __syncwarp();
+  }
+}
+
 // radius, exact: warp per (query, bitmap word), lane = node of the word
 __global__ void near_split_kernel(const double* __restrict__ qs, const float* __restrict__ qs32, long long Q,
                                   const int* __restrict__ q_mode, const double* __restrict__ nodes,
@@ -1737,6 +1994,77 @@ static cudaError_t knn_split_query(KnnStore* s, KnnScratch* scr, const double* d
   return e;
 }
 
+// node-parallel k nearest with the FP32 candidate pass (euclidean and max
+// over agents, k <= 31): candidates, certified FP64 re-rank, and the FP64
+// kernels for the queries whose certificate fails
+static cudaError_t knn_split32_query(KnnStore* s, KnnScratch* scr, const double* d_qs, long long Q,
+                                     const int* h_q_mode, int k, long long* d_idx, double* d_dist, int num_sms,
+                                     int* n_fallback, cudaStream_t st) {
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b_qm = al(sizeof(int) * std::max<long long>(Q, 1)), b_off = al(sizeof(long long) * (Q + 1));
+  const size_t b_up = b_qm + b_off;
+  cudaError_t e = scratch_reserve(scr, 0, b_up + 256);
+  if (e != cudaSuccess) return e;
+  unsigned char* hp = (unsigned char*)scr->host;
+  std::memcpy(hp, h_q_mode, sizeof(int) * Q);
+  long long* ioff = (long long*)(hp + b_qm);
+  ioff[0] = 0;
+  for (long long q = 0; q < Q; q++) ioff[q + 1] = ioff[q] + (s->cnt[h_q_mode[q]] + kSplitNodes - 1) / kSplitNodes;
+  const long long n_items = ioff[Q];
+  const size_t b_ck = al(sizeof(float) * std::max<long long>(n_items, 1) * k);
+  const size_t b_it = al(sizeof(float) * std::max<long long>(n_items, 1));
+  const size_t b_fb = al(sizeof(long long) * std::max<long long>(Q, 1));
+  e = scratch_reserve(scr, b_up + 2 * b_ck + 2 * b_it + b_fb + 256, 0);
+  if (e != cudaSuccess) return e;
+  unsigned char* p = (unsigned char*)scr->block;
+  const int* d_qm = (const int*)p;
+  const long long* d_ioff = (const long long*)(p + b_qm);
+  float* d_ck = (float*)(p + b_up);
+  int* d_ci = (int*)(p + b_up + b_ck);
+  float* d_next = (float*)(p + b_up + 2 * b_ck);
+  float* d_band = (float*)(p + b_up + 2 * b_ck + b_it);
+  long long* d_fb = (long long*)(p + b_up + 2 * b_ck + 2 * b_it);
+  int* d_ctr = (int*)(p + b_up + 2 * b_ck + 2 * b_it + b_fb);
+  int* h_ctr = (int*)(hp + b_up);
+  e = cudaMemcpyAsync(p, hp, b_up, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const int grid = (int)std::max<long long>(1, std::min<long long>((n_items + kSplitWarps - 1) / kSplitWarps,
+                                                                    (long long)num_sms * 16));
+  const int mgrid = (int)std::max<long long>(1, std::min<long long>((Q + kSplitWarps - 1) / kSplitWarps,
+                                                                     (long long)num_sms * 16));
+  if (k <= 15) {
+    if (n_items > 0)
+      knn_split32_kernel<16><<<grid, 32 * kSplitWarps, 0, st>>>(d_qs, nullptr, Q, d_qm, d_ioff, s->nodes32, s->d_beg,
+                                                                s->d_end, s->slices, s->metric, k, d_ck, d_ci, d_next,
+                                                                d_band);
+    knn_split32_merge_kernel<16><<<mgrid, 32 * kSplitWarps, 0, st>>>(d_qs, nullptr, Q, d_qm, d_ioff, s->nodes, s->d_beg,
+                                                                     s->d_end, s->slices, s->metric, k, d_ck, d_ci,
+                                                                     d_next, d_band, d_idx, d_dist, d_fb, d_ctr);
+  } else {
+    if (n_items > 0)
+      knn_split32_kernel<32><<<grid, 32 * kSplitWarps, 0, st>>>(d_qs, nullptr, Q, d_qm, d_ioff, s->nodes32, s->d_beg,
+                                                                s->d_end, s->slices, s->metric, k, d_ck, d_ci, d_next,
+                                                                d_band);
+    knn_split32_merge_kernel<32><<<mgrid, 32 * kSplitWarps, 0, st>>>(d_qs, nullptr, Q, d_qm, d_ioff, s->nodes, s->d_beg,
+                                                                     s->d_end, s->slices, s->metric, k, d_ck, d_ci,
+                                                                     d_next, d_band, d_idx, d_dist, d_fb, d_ctr);
+  }
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_ctr, d_ctr, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  *n_fallback = h_ctr[0];
+  if (h_ctr[0] > 0) {   // uncertified: the FP64 kernels (the list leaves the scratch first)
+    std::vector<long long> fb(h_ctr[0]);
+    e = cudaMemcpyAsync(fb.data(), d_fb, sizeof(long long) * fb.size(), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess)
+      e = knn_split_query(s, scr, d_qs, Q, h_q_mode, k, d_idx, d_dist, num_sms, st, fb.data(), (long long)fb.size());
+  }
+  return e;
+}
+
 // k nearest on the store: the node-parallel exact path for small batches,
 // the tensor-core path for its formats and k <= 16, else the exact
 // warp-per-query kernel
@@ -1746,8 +2074,12 @@ cudaError_t knn_store_query(KnnStore* s, KnnScratch* scr, const double* d_qs, lo
   *used_tc = 0;
   *n_fallback = 0;
   const bool small = batch_work(s, h_q_mode, Q) <= kSmallWork;
-  if (small || (!(s->tc && k <= 16) && Q < 2048))
+  if (small || (!(s->tc && k <= 16) && Q < 2048)) {
+    // (the candidate kernel stages the query in 64 floats of shared memory)
+    if ((s->metric == MRMG_METRIC_EUCLIDEAN || s->metric == MRMG_METRIC_MAX_EUCLIDEAN) && k <= 31 && s->D <= 64)
+      return knn_split32_query(s, scr, d_qs, Q, h_q_mode, k, d_idx, d_dist, num_sms, n_fallback, st);
     return knn_split_query(s, scr, d_qs, Q, h_q_mode, k, d_idx, d_dist, num_sms, st);
+  }
   if (s->tc && k <= 16) {
     *used_tc = 1;
     cudaError_t e = knn_query(s, d_qs, Q, h_q_mode, k, d_idx, d_dist, scr, num_sms, n_fallback, st);

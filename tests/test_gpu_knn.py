@@ -259,10 +259,12 @@ def test_node_store_grow_from_empty(gpu, oracle):
     assert store.size(0) + store.size(1) == 300
 
 
-def test_knn_uncertified_queries_rerun(gpu, oracle):
+@pytest.mark.parametrize("path", ["tensor_core", "exact"])
+def test_knn_uncertified_queries_rerun(gpu, oracle, path):
     """Nodes repeated many times fill the kept candidate lists with ties, so
-    the certificate fails and those queries are answered by the node-parallel
-    exact kernels; the result is still the oracle's (ties to the lower index)."""
+    the certificate (of the tensor-core path, or of the node-parallel FP32
+    candidate pass) fails and those queries are answered by the node-parallel
+    FP64 kernels; the result is still the oracle's (ties to the lower index)."""
     knn = pkg("knn")
     rng = np.random.default_rng(13)
     base = rng.uniform(-1, 1, (40, 28))
@@ -271,7 +273,7 @@ def test_knn_uncertified_queries_rerun(gpu, oracle):
     qs = np.concatenate([base[:20] + 1e-3, rng.uniform(-1, 1, (200, 28))])
     qm = np.concatenate([np.zeros(20, np.int32), rng.integers(0, 2, 200).astype(np.int32)])
     sl = [[0, 7], [7, 14], [14, 21], [21, 28]]
-    store = knn.NodeStore(nodes, off, sl, "euclidean", path="tensor_core")
+    store = knn.NodeStore(nodes, off, sl, "euclidean", path=path)
     for k in (10, 16):
         idx, dist = store.knn(qs, qm, k)
         oi, od = oracle.knn(qs, qm, nodes, off, sl, "euclidean", k)
