@@ -345,11 +345,13 @@ int mrmg_node_store_append(mrmg_node_store *store, int32_t mode, const double *r
 int mrmg_node_store_remove(mrmg_node_store *store, int32_t mode, int64_t idx, void *stream);
 
 /* Query path of the store (all give identical results): 0 = automatic (the
- * node-parallel exact path for batches of less than about 4M node-row x
- * coordinate FP64 work, else the tensor-core path where the metric and shape
+ * node-parallel path for batches of less than about 4M node-row x
+ * coordinate work, else the tensor-core path where the metric and shape
  * allow it), 1 = the tensor-core path wherever it applies, 2 = the
- * node-parallel exact path (FP64 distance of every node; work items are
- * (query, 256-node chunk) pairs). */
+ * node-parallel path (work items are (query, 256-node chunk) pairs; for
+ * euclidean and max_euclidean with k <= 31 an FP32 candidate pass on the
+ * store's FP32 node copy, certified and re-ranked in FP64, else the FP64
+ * distance of every node). */
 int mrmg_node_store_set_path(mrmg_node_store *store, int32_t path);
 
 /* out3: [0] number of modes, [1] nodes in `mode`, [2] tensor-core path. */

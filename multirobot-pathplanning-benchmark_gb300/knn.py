@@ -77,7 +77,8 @@ class NodeStore:
 
     def set_path(self, path: str):
         """'auto', 'tensor_core' (wherever the metric allows) or 'exact'
-        (node-parallel FP64); the results are identical."""
+        (node-parallel: certified FP32 candidates re-ranked in FP64, or FP64
+        throughout); the results are identical."""
         _lib.check(self.lib.mrmg_node_store_set_path(self.h, self.PATHS[path]), "set_path")
         self.path = path
 
