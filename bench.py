@@ -686,7 +686,8 @@ def bench_prm_lazy(n_nodes: int = 3000, k: int = 10, window: int = 256) -> dict:
     device call per popped edge (the reference's call pattern) against
     speculative batches of up to 256 upcoming edges.  Edge costs and the
     heuristic (cost to the goal) are precomputed in one batched call each, so
-    the timings isolate the edge checks; both searches give the same path."""
+    the timings isolate the edge checks; both searches give the same path.
+    Each timing is the best of three runs."""
     lazy, scenes, envm, knn = pkg("lazy"), pkg("scenes"), pkg("env"), pkg("knn")
     scene = scenes.make_arm_scene(1, n_boxes=5)
     env = envm.Gb300ArmEnvironment(scene, collision_resolution=0.05, tune_samples=1024)
@@ -724,7 +725,10 @@ def bench_prm_lazy(n_nodes: int = 3000, k: int = 10, window: int = 256) -> dict:
     out = {"roadmap_nodes": n, "k": k, "resolution": 0.05, "window": window, "goal_found": goal is not None}
     if goal is None:
         return out
-    seq, bat = search(goal, 1), search(goal, window)
+    # best of three runs each: the searches are host-bound, so the host's
+    # load on a shared machine shows in single runs
+    seq = min((search(goal, 1) for _ in range(3)), key=lambda r: r["seconds"])
+    bat = min((search(goal, window) for _ in range(3)), key=lambda r: r["seconds"])
     for tag, r in (("per_edge_calls", seq), ("batched", bat)):
         out[tag] = {"seconds": r["seconds"], "device_calls": r["calls"], "edges_checked": r["edges_checked"],
                     "edge_lookups": r["lookups"], "processed_edges": r["processed_edges"]}
