@@ -357,7 +357,9 @@ int mrmg_node_store_set_path(mrmg_node_store *store, int32_t path);
 /* out3: [0] number of modes, [1] nodes in `mode`, [2] tensor-core path. */
 int mrmg_node_store_info(const mrmg_node_store *store, int32_t mode, int64_t *out3);
 
-/* k nearest neighbours of d_queries[Q, D] within their modes h_query_mode[Q]
+/* (Queries of mrmg_knn and mrmg_near may be in device or host memory; host
+ * rows are copied to a staging buffer of the store.)
+ * k nearest neighbours of d_queries[Q, D] within their modes h_query_mode[Q]
  * (host array): same result as mrmg_knn_exact -- on the tensor-core path the
  * tcgen05 distance GEMM selects candidates, a certificate proves they contain
  * the true k nearest (else the query reruns exactly) and FP64 re-ranks them.

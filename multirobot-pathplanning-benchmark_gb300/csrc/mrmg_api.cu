@@ -1085,7 +1085,41 @@ struct mrmg_node_store {
   bool near_valid = false;
   int D = 0;
   long long last_fallback = 0;
+  // device copies of host-resident queries: one for k-NN calls, one for
+  // radius calls (kept for mrmg_near_fetch)
+  double* qbuf[2] = {nullptr, nullptr};
+  long long qcap[2] = {0, 0};
 };
+
+// queries in host memory are copied to the store's staging buffer `which`
+// (the copy is stream-ordered; pageable sources are staged by the driver
+// before the call returns); device pointers pass through
+static cudaError_t stage_queries(mrmg_node_store* s, int which, const double* q, long long Q, const double** out,
+                                 cudaStream_t st) {
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, q);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    at.type = cudaMemoryTypeUnregistered;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+    *out = q;
+    return cudaSuccess;
+  }
+  const long long n = Q * (long long)s->D;
+  if (s->qcap[which] < n) {
+    const long long cap = std::max(n, 2 * s->qcap[which]);
+    if (s->qbuf[which]) cudaFree(s->qbuf[which]);
+    s->qbuf[which] = nullptr;
+    s->qcap[which] = 0;
+    e = cudaMalloc(&s->qbuf[which], sizeof(double) * cap);
+    if (e != cudaSuccess) return e;
+    s->qcap[which] = cap;
+  }
+  e = cudaMemcpyAsync(s->qbuf[which], q, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+  *out = s->qbuf[which];
+  return e;
+}
 
 extern "C" {
 
@@ -1120,6 +1154,8 @@ int mrmg_node_store_destroy(mrmg_node_store* s) {
   knn_store_delete(s->store);
   knn_scratch_delete(s->scratch);
   near_state_delete(s->near);
+  for (double* b : s->qbuf)
+    if (b) cudaFree(b);
   delete s;
   return MRMG_OK;
 }
@@ -1178,8 +1214,11 @@ int mrmg_knn(mrmg_node_store* s, const double* d_queries, int64_t Q, const int32
   int rc = check_query_modes(s, h_query_mode, Q);
   if (rc) return rc;
   int used_tc = 0, nfb = 0;
-  cudaError_t e = knn_store_query(s->store, s->scratch, d_queries, Q, h_query_mode, k, (long long*)d_idx, d_dist,
-                                  device_sms(), &used_tc, &nfb, (cudaStream_t)stream);
+  const double* dq = nullptr;
+  cudaError_t e = stage_queries(s, 0, d_queries, Q, &dq, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "knn query copy");
+  e = knn_store_query(s->store, s->scratch, dq, Q, h_query_mode, k, (long long*)d_idx, d_dist, device_sms(), &used_tc,
+                      &nfb, (cudaStream_t)stream);
   if (e == cudaErrorLaunchTimeout) return fail(MRMG_ERR_TIMEOUT, "a bounded tensor-core pipeline wait ran out");
   if (e != cudaSuccess) return cuda_fail(e, "knn");
   s->last_fallback = nfb;
@@ -1207,8 +1246,11 @@ int mrmg_near(mrmg_node_store* s, const double* d_queries, int64_t Q, const int3
     return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "near");
   }
   long long total = 0;
-  cudaError_t e = near_query(s->near, s->store, d_queries, Q, h_query_mode, h_radius, add_eps, (long long*)d_offsets,
-                             (long long*)d_idx, d_dist, cap, device_sms(), &total, st);
+  const double* dq = nullptr;
+  cudaError_t e = stage_queries(s, 1, d_queries, Q, &dq, st);
+  if (e != cudaSuccess) return cuda_fail(e, "near query copy");
+  e = near_query(s->near, s->store, dq, Q, h_query_mode, h_radius, add_eps, (long long*)d_offsets, (long long*)d_idx,
+                 d_dist, cap, device_sms(), &total, st);
   if (e == cudaErrorLaunchTimeout) return fail(MRMG_ERR_TIMEOUT, "a bounded tensor-core pipeline wait ran out");
   if (e != cudaSuccess) return cuda_fail(e, "near");
   s->near_valid = true;

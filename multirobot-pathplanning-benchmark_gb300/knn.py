@@ -135,16 +135,26 @@ class NodeStore:
         except Exception:
             pass
 
+    def _queries(self, queries):
+        """(pointer, Q, keep-alive, device): CUDA tensors pass as they are;
+        host arrays go to the library as host memory (it stages them)."""
+        if isinstance(queries, torch.Tensor) and queries.is_cuda:
+            qs = _dev_tensor(queries, dtype=torch.float64)
+            return qs.data_ptr(), qs.shape[0], qs, qs.device
+        a = queries.numpy() if isinstance(queries, torch.Tensor) else queries
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1, self.D))
+        return a.ctypes.data, a.shape[0], a, torch.device("cuda", torch.cuda.current_device())
+
     def knn(self, queries, query_mode, k: int, stream=None):
         """(idx [Q, k] int64, dist [Q, k] float64) on the device; idx local to the mode."""
-        qs = _dev_tensor(queries, dtype=torch.float64)
+        ptr, Q, keep, dev = self._queries(queries)
         qm = np.ascontiguousarray(np.asarray(query_mode, dtype=np.int32))
-        Q = qs.shape[0]
-        idx = torch.empty((Q, k), dtype=torch.int64, device=qs.device)
-        dist = torch.empty((Q, k), dtype=torch.float64, device=qs.device)
+        idx = torch.empty((Q, k), dtype=torch.int64, device=dev)
+        dist = torch.empty((Q, k), dtype=torch.float64, device=dev)
         st = np.zeros(2, dtype=np.int64)
-        _lib.check(self.lib.mrmg_knn(self.h, qs.data_ptr(), Q, qm.ctypes.data, int(k), idx.data_ptr(),
+        _lib.check(self.lib.mrmg_knn(self.h, ptr, Q, qm.ctypes.data, int(k), idx.data_ptr(),
                                      dist.data_ptr(), st.ctypes.data, _lib.stream_handle(stream)), "knn")
+        del keep
         self.last_stats = {"tensor_core": bool(st[0]), "rerun_exact": int(st[1])}
         return idx, dist
 
@@ -156,25 +166,24 @@ class NodeStore:
         ``radius`` is a scalar or one value per query.  Returns CSR device
         tensors (offsets [Q + 1], idx [total], dist [total] float64; dist is
         None when ``distances`` is False)."""
-        qs = _dev_tensor(queries, dtype=torch.float64)
+        ptr, Q, keep, dev = self._queries(queries)
         qm = np.ascontiguousarray(np.asarray(query_mode, dtype=np.int32).reshape(-1))
-        Q = qs.shape[0]
         if qm.shape[0] != Q:
             raise ValueError("one mode per query")
         r = np.ascontiguousarray(np.broadcast_to(np.asarray(radius, dtype=np.float64), (Q,)))
         if cap is None:
             cap = max(1024, 64 * Q)
-        offs = torch.empty(Q + 1, dtype=torch.int64, device=qs.device)
-        idx = torch.empty(max(cap, 1), dtype=torch.int64, device=qs.device)
-        dist = torch.empty(max(cap, 1), dtype=torch.float64, device=qs.device) if distances else None
+        offs = torch.empty(Q + 1, dtype=torch.int64, device=dev)
+        idx = torch.empty(max(cap, 1), dtype=torch.int64, device=dev)
+        dist = torch.empty(max(cap, 1), dtype=torch.float64, device=dev) if distances else None
         tot = np.zeros(1, dtype=np.int64)
-        _lib.check(self.lib.mrmg_near(self.h, qs.data_ptr(), Q, qm.ctypes.data, r.ctypes.data, float(add_eps),
+        _lib.check(self.lib.mrmg_near(self.h, ptr, Q, qm.ctypes.data, r.ctypes.data, float(add_eps),
                                       offs.data_ptr(), idx.data_ptr(), None if dist is None else dist.data_ptr(),
                                       int(cap), tot.ctypes.data, _lib.stream_handle(stream)), "near")
         total = int(tot[0])
         if total > cap:
-            idx = torch.empty(total, dtype=torch.int64, device=qs.device)
-            dist = torch.empty(total, dtype=torch.float64, device=qs.device) if distances else None
+            idx = torch.empty(total, dtype=torch.int64, device=dev)
+            dist = torch.empty(total, dtype=torch.float64, device=dev) if distances else None
             _lib.check(self.lib.mrmg_near_fetch(self.h, idx.data_ptr(), None if dist is None else dist.data_ptr(),
                                                 total, _lib.stream_handle(stream)), "near fetch")
         return offs, idx[:total], (dist[:total] if dist is not None else None)
