@@ -141,7 +141,10 @@ def lazy_astar(start, goal_nodes, get_neighbors: Callable, config_cost: Callable
     the search counters."""
     if best_cost is None:
         best_cost = np.inf
-    goal_set = set(goal_nodes) if not isinstance(goal_nodes, set) else goal_nodes
+    try:
+        goal_set = goal_nodes if isinstance(goal_nodes, (set, frozenset)) else set(goal_nodes)
+    except TypeError:   # unhashable nodes: membership as the reference tests it, in the list
+        goal_set = list(goal_nodes)
     parents = {start: None}
     gs = {start.id: 0}
     queue = _Heap()
