@@ -84,3 +84,85 @@ def test_radius_fp32_band():
         ratio = np.abs(m[:400].astype(np.float64) - exact) / (e * e)
         worst = max(worst, float(ratio.max()))
     assert worst <= 2.4e-6, worst
+
+
+def test_mode_tables_and_views():
+    """Per-mode scene declarations: the flat arrays the library receives and
+    the reduced scene a mode sees (its boxes, robot spheres plus the attached
+    objects it lists)."""
+    scenes = pkg("scenes")
+    sc = scenes.make_arm_mode_scene(0, n_objects=5, n_modes=6)
+    t = sc.mode_tables()
+    assert t["box_off"][0] == 0 and t["box_off"][-1] == len(t["boxes"]) and len(t["box_off"]) == 7
+    assert t["attach_off"][-1] == len(t["attach"]) and t["sphere_attach"].shape == (len(sc.sphere_radius),)
+    for m in range(sc.n_modes):
+        v = sc.for_mode(m)
+        assert len(v.box_lo) == len(sc.mode_boxes[m])
+        n_robot = int((sc.sphere_attach < 0).sum())
+        assert len(v.sphere_radius) == n_robot + 3 * len(sc.mode_attach[m])
+        held = {j % sc.n_robots for j in sc.mode_attach[m]}
+        assert len(held) == len(sc.mode_attach[m])          # one object per gripper
+        lo = np.asarray(sc.box_lo)[np.asarray(sc.mode_boxes[m], dtype=np.int64)]
+        assert np.array_equal(v.box_lo, lo)
+
+
+def test_speculative_checker_batches_by_mode():
+    """The checker sends a missed edge with the upcoming ones, at most
+    `window` edges, one call per mode, and answers later lookups from its
+    cache without further calls."""
+    lazy = pkg("lazy")
+    calls = []
+
+    def check(q0, q1, mode):
+        calls.append((mode, len(q0)))
+        return q0[:, 0] < 0.5
+
+    class N:
+        def __init__(self, i, mode):
+            self.id = i
+            self.state = type("S", (), {"q": np.array([i / 20.0, 0.0]), "mode": mode})()
+
+    nodes = [N(i, i % 2) for i in range(20)]
+    ck = lazy.SpeculativeEdgeChecker(check=check, window=6)
+    up = [(nodes[i], nodes[i + 1]) for i in range(1, 19)]
+    assert ck.is_free(nodes[0], nodes[1], up) is True
+    assert sum(n for _, n in calls) == 6 and {m for m, _ in calls} == {0, 1}
+    assert len(calls) == 2
+    before = len(calls)
+    assert ck.is_free(nodes[3], nodes[4]) is True          # speculated: from the cache
+    assert len(calls) == before
+    assert ck.is_free(nodes[11], nodes[12]) is False      # a miss: one more batch
+    assert len(calls) == before + 1
+    assert ck.stats()["lookups"] == 3
+
+
+def test_importer_options():
+    imp = pkg("importers")
+    base = """<mujoco>{comp}<worldbody>
+      <body name="r" pos="0 0 0.1">
+        <joint type="slide" axis="1 0 0" range="-1 1"/>
+        <joint type="slide" axis="0 1 0" range="-1 1"/>
+        <joint type="hinge" axis="0 0 1" range="-1.5 1.5"/>
+        {geom}
+      </body>
+      <body name="s" pos="0 0 0.1">
+        <joint type="slide" axis="1 0 0" range="-1 1"/>
+        <joint type="slide" axis="0 1 0" range="-1 1"/>
+        <joint type="hinge" axis="0 0 1" range="-90 90"/>
+        <geom type="sphere" size="0.1"/>
+      </body>
+      <geom type="box" pos="0.5 0 0.1" size="0.1 0.1 0.1"/>
+    </worldbody></mujoco>"""
+    sc = imp.load_mjcf_planar(base.format(comp='<compiler angle="radian"/>', geom='<geom type="capsule" size="0.07 0.1"/>'))
+    np.testing.assert_allclose(sc.limits[:, 2], [-1.5, 1.5])           # radians as given
+    np.testing.assert_allclose(sc.limits[:, 5], [-90.0, 90.0])         # radian compiler: no conversion
+    assert sc.sphere_radius.tolist() == [0.07, 0.1] and len(sc.box_lo) == 1
+    sc = imp.load_mjcf_planar(base.format(comp="", geom='<geom type="sphere" size="0.2"/>'), robots=["s", "r"])
+    assert sc.sphere_radius.tolist() == [0.1, 0.2]                     # configuration order as asked
+    np.testing.assert_allclose(sc.limits[:, 2], np.deg2rad([-90.0, 90.0]))
+    with pytest.raises(NotImplementedError):
+        imp.load_mjcf_planar(base.format(comp="", geom='<geom type="capsule" fromto="0 0 0 0.2 0 0" size="0.05"/>'))
+    with pytest.raises(ValueError):
+        imp.load_mjcf_planar(base.format(comp="", geom="<geom type='sphere' size='0.1'/>").replace(' range="-1 1"', "", 1))
+    with pytest.raises(ValueError):
+        imp.load_mjcf_planar(base.format(comp="", geom="<geom type='sphere' size='0.1'/>"), robots=["nobody"])
