@@ -63,3 +63,44 @@ def test_reference_arm_other_ranks_do_nothing(monkeypatch):
 
     # rank 1 of the reference arm exits 0 without work (rank 0 alone runs it)
     assert bench.run_reference(A()) == 0
+
+
+def _rank_fail_main(rank, world, port, out_dir):
+    """Rank 1 leaves between steps (raises before the next barrier); rank 0
+    learns of it from the process group within its short timeout instead of
+    waiting forever, and records the error."""
+    import datetime
+    import sys
+
+    sys.path.insert(0, str(ROOT))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import torch.distributed as dist
+
+    import bench
+
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=5))
+    bench.barrier(world)                      # step 1: both ranks
+    if rank == 1:
+        os._exit(0)                           # leaves with nothing in flight
+    try:
+        bench.reduce_max(1.0, world)          # step 2: the peer is gone
+        outcome = "returned"
+    except Exception as e:                    # noqa: BLE001 - any process-group error counts
+        outcome = "error: " + type(e).__name__
+    with open(os.path.join(out_dir, "rank0.txt"), "w") as f:
+        f.write(outcome)
+    os._exit(0)
+
+
+def test_failed_rank_is_detected_by_the_other(tmp_path):
+    world, port = 2, _free_port()
+    ctx = mp.spawn(_rank_fail_main, args=(world, port, str(tmp_path)), nprocs=world, join=False)
+    for p in ctx.processes:
+        p.join(timeout=60)
+    alive = [p for p in ctx.processes if p.is_alive()]
+    for p in alive:
+        p.kill()
+    assert not alive, "a rank hung instead of failing"
+    outcome = (tmp_path / "rank0.txt").read_text()
+    assert outcome.startswith("error:"), outcome
