@@ -1092,7 +1092,7 @@ struct mrmg_node_store {
 };
 
 // queries in host memory are copied to the store's staging buffer `which`
-// (the copy is stream-ordered; pageable sources are staged by the driver
+// (the copy is stream-ordered; pageable sources are staged by the CUDA driver
 // before the call returns); device pointers pass through
 static cudaError_t stage_queries(mrmg_node_store* s, int which, const double* q, long long Q, const double** out,
                                  cudaStream_t st) {
