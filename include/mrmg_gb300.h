@@ -37,7 +37,9 @@ enum {
   MRMG_ERR_CUDA = -2,         /* CUDA runtime error                             */
   MRMG_ERR_TIMEOUT = -3,      /* a bounded device wait ran out                  */
   MRMG_ERR_UNSUPPORTED = -4,  /* shape outside the compiled kernel variants     */
-  MRMG_ERR_N_START = -5       /* N_start > N (the reference asserts)            */
+  MRMG_ERR_N_START = -5,      /* N_start > N (the reference asserts)            */
+  MRMG_ERR_HOST = -6          /* host memory allocation failed (MemoryError);
+                                 no C++ exception leaves an entry point         */
 };
 
 enum { MRMG_F32 = 0, MRMG_F64 = 1 };
@@ -336,8 +338,10 @@ int mrmg_node_store_destroy(mrmg_node_store *store);
  * MultimodalGraph.add_nodes, prm_graph.py:289-291): appends rows[n, D] (FP64,
  * host or device memory) to `mode`, after its existing nodes, so that the
  * mode-local index of a node is its insertion order.  A mode index past the
- * last creates the modes in between, empty.  Only the tiles the new rows touch
- * are packed; a full mode segment doubles its capacity.  Synchronises. */
+ * last creates the modes in between, empty (mode < MRMG_MAX_STORE_MODES).
+ * Only the tiles the new rows touch are packed; a full mode segment doubles
+ * its capacity.  Synchronises. */
+#define MRMG_MAX_STORE_MODES (1 << 20)
 int mrmg_node_store_append(mrmg_node_store *store, int32_t mode, const double *rows, int64_t n, void *stream);
 
 /* Removal as SingleTree.remove_node (rrtstar_base.py:278-289): the mode's

@@ -18,6 +18,8 @@ MRMG_ERR_CUDA = -2
 MRMG_ERR_TIMEOUT = -3
 MRMG_ERR_UNSUPPORTED = -4
 MRMG_ERR_N_START = -5
+MRMG_ERR_HOST = -6
+MRMG_MAX_STORE_MODES = 1 << 20
 
 MRMG_F32 = 0
 MRMG_F64 = 1
@@ -122,6 +124,8 @@ def check(rc: int, what: str = "") -> int:
         raise ValueError(msg)
     if rc == MRMG_ERR_UNSUPPORTED:
         raise NotImplementedError(msg)
+    if rc == MRMG_ERR_HOST:
+        raise MemoryError(msg)
     raise Gb300Error(msg)
 
 

@@ -4,7 +4,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <mutex>
+#include <new>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -23,12 +25,30 @@ int fail(int code, const char* fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(buf, sizeof(buf), fmt, ap);
   va_end(ap);
-  g_last_error = buf;
+  try {
+    g_last_error = buf;
+  } catch (...) {
+    g_last_error.clear();
+  }
   return code;
 }
 
 int cuda_fail(cudaError_t e, const char* where) {
   return fail(MRMG_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+// The handler of the entry points whose host allocations grow with their
+// inputs (function-try-blocks): no C++ exception unwinds through the C ABI.
+int host_fail() {
+  try {
+    throw;
+  } catch (const std::bad_alloc&) {
+    return fail(MRMG_ERR_HOST, "host memory allocation failed");
+  } catch (const std::exception& ex) {
+    return fail(MRMG_ERR_HOST, "host exception: %s", ex.what());
+  } catch (...) {
+    return fail(MRMG_ERR_HOST, "unknown host exception");
+  }
 }
 
 // One device allocation holding every table of a scene.
@@ -329,7 +349,7 @@ int mrmg_abstract_scene_create(int32_t n_agents, int32_t dim, int32_t q_dim, con
                                const double* h_agent_radius_sq, int32_t n_boxes, const double* h_box_lo,
                                const double* h_box_hi, int32_t n_spheres, const double* h_sphere_pos,
                                const double* h_sphere_radius, const double* h_sphere_threshold,
-                               mrmg_scene** out) {
+                               mrmg_scene** out) try {
   if (!out) return fail(MRMG_ERR_ARG, "out is NULL");
   *out = nullptr;
   if (n_agents < 1 || n_agents > kMaxAgents) return fail(MRMG_ERR_UNSUPPORTED, "agents must be 1..%d", kMaxAgents);
@@ -387,13 +407,15 @@ int mrmg_abstract_scene_create(int32_t n_agents, int32_t dim, int32_t q_dim, con
   sc->band = d.delta_k * d.omax;
   *out = sc;
   return MRMG_OK;
+} catch (...) {
+  return host_fail();
 }
 
 int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const int32_t* h_base_kind,
                           const double* h_base_pose, const int32_t* h_n_links, const double* h_dh, int32_t S,
                           const int32_t* h_sphere_robot, const int32_t* h_sphere_link, const double* h_sphere_local,
                           const double* h_sphere_radius, int32_t B, const double* h_box_lo, const double* h_box_hi,
-                          double band, mrmg_scene** out) {
+                          double band, mrmg_scene** out) try {
   if (!out) return fail(MRMG_ERR_ARG, "out is NULL");
   *out = nullptr;
   if (R < 1 || R > kMaxRobots) return fail(MRMG_ERR_UNSUPPORTED, "robots must be 1..%d", kMaxRobots);
@@ -562,11 +584,13 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   sc->slot_to_sphere = slot_sphere;
   *out = sc;
   return MRMG_OK;
+} catch (...) {
+  return host_fail();
 }
 
 int mrmg_arm_scene_set_modes(mrmg_scene* sc, int32_t n_modes, const int32_t* h_sphere_attach,
                              const int64_t* h_mode_box_off, const int32_t* h_mode_boxes,
-                             const int64_t* h_mode_attach_off, const int32_t* h_mode_attach) {
+                             const int64_t* h_mode_attach_off, const int32_t* h_mode_attach) try {
   if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
   if (!sc->modes.empty()) return fail(MRMG_ERR_ARG, "the scene's modes are already set");
   if (n_modes < 1 || n_modes > (1 << 16)) return fail(MRMG_ERR_ARG, "modes must be 1..65536");
@@ -618,6 +642,14 @@ int mrmg_arm_scene_set_modes(mrmg_scene* sc, int32_t n_modes, const int32_t* h_s
     trim_tables(&t);
   }
   return MRMG_OK;
+} catch (...) {
+  // the scene keeps working as created, without modes
+  if (sc) {
+    sc->modes.clear();
+    if (sc->d_mode_tables) cudaFree(sc->d_mode_tables);
+    sc->d_mode_tables = nullptr;
+  }
+  return host_fail();
 }
 
 int mrmg_scene_set_mode(mrmg_scene* sc, int32_t mode) {
@@ -671,18 +703,18 @@ int mrmg_arm_slot_map(const mrmg_scene* sc, int32_t* out, int64_t cap) {
 }
 
 int mrmg_arm_scene_tune_order(mrmg_scene* sc, const void* d_q, int32_t dtype, int64_t n, int32_t* h_order_out,
-                              void* stream) {
+                              void* stream) try {
   if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
   if (n < 1 || (dtype != MRMG_F32 && dtype != MRMG_F64) || !d_q) return fail(MRMG_ERR_ARG, "samples / dtype");
   const int B = sc->arm.B;
   if (B < 2) return MRMG_OK;
   const int words = (B + 31) / 32;
   cudaStream_t st = (cudaStream_t)stream;
+  std::vector<uint32_t> hits((size_t)words * n);   // host first: nothing to free if it throws
   uint32_t* d_hits = nullptr;
   cudaError_t e = cudaMalloc(&d_hits, sizeof(uint32_t) * words * n);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(hits)");
   e = arm_box_hits(sc->arm, d_q, dtype, n, d_hits, words, st);
-  std::vector<uint32_t> hits((size_t)words * n);
   if (e == cudaSuccess) e = cudaMemcpyAsync(hits.data(), d_hits, sizeof(uint32_t) * words * n, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFree(d_hits);
@@ -725,6 +757,8 @@ int mrmg_arm_scene_tune_order(mrmg_scene* sc, const void* d_q, int32_t dtype, in
   if (h_order_out)
     for (int k = 0; k < B; k++) h_order_out[k] = order[k];
   return MRMG_OK;
+} catch (...) {
+  return host_fail();
 }
 
 int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype, int64_t n, uint8_t* d_out,
@@ -1125,10 +1159,11 @@ extern "C" {
 
 int mrmg_node_store_create(const double* d_nodes, int64_t M, int32_t D, const int64_t* h_mode_offsets,
                            int32_t n_modes, const int64_t* h_slices, int32_t A, int32_t metric,
-                           mrmg_node_store** out, void* stream) {
+                           mrmg_node_store** out, void* stream) try {
   if (!out) return fail(MRMG_ERR_ARG, "out is NULL");
   *out = nullptr;
-  if (M < 0 || n_modes < 1 || metric < 0 || metric > 3 || !h_mode_offsets) return fail(MRMG_ERR_ARG, "M / modes / metric");
+  if (M < 0 || n_modes < 1 || n_modes > MRMG_MAX_STORE_MODES || metric < 0 || metric > 3 || !h_mode_offsets)
+    return fail(MRMG_ERR_ARG, "M / modes (1..%d) / metric", (int)MRMG_MAX_STORE_MODES);
   if (h_mode_offsets[0] != 0 || h_mode_offsets[n_modes] != M) return fail(MRMG_ERR_ARG, "mode offsets must span [0, M]");
   for (int m = 0; m < n_modes; m++)
     if (h_mode_offsets[m + 1] < h_mode_offsets[m]) return fail(MRMG_ERR_ARG, "mode offsets must not decrease");
@@ -1138,15 +1173,23 @@ int mrmg_node_store_create(const double* d_nodes, int64_t M, int32_t D, const in
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   mrmg_node_store* s = new mrmg_node_store();
-  s->D = D;
-  s->scratch = knn_scratch_new();
-  s->near = near_state_new();
-  s->store = knn_store_new();
-  cudaError_t e = knn_store_build(s->store, d_nodes, M, (const long long*)h_mode_offsets, n_modes, t, metric, D, st);
+  cudaError_t e = cudaSuccess;
+  try {
+    s->D = D;
+    s->scratch = knn_scratch_new();
+    s->near = near_state_new();
+    s->store = knn_store_new();
+    e = knn_store_build(s->store, d_nodes, M, (const long long*)h_mode_offsets, n_modes, t, metric, D, st);
+  } catch (...) {
+    mrmg_node_store_destroy(s);
+    throw;
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) { mrmg_node_store_destroy(s); return cuda_fail(e, "node store"); }
   *out = s;
   return MRMG_OK;
+} catch (...) {
+  return host_fail();
 }
 
 int mrmg_node_store_destroy(mrmg_node_store* s) {
@@ -1160,9 +1203,11 @@ int mrmg_node_store_destroy(mrmg_node_store* s) {
   return MRMG_OK;
 }
 
-int mrmg_node_store_append(mrmg_node_store* s, int32_t mode, const double* rows, int64_t n, void* stream) {
+int mrmg_node_store_append(mrmg_node_store* s, int32_t mode, const double* rows, int64_t n, void* stream) try {
   if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
   if (mode < 0 || n < 0) return fail(MRMG_ERR_ARG, "mode / n must be >= 0");
+  if (mode >= MRMG_MAX_STORE_MODES) return fail(MRMG_ERR_ARG, "mode %d: a store holds < %d modes", mode,
+                                                 (int)MRMG_MAX_STORE_MODES);
   if (n > 0 && !rows) return fail(MRMG_ERR_ARG, "NULL rows");
   if (knn_store_count(s->store, mode) + n > (1ll << 31) - 1) return fail(MRMG_ERR_ARG, "a mode holds < 2^31 nodes");
   cudaStream_t st = (cudaStream_t)stream;
@@ -1170,6 +1215,8 @@ int mrmg_node_store_append(mrmg_node_store* s, int32_t mode, const double* rows,
   cudaError_t e = knn_store_append(s->store, mode, rows, n, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "node store append");
+} catch (...) {
+  return host_fail();
 }
 
 int mrmg_node_store_remove(mrmg_node_store* s, int32_t mode, int64_t idx, void* stream) {
@@ -1206,7 +1253,7 @@ static int check_query_modes(const mrmg_node_store* s, const int32_t* h_query_mo
 }
 
 int mrmg_knn(mrmg_node_store* s, const double* d_queries, int64_t Q, const int32_t* h_query_mode, int32_t k,
-             int64_t* d_idx, double* d_dist, int64_t* out_stats2, void* stream) {
+             int64_t* d_idx, double* d_dist, int64_t* out_stats2, void* stream) try {
   if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
   if (Q < 0 || k < 1 || k > 64) return fail(MRMG_ERR_ARG, "Q / k (1..64)");
   if (Q == 0) return MRMG_OK;
@@ -1224,11 +1271,13 @@ int mrmg_knn(mrmg_node_store* s, const double* d_queries, int64_t Q, const int32
   s->last_fallback = nfb;
   if (out_stats2) { out_stats2[0] = used_tc; out_stats2[1] = nfb; }
   return MRMG_OK;
+} catch (...) {
+  return host_fail();
 }
 
 int mrmg_near(mrmg_node_store* s, const double* d_queries, int64_t Q, const int32_t* h_query_mode,
               const double* h_radius, double add_eps, int64_t* d_offsets, int64_t* d_idx, double* d_dist, int64_t cap,
-              int64_t* out_total, void* stream) {
+              int64_t* out_total, void* stream) try {
   if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
   if (Q < 0 || cap < 0) return fail(MRMG_ERR_ARG, "Q / cap must be >= 0");
   if (!d_offsets || !out_total) return fail(MRMG_ERR_ARG, "NULL offsets / total");
@@ -1256,9 +1305,11 @@ int mrmg_near(mrmg_node_store* s, const double* d_queries, int64_t Q, const int3
   s->near_valid = true;
   *out_total = total;
   return MRMG_OK;
+} catch (...) {
+  return host_fail();
 }
 
-int mrmg_near_fetch(mrmg_node_store* s, int64_t* d_idx, double* d_dist, int64_t cap, void* stream) {
+int mrmg_near_fetch(mrmg_node_store* s, int64_t* d_idx, double* d_dist, int64_t cap, void* stream) try {
   if (!s) return fail(MRMG_ERR_ARG, "store is NULL");
   if (!s->near_valid) return fail(MRMG_ERR_ARG, "no radius query to fetch");
   if (cap < near_last_total(s->near)) return fail(MRMG_ERR_ARG, "cap %lld < total %lld", (long long)cap,
@@ -1266,6 +1317,8 @@ int mrmg_near_fetch(mrmg_node_store* s, int64_t* d_idx, double* d_dist, int64_t 
   if (cap > 0 && !d_idx) return fail(MRMG_ERR_ARG, "NULL index output");
   cudaError_t e = near_fetch(s->near, (long long*)d_idx, d_dist, cap, device_sms(), (cudaStream_t)stream);
   return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "near fetch");
+} catch (...) {
+  return host_fail();
 }
 
 int mrmg_selftest_umma(const void* d_a, const void* d_b, int32_t n, float* d_c, void* stream) {

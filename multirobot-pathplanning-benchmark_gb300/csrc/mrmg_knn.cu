@@ -1533,6 +1533,13 @@ static cudaError_t upload_meta(KnnStore* s, cudaStream_t st) {
 // new buffers for `n_new` modes with capacities `cap_new` (rows, multiples of
 // NT); the old modes' rows, tiles and norm bounds move over
 static cudaError_t relayout(KnnStore* s, int n_new, const std::vector<long long>& cap_new, cudaStream_t st) {
+  // every host allocation happens here, before the device buffers change
+  // hands: a host allocation failure leaves the store as it was
+  s->cnt.reserve(n_new);
+  s->mode_tiles.reserve(n_new);
+  s->cap.reserve(n_new);
+  s->h_meta.reserve(2 * (size_t)std::max(n_new, 1));
+  s->h_tile0.reserve(std::max(n_new, 1));
   std::vector<long long> beg_new(n_new, 0);
   long long total = 0;
   for (int m = 0; m < n_new; m++) { beg_new[m] = total; total += cap_new[m]; }
@@ -1592,8 +1599,8 @@ static cudaError_t relayout(KnnStore* s, int n_new, const std::vector<long long>
   s->d_xmax = d_xmax;
   s->cnt.resize(n_new, 0);
   s->mode_tiles.resize(n_new, 0);
-  s->beg = beg_new;
-  s->cap = cap_new;
+  s->beg.swap(beg_new);
+  s->cap.assign(cap_new.begin(), cap_new.end());
   s->n_modes = n_new;
   s->cap_total = total;
   set_dev_view(s);

@@ -43,3 +43,26 @@ def test_version_and_error_without_gpu(cuda_lib):
     rc = cuda_lib.mrmg_is_collision_free_batch(None, None, 0, 1, None, None, 0)
     assert rc == _lib.MRMG_ERR_ARG
     assert b"NULL" in cuda_lib.mrmg_last_error() or b"scene" in cuda_lib.mrmg_last_error()
+
+
+def test_status_codes_match_header_and_map_to_exceptions(cuda_lib):
+    """The header's status codes are the binding's, and each maps to the
+    exception type the reference's callers expect."""
+    import pytest
+
+    _lib = pkg("_lib")
+    text = HEADER.read_text()
+    codes = dict((k, int(v)) for k, v in re.findall(r"\b(MRMG_(?:OK|ERR_[A-Z_]+))\s*=\s*(-?\d+)", text))
+    assert codes == {k: getattr(_lib, k) for k in codes} and len(codes) == 7
+    assert int(re.search(r"#define MRMG_MAX_STORE_MODES \(1 << (\d+)\)", text).group(1)) == 20
+    assert _lib.MRMG_MAX_STORE_MODES == 1 << 20
+    want = {"MRMG_ERR_ARG": ValueError, "MRMG_ERR_N_START": AssertionError,
+            "MRMG_ERR_UNSUPPORTED": NotImplementedError, "MRMG_ERR_HOST": MemoryError,
+            "MRMG_ERR_CUDA": _lib.Gb300Error, "MRMG_ERR_TIMEOUT": _lib.Gb300Error}
+    for name, exc in want.items():
+        with pytest.raises(exc):
+            _lib.check(codes[name], name)
+    assert _lib.check(0) == 0
+    # store entry points validate their handle before any device call
+    assert cuda_lib.mrmg_node_store_append(None, 0, None, 0, None) == _lib.MRMG_ERR_ARG
+    assert cuda_lib.mrmg_near_fetch(None, None, None, 0, None) == _lib.MRMG_ERR_ARG

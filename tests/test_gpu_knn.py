@@ -257,6 +257,17 @@ def test_node_store_grow_from_empty(gpu, oracle):
         store.append(m, q)
         host.append(m, q)
     assert store.size(0) + store.size(1) == 300
+    # a mode index past the last creates the modes between, empty; one at or
+    # beyond the store's mode limit is refused and leaves the store as it was
+    store.append(5, rng.uniform(-1, 1, (2, D)))
+    assert store.n_modes == 6 and store.size(3) == 0 and store.size(5) == 2
+    with pytest.raises(ValueError):
+        store.append(pkg("_lib").MRMG_MAX_STORE_MODES, np.zeros((1, D)))
+    assert store.n_modes == 6 and store.size(0) + store.size(1) == 300
+    allnodes, alloff = host.arrays()
+    q = rng.uniform(-1, 1, (4, D))
+    oi, _ = oracle.knn(q, [0, 1, 0, 1], allnodes, alloff, sl, "euclidean", 3)
+    assert np.array_equal(store.knn(q, [0, 1, 0, 1], 3)[0].cpu().numpy(), oi)
 
 
 @pytest.mark.parametrize("path", ["tensor_core", "exact"])
