@@ -272,7 +272,7 @@ def run_gb300(args):
     # ---- end to end through the public API: a graph-captured edge-check plan
     # (pinned host buffers; every step copies the endpoints host->device in
     # chunks overlapped with the checks and reads the verdicts back)
-    plan = env.edge_check_plan(n, chunks=args.chunks)
+    plan = env.edge_check_plan(n, chunks=args.chunks, dtype=torch.float32)   # the workload's FP32 endpoints
     plan.q1_host[:] = q1
     plan.q2_host[:] = q2
     for _ in range(args.warmup):
@@ -290,7 +290,7 @@ def run_gb300(args):
     # the device while earlier steps' checks run, and independent steps
     # overlap each other's kernel tails (every step still copies its own
     # inputs and reads its own verdicts back inside the timed region)
-    pipe = env.edge_check_pipeline(n, depth=E2E_DEPTH)
+    pipe = env.edge_check_pipeline(n, depth=E2E_DEPTH, dtype=torch.float32)
     for p in pipe.plans:
         p.q1_host[:] = q1
         p.q2_host[:] = q2
@@ -628,6 +628,45 @@ def bench_abstract(orc, reps: int = 20) -> dict:
 
     mat_ms = timed(dmat, flush_l2=True)
     ref_v, ref_e = o.configs_free(q), o.edges_free(q1, q2, 0.01)
+
+    # The same calls replayed as CUDA graphs, end to end from pinned host
+    # memory (inputs host->device, the checks, verdicts device->host, one
+    # graph launch and one wait per call): what a caller that repeats calls
+    # of one size pays once the per-call launches and the synchronous status
+    # read are gone.  Host wall clock per call, median of `reps * 10` calls.
+    plan = col.EdgeCheckPlan(s, 1000, 0.01, dtype=torch.float64, chunks=1)
+    plan.q1_host[:] = q1
+    plan.q2_host[:] = q2
+    g_edges = plan.run().copy()
+    st = torch.cuda.Stream()
+    q_pin = torch.from_numpy(q).pin_memory()
+    q_dev = torch.empty_like(qd)
+    v_dev = torch.empty(len(q), dtype=torch.uint8, device="cuda")
+    v_pin = torch.empty(len(q), dtype=torch.uint8).pin_memory()
+    torch.cuda.synchronize()
+    cfg_graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(cfg_graph, stream=st):
+        q_dev.copy_(q_pin, non_blocking=True)
+        s.is_collision_free_batch(q_dev, out=v_dev, stream=st, flags=_lib.MRMG_FLAG_ASYNC)
+        v_pin.copy_(v_dev, non_blocking=True)
+
+    def cfg_run():
+        with torch.cuda.stream(st):
+            cfg_graph.replay()
+        st.synchronize()
+        return v_pin.numpy()
+
+    g_cfg = cfg_run().copy()
+
+    def wall(f):
+        ts = []
+        for _ in range(reps * 10):
+            t0 = time.perf_counter()
+            f()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts)) * 1e3
+
+    edge_graph_ms, cfg_graph_ms = wall(plan.run), wall(cfg_run)
     t0 = time.perf_counter()
     ref_d = orc.dist_matrix(q1, q, sl, "euclidean")
     cpu_mat_s = time.perf_counter() - t0
@@ -650,9 +689,18 @@ def bench_abstract(orc, reps: int = 20) -> dict:
         "workload": "2 discs r = 0.1 in [-1, 1]^4, 10 boxes (centres U[-0.8, 0.8]^2, half extents U[0.05, 0.2]); "
                     "10,000 configurations, 1,000 edges at resolution 0.01, 1,000 x 10,000 euclidean matrix",
         "configs": {"ms_per_call": cfg_ms, "configs_per_s": 1e4 / (cfg_ms * 1e-3),
-                    "mismatches": int((v.cpu().numpy() != ref_v).sum()), "cpu_configs_per_s": 1e4 / cpu_cfg_s},
+                    "mismatches": int((v.cpu().numpy() != ref_v).sum()), "cpu_configs_per_s": 1e4 / cpu_cfg_s,
+                    "graph_e2e": {"ms_per_call": cfg_graph_ms, "configs_per_s": 1e4 / (cfg_graph_ms * 1e-3),
+                                  "mismatches": int((g_cfg != ref_v).sum()),
+                                  "h2d_bytes": int(q.nbytes), "d2h_bytes": len(q)}},
         "edges": {"ms_per_call": edge_ms, "edges_per_s": 1e3 / (edge_ms * 1e-3),
-                  "mismatches": int((e.cpu().numpy() != ref_e).sum()), "cpu_edges_per_s": 1e3 / cpu_edge_s},
+                  "mismatches": int((e.cpu().numpy() != ref_e).sum()), "cpu_edges_per_s": 1e3 / cpu_edge_s,
+                  "graph_e2e": {"ms_per_call": edge_graph_ms, "edges_per_s": 1e3 / (edge_graph_ms * 1e-3),
+                                "mismatches": int((g_edges != ref_e).sum()),
+                                "h2d_bytes": int(q1.nbytes + q2.nbytes), "d2h_bytes": len(q1),
+                                "api": "collision.EdgeCheckPlan(scene, 1000, 0.01, dtype=float64).run()"}},
+        "timing": "synchronous calls: CUDA events around one call with inputs resident (launches, the status "
+                  "read and the host's return included); graph_e2e: host wall clock per graph replay and wait",
         "dist_matrix": {"ms_per_launch": mat_ms, "distances_per_s": 1e7 / (mat_ms * 1e-3),
                         "bit_identical": bool(np.array_equal(out.cpu().numpy(), ref_d)),
                         "cpu_distances_per_s": 1e7 / cpu_mat_s,

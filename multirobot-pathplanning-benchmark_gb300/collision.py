@@ -239,7 +239,7 @@ class EdgeCheckPlan:
     """
 
     def __init__(self, scene: "Gb300Scene", n: int, resolution: float, include_endpoints: bool = False,
-                 dtype=torch.float32, chunks: int = 4):
+                 dtype=torch.float64, chunks: int = 4):
         self.scene = scene
         self.n = int(n)
         D = scene.q_dim

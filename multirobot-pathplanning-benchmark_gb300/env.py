@@ -162,18 +162,21 @@ class Gb300CollisionBackend:
         return v.bool().cpu().numpy() if not isinstance(q1s, torch.Tensor) else v.bool()
 
     def edge_check_plan(self, n: int, resolution: Optional[float] = None, include_endpoints: bool = False,
-                        chunks: int = 1, dtype=torch.float32):
+                        chunks: int = 1, dtype=torch.float64):
         """A reusable, graph-captured batched edge check for batches of `n`
         edges: fill ``plan.q1_host`` / ``plan.q2_host`` (pinned) and call
         ``plan.run()`` -> verdicts.  One graph launch per call; host->device
-        copies overlap the checks."""
+        copies overlap the checks.  The endpoint buffers are FP64 by default,
+        as the reference's configurations; ``dtype=torch.float32`` halves the
+        copies and checks the FP32 endpoints exactly (an FP64 endpoint
+        written into an FP32 buffer is rounded first)."""
         from .collision import EdgeCheckPlan
 
         return EdgeCheckPlan(self._gb300, n, self.collision_resolution if resolution is None else resolution,
                              include_endpoints, dtype=dtype, chunks=chunks)
 
     def edge_check_pipeline(self, n: int, depth: int = 2, resolution: Optional[float] = None,
-                            include_endpoints: bool = False, dtype=torch.float32):
+                            include_endpoints: bool = False, dtype=torch.float64):
         """``depth`` plans of ``n`` edges on separate scene handles and streams
         (see ``collision.EdgeCheckPipeline``): batch k+1's copies overlap
         batch k's checks."""

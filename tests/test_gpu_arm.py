@@ -187,16 +187,21 @@ def test_tuned_test_order_keeps_verdicts(gpu, oracle):
                           o.edges_free(w["q1"], w["q2"], w["resolution"]))
 
 
-def test_edge_check_plan_graph(gpu, oracle):
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_edge_check_plan_graph(gpu, oracle, dtype):
     """The graph-captured plan (pipelined host->device chunks) gives the oracle's
-    verdicts, run after run, and reports bad edges as the plain call does."""
+    verdicts, run after run, and reports bad edges as the plain call does;
+    FP64 endpoint buffers (the default) and FP32 ones."""
+    import torch
+
     scenes, envm = pkg("scenes"), pkg("env")
     scene = scenes.make_arm_scene(0)
     env = envm.Gb300ArmEnvironment(scene, tune_samples=0)
     o = oracle.OracleScene(scene)
     w = scenes.make_arm_workload(scene, seed=2, n_configs=10, n_edges=6000)
     ref = o.edges_free(w["q1"], w["q2"], w["resolution"])
-    plan = env.edge_check_plan(6000, chunks=3)
+    plan = env.edge_check_plan(6000, chunks=3, dtype=getattr(torch, dtype))
+    assert plan.q1_host.dtype == np.dtype(dtype)
     plan.q1_host[:] = w["q1"]
     plan.q2_host[:] = w["q2"]
     for _ in range(3):

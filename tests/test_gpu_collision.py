@@ -4,6 +4,7 @@ import json
 
 import numpy as np
 import pytest
+import torch
 
 from conftest import golden, pkg
 
@@ -51,6 +52,25 @@ def test_disc_edges_golden_all_variants(gpu):
                 sc.is_edge_collision_free_batch(g["q1"][~ok], g["q2"][~ok], v["resolution"],
                                                 v.get("include_endpoints", False), None, v.get("N_start", 0),
                                                 v.get("N_max"))
+
+
+def test_disc_edges_graph_plan_golden(gpu):
+    """The graph-captured plan over the abstract scene (FP64 endpoints, as the
+    reference's configurations) gives the golden verdicts of the reference's
+    own edge check, replay after replay and for new endpoints."""
+    g = golden("abstract_disc.npz")
+    col = pkg("collision")
+    sc = col.Gb300Scene(_disc_scene(g))
+    v = json.loads(str(g["variants"]))[0]
+    assert v.get("N_start", 0) == 0 and v.get("N_max") is None and not v.get("include_endpoints", False)
+    ref = g["edge_free"][0]
+    assert (ref != 255).all()
+    half = len(ref) // 2
+    plan = col.EdgeCheckPlan(sc, half, v["resolution"], dtype=torch.float64, chunks=2)
+    for lo in (0, half, 0):
+        plan.q1_host[:] = g["q1"][lo:lo + half]
+        plan.q2_host[:] = g["q2"][lo:lo + half]
+        assert np.array_equal(plan.run(), ref[lo:lo + half]), lo
 
 
 def test_disc_env_api_golden(gpu):
