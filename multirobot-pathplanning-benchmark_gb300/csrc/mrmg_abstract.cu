@@ -10,6 +10,13 @@
 //          whose only doubt is a pending configuration is queued.
 //  pass 2  the queued items again, with each pending configuration decided
 //          by the exact FP64 restatement of the reference's arithmetic.
+//
+// The FP64 pipe of this part is narrow and issues a warp instruction at the
+// same cost whatever the number of active lanes, so FP64 work is kept off
+// long dependent chains: edge positions are interpolated in double-float
+// FP32, step counts come from an FP32 quotient with an integer-distance
+// certificate, and a pending configuration is decided by a whole warp at
+// once, one agent pair, box or sphere test per lane.
 #include "mrmg_internal.cuh"
 
 namespace mrmg {
@@ -25,22 +32,11 @@ __device__ __forceinline__ double ldq(const void* p, int dtype, long long i) {
 }
 
 // ---------------------------------------------------------------------------
-// FP32 classification of one configuration; coordinates come from `acc(k)`.
+// FP32 classification of one configuration qf[D] whose coordinates lie within
+// 2^-24 |q| of the exact ones (plus `extra`, a distance), qmax = max |qf|.
 // ---------------------------------------------------------------------------
-template <class Acc>
-__device__ uint8_t classify32(const AbstractDev& s, Acc acc) {
-  float qf[kMaxAgents * kMaxAgentDim];
-  float qmax = 0.f;
-  bool bad = false;
-  for (int k = 0; k < s.D; k++) {
-    double v = acc(k);
-    bad |= !(fabs(v) <= 1e30);            // NaN, inf or huge: exact path decides
-    float f = (float)v;
-    qf[k] = f;
-    qmax = fmaxf(qmax, fabsf(f));
-  }
-  if (bad) return V_PENDING;
-  const float delta = s.delta_k * (qmax + s.omax);
+__device__ uint8_t classify_core(const AbstractDev& s, const float* qf, float qmax, float extra) {
+  const float delta = s.delta_k * (qmax + s.omax) + extra;
   bool unc = false;
   const int A = s.A, dim = s.dim;
   // agent - agent  (abstract_env.py:261-268)
@@ -90,61 +86,93 @@ __device__ uint8_t classify32(const AbstractDev& s, Acc acc) {
   return unc ? V_PENDING : V_FREE;
 }
 
+// A configuration given as FP32 values x(k) (rounded once from the exact
+// coordinates); NaN, inf or huge coordinates leave it pending (the exact
+// path decides).
+template <class Acc>
+__device__ uint8_t classify32(const AbstractDev& s, Acc x, float extra) {
+  float qf[kMaxAgents * kMaxAgentDim];
+  float qmax = 0.f;
+  bool bad = false;
+  for (int k = 0; k < s.D; k++) {
+    const float f = x(k);
+    bad |= !(fabsf(f) <= 1e30f);
+    qf[k] = f;
+    qmax = fmaxf(qmax, fabsf(f));
+  }
+  return bad ? V_PENDING : classify_core(s, qf, qmax, extra);
+}
+
 // ---------------------------------------------------------------------------
-// Exact FP64 restatement (same operation order as the reference).
-// np.linalg.norm -> sqrt of a fused multiply-add chain from 0 (OpenBLAS ddot);
-// np.sum of the squared clip residuals -> numpy pairwise order.
+// Exact FP64 restatement of one configuration (same operation order as the
+// reference), evaluated by all lanes of a warp together: lane t takes test t,
+// t + 32, ... of the agent pairs, then the agent-box and agent-sphere tests.
+// acc(k) is coordinate k in FP64.  np.linalg.norm -> sqrt of a fused
+// multiply-add chain from 0 (OpenBLAS ddot); np.sum of the squared clip
+// residuals -> numpy pairwise order.  Each test is the one the reference's
+// loops make, so "any test collides" is their verdict.  Warp-uniform.
 // ---------------------------------------------------------------------------
 template <class Acc>
-__device__ bool exact_free(const AbstractDev& s, Acc acc) {
+__device__ bool exact_free_warp(const AbstractDev& s, Acc acc, int lane) {
   const int A = s.A, dim = s.dim;
-  double d[kMaxAgentDim];
-  for (int i = 0; i < A; i++)
-    for (int j = i + 1; j < A; j++) {
+  const int n_pair = A * (A - 1) / 2, n_box = A * s.nb, n_all = n_pair + n_box + A * s.ns;
+  for (int t0 = 0; t0 < n_all; t0 += 32) {
+    const int t = t0 + lane;
+    bool hit = false;
+    if (t < n_pair) {
+      int i = 0, r = t;
+      while (r >= A - 1 - i) { r -= A - 1 - i; i++; }
+      const int j = i + 1 + r;
       double ss = 0.0;
       for (int k = 0; k < dim; k++) {
-        double t = __dsub_rn(acc(s.agent_off[i] + k), acc(s.agent_off[j] + k));
-        ss = __fma_rn(t, t, ss);
+        const double d = __dsub_rn(acc(s.agent_off[i] + k), acc(s.agent_off[j] + k));
+        ss = __fma_rn(d, d, ss);
       }
-      if (sqrt(ss) < s.pair_thr[i * A + j]) return false;
-    }
-  for (int i = 0; i < A; i++) {
-    const int off = s.agent_off[i];
-    for (int b = 0; b < s.nb; b++) {
+      hit = sqrt(ss) < s.pair_thr[i * A + j];
+    } else if (t < n_pair + n_box) {
+      const int i = (t - n_pair) / s.nb, b = t - n_pair - i * s.nb;
+      const int off = s.agent_off[i];
       const double* lo = s.box_lo + b * dim;
       const double* hi = s.box_hi + b * dim;
+      double d[kMaxAgentDim];
       for (int k = 0; k < dim; k++) {
-        double c = acc(off + k);
+        const double c = acc(off + k);
         double v = c > lo[k] ? c : lo[k];
         v = v < hi[k] ? v : hi[k];
-        double e = __dsub_rn(v, c);
+        const double e = __dsub_rn(v, c);
         d[k] = __dmul_rn(e, e);
       }
-      if (np_sum_dyn(d, dim) <= s.r2[i]) return false;
-    }
-    for (int o = 0; o < s.ns; o++) {
+      hit = np_sum_dyn(d, dim) <= s.r2[i];
+    } else if (t < n_all) {
+      const int u = t - n_pair - n_box;
+      const int i = u / s.ns, o = u - i * s.ns;
+      const int off = s.agent_off[i];
       const double* p = s.sph_pos + o * dim;
       double ss = 0.0;
       for (int k = 0; k < dim; k++) {
-        double t = __dsub_rn(p[k], acc(off + k));
-        ss = __fma_rn(t, t, ss);
+        const double d = __dsub_rn(p[k], acc(off + k));
+        ss = __fma_rn(d, d, ss);
       }
-      if (sqrt(ss) < s.sph_thr[o * A + i]) return false;
+      hit = sqrt(ss) < s.sph_thr[o * A + i];
     }
+    if (__any_sync(MRMG_FULL, hit)) return false;
   }
   return true;
 }
 
 // ---------------------------------------------------------------------------
-// Configurations: one thread per configuration.
+// Configurations: one thread per configuration in pass 1, one warp per
+// pending configuration in pass 2.
 // ---------------------------------------------------------------------------
 __global__ void configs_pass1(AbstractDev s, const void* q, int dtype, long long n, uint8_t* out,
                               int* ctr, long long* pend) {
   const int D = s.D;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    auto acc = [&](int k) { return ldq(q, dtype, i * D + k); };
-    uint8_t v = classify32(s, acc);
+    auto x = [&](int k) {
+      return dtype == MRMG_F32 ? ((const float*)q)[i * D + k] : (float)((const double*)q)[i * D + k];
+    };
+    uint8_t v = classify32(s, x, 0.f);
     out[i] = v;
     if (v == V_PENDING) {
       int slot = atomicAdd(&ctr[kCtrPending], 1);
@@ -157,17 +185,34 @@ __global__ void configs_pass2(AbstractDev s, const void* q, int dtype, uint8_t* 
                               const long long* pend) {
   const int D = s.D;
   const int np = ctr[kCtrPending];
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x) {
-    long long i = pend[k];
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int n_warps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int k = warp; k < np; k += n_warps) {
+    const long long i = pend[k];
     auto acc = [&](int j) { return ldq(q, dtype, i * D + j); };
-    out[i] = exact_free(s, acc) ? 1 : 0;
+    const bool ok = exact_free_warp(s, acc, lane);
+    if (lane == 0) out[i] = ok ? 1 : 0;
   }
 }
 
 // ---------------------------------------------------------------------------
 // Edges: one warp per edge; the lanes check consecutive chunks of the
 // reference's binary-search order, with a warp vote after each chunk.
+//
+// Positions q1 + (q2 - q1) * i / (N - 1) are formed in double-float FP32
+// (interp_df: q1 and q2 - q1 as hi + lo pairs, ~44 significant bits) and
+// rounded once, so each coordinate lies within 2^-24 |q| + 2^-42 (|q1| + |q2|)
+// of the reference's FP64 position; `extra` = 2^-30 * max(|q1| + |q2|) * dim
+// covers the second term (with a wide margin) in every distance, agent pairs
+// included.  Pass 2 decides a pending position from the reference's own FP64
+// arithmetic, q1 + ((q2 - q1) / (N - 1)) * i.
+//
+// Shared memory per warp: the double-float endpoints ah, al, dh, dl [D]
+// (floats) and, in pass 2, q1 and the FP64 direction [D] (doubles).
 // ---------------------------------------------------------------------------
+constexpr size_t edge_warp_bytes(int D, bool resolve) { return (size_t)D * (resolve ? 32 : 16); }
+
 template <bool RESOLVE>
 __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int dtype, long long n,
                              double res, int incl, const long long* Np, long long N_start,
@@ -175,8 +220,14 @@ __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int 
   extern __shared__ double sm_ab[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int D = s.D;
-  double* wq1 = sm_ab + (size_t)wib * 2 * D;
-  double* wdir = wq1 + D;
+  unsigned char* wbase = (unsigned char*)sm_ab + (size_t)wib * edge_warp_bytes(D, RESOLVE);
+  double* w64a = (double*)wbase;                 // pass 2 only
+  double* w64d = w64a + D;
+  float* wah = (float*)(wbase + (RESOLVE ? (size_t)16 * D : 0));
+  float* wal = wah + D;
+  float* wdh = wal + D;
+  float* wdl = wdh + D;
+  const float res32 = (float)res;
   const unsigned lt_mask = (1u << lane) - 1u;
 
   while (true) {
@@ -193,30 +244,53 @@ __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int 
         e = k;
       }
     }
-    // endpoints (NpConfiguration stores float64) and N
-    double mloc = -1.0;
-    bool nan0 = false;
+    // endpoints as double-float: a = q1 and d = q2 - q1 (exact for FP32
+    // endpoints; for FP64 ones d is the reference's FP64 difference, split)
+    float mloc = 0.f, emax = 0.f;
+    bool nanf = false;
     for (int k = lane; k < D; k += 32) {
-      double a = ldq(q1, dtype, e * D + k), b = ldq(q2, dtype, e * D + k);
-      wq1[k] = a;
-      wdir[k] = b;
-      double v = fabs(__dsub_rn(a, b));
-      if (k == 0) nan0 = (v != v);
-      mloc = fmax(mloc, v);
+      float a_h, a_l = 0.f, d_h, d_l;
+      if (dtype == MRMG_F32) {
+        const float a = ((const float*)q1)[e * D + k], b = ((const float*)q2)[e * D + k];
+        a_h = a;
+        two_sum(b, -a, &d_h, &d_l);
+      } else {
+        const double a = ((const double*)q1)[e * D + k], b = ((const double*)q2)[e * D + k];
+        const double d = __dsub_rn(b, a);
+        a_h = (float)a;
+        a_l = (float)__dsub_rn(a, (double)a_h);
+        d_h = (float)d;
+        d_l = (float)__dsub_rn(d, (double)d_h);
+      }
+      wah[k] = a_h; wal[k] = a_l; wdh[k] = d_h; wdl[k] = d_l;
+      nanf |= d_h != d_h;
+      mloc = fmaxf(mloc, fabsf(d_h));
+      emax = fmaxf(emax, fabsf(a_h) + fabsf(__fadd_rn(a_h, d_h)));
     }
-    long long N;
+    long long N = 2;
     bool bad = false;
     if (Np) {
       N = Np[e];
       bad = N < 1;
     } else {
-      // config_dist(q1, q2, "max") / resolution  (abstract_env.py:321-323)
-      double m = warp_max_d(mloc);
-      nan0 = __any_sync(MRMG_FULL, nan0);
-      double t = __ddiv_rn(m, res);
-      if (nan0 || !(t < 9.0e15)) bad = true;
-      N = bad ? 2 : (long long)t + 1;
-      if (N < 2) N = 2;
+      const float m32 = warp_max(mloc);
+      const bool anynan = __any_sync(MRMG_FULL, nanf);
+      if (!steps_fp32(m32, anynan, res32, &N)) {
+        // config_dist(q1, q2, "max") / resolution in FP64 (abstract_env.py:321-323)
+        double mx = -1.0;
+        bool nan0 = false;
+        for (int k = lane; k < D; k += 32) {
+          const double v = fabs(__dsub_rn(ldq(q1, dtype, e * D + k), ldq(q2, dtype, e * D + k)));
+          if (k == 0) nan0 = (v != v);
+          mx = fmax(mx, v);
+        }
+        const double m = warp_max_d(mx);
+        nan0 = __any_sync(MRMG_FULL, nan0);
+        const double t = __ddiv_rn(m, res);
+        if (nan0 || !(t < 9.0e15)) bad = true;
+        N = bad ? 2 : (long long)t + 1;
+        if (N < 2) N = 2;
+      }
     }
     if (bad) {
       if (lane == 0) { atomicOr(&ctr[kCtrErr], E_BAD_INPUT); out[e] = 0; }
@@ -229,30 +303,70 @@ __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int 
       continue;
     }
     const long long nmax = (N_max < 0 || N_max > N) ? N : N_max;
-    const double denom = (double)(N - 1);
-    __syncwarp();
-    for (int k = lane; k < D; k += 32) wdir[k] = __ddiv_rn(__dsub_rn(wdir[k], wq1[k]), denom);
-    __syncwarp();
-
-    BfsChunker ch;
-    ch.init(N);
-    long long v;
-    unsigned m;
-    long long pos0;
-    bool coll = false, pending = false;
-    while (ch.next(lane, &v, &m, &pos0)) {
-      if (pos0 >= nmax) break;
-      long long my_pos = pos0 + __popc(m & lt_mask);
-      bool active = v >= 0 && my_pos >= N_start && my_pos < nmax && (incl || (v != 0 && v != N - 1));
-      uint8_t code = V_FREE;
-      if (active) {
-        const double di = (double)v;
-        auto acc = [&](int k) { return __dadd_rn(wq1[k], __dmul_rn(wdir[k], di)); };
-        code = classify32(s, acc);
-        if (RESOLVE && code == V_PENDING) code = exact_free(s, acc) ? V_FREE : V_COLLIDE;
+    // positions are exact FP32 integers up to 2^24; beyond, pass 1 leaves
+    // the edge to pass 2, which interpolates those in FP64
+    const bool df_ok = N <= (1ll << 24);
+    const float nm1 = df_ok ? (float)(int)(N - 1) : 1.f;
+    const float rn = __frcp_rn(nm1);
+    const float extra = ldexpf(warp_max(emax) * (float)s.dim, -30);
+    bool have64 = false;
+    auto load64 = [&]() {   // the reference's q1 and (q2 - q1) / (N - 1), once per edge
+      const double denom = (double)(N - 1);
+      for (int k = lane; k < D; k += 32) {
+        const double a = ldq(q1, dtype, e * D + k), b = ldq(q2, dtype, e * D + k);
+        w64a[k] = a;
+        w64d[k] = __ddiv_rn(__dsub_rn(b, a), denom);
       }
-      if (__any_sync(MRMG_FULL, code == V_COLLIDE)) { coll = true; break; }
-      pending |= __any_sync(MRMG_FULL, code == V_PENDING);
+      __syncwarp();
+      have64 = true;
+    };
+    __syncwarp();
+    if (RESOLVE && !df_ok) load64();
+
+    bool coll = false, pending = false;
+    if (!RESOLVE && !df_ok) {
+      pending = true;
+    } else {
+      BfsChunker ch;
+      ch.init(N);
+      long long v;
+      unsigned m;
+      long long pos0;
+      while (ch.next(lane, &v, &m, &pos0)) {
+        if (pos0 >= nmax) break;
+        const long long my_pos = pos0 + __popc(m & lt_mask);
+        const bool active = v >= 0 && my_pos >= N_start && my_pos < nmax && (incl || (v != 0 && v != N - 1));
+        uint8_t code = V_FREE;
+        if (active) {
+          if (df_ok) {
+            const float fi = (float)(int)v;
+            auto x = [&](int k) {
+              float h, l;
+              interp_df(wah[k], wal[k], wdh[k], wdl[k], fi, nm1, rn, &h, &l);
+              return __fadd_rn(h, l);
+            };
+            code = classify32(s, x, extra);
+          } else {
+            const double di = (double)v;
+            auto x = [&](int k) { return (float)__dadd_rn(w64a[k], __dmul_rn(w64d[k], di)); };
+            code = classify32(s, x, 0.f);
+          }
+        }
+        if (RESOLVE) {
+          unsigned pm = __ballot_sync(MRMG_FULL, code == V_PENDING);
+          if (pm && !have64) load64();
+          while (pm) {
+            const int src = __ffs(pm) - 1;
+            pm &= pm - 1;
+            const double di = (double)__shfl_sync(MRMG_FULL, v, src);
+            auto acc = [&](int k) { return __dadd_rn(w64a[k], __dmul_rn(w64d[k], di)); };
+            const bool ok = exact_free_warp(s, acc, lane);
+            if (lane == src) code = ok ? V_FREE : V_COLLIDE;
+          }
+        }
+        if (__any_sync(MRMG_FULL, code == V_COLLIDE)) { coll = true; break; }
+        if (!RESOLVE) pending |= __any_sync(MRMG_FULL, code == V_PENDING);
+      }
     }
     if (lane == 0) {
       uint8_t r = coll ? V_COLLIDE : (pending ? V_PENDING : V_FREE);
@@ -284,13 +398,20 @@ cudaError_t abstract_edges(const AbstractDev& s, const void* q1, const void* q2,
                            long long N_start, long long N_max, uint8_t* out,
                            const CallScratch& sc, const LaunchShape& ls, cudaStream_t st) {
   const int warps = 8;
-  size_t smem = (size_t)warps * 2 * s.D * sizeof(double);
+  const size_t smem1 = (size_t)warps * edge_warp_bytes(s.D, false);
+  const size_t smem2 = (size_t)warps * edge_warp_bytes(s.D, true);
+  cudaError_t e = cudaSuccess;
+  if (smem1 > 48 * 1024)
+    e = cudaFuncSetAttribute(edges_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  if (e == cudaSuccess && smem2 > 48 * 1024)
+    e = cudaFuncSetAttribute(edges_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+  if (e != cudaSuccess) return e;
   long long want = (n + warps - 1) / warps;
   int grid = (int)(want < (long long)ls.num_sms * 8 ? (want > 0 ? want : 1) : (long long)ls.num_sms * 8);
-  edges_kernel<false><<<grid, warps * 32, smem, st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start,
-                                                      N_max, out, sc.ctr, sc.pend);
-  edges_kernel<true><<<ls.num_sms, warps * 32, smem, st>>>(s, q1, q2, dtype, n, res, incl, Np,
-                                                           N_start, N_max, out, sc.ctr, sc.pend);
+  edges_kernel<false><<<grid, warps * 32, smem1, st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start,
+                                                       N_max, out, sc.ctr, sc.pend);
+  edges_kernel<true><<<ls.num_sms, warps * 32, smem2, st>>>(s, q1, q2, dtype, n, res, incl, Np,
+                                                            N_start, N_max, out, sc.ctr, sc.pend);
   return cudaGetLastError();
 }
 

@@ -852,16 +852,7 @@ __device__ __forceinline__ bool edge_N(const void* q1, const void* q2, int dtype
   if (allow_fast) {
     const float m32 = warp_max(mloc);
     const bool anynan = __any_sync(MRMG_FULL, nanf);
-    const float t32 = __fdiv_rn(m32, res32);
-    if (!anynan && t32 < 4194304.f) {
-      const float fl = floorf(t32);
-      const float fr = t32 - fl;
-      const float tol = 4.8e-7f * fmaxf(t32, 1.f);
-      if (fr > tol && fr < 1.f - tol) {
-        *N_out = max(2, (int)fl + 1);   // through int32: fl < 2^22
-        return true;
-      }
-    }
+    if (steps_fp32(m32, anynan, res32, N_out)) return true;
   }
   double mx = -1.0;
   bool nan0 = false;

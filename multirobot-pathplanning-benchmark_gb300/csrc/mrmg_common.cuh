@@ -236,6 +236,25 @@ __device__ __forceinline__ double warp_max_d(double v) {
   return v;
 }
 
+// Step count N = max(2, int(m / res) + 1) of an edge from FP32 values, when
+// that is certain (abstract_env.py:321-323).  m32 = fl32(m), m the FP64
+// max |q2 - q1| (for FP32 endpoints the FP64 difference is exact), res32 =
+// fl32(res): with both normal, t32 = m32 / res32 lies within a relative
+// 4 * 2^-24 of the FP64 quotient, so when t32 is farther than
+// 4.8e-7 * max(t32, 1) from an integer both have the same integer part.
+// False when that is not shown (the caller divides in FP64).
+__device__ __forceinline__ bool steps_fp32(float m32, bool anynan, float res32, long long* N) {
+  if (anynan || !(res32 >= 0x1p-60f) || !(m32 >= 0x1p-60f)) return false;
+  const float t32 = __fdiv_rn(m32, res32);
+  if (!(t32 < 4194304.f)) return false;
+  const float fl = floorf(t32);
+  const float fr = t32 - fl;
+  const float tol = 4.8e-7f * fmaxf(t32, 1.f);
+  if (!(fr > tol && fr < 1.f - tol)) return false;
+  *N = max(2, (int)fl + 1);   // through int32: fl < 2^22
+  return true;
+}
+
 // Per-item verdict codes written by the FP32 pass.
 enum : uint8_t { V_COLLIDE = 0, V_FREE = 1, V_PENDING = 2 };
 
