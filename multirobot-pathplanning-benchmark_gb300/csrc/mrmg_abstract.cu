@@ -58,7 +58,31 @@ __device__ uint8_t classify_core(const AbstractDev& s, const float* qf, float qm
     const float* c = qf + s.agent_off[i];
     const float r = s.r32[i];
     const float rhi = r + delta, rlo = r - delta;
-    for (int b = 0; b < s.nb; b++) {
+    int b = 0;
+    // two boxes per step (independent chains; any definite collision decides,
+    // so the order of the tests does not change the result)
+    for (; b + 1 < s.nb; b += 2) {
+      const float* lo0 = s.box_lo32 + b * dim;
+      const float* hi0 = s.box_hi32 + b * dim;
+      const float* lo1 = lo0 + dim;
+      const float* hi1 = hi0 + dim;
+      float ss0 = 0.f, ss1 = 0.f;
+      for (int k = 0; k < dim; k++) {
+        const float v0 = fminf(fmaxf(c[k], lo0[k]), hi0[k]) - c[k];
+        const float v1 = fminf(fmaxf(c[k], lo1[k]), hi1[k]) - c[k];
+        ss0 = fmaf(v0, v0, ss0);
+        ss1 = fmaf(v1, v1, ss1);
+      }
+      if (!(ss0 > rhi * rhi)) {
+        if (rlo > 0.f && ss0 < rlo * rlo) return V_COLLIDE;
+        unc = true;
+      }
+      if (!(ss1 > rhi * rhi)) {
+        if (rlo > 0.f && ss1 < rlo * rlo) return V_COLLIDE;
+        unc = true;
+      }
+    }
+    for (; b < s.nb; b++) {
       const float* lo = s.box_lo32 + b * dim;
       const float* hi = s.box_hi32 + b * dim;
       float ss = 0.f;
@@ -161,18 +185,61 @@ __device__ bool exact_free_warp(const AbstractDev& s, Acc acc, int lane) {
 }
 
 // ---------------------------------------------------------------------------
+// The FP32 tables of the bulk pass, staged once per CTA in shared memory when
+// they fit in kTabSmem bytes, so that the classification loop reads no global
+// memory.  Every table holds 4-byte elements; each starts on 16 bytes.
+// ---------------------------------------------------------------------------
+constexpr size_t kTabSmem = 16384;
+
+__host__ __device__ inline size_t tab_pad(size_t n) { return (n * 4 + 15) & ~(size_t)15; }
+
+// bytes of the staged tables, 0 when they are read from global memory
+__host__ __device__ inline size_t tab_bytes(const AbstractDev& s) {
+  const size_t A = s.A, dim = s.dim, nb = s.nb, ns = s.ns;
+  const size_t b = 2 * tab_pad(A) + tab_pad(A * A) + 2 * tab_pad(nb * dim) + tab_pad(ns * dim) + tab_pad(ns * A);
+  return b <= kTabSmem ? b : 0;
+}
+
+template <typename T>
+__device__ __forceinline__ const T* stage(const T* src, size_t n, unsigned char** p) {
+  T* dst = (T*)*p;
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  *p += tab_pad(n);
+  return dst;
+}
+
+// The scene with its FP32 tables in shared memory at `sm` (tab_bytes(s)
+// bytes, in the order tab_bytes counts them); a __syncthreads() must follow.
+__device__ AbstractDev staged_view(const AbstractDev& s, unsigned char* sm) {
+  AbstractDev t = s;
+  if (tab_bytes(s) == 0) return t;
+  unsigned char* p = sm;
+  t.agent_off = stage(s.agent_off, (size_t)s.A, &p);
+  t.r32 = stage(s.r32, (size_t)s.A, &p);
+  t.pair_thr32 = stage(s.pair_thr32, (size_t)s.A * s.A, &p);
+  t.box_lo32 = stage(s.box_lo32, (size_t)s.nb * s.dim, &p);
+  t.box_hi32 = stage(s.box_hi32, (size_t)s.nb * s.dim, &p);
+  t.sph_pos32 = stage(s.sph_pos32, (size_t)s.ns * s.dim, &p);
+  t.sph_thr32 = stage(s.sph_thr32, (size_t)s.ns * s.A, &p);
+  return t;
+}
+
+// ---------------------------------------------------------------------------
 // Configurations: one thread per configuration in pass 1, one warp per
 // pending configuration in pass 2.
 // ---------------------------------------------------------------------------
 __global__ void configs_pass1(AbstractDev s, const void* q, int dtype, long long n, uint8_t* out,
                               int* ctr, long long* pend) {
+  extern __shared__ double sm_cfg[];
+  const AbstractDev cs = staged_view(s, (unsigned char*)sm_cfg);
+  __syncthreads();
   const int D = s.D;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     auto x = [&](int k) {
       return dtype == MRMG_F32 ? ((const float*)q)[i * D + k] : (float)((const double*)q)[i * D + k];
     };
-    uint8_t v = classify32(s, x, 0.f);
+    uint8_t v = classify32(cs, x, 0.f);
     out[i] = v;
     if (v == V_PENDING) {
       int slot = atomicAdd(&ctr[kCtrPending], 1);
@@ -220,7 +287,11 @@ __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int 
   extern __shared__ double sm_ab[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int D = s.D;
-  unsigned char* wbase = (unsigned char*)sm_ab + (size_t)wib * edge_warp_bytes(D, RESOLVE);
+  // pass 1 classifies from staged tables (pass 2 is rare and reads them in place)
+  const size_t tb = RESOLVE ? 0 : tab_bytes(s);
+  const AbstractDev cs = RESOLVE ? s : staged_view(s, (unsigned char*)sm_ab);
+  if (!RESOLVE) __syncthreads();
+  unsigned char* wbase = (unsigned char*)sm_ab + tb + (size_t)wib * edge_warp_bytes(D, RESOLVE);
   double* w64a = (double*)wbase;                 // pass 2 only
   double* w64d = w64a + D;
   float* wah = (float*)(wbase + (RESOLVE ? (size_t)16 * D : 0));
@@ -345,11 +416,11 @@ __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int 
               interp_df(wah[k], wal[k], wdh[k], wdl[k], fi, nm1, rn, &h, &l);
               return __fadd_rn(h, l);
             };
-            code = classify32(s, x, extra);
+            code = classify32(cs, x, extra);
           } else {
             const double di = (double)v;
             auto x = [&](int k) { return (float)__dadd_rn(w64a[k], __dmul_rn(w64d[k], di)); };
-            code = classify32(s, x, 0.f);
+            code = classify32(cs, x, 0.f);
           }
         }
         if (RESOLVE) {
@@ -388,7 +459,7 @@ cudaError_t abstract_configs(const AbstractDev& s, const void* q, int dtype, lon
   int threads = 256;
   long long want = (n + threads - 1) / threads;
   int grid = (int)(want < (long long)ls.num_sms * 8 ? (want > 0 ? want : 1) : (long long)ls.num_sms * 8);
-  configs_pass1<<<grid, threads, 0, st>>>(s, q, dtype, n, out, sc.ctr, sc.pend);
+  configs_pass1<<<grid, threads, tab_bytes(s), st>>>(s, q, dtype, n, out, sc.ctr, sc.pend);
   configs_pass2<<<ls.num_sms, 128, 0, st>>>(s, q, dtype, out, sc.ctr, sc.pend);
   return cudaGetLastError();
 }
@@ -398,7 +469,7 @@ cudaError_t abstract_edges(const AbstractDev& s, const void* q1, const void* q2,
                            long long N_start, long long N_max, uint8_t* out,
                            const CallScratch& sc, const LaunchShape& ls, cudaStream_t st) {
   const int warps = 8;
-  const size_t smem1 = (size_t)warps * edge_warp_bytes(s.D, false);
+  const size_t smem1 = tab_bytes(s) + (size_t)warps * edge_warp_bytes(s.D, false);
   const size_t smem2 = (size_t)warps * edge_warp_bytes(s.D, true);
   cudaError_t e = cudaSuccess;
   if (smem1 > 48 * 1024)
