@@ -1,6 +1,8 @@
 """Host-side logic that needs no GPU: the edge step-count formula of the
-serving batcher, the workload generators, the penetration parameter record
-and the C library's export of the new entry points."""
+serving batcher, the workload generators, the penetration parameter record,
+the C library's export of the new entry points, and the FP32 error bounds
+the kernels rely on (radius pre-test band, step-count certificate,
+double-float edge positions), restated with numpy FP32 arithmetic."""
 import math
 
 import numpy as np
@@ -84,6 +86,87 @@ def test_radius_fp32_band():
         ratio = np.abs(m[:400].astype(np.float64) - exact) / (e * e)
         worst = max(worst, float(ratio.max()))
     assert worst <= 2.4e-6, worst
+
+
+def test_fp32_step_count_certificate():
+    """The edge kernels take N = int(m / res) + 1 from the FP32 quotient
+    fl32(m) / fl32(res) when its fractional part is farther than
+    4.8e-7 * max(t, 1) from an integer (`steps_fp32`); the integer part is
+    then the FP64 quotient's.  Checked with numpy FP32 division on random
+    lengths and on lengths a few ulps around every multiple of res."""
+    rng = np.random.default_rng(5)
+    f32 = np.float32
+    for res in (0.01, 0.05, 0.003, 0.1, 1.0 / 3.0, 0.0125):
+        k = rng.integers(1, 4_000_000, 20_000).astype(np.float64)
+        near = k * res
+        m = np.concatenate([
+            np.exp(rng.uniform(np.log(1e-6), np.log(2e4 * res), 40_000)),
+            near, np.nextafter(near, 0.0), np.nextafter(near, np.inf),
+            near * (1 + 3e-16), near * (1 - 3e-16), near * (1 + 2e-7), near * (1 - 2e-7)])
+        t64 = m / res
+        t32 = (m.astype(f32) / f32(res)).astype(f32)
+        fl = np.floor(t32).astype(f32)
+        fr = (t32 - fl).astype(f32)
+        tol = (f32(4.8e-7) * np.maximum(t32, f32(1.0))).astype(f32)
+        cert = (t32 < f32(4194304.0)) & (m.astype(f32) >= f32(2.0 ** -60)) & (fr > tol) & (fr < f32(1.0) - tol)
+        assert cert[:40_000].mean() > 0.99         # random lengths: the certificate decides
+        assert cert[40_000:60_000].sum() == 0      # exact multiples of res: it declines
+        assert np.array_equal(np.floor(t32[cert]).astype(np.int64), np.floor(t64[cert]).astype(np.int64)), res
+
+
+def _interp_df(ah, al, dh, dl, fi, nm1, rn):
+    """numpy FP32 restatement of interp_df (fused multiply-adds emulated in
+    FP64, then rounded to FP32)."""
+    f32 = np.float32
+
+    def fma(a, b, c):
+        return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(f32)
+
+    def two_sum(a, b):
+        t = (a + b).astype(f32)
+        bb = (t - a).astype(f32)
+        return t, ((a - (t - bb).astype(f32)).astype(f32) + (b - bb).astype(f32)).astype(f32)
+
+    th = (fi * rn).astype(f32)
+    tl = (fma(-th, nm1, fi) * rn).astype(f32)
+    ph = (dh * th).astype(f32)
+    pl = fma(dh, th, -ph)
+    pl = fma(dh, tl, fma(dl, th, pl))
+    sh, sl = two_sum(ah, ph)
+    return sh, (((sl + pl).astype(f32)) + al).astype(f32)
+
+
+def test_double_float_edge_positions_within_band():
+    """Abstract-scene edge positions q1 + (q2 - q1) * i / (N - 1), formed in
+    double-float FP32 and rounded once, lie within 2^-24 |Q| + 2^-42 (|q1| +
+    |q2|) of the reference's FP64 position Q = q1 + ((q2 - q1) / (N - 1)) * i;
+    the kernel's band adds 2^-30 (|q1| + |q2|) per coordinate for the second
+    term.  FP64 and FP32-valued endpoints."""
+    rng = np.random.default_rng(6)
+    f32 = np.float32
+    n = 200_000
+    q1 = rng.uniform(-4, 4, n)
+    q2 = q1 + rng.normal(0, 1.5, n)
+    half = rng.random(n) < 0.5
+    q1 = np.where(half, q1.astype(f32).astype(np.float64), q1)
+    q2 = np.where(half, q2.astype(f32).astype(np.float64), q2)
+    res = rng.choice([0.01, 0.05, 0.003], n)
+    N = np.maximum(2, (np.abs(q2 - q1) / res).astype(np.int64) + 1)
+    i = (rng.random(n) * N).astype(np.int64)
+    d = q2 - q1
+    ah = q1.astype(f32)
+    al = (q1 - ah.astype(np.float64)).astype(f32)
+    dh = d.astype(f32)
+    dl = (d - dh.astype(np.float64)).astype(f32)
+    nm1 = (N - 1).astype(f32)
+    rn = (f32(1.0) / nm1).astype(f32)
+    h, l = _interp_df(ah, al, dh, dl, i.astype(f32), nm1, rn)
+    x = (h + l).astype(f32).astype(np.float64)
+    Q = q1 + (d / (N - 1)) * i
+    S = np.abs(q1) + np.abs(q2)
+    err = np.abs(x - Q)
+    assert np.all(err <= 2.0 ** -24 * np.abs(Q) + 2.0 ** -42 * S)
+    assert np.all(err <= 2.0 ** -24 * np.abs(Q) + 2.0 ** -30 * S)
 
 
 def test_mode_tables_and_views():
