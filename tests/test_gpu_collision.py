@@ -152,6 +152,72 @@ def test_disc_workload_vs_oracle(gpu, oracle):
                           o.edges_free(w["q1"], w["q2"], 0.01))
 
 
+BOUNDARY_EPS = [-1e-6, -1e-9, -1e-12, -1e-15, 0.0, 1e-15, 1e-12, 1e-9, 1e-8, 1e-7, 1e-6, 1e-5]
+
+
+def _face_edges(scene, r):
+    """Edges that slide along each face of each box at distance r + eps from
+    it (their positions over the face are that far from the box), for every
+    eps of BOUNDARY_EPS: inside the FP32 band, so the exact pass decides."""
+    lo = scene.box_center - scene.box_bounds / 2
+    hi = scene.box_center + scene.box_bounds / 2
+    q1, q2 = [], []
+    for b in range(len(lo)):
+        for e in BOUNDARY_EPS:
+            y = hi[b, 1] + r + e
+            q1.append([lo[b, 0] - 0.3, y]); q2.append([hi[b, 0] + 0.3, y])
+            y = lo[b, 1] - r - e
+            q1.append([hi[b, 0] + 0.3, y]); q2.append([lo[b, 0] - 0.3, y])
+            x = hi[b, 0] + r + e
+            q1.append([x, lo[b, 1] - 0.3]); q2.append([x, hi[b, 1] + 0.3])
+            x = lo[b, 0] - r - e
+            q1.append([x, hi[b, 1] + 0.3]); q2.append([x, lo[b, 1] - 0.3])
+    return np.array(q1), np.array(q2)
+
+
+def test_near_boundary_cases_vs_oracle(gpu, oracle):
+    """Configurations and edges placed at distance r + eps from box faces
+    and agent pairs at distance r_i + r_j + eps, eps from -1e-6 to 1e-5
+    (exact contact included): the verdicts of the FP32 band and the FP64
+    re-check equal the oracle's, for FP64 inputs as the reference's."""
+    scenes, col = pkg("scenes"), pkg("collision")
+    base = scenes.make_disc_scene(0)
+    one = scenes.AbstractScene(agent_slices=np.array([[0, 2]]), agent_radii=[0.1], box_center=base.box_center,
+                               box_bounds=base.box_bounds, sphere_pos=np.zeros((0, 2)), sphere_radius=[], q_dim=2)
+    q1, q2 = _face_edges(one, 0.1)
+    o, sc = oracle.OracleScene(one), col.Gb300Scene(one)
+    for incl in (False, True):
+        want = o.edges_free(q1, q2, 0.01, include_endpoints=incl)
+        assert 0.05 < want.mean() < 0.95
+        assert np.array_equal(sc.is_edge_collision_free_batch(q1, q2, 0.01, incl).cpu().numpy(), want), incl
+    cfg = np.concatenate([0.5 * (q1 + q2), q1])
+    want = o.configs_free(cfg)
+    assert 0.05 < want.mean() < 0.95
+    assert np.array_equal(sc.is_collision_free_batch(cfg).cpu().numpy(), want)
+
+    pair = scenes.AbstractScene(agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1],
+                                box_center=np.zeros((0, 2)), box_bounds=np.zeros((0, 2)),
+                                sphere_pos=np.zeros((0, 2)), sphere_radius=[], q_dim=4)
+    rng = np.random.default_rng(3)
+    c, p1, p2 = [], [], []
+    for e in BOUNDARY_EPS:
+        for ang in rng.uniform(0, 2 * np.pi, 8):
+            u = np.array([np.cos(ang), np.sin(ang)])
+            nrm = np.array([-u[1], u[0]])
+            a0 = rng.uniform(-0.5, 0.5, 2)
+            a1 = a0 + nrm * (0.2 + e)
+            c.append(np.concatenate([a0, a1]))
+            p1.append(np.concatenate([a0, a1 - 0.4 * u]))
+            p2.append(np.concatenate([a0, a1 + 0.4 * u]))
+    c, p1, p2 = np.array(c), np.array(p1), np.array(p2)
+    op, sp = oracle.OracleScene(pair), col.Gb300Scene(pair)
+    want = op.configs_free(c)
+    assert 0.05 < want.mean() < 0.95
+    assert np.array_equal(sp.is_collision_free_batch(c).cpu().numpy(), want)
+    want = op.edges_free(p1, p2, 0.01, include_endpoints=True)
+    assert np.array_equal(sp.is_edge_collision_free_batch(p1, p2, 0.01, True).cpu().numpy(), want)
+
+
 def test_edge_errors(gpu):
     g = golden("abstract_disc.npz")
     sc = pkg("collision").Gb300Scene(_disc_scene(g))
