@@ -17,7 +17,12 @@ one CUDA graph launch:
 
 The graph copies the packed endpoints and counts host->device, runs the
 persistent edge pipeline once over the whole step, and copies the verdicts
-back.  Graphs are cached per capacity bucket (configurations and edges
+back.  The staging buffers hold FP32 endpoints (half the copy of FP64): the
+verdicts (and step counts N) are the reference's for the FP32 values, so
+FP64 requests are rounded to FP32 first.  Callers that need the FP64
+verdicts of FP64 configurations use
+``Gb300Scene`` / the env methods, or ``EdgeCheckPlan`` with its default
+FP64 buffers.  Graphs are cached per capacity bucket (configurations and edges
 rounded up to a quantum).  ``autotune_launch`` picks the persistent grid
 (CTAs per SM, warps per CTA) by timing candidates on a sample step; the
 verdicts never depend on it.
