@@ -17,6 +17,19 @@ def _slices_arr(slices) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(slices, dtype=np.int64).reshape(-1, 2))
 
 
+def _query_modes(query_mode, Q: int) -> np.ndarray:
+    """One int32 mode per query (the library reads exactly Q of them); a
+    single mode applies to every query."""
+    if isinstance(query_mode, torch.Tensor):
+        query_mode = query_mode.detach().cpu().numpy()
+    qm = np.asarray(query_mode, dtype=np.int32).reshape(-1)
+    if qm.shape[0] == 1 and Q != 1:
+        qm = np.repeat(qm, Q)
+    if qm.shape[0] != Q:
+        raise ValueError(f"one mode per query: {qm.shape[0]} modes for {Q} queries")
+    return np.ascontiguousarray(qm, dtype=np.int32)
+
+
 def knn_exact(queries, query_mode, nodes, mode_offsets, slices, metric: str, k: int, stream=None):
     """Exact FP64 k-NN (warp per query).  Returns (idx int64 [Q, k], dist float64 [Q, k]) on the device."""
     lib = _lib.load()
@@ -91,12 +104,11 @@ class NodeStore:
         """Appends rows [n, D] (host or device) to ``mode``; their mode-local
         indices continue the mode's insertion order."""
         if isinstance(rows, torch.Tensor):
-            t = rows.detach().to(torch.float64).contiguous()
-            if t.dim() == 1:
-                t = t.unsqueeze(0)
-            ptr, n, keep = t.data_ptr(), t.shape[0], t
+            t = rows.detach().to(torch.float64)
             if t.shape[-1] != self.D:
                 raise ValueError(f"rows must have {self.D} columns")
+            t = t.reshape(-1, self.D).contiguous()
+            ptr, n, keep = t.data_ptr(), t.shape[0], t
         else:
             a = np.ascontiguousarray(np.asarray(rows, dtype=np.float64).reshape(-1, self.D))
             ptr, n, keep = a.ctypes.data, a.shape[0], a
@@ -141,14 +153,14 @@ class NodeStore:
         if isinstance(queries, torch.Tensor) and queries.is_cuda:
             qs = _dev_tensor(queries, dtype=torch.float64)
             return qs.data_ptr(), qs.shape[0], qs, qs.device
-        a = queries.numpy() if isinstance(queries, torch.Tensor) else queries
+        a = queries.detach().numpy() if isinstance(queries, torch.Tensor) else queries
         a = np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1, self.D))
         return a.ctypes.data, a.shape[0], a, torch.device("cuda", torch.cuda.current_device())
 
     def knn(self, queries, query_mode, k: int, stream=None):
         """(idx [Q, k] int64, dist [Q, k] float64) on the device; idx local to the mode."""
         ptr, Q, keep, dev = self._queries(queries)
-        qm = np.ascontiguousarray(np.asarray(query_mode, dtype=np.int32))
+        qm = _query_modes(query_mode, Q)
         idx = torch.empty((Q, k), dtype=torch.int64, device=dev)
         dist = torch.empty((Q, k), dtype=torch.float64, device=dev)
         st = np.zeros(2, dtype=np.int64)
@@ -167,9 +179,7 @@ class NodeStore:
         tensors (offsets [Q + 1], idx [total], dist [total] float64; dist is
         None when ``distances`` is False)."""
         ptr, Q, keep, dev = self._queries(queries)
-        qm = np.ascontiguousarray(np.asarray(query_mode, dtype=np.int32).reshape(-1))
-        if qm.shape[0] != Q:
-            raise ValueError("one mode per query")
+        qm = _query_modes(query_mode, Q)
         r = np.ascontiguousarray(np.broadcast_to(np.asarray(radius, dtype=np.float64), (Q,)))
         if cap is None:
             cap = max(1024, 64 * Q)

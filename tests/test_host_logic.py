@@ -169,6 +169,23 @@ def test_double_float_edge_positions_within_band():
     assert np.all(err <= 2.0 ** -24 * np.abs(Q) + 2.0 ** -30 * S)
 
 
+def test_query_modes_one_per_query():
+    """NodeStore queries hand the library exactly Q int32 modes: a single
+    mode applies to every query, any other count is refused (the library
+    would read past a short array)."""
+    qmodes = pkg("knn")._query_modes
+    assert qmodes([2, 0, 1], 3).tolist() == [2, 0, 1] and qmodes([2, 0, 1], 3).dtype == np.int32
+    assert qmodes(4, 3).tolist() == [4, 4, 4] and qmodes([4], 2).tolist() == [4, 4]
+    assert qmodes(np.array([1, 2], dtype=np.int64), 2).flags["C_CONTIGUOUS"]
+    assert qmodes([], 0).shape == (0,) and qmodes(3, 0).shape == (0,)
+    import torch
+
+    assert qmodes(torch.tensor([1, 0]), 2).tolist() == [1, 0]
+    for bad, Q in (([1, 2], 3), ([1, 2, 3], 2), ([], 1)):
+        with pytest.raises(ValueError):
+            qmodes(bad, Q)
+
+
 def test_mode_tables_and_views():
     """Per-mode scene declarations: the flat arrays the library receives and
     the reduced scene a mode sees (its boxes, robot spheres plus the attached
