@@ -43,12 +43,22 @@ class AbstractScene:
         """Exact FP64 tables computed with the reference's own expressions."""
         A = len(self.agent_radii)
         dim = self.dim
+        if np.shape(self.agent_slices) != (A, 2):
+            raise ValueError(f"agent_slices {np.shape(self.agent_slices)} must be [{A}, 2] (one per agent radius)")
         for s, e in self.agent_slices:
             if e - s != dim:
                 raise ValueError("all agents must have the obstacle dimension")
+        nb = np.size(self.box_center) // max(dim, 1)
+        if np.size(self.box_center) != nb * dim or np.size(self.box_bounds) != nb * dim:
+            raise ValueError(f"box_center {np.shape(self.box_center)} and box_bounds {np.shape(self.box_bounds)} "
+                             f"must both be [nb, {dim}]")
+        if np.size(self.sphere_pos) != len(self.sphere_radius) * dim:
+            raise ValueError(f"sphere_pos {np.shape(self.sphere_pos)} must be [{len(self.sphere_radius)}, {dim}]")
         # Rectangle.__init__ (abstract_env.py:66-67)
-        lo = self.box_center - self.box_bounds / 2
-        hi = self.box_center + self.box_bounds / 2
+        bc = np.asarray(self.box_center, dtype=np.float64).reshape(-1, dim)
+        bb = np.asarray(self.box_bounds, dtype=np.float64).reshape(-1, dim)
+        lo = bc - bb / 2
+        hi = bc + bb / 2
         pair = np.zeros((A, A))
         for i in range(A):
             for j in range(A):
@@ -134,10 +144,18 @@ class ArmScene:
     def n_modes(self) -> int:
         return 0 if self.mode_boxes is None else len(self.mode_boxes)
 
+    def _mode_attach(self) -> list:
+        """Attached-object ids per mode (none when ``mode_attach`` is None)."""
+        if self.mode_attach is None:
+            return [[] for _ in range(self.n_modes)]
+        if len(self.mode_attach) != self.n_modes:
+            raise ValueError(f"mode_attach has {len(self.mode_attach)} entries for {self.n_modes} modes")
+        return list(self.mode_attach)
+
     def for_mode(self, m: int) -> "ArmScene":
         """The scene as mode ``m`` sees it: its boxes and the spheres present."""
         att = np.full(len(self.sphere_radius), -1) if self.sphere_attach is None else np.asarray(self.sphere_attach)
-        on = (att < 0) | np.isin(att, np.asarray(self.mode_attach[m], dtype=np.int64))
+        on = (att < 0) | np.isin(att, np.asarray(self._mode_attach()[m], dtype=np.int64))
         bx = np.asarray(self.mode_boxes[m], dtype=np.int64)
         return ArmScene(
             q_offset=self.q_offset, base_kind=self.base_kind, base_pose=self.base_pose, n_links=self.n_links,
@@ -150,8 +168,11 @@ class ArmScene:
         """Flat arrays for the library: attachment ids and per-mode lists."""
         S = len(self.sphere_radius)
         att = np.full(S, -1, dtype=np.int32) if self.sphere_attach is None else np.asarray(self.sphere_attach, np.int32)
+        if att.shape != (S,):
+            raise ValueError(f"sphere_attach {att.shape} must hold one id per sphere ({S})")
+        attach = self._mode_attach()
         bl = [np.asarray(b, dtype=np.int32).reshape(-1) for b in self.mode_boxes]
-        al = [np.asarray(a, dtype=np.int32).reshape(-1) for a in self.mode_attach]
+        al = [np.asarray(a, dtype=np.int32).reshape(-1) for a in attach]
         off = lambda ls: np.concatenate([[0], np.cumsum([len(x) for x in ls])]).astype(np.int64)
         cat = lambda ls: np.ascontiguousarray(np.concatenate(ls) if ls else np.zeros(0), dtype=np.int32)
         return dict(sphere_attach=np.ascontiguousarray(att), box_off=off(bl), boxes=cat(bl), attach_off=off(al),
@@ -164,19 +185,35 @@ class ArmScene:
         return np.array([[o, o + d] for o, d in zip(self.q_offset, self.robot_dofs())], dtype=np.int64)
 
     def arrays(self) -> dict:
-        return dict(
-            q_offset=np.ascontiguousarray(self.q_offset, dtype=np.int32),
-            base_kind=np.ascontiguousarray(self.base_kind, dtype=np.int32),
+        """Flat arrays for the library, their shapes checked against the robot,
+        sphere and box counts (the library reads exactly that many values)."""
+        R = len(self.q_offset)
+        S = len(self.sphere_radius)
+        a = dict(
+            q_offset=np.ascontiguousarray(self.q_offset, dtype=np.int32).reshape(-1),
+            base_kind=np.ascontiguousarray(self.base_kind, dtype=np.int32).reshape(-1),
             base_pose=np.ascontiguousarray(self.base_pose, dtype=np.float64),
-            n_links=np.ascontiguousarray(self.n_links, dtype=np.int32),
+            n_links=np.ascontiguousarray(self.n_links, dtype=np.int32).reshape(-1),
             dh=np.ascontiguousarray(self.dh, dtype=np.float64),
-            sphere_robot=np.ascontiguousarray(self.sphere_robot, dtype=np.int32),
-            sphere_link=np.ascontiguousarray(self.sphere_link, dtype=np.int32),
+            sphere_robot=np.ascontiguousarray(self.sphere_robot, dtype=np.int32).reshape(-1),
+            sphere_link=np.ascontiguousarray(self.sphere_link, dtype=np.int32).reshape(-1),
             sphere_local=np.ascontiguousarray(self.sphere_local, dtype=np.float64),
-            sphere_radius=np.ascontiguousarray(self.sphere_radius, dtype=np.float64),
-            box_lo=np.ascontiguousarray(self.box_lo, dtype=np.float64).reshape(-1, 3),
-            box_hi=np.ascontiguousarray(self.box_hi, dtype=np.float64).reshape(-1, 3),
+            sphere_radius=np.ascontiguousarray(self.sphere_radius, dtype=np.float64).reshape(-1),
+            box_lo=np.ascontiguousarray(self.box_lo, dtype=np.float64),
+            box_hi=np.ascontiguousarray(self.box_hi, dtype=np.float64),
         )
+        want = dict(q_offset=(R,), base_kind=(R,), base_pose=(R, 12), n_links=(R,), dh=(R, MAX_LINKS, 4),
+                    sphere_robot=(S,), sphere_link=(S,), sphere_local=(S, 3), sphere_radius=(S,))
+        for k, shape in want.items():
+            if a[k].size != int(np.prod(shape)):
+                raise ValueError(f"ArmScene.{k}: {a[k].shape} does not hold {shape} values")
+            a[k] = a[k].reshape(shape)
+        if a["box_lo"].size % 3 or a["box_lo"].size != a["box_hi"].size:
+            raise ValueError(f"ArmScene boxes: box_lo {a['box_lo'].shape} and box_hi {a['box_hi'].shape} "
+                             "must both be [B, 3]")
+        a["box_lo"] = a["box_lo"].reshape(-1, 3)
+        a["box_hi"] = a["box_hi"].reshape(-1, 3)
+        return a
 
 
 def _rz(theta: float) -> np.ndarray:

@@ -186,6 +186,50 @@ def test_query_modes_one_per_query():
             qmodes(bad, Q)
 
 
+def test_scene_arrays_refuse_inconsistent_shapes():
+    """The library reads exactly the robot, sphere and box counts it is given:
+    scene arrays whose shapes disagree with those counts are refused on the
+    host with ValueError, before any library call."""
+    import copy
+
+    scenes = pkg("scenes")
+    arm = scenes.make_arm_scene(0)
+    a = arm.arrays()
+    assert a["base_pose"].shape == (4, 12) and a["dh"].shape == (4, scenes.MAX_LINKS, 4)
+    assert a["sphere_local"].shape == (168, 3) and a["box_lo"].shape == (50, 3)
+    for field, value in (("base_pose", arm.base_pose[:, :9]), ("dh", arm.dh[:, :7]),
+                         ("sphere_local", arm.sphere_local[:-1]), ("sphere_robot", arm.sphere_robot[:-1]),
+                         ("sphere_link", arm.sphere_link[:, None].repeat(2, 1)), ("base_kind", arm.base_kind[:3]),
+                         ("box_hi", arm.box_hi[:-1]), ("box_lo", arm.box_lo[:, :2])):
+        bad = copy.deepcopy(arm)
+        setattr(bad, field, value)
+        with pytest.raises(ValueError):
+            bad.arrays()
+    modes = scenes.make_arm_mode_scene(1, n_objects=4, n_modes=3)
+    modes.mode_tables()
+    bad = copy.deepcopy(modes)
+    bad.mode_attach = bad.mode_attach[:2]
+    with pytest.raises(ValueError):
+        bad.mode_tables()
+    bad = copy.deepcopy(modes)
+    bad.sphere_attach = np.asarray(bad.sphere_attach)[:-1]
+    with pytest.raises(ValueError):
+        bad.mode_tables()
+    no_attach = copy.deepcopy(modes)
+    no_attach.sphere_attach, no_attach.mode_attach = None, None
+    t = no_attach.mode_tables()
+    assert t["attach_off"].tolist() == [0, 0, 0, 0] and (t["sphere_attach"] == -1).all()
+
+    disc = scenes.make_disc_scene(0)
+    assert disc.tables()["box_lo"].shape == (10, 2)
+    for field, value in (("box_bounds", disc.box_bounds[:-1]), ("box_center", disc.box_center[:, :1]),
+                         ("agent_slices", disc.agent_slices[:1]), ("sphere_pos", np.zeros((1, 2)))):
+        bad = copy.deepcopy(disc)
+        setattr(bad, field, value)
+        with pytest.raises(ValueError):
+            bad.tables()
+
+
 def test_mode_tables_and_views():
     """Per-mode scene declarations: the flat arrays the library receives and
     the reduced scene a mode sees (its boxes, robot spheres plus the attached
