@@ -56,15 +56,22 @@ def _cost(starts, ends, slices, metric, reduction, w, mode) -> torch.Tensor:
     lib = _lib.load()
     a = _dev_tensor(starts, dtype=torch.float64)
     b = None if ends is None else _dev_tensor(ends, dtype=torch.float64, device=a.device)
+    if mode == 1 and b.shape != a.shape:
+        # diff = starts - batch_other with numpy broadcasting (configuration.py:457-459)
+        try:
+            a, b = torch.broadcast_tensors(a, b)
+        except RuntimeError:
+            raise ValueError("operands could not be broadcast together") from None
+        a, b = a.contiguous(), b.contiguous()
     D = a.shape[-1]
     if mode == 0:
-        M = b.reshape(-1, D).shape[0]
-    elif mode == 1:
-        M = a.shape[0]
-        if b.shape != a.shape:
+        if b.shape[-1] != D:
             raise ValueError("operands could not be broadcast together")
+        M = b.reshape(-1, D).shape[0]
     else:
-        M = a.shape[0] - 1
+        if a.dim() != 2:   # the reference indexes diff[:, s:e]
+            raise ValueError(f"cost operands must be [M, D] arrays, got {tuple(a.shape)}")
+        M = a.shape[0] if mode == 1 else a.shape[0] - 1
     sl = _slices_arr(slices)
     out = torch.empty(max(M, 0), dtype=torch.float64, device=a.device)
     cm = _lib.COST_METRICS["euclidean" if metric == "euclidean" else "max"]

@@ -35,6 +35,15 @@ def test_batch_config_cost_golden(gpu, tag):
                                   g[f"{tag}_rowcost_{metric}_{red}"])
             assert np.array_equal(cfg.batch_config_cost(list(pts[:100]), None, metric, red, tmp_agent_slice=sl),
                                   g[f"{tag}_pathcost_{metric}_{red}"])
+            # ndarray x ndarray broadcasts as `starts - batch_other` does (one row against many,
+            # either way round: |d| and d*d do not see the sign)
+            want = g[f"{tag}_cost_{metric}_{red}"]
+            assert np.array_equal(cfg.batch_config_cost(pt, pts, metric, red, tmp_agent_slice=sl), want)
+            assert np.array_equal(cfg.batch_config_cost(pts, pt[None], metric, red, tmp_agent_slice=sl), want)
+    with pytest.raises(ValueError):      # a 1-D difference: the reference's diff[:, s:e] fails too
+        cfg.batch_config_cost(pt, pts[0], "max", "max", tmp_agent_slice=sl)
+    with pytest.raises(ValueError):
+        cfg.batch_config_cost(pts[:3], pts[:2], "max", "max", tmp_agent_slice=sl)
     # path_cost (problems/util.py:51-67): per-edge costs, then np.sum
     costs = g[f"{tag}_pathcost_euclidean_max"]
     assert cfg.path_cost(list(pts[:100]), lambda a, b, tmp_agent_slice: cfg.batch_config_cost(
