@@ -33,14 +33,26 @@ def _query_modes(query_mode, Q: int) -> np.ndarray:
 def knn_exact(queries, query_mode, nodes, mode_offsets, slices, metric: str, k: int, stream=None):
     """Exact FP64 k-NN (warp per query).  Returns (idx int64 [Q, k], dist float64 [Q, k]) on the device."""
     lib = _lib.load()
-    qs = _dev_tensor(queries, dtype=torch.float64)
+    qshape, nshape = tuple(np.shape(queries)), tuple(np.shape(nodes))
+    if len(qshape) == 1:
+        qshape = (1,) + qshape
+    if len(qshape) != 2 or len(nshape) != 2 or nshape[1] != qshape[1]:
+        raise ValueError(f"queries {qshape} and nodes {nshape} must be [Q, D] and [M, D]")
+    Q, D = qshape
+    # the kernel reads the offsets of each query's mode without a bound: check
+    # modes and offsets here (host copies of device arguments)
+    qm_h = _query_modes(query_mode, Q)
+    mo_h = np.asarray(mode_offsets.detach().cpu().numpy() if isinstance(mode_offsets, torch.Tensor) else mode_offsets,
+                      dtype=np.int64).reshape(-1)
+    if mo_h.shape[0] < 2 or mo_h[0] != 0 or mo_h[-1] != nshape[0] or np.any(np.diff(mo_h) < 0):
+        raise ValueError("mode_offsets must rise from 0 to the number of nodes")
+    if Q and (qm_h.min() < 0 or qm_h.max() >= mo_h.shape[0] - 1):
+        raise ValueError("query mode out of range")
+    qs = _dev_tensor(queries, dtype=torch.float64).reshape(Q, D)
     nd = _dev_tensor(nodes, dtype=torch.float64, device=qs.device)
-    qm = torch.as_tensor(np.asarray(query_mode, dtype=np.int32) if not isinstance(query_mode, torch.Tensor)
-                         else query_mode.to(torch.int32)).to(qs.device).contiguous()
-    mo = torch.as_tensor(np.asarray(mode_offsets, dtype=np.int64) if not isinstance(mode_offsets, torch.Tensor)
-                         else mode_offsets.to(torch.int64)).to(qs.device).contiguous()
+    qm = torch.from_numpy(qm_h).to(qs.device)
+    mo = torch.from_numpy(np.ascontiguousarray(mo_h)).to(qs.device)
     sl = _slices_arr(slices)
-    Q, D = qs.shape
     idx = torch.empty((Q, k), dtype=torch.int64, device=qs.device)
     dist = torch.empty((Q, k), dtype=torch.float64, device=qs.device)
     _lib.check(lib.mrmg_knn_exact(qs.data_ptr(), Q, qm.data_ptr(), nd.data_ptr(), mo.data_ptr(), D, sl.ctypes.data,

@@ -186,6 +186,20 @@ def test_query_modes_one_per_query():
             qmodes(bad, Q)
 
 
+def test_knn_exact_refuses_bad_modes_on_the_host(cuda_lib):
+    """knn_exact's kernel reads the offsets of each query's mode without a
+    bound, so modes and offsets are checked before anything reaches the
+    device (these raise without a GPU)."""
+    knn = pkg("knn")
+    nodes, qs, sl = np.zeros((10, 4)), np.zeros((3, 4)), [[0, 2], [2, 4]]
+    for qm, off in (([0, 1, 2], [0, 5, 10]), ([0, -1, 1], [0, 5, 10]), ([0, 0], [0, 5, 10]),
+                    ([0, 0, 0], [0, 5, 9]), ([0, 0, 0], [1, 5, 10]), ([0, 0, 0], [0, 6, 5, 10]), ([0, 0, 0], [0])):
+        with pytest.raises(ValueError):
+            knn.knn_exact(qs, qm, nodes, off, sl, "euclidean", 1)
+    with pytest.raises(ValueError):
+        knn.knn_exact(np.zeros((3, 5)), [0, 0, 0], nodes, [0, 10], sl, "euclidean", 1)
+
+
 def test_scene_arrays_refuse_inconsistent_shapes():
     """The library reads exactly the robot, sphere and box counts it is given:
     scene arrays whose shapes disagree with those counts are refused on the
