@@ -35,6 +35,17 @@ def _dev_tensor(x, dtype=None, device=None):
     return t.to(device or "cuda")
 
 
+def _out_tensor(out, n: int, device) -> torch.Tensor:
+    """The verdict buffer: a new one, or the caller's (a contiguous uint8
+    device tensor with room for n verdicts; the kernels write n bytes)."""
+    if out is None:
+        return torch.empty(n, dtype=torch.uint8, device=device)
+    if not isinstance(out, torch.Tensor) or out.dtype != torch.uint8 or not out.is_cuda or not out.is_contiguous() \
+            or out.numel() < n:
+        raise ValueError(f"out must be a contiguous uint8 CUDA tensor of at least {n} elements")
+    return out
+
+
 def _dt_code(t: torch.Tensor) -> int:
     if t.dtype == torch.float32:
         return _lib.MRMG_F32
@@ -147,8 +158,7 @@ class Gb300Scene:
         if qt.shape[-1] != self.q_dim:
             raise ValueError(f"configurations must have {self.q_dim} coordinates")
         n = qt.shape[0]
-        if out is None:
-            out = torch.empty(n, dtype=torch.uint8, device=qt.device)
+        out = _out_tensor(out, n, qt.device)
         _lib.check(self.lib.mrmg_is_collision_free_batch(self.h, qt.data_ptr(), _dt_code(qt), n, out.data_ptr(),
                                                          _lib.stream_handle(stream), flags), "is_collision_free")
         return out
@@ -165,8 +175,7 @@ class Gb300Scene:
         if qt.shape[-1] != self.q_dim:
             raise ValueError(f"configurations must have {self.q_dim} coordinates")
         n = qt.shape[0]
-        if out is None:
-            out = torch.empty(n, dtype=torch.uint8, device=qt.device)
+        out = _out_tensor(out, n, qt.device)
         _lib.check(self.lib.mrmg_is_collision_free_batch_robots(self.h, qt.data_ptr(), _dt_code(qt), n,
                                                                 int(robot_mask), out.data_ptr(),
                                                                 _lib.stream_handle(stream), flags),
@@ -185,10 +194,20 @@ class Gb300Scene:
         n = a.shape[0]
         Nt = None
         if N is not None:
-            Nt = _dev_tensor(np.asarray(N, dtype=np.int64).reshape(-1), dtype=torch.int64, device=a.device) \
-                if not isinstance(N, torch.Tensor) else N.to(device=a.device, dtype=torch.int64).contiguous()
-        if out is None:
-            out = torch.empty(n, dtype=torch.uint8, device=a.device)
+            # one step count per edge (the kernel reads N[e] for every edge); a single one applies to all
+            if isinstance(N, torch.Tensor):
+                Nt = N.to(device=a.device, dtype=torch.int64).reshape(-1)
+                if Nt.numel() == 1 and n != 1:
+                    Nt = Nt.expand(n)
+                Nt = Nt.contiguous()
+            else:
+                Nh = np.asarray(N, dtype=np.int64).reshape(-1)
+                if Nh.shape[0] == 1 and n != 1:
+                    Nh = np.repeat(Nh, n)
+                Nt = _dev_tensor(Nh, dtype=torch.int64, device=a.device)
+            if Nt.numel() != n:
+                raise ValueError(f"N must hold one step count per edge: {Nt.numel()} for {n} edges")
+        out = _out_tensor(out, n, a.device)
         rc = self.lib.mrmg_is_edge_collision_free_batch(
             self.h, a.data_ptr(), b.data_ptr(), _dt_code(a), n, float(resolution if resolution is not None else 0.0),
             int(bool(include_endpoints)), None if Nt is None else Nt.data_ptr(), int(N_start),

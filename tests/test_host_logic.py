@@ -200,6 +200,19 @@ def test_knn_exact_refuses_bad_modes_on_the_host(cuda_lib):
         knn.knn_exact(np.zeros((3, 5)), [0, 0, 0], nodes, [0, 10], sl, "euclidean", 1)
 
 
+def test_verdict_buffer_is_checked():
+    """A caller's verdict buffer must be a contiguous uint8 CUDA tensor with
+    room for every verdict (the kernels write n bytes); anything else is
+    refused before a launch."""
+    import torch
+
+    out_tensor = pkg("collision")._out_tensor
+    for bad in (np.zeros(4, dtype=np.uint8), torch.zeros(4, dtype=torch.uint8),
+                torch.zeros(4, dtype=torch.int32), torch.zeros((4, 2), dtype=torch.uint8)[:, 0]):
+        with pytest.raises(ValueError):
+            out_tensor(bad, 4, None)
+
+
 def test_scene_arrays_refuse_inconsistent_shapes():
     """The library reads exactly the robot, sphere and box counts it is given:
     scene arrays whose shapes disagree with those counts are refused on the
