@@ -44,6 +44,9 @@ def config_dist_matrix(queries, nodes, slices, metric: str = "euclidean", out=No
     sl = _slices_arr(slices)
     if out is None:
         out = torch.empty((qs.shape[0], nd.shape[0]), dtype=torch.float64, device=qs.device)
+    elif not isinstance(out, torch.Tensor) or out.dtype != torch.float64 or not out.is_cuda \
+            or not out.is_contiguous() or out.numel() < qs.shape[0] * nd.shape[0]:
+        raise ValueError(f"out must be a contiguous float64 CUDA tensor of {qs.shape[0]} x {nd.shape[0]} elements")
     _lib.check(lib.mrmg_config_dist_matrix(qs.data_ptr(), qs.shape[0], nd.data_ptr(), nd.shape[0], D, sl.ctypes.data,
                                            len(sl), _lib.METRICS[metric], out.data_ptr(), _lib.stream_handle(stream), 0),
                "config_dist_matrix")
