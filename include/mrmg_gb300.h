@@ -189,7 +189,11 @@ int mrmg_is_collision_free_batch_robots(mrmg_scene *scene, const void *d_q, int3
  *   indices generate_binary_search_indices(N)[N_start : min(N, N_max)]
  *   (planning_env.py:34-51), endpoints 0 and N-1 skipped unless
  *   include_endpoints, q = q1 + ((q2 - q1) / (N - 1)) * i in FP64.
- * d_N may be NULL; N_max < 0 means None.  N_start > N gives MRMG_ERR_N_START. */
+ * d_N may be NULL; N_max < 0 means None.  N_start > N gives MRMG_ERR_N_START.
+ * Buffers (device memory, not checked by the library): d_q1 and d_q2 hold
+ * n * q_dim values of `dtype`, d_N (when given) n int64 step counts, d_out n
+ * bytes.  The same holds for every batched call: d_q[n, q_dim] in, d_out[n]
+ * out. */
 int mrmg_is_edge_collision_free_batch(mrmg_scene *scene, const void *d_q1, const void *d_q2,
                                       int32_t dtype, int64_t n, double resolution,
                                       int32_t include_endpoints, const int64_t *d_N,
@@ -314,7 +318,10 @@ int mrmg_batch_config_cost(const double *d_starts, const double *d_ends, int64_t
  * with k = 1, RRT nearest (planners/rrtstar_base.py:1228-1254, argmin).
  *   d_query_mode[Q]: mode of each query; d_mode_offsets[n_modes + 1]: the
  *   node range of each mode in d_nodes[M, D]; indices are local to the mode.
- *   Rows beyond the mode's size get index -1 and distance +inf.  k <= 64. */
+ *   Rows beyond the mode's size get index -1 and distance +inf.  k <= 64.
+ *   The device arrays are read as given: every d_query_mode value must lie
+ *   in [0, n_modes) and d_mode_offsets must rise from 0 to M (the Python
+ *   binding checks both on the host). */
 int mrmg_knn_exact(const double *d_queries, int64_t Q, const int32_t *d_query_mode,
                    const double *d_nodes, const int64_t *d_mode_offsets, int32_t D,
                    const int64_t *h_slices, int32_t A, int32_t metric, int32_t k, int64_t *d_idx,
