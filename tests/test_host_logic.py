@@ -8,7 +8,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import pkg
+from conftest import golden, pkg
 
 
 def test_edge_steps_matches_reference_formula():
@@ -198,6 +198,47 @@ def test_knn_exact_refuses_bad_modes_on_the_host(cuda_lib):
             knn.knn_exact(qs, qm, nodes, off, sl, "euclidean", 1)
     with pytest.raises(ValueError):
         knn.knn_exact(np.zeros((3, 5)), [0, 0, 0], nodes, [0, 10], sl, "euclidean", 1)
+
+
+def test_path_check_covers_the_reference_calls():
+    """tests/test.py:93-122 of the reference counts the is_collision_free calls
+    of is_path_collision_free on a three-state path: 5 at resolution 0.5 and
+    21 at 0.1, with and without check_edges_in_order.  The batched path check
+    submits the same configurations at once: the checked vertices and the
+    interior of every edge.  A stand-in for the device scene counts them."""
+    import torch
+
+    envm = pkg("env")
+    ka = golden("known_answers.json")
+
+    class CountingScene:
+        mode = -1
+
+        def __init__(self):
+            self.configs = 0
+
+        def is_collision_free_batch(self, qs):
+            self.configs += len(qs)
+            return torch.ones(len(qs), dtype=torch.uint8)
+
+        def is_edge_collision_free_batch(self, q1s, q2s, resolution, include_endpoints=False, N=None):
+            assert not include_endpoints and N is None
+            self.configs += sum(envm._edge_N(a, b, resolution) - 2 for a, b in zip(q1s, q2s))
+            return torch.ones(len(q1s), dtype=torch.uint8)
+
+    env = object.__new__(envm.Gb300AbstractEnvironment)
+
+    class S:
+        def __init__(self, q):
+            self.q, self.mode = np.array(q, dtype=np.float64), None
+
+    path = [S([-1, 0, 1, 1]), S([-1, 1, 1, 0]), S([-1, 2, 1, -1])]
+    counts = []
+    for res, in_order in ((0.5, True), (0.5, False), (0.1, True), (0.1, False)):
+        env._gb300 = CountingScene()
+        assert env.is_path_collision_free(path, resolution=res, check_edges_in_order=in_order)
+        counts.append(env._gb300.configs)
+    assert counts == ka["path_calls"]
 
 
 def test_verdict_buffer_is_checked():
