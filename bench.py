@@ -884,8 +884,9 @@ def _profile_traffic():
 
 def run_profile(args):
     """Short run for ncu: the first-pass edge kernel on the benchmark workload,
-    early-exit ('early') or full-evaluation ('full') mode, or the per-mode k-NN
-    batch ('knn', euclidean), `--steps` launches."""
+    early-exit ('early') or full-evaluation ('full') mode, the per-mode k-NN
+    batch ('knn', euclidean), radius queries ('near'), the penetration cost
+    ('pen') or the two-disc scene's calls ('abstract'), `--steps` times."""
     import torch
 
     if args.profile == "knn":
@@ -914,6 +915,24 @@ def run_profile(args):
         torch.cuda.synchronize()
         print(json.dumps({"profile": "near", "launches": args.steps, "s": time.perf_counter() - t0,
                           "neighbours": int(offs[-1].item())}), flush=True)
+        return 0
+
+    if args.profile == "abstract":
+        # the two-disc scene's synchronous calls: 1,000 edges at 0.01 and
+        # 10,000 configurations per step (edges_kernel / configs_pass launches)
+        col, scenes = pkg("collision"), pkg("scenes")
+        s = col.Gb300Scene(scenes.make_disc_scene(0))
+        rng = np.random.default_rng(0)
+        qd = torch.from_numpy(rng.uniform(-1, 1, (10_000, 4))).cuda()
+        q1d = torch.from_numpy(rng.uniform(-1, 1, (1000, 4))).cuda()
+        q2d = torch.from_numpy(rng.uniform(-1, 1, (1000, 4))).cuda()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e = s.is_edge_collision_free_batch(q1d, q2d, 0.01)
+            v = s.is_collision_free_batch(qd)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "abstract", "launches": 4 * args.steps, "s": time.perf_counter() - t0,
+                          "free_edges": int(e.sum().item()), "free_configs": int(v.sum().item())}), flush=True)
         return 0
 
     if args.profile == "pen":
@@ -955,8 +974,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--chunks", type=int, default=1, help="pipelined chunks of the end-to-end plan")
     ap.add_argument("--skip-extra", action="store_true", help="only the headline edge-check workload")
-    ap.add_argument("--profile", choices=["early", "full", "knn", "near", "pen"], default=None,
-                    help="short run of the first-pass edge kernel for ncu captures")
+    ap.add_argument("--profile", choices=["early", "full", "knn", "near", "pen", "abstract"], default=None,
+                    help="short runs of one workload's kernels for ncu captures")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
