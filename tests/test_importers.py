@@ -2,7 +2,11 @@
 limits, exactness of the cylinder-to-sphere mapping against a direct 2-D
 restatement of the planar problem (disc against rectangle, disc against
 disc), the conservative cover of box robots (never free where the rotated
-box touches an obstacle), and the refused forms."""
+box touches an obstacle), the reference's own planar scene files (when its
+checkout is present), and the refused forms."""
+import os
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -119,6 +123,43 @@ def test_box_robot_cover_is_conservative(oracle):
     for i in np.nonzero(free)[0]:
         assert not _box_touches_rect(q[i, :2], q[i, 2], (0.06, 0.3), lo, hi), i
     assert keep.sum() == 5 and 0.05 < free.mean() < 0.95
+
+
+REF_MUJOCO = (Path(os.environ.get("MRMG_REFERENCE_ROOT", "/root/reference")) / "src" / "multi_robot_multi_goal_planning"
+              / "assets" / "models" / "mujoco")
+
+
+@pytest.mark.skipif(not REF_MUJOCO.is_dir(), reason="the reference checkout is not on this machine")
+@pytest.mark.parametrize("name", ["mj_two_dim.xml", "mj_hallway.xml", "mj_manip.xml", "mj_piano.xml"])
+def test_reference_mujoco_scenes_import(oracle, name):
+    """The reference's planar MuJoCo scene files (envs mujoco_env.py:891-1060)
+    import as two planar-base robots a1, a2 (x, y, yaw each).  The limits are
+    the compiled model's jnt_range (mujoco_env.py:194-198): slide ranges as
+    written, hinge ranges in degrees (these files set no <compiler
+    angle="radian">; mj_two_dim.xml's "-3.14 3.14" is therefore 0.0548 rad).
+    Free bodies become movable boxes.  The start-free checks run on the
+    oracle."""
+    import xml.etree.ElementTree as ET
+
+    path = REF_MUJOCO / name
+    root = ET.fromstring(path.read_text())
+    assert root.find("compiler") is None
+    sc = pkg("importers").load_mjcf_planar(path)
+    assert sc.n_robots == 2 and sc.q_dim == 6
+    want = []
+    for body in ("a1", "a2"):
+        for j in root.find(".//body[@name='%s']" % body).findall("joint"):
+            r = [float(x) for x in j.get("range").split()]
+            want.append(np.deg2rad(r) if j.get("type") == "hinge" else r)
+    np.testing.assert_allclose(sc.limits, np.array(want).T)
+    free = {b.get("name") for b in root.iter("body") if b.find("freejoint") is not None}
+    assert set(sc.movable_boxes) == free
+    assert np.all(sc.sphere_radius > 0) and np.all(sc.box_hi > sc.box_lo)
+    o = oracle.OracleScene(sc)
+    rng = np.random.default_rng(0)
+    q = rng.uniform(sc.limits[0], sc.limits[1], (2000, 6))
+    free_frac = o.configs_free(q).mean()
+    assert 0.0 < free_frac < 1.0
 
 
 @pytest.mark.parametrize("bad, err", [
