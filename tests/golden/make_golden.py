@@ -25,6 +25,8 @@ Outputs (numpy .npz, seeded, small):
   prm_search.npz         the composite PRM's lazy A* (MultimodalGraph.search, prm_graph.py:552-746)
                          on the disc scene over a fixed k-NN graph: path and printed counters
   known_answers.json     the reference tests' own known answers (tests/test.py)
+  paths.npz              is_path_collision_free verdicts on the disc scene under four flag variants
+                         (python tests/golden/make_golden.py <reference root> paths)
 """
 from __future__ import annotations
 
@@ -447,8 +449,49 @@ def make_prm_search(pe, ae, cf, reg):
                         resolution=0.1, **res)
 
 
+PATH_VARIANTS = [dict(resolution=0.01), dict(resolution=0.01, check_edges_in_order=True),
+                 dict(resolution=0.02, check_start_and_end=False),
+                 dict(resolution=0.02, check_edges_in_order=True, check_start_and_end=False)]
+
+
+def make_paths(pe, ae, reg):
+    """Verdicts of the reference's own is_path_collision_free
+    (planning_env.py:1765-1881) on the disc scene: 400 paths of 2 to 6 states
+    (random walks with steps up to 0.15 per coordinate, and some long jumps),
+    under the flag variants of PATH_VARIANTS.  A one-state path makes the
+    reference raise (generate_binary_search_indices(0) indexes an empty
+    list), so none is generated."""
+    srng = np.random.default_rng(0)
+    centers = srng.uniform(-0.8, 0.8, (10, 2))
+    half = srng.uniform(0.05, 0.2, (10, 2))
+    env = disc_env(ae, reg, centers, half)
+    rng = np.random.default_rng(77)
+    paths, lens = [], []
+    for p in range(400):
+        P = int(rng.integers(2, 7))
+        step = 0.15 if p % 4 else 0.8
+        q = [rng.uniform(-1, 1, 4)]
+        for _ in range(P - 1):
+            q.append(np.clip(q[-1] + rng.uniform(-step, step, 4), -1, 1))
+        paths.append(np.array(q))
+        lens.append(P)
+    free = []
+    for v in PATH_VARIANTS:
+        row = []
+        for qs in paths:
+            states = [pe.State(env.start_pos.from_flat(q), env.start_mode) for q in qs]
+            row.append(int(env.is_path_collision_free(states, **v)))
+        free.append(row)
+    np.savez_compressed(OUT / "paths.npz", centers=centers, half=half, states=np.concatenate(paths),
+                        offsets=np.concatenate([[0], np.cumsum(lens)]).astype(np.int64),
+                        free=np.array(free, dtype=np.uint8), variants=json.dumps(PATH_VARIANTS))
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "prm_search":
+    if len(sys.argv) > 2 and sys.argv[2] == "paths":
+        pe_, ae_, cf_, reg_ = import_reference(Path(sys.argv[1]))
+        make_paths(pe_, ae_, reg_)
+    elif len(sys.argv) > 2 and sys.argv[2] == "prm_search":
         pe_, ae_, cf_, reg_ = import_reference(Path(sys.argv[1]))
         make_prm_search(pe_, ae_, cf_, reg_)
     elif len(sys.argv) > 2 and sys.argv[2] == "near":

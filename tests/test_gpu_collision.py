@@ -229,3 +229,24 @@ def test_edge_errors(gpu):
         sc.is_edge_collision_free_batch(q1, q1 + 0.001, 0.01, N_start=5)
     # empty batch
     assert sc.is_edge_collision_free_batch(np.zeros((0, 4)), np.zeros((0, 4)), 0.01).numel() == 0
+
+
+def test_path_check_golden(gpu):
+    """is_path_collision_free through the env on the device: the reference's
+    own verdicts on 400 disc-scene paths under four flag variants
+    (tests/golden/paths.npz)."""
+    g = golden("paths.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=g["centers"],
+        box_bounds=2.0 * g["half"], sphere_pos=np.zeros((0, 2)), sphere_radius=[], q_dim=4)
+    env = pkg("env").Gb300AbstractEnvironment(scene)
+    off = g["offsets"]
+
+    class S:
+        def __init__(self, q):
+            self.q, self.mode = env.start_pos.from_flat(q), None
+
+    for vi, v in enumerate(json.loads(str(g["variants"]))):
+        got = [int(env.is_path_collision_free([S(q) for q in g["states"][off[i]:off[i + 1]]], **v))
+               for i in range(len(off) - 1)]
+        assert got == g["free"][vi].tolist(), v

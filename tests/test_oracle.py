@@ -225,3 +225,46 @@ def test_oracle_robot_mask_semantics(oracle):
     both = o.configs_free_for_robots(q, 0b0011)
     # a pair of robots is free only if each robot alone is free
     assert np.all(both <= single[0] & single[1])
+
+
+def _path_fixture():
+    g = golden("paths.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=g["centers"],
+        box_bounds=2.0 * g["half"], sphere_pos=np.zeros((0, 2)), sphere_radius=[], q_dim=4)
+    off = g["offsets"]
+    paths = [g["states"][off[i]:off[i + 1]] for i in range(len(off) - 1)]
+    return g, scene, paths, json.loads(str(g["variants"]))
+
+
+def test_path_check_golden(oracle):
+    """is_path_collision_free (planning_env.py:1765-1881): the env's batched
+    path check (its vertex rules, every edge interior submitted at once) with
+    the oracle's exact verdicts in place of the device gives the reference's
+    own verdicts on 400 disc-scene paths under four flag variants."""
+    import torch
+
+    envm = pkg("env")
+    g, scene, paths, variants = _path_fixture()
+    o = oracle.OracleScene(scene)
+
+    class OracleBacked:
+        mode = -1
+
+        def is_collision_free_batch(self, qs):
+            return torch.from_numpy(o.configs_free(np.asarray(qs)).astype(np.uint8))
+
+        def is_edge_collision_free_batch(self, q1s, q2s, resolution, include_endpoints=False, N=None):
+            return torch.from_numpy(o.edges_free(np.asarray(q1s), np.asarray(q2s), resolution,
+                                                 include_endpoints=include_endpoints, N=N).astype(np.uint8))
+
+    env = object.__new__(envm.Gb300AbstractEnvironment)
+    env._gb300 = OracleBacked()
+
+    class S:
+        def __init__(self, q):
+            self.q, self.mode = q, None
+
+    for vi, v in enumerate(variants):
+        got = [int(env.is_path_collision_free([S(q) for q in qs], **v)) for qs in paths]
+        assert got == g["free"][vi].tolist(), v
