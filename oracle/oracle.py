@@ -300,5 +300,38 @@ def near(qs, q_mode, nodes, mode_off, slices, metric, radius, add_eps=1e-10):
     return np.array(offs, dtype=np.int64), cat(idx, np.int64), cat(dist, np.float64)
 
 
+def batch_free_batched_form(scene, qs) -> bool:
+    """AbstractEnvironment._batch_is_collision_free (abstract_env.py:278-299):
+    True iff no configuration of qs [n, D] collides, with the obstacle tests
+    in their batched numpy forms -- Rectangle.batch_collides_with_sphere
+    (:86-104: clip, np.sum of squares along axis 1, <= r^2) and
+    Sphere.batch_collides_with_sphere (:52-55: np.linalg.norm along axis 1,
+    i.e. rounded squares, numpy's sum and sqrt, < r_o + r) -- and the agent
+    pairs as the single check tests them (np.linalg.norm of one vector, < r_i +
+    r_j).  numpy restatement: it computes what the reference's numpy calls
+    compute on this host."""
+    t = scene.tables()
+    qs = np.asarray(qs, dtype=np.float64).reshape(len(qs), -1)
+    A, dim = len(scene.agent_radii), scene.dim
+    off = t["agent_offsets"]
+    for i in range(A):
+        c = qs[:, off[i]:off[i] + dim]
+        r = scene.agent_radii[i]
+        for o in range(len(scene.sphere_radius)):
+            if (np.linalg.norm(t["sphere_pos"][o] - c, axis=1) < scene.sphere_radius[o] + r).any():
+                return False
+        for b in range(len(t["box_lo"])):
+            closest = np.clip(c, t["box_lo"][b], t["box_hi"][b])
+            if (np.sum((closest - c) ** 2, axis=1) <= r ** 2).any():
+                return False
+    for k in range(len(qs)):
+        for i in range(A):
+            for j in range(i + 1, A):
+                if np.linalg.norm(qs[k, off[i]:off[i] + dim] - qs[k, off[j]:off[j] + dim]) < \
+                        scene.agent_radii[i] + scene.agent_radii[j]:
+                    return False
+    return True
+
+
 def num_threads() -> int:
     return int(lib().orc_num_threads())

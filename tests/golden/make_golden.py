@@ -27,6 +27,8 @@ Outputs (numpy .npz, seeded, small):
   known_answers.json     the reference tests' own known answers (tests/test.py)
   paths.npz              is_path_collision_free verdicts on the disc scene under four flag variants
                          (python tests/golden/make_golden.py <reference root> paths)
+  batch_forms.npz        is_collision_free vs _batch_is_collision_free near a Sphere obstacle's contact
+                         distance on 'abstract.test' (... <reference root> batch_forms)
 """
 from __future__ import annotations
 
@@ -487,8 +489,36 @@ def make_paths(pe, ae, reg):
                         free=np.array(free, dtype=np.uint8), variants=json.dumps(PATH_VARIANTS))
 
 
+def make_batch_forms(reg):
+    """The reference's two forms of the configuration check on its
+    'abstract.test' scene (Sphere r 0.2 at the origin, Rectangle above it):
+    is_collision_free (abstract_env.py:255-276) and _batch_is_collision_free
+    (:278-299) of one configuration at a time, for 4,000 configurations whose
+    first or second disc sits within 2e-16 of the sphere obstacle's contact
+    distance (the other disc far away), plus 200 batches of 8 of them."""
+    env = reg.get_env_by_name("abstract.test")
+    rng = np.random.default_rng(91)
+    qs = []
+    for k in range(4000):
+        ang = rng.uniform(np.pi, 2 * np.pi)          # below the sphere: clear of the rectangle
+        eps = rng.choice([0.0, 1e-17, -1e-17, 5e-17, -5e-17, 1e-16, -1e-16, 2e-16, -2e-16])
+        p = (0.3 + eps) * np.array([np.cos(ang), np.sin(ang)])
+        far = np.array([1.5, -1.5])
+        qs.append(np.concatenate([p, far]) if k % 2 == 0 else np.concatenate([far, p]))
+    qs = np.array(qs)
+    single = np.array([env.is_collision_free(env.start_pos.from_flat(q), None) for q in qs], dtype=np.uint8)
+    batch1 = np.array([env._batch_is_collision_free([env.start_pos.from_flat(q)], None) for q in qs], dtype=np.uint8)
+    groups = rng.integers(0, len(qs), (200, 8))
+    batch8 = np.array([env._batch_is_collision_free([env.start_pos.from_flat(qs[j]) for j in g], None)
+                       for g in groups], dtype=np.uint8)
+    np.savez_compressed(OUT / "batch_forms.npz", configs=qs, single=single, batch1=batch1, groups=groups,
+                        batch8=batch8)
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "paths":
+    if len(sys.argv) > 2 and sys.argv[2] == "batch_forms":
+        make_batch_forms(import_reference(Path(sys.argv[1]))[3])
+    elif len(sys.argv) > 2 and sys.argv[2] == "paths":
         pe_, ae_, cf_, reg_ = import_reference(Path(sys.argv[1]))
         make_paths(pe_, ae_, reg_)
     elif len(sys.argv) > 2 and sys.argv[2] == "prm_search":

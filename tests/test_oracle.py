@@ -268,3 +268,23 @@ def test_path_check_golden(oracle):
     for vi, v in enumerate(variants):
         got = [int(env.is_path_collision_free([S(q) for q in qs], **v)) for qs in paths]
         assert got == g["free"][vi].tolist(), v
+
+
+def test_batched_check_forms_golden(oracle):
+    """The reference's is_collision_free and _batch_is_collision_free on
+    configurations within 2e-16 of a Sphere obstacle's contact distance
+    ('abstract.test'): the oracle's single-configuration check (the kernels'
+    semantics) reproduces the first, its numpy restatement of the batched
+    form the second, and the two reference forms differ on some of these
+    ties (batch_forms.npz)."""
+    g, a = golden("batch_forms.npz"), golden("abstract_test.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=a["box_center"],
+        box_bounds=a["box_bounds"], sphere_pos=a["sphere_pos"], sphere_radius=[float(a["sphere_radius"][0])], q_dim=4)
+    o = oracle.OracleScene(scene)
+    assert np.array_equal(o.configs_free(g["configs"]), g["single"])
+    got1 = np.array([oracle.batch_free_batched_form(scene, q[None]) for q in g["configs"]], dtype=np.uint8)
+    assert np.array_equal(got1, g["batch1"])
+    got8 = np.array([oracle.batch_free_batched_form(scene, g["configs"][grp]) for grp in g["groups"]], dtype=np.uint8)
+    assert np.array_equal(got8, g["batch8"])
+    assert 0 < int((g["single"] != g["batch1"]).sum()) < 200
