@@ -250,3 +250,15 @@ def test_path_check_golden(gpu):
         got = [int(env.is_path_collision_free([S(q) for q in g["states"][off[i]:off[i + 1]]], **v))
                for i in range(len(off) - 1)]
         assert got == g["free"][vi].tolist(), v
+
+
+def test_sphere_obstacle_ties_golden(gpu):
+    """Configurations within 2e-16 of a Sphere obstacle's contact distance on
+    the reference's 'abstract.test' scene: the device's verdicts are the
+    reference's own is_collision_free verdicts (batch_forms.npz)."""
+    g, a = golden("batch_forms.npz"), golden("abstract_test.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=a["box_center"],
+        box_bounds=a["box_bounds"], sphere_pos=a["sphere_pos"], sphere_radius=[float(a["sphere_radius"][0])], q_dim=4)
+    sc = pkg("collision").Gb300Scene(scene)
+    assert np.array_equal(sc.is_collision_free_batch(g["configs"]).cpu().numpy(), g["single"])
