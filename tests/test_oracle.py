@@ -288,3 +288,58 @@ def test_batched_check_forms_golden(oracle):
     got8 = np.array([oracle.batch_free_batched_form(scene, g["configs"][grp]) for grp in g["groups"]], dtype=np.uint8)
     assert np.array_equal(got8, g["batch8"])
     assert 0 < int((g["single"] != g["batch1"]).sum()) < 200
+
+
+def _fk_homogeneous(scene, q):
+    """Sphere centres [S, 3] of one configuration from 4x4 homogeneous
+    transforms: the base pose (planar bases: translation (x, y), then Rz(yaw),
+    then the mount pose), then per link Rz(theta) Tz(d) Tx(a) Rx(alpha)
+    (standard DH), spheres at their local offsets in their link frames."""
+    def hom(R, p):
+        T = np.eye(4)
+        T[:3, :3], T[:3, 3] = R, p
+        return T
+
+    def rz(t):
+        c, s = np.cos(t), np.sin(t)
+        return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1.0]])
+
+    frames = []
+    for r in range(scene.n_robots):
+        bp = np.asarray(scene.base_pose[r], dtype=np.float64)
+        mount = hom(bp[:9].reshape(3, 3), bp[9:])
+        j = int(scene.q_offset[r])
+        if scene.base_kind[r] == 1:
+            T = hom(np.eye(3), [q[j], q[j + 1], 0.0]) @ hom(rz(q[j + 2]), np.zeros(3)) @ mount
+            j += 3
+        else:
+            T = mount
+        fr = [T]
+        for k in range(int(scene.n_links[r])):
+            a, d, ca, sa = scene.dh[r][k]
+            rx = np.array([[1, 0, 0], [0, ca, -sa], [0, sa, ca]])
+            T = T @ hom(rz(q[j + k]), [0, 0, 0]) @ hom(np.eye(3), [0, 0, d]) @ hom(np.eye(3), [a, 0, 0]) \
+                @ hom(rx, np.zeros(3))
+            fr.append(T)
+        frames.append(fr)
+    out = []
+    for s in range(len(scene.sphere_radius)):
+        T = frames[int(scene.sphere_robot[s])][int(scene.sphere_link[s])]
+        out.append(T[:3, :3] @ np.asarray(scene.sphere_local[s]) + T[:3, 3])
+    return np.array(out)
+
+
+@pytest.mark.parametrize("factory", ["make_arm_scene", "make_mobile_scene"])
+def test_arm_kinematics_independent_restatement(oracle, factory):
+    """The arm kinematics have no counterpart in the reference: the oracle's
+    C frames (composed row by row) agree with an independent homogeneous-
+    matrix restatement of the same convention to 1e-12 of the reach, for
+    fixed DH arms and planar mobile bases."""
+    scenes = pkg("scenes")
+    sc = getattr(scenes, factory)(0)
+    o = oracle.OracleScene(sc)
+    q = scenes.uniform_configs(sc, 50, seed=3, dtype=np.float64)
+    for i in range(len(q)):
+        got, want = o.sphere_centers(q[i]), _fk_homogeneous(sc, q[i])
+        assert got.shape == want.shape == (len(sc.sphere_radius), 3)
+        assert np.max(np.abs(got - want)) <= 1e-12 * (1.0 + np.max(np.abs(want))), i
