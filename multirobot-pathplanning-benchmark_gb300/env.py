@@ -89,6 +89,21 @@ class Gb300CollisionBackend:
         if idx != self._gb300.mode:
             self._gb300.set_mode(idx)
 
+    # --- mode hooks the planners and the mode logic call ---------------------
+    def get_scenegraph_info_for_mode(self, mode, is_start_mode: bool = False) -> dict:
+        """Stored with every new mode by the mode logic (planning_env.py:466).
+        A sphere-set scene has no scene graph: empty, as the abstract env's
+        (abstract_env.py:161-162)."""
+        return {}
+
+    def set_to_mode(self, m) -> None:
+        """Selects the tables of mode ``m`` on a per-mode scene (the receding-
+        horizon wrapper and the prioritized planner call it,
+        planners/receding_horizon_wrapper.py:173-178,
+        prioritized_planner.py:244); on a scene without modes nothing changes,
+        as with the abstract env (abstract_env.py:356-360)."""
+        self._use_mode(m)
+
     # --- single queries (planning_env.py:1724-1763) ------------------------
     def is_collision_free(self, q, mode) -> bool:
         if q is None:

@@ -241,6 +241,41 @@ def test_path_check_covers_the_reference_calls():
     assert counts == ka["path_calls"]
 
 
+def test_env_mode_hooks():
+    """The reference's mode logic stores get_scenegraph_info_for_mode(mode)
+    with every new mode (planning_env.py:466) and planners call
+    set_to_mode: both exist on the backend.  A scene without modes keeps its
+    tables; a per-mode scene switches to the mode's table set."""
+    envm = pkg("env")
+
+    class Switches:
+        def __init__(self):
+            self.mode, self.calls = -1, []
+
+        def set_mode(self, m):
+            self.mode = m
+            self.calls.append(m)
+
+    plain = object.__new__(envm.Gb300AbstractEnvironment)
+    plain._gb300 = Switches()
+    assert plain.get_scenegraph_info_for_mode(object()) == {} and plain.get_scenegraph_info_for_mode(None, True) == {}
+    plain.set_to_mode(3)
+    assert plain._gb300.calls == []
+
+    class Mode:
+        def __init__(self, i):
+            self.id = i
+
+    per_mode = object.__new__(envm.Gb300ArmEnvironment)
+    per_mode._gb300 = Switches()
+    per_mode._mode_index = lambda m: m if isinstance(m, (int, np.integer)) else m.id
+    per_mode.set_to_mode(Mode(2))
+    per_mode.set_to_mode(Mode(2))          # already selected: no switch
+    per_mode.set_to_mode(0)
+    per_mode.set_to_mode(None)             # None leaves the tables as they are
+    assert per_mode._gb300.calls == [2, 0] and per_mode._gb300.mode == 0
+
+
 def test_verdict_buffer_is_checked():
     """A caller's verdict buffer must be a contiguous uint8 CUDA tensor with
     room for every verdict (the kernels write n bytes); anything else is
