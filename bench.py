@@ -66,9 +66,23 @@ def workload(rank: int):
 
 
 def config_flops(scene) -> int:
-    """Algorithmic FP32 flops of one full configuration evaluation:
-    63 per DH link composition, 18 per sphere centre, 15 per sphere-box test,
-    11 per inter-robot sphere pair test."""
+    """Algorithmic FP32 flops of one full configuration evaluation, counted
+    as the work-unit table of the hot path fixes them: 63 per DH link
+    composition, 18 per sphere centre, 9 per sphere-box test and 9 per
+    inter-robot sphere pair test (four arms: 28 x 63 + 168 x 18 + 8,400 x 9 +
+    10,584 x 9 = 175,644)."""
+    links = int(np.sum(scene.n_links))
+    S = len(scene.sphere_radius)
+    B = len(scene.box_lo)
+    counts = np.bincount(scene.sphere_robot, minlength=scene.n_robots)
+    pairs = int((counts.sum() ** 2 - (counts ** 2).sum()) // 2)
+    return 63 * links + 18 * S + 9 * S * B + 9 * pairs
+
+
+def config_ops_with_compares(scene) -> int:
+    """The same work with the clamps and compares counted as operations too
+    (15 per sphere-box test, 11 per sphere pair): a second, labelled figure,
+    not the roofline numerator."""
     links = int(np.sum(scene.n_links))
     S = len(scene.sphere_radius)
     B = len(scene.box_lo)
@@ -84,49 +98,72 @@ WORKLOAD_DESC = ("four 7-DoF DH arms on a 1.2 m table (168 spheres r 0.03-0.07 m
 
 # ---------------------------------------------------------------------------
 class ClockSampler:
+    """SM clocks, power and throttle reasons sampled every ~200 ms while a run
+    is under way: a thread runs one-shot `nvidia-smi --query-gpu` calls (a
+    looping nvidia-smi writing to a file buffers its output and loses it when
+    stopped).  The GPU is named by its UUID when torch reports one, so the
+    sample is of the device this process uses."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
-    def __init__(self, index: int):
-        self.path = Path(tempfile.mkstemp(prefix="clocks_", suffix=".csv")[1])
-        self.proc = None
-        try:
-            self.fh = open(self.path, "w")
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=self.fh, stderr=subprocess.DEVNULL)
-        except Exception:
-            self.proc = None
+    def __init__(self, index: int, period_s: float = 0.2):
+        import threading
 
-    def stop(self) -> dict:
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
-        self.proc.terminate()
+        self.gpu = str(index)
         try:
-            self.proc.wait(timeout=5)
+            import torch
+
+            u = getattr(torch.cuda.get_device_properties(index), "uuid", None)
+            if u is not None:
+                u = str(u)
+                self.gpu = u if u.startswith("GPU-") else f"GPU-{u}"
         except Exception:
-            self.proc.kill()
-        self.fh.close()
-        rows = []
-        for line in self.path.read_text().splitlines():
+            pass
+        self.rows, self.errors = [], []
+        self.period = period_s
+        self._stop = threading.Event()
+        self._t = threading.Thread(target=self._loop, daemon=True)
+        self._t.start()
+
+    def _query(self):
+        r = subprocess.run(["nvidia-smi", "-i", self.gpu, f"--query-gpu={self.FIELDS}",
+                            "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
             p = [x.strip() for x in line.split(",")]
             if len(p) != 7:
                 continue
             try:
-                rows.append((float(p[0]), float(p[1]), float(p[2]), p[3:]))
+                self.rows.append((float(p[0]), float(p[1]), float(p[2]), p[3:]))
             except ValueError:
                 continue
-        self.path.unlink(missing_ok=True)
+        if r.returncode != 0 and not self.errors:
+            self.errors.append((r.stderr or r.stdout).strip()[:200])
+
+    def _loop(self):
+        while not self._stop.is_set():
+            try:
+                self._query()
+            except Exception as e:   # nvidia-smi missing or hung: report, keep the run going
+                self.errors.append(repr(e)[:200])
+                return
+            self._stop.wait(self.period)
+
+    def stop(self) -> dict:
+        self._stop.set()
+        self._t.join(timeout=15)
+        rows = list(self.rows)
         if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0,
+                    "errors": self.errors[:1]}
         pmin = min(r[2] for r in rows)
         load = [r for r in rows if r[2] > pmin * 1.15] or rows
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in load for i, v in enumerate(r[3]) if v.lower() == "active"})
+        reasons = sorted({self.NAMES[i] for r in load for i, v in enumerate(r[3]) if v.lower() == "active"})
         return {"sm_mhz": float(np.median([r[0] for r in load])), "sm_max_mhz": max(r[1] for r in rows),
                 "reasons": reasons, "samples": len(rows), "samples_under_load": len(load),
-                "power_w_max": max(r[2] for r in rows)}
+                "power_w_max": max(r[2] for r in rows),
+                "window": "the whole run (headline steps, end-to-end steps and the extra workloads)"}
 
 
 def dist_env():
@@ -174,6 +211,15 @@ def cpu_baseline(orc, scene, q1, q2, budget_s: float = 12.0, max_passes: int = 2
                       f"restatement, OpenMP {orc.num_threads()} threads, {os.cpu_count()} host cores"}
 
 
+def bench_config(world: int, n: int) -> dict:
+    """The workload's `config`, identical in both arms of the benchmark."""
+    return {"workload": WORKLOAD_DESC, "edges_per_step": n, "edges_total": n * world,
+            "l2": "GPU arm: flushed between timed steps (256 MB write outside the timed events)",
+            "parallelism": f"replicas x{world}",
+            "fk_parity": "the four arms' kinematics (standard DH) are defined by this library and checked against "
+                         "the oracle's C restatement; the reference delegates robots to external engines"}
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -190,10 +236,11 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     v = args.steps * len(a) / dt
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD_DESC, "edges_per_step": len(a), "parallelism": "cpu-openmp"},
+        "config": bench_config(world, len(a)),
+        "form": f"CPU FP64 restatement (oracle/oracle.c), OpenMP {orc.num_threads()} threads on rank 0",
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
                          "sample": f"each step: the full 100,000-edge workload on the CPU FP64 restatement "
                                    f"(oracle/oracle.c), OpenMP {orc.num_threads()} threads"},
@@ -217,6 +264,7 @@ def run_gb300(args):
     _lib, envm = pkg("_lib"), pkg("env")
     orc = oracle_mod()
 
+    clocks = ClockSampler(dev.index) if rank == 0 else None
     scene, q1, q2, N = workload(rank)
     n = len(q1)
     env = envm.Gb300ArmEnvironment(scene, collision_resolution=RESOLUTION)
@@ -243,7 +291,6 @@ def run_gb300(args):
         return g
 
     g = capture(_lib.MRMG_FLAG_ASYNC)
-    clocks = ClockSampler(dev.index)
     with torch.cuda.stream(s):
         for _ in range(args.warmup):
             flush.zero_()
@@ -263,7 +310,6 @@ def run_gb300(args):
     t_wall = time.perf_counter() - t_wall0
     torch.cuda.synchronize()
     barrier(world)
-    clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in evs]
     total_ms = reduce_max(float(np.sum(step_ms)), world)
     value = world * n * args.steps / (total_ms * 1e-3)
@@ -332,6 +378,14 @@ def run_gb300(args):
         plain_v = [env.is_edge_collision_free(q1[i], q2[i], None) for i in range(m)]
         plain = m / (time.perf_counter() - t0)
         mism += int((np.array(plain_v, dtype=np.uint8) != ref[:m]).sum())
+        # one is_collision_free call per configuration (the sampler's pattern)
+        qc = np.asarray(q1[:m], np.float64)
+        ref_c = o.configs_free(qc)
+        env.is_collision_free(qc[0], None)
+        t0 = time.perf_counter()
+        plain_c = [env.is_collision_free(qc[i], None) for i in range(m)]
+        plain_cfg = m / (time.perf_counter() - t0)
+        mism += int((np.array(plain_c, dtype=np.uint8) != ref_c).sum())
 
         # ---- roofline: first-pass kernel in full-evaluation mode
         full_flags = _lib.MRMG_FLAG_ASYNC | _lib.MRMG_FLAG_FULL_EVAL
@@ -351,18 +405,27 @@ def run_gb300(args):
         s.synchronize()
         full_ms = float(np.mean([a.elapsed_time(b) for a, b in fev]))
         F1 = config_flops(scene)
+        F1c = config_ops_with_compares(scene)
         achieved = cfgs * F1 / (full_ms * 1e-3) / 1e12
         peak = _measure_fp32_peak(_lib)
         traffic = _profile_traffic()
         extra = dict(
-            plain={"value": plain, "unit": UNIT, "edges_sampled": m,
-                   "form": "env.is_edge_collision_free per edge: one launch, one host round trip"},
+            plain={"value": plain, "unit": UNIT, "edges_sampled": m, "us_per_call": 1e6 / plain,
+                   "form": "env.is_edge_collision_free per edge: one call, one host round trip"},
+            plain_configs={"value": plain_cfg, "unit": "configs/s", "configs_sampled": m,
+                           "us_per_call": 1e6 / plain_cfg,
+                           "form": "env.is_collision_free per configuration: one call, one host round trip"},
             batched_over_plain=value / plain,
             roofline={"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                       "frac": achieved / peak, "traffic": traffic,
                       "kernel": "first pass (arm_edges_kernel phase A + arm_edges_phase_b), full-evaluation mode",
-                      "algorithmic": f"{cfgs} configurations x {F1} flops per launch",
+                      "algorithmic": f"{cfgs} configurations x {F1} flops per launch (per configuration: 28 DH "
+                                     f"links x 63 + 168 sphere centres x 18 + 8,400 sphere-box tests x 9 + 10,584 "
+                                     f"sphere pairs x 9)",
                       "ms_per_launch": full_ms,
+                      "frac_with_compares": cfgs * F1c / (full_ms * 1e-3) / 1e12 / peak,
+                      "with_compares": f"{F1c} operations per configuration when the clamps and compares count "
+                                       "(15 per sphere-box test, 11 per pair)",
                       "peak_source": "measured FP32 FFMA microbenchmark (mrmg_microbench_fma) in this run; "
                                      "MEASURED_PEAKS.json holds HBM and BF16 only"},
             full_eval_mismatches=full_mism,
@@ -381,15 +444,15 @@ def run_gb300(args):
                 extra["abstract"] = bench_abstract(orc)
 
     mism = int(reduce_max(float(mism), world))
+    clk = clocks.stop() if clocks is not None else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD_DESC, "edges_per_step": n, "edges_total": n * world,
-                       "l2": "flushed between timed steps (256 MB write outside the timed events)",
-                       "form": "batched, CUDA-graph captured (counter reset, phase A, phase B1, phase B2 + finalize, FP64 "
-                               "re-check pass, status copy)", "parallelism": f"replicas x{world}"},
+            "config": bench_config(world, n),
+            "form": "batched, CUDA-graph captured (counter reset, phase A, phase B1, phase B2 + finalize, FP64 "
+                    "re-check pass, status copy)",
             "verdict_mismatches": mism,
             "clocks": clk,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(q1.nbytes + q2.nbytes),
@@ -406,6 +469,7 @@ def run_gb300(args):
             "wall_s_timed": t_wall,
         }
         line.update(extra)
+        line["summary"] = _summary(line)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -444,10 +508,25 @@ def bench_knn(orc, steps: int = 20) -> dict:
         orc.knn(w["queries"][sub], w["q_mode"][sub], w["nodes"], w["mode_offsets"], w["slices"], metric, w["k"])
         cpu_s = (time.perf_counter() - t1) * len(w["queries"]) / 256
         issued = 2 * (96 if metric == "euclidean" else 128) * pairs
+        alg = 2 * 32 * pairs                 # K = 28 padded to 32 (four 8-wide agent blocks for max over agents)
+        node_bytes = w["nodes"].shape[0] * w["nodes"].shape[1] * 4
+        peaks = _peaks()
         out[metric] = {"queries_per_s": len(w["queries"]) / dt, "ms_per_batch": 1e3 * dt, "index_mismatches": mism,
                        "tensor_core": store.last_stats.get("tensor_core"),
                        "rerun_exact": store.last_stats.get("rerun_exact"),
                        "gemm_tflops_issued": issued / dt / 1e12,
+                       "roofline": {"bound": "tensor", "achieved": alg / dt / 1e12, "peak": peaks["bf16_tflops"],
+                                    "unit": "TFLOP/s", "frac": alg / dt / 1e12 / peaks["bf16_tflops"],
+                                    "algorithmic": f"2 x 32 x {pairs} query-node pairs per batch (K = 28 padded "
+                                                   f"to 32)",
+                                    "issued_frac": issued / dt / 1e12 / peaks["bf16_tflops"],
+                                    "issued": f"split-BF16 operands: K = {96 if metric == 'euclidean' else 128} "
+                                              f"per pair on the tensor pipe",
+                                    "hbm_achieved_gbs": node_bytes / dt / 1e9, "hbm_peak_gbs": peaks["hbm_gbs"],
+                                    "hbm_frac": node_bytes / dt / 1e9 / peaks["hbm_gbs"],
+                                    "hbm_bytes": f"{node_bytes} B: the nodes once in FP32",
+                                    "peak_source": peaks["source"],
+                                    "timing": "host wall clock per synchronous batch call (inputs resident)"},
                        "cpu_queries_per_s": len(w["queries"]) / cpu_s, "cpu_cores": orc.num_threads()}
         # radius queries: each query's radius is its 16th-nearest distance
         _, d16 = store.knn(qs, w["q_mode"], 16)
@@ -679,7 +758,7 @@ def bench_abstract(orc, reps: int = 20) -> dict:
     import ctypes as C
     fp64 = C.c_double(0.0)
     _lib.check(lib.mrmg_microbench_fma(1, 20000, C.byref(fp64), None))
-    hbm = json.load(open(ROOT / "MEASURED_PEAKS.json"))["hbm_gbs"] if (ROOT / "MEASURED_PEAKS.json").exists() else 6800.0
+    hbm = _peaks()["hbm_gbs"]
     bytes_out = 1000 * 10_000 * 8
     # FP64 work per distance in the reference's order: 4 subtractions, 4
     # products, 3 sums, 1 square root (counted as one operation; it is an
@@ -859,6 +938,46 @@ def bench_serving(orc, steps: int = 24, warmup: int = 3) -> dict:
     }
 
 
+def _summary(line: dict) -> dict:
+    """The figures a reader looks for first, repeated at the end of the line
+    (a log that keeps only the tail of the output still shows them)."""
+    def g(*keys):
+        d = line
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    out = {"edges_per_s": line.get("value"), "e2e_edges_per_s": g("e2e", "value"),
+           "verdict_mismatches": line.get("verdict_mismatches"),
+           "plain_us_per_edge_call": g("plain", "us_per_call"),
+           "plain_us_per_config_call": g("plain_configs", "us_per_call"),
+           "batched_over_plain": line.get("batched_over_plain"),
+           "roofline_frac_fp32": g("roofline", "frac"),
+           "cpu_port_edges_per_s": g("cpu_baseline", "value")}
+    for m in ("euclidean", "max_euclidean"):
+        out[f"knn_{m}_ms"] = g("knn", m, "ms_per_batch")
+        out[f"knn_{m}_index_mismatches"] = g("knn", m, "index_mismatches")
+        out[f"knn_{m}_tensor_frac"] = g("knn", m, "roofline", "frac")
+    out["abstract_edges_per_s"] = g("abstract", "edges", "edges_per_s")
+    out["abstract_cpu_edges_per_s"] = g("abstract", "edges", "cpu_edges_per_s")
+    out["serving_p50_p99_ms"] = [g("serving", "latency", "p50_ms"), g("serving", "latency", "p99_ms")]
+    out["penetration_ms_cost_and_grad"] = g("penetration", "ms_cost_and_grad")
+    return out
+
+
+def _peaks() -> dict:
+    """HBM copy bandwidth and dense BF16 burst throughput measured on this
+    pool's GPUs (MEASURED_PEAKS.json), else the fallback figures."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]),
+                "source": "of measured (MEASURED_PEAKS.json: burst BF16 GEMM, copy bandwidth)"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "of fallback (6.8 TB/s, 1.9 PFLOP/s BF16)"}
+
+
 def _measure_fp32_peak(_lib) -> float:
     import ctypes as C
 
@@ -964,6 +1083,64 @@ def run_profile(args):
     return 0
 
 
+def run_dry(args):
+    """The replica orchestration without a GPU: every rank builds its own
+    seeded shard, joins the barrier and the max-over-ranks reduction (gloo),
+    and rank 0 prints the line's shape with n_gpus = the world size.  No
+    edge is checked, so no value is reported; used to test the host logic."""
+    world, rank, _ = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    scene, q1, q2, N = workload(rank)
+    barrier(world)
+    t0 = time.perf_counter()
+    barrier(world)
+    t = reduce_max(time.perf_counter() - t0, world)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": None, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "dry_run": True,
+                          "config": bench_config(world, len(q1)), "barrier_s_max": t,
+                          "shard_first_edge_norm": float(np.linalg.norm(q1[0]))}), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def _free_port() -> int:
+    import socket
+
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        return so.getsockname()[1]
+
+
+def _replica_main(rank: int, args, port: int):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(args.gpus),
+                      LOCAL_RANK=str(rank))
+    fn = run_dry if args.dry_run else (run_reference if args.impl == "reference" else run_gb300)
+    rc = fn(args)
+    if rc:
+        sys.exit(rc)
+
+
+def spawn_replicas(args) -> int:
+    """`--gpus N` without an external launcher: one process per GPU (replicas,
+    rank r on GPU r), rendezvous on 127.0.0.1, the same code path as under
+    torchrun."""
+    import torch.multiprocessing as mp
+
+    try:
+        mp.spawn(_replica_main, args=(args, _free_port()), nprocs=args.gpus, join=True)
+    except mp.ProcessExitedException as e:
+        return int(e.exit_code or 1)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -976,11 +1153,17 @@ def main():
     ap.add_argument("--skip-extra", action="store_true", help="only the headline edge-check workload")
     ap.add_argument("--profile", choices=["early", "full", "knn", "near", "pen", "abstract"], default=None,
                     help="short runs of one workload's kernels for ncu captures")
+    ap.add_argument("--dry-run", action="store_true",
+                    help="replica orchestration only (gloo, no GPU work, no value): tests the host logic")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return spawn_replicas(args)
+    if args.dry_run:
+        return run_dry(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

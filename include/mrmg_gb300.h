@@ -63,8 +63,20 @@ enum { MRMG_REDUCE_MAX = 0, MRMG_REDUCE_SUM = 1 };
  *  MRMG_FLAG_FULL_EVAL  arm scenes: evaluate every interpolated configuration
  *                       and every sphere pair without stopping at the first
  *                       collision (same verdicts; used to measure the
- *                       kernel's throughput against its roofline) */
-enum { MRMG_FLAG_ASYNC = 1, MRMG_FLAG_FULL_EVAL = 2 };
+ *                       kernel's throughput against its roofline)
+ *  MRMG_FLAG_BATCH_FORM abstract scenes, mrmg_is_collision_free_batch: decide
+ *                       Sphere obstacles with the arithmetic of
+ *                       Sphere.batch_collides_with_sphere (abstract_env.py:
+ *                       51-55: np.linalg.norm(..., axis=1) = rounded squares,
+ *                       numpy's sum, sqrt) instead of the single form's
+ *                       (:44-47: the norm of one vector, a fused dot
+ *                       product); the two differ on ties within an ulp of the
+ *                       contact distance.  _batch_is_collision_free
+ *                       (abstract_env.py:278-299) is the AND of the verdicts
+ *                       of this form.  Rectangle obstacles and agent pairs
+ *                       use the same arithmetic in both forms; arm scenes
+ *                       have no Sphere obstacles and ignore the flag. */
+enum { MRMG_FLAG_ASYNC = 1, MRMG_FLAG_FULL_EVAL = 2, MRMG_FLAG_BATCH_FORM = 4 };
 
 const char *mrmg_version(void);
 const char *mrmg_last_error(void);
@@ -166,7 +178,7 @@ int mrmg_arm_scene_tune_order(mrmg_scene *scene, const void *d_q, int32_t dtype,
 /* Per-configuration verdicts for d_q[n, q_dim] (dtype MRMG_F32 or MRMG_F64).
  * Batched form of BaseProblem.is_collision_free (planning_env.py:1724-1734;
  * abstract_env.py:255-276); _batch_is_collision_free (abstract_env.py:278-299)
- * is the AND of these verdicts. */
+ * is the AND of these verdicts computed with MRMG_FLAG_BATCH_FORM. */
 int mrmg_is_collision_free_batch(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n,
                                  uint8_t *d_out, void *stream, int32_t flags);
 
@@ -213,8 +225,17 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene *scene, const void *d_q1, const
  *   held by every GPU that loads the library until the process exits.
  *   The first call on a device looks up the array's device address
  *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   The address is cached with the id of the device's CUDA context; a call
+ *   in a new context (after cudaDeviceReset) looks it up again, and that
+ *   call too should come before any stream capture.
  *   All calls share the array: calls that overlap on the GPU (other streams,
- *   threads or scenes) race and must be serialised by the caller. */
+ *   threads or scenes) race and must be serialised by the caller.  A call
+ *   also copies its counters into the scene's own counter words, so the
+ *   word of mrmg_scene_error_word and mrmg_last_call_stats describe it (also
+ *   when it was recorded into a graph with MRMG_FLAG_ASYNC), and its status
+ *   lands in the scene's pinned host mirror: two calls on one scene that
+ *   overlap on the GPU race there as well, whichever entry points they use.
+ *   Flags: as the regular entry point (MRMG_FLAG_ASYNC, MRMG_FLAG_FULL_EVAL). */
 #define MRMG_NOALLOC_MAX_EDGES 16384
 int mrmg_is_edge_collision_free_batch_noalloc(mrmg_scene *scene, const void *d_q1, const void *d_q2,
                                               int32_t dtype, int64_t n, double resolution,

@@ -25,6 +25,7 @@ MRMG_F32 = 0
 MRMG_F64 = 1
 MRMG_FLAG_ASYNC = 1
 MRMG_FLAG_FULL_EVAL = 2
+MRMG_FLAG_BATCH_FORM = 4
 MRMG_NOALLOC_MAX_EDGES = 16384
 
 METRICS = {"euclidean": 0, "sum_euclidean": 1, "max_euclidean": 2, "max": 3}

@@ -173,9 +173,21 @@ __device__ bool exact_free_warp(const AbstractDev& s, Acc acc, int lane) {
       const int off = s.agent_off[i];
       const double* p = s.sph_pos + o * dim;
       double ss = 0.0;
-      for (int k = 0; k < dim; k++) {
-        const double d = __dsub_rn(p[k], acc(off + k));
-        ss = __fma_rn(d, d, ss);
+      if (s.sph_batch_form) {
+        // Sphere.batch_collides_with_sphere (abstract_env.py:51-55):
+        // np.linalg.norm(pos - centers, axis=1) = sqrt(add.reduce(d * d))
+        double d2[kMaxAgentDim];
+        for (int k = 0; k < dim; k++) {
+          const double d = __dsub_rn(p[k], acc(off + k));
+          d2[k] = __dmul_rn(d, d);
+        }
+        ss = np_sum_dyn(d2, dim);
+      } else {
+        // Sphere.collides_with_sphere (:44-47): the norm of one vector (ddot)
+        for (int k = 0; k < dim; k++) {
+          const double d = __dsub_rn(p[k], acc(off + k));
+          ss = __fma_rn(d, d, ss);
+        }
       }
       hit = sqrt(ss) < s.sph_thr[o * A + i];
     }

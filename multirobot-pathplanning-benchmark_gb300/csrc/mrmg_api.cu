@@ -11,6 +11,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+
 #include "mrmg_internal.cuh"
 
 using namespace mrmg;
@@ -775,7 +777,9 @@ int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype,
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   CallScratch cs{sc->d_ctr, sc->d_pend, sc->d_surv, sc->pend_cap};
   LaunchShape ls = shape(sc);
-  e = sc->kind == 0 ? abstract_configs(sc->ab, d_q, dtype, n, d_out, cs, ls, st)
+  AbstractDev ab = sc->ab;
+  ab.sph_batch_form = (flags & MRMG_FLAG_BATCH_FORM) ? 1 : 0;
+  e = sc->kind == 0 ? abstract_configs(ab, d_q, dtype, n, d_out, cs, ls, st)
                     : arm_configs(sc->arm, d_q, dtype, n, d_out, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
   if (e != cudaSuccess) return cuda_fail(e, "launch configs");
   return finish_call(sc, st, flags);
@@ -866,7 +870,11 @@ int mrmg_status_from_error_bits(int32_t bits) {
 // loads the library holds it until the process exits.  All calls share it
 // and it keeps the last call's contents; each call clears its counters
 // before use.  Calls that overlap on the GPU (other streams, threads or
-// scenes) race on it and must be serialised by the caller.
+// scenes) race on it and must be serialised by the caller.  A call also
+// writes the scene's counter words and their pinned host mirror (the error
+// word and the statistics), as the regular entry point does: two calls on one
+// scene that overlap on the GPU race there too, whichever entry points they
+// use.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -878,9 +886,44 @@ static_assert(sizeof(int) * kNumCtr <= kNoAllocCtrBytes, "counters fit");
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocCtrBytes + kNoAllocPendBytes + kNoAllocSurvBytes];
 
 // Host code only has a stand-in for g_noalloc_scratch; its device address is
-// looked up once per device (with that device current) and cached.
+// looked up with that device current and cached per device, together with
+// the id of the CUDA context it belongs to.  A new context on the device
+// (after cudaDeviceReset, for instance) reloads the module at another
+// address, so a changed context id triggers a fresh lookup.  The context id
+// comes from the driver (cuCtxGetCurrent / cuCtxGetId, resolved through the
+// runtime's entry-point query, so the library does not link libcuda).
+struct NoAllocSlot {
+  unsigned long long ctx;   // 0: unknown
+  void* addr;
+};
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[256] = {};
+NoAllocSlot g_noalloc_slot[256] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// id of the calling thread's current context; false when unavailable
+bool current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_cur = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = (CtxGetCurrentFn)f;
+    f = nullptr;
+    q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (CtxGetIdFn)f;
+  });
+  if (!get_cur || !get_id) return false;
+  CUcontext c = nullptr;
+  if (get_cur(&c) != CUDA_SUCCESS || !c) return false;
+  return get_id(c, id) == CUDA_SUCCESS && *id != 0;
+}
 
 int noalloc_scratch(unsigned char** out) {
   int dev = 0;
@@ -888,13 +931,19 @@ int noalloc_scratch(unsigned char** out) {
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if (dev < 0 || dev >= 256) return fail(MRMG_ERR_UNSUPPORTED, "device index %d", dev);
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
-    g_noalloc_addr[dev] = p;
+  NoAllocSlot& slot = g_noalloc_slot[dev];
+  unsigned long long ctx = 0;
+  if (slot.addr && slot.ctx && current_context_id(&ctx) && ctx == slot.ctx) {
+    *out = (unsigned char*)slot.addr;
+    return MRMG_OK;
   }
-  *out = (unsigned char*)g_noalloc_addr[dev];
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+  if (!current_context_id(&ctx)) ctx = 0;   // unknown context: look the address up on every call
+  slot.ctx = ctx;
+  slot.addr = p;
+  *out = (unsigned char*)p;
   return MRMG_OK;
 }
 
@@ -928,10 +977,14 @@ int mrmg_is_edge_collision_free_batch_noalloc(mrmg_scene* sc, const void* d_q1, 
           ? abstract_edges(sc->ab, d_q1, d_q2, dtype, n, resolution, include_endpoints, (const long long*)d_N,
                            N_start, N_max, d_out, cs, ls, st)
           : arm_edges(sc->arm, d_q1, d_q2, dtype, n, resolution, include_endpoints, (const long long*)d_N, N_start,
-                      N_max, d_out, cs, ls, 0, st);
+                      N_max, d_out, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
   if (e != cudaSuccess) return cuda_fail(e, "launch edges");
-  // status: the counters go to the scene's pinned mirror (allocated with the scene)
-  e = cudaMemcpyAsync(sc->h_ctr, cs.ctr, sizeof(int) * kNumCtr, cudaMemcpyDeviceToHost, st);
+  // status: the counters are copied into the scene's own counter words (so the
+  // word of mrmg_scene_error_word and mrmg_last_call_stats describe this call,
+  // also when it was recorded into a graph), then to their pinned mirror
+  e = cudaMemcpyAsync(sc->d_ctr, cs.ctr, sizeof(int) * kNumCtr, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(counters)");
+  e = cudaMemcpyAsync(sc->h_ctr, sc->d_ctr, sizeof(int) * kNumCtr, cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(status)");
   if (flags & MRMG_FLAG_ASYNC) return MRMG_OK;
   e = cudaStreamSynchronize(st);

@@ -26,6 +26,8 @@ struct AbstractDev {
   const float *r32, *pair_thr32, *box_lo32, *box_hi32, *sph_pos32, *sph_thr32;
   float omax;       // max |coordinate| / threshold of any obstacle or agent radius
   float delta_k;    // FP32 band per unit magnitude: 8 * dim * 2^-24
+  int sph_batch_form;   // per call: Sphere obstacles in the axis=1 norm form (rounded squares,
+                        // numpy sum, sqrt) of Sphere.batch_collides_with_sphere, not the ddot form
 };
 
 // ---------------------------------------------------------------------------

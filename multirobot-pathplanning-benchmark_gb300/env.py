@@ -24,6 +24,7 @@ from typing import List, Optional
 import numpy as np
 import torch
 
+from . import _lib
 from .collision import Gb300Scene
 from .configuration import Gb300Configuration, batch_config_cost as _batch_config_cost, config_cost as _config_cost
 from .scenes import AbstractScene, ArmScene
@@ -155,10 +156,16 @@ class Gb300CollisionBackend:
         return mask
 
     def _batch_is_collision_free(self, qs: List, mode) -> bool:
-        """abstract_env.py:278-299: True iff every configuration is free."""
+        """abstract_env.py:278-299: True iff every configuration is free, with
+        Sphere obstacles tested in the arithmetic of the reference's batched
+        form (Sphere.batch_collides_with_sphere, abstract_env.py:51-55: the
+        axis=1 norm), which differs from the single check's on ties within an
+        ulp of the contact distance."""
         if len(qs) == 0:
             return True
-        return bool(self.batch_is_collision_free(np.array([_state(q) for q in qs]), mode).all())
+        self._use_mode(mode)
+        v = self._gb300.is_collision_free_batch(np.array([_state(q) for q in qs]), flags=_lib.MRMG_FLAG_BATCH_FORM)
+        return bool(v.bool().all().item())
 
     # --- batched (additive) ------------------------------------------------
     def batch_is_collision_free(self, qs, mode=None) -> np.ndarray:

@@ -527,4 +527,6 @@ if __name__ == "__main__":
     elif len(sys.argv) > 2 and sys.argv[2] == "near":
         make_near(import_reference(Path(sys.argv[1]))[2])
     else:
-        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+        if len(sys.argv) < 2:
+            sys.exit("usage: make_golden.py <reference root> [batch_forms|paths|prm_search|near]")
+        main(sys.argv[1])

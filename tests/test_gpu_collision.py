@@ -262,3 +262,28 @@ def test_sphere_obstacle_ties_golden(gpu):
         box_bounds=a["box_bounds"], sphere_pos=a["sphere_pos"], sphere_radius=[float(a["sphere_radius"][0])], q_dim=4)
     sc = pkg("collision").Gb300Scene(scene)
     assert np.array_equal(sc.is_collision_free_batch(g["configs"]).cpu().numpy(), g["single"])
+
+
+def test_batched_form_ties_golden(gpu):
+    """The same near-contact configurations through the batched form: the
+    device's MRMG_FLAG_BATCH_FORM verdicts are the reference's own
+    _batch_is_collision_free answers, per configuration and for 200 groups
+    of 8 (batch_forms.npz), through the C ABI flag and through the env
+    method; on these ties they differ from the single form."""
+    g, a = golden("batch_forms.npz"), golden("abstract_test.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=a["box_center"],
+        box_bounds=a["box_bounds"], sphere_pos=a["sphere_pos"], sphere_radius=[float(a["sphere_radius"][0])], q_dim=4)
+    lib = pkg("_lib")
+    env = pkg("env").Gb300AbstractEnvironment(scene)
+    v = env._gb300.is_collision_free_batch(g["configs"], flags=lib.MRMG_FLAG_BATCH_FORM).cpu().numpy()
+    assert np.array_equal(v, g["batch1"])
+    assert not np.array_equal(v, g["single"])
+    got8 = np.array([v[grp].all() for grp in g["groups"]], dtype=np.uint8)
+    assert np.array_equal(got8, g["batch8"])
+    S = pkg("configuration").Gb300Configuration
+    sl = [(0, 2), (2, 4)]
+    for i in range(0, len(g["configs"]), 97):
+        assert env._batch_is_collision_free([S(g["configs"][i], sl)], None) == bool(g["batch1"][i])
+    for j, grp in enumerate(g["groups"][:40]):
+        assert env._batch_is_collision_free([S(g["configs"][k], sl) for k in grp], None) == bool(g["batch8"][j])

@@ -125,11 +125,14 @@ def test_box_robot_cover_is_conservative(oracle):
     assert keep.sum() == 5 and 0.05 < free.mean() < 0.95
 
 
-REF_MUJOCO = (Path(os.environ.get("MRMG_REFERENCE_ROOT", "/root/reference")) / "src" / "multi_robot_multi_goal_planning"
-              / "assets" / "models" / "mujoco")
+# the reference checkout, named by MRMG_REFERENCE_ROOT (the test is skipped without it)
+_REF_ROOT = os.environ.get("MRMG_REFERENCE_ROOT", "")
+REF_MUJOCO = (Path(_REF_ROOT) / "src" / "multi_robot_multi_goal_planning" / "assets" / "models" / "mujoco"
+              if _REF_ROOT else None)
 
 
-@pytest.mark.skipif(not REF_MUJOCO.is_dir(), reason="the reference checkout is not on this machine")
+@pytest.mark.skipif(REF_MUJOCO is None or not REF_MUJOCO.is_dir(),
+                    reason="MRMG_REFERENCE_ROOT does not name a reference checkout")
 @pytest.mark.parametrize("name", ["mj_two_dim.xml", "mj_hallway.xml", "mj_manip.xml", "mj_piano.xml"])
 def test_reference_mujoco_scenes_import(oracle, name):
     """The reference's planar MuJoCo scene files (envs mujoco_env.py:891-1060)

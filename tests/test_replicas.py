@@ -104,3 +104,22 @@ def test_failed_rank_is_detected_by_the_other(tmp_path):
     assert not alive, "a rank hung instead of failing"
     outcome = (tmp_path / "rank0.txt").read_text()
     assert outcome.startswith("error:"), outcome
+
+
+def test_bench_spawns_its_own_replicas():
+    """`bench.py --gpus 2` without torchrun starts two replica processes
+    itself (gloo in the dry run: no GPU work) and rank 0 alone prints one
+    line whose n_gpus is the world size."""
+    import json
+    import subprocess
+    import sys
+
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--dry-run", "--steps", "3",
+                        "--warmup", "3"], capture_output=True, text=True, timeout=300,
+                       env={k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")})
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["n_gpus"] == 2 and d["config"]["parallelism"] == "replicas x2"
+    assert d["config"]["edges_total"] == 2 * d["config"]["edges_per_step"]
