@@ -212,6 +212,33 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene *scene, const void *d_q1, const
                                       int64_t N_start, int64_t N_max, uint8_t *d_out,
                                       void *stream, int32_t flags);
 
+/* Host-pointer forms of the two checks, for the planners' one-call-at-a-time
+ * pattern: is_collision_free (planning_env.py:1724-1734; callers
+ * planners/rrtstar_base.py:626-629 via the samplers,
+ * collision_free_sampler.py:110) and is_edge_collision_free
+ * (planning_env.py:1746-1763; callers rrtstar_base.py:626-629,
+ * prm_graph.py:675).  Inputs and verdicts are HOST memory: the library
+ * copies the inputs into a pinned staging buffer of the scene, moves them to
+ * the device in one copy together with the zeroed counters, checks them and
+ * returns the verdicts (1 = free) and the status in one copy back; the call
+ * is synchronous on the scene's own stream.  Arm scenes with up to 4,096
+ * configurations or 256 edges (65,536 edge positions) run one kernel launch
+ * in which every configuration or edge position is a warp's work item and a
+ * configuration left pending by the FP32 pass is decided in FP64 at once;
+ * other batches run the batched kernels on the staged inputs.  Verdicts and
+ * status codes are those of mrmg_is_collision_free_batch /
+ * mrmg_is_edge_collision_free_batch (robot_mask: 0 = every robot, else as
+ * mrmg_is_collision_free_batch_robots; arm scenes only).  Buffers: h_q /
+ * h_q1 / h_q2 hold n * q_dim values of `dtype`, h_N (optional) n int64, h_out
+ * n bytes.  Calls on one scene must not overlap (one staging buffer per
+ * scene); the staging buffer grows with the largest batch seen. */
+int mrmg_is_collision_free_host(mrmg_scene *scene, const void *h_q, int32_t dtype, int64_t n,
+                                uint32_t robot_mask, uint8_t *h_out, int32_t flags);
+int mrmg_is_edge_collision_free_host(mrmg_scene *scene, const void *h_q1, const void *h_q2, int32_t dtype,
+                                     int64_t n, double resolution, int32_t include_endpoints,
+                                     const int64_t *h_N, int64_t N_start, int64_t N_max, uint8_t *h_out,
+                                     int32_t flags);
+
 /* Edge check that allocates nothing.  No counterpart in the reference.
  * Same arguments, semantics and verdicts as mrmg_is_edge_collision_free_batch,
  * for callers that cannot allocate device memory while they check edges:

@@ -54,6 +54,8 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_is_collision_free_batch_robots": (i32, [vp, vp, i32, i64, C.c_uint32, vp, vp, i32]),
     "mrmg_is_edge_collision_free_batch": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, vp, i32]),
     "mrmg_is_edge_collision_free_batch_noalloc": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, vp, i32]),
+    "mrmg_is_collision_free_host": (i32, [vp, vp, i32, i64, C.c_uint32, vp, i32]),
+    "mrmg_is_edge_collision_free_host": (i32, [vp, vp, vp, i32, i64, f64, i32, vp, i64, i64, vp, i32]),
     "mrmg_arm_sphere_centers": (i32, [vp, vp, i32, i64, vp, vp, vp]),
     "mrmg_path_penetration": (i32, [vp, vp, i64, i32, vp, vp, vp, vp, vp, i32, vp, i32]),
     "mrmg_penetration_info": (i32, [vp, vp]),

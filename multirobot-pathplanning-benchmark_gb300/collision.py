@@ -54,6 +54,10 @@ def _dt_code(t: torch.Tensor) -> int:
     raise TypeError(f"configurations must be float32 or float64, got {t.dtype}")
 
 
+def _np_code(a: np.ndarray) -> int:
+    return _lib.MRMG_F32 if a.dtype == np.float32 else _lib.MRMG_F64
+
+
 class Gb300Scene:
     """One scene of libmrmg_gb300 on the current CUDA device."""
 
@@ -89,6 +93,13 @@ class Gb300Scene:
         _lib.check(rc, "scene create")
         self.h = h
         self.q_dim = scene.q_dim
+        # single-call buffers and bound entry points (no allocation per call)
+        self._one = np.zeros(1, dtype=np.uint8)
+        self._one_ptr = self._one.ctypes.data
+        self._N1 = np.zeros(1, dtype=np.int64)
+        self._N1_ptr = self._N1.ctypes.data
+        self._cfg_host = self.lib.mrmg_is_collision_free_host
+        self._edge_host = self.lib.mrmg_is_edge_collision_free_host
         self._slot_map = None
         self.mode = -1
         if self.kind == 1 and scene.n_modes:
@@ -214,6 +225,78 @@ class Gb300Scene:
             -1 if N_max is None else int(N_max), out.data_ptr(), _lib.stream_handle(stream), flags)
         _lib.check(rc, "is_edge_collision_free")
         return out
+
+    # --- host-pointer calls: the planners' one-at-a-time pattern ----------
+    # (inputs and verdicts in host memory; one staging copy each way, one
+    # launch for small arm batches, synchronous on the scene's own stream)
+    def _host_rows(self, x) -> np.ndarray:
+        a = np.asarray(x)
+        if a.dtype != np.float64 and a.dtype != np.float32:
+            a = a.astype(np.float64)
+        if a.ndim == 1:
+            a = a.reshape(1, -1)
+        if a.ndim != 2 or a.shape[1] != self.q_dim:
+            raise ValueError(f"configurations must be [n, {self.q_dim}] arrays")
+        if not a.flags.c_contiguous:
+            a = np.ascontiguousarray(a)
+        return a
+
+    def is_collision_free_host(self, q, robot_mask: int = 0, flags: int = 0) -> np.ndarray:
+        """Per-configuration verdicts (1 = free) for host configurations
+        q[n, q_dim] (numpy); robot_mask as is_collision_free_batch_robots
+        (0: every robot)."""
+        a = self._host_rows(q)
+        out = np.empty(a.shape[0], dtype=np.uint8)
+        _lib.check(self.lib.mrmg_is_collision_free_host(self.h, a.ctypes.data, _np_code(a), a.shape[0],
+                                                        int(robot_mask), out.ctypes.data, flags), "is_collision_free")
+        return out
+
+    def is_edge_collision_free_host(self, q1, q2, resolution: float, include_endpoints: bool = False, N=None,
+                                    N_start: int = 0, N_max=None, flags: int = 0) -> np.ndarray:
+        """Per-edge verdicts (1 = free) for host endpoint arrays q1, q2 [n, q_dim]."""
+        a = self._host_rows(q1)
+        b = self._host_rows(q2).astype(a.dtype, copy=False)
+        if a.shape != b.shape:
+            raise ValueError("edge endpoints must be [n, q_dim] arrays of equal shape")
+        n = a.shape[0]
+        Nh = None
+        if N is not None:
+            Nh = np.ascontiguousarray(np.asarray(N, dtype=np.int64).reshape(-1))
+            if Nh.shape[0] == 1 and n != 1:
+                Nh = np.repeat(Nh, n)
+            if Nh.shape[0] != n:
+                raise ValueError(f"N must hold one step count per edge: {Nh.shape[0]} for {n} edges")
+        out = np.empty(n, dtype=np.uint8)
+        rc = self.lib.mrmg_is_edge_collision_free_host(
+            self.h, a.ctypes.data, b.ctypes.data, _np_code(a), n, float(resolution if resolution is not None else 0.0),
+            int(bool(include_endpoints)), None if Nh is None else Nh.ctypes.data, int(N_start),
+            -1 if N_max is None else int(N_max), out.ctypes.data, flags)
+        _lib.check(rc, "is_edge_collision_free")
+        return out
+
+    def config_free1(self, q, robot_mask: int = 0) -> bool:
+        """One configuration (a float64 vector of q_dim values) -> bool."""
+        a = q if (type(q) is np.ndarray and q.dtype == np.float64 and q.flags.c_contiguous
+                  and q.size == self.q_dim) else self._host_rows(q)
+        _lib.check(self._cfg_host(self.h, a.ctypes.data, 1 if a.dtype == np.float64 else 0, 1, robot_mask,
+                                  self._one_ptr, 0), "is_collision_free")
+        return bool(self._one[0])
+
+    def edge_free1(self, q1, q2, resolution: float, include_endpoints: bool = False, N=None, N_start: int = 0,
+                   N_max=None) -> bool:
+        """One edge (two float64 vectors of q_dim values) -> bool."""
+        ok1 = type(q1) is np.ndarray and q1.dtype == np.float64 and q1.flags.c_contiguous and q1.size == self.q_dim
+        ok2 = type(q2) is np.ndarray and q2.dtype == np.float64 and q2.flags.c_contiguous and q2.size == self.q_dim
+        a = q1 if ok1 else self._host_rows(q1).astype(np.float64, copy=False)
+        b = q2 if ok2 else self._host_rows(q2).astype(np.float64, copy=False)
+        Np = None
+        if N is not None:
+            self._N1[0] = int(N)
+            Np = self._N1_ptr
+        _lib.check(self._edge_host(self.h, a.ctypes.data, b.ctypes.data, 1, 1, float(resolution),
+                                   1 if include_endpoints else 0, Np, int(N_start), -1 if N_max is None else int(N_max),
+                                   self._one_ptr, 0), "is_edge_collision_free")
+        return bool(self._one[0])
 
     # ------------------------------------------------------------------
     def slot_map(self) -> np.ndarray:

@@ -129,6 +129,15 @@ struct mrmg_scene {
   void* d_mode_tables = nullptr;
   ArmSrc src;
   ArmTables& tabs() { return cur_mode < 0 ? base : modes[cur_mode]; }
+  // host-pointer calls: the scene's own stream and one staging buffer (pinned
+  // host image + device copy) holding a call's counters, hits and inputs
+  cudaStream_t own_stream = nullptr;
+  unsigned char* h_stage = nullptr;   // mapped pinned host memory
+  unsigned char* m_stage = nullptr;   // its device address
+  unsigned char* d_stage = nullptr;   // device memory of the same size
+  size_t stage_cap = 0;
+  unsigned* d_small_flags = nullptr;  // single-launch path: per-edge "collides in call epoch" flags
+  unsigned small_epoch = 0;
 };
 
 namespace {
@@ -672,6 +681,11 @@ int mrmg_scene_destroy(mrmg_scene* sc) {
   if (sc->d_surv) cudaFree(sc->d_surv);
   if (sc->d_pen_seg) cudaFree(sc->d_pen_seg);
   if (sc->h_ctr) cudaFreeHost(sc->h_ctr);
+  if (sc->own_stream) cudaStreamSynchronize(sc->own_stream);
+  if (sc->h_stage) cudaFreeHost(sc->h_stage);
+  if (sc->d_stage) cudaFree(sc->d_stage);
+  if (sc->d_small_flags) cudaFree(sc->d_small_flags);
+  if (sc->own_stream) cudaStreamDestroy(sc->own_stream);
   delete sc;
   return MRMG_OK;
 }
@@ -849,6 +863,269 @@ int mrmg_status_from_error_bits(int32_t bits) {
   if (bits & E_BAD_INPUT) return fail(MRMG_ERR_ARG, "non-finite or out-of-range edge length (int() of nan/inf)");
   if (bits & E_TIMEOUT) return fail(MRMG_ERR_TIMEOUT, "a bounded device wait ran out");
   return MRMG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Host-pointer calls (the planners' one-at-a-time pattern).
+//
+// Small arm batches run one kernel launch that reads its inputs straight from
+// a mapped pinned staging buffer and writes its hits and statistics back into
+// it (zero-copy over the CPU-GPU link), so a call is: inputs written into the
+// buffer, one launch, one wait on the scene's own stream.  Everything else is
+// staged: the inputs cross to the device in one copy, the batched kernels run,
+// and the verdicts and counters come back in one copy each.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr long long kSmallEdges = 256;      // edges per call on the single-launch path
+constexpr long long kSmallItems = 1 << 16;  // (edge, position) items on that path
+constexpr long long kSmallConfigs = 4096;   // configurations per call on that path
+constexpr size_t kStageStats = 16 * 1024;   // per-CTA statistics at the head of the mapped buffer
+
+size_t pad16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+int ensure_stage(mrmg_scene* sc, size_t bytes) {
+  if (!sc->own_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&sc->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+  }
+  if (!sc->d_small_flags) {
+    cudaError_t e = cudaMalloc(&sc->d_small_flags, sizeof(unsigned) * kSmallConfigs);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(edge flags)");
+    e = cudaMemset(sc->d_small_flags, 0, sizeof(unsigned) * kSmallConfigs);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(edge flags)");
+  }
+  if (bytes <= sc->stage_cap) return MRMG_OK;
+  const size_t cap = std::max(bytes, std::max((size_t)65536, 2 * sc->stage_cap));
+  cudaError_t e = cudaStreamSynchronize(sc->own_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  if (sc->h_stage) cudaFreeHost(sc->h_stage);
+  if (sc->d_stage) cudaFree(sc->d_stage);
+  sc->h_stage = nullptr;
+  sc->m_stage = nullptr;
+  sc->d_stage = nullptr;
+  sc->stage_cap = 0;
+  e = cudaHostAlloc((void**)&sc->h_stage, cap, cudaHostAllocMapped);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaHostAlloc(staging)");
+  e = cudaHostGetDevicePointer((void**)&sc->m_stage, sc->h_stage, 0);
+  if (e == cudaSuccess) e = cudaMalloc(&sc->d_stage, cap);
+  if (e != cudaSuccess) {
+    cudaFreeHost(sc->h_stage);
+    sc->h_stage = nullptr;
+    sc->m_stage = nullptr;
+    return cuda_fail(e, "staging buffers");
+  }
+  sc->stage_cap = cap;
+  return MRMG_OK;
+}
+
+// the next call's flag epoch (flags of earlier calls never match it); the
+// flags are cleared when the 32-bit epoch wraps
+int next_epoch(mrmg_scene* sc, unsigned* ep) {
+  if (++sc->small_epoch == 0) {
+    cudaError_t e = cudaMemsetAsync(sc->d_small_flags, 0, sizeof(unsigned) * kSmallConfigs, sc->own_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(edge flags)");
+    sc->small_epoch = 1;
+  }
+  *ep = sc->small_epoch;
+  return MRMG_OK;
+}
+
+// N of one edge as the reference computes it (abstract_env.py:321-323):
+// max(2, int(max_k |q1_k - q2_k| / resolution) + 1); false when int() would
+// raise (NaN in the first coordinate, an infinite or huge quotient)
+bool host_edge_N(const void* q1, const void* q2, int dtype, long long e, int D, double res, long long* N) {
+  double m = 0.0;
+  bool nan0 = false;
+  for (int k = 0; k < D; k++) {
+    const double a = dtype == MRMG_F32 ? (double)((const float*)q1)[e * D + k] : ((const double*)q1)[e * D + k];
+    const double b = dtype == MRMG_F32 ? (double)((const float*)q2)[e * D + k] : ((const double*)q2)[e * D + k];
+    const double v = std::fabs(a - b);
+    if (k == 0) {
+      m = v;
+      nan0 = v != v;
+    } else if (v > m) {
+      m = v;
+    }
+  }
+  const double t = m / res;
+  if (nan0 || !(t < 9.0e15)) return false;
+  *N = std::max(2ll, (long long)t + 1);
+  return true;
+}
+
+// launch the single-launch kernel on the mapped buffer, wait, and fill the
+// scene's statistics from the per-CTA slots
+int run_small(mrmg_scene* sc, const ArmDev& a, SmallBatch& b) {
+  int grid = 0;
+  cudaError_t e = arm_small(a, b, sc->num_sms, sc->own_stream, &grid);
+  if (e != cudaSuccess) return cuda_fail(e, "launch small batch");
+  e = cudaStreamSynchronize(sc->own_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+  const int* st = (const int*)sc->h_stage;
+  long long cfg = 0, pend = 0;
+  for (int c = 0; c < grid; c++) {
+    cfg += st[2 * c];
+    pend += st[2 * c + 1];
+  }
+  std::memset(sc->h_ctr, 0, sizeof(int) * kNumCtr);
+  sc->h_ctr[kCtrPending] = (int)pend;
+  std::memcpy(sc->h_ctr + kCtrStat0, &cfg, sizeof(cfg));
+  return MRMG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mrmg_is_collision_free_host(mrmg_scene* sc, const void* h_q, int32_t dtype, int64_t n, uint32_t robot_mask,
+                                uint8_t* h_out, int32_t flags) try {
+  if (!sc) return fail(MRMG_ERR_ARG, "scene is NULL");
+  if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
+  if (n > kMaxBatch) return fail(MRMG_ERR_ARG, "batch of %lld exceeds %lld items; split it", (long long)n, kMaxBatch);
+  if (robot_mask && sc->kind != 1) return fail(MRMG_ERR_UNSUPPORTED, "per-robot checks need an arm scene");
+  if (sc->kind == 1) {
+    const uint32_t all = sc->arm.R >= 32 ? 0xffffffffu : ((1u << sc->arm.R) - 1u);
+    if (robot_mask & ~all) return fail(MRMG_ERR_ARG, "robot mask must select robots of the scene");
+  }
+  if (n == 0) return MRMG_OK;
+  if (!h_q || !h_out) return fail(MRMG_ERR_ARG, "NULL host pointer");
+  const size_t es = dtype == MRMG_F32 ? 4 : 8;
+  const size_t qbytes = (size_t)n * sc->q_dim * es;
+  const size_t o_hit = kStageStats, o_q = o_hit + pad16((size_t)n), total = o_q + pad16(qbytes);
+  int rc = ensure_stage(sc, total);
+  if (rc) return rc;
+  unsigned char* H = sc->h_stage;
+  ArmDev a = sc->arm;
+  if (robot_mask) a.robot_mask = robot_mask;
+  std::memset(H + o_hit, 0, (size_t)n);
+  std::memcpy(H + o_q, h_q, qbytes);
+  if (sc->kind == 1 && n <= kSmallConfigs && !(flags & MRMG_FLAG_FULL_EVAL) && arm_small_ok(a)) {
+    SmallBatch b{};
+    b.n = (int)n; b.items = (int)n; b.edges = 0; b.dtype = dtype; b.incl = 0; b.N_start = 0;
+    b.q1 = sc->m_stage + o_q; b.hit = sc->m_stage + o_hit; b.stats = (int*)sc->m_stage;
+    b.flags = sc->d_small_flags;
+    rc = next_epoch(sc, &b.epoch);
+    if (rc) return rc;
+    rc = run_small(sc, a, b);
+    if (rc) return rc;
+    for (long long i = 0; i < n; i++) h_out[i] = H[o_hit + i] ? 0 : 1;
+    return MRMG_OK;
+  }
+  cudaStream_t st = sc->own_stream;
+  unsigned char* Dv = sc->d_stage;
+  cudaError_t e = cudaMemcpyAsync(Dv + o_q, H + o_q, qbytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(inputs)");
+  rc = ensure_pending(sc, n, st);
+  if (rc) return rc;
+  e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  CallScratch cs{sc->d_ctr, sc->d_pend, sc->d_surv, sc->pend_cap};
+  LaunchShape ls = shape(sc);
+  if (sc->kind == 0) {
+    AbstractDev ab = sc->ab;
+    ab.sph_batch_form = (flags & MRMG_FLAG_BATCH_FORM) ? 1 : 0;
+    e = abstract_configs(ab, Dv + o_q, dtype, n, Dv + o_hit, cs, ls, st);
+  } else {
+    e = arm_configs(a, Dv + o_q, dtype, n, Dv + o_hit, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "launch configs");
+  e = cudaMemcpyAsync(H + o_hit, Dv + o_hit, (size_t)n, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(verdicts)");
+  rc = finish_call(sc, st, 0);
+  std::memcpy(h_out, H + o_hit, (size_t)n);
+  return rc;
+} catch (...) {
+  return host_fail();
+}
+
+int mrmg_is_edge_collision_free_host(mrmg_scene* sc, const void* h_q1, const void* h_q2, int32_t dtype, int64_t n,
+                                     double resolution, int32_t include_endpoints, const int64_t* h_N,
+                                     int64_t N_start, int64_t N_max, uint8_t* h_out, int32_t flags) try {
+  if (!sc) return fail(MRMG_ERR_ARG, "scene is NULL");
+  if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
+  if (!h_N && !(resolution > 0.0)) return fail(MRMG_ERR_ARG, "resolution must be > 0");
+  if (N_start < 0) return fail(MRMG_ERR_ARG, "N_start must be >= 0");
+  if (n > kMaxBatch) return fail(MRMG_ERR_ARG, "batch of %lld exceeds %lld items; split it", (long long)n, kMaxBatch);
+  if (n == 0) return MRMG_OK;
+  if (!h_q1 || !h_q2 || !h_out) return fail(MRMG_ERR_ARG, "NULL host pointer");
+  const int D = sc->q_dim;
+  const size_t es = dtype == MRMG_F32 ? 4 : 8;
+  const size_t qbytes = (size_t)n * D * es;
+  const size_t o_hit = kStageStats, o_off = o_hit + pad16((size_t)n), o_N32 = o_off + pad16(4 * ((size_t)n + 1)),
+               o_N64 = o_N32 + pad16(4 * (size_t)n), o_q1 = o_N64 + pad16(8 * (size_t)n),
+               o_q2 = o_q1 + pad16(qbytes), total = o_q2 + pad16(qbytes);
+  int rc = ensure_stage(sc, total);
+  if (rc) return rc;
+  unsigned char* H = sc->h_stage;
+  std::memset(H + o_hit, 0, (size_t)n);
+  std::memcpy(H + o_q1, h_q1, qbytes);
+  std::memcpy(H + o_q2, h_q2, qbytes);
+  // the single-launch path: arm scenes, few edges, every N known and valid
+  bool small = sc->kind == 1 && n <= kSmallEdges && !(flags & MRMG_FLAG_FULL_EVAL) && arm_small_ok(sc->arm);
+  long long items = 0;
+  if (small) {
+    int* off = (int*)(H + o_off);
+    int* N32 = (int*)(H + o_N32);
+    for (long long e = 0; e < n && small; e++) {
+      long long N = 0;
+      if (h_N) {
+        N = h_N[e];
+        small = N >= 2;
+      } else {
+        small = host_edge_N(h_q1, h_q2, dtype, e, D, resolution, &N);
+      }
+      small = small && N_start <= N && N <= (1ll << 24);
+      const long long nmax = (N_max < 0 || N_max > N) ? N : N_max;
+      off[e] = (int)items;
+      N32[e] = (int)N;
+      if (nmax > N_start) items += nmax - N_start;
+      small = small && items <= kSmallItems;
+    }
+    off[n] = (int)items;
+  }
+  if (small) {
+    SmallBatch b{};
+    b.n = (int)n; b.items = (int)items; b.edges = 1; b.dtype = dtype; b.incl = include_endpoints ? 1 : 0;
+    b.N_start = N_start;
+    b.off = (const int*)(sc->m_stage + o_off); b.N = (const int*)(sc->m_stage + o_N32);
+    b.q1 = sc->m_stage + o_q1; b.q2 = sc->m_stage + o_q2; b.hit = sc->m_stage + o_hit;
+    b.stats = (int*)sc->m_stage;
+    b.flags = sc->d_small_flags;
+    rc = next_epoch(sc, &b.epoch);
+    if (rc) return rc;
+    rc = run_small(sc, sc->arm, b);
+    if (rc) return rc;
+    for (long long i = 0; i < n; i++) h_out[i] = H[o_hit + i] ? 0 : 1;
+    return MRMG_OK;
+  }
+  if (h_N) std::memcpy(H + o_N64, h_N, 8 * (size_t)n);
+  cudaStream_t st = sc->own_stream;
+  unsigned char* Dv = sc->d_stage;
+  cudaError_t e = cudaMemcpyAsync(Dv + o_N64, H + o_N64, total - o_N64, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(inputs)");
+  rc = ensure_pending(sc, n, st);
+  if (rc) return rc;
+  e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  CallScratch cs{sc->d_ctr, sc->d_pend, sc->d_surv, sc->pend_cap};
+  LaunchShape ls = shape(sc);
+  const long long* dN = h_N ? (const long long*)(Dv + o_N64) : nullptr;
+  e = sc->kind == 0
+          ? abstract_edges(sc->ab, Dv + o_q1, Dv + o_q2, dtype, n, resolution, include_endpoints, dN, N_start, N_max,
+                           Dv + o_hit, cs, ls, st)
+          : arm_edges(sc->arm, Dv + o_q1, Dv + o_q2, dtype, n, resolution, include_endpoints, dN, N_start, N_max,
+                      Dv + o_hit, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch edges");
+  e = cudaMemcpyAsync(H + o_hit, Dv + o_hit, (size_t)n, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(verdicts)");
+  rc = finish_call(sc, st, 0);
+  std::memcpy(h_out, H + o_hit, (size_t)n);
+  return rc;
+} catch (...) {
+  return host_fail();
 }
 
 }  // extern "C"

@@ -1112,6 +1112,98 @@ __global__ void __launch_bounds__(256, GPL == 1 ? 3 : (GPL == 2 ? 2 : 1)) arm_ed
 
 
 
+// ---------------------------------------------------------------------------
+// Small synchronous batches (a planner's single is_collision_free /
+// is_edge_collision_free call, or a few): one launch that reads its inputs
+// from mapped pinned host memory and writes its hits there.  Items are the
+// configurations, or every (edge, position) pair of the edges' checked
+// position ranges, laid out edge by edge (offsets and step counts computed on
+// the host).  Warp w takes items w, w + W, ...; a configuration the FP32 pass
+// leaves pending is decided at once in FP64 by the same warp (the reference's
+// interpolation q1 + ((q2 - q1) / (N - 1)) * i for edge positions).  A
+// collision sets the edge's device flag to the call's epoch and its host hit
+// byte; positions of an edge already seen to collide are skipped.
+// ---------------------------------------------------------------------------
+template <int GPL, int SPG>
+__global__ void __launch_bounds__(128, 1) arm_small_kernel(ArmDev s, SmallBatch b) {
+  extern __shared__ __align__(16) unsigned char smem_arm[];
+  __shared__ int s_stat[2];
+  ArmSmem t;
+  stage_tables(s, smem_arm, &t);
+  if (threadIdx.x < 2) s_stat[threadIdx.x] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float2* wcs; float* wqv; float4* wsph; double* w64;
+  warp_areas(s, smem_arm, table_bytes(s), wib, true, &wcs, &wqv, &wsph, &w64);
+  const int D = s.D;
+  const int W = (int)(gridDim.x * (blockDim.x >> 5));
+  int stat_cfg = 0, stat_pend = 0;
+  volatile unsigned* flags = b.flags;
+  for (int it = (int)(blockIdx.x * (blockDim.x >> 5)) + wib; it < b.items; it += W) {
+    if (!b.edges) {
+      const CfgSource src{b.q1, b.dtype, (long long)it, D};
+      uint8_t code = eval_config<GPL, SPG, false>(s, t, wcs, wqv, wsph, w64, lane, src, false);
+      stat_cfg++;
+      if (code == V_PENDING) {
+        stat_pend++;
+        code = eval_config<GPL, SPG, true>(s, t, wcs, wqv, wsph, w64, lane, src, false);
+      }
+      if (lane == 0 && code == V_COLLIDE) b.hit[it] = 1;
+      __syncwarp();
+      continue;
+    }
+    // the edge holding item `it`: the last e with off[e] <= it
+    int lo = 0, hi = b.n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (b.off[mid] <= it) lo = mid;
+      else hi = mid - 1;
+    }
+    const int e = lo;
+    const long long N = b.N[e];
+    const long long iv = bfs_at(N, b.N_start + (it - b.off[e]));
+    if (!b.incl && (iv == 0 || iv == N - 1)) continue;
+    if (flags[e] == b.epoch) continue;                      // another position already collides
+    EdgeSourceDF sdf;
+    float mloc;
+    bool nanf;
+    load_edge(b.q1, b.q2, b.dtype, e, D, lane, &sdf, &mloc, &nanf);
+    sdf.nm1 = (float)(int)(N - 1);                          // N <= 2^24 on this path
+    sdf.rn = __frcp_rn(sdf.nm1);
+    sdf.fi = (float)(int)iv;
+    uint8_t code = eval_config<GPL, SPG, false, BOX_BLOCKS>(s, t, wcs, wqv, wsph, w64, lane, sdf, false);
+    stat_cfg++;
+    if (code == V_PENDING) {
+      stat_pend++;
+      EdgeSource64 s64;
+      const double denom = (double)(N - 1);
+#pragma unroll
+      for (int u = 0; u < kJPL; u++) {
+        const int j = lane + 32 * u;
+        s64.a1[u] = 0.0; s64.dir[u] = 0.0;
+        if (j < D) {
+          const double a = ldq(b.q1, b.dtype, (long long)e * D + j), c = ldq(b.q2, b.dtype, (long long)e * D + j);
+          s64.a1[u] = a;
+          s64.dir[u] = __ddiv_rn(__dsub_rn(c, a), denom);   // (q2 - q1) / (N - 1)
+        }
+      }
+      s64.di = (double)iv;
+      code = eval_config<GPL, SPG, true>(s, t, wcs, wqv, wsph, w64, lane, s64, false);
+    }
+    if (lane == 0 && code == V_COLLIDE) {
+      flags[e] = b.epoch;
+      b.hit[e] = 1;
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && stat_cfg) {
+    atomicAdd(&s_stat[0], stat_cfg);
+    if (stat_pend) atomicAdd(&s_stat[1], stat_pend);
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) b.stats[2 * blockIdx.x + threadIdx.x] = s_stat[threadIdx.x];
+}
+
 // sphere centres for the error-bound check: warp per configuration
 __global__ void arm_centers_kernel(ArmDev s, const void* q, int dtype, long long n, float* c32, double* c64) {
   extern __shared__ __align__(16) unsigned char smem_arm[];
@@ -1332,6 +1424,7 @@ int arm_prepare(const ArmDev& s, int warps) {
     cudaFuncSetAttribute(arm_configs_kernel<G_, S_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1); \
     cudaFuncSetAttribute(arm_configs_kernel<G_, S_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s2);  \
     cudaFuncSetAttribute(arm_edges_phase_b<G_, S_>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1);        \
+    cudaFuncSetAttribute(arm_small_kernel<G_, S_>, cudaFuncAttributeMaxDynamicSharedMemorySize, s3);         \
     err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, arm_edges_kernel<G_, S_, false>, warps * 32, \
                                                         smem_pass(s, warps, false));              \
   }
@@ -1379,6 +1472,32 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
   const int w2 = 2;
   return launch_edges<true>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc, ls.num_sms,
                             w2, smem_pass(s, w2, true), 0, st);
+}
+
+bool arm_small_ok(const ArmDev& s) {
+  // four warps with FP32 and FP64 work areas within the 227 KB a CTA can use
+  return arm_gpl_for_spg(s.SPG) > 0 && smem_pass(s, kSmallWarps, true) <= (size_t)227 * 1024;
+}
+
+cudaError_t arm_small(const ArmDev& s, const SmallBatch& b, int num_sms, cudaStream_t st, int* grid_out) {
+  *grid_out = 0;
+  if (b.items <= 0) return cudaSuccess;
+  const int gpl = arm_gpl_for_spg(s.SPG);
+  const int warps = kSmallWarps;
+  const size_t smem = smem_pass(s, warps, true);
+  const int grid = (int)std::max(1ll, std::min({(long long)(b.items + warps - 1) / warps, (long long)num_sms * 4,
+                                                (long long)kSmallMaxCtas}));
+  *grid_out = grid;
+#define MRMG_ARM_SMALL(G_, S_)                                                                     \
+  if (gpl == G_ && s.SPG == S_) {                                                                  \
+    arm_small_kernel<G_, S_><<<grid, warps * 32, smem, st>>>(s, b);                                \
+    return cudaGetLastError();                                                                     \
+  }
+  MRMG_ARM_SMALL(1, 6)
+  MRMG_ARM_SMALL(2, 5)
+  MRMG_ARM_SMALL(4, 8)
+#undef MRMG_ARM_SMALL
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t arm_box_hits(const ArmDev& s, const void* q, int dtype, long long n, uint32_t* hits, int words,

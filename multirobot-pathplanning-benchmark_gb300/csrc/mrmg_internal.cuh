@@ -109,6 +109,26 @@ struct LaunchShape {
   int num_sms;
 };
 
+// one small synchronous batch (arm_small): inputs, hits and statistics in
+// mapped pinned host memory, per-edge flags in device memory
+constexpr int kSmallWarps = 4;   // warps per CTA of the small-batch kernel
+constexpr int kSmallMaxCtas = 2048;
+struct SmallBatch {
+  int n;                 // configurations or edges
+  int items;             // configurations, or the edges' position ranges summed
+  int edges;             // 0: configurations, 1: edges
+  int dtype, incl;
+  long long N_start;
+  const int* off;        // [n + 1] first item of each edge
+  const int* N;          // [n]     step count of each edge (<= 2^24)
+  const void* q1;        // [n, D]  configurations, or the edges' first endpoints
+  const void* q2;        // [n, D]  the edges' second endpoints
+  uint8_t* hit;          // [n]     set to 1 on a collision (zeroed by the caller)
+  int* stats;            // [2 * CTAs] per CTA: configurations evaluated, FP64 decisions
+  unsigned* flags;       // [n]     device: edge e collides in this call iff flags[e] == epoch
+  unsigned epoch;
+};
+
 struct SliceTab {
   int A, D, end_all;
   int s[64], e[64];
@@ -155,6 +175,8 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
                       double res, int incl, const long long* Np, long long N_start,
                       long long N_max, uint8_t* out, const CallScratch& sc,
                       const LaunchShape& ls, int full, cudaStream_t st);
+bool arm_small_ok(const ArmDev& s);   // the single-launch kernel fits the scene's shared memory
+cudaError_t arm_small(const ArmDev& s, const SmallBatch& b, int num_sms, cudaStream_t st, int* grid_out);
 cudaError_t arm_box_hits(const ArmDev& s, const void* q, int dtype, long long n, uint32_t* hits, int words,
                          cudaStream_t st);
 cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, float* c32,

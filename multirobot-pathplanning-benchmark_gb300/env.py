@@ -107,11 +107,12 @@ class Gb300CollisionBackend:
 
     # --- single queries (planning_env.py:1724-1763) ------------------------
     def is_collision_free(self, q, mode) -> bool:
+        """One configuration from host memory: one staged copy each way and,
+        on arm scenes, one kernel launch (Gb300Scene.config_free1)."""
         if q is None:
             raise ValueError
         self._use_mode(mode)
-        v = self._gb300.is_collision_free_batch(_state(q).reshape(1, -1))
-        return bool(v.item())
+        return self._gb300.config_free1(_state(q))
 
     def is_edge_collision_free(self, q1, q2, mode, resolution: Optional[float] = None,
                                tolerance: Optional[float] = None, include_endpoints: bool = False,
@@ -122,9 +123,7 @@ class Gb300CollisionBackend:
         if N is not None and N_start > N:
             raise AssertionError
         self._use_mode(mode)
-        v = self._gb300.is_edge_collision_free_batch(a.reshape(1, -1), b.reshape(1, -1), resolution,
-                                                     include_endpoints, None if N is None else [int(N)], N_start, N_max)
-        return bool(v.item())
+        return self._gb300.edge_free1(a, b, resolution, include_endpoints, N, N_start, N_max)
 
     def is_collision_free_for_robot(self, r, q, m=None, collision_tolerance: Optional[float] = None,
                                     set_mode: bool = True) -> bool:
@@ -135,8 +134,7 @@ class Gb300CollisionBackend:
         for the signature; the engines' summed-penetration allowance is not
         modelled)."""
         self._use_mode(m)
-        v = self._gb300.is_collision_free_batch_robots(_state(q).reshape(1, -1), self._robot_mask(r))
-        return bool(v.item())
+        return self._gb300.config_free1(_state(q), self._robot_mask(r))
 
     def batch_is_collision_free_for_robot(self, r, qs, mode=None) -> np.ndarray:
         """Per-configuration verdicts of is_collision_free_for_robot."""
