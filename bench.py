@@ -746,6 +746,13 @@ def bench_abstract(orc, reps: int = 20) -> dict:
         return float(np.median(ts)) * 1e3
 
     edge_graph_ms, cfg_graph_ms = wall(plan.run), wall(cfg_run)
+    # the host-pointer calls (numpy in, numpy verdicts out: what the env's
+    # batch methods run for host arrays): inputs through mapped pinned memory,
+    # one launch, one wait
+    h_cfg = s.is_collision_free_host(q)
+    h_edge = s.is_edge_collision_free_host(q1, q2, 0.01)
+    host_cfg_ms = wall(lambda: s.is_collision_free_host(q))
+    host_edge_ms = wall(lambda: s.is_edge_collision_free_host(q1, q2, 0.01))
     t0 = time.perf_counter()
     ref_d = orc.dist_matrix(q1, q, sl, "euclidean")
     cpu_mat_s = time.perf_counter() - t0
@@ -772,6 +779,12 @@ def bench_abstract(orc, reps: int = 20) -> dict:
                     "graph_e2e": {"ms_per_call": cfg_graph_ms, "configs_per_s": 1e4 / (cfg_graph_ms * 1e-3),
                                   "mismatches": int((g_cfg != ref_v).sum()),
                                   "h2d_bytes": int(q.nbytes), "d2h_bytes": len(q)}},
+        "configs_host_call": {"ms_per_call": host_cfg_ms, "configs_per_s": 1e4 / (host_cfg_ms * 1e-3),
+                              "mismatches": int((h_cfg != ref_v).sum()),
+                              "api": "Gb300Scene.is_collision_free_host(numpy [10000, 4])"},
+        "edges_host_call": {"ms_per_call": host_edge_ms, "edges_per_s": 1e3 / (host_edge_ms * 1e-3),
+                            "mismatches": int((h_edge != ref_e).sum()),
+                            "api": "Gb300Scene.is_edge_collision_free_host(numpy [1000, 4] x 2, 0.01)"},
         "edges": {"ms_per_call": edge_ms, "edges_per_s": 1e3 / (edge_ms * 1e-3),
                   "mismatches": int((e.cpu().numpy() != ref_e).sum()), "cpu_edges_per_s": 1e3 / cpu_edge_s,
                   "graph_e2e": {"ms_per_call": edge_graph_ms, "edges_per_s": 1e3 / (edge_graph_ms * 1e-3),
@@ -961,6 +974,9 @@ def _summary(line: dict) -> dict:
         out[f"knn_{m}_index_mismatches"] = g("knn", m, "index_mismatches")
         out[f"knn_{m}_tensor_frac"] = g("knn", m, "roofline", "frac")
     out["abstract_edges_per_s"] = g("abstract", "edges", "edges_per_s")
+    out["abstract_host_call_edges_per_s"] = g("abstract", "edges_host_call", "edges_per_s")
+    out["abstract_configs_per_s"] = g("abstract", "configs", "configs_per_s")
+    out["abstract_cpu_configs_per_s"] = g("abstract", "configs", "cpu_configs_per_s")
     out["abstract_cpu_edges_per_s"] = g("abstract", "edges", "cpu_edges_per_s")
     out["serving_p50_p99_ms"] = [g("serving", "latency", "p50_ms"), g("serving", "latency", "p99_ms")]
     out["penetration_ms_cost_and_grad"] = g("penetration", "ms_cost_and_grad")

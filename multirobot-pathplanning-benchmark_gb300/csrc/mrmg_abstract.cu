@@ -3,13 +3,12 @@
 // AbstractEnvironment.is_collision_free :255-276, is_edge_collision_free
 // :301-354).
 //
-// Two passes per call:
-//  pass 1  FP32 classification of every configuration against a band that
-//          bounds the FP32 error: definitely colliding, definitely free, or
-//          pending.  An item with a definite collision is decided; an item
-//          whose only doubt is a pending configuration is queued.
-//  pass 2  the queued items again, with each pending configuration decided
-//          by the exact FP64 restatement of the reference's arithmetic.
+// Every configuration is first classified in FP32 against a band that
+// bounds the FP32 error: definitely colliding, definitely free, or pending.
+// A pending configuration is decided by the exact FP64 restatement of the
+// reference's arithmetic: at once, by the warp that met it (configurations
+// and edge batches up to kFlatMaxEdges: one launch per call), or, for larger
+// edge batches, in a second pass over the queued edges.
 //
 // The FP64 pipe of this part is narrow and issues a warp instruction at the
 // same cost whatever the number of active lanes, so FP64 work is kept off
@@ -17,6 +16,8 @@
 // FP32, step counts come from an FP32 quotient with an integer-distance
 // certificate, and a pending configuration is decided by a whole warp at
 // once, one agent pair, box or sphere test per lane.
+#include <algorithm>
+
 #include "mrmg_internal.cuh"
 
 namespace mrmg {
@@ -237,45 +238,6 @@ __device__ AbstractDev staged_view(const AbstractDev& s, unsigned char* sm) {
 }
 
 // ---------------------------------------------------------------------------
-// Configurations: one thread per configuration in pass 1, one warp per
-// pending configuration in pass 2.
-// ---------------------------------------------------------------------------
-__global__ void configs_pass1(AbstractDev s, const void* q, int dtype, long long n, uint8_t* out,
-                              int* ctr, long long* pend) {
-  extern __shared__ double sm_cfg[];
-  const AbstractDev cs = staged_view(s, (unsigned char*)sm_cfg);
-  __syncthreads();
-  const int D = s.D;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    auto x = [&](int k) {
-      return dtype == MRMG_F32 ? ((const float*)q)[i * D + k] : (float)((const double*)q)[i * D + k];
-    };
-    uint8_t v = classify32(cs, x, 0.f);
-    out[i] = v;
-    if (v == V_PENDING) {
-      int slot = atomicAdd(&ctr[kCtrPending], 1);
-      pend[slot] = i;
-    }
-  }
-}
-
-__global__ void configs_pass2(AbstractDev s, const void* q, int dtype, uint8_t* out, const int* ctr,
-                              const long long* pend) {
-  const int D = s.D;
-  const int np = ctr[kCtrPending];
-  const int lane = threadIdx.x & 31;
-  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int n_warps = (int)((gridDim.x * blockDim.x) >> 5);
-  for (int k = warp; k < np; k += n_warps) {
-    const long long i = pend[k];
-    auto acc = [&](int j) { return ldq(q, dtype, i * D + j); };
-    const bool ok = exact_free_warp(s, acc, lane);
-    if (lane == 0) out[i] = ok ? 1 : 0;
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Edges: one warp per edge; the lanes check consecutive chunks of the
 // reference's binary-search order, with a warp vote after each chunk.
 //
@@ -463,23 +425,266 @@ __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Single-launch forms.  A pending classification is decided at once by the
+// warp that met it (the lanes' pending items are taken one by one, each by
+// the whole warp with the exact FP64 restatement), so no second pass, no
+// pending list and no counter reset are needed: one launch per call.
+// ctr may be NULL (no statistics, and no error bits: the host-pointer calls
+// validate step counts on the host before launching).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) configs_fused_kernel(AbstractDev s, const void* q, int dtype, long long n,
+                                                            uint8_t* out, int* ctr) {
+  extern __shared__ double sm_cfg[];
+  const AbstractDev cs = staged_view(s, (unsigned char*)sm_cfg);
+  __syncthreads();
+  const int D = s.D;
+  const int lane = threadIdx.x & 31;
+  int npend = 0;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x; i0 < n; i0 += (long long)gridDim.x * blockDim.x) {
+    const long long i = i0 + threadIdx.x;
+    uint8_t v = V_FREE;
+    if (i < n) {
+      auto x = [&](int k) {
+        return dtype == MRMG_F32 ? ((const float*)q)[i * D + k] : (float)((const double*)q)[i * D + k];
+      };
+      v = classify32(cs, x, 0.f);
+    }
+    unsigned pm = __ballot_sync(MRMG_FULL, v == V_PENDING);
+    npend += __popc(pm);
+    while (pm) {
+      const int src = __ffs(pm) - 1;
+      pm &= pm - 1;
+      const long long j = __shfl_sync(MRMG_FULL, i, src);
+      auto acc = [&](int k) { return ldq(q, dtype, j * D + k); };
+      const bool ok = exact_free_warp(s, acc, lane);
+      if (lane == src) v = ok ? V_FREE : V_COLLIDE;
+    }
+    if (i < n) out[i] = v;
+  }
+  if (ctr && lane == 0 && npend) atomicAdd(&ctr[kCtrPending], npend);
+}
+
+// Edges, flat: each CTA takes `epc` edges at a time; its warps compute the
+// edges' step counts and double-float endpoints, then every thread takes
+// (edge, BFS position) items of the group, so the positions of an edge are
+// checked side by side instead of chunk after chunk by one warp.  A position
+// of an edge already seen to collide is skipped.
+constexpr int kFlatMaxEpc = 8;
+
+__global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const void* q1, const void* q2, int dtype,
+                                                         long long n, double res, int incl, const long long* Np,
+                                                         long long N_start, long long N_max, uint8_t* out, int* ctr,
+                                                         int epc, uint8_t* cta_err) {
+  extern __shared__ double sm_ab[];
+  const AbstractDev cs = staged_view(s, (unsigned char*)sm_ab);
+  __shared__ int s_err;   // error bits of this CTA when reported per CTA (cta_err)
+  __shared__ long long sN[kFlatMaxEpc];
+  __shared__ int soff[kFlatMaxEpc + 1];
+  __shared__ float sext[kFlatMaxEpc];
+  __shared__ int sst[kFlatMaxEpc];   // bit 0 collides, bit 1 decided already (error, or positions beyond FP32)
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int D = s.D;
+  float* eah = (float*)((unsigned char*)sm_ab + tab_bytes(s));   // [epc][D] x 4 arrays
+  float* eal = eah + kFlatMaxEpc * D;
+  float* edh = eal + kFlatMaxEpc * D;
+  float* edl = edh + kFlatMaxEpc * D;
+  const float res32 = (float)res;
+  int npend = 0;
+  if (threadIdx.x == 0) s_err = 0;
+  __syncthreads();
+  for (long long e0 = (long long)blockIdx.x * epc; e0 < n; e0 += (long long)gridDim.x * epc) {
+    const int ne = (int)min((long long)epc, n - e0);
+    // ---- per edge: endpoints as double-float, N, error checks
+    for (int w = wib; w < ne; w += nw) {
+      const long long e = e0 + w;
+      float mloc = 0.f, emax = 0.f;
+      bool nanf = false;
+      for (int k = lane; k < D; k += 32) {
+        float a_h, a_l = 0.f, d_h, d_l;
+        if (dtype == MRMG_F32) {
+          const float a = ((const float*)q1)[e * D + k], b = ((const float*)q2)[e * D + k];
+          a_h = a;
+          two_sum(b, -a, &d_h, &d_l);
+        } else {
+          const double a = ((const double*)q1)[e * D + k], b = ((const double*)q2)[e * D + k];
+          const double d = __dsub_rn(b, a);
+          a_h = (float)a;
+          a_l = (float)__dsub_rn(a, (double)a_h);
+          d_h = (float)d;
+          d_l = (float)__dsub_rn(d, (double)d_h);
+        }
+        eah[w * D + k] = a_h; eal[w * D + k] = a_l; edh[w * D + k] = d_h; edl[w * D + k] = d_l;
+        nanf |= d_h != d_h;
+        mloc = fmaxf(mloc, fabsf(d_h));
+        emax = fmaxf(emax, fabsf(a_h) + fabsf(__fadd_rn(a_h, d_h)));
+      }
+      long long N = 2;
+      bool bad = false;
+      if (Np) {
+        N = Np[e];
+        bad = N < 1;
+      } else {
+        const float m32 = warp_max(mloc);
+        const bool anynan = __any_sync(MRMG_FULL, nanf);
+        if (!steps_fp32(m32, anynan, res32, &N)) {
+          // config_dist(q1, q2, "max") / resolution in FP64 (abstract_env.py:321-323)
+          double mx = -1.0;
+          bool nan0 = false;
+          for (int k = lane; k < D; k += 32) {
+            const double v = fabs(__dsub_rn(ldq(q1, dtype, e * D + k), ldq(q2, dtype, e * D + k)));
+            if (k == 0) nan0 = (v != v);
+            mx = fmax(mx, v);
+          }
+          const double m = warp_max_d(mx);
+          nan0 = __any_sync(MRMG_FULL, nan0);
+          const double t = __ddiv_rn(m, res);
+          if (nan0 || !(t < 9.0e15)) bad = true;
+          N = bad ? 2 : (long long)t + 1;
+          if (N < 2) N = 2;
+        }
+      }
+      const float ext = ldexpf(warp_max(emax) * (float)s.dim, -30);
+      if (lane == 0) {
+        sN[w] = N;
+        sext[w] = ext;
+        sst[w] = 0;
+        if (bad || N_start > N) {   // the reference raises / asserts (abstract_env.py:321-326)
+          if (ctr) atomicOr(&ctr[kCtrErr], bad ? E_BAD_INPUT : E_N_START);
+          else atomicOr(&s_err, bad ? E_BAD_INPUT : E_N_START);
+          out[e] = 0;
+          sst[w] = 2;
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      for (int w = 0; w < ne; w++) {
+        soff[w] = acc;
+        const long long N = sN[w];
+        const long long nmax = (N_max < 0 || N_max > N) ? N : N_max;
+        if (!(sst[w] & 2) && nmax > N_start) acc += (int)(nmax - N_start);
+      }
+      soff[ne] = acc;
+    }
+    __syncthreads();
+    const int total = soff[ne];
+    for (int t0 = 0; t0 < total; t0 += blockDim.x) {
+      const int t = t0 + threadIdx.x;
+      int w = 0;
+      long long iv = -1, N = 2;
+      uint8_t code = V_FREE;
+      if (t < total) {
+        while (t >= soff[w + 1]) w++;
+        N = sN[w];
+        iv = bfs_at(N, N_start + (t - soff[w]));
+        const bool skip = (!incl && (iv == 0 || iv == N - 1)) || (*(volatile int*)&sst[w] & 1);
+        if (skip) {
+          iv = -1;
+        } else if (N <= (1ll << 24)) {
+          const float nm1 = (float)(int)(N - 1), rn = __frcp_rn(nm1), fi = (float)(int)iv;
+          const float* ah = eah + w * D; const float* al = eal + w * D;
+          const float* dh = edh + w * D; const float* dl = edl + w * D;
+          auto x = [&](int k) {
+            float h, l;
+            interp_df(ah[k], al[k], dh[k], dl[k], fi, nm1, rn, &h, &l);
+            return __fadd_rn(h, l);
+          };
+          code = classify32(cs, x, sext[w]);
+        } else {
+          code = V_PENDING;   // positions beyond exact FP32 integers: FP64 at once
+        }
+      }
+      // pending positions: the reference's FP64 position q1 + ((q2 - q1) / (N - 1)) * i, decided by the warp
+      unsigned pm = __ballot_sync(MRMG_FULL, code == V_PENDING);
+      npend += __popc(pm);
+      while (pm) {
+        const int src = __ffs(pm) - 1;
+        pm &= pm - 1;
+        const int ws = __shfl_sync(MRMG_FULL, w, src);
+        const long long Ns = __shfl_sync(MRMG_FULL, N, src);
+        const double di = (double)__shfl_sync(MRMG_FULL, iv, src);
+        const long long e = e0 + ws;
+        const double denom = (double)(Ns - 1);
+        auto acc = [&](int k) {
+          const double a = ldq(q1, dtype, e * D + k), b = ldq(q2, dtype, e * D + k);
+          return __dadd_rn(a, __dmul_rn(__ddiv_rn(__dsub_rn(b, a), denom), di));
+        };
+        const bool ok = exact_free_warp(s, acc, lane);
+        if (lane == src) code = ok ? V_FREE : V_COLLIDE;
+      }
+      if (t < total && code == V_COLLIDE) atomicOr(&sst[w], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < ne && !(sst[threadIdx.x] & 2)) out[e0 + threadIdx.x] = (sst[threadIdx.x] & 1) ? V_COLLIDE : V_FREE;
+    __syncthreads();
+  }
+  if (ctr && lane == 0 && npend) atomicAdd(&ctr[kCtrPending], npend);
+  if (cta_err && threadIdx.x == 0) cta_err[blockIdx.x] = (uint8_t)s_err;   // after the loop's last barrier
+}
+
 }  // namespace
 
 cudaError_t abstract_configs(const AbstractDev& s, const void* q, int dtype, long long n,
                              uint8_t* out, const CallScratch& sc, const LaunchShape& ls,
                              cudaStream_t st) {
-  int threads = 256;
-  long long want = (n + threads - 1) / threads;
-  int grid = (int)(want < (long long)ls.num_sms * 8 ? (want > 0 ? want : 1) : (long long)ls.num_sms * 8);
-  configs_pass1<<<grid, threads, tab_bytes(s), st>>>(s, q, dtype, n, out, sc.ctr, sc.pend);
-  configs_pass2<<<ls.num_sms, 128, 0, st>>>(s, q, dtype, out, sc.ctr, sc.pend);
+  const int threads = 256;
+  const long long want = (n + threads - 1) / threads;
+  const int grid = (int)(want < (long long)ls.num_sms * 8 ? (want > 0 ? want : 1) : (long long)ls.num_sms * 8);
+  configs_fused_kernel<<<grid, threads, tab_bytes(s), st>>>(s, q, dtype, n, out, sc.ctr);
   return cudaGetLastError();
+}
+
+// edges per CTA of the flat kernel: enough CTAs to fill the GPU
+static int flat_epc(long long n, int num_sms) {
+  const long long per = (n + (long long)num_sms * 4 - 1) / ((long long)num_sms * 4);
+  return (int)std::max(1ll, std::min((long long)kFlatMaxEpc, per));
+}
+
+static size_t flat_smem(const AbstractDev& s) { return tab_bytes(s) + (size_t)kFlatMaxEpc * s.D * 16; }
+
+cudaError_t abstract_configs_mapped(const AbstractDev& s, const void* q, int dtype, long long n, uint8_t* out,
+                                    int num_sms, cudaStream_t st) {
+  const int threads = 256;
+  const long long want = (n + threads - 1) / threads;
+  const int grid = (int)std::max(1ll, std::min(want, (long long)num_sms * 8));
+  configs_fused_kernel<<<grid, threads, tab_bytes(s), st>>>(s, q, dtype, n, out, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t abstract_edges_mapped(const AbstractDev& s, const void* q1, const void* q2, int dtype, long long n,
+                                  double res, int incl, const long long* Np, long long N_start, long long N_max,
+                                  uint8_t* out, uint8_t* cta_err, int num_sms, cudaStream_t st, int* grid_out) {
+  const int epc = flat_epc(n, num_sms);
+  const long long want = (n + epc - 1) / epc;
+  const int grid = (int)std::max(1ll, std::min(want, (long long)num_sms * 8));
+  *grid_out = grid;
+  edges_flat_kernel<<<grid, 256, flat_smem(s), st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out,
+                                                       nullptr, epc, cta_err);
+  return cudaGetLastError();
+}
+
+int abstract_prepare(const AbstractDev& s) {
+  const size_t sm = flat_smem(s);
+  if (sm > 48 * 1024 && cudaFuncSetAttribute(edges_flat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sm) != cudaSuccess)
+    return -1;
+  return 0;
 }
 
 cudaError_t abstract_edges(const AbstractDev& s, const void* q1, const void* q2, int dtype,
                            long long n, double res, int incl, const long long* Np,
                            long long N_start, long long N_max, uint8_t* out,
                            const CallScratch& sc, const LaunchShape& ls, cudaStream_t st) {
+  if (n <= kFlatMaxEdges) {
+    const int epc = flat_epc(n, ls.num_sms);
+    const long long want = (n + epc - 1) / epc;
+    const int grid = (int)std::min(want, (long long)ls.num_sms * 8);
+    edges_flat_kernel<<<grid, 256, flat_smem(s), st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out,
+                                                         sc.ctr, epc, nullptr);
+    return cudaGetLastError();
+  }
   const int warps = 8;
   const size_t smem1 = tab_bytes(s) + (size_t)warps * edge_warp_bytes(s.D, false);
   const size_t smem2 = (size_t)warps * edge_warp_bytes(s.D, true);

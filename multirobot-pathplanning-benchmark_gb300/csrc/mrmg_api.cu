@@ -415,6 +415,7 @@ int mrmg_abstract_scene_create(int32_t n_agents, int32_t dim, int32_t q_dim, con
   blk.add(sthr32.data(), sthr32.size(), &d.sph_thr32);
   cudaError_t e = blk.upload(&sc->d_tables);
   if (e != cudaSuccess) { mrmg_scene_destroy(sc); return cuda_fail(e, "upload abstract scene"); }
+  if (abstract_prepare(sc->ab)) { mrmg_scene_destroy(sc); return fail(MRMG_ERR_UNSUPPORTED, "scene too large"); }
   sc->band = d.delta_k * d.omax;
   *out = sc;
   return MRMG_OK;
@@ -1002,6 +1003,18 @@ int mrmg_is_collision_free_host(mrmg_scene* sc, const void* h_q, int32_t dtype, 
   if (robot_mask) a.robot_mask = robot_mask;
   std::memset(H + o_hit, 0, (size_t)n);
   std::memcpy(H + o_q, h_q, qbytes);
+  if (sc->kind == 0 && n <= kSmallConfigs) {
+    // one launch on the mapped buffer, verdicts written straight into it
+    AbstractDev ab = sc->ab;
+    ab.sph_batch_form = (flags & MRMG_FLAG_BATCH_FORM) ? 1 : 0;
+    cudaError_t e = abstract_configs_mapped(ab, sc->m_stage + o_q, dtype, n, sc->m_stage + o_hit, sc->num_sms,
+                                            sc->own_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "launch configs");
+    e = cudaStreamSynchronize(sc->own_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+    std::memcpy(h_out, H + o_hit, (size_t)n);
+    return MRMG_OK;
+  }
   if (sc->kind == 1 && n <= kSmallConfigs && !(flags & MRMG_FLAG_FULL_EVAL) && arm_small_ok(a)) {
     SmallBatch b{};
     b.n = (int)n; b.items = (int)n; b.edges = 0; b.dtype = dtype; b.incl = 0; b.N_start = 0;
@@ -1085,6 +1098,25 @@ int mrmg_is_edge_collision_free_host(mrmg_scene* sc, const void* h_q1, const voi
       small = small && items <= kSmallItems;
     }
     off[n] = (int)items;
+  }
+  if (sc->kind == 0 && n <= kFlatMaxEdges) {
+    // abstract scenes: the flat edge kernel on the mapped buffer; its error
+    // bits come back per CTA in the head of the buffer
+    if (h_N) std::memcpy(H + o_N64, h_N, 8 * (size_t)n);
+    int grid = 0;
+    cudaError_t e = abstract_edges_mapped(sc->ab, sc->m_stage + o_q1, sc->m_stage + o_q2, dtype, n, resolution,
+                                          include_endpoints, h_N ? (const long long*)(sc->m_stage + o_N64) : nullptr,
+                                          N_start, N_max, sc->m_stage + o_hit, sc->m_stage, sc->num_sms,
+                                          sc->own_stream, &grid);
+    if (e != cudaSuccess) return cuda_fail(e, "launch edges");
+    e = cudaStreamSynchronize(sc->own_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+    int bits = 0;
+    for (int c = 0; c < grid; c++) bits |= H[c];
+    std::memset(sc->h_ctr, 0, sizeof(int) * kNumCtr);
+    sc->h_ctr[kCtrErr] = bits;
+    std::memcpy(h_out, H + o_hit, (size_t)n);
+    return bits ? mrmg_status_from_error_bits(bits) : MRMG_OK;
   }
   if (small) {
     SmallBatch b{};

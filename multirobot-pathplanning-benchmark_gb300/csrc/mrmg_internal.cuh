@@ -164,10 +164,20 @@ __device__ __forceinline__ double dist_of(const SliceTab& t, int metric, Diff d)
 cudaError_t abstract_configs(const AbstractDev& s, const void* q, int dtype, long long n,
                              uint8_t* out, const CallScratch& sc, const LaunchShape& ls,
                              cudaStream_t st);
+// edges per call up to which the abstract edge check runs the flat single-launch kernel
+constexpr long long kFlatMaxEdges = 65536;
 cudaError_t abstract_edges(const AbstractDev& s, const void* q1, const void* q2, int dtype,
                            long long n, double res, int incl, const long long* Np,
                            long long N_start, long long N_max, uint8_t* out,
                            const CallScratch& sc, const LaunchShape& ls, cudaStream_t st);
+int abstract_prepare(const AbstractDev& s);   // kernel attributes, once per scene (before any capture)
+// single launches on caller-visible (e.g. mapped host) buffers, no counters;
+// the edge kernel reports its error bits per CTA in cta_err[grid] (plain stores)
+cudaError_t abstract_configs_mapped(const AbstractDev& s, const void* q, int dtype, long long n, uint8_t* out,
+                                    int num_sms, cudaStream_t st);
+cudaError_t abstract_edges_mapped(const AbstractDev& s, const void* q1, const void* q2, int dtype, long long n,
+                                  double res, int incl, const long long* Np, long long N_start, long long N_max,
+                                  uint8_t* out, uint8_t* cta_err, int num_sms, cudaStream_t st, int* grid_out);
 
 cudaError_t arm_configs(const ArmDev& s, const void* q, int dtype, long long n, uint8_t* out,
                         const CallScratch& sc, const LaunchShape& ls, int full, cudaStream_t st);

@@ -139,8 +139,9 @@ class Gb300CollisionBackend:
     def batch_is_collision_free_for_robot(self, r, qs, mode=None) -> np.ndarray:
         """Per-configuration verdicts of is_collision_free_for_robot."""
         self._use_mode(mode)
-        v = self._gb300.is_collision_free_batch_robots(qs, self._robot_mask(r))
-        return v.bool().cpu().numpy() if not isinstance(qs, torch.Tensor) else v.bool()
+        if isinstance(qs, torch.Tensor):
+            return self._gb300.is_collision_free_batch_robots(qs, self._robot_mask(r)).bool()
+        return self._gb300.is_collision_free_host(qs, self._robot_mask(r)).view(np.bool_)
 
     def _robot_mask(self, r) -> int:
         names = [r] if isinstance(r, str) else list(r)
@@ -162,15 +163,18 @@ class Gb300CollisionBackend:
         if len(qs) == 0:
             return True
         self._use_mode(mode)
-        v = self._gb300.is_collision_free_batch(np.array([_state(q) for q in qs]), flags=_lib.MRMG_FLAG_BATCH_FORM)
-        return bool(v.bool().all().item())
+        v = self._gb300.is_collision_free_host(np.array([_state(q) for q in qs]), flags=_lib.MRMG_FLAG_BATCH_FORM)
+        return bool(v.all())
 
     # --- batched (additive) ------------------------------------------------
     def batch_is_collision_free(self, qs, mode=None) -> np.ndarray:
-        """Per-configuration verdicts for an [n, D] array (or device tensor)."""
+        """Per-configuration verdicts for an [n, D] array (host memory: one
+        staged call, numpy bools back) or device tensor (checked in place,
+        bool tensor back)."""
         self._use_mode(mode)
-        v = self._gb300.is_collision_free_batch(qs)
-        return v.bool().cpu().numpy() if not isinstance(qs, torch.Tensor) else v.bool()
+        if isinstance(qs, torch.Tensor):
+            return self._gb300.is_collision_free_batch(qs).bool()
+        return self._gb300.is_collision_free_host(qs).view(np.bool_)
 
     def batch_is_edge_collision_free(self, q1s, q2s, mode=None, resolution: Optional[float] = None,
                                      include_endpoints: bool = False, N=None) -> np.ndarray:
@@ -178,8 +182,9 @@ class Gb300CollisionBackend:
         if resolution is None:
             resolution = self.collision_resolution
         self._use_mode(mode)
-        v = self._gb300.is_edge_collision_free_batch(q1s, q2s, resolution, include_endpoints, N)
-        return v.bool().cpu().numpy() if not isinstance(q1s, torch.Tensor) else v.bool()
+        if isinstance(q1s, torch.Tensor):
+            return self._gb300.is_edge_collision_free_batch(q1s, q2s, resolution, include_endpoints, N).bool()
+        return self._gb300.is_edge_collision_free_host(q1s, q2s, resolution, include_endpoints, N).view(np.bool_)
 
     def edge_check_plan(self, n: int, resolution: Optional[float] = None, include_endpoints: bool = False,
                         chunks: int = 1, dtype=torch.float64):
@@ -266,10 +271,10 @@ class Gb300CollisionBackend:
             es = [i for i in range(P - 1) if idx[i] == m]
             if self._gb300.mode != m:
                 self._gb300.set_mode(m)
-            if vs and not self._gb300.is_collision_free_batch(qs[vs]).bool().all():
+            if vs and not self._gb300.is_collision_free_host(qs[vs]).all():
                 return False
-            if es and not self._gb300.is_edge_collision_free_batch(qs[es], qs[[i + 1 for i in es]], resolution,
-                                                                    False).bool().all():
+            if es and not self._gb300.is_edge_collision_free_host(qs[es], qs[[i + 1 for i in es]], resolution,
+                                                                   False).all():
                 return False
         return True
 

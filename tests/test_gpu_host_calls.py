@@ -162,3 +162,52 @@ def test_host_robot_mask_and_modes(gpu, oracle):
         got = np.array([env.is_collision_free_for_robot(names, x) for x in q[:120]], dtype=np.uint8)
         assert np.array_equal(got, want[:120]), m
         assert np.array_equal(env._gb300.is_collision_free_host(q, robot_mask=m), want), m
+
+
+def test_abstract_edges_both_kernels_vs_oracle(gpu, oracle):
+    """Two-disc scene: batches up to 65,536 edges run the flat single-launch
+    kernel (positions side by side, pending ones decided in FP64 at once),
+    larger ones the warp-per-edge kernel with its FP64 pass; device and host
+    inputs, FP64 and FP32 endpoints, against the oracle."""
+    import torch
+
+    scenes, col = pkg("scenes"), pkg("collision")
+    scene = scenes.make_disc_scene(0)
+    sc, o = col.Gb300Scene(scene), oracle.OracleScene(scene)
+    rng = np.random.default_rng(12)
+    for n in (1, 999, 65536, 70000):
+        q1 = rng.uniform(-1, 1, (n, 4))
+        q2 = q1 + rng.uniform(-0.3, 0.3, (n, 4))
+        for dt in (np.float64, np.float32):
+            a, b = q1.astype(dt), q2.astype(dt)
+            ref = o.edges_free(a, b, 0.01)
+            assert np.array_equal(sc.is_edge_collision_free_host(a, b, 0.01), ref), (n, dt)
+            got = sc.is_edge_collision_free_batch(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), 0.01)
+            assert np.array_equal(got.cpu().numpy(), ref), (n, dt)
+        assert 0 < ref.sum() < n or n < 10
+    # near-tangent positions: pending classifications decided in FP64
+    g = golden("abstract_disc.npz")
+    scene = pkg("scenes").AbstractScene(
+        agent_slices=np.array([[0, 2], [2, 4]]), agent_radii=[0.1, 0.1], box_center=g["centers"],
+        box_bounds=2.0 * g["half"], sphere_pos=np.zeros((0, 2)), sphere_radius=[], q_dim=4)
+    sc = col.Gb300Scene(scene)
+    assert np.array_equal(sc.is_collision_free_host(g["configs"]), g["config_free"])
+    assert sc.last_call_stats() is not None
+
+
+def test_abstract_host_edge_errors(gpu):
+    """Errors found by the flat kernel on the mapped buffer come back as the
+    batched call's status: N_start > N -> AssertionError, a NaN edge length
+    -> ValueError; the scene stays usable."""
+    scenes, col = pkg("scenes"), pkg("collision")
+    sc = col.Gb300Scene(scenes.make_disc_scene(0))
+    rng = np.random.default_rng(3)
+    q1, q2 = rng.uniform(-1, 1, (50, 4)), rng.uniform(-1, 1, (50, 4))
+    with pytest.raises(AssertionError):
+        sc.is_edge_collision_free_host(q1, q2, 0.01, N=np.full(50, 3), N_start=5)
+    bad = q1.copy()
+    bad[7, 0] = np.nan
+    with pytest.raises(ValueError):
+        sc.is_edge_collision_free_host(bad, q2, 0.01)
+    ok = sc.is_edge_collision_free_host(q1, q2, 0.01)
+    assert np.array_equal(ok, sc.is_edge_collision_free_batch(q1, q2, 0.01).cpu().numpy())

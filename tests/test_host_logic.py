@@ -217,14 +217,14 @@ def test_path_check_covers_the_reference_calls():
         def __init__(self):
             self.configs = 0
 
-        def is_collision_free_batch(self, qs):
+        def is_collision_free_host(self, qs):
             self.configs += len(qs)
-            return torch.ones(len(qs), dtype=torch.uint8)
+            return np.ones(len(qs), dtype=np.uint8)
 
-        def is_edge_collision_free_batch(self, q1s, q2s, resolution, include_endpoints=False, N=None):
+        def is_edge_collision_free_host(self, q1s, q2s, resolution, include_endpoints=False, N=None):
             assert not include_endpoints and N is None
             self.configs += sum(envm._edge_N(a, b, resolution) - 2 for a, b in zip(q1s, q2s))
-            return torch.ones(len(q1s), dtype=torch.uint8)
+            return np.ones(len(q1s), dtype=np.uint8)
 
     env = object.__new__(envm.Gb300AbstractEnvironment)
 

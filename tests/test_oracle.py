@@ -251,12 +251,12 @@ def test_path_check_golden(oracle):
     class OracleBacked:
         mode = -1
 
-        def is_collision_free_batch(self, qs):
-            return torch.from_numpy(o.configs_free(np.asarray(qs)).astype(np.uint8))
+        def is_collision_free_host(self, qs):
+            return o.configs_free(np.asarray(qs)).astype(np.uint8)
 
-        def is_edge_collision_free_batch(self, q1s, q2s, resolution, include_endpoints=False, N=None):
-            return torch.from_numpy(o.edges_free(np.asarray(q1s), np.asarray(q2s), resolution,
-                                                 include_endpoints=include_endpoints, N=N).astype(np.uint8))
+        def is_edge_collision_free_host(self, q1s, q2s, resolution, include_endpoints=False, N=None):
+            return o.edges_free(np.asarray(q1s), np.asarray(q2s), resolution,
+                                include_endpoints=include_endpoints, N=N).astype(np.uint8)
 
     env = object.__new__(envm.Gb300AbstractEnvironment)
     env._gb300 = OracleBacked()
