@@ -1061,13 +1061,49 @@ def run_profile(args):
         qd = torch.from_numpy(rng.uniform(-1, 1, (10_000, 4))).cuda()
         q1d = torch.from_numpy(rng.uniform(-1, 1, (1000, 4))).cuda()
         q2d = torch.from_numpy(rng.uniform(-1, 1, (1000, 4))).cuda()
+        q1h, q2h, qh = q1d.cpu().numpy(), q2d.cpu().numpy(), qd.cpu().numpy()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             e = s.is_edge_collision_free_batch(q1d, q2d, 0.01)
             v = s.is_collision_free_batch(qd)
+            s.is_edge_collision_free_host(q1h, q2h, 0.01)
+            s.is_collision_free_host(qh)
         torch.cuda.synchronize()
         print(json.dumps({"profile": "abstract", "launches": 4 * args.steps, "s": time.perf_counter() - t0,
                           "free_edges": int(e.sum().item()), "free_configs": int(v.sum().item())}), flush=True)
+        return 0
+
+    if args.profile == "dist":
+        # the two-disc scene's 1,000 x 10,000 euclidean distance matrix (FP64)
+        scenes, _lib = pkg("scenes"), pkg("_lib")
+        lib = _lib.load()
+        sc = scenes.make_disc_scene(0)
+        rng = np.random.default_rng(0)
+        qd = torch.from_numpy(rng.uniform(-1, 1, (10_000, 4))).cuda()
+        q1d = torch.from_numpy(rng.uniform(-1, 1, (1000, 4))).cuda()
+        sl = np.ascontiguousarray(sc.agent_slices, dtype=np.int64)
+        out = torch.empty((1000, 10_000), dtype=torch.float64, device="cuda")
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            _lib.check(lib.mrmg_config_dist_matrix(q1d.data_ptr(), 1000, qd.data_ptr(), 10_000, 4, sl.ctypes.data,
+                                                   len(sl), _lib.METRICS["euclidean"], out.data_ptr(),
+                                                   _lib.stream_handle(None), 0), "dist matrix")
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "dist", "launches": args.steps, "s": time.perf_counter() - t0}), flush=True)
+        return 0
+
+    if args.profile == "configs":
+        # 100,000 uniform configurations of the four-arm scene per call
+        envm, scenes = pkg("env"), pkg("scenes")
+        scene = scenes.make_arm_scene(0)
+        sc = envm.Gb300ArmEnvironment(scene, collision_resolution=RESOLUTION)._gb300
+        q = torch.from_numpy(scenes.uniform_configs(scene, 100_000, seed=3)).cuda()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            v = sc.is_collision_free_batch(q)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "configs", "launches": 2 * args.steps, "s": time.perf_counter() - t0,
+                          "free": int(v.sum().item())}), flush=True)
         return 0
 
     if args.profile == "pen":
@@ -1167,7 +1203,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--chunks", type=int, default=1, help="pipelined chunks of the end-to-end plan")
     ap.add_argument("--skip-extra", action="store_true", help="only the headline edge-check workload")
-    ap.add_argument("--profile", choices=["early", "full", "knn", "near", "pen", "abstract"], default=None,
+    ap.add_argument("--profile", choices=["early", "full", "knn", "near", "pen", "abstract", "dist", "configs"],
+                    default=None,
                     help="short runs of one workload's kernels for ncu captures")
     ap.add_argument("--dry-run", action="store_true",
                     help="replica orchestration only (gloo, no GPU work, no value): tests the host logic")

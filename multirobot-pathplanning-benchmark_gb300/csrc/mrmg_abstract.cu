@@ -128,6 +128,112 @@ __device__ uint8_t classify32(const AbstractDev& s, Acc x, float extra) {
   return bad ? V_PENDING : classify_core(s, qf, qmax, extra);
 }
 
+// The same classification with the agent dimension known at compile time:
+// each agent's coordinates are fetched into registers when a test needs them
+// (x(k) is a cheap load or interpolation), so no per-thread array is indexed
+// at run time (such arrays live in local memory).  Thresholds, band and test
+// order are those of classify_core.
+template <int DIM, class Acc>
+__device__ uint8_t classify_dim(const AbstractDev& s, Acc x, float extra) {
+  float qmax = 0.f;
+  bool bad = false;
+  for (int k = 0; k < s.D; k++) {
+    const float f = x(k);
+    bad |= !(fabsf(f) <= 1e30f);
+    qmax = fmaxf(qmax, fabsf(f));
+  }
+  if (bad) return V_PENDING;
+  const float delta = s.delta_k * (qmax + s.omax) + extra;
+  bool unc = false;
+  const int A = s.A;
+  // agent - agent  (abstract_env.py:261-268)
+  for (int i = 0; i < A; i++) {
+    float a[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; k++) a[k] = x(s.agent_off[i] + k);
+    for (int j = i + 1; j < A; j++) {
+      float ss = 0.f;
+#pragma unroll
+      for (int k = 0; k < DIM; k++) {
+        const float d = a[k] - x(s.agent_off[j] + k);
+        ss = fmaf(d, d, ss);
+      }
+      const float thr = s.pair_thr32[i * A + j];
+      const float hi = thr + 2.f * delta, lo = thr - 2.f * delta;
+      if (!(ss > hi * hi)) {
+        if (lo > 0.f && ss < lo * lo) return V_COLLIDE;
+        unc = true;
+      }
+    }
+  }
+  // agent - obstacle  (abstract_env.py:270-274)
+  for (int i = 0; i < A; i++) {
+    float c[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; k++) c[k] = x(s.agent_off[i] + k);
+    const float r = s.r32[i];
+    const float rhi = r + delta, rlo = r - delta;
+    int b = 0;
+    for (; b + 1 < s.nb; b += 2) {
+      const float* lo0 = s.box_lo32 + b * DIM;
+      const float* hi0 = s.box_hi32 + b * DIM;
+      float ss0 = 0.f, ss1 = 0.f;
+#pragma unroll
+      for (int k = 0; k < DIM; k++) {
+        const float v0 = fminf(fmaxf(c[k], lo0[k]), hi0[k]) - c[k];
+        const float v1 = fminf(fmaxf(c[k], lo0[DIM + k]), hi0[DIM + k]) - c[k];
+        ss0 = fmaf(v0, v0, ss0);
+        ss1 = fmaf(v1, v1, ss1);
+      }
+      if (!(ss0 > rhi * rhi)) {
+        if (rlo > 0.f && ss0 < rlo * rlo) return V_COLLIDE;
+        unc = true;
+      }
+      if (!(ss1 > rhi * rhi)) {
+        if (rlo > 0.f && ss1 < rlo * rlo) return V_COLLIDE;
+        unc = true;
+      }
+    }
+    for (; b < s.nb; b++) {
+      const float* lo = s.box_lo32 + b * DIM;
+      const float* hi = s.box_hi32 + b * DIM;
+      float ss = 0.f;
+#pragma unroll
+      for (int k = 0; k < DIM; k++) {
+        const float v = fminf(fmaxf(c[k], lo[k]), hi[k]) - c[k];
+        ss = fmaf(v, v, ss);
+      }
+      if (!(ss > rhi * rhi)) {
+        if (rlo > 0.f && ss < rlo * rlo) return V_COLLIDE;
+        unc = true;
+      }
+    }
+    for (int o = 0; o < s.ns; o++) {
+      const float* p = s.sph_pos32 + o * DIM;
+      float ss = 0.f;
+#pragma unroll
+      for (int k = 0; k < DIM; k++) {
+        const float d = p[k] - c[k];
+        ss = fmaf(d, d, ss);
+      }
+      const float thr = s.sph_thr32[o * A + i];
+      const float hi = thr + 2.f * delta, lo = thr - 2.f * delta;
+      if (!(ss > hi * hi)) {
+        if (lo > 0.f && ss < lo * lo) return V_COLLIDE;
+        unc = true;
+      }
+    }
+  }
+  return unc ? V_PENDING : V_FREE;
+}
+
+// DIM > 0: the compile-time form; 0: any agent dimension
+template <int DIM, class Acc>
+__device__ __forceinline__ uint8_t classify_any(const AbstractDev& s, Acc x, float extra) {
+  if constexpr (DIM == 0) return classify32(s, x, extra);
+  else return classify_dim<DIM>(s, x, extra);
+}
+
 // ---------------------------------------------------------------------------
 // Exact FP64 restatement of one configuration (same operation order as the
 // reference), evaluated by all lanes of a warp together: lane t takes test t,
@@ -433,6 +539,7 @@ __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int 
 // ctr may be NULL (no statistics, and no error bits: the host-pointer calls
 // validate step counts on the host before launching).
 // ---------------------------------------------------------------------------
+template <int DIM>
 __global__ void __launch_bounds__(256) configs_fused_kernel(AbstractDev s, const void* q, int dtype, long long n,
                                                             uint8_t* out, int* ctr) {
   extern __shared__ double sm_cfg[];
@@ -448,7 +555,7 @@ __global__ void __launch_bounds__(256) configs_fused_kernel(AbstractDev s, const
       auto x = [&](int k) {
         return dtype == MRMG_F32 ? ((const float*)q)[i * D + k] : (float)((const double*)q)[i * D + k];
       };
-      v = classify32(cs, x, 0.f);
+      v = classify_any<DIM>(cs, x, 0.f);
     }
     unsigned pm = __ballot_sync(MRMG_FULL, v == V_PENDING);
     npend += __popc(pm);
@@ -472,6 +579,7 @@ __global__ void __launch_bounds__(256) configs_fused_kernel(AbstractDev s, const
 // of an edge already seen to collide is skipped.
 constexpr int kFlatMaxEpc = 8;
 
+template <int DIM>
 __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const void* q1, const void* q2, int dtype,
                                                          long long n, double res, int incl, const long long* Np,
                                                          long long N_start, long long N_max, uint8_t* out, int* ctr,
@@ -578,7 +686,8 @@ __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const vo
       if (t < total) {
         while (t >= soff[w + 1]) w++;
         N = sN[w];
-        iv = bfs_at(N, N_start + (t - soff[w]));
+        iv = N <= (1ll << 24) ? (long long)bfs_at32((int)N, (int)(N_start + (t - soff[w])))
+                              : bfs_at(N, N_start + (t - soff[w]));
         const bool skip = (!incl && (iv == 0 || iv == N - 1)) || (*(volatile int*)&sst[w] & 1);
         if (skip) {
           iv = -1;
@@ -591,7 +700,7 @@ __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const vo
             interp_df(ah[k], al[k], dh[k], dl[k], fi, nm1, rn, &h, &l);
             return __fadd_rn(h, l);
           };
-          code = classify32(cs, x, sext[w]);
+          code = classify_any<DIM>(cs, x, sext[w]);
         } else {
           code = V_PENDING;   // positions beyond exact FP32 integers: FP64 at once
         }
@@ -626,13 +735,41 @@ __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const vo
 
 }  // namespace
 
+// the fused kernels, compiled for agent dimensions 2 and 3 and for any
+static void launch_configs_fused(const AbstractDev& s, int grid, int threads, cudaStream_t st, const void* q,
+                                 int dtype, long long n, uint8_t* out, int* ctr) {
+  const size_t sm = tab_bytes(s);
+  if (s.dim == 2) configs_fused_kernel<2><<<grid, threads, sm, st>>>(s, q, dtype, n, out, ctr);
+  else if (s.dim == 3) configs_fused_kernel<3><<<grid, threads, sm, st>>>(s, q, dtype, n, out, ctr);
+  else configs_fused_kernel<0><<<grid, threads, sm, st>>>(s, q, dtype, n, out, ctr);
+}
+
+static size_t flat_smem(const AbstractDev& s) { return tab_bytes(s) + (size_t)kFlatMaxEpc * s.D * 16; }
+
+static void launch_edges_flat(const AbstractDev& s, int grid, cudaStream_t st, const void* q1, const void* q2,
+                              int dtype, long long n, double res, int incl, const long long* Np, long long N_start,
+                              long long N_max, uint8_t* out, int* ctr, int epc, uint8_t* cta_err) {
+  const size_t sm = flat_smem(s);
+  if (s.dim == 2)
+    edges_flat_kernel<2><<<grid, 256, sm, st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, ctr, epc,
+                                                cta_err);
+  else if (s.dim == 3)
+    edges_flat_kernel<3><<<grid, 256, sm, st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, ctr, epc,
+                                                cta_err);
+  else
+    edges_flat_kernel<0><<<grid, 256, sm, st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, ctr, epc,
+                                                cta_err);
+}
+
 cudaError_t abstract_configs(const AbstractDev& s, const void* q, int dtype, long long n,
                              uint8_t* out, const CallScratch& sc, const LaunchShape& ls,
                              cudaStream_t st) {
-  const int threads = 256;
+  // 128-thread CTAs: a batch of a few thousand configurations spreads over
+  // more SMs (each thread's chain is latency-bound, not issue-bound)
+  const int threads = 128;
   const long long want = (n + threads - 1) / threads;
-  const int grid = (int)(want < (long long)ls.num_sms * 8 ? (want > 0 ? want : 1) : (long long)ls.num_sms * 8);
-  configs_fused_kernel<<<grid, threads, tab_bytes(s), st>>>(s, q, dtype, n, out, sc.ctr);
+  const int grid = (int)std::max(1ll, std::min(want, (long long)ls.num_sms * 16));
+  launch_configs_fused(s, grid, threads, st, q, dtype, n, out, sc.ctr);
   return cudaGetLastError();
 }
 
@@ -642,14 +779,13 @@ static int flat_epc(long long n, int num_sms) {
   return (int)std::max(1ll, std::min((long long)kFlatMaxEpc, per));
 }
 
-static size_t flat_smem(const AbstractDev& s) { return tab_bytes(s) + (size_t)kFlatMaxEpc * s.D * 16; }
 
 cudaError_t abstract_configs_mapped(const AbstractDev& s, const void* q, int dtype, long long n, uint8_t* out,
                                     int num_sms, cudaStream_t st) {
-  const int threads = 256;
+  const int threads = 128;
   const long long want = (n + threads - 1) / threads;
-  const int grid = (int)std::max(1ll, std::min(want, (long long)num_sms * 8));
-  configs_fused_kernel<<<grid, threads, tab_bytes(s), st>>>(s, q, dtype, n, out, nullptr);
+  const int grid = (int)std::max(1ll, std::min(want, (long long)num_sms * 16));
+  launch_configs_fused(s, grid, threads, st, q, dtype, n, out, nullptr);
   return cudaGetLastError();
 }
 
@@ -660,15 +796,16 @@ cudaError_t abstract_edges_mapped(const AbstractDev& s, const void* q1, const vo
   const long long want = (n + epc - 1) / epc;
   const int grid = (int)std::max(1ll, std::min(want, (long long)num_sms * 8));
   *grid_out = grid;
-  edges_flat_kernel<<<grid, 256, flat_smem(s), st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out,
-                                                       nullptr, epc, cta_err);
+  launch_edges_flat(s, grid, st, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, nullptr, epc, cta_err);
   return cudaGetLastError();
 }
 
 int abstract_prepare(const AbstractDev& s) {
   const size_t sm = flat_smem(s);
-  if (sm > 48 * 1024 && cudaFuncSetAttribute(edges_flat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)sm) != cudaSuccess)
+  if (sm > 48 * 1024 &&
+      (cudaFuncSetAttribute(edges_flat_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess ||
+       cudaFuncSetAttribute(edges_flat_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess ||
+       cudaFuncSetAttribute(edges_flat_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess))
     return -1;
   return 0;
 }
@@ -681,8 +818,7 @@ cudaError_t abstract_edges(const AbstractDev& s, const void* q1, const void* q2,
     const int epc = flat_epc(n, ls.num_sms);
     const long long want = (n + epc - 1) / epc;
     const int grid = (int)std::min(want, (long long)ls.num_sms * 8);
-    edges_flat_kernel<<<grid, 256, flat_smem(s), st>>>(s, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out,
-                                                         sc.ctr, epc, nullptr);
+    launch_edges_flat(s, grid, st, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc.ctr, epc, nullptr);
     return cudaGetLastError();
   }
   const int warps = 8;

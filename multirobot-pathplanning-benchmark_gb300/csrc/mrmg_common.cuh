@@ -187,6 +187,31 @@ __device__ __forceinline__ long long bfs_at(long long N, long long p) {
   return a;
 }
 
+// bfs_at in 32-bit arithmetic, for N <= 2^24 (the FP32 edge paths)
+__device__ __forceinline__ int bfs_at32(int N, int p) {
+  const int L = 31 - __clz(N + 1);
+  const int full = (1 << L) - 1;
+  if (p < full) {
+    const int lv = 31 - __clz(p + 1);
+    const int slot = p + 1 - (1 << lv);
+    int s = 0, e = N - 1;
+    for (int b = lv - 1; b >= 0; b--) {
+      const int mid = (s + e) >> 1;
+      if ((slot >> b) & 1) s = mid + 1;
+      else e = mid - 1;
+    }
+    return (s + e) >> 1;   // levels above the last are full: the node exists
+  }
+  int r = p - full, a = 0, b = N - 1;
+  for (int d = 0; d < L; d++) {
+    const int m = (a + b) >> 1;
+    const int cnt = (m - a) - ((1 << (L - d - 1)) - 1);
+    if (r < cnt) b = m - 1;
+    else { r -= cnt; a = m + 1; }
+  }
+  return a;
+}
+
 // Warp-uniform iterator over the BFS order in chunks of up to 32 slots of one
 // level.  next() returns, per lane, the index held by that lane's slot (or -1
 // where the slot is empty), the ballot of non-empty slots and the BFS position

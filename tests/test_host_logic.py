@@ -413,3 +413,44 @@ def test_importer_options():
         imp.load_mjcf_planar(base.format(comp="", geom="<geom type='sphere' size='0.1'/>").replace(' range="-1 1"', "", 1))
     with pytest.raises(ValueError):
         imp.load_mjcf_planar(base.format(comp="", geom="<geom type='sphere' size='0.1'/>"), robots=["nobody"])
+
+
+def _bfs_at32(N: int, p: int) -> int:
+    """Python restatement of the kernels' 32-bit closed-form BFS position map
+    (bfs_at32 in csrc/mrmg_common.cuh)."""
+    L = (N + 1).bit_length() - 1
+    full = (1 << L) - 1
+    if p < full:
+        lv = (p + 1).bit_length() - 1
+        slot = p + 1 - (1 << lv)
+        s, e = 0, N - 1
+        for b in range(lv - 1, -1, -1):
+            mid = (s + e) >> 1
+            if (slot >> b) & 1:
+                s = mid + 1
+            else:
+                e = mid - 1
+        return (s + e) >> 1
+    r, a, b = p - full, 0, N - 1
+    for d in range(L):
+        m = (a + b) >> 1
+        cnt = (m - a) - ((1 << (L - d - 1)) - 1)
+        if r < cnt:
+            b = m - 1
+        else:
+            r -= cnt
+            a = m + 1
+    return a
+
+
+def test_bfs_at32_matches_reference_order():
+    """The closed-form position map equals generate_binary_search_indices
+    (planning_env.py:34-51) position by position (golden vectors of the
+    reference, N = 1..300 and larger)."""
+    g = golden("binary_indices.npz")
+    off = 0
+    for N in g["Ns"]:
+        N = int(N)
+        ref = g["flat"][off:off + N]
+        off += N
+        assert [_bfs_at32(N, p) for p in range(N)] == ref.tolist(), N
