@@ -31,6 +31,7 @@ constexpr int kKeep = 16;          // candidates kept per query per node chunk
 constexpr int kTileM = 128;        // queries per tile (TMEM lanes)
 constexpr int kRowBytes = 128;     // one SW128 row: 64 bf16
 constexpr long long kWaitSpins = 1ll << 22;
+constexpr int kStagesB = 3;        // node-tile buffers in flight per candidate CTA
 
 // ---------------------------------------------------------------------------
 // Exact FP64 k-NN: warp per query
@@ -956,10 +957,10 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   unsigned char* base = (unsigned char*)(((uintptr_t)sm_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sA1 = base;
   unsigned char* sA2 = base + kTileM * kRowBytes;
-  unsigned char* sB0 = base + 2 * kTileM * kRowBytes;
+  unsigned char* sB0 = base + 2 * kTileM * kRowBytes;   // kStagesB node-tile buffers
   // per-thread candidate column: [32][blockDim] floats after the operand buffers
-  float* cand = (float*)(sB0 + 2 * (size_t)BT) + threadIdx.x;
-  __shared__ uint64_t bar_load[2], bar_mma[2];
+  float* cand = (float*)(sB0 + kStagesB * (size_t)BT) + threadIdx.x;
+  __shared__ uint64_t bar_load[kStagesB], bar_mma[2];
   __shared__ uint32_t tbase;
   __shared__ int s_fail;
   __shared__ float s_qn[kTileM], s_qna[4][kTileM];
@@ -971,7 +972,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   const int D = st.D;
 
   if (tid == 0) {
-    mbar_init(&bar_load[0], 1); mbar_init(&bar_load[1], 1);
+    for (int b = 0; b < kStagesB; b++) mbar_init(&bar_load[b], 1);
     mbar_init(&bar_mma[0], 1); mbar_init(&bar_mma[1], 1);
     s_fail = 0;
     fence_barrier_init();
@@ -1042,12 +1043,12 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   const uint32_t idesc = idesc_bf16(kTileM, NT);
 
   auto issue_load = [&](int t) {
-    unsigned char* dst = sB0 + (t & 1) * BT;
-    mbar_expect_tx(&bar_load[t & 1], BT);
-    bulk_g2s(dst, gtiles + (long long)t * BT, BT, &bar_load[t & 1]);
+    unsigned char* dst = sB0 + (t % kStagesB) * BT;
+    mbar_expect_tx(&bar_load[t % kStagesB], BT);
+    bulk_g2s(dst, gtiles + (long long)t * BT, BT, &bar_load[t % kStagesB]);
   };
   auto issue_mma = [&](int t) {
-    const uint32_t a1 = su32(sA1), a2 = su32(sA2), b = su32(sB0 + (t & 1) * BT);
+    const uint32_t a1 = su32(sA1), a2 = su32(sA2), b = su32(sB0 + (t % kStagesB) * BT);
     const uint32_t dcol = tm + (uint32_t)((t & 1) * (kTm / 2));
     if (FMT == KNN_FMT_EUCL) {
       for (int s = 0; s < 4; s++) umma_bf16(dcol, sw128_desc(a1 + 32 * s), sw128_desc(b + 32 * s), idesc, s > 0);
@@ -1063,8 +1064,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   };
 
   if (tid == 0 && T > 0) {
-    issue_load(0);
-    if (T > 1) issue_load(1);
+    for (int t = 0; t < kStagesB && t < T; t++) issue_load(t);
     if (mbar_wait(&bar_load[0], 0)) issue_mma(0);
     else s_fail = 1;
   }
@@ -1076,13 +1076,13 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
 
   for (int t = 0; t < T; t++) {
     if (tid == 0 && t + 1 < T && !s_fail) {
-      if (mbar_wait(&bar_load[(t + 1) & 1], ((t + 1) >> 1) & 1)) issue_mma(t + 1);
+      if (mbar_wait(&bar_load[(t + 1) % kStagesB], ((t + 1) / kStagesB) & 1)) issue_mma(t + 1);
       else s_fail = 1;
     }
     const bool done = mbar_wait(&bar_mma[t & 1], (t >> 1) & 1);
     if (!done) s_fail = 1;
     tc_fence_after();
-    if (tid == 0 && t + 2 < T && done) issue_load(t + 2);   // tile t's MMAs have read its buffer
+    if (tid == 0 && t + kStagesB < T && done) issue_load(t + kStagesB);   // tile t's MMAs have read its buffer
     if (done) {
       const int col_node0 = (it.tile0 + t) * NT;
       const uint32_t lane_base = tm + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((t & 1) * (kTm / 2));
@@ -1091,8 +1091,20 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
         for (int c0 = slice * NCOL; c0 < slice * NCOL + NCOL; c0 += 32) {
           float v[32];
           tmem_ld32(lane_base + c0, v);
-          if (RAD) rad_chunk<true>(v, qn, s_tau[row], s_qid[row], col_node0 + c0, ro);
-          else keep_chunk<true>(kd, ki, v, qn, cand, col_node0 + c0);
+          if (RAD) {
+            rad_chunk<true>(v, qn, s_tau[row], s_qid[row], col_node0 + c0, ro);
+          } else {
+            // pre-filter: the chunk's largest dot product against the row's
+            // threshold in dot space, (qn - kd[15]) / 2, lowered by a margin
+            // that covers the FP32 rounding of both forms; a chunk that fails
+            // holds no value the kept list would take
+            float vm = v[0];
+#pragma unroll
+            for (int i = 1; i < 32; i++) vm = fmaxf(vm, v[i]);
+            const float thr = kd[kKeep - 1];
+            const float th = 0.5f * (qn - thr);
+            if (vm > th - 1e-6f * (fabsf(qn) + fabsf(thr))) keep_chunk<true>(kd, ki, v, qn, cand, col_node0 + c0);
+          }
         }
       } else {
 #pragma unroll 1
@@ -1107,8 +1119,14 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
 #pragma unroll
             for (int i = 0; i < 32; i++) m[i] = fmaxf(m[i], fmaf(-2.f, v[i], qa));
           }
-          if (RAD) rad_chunk<false>(m, 0.f, s_tau[row], s_qid[row], col_node0 + c0, ro);
-          else keep_chunk<false>(kd, ki, m, 0.f, cand, col_node0 + c0);
+          if (RAD) {
+            rad_chunk<false>(m, 0.f, s_tau[row], s_qid[row], col_node0 + c0, ro);
+          } else {
+            float mm = m[0];   // the chunk's smallest value against the row's 16th kept one
+#pragma unroll
+            for (int i = 1; i < 32; i++) mm = fminf(mm, m[i]);
+            if (mm < kd[kKeep - 1]) keep_chunk<false>(kd, ki, m, 0.f, cand, col_node0 + c0);
+          }
         }
       }
     }
@@ -1785,10 +1803,15 @@ static void plan_items(const KnnStore* s, const int* h_q_mode, long long Q, int 
         pl->items.push_back(it);
       }
   }
+  // longest items first (CTAs start in index order: the short ones fill the
+  // tail of the last wave); the outputs do not depend on the order
+  std::stable_sort(pl->items.begin(), pl->items.end(), [](const KnnItem& a, const KnnItem& b) {
+    return (long long)(a.tile1 - a.tile0) * a.qn > (long long)(b.tile1 - b.tile0) * b.qn;
+  });
 }
 
 // Shared memory of a candidate CTA.  The euclidean kernel takes 256 tensor-
-// memory columns and about 81 KB, so two CTAs share an SM (a third does not
+// memory columns and about 97 KB (three node-tile buffers), so two CTAs share an SM (a third does not
 // fit in shared memory, so no CTA waits for columns); the per-agent kernel
 // takes all 512 columns and is held to one CTA per SM by asking for at least
 // 120 KB, so two CTAs never wait on each other for the columns.
@@ -1796,7 +1819,7 @@ static size_t tc_smem_bytes(const KnnStore* s) {
   const int NT = s->dev.NT;
   const bool eucl = s->dev.fmt == KNN_FMT_EUCL;
   const int nthreads = 128 * (eucl ? TcSplit<KNN_FMT_EUCL>::S : TcSplit<KNN_FMT_AGENT>::S);
-  const size_t need = 1024 + 2 * (size_t)kTileM * kRowBytes + 2 * (size_t)NT * kRowBytes +
+  const size_t need = 1024 + 2 * (size_t)kTileM * kRowBytes + kStagesB * (size_t)NT * kRowBytes +
                       32 * sizeof(float) * (size_t)nthreads;
   return eucl ? need : std::max<size_t>(need, 120 * 1024);
 }
