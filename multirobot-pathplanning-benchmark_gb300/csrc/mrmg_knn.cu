@@ -895,8 +895,7 @@ __device__ __forceinline__ void keep_insert(float (&kd)[kKeep], int (&ki)[kKeep]
 // instead of one per column whenever any lane inserts.
 template <bool FROM_DOT>
 __device__ __forceinline__ void keep_chunk(float (&kd)[kKeep], int (&ki)[kKeep], const float (&v)[32], float qn,
-                                           float* cand, int col0) {
-  const float thr = kd[kKeep - 1];
+                                           float* cand, int col0, float thr) {
   const int nth = blockDim.x;
   unsigned m = 0;
 #pragma unroll
@@ -943,7 +942,8 @@ template <int FMT, bool RAD>
 __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnStoreDev st, const double* __restrict__ qs,
                                                         const int* __restrict__ qorder, const KnnItem* __restrict__ items,
                                                         int chunks_max, float* __restrict__ cand_d,
-                                                        int* __restrict__ cand_i, float* __restrict__ q_eps,
+                                                        int* __restrict__ cand_i, float* __restrict__ cand_b,
+                                                        unsigned* __restrict__ g_thr, float* __restrict__ q_eps,
                                                         int* __restrict__ err, RadOut ro) {
   constexpr int NT = FMT == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
   constexpr uint32_t BT = NT * kRowBytes;   // bytes per node tile
@@ -965,7 +965,8 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   __shared__ int s_fail;
   __shared__ float s_qn[kTileM], s_qna[4][kTileM];
   __shared__ float s_tau[RAD ? kTileM : 1];
-  __shared__ long long s_qid[RAD ? kTileM : 1];
+  __shared__ long long s_qid[kTileM];
+  __shared__ float s_bound[RAD ? 1 : kTileM];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row = tid & (kTileM - 1), slice = tid / kTileM;
   const KnnItem it = items[blockIdx.x];
@@ -1028,7 +1029,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
       if (!RAD && it.chunk == 0) q_eps[qid] = eps;
       if (RAD) s_tau[r] = ro.rad2[qid] < 0.f ? -__int_as_float(0x7f800000) : ro.rad2[qid] + 1.0001f * eps;
     }
-    if (RAD) s_qid[r] = qid;
+    s_qid[r] = qid;
     s_qn[r] = qn;
     for (int a = 0; a < 4; a++) s_qna[a][r] = qna[a];
   }
@@ -1073,6 +1074,14 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   int ki[kKeep];
 #pragma unroll
   for (int i = 0; i < kKeep; i++) { kd[i] = __int_as_float(0x7f800000); ki[i] = -1; }
+  // Threshold shared by the CTAs that scan other node chunks of the same
+  // query: g_thr[q] holds the smallest 16th-kept value any of them has
+  // published (FP32 bits of a non-negative value, so unsigned order is value
+  // order).  A row filters with min(own 16th, shared), read one tile ahead;
+  // `bound` is the smallest threshold this row has filtered with: every node
+  // of the chunk left out of the list lies at or above min(bound, 16th).
+  const long long qrow = RAD ? -1 : s_qid[row];
+  float gcur = __int_as_float(0x7f800000), gnext = gcur, bound = gcur, published = gcur;
 
   for (int t = 0; t < T; t++) {
     if (tid == 0 && t + 1 < T && !s_fail) {
@@ -1083,6 +1092,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
     if (!done) s_fail = 1;
     tc_fence_after();
     if (tid == 0 && t + kStagesB < T && done) issue_load(t + kStagesB);   // tile t's MMAs have read its buffer
+    if (!RAD && qrow >= 0) gnext = __uint_as_float(*(volatile const unsigned*)&g_thr[qrow]);
     if (done) {
       const int col_node0 = (it.tile0 + t) * NT;
       const uint32_t lane_base = tm + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((t & 1) * (kTm / 2));
@@ -1101,9 +1111,10 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
             float vm = v[0];
 #pragma unroll
             for (int i = 1; i < 32; i++) vm = fmaxf(vm, v[i]);
-            const float thr = kd[kKeep - 1];
+            const float thr = fminf(kd[kKeep - 1], gcur);
             const float th = 0.5f * (qn - thr);
-            if (vm > th - 1e-6f * (fabsf(qn) + fabsf(thr))) keep_chunk<true>(kd, ki, v, qn, cand, col_node0 + c0);
+            if (vm > th - 1e-6f * (fabsf(qn) + fabsf(thr)))
+              keep_chunk<true>(kd, ki, v, qn, cand, col_node0 + c0, thr);
           }
         }
       } else {
@@ -1122,13 +1133,22 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
           if (RAD) {
             rad_chunk<false>(m, 0.f, s_tau[row], s_qid[row], col_node0 + c0, ro);
           } else {
-            float mm = m[0];   // the chunk's smallest value against the row's 16th kept one
+            float mm = m[0];   // the chunk's smallest value against the row's threshold
 #pragma unroll
             for (int i = 1; i < 32; i++) mm = fminf(mm, m[i]);
-            if (mm < kd[kKeep - 1]) keep_chunk<false>(kd, ki, m, 0.f, cand, col_node0 + c0);
+            const float thr = fminf(kd[kKeep - 1], gcur);
+            if (mm < thr) keep_chunk<false>(kd, ki, m, 0.f, cand, col_node0 + c0, thr);
           }
         }
       }
+    }
+    if (!RAD && qrow >= 0) {
+      bound = fminf(bound, gcur);
+      if (kd[kKeep - 1] < published) {   // publish a better 16th value
+        published = kd[kKeep - 1];
+        atomicMin(&g_thr[qrow], __float_as_uint(fmaxf(published, 0.f)));
+      }
+      gcur = fminf(gcur, gnext);
     }
     tc_fence_before();
     __syncthreads();
@@ -1148,6 +1168,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
         md[((size_t)(slice - 1) * kKeep + i) * kTileM + row] = kd[i];
         mi[((size_t)(slice - 1) * kKeep + i) * kTileM + row] = ki[i];
       }
+      if (S > 1) s_bound[row] = bound;   // (S <= 2)
     }
     __syncthreads();
     if (slice == 0) {
@@ -1157,6 +1178,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
           if (!(d < kd[kKeep - 1])) break;   // each list is sorted
           keep_insert(kd, ki, d, mi[((size_t)o * kKeep + i) * kTileM + row]);
         }
+      if (S > 1) bound = fminf(bound, s_bound[row]);
     }
   }
   if (!RAD && qid >= 0) {
@@ -1164,6 +1186,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
     int* oi = cand_i + ((size_t)qid * chunks_max + it.chunk) * kKeep;
 #pragma unroll
     for (int i = 0; i < kKeep; i++) { od[i] = kd[i]; oi[i] = ki[i]; }
+    cand_b[(size_t)qid * chunks_max + it.chunk] = fminf(bound, kd[kKeep - 1]);
   }
   tc_fence_before();
   __syncthreads();
@@ -1179,7 +1202,8 @@ constexpr int kMergeWarps = 4;   // warps per merge CTA
 __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
                                  const double* __restrict__ nodes, const long long* __restrict__ mode_beg,
                                  const long long* __restrict__ mode_end, const int* __restrict__ mode_chunks, int chunks_max, const float* __restrict__ cand_d,
-                                 const int* __restrict__ cand_i, const float* __restrict__ q_eps, SliceTab t,
+                                 const int* __restrict__ cand_i, const float* __restrict__ cand_b,
+                                 const float* __restrict__ q_eps, SliceTab t,
                                  int metric, int k, long long* __restrict__ out_idx, double* __restrict__ out_dist,
                                  long long* __restrict__ fallback, int* __restrict__ n_fallback) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -1226,10 +1250,12 @@ __global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, con
       if (lane == __ffs(who) - 1) { if (v0 <= v1) h0++; else h1++; }
     }
     const float tau = kth == INF ? INF : kth + 2.f * q_eps[q];
-    // certified when every full list ends above tau
+    // certified when every chunk's bound (all its nodes left out of its list
+    // lie at or above it) is above tau
     bool unsafe = false;
-    if (c0 < C) unsafe |= ci[c0 * kKeep + kKeep - 1] >= 0 && !(sv[c0 * kKeep + kKeep - 1] > tau);
-    if (c1 < C) unsafe |= ci[c1 * kKeep + kKeep - 1] >= 0 && !(sv[c1 * kKeep + kKeep - 1] > tau);
+    const float* cb = cand_b + (size_t)q * chunks_max;
+    if (c0 < C) unsafe |= !(cb[c0] > tau);
+    if (c1 < C) unsafe |= !(cb[c1] > tau);
     if (__any_sync(MRMG_FULL, unsafe)) {
       if (lane == 0) { const int s = atomicAdd(n_fallback, 1); fallback[s] = q; }
       continue;
@@ -1860,12 +1886,14 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   const size_t b_qmode = b_order;
   const size_t b_items = al(sizeof(KnnItem) * std::max<size_t>(items.size(), 1));
   const size_t b_mch = al(sizeof(int) * std::max(n_modes, 1));
+  const size_t b_g = al(sizeof(unsigned) * std::max<long long>(Q, 1));
   const size_t b_cd = al(sizeof(float) * std::max<long long>(Q, 1) * chunks_max * kKeep);
   const size_t b_ci = b_cd;
+  const size_t b_cb = al(sizeof(float) * std::max<long long>(Q, 1) * chunks_max);
   const size_t b_eps = al(sizeof(float) * std::max<long long>(Q, 1));
   const size_t b_fb = al(sizeof(long long) * std::max<long long>(Q, 1));
   const size_t b_ctr = 256;
-  const size_t need = b_order + b_qmode + b_items + b_mch + b_cd + b_ci + b_eps + b_fb + b_ctr;
+  const size_t need = b_order + b_qmode + b_items + b_mch + b_g + b_cd + b_ci + b_cb + b_eps + b_fb + b_ctr;
   if (scr->bytes < need) {
     if (scr->block) cudaFree(scr->block);
     scr->block = nullptr;
@@ -1878,14 +1906,17 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   int* d_qmode = (int*)p; p += b_qmode;
   KnnItem* d_items = (KnnItem*)p; p += b_items;
   int* d_mch = (int*)p; p += b_mch;
+  unsigned* d_g = (unsigned*)p; p += b_g;
   float* d_cd = (float*)p; p += b_cd;
   int* d_ci = (int*)p; p += b_ci;
+  float* d_cb = (float*)p; p += b_cb;
   float* d_eps = (float*)p; p += b_eps;
   long long* d_fb = (long long*)p; p += b_fb;
   int* d_ctr = (int*)p;   // [0] fallback count, [1] error bits
-  // order, query modes, items and chunk counts sit back to back in the device
-  // block: stage them in pinned memory with the same layout, one copy
-  const size_t b_up = b_order + b_qmode + b_items + b_mch;
+  // order, query modes, items, chunk counts and the shared thresholds' start
+  // values sit back to back in the device block: stage them in pinned memory
+  // with the same layout, one copy
+  const size_t b_up = b_order + b_qmode + b_items + b_mch + b_g;
   if (scr->host_bytes < b_up + 256) {
     if (scr->host) cudaFreeHost(scr->host);
     scr->host = nullptr;
@@ -1899,6 +1930,7 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   std::memcpy(hp + b_order, h_q_mode, sizeof(int) * Q);
   if (!items.empty()) std::memcpy(hp + b_order + b_qmode, items.data(), sizeof(KnnItem) * items.size());
   std::memcpy(hp + b_order + b_qmode + b_items, mode_chunks.data(), sizeof(int) * n_modes);
+  std::memset(hp + b_order + b_qmode + b_items + b_mch, 0x7f, b_g);   // 0x7f7f7f7f: a huge FP32 threshold
   int* h_ctr = (int*)(hp + b_up);
   cudaError_t e = cudaMemcpyAsync(d_order, hp, b_up, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, 256, st);
@@ -1909,17 +1941,17 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   if (!items.empty()) {
     if (s->dev.fmt == KNN_FMT_EUCL) {
       knn_tc_kernel<KNN_FMT_EUCL, false><<<(int)items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
-                                                                         d_cd, d_ci, d_eps, d_ctr + 1, RadOut{});
+                                                                         d_cd, d_ci, d_cb, d_g, d_eps, d_ctr + 1, RadOut{});
     } else {
       knn_tc_kernel<KNN_FMT_AGENT, false><<<(int)items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
-                                                                          d_cd, d_ci, d_eps, d_ctr + 1, RadOut{});
+                                                                          d_cd, d_ci, d_cb, d_g, d_eps, d_ctr + 1, RadOut{});
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   const int mgrid = (int)std::min<long long>((Q + 3) / 4, (long long)num_sms * 16);
   knn_merge_kernel<<<std::max(mgrid, 1), 32 * kMergeWarps, 0, st>>>(d_qs, Q, d_qmode, s->nodes, s->d_beg, s->d_end, d_mch, chunks_max,
-                                                       d_cd, d_ci, d_eps, s->slices, s->metric, k, d_idx, d_dist, d_fb,
+                                                       d_cd, d_ci, d_cb, d_eps, s->slices, s->metric, k, d_idx, d_dist, d_fb,
                                                        d_ctr);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -2258,11 +2290,13 @@ cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long
     if (s->dev.fmt == KNN_FMT_EUCL) {
       raise_smem_limit<KNN_FMT_EUCL, true>();
       knn_tc_kernel<KNN_FMT_EUCL, true><<<(int)pl.items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(
-          tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, (int*)(d_ctr + 1), ro);
+          tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, nullptr, nullptr,
+          (int*)(d_ctr + 1), ro);
     } else {
       raise_smem_limit<KNN_FMT_AGENT, true>();
       knn_tc_kernel<KNN_FMT_AGENT, true><<<(int)pl.items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(
-          tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, (int*)(d_ctr + 1), ro);
+          tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, nullptr, nullptr,
+          (int*)(d_ctr + 1), ro);
     }
   }
   if (e == cudaSuccess) e = cudaGetLastError();
