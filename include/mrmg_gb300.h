@@ -231,7 +231,11 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene *scene, const void *d_q1, const
  * mrmg_is_collision_free_batch_robots; arm scenes only).  Buffers: h_q /
  * h_q1 / h_q2 hold n * q_dim values of `dtype`, h_N (optional) n int64, h_out
  * n bytes.  Calls on one scene must not overlap (one staging buffer per
- * scene); the staging buffer grows with the largest batch seen. */
+ * scene); the staging buffer grows with the largest batch seen.  Where the
+ * device reads pageable host memory coherently (cudaDevAttrPageableMemoryAccess,
+ * e.g. a Grace CPU over NVLink-C2C), the kernels read the caller's input
+ * arrays in place instead of a staged copy; the environment variable
+ * MRMG_STAGE_HOST_INPUTS=1, read when a scene is created, forces staging. */
 int mrmg_is_collision_free_host(mrmg_scene *scene, const void *h_q, int32_t dtype, int64_t n,
                                 uint32_t robot_mask, uint8_t *h_out, int32_t flags);
 int mrmg_is_edge_collision_free_host(mrmg_scene *scene, const void *h_q1, const void *h_q2, int32_t dtype,

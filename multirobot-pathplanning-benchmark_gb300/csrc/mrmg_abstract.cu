@@ -547,6 +547,7 @@ __global__ void __launch_bounds__(256) configs_fused_kernel(AbstractDev s, const
   __syncthreads();
   const int D = s.D;
   const int lane = threadIdx.x & 31;
+  double* wq = (double*)((unsigned char*)sm_cfg + tab_bytes(s)) + (size_t)(threadIdx.x >> 5) * D;
   int npend = 0;
   for (long long i0 = blockIdx.x * (long long)blockDim.x; i0 < n; i0 += (long long)gridDim.x * blockDim.x) {
     const long long i = i0 + threadIdx.x;
@@ -563,9 +564,14 @@ __global__ void __launch_bounds__(256) configs_fused_kernel(AbstractDev s, const
       const int src = __ffs(pm) - 1;
       pm &= pm - 1;
       const long long j = __shfl_sync(MRMG_FULL, i, src);
-      auto acc = [&](int k) { return ldq(q, dtype, j * D + k); };
+      // the configuration's coordinates into the warp's shared area once
+      // (the inputs may sit in host memory mapped for the device)
+      for (int k = lane; k < D; k += 32) wq[k] = ldq(q, dtype, j * D + k);
+      __syncwarp();
+      auto acc = [&](int k) { return wq[k]; };
       const bool ok = exact_free_warp(s, acc, lane);
       if (lane == src) v = ok ? V_FREE : V_COLLIDE;
+      __syncwarp();
     }
     if (i < n) out[i] = v;
   }
@@ -597,6 +603,9 @@ __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const vo
   float* eal = eah + kFlatMaxEpc * D;
   float* edh = eal + kFlatMaxEpc * D;
   float* edl = edh + kFlatMaxEpc * D;
+  // the reference's FP64 q1 and (q2 - q1) / (N - 1) of each edge, for the exact path
+  double* e64a = (double*)(edl + kFlatMaxEpc * D);
+  double* e64d = e64a + kFlatMaxEpc * D;
   const float res32 = (float)res;
   int npend = 0;
   if (threadIdx.x == 0) s_err = 0;
@@ -653,6 +662,14 @@ __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const vo
         }
       }
       const float ext = ldexpf(warp_max(emax) * (float)s.dim, -30);
+      {
+        const double denom = (double)(N - 1);
+        for (int k = lane; k < D; k += 32) {
+          const double a = ldq(q1, dtype, e * D + k), b = ldq(q2, dtype, e * D + k);
+          e64a[w * D + k] = a;
+          e64d[w * D + k] = __ddiv_rn(__dsub_rn(b, a), denom);
+        }
+      }
       if (lane == 0) {
         sN[w] = N;
         sext[w] = ext;
@@ -666,15 +683,21 @@ __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const vo
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int acc = 0;
-      for (int w = 0; w < ne; w++) {
-        soff[w] = acc;
-        const long long N = sN[w];
+    if (wib == 0) {   // item offsets: an inclusive scan over the group's edges (ne <= 8)
+      int cnt = 0;
+      if (lane < ne) {
+        const long long N = sN[lane];
         const long long nmax = (N_max < 0 || N_max > N) ? N : N_max;
-        if (!(sst[w] & 2) && nmax > N_start) acc += (int)(nmax - N_start);
+        if (!(sst[lane] & 2) && nmax > N_start) cnt = (int)(nmax - N_start);
       }
-      soff[ne] = acc;
+      int inc = cnt;
+#pragma unroll
+      for (int o = 1; o < kFlatMaxEpc; o <<= 1) {
+        const int y = __shfl_up_sync(MRMG_FULL, inc, o);
+        if (lane >= o) inc += y;
+      }
+      if (lane < ne) soff[lane + 1] = inc;
+      if (lane == 0) soff[0] = 0;
     }
     __syncthreads();
     const int total = soff[ne];
@@ -712,14 +735,10 @@ __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const vo
         const int src = __ffs(pm) - 1;
         pm &= pm - 1;
         const int ws = __shfl_sync(MRMG_FULL, w, src);
-        const long long Ns = __shfl_sync(MRMG_FULL, N, src);
         const double di = (double)__shfl_sync(MRMG_FULL, iv, src);
-        const long long e = e0 + ws;
-        const double denom = (double)(Ns - 1);
-        auto acc = [&](int k) {
-          const double a = ldq(q1, dtype, e * D + k), b = ldq(q2, dtype, e * D + k);
-          return __dadd_rn(a, __dmul_rn(__ddiv_rn(__dsub_rn(b, a), denom), di));
-        };
+        const double* a64 = e64a + ws * D;
+        const double* d64 = e64d + ws * D;
+        auto acc = [&](int k) { return __dadd_rn(a64[k], __dmul_rn(d64[k], di)); };
         const bool ok = exact_free_warp(s, acc, lane);
         if (lane == src) code = ok ? V_FREE : V_COLLIDE;
       }
@@ -738,13 +757,13 @@ __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const vo
 // the fused kernels, compiled for agent dimensions 2 and 3 and for any
 static void launch_configs_fused(const AbstractDev& s, int grid, int threads, cudaStream_t st, const void* q,
                                  int dtype, long long n, uint8_t* out, int* ctr) {
-  const size_t sm = tab_bytes(s);
+  const size_t sm = tab_bytes(s) + (size_t)(threads / 32) * s.D * sizeof(double);   // tables, per-warp coordinates
   if (s.dim == 2) configs_fused_kernel<2><<<grid, threads, sm, st>>>(s, q, dtype, n, out, ctr);
   else if (s.dim == 3) configs_fused_kernel<3><<<grid, threads, sm, st>>>(s, q, dtype, n, out, ctr);
   else configs_fused_kernel<0><<<grid, threads, sm, st>>>(s, q, dtype, n, out, ctr);
 }
 
-static size_t flat_smem(const AbstractDev& s) { return tab_bytes(s) + (size_t)kFlatMaxEpc * s.D * 16; }
+static size_t flat_smem(const AbstractDev& s) { return tab_bytes(s) + (size_t)kFlatMaxEpc * s.D * 32; }
 
 static void launch_edges_flat(const AbstractDev& s, int grid, cudaStream_t st, const void* q1, const void* q2,
                               int dtype, long long n, double res, int incl, const long long* Np, long long N_start,

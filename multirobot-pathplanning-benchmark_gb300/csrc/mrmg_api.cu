@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <exception>
 #include <mutex>
@@ -138,6 +139,10 @@ struct mrmg_scene {
   size_t stage_cap = 0;
   unsigned* d_small_flags = nullptr;  // single-launch path: per-edge "collides in call epoch" flags
   unsigned small_epoch = 0;
+  // the device reads pageable host memory coherently (a CPU-GPU link with
+  // address translation): host-pointer calls hand the caller's input arrays
+  // to the kernels instead of staging them
+  bool pageable = false;
 };
 
 namespace {
@@ -147,6 +152,10 @@ int init_common(mrmg_scene* sc) {
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   e = cudaDeviceGetAttribute(&sc->num_sms, cudaDevAttrMultiProcessorCount, sc->device);
   if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  int pg = 0;
+  if (cudaDeviceGetAttribute(&pg, cudaDevAttrPageableMemoryAccess, sc->device) != cudaSuccess) pg = 0;
+  const char* stage = std::getenv("MRMG_STAGE_HOST_INPUTS");   // "1": always stage host inputs
+  sc->pageable = pg != 0 && !(stage && stage[0] == '1');
   e = cudaMalloc(&sc->d_ctr, sizeof(int) * kNumCtr);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(counters)");
   e = cudaMallocHost(&sc->h_ctr, sizeof(int) * kNumCtr);
@@ -1002,12 +1011,18 @@ int mrmg_is_collision_free_host(mrmg_scene* sc, const void* h_q, int32_t dtype, 
   ArmDev a = sc->arm;
   if (robot_mask) a.robot_mask = robot_mask;
   std::memset(H + o_hit, 0, (size_t)n);
-  std::memcpy(H + o_q, h_q, qbytes);
+  // the inputs as the kernels read them: the caller's array itself where the
+  // device reads pageable host memory, else a copy in the mapped buffer
+  const void* in_q = h_q;
+  if (!sc->pageable) {
+    std::memcpy(H + o_q, h_q, qbytes);
+    in_q = sc->m_stage + o_q;
+  }
   if (sc->kind == 0 && n <= kSmallConfigs) {
-    // one launch on the mapped buffer, verdicts written straight into it
+    // one launch, verdicts written straight into the mapped buffer
     AbstractDev ab = sc->ab;
     ab.sph_batch_form = (flags & MRMG_FLAG_BATCH_FORM) ? 1 : 0;
-    cudaError_t e = abstract_configs_mapped(ab, sc->m_stage + o_q, dtype, n, sc->m_stage + o_hit, sc->num_sms,
+    cudaError_t e = abstract_configs_mapped(ab, in_q, dtype, n, sc->m_stage + o_hit, sc->num_sms,
                                             sc->own_stream);
     if (e != cudaSuccess) return cuda_fail(e, "launch configs");
     e = cudaStreamSynchronize(sc->own_stream);
@@ -1018,7 +1033,7 @@ int mrmg_is_collision_free_host(mrmg_scene* sc, const void* h_q, int32_t dtype, 
   if (sc->kind == 1 && n <= kSmallConfigs && !(flags & MRMG_FLAG_FULL_EVAL) && arm_small_ok(a)) {
     SmallBatch b{};
     b.n = (int)n; b.items = (int)n; b.edges = 0; b.dtype = dtype; b.incl = 0; b.N_start = 0;
-    b.q1 = sc->m_stage + o_q; b.hit = sc->m_stage + o_hit; b.stats = (int*)sc->m_stage;
+    b.q1 = in_q; b.hit = sc->m_stage + o_hit; b.stats = (int*)sc->m_stage;
     b.flags = sc->d_small_flags;
     rc = next_epoch(sc, &b.epoch);
     if (rc) return rc;
@@ -1029,7 +1044,8 @@ int mrmg_is_collision_free_host(mrmg_scene* sc, const void* h_q, int32_t dtype, 
   }
   cudaStream_t st = sc->own_stream;
   unsigned char* Dv = sc->d_stage;
-  cudaError_t e = cudaMemcpyAsync(Dv + o_q, H + o_q, qbytes, cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaMemcpyAsync(Dv + o_q, sc->pageable ? h_q : (const void*)(H + o_q), qbytes,
+                                  cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(inputs)");
   rc = ensure_pending(sc, n, st);
   if (rc) return rc;
@@ -1074,8 +1090,17 @@ int mrmg_is_edge_collision_free_host(mrmg_scene* sc, const void* h_q1, const voi
   if (rc) return rc;
   unsigned char* H = sc->h_stage;
   std::memset(H + o_hit, 0, (size_t)n);
-  std::memcpy(H + o_q1, h_q1, qbytes);
-  std::memcpy(H + o_q2, h_q2, qbytes);
+  const void* in_q1 = h_q1;
+  const void* in_q2 = h_q2;
+  const long long* in_N = (const long long*)h_N;
+  if (!sc->pageable) {   // copies in the mapped buffer (see the configurations above)
+    std::memcpy(H + o_q1, h_q1, qbytes);
+    std::memcpy(H + o_q2, h_q2, qbytes);
+    if (h_N) std::memcpy(H + o_N64, h_N, 8 * (size_t)n);
+    in_q1 = sc->m_stage + o_q1;
+    in_q2 = sc->m_stage + o_q2;
+    in_N = h_N ? (const long long*)(sc->m_stage + o_N64) : nullptr;
+  }
   // the single-launch path: arm scenes, few edges, every N known and valid
   bool small = sc->kind == 1 && n <= kSmallEdges && !(flags & MRMG_FLAG_FULL_EVAL) && arm_small_ok(sc->arm);
   long long items = 0;
@@ -1102,10 +1127,8 @@ int mrmg_is_edge_collision_free_host(mrmg_scene* sc, const void* h_q1, const voi
   if (sc->kind == 0 && n <= kFlatMaxEdges) {
     // abstract scenes: the flat edge kernel on the mapped buffer; its error
     // bits come back per CTA in the head of the buffer
-    if (h_N) std::memcpy(H + o_N64, h_N, 8 * (size_t)n);
     int grid = 0;
-    cudaError_t e = abstract_edges_mapped(sc->ab, sc->m_stage + o_q1, sc->m_stage + o_q2, dtype, n, resolution,
-                                          include_endpoints, h_N ? (const long long*)(sc->m_stage + o_N64) : nullptr,
+    cudaError_t e = abstract_edges_mapped(sc->ab, in_q1, in_q2, dtype, n, resolution, include_endpoints, in_N,
                                           N_start, N_max, sc->m_stage + o_hit, sc->m_stage, sc->num_sms,
                                           sc->own_stream, &grid);
     if (e != cudaSuccess) return cuda_fail(e, "launch edges");
@@ -1123,7 +1146,7 @@ int mrmg_is_edge_collision_free_host(mrmg_scene* sc, const void* h_q1, const voi
     b.n = (int)n; b.items = (int)items; b.edges = 1; b.dtype = dtype; b.incl = include_endpoints ? 1 : 0;
     b.N_start = N_start;
     b.off = (const int*)(sc->m_stage + o_off); b.N = (const int*)(sc->m_stage + o_N32);
-    b.q1 = sc->m_stage + o_q1; b.q2 = sc->m_stage + o_q2; b.hit = sc->m_stage + o_hit;
+    b.q1 = in_q1; b.q2 = in_q2; b.hit = sc->m_stage + o_hit;
     b.stats = (int*)sc->m_stage;
     b.flags = sc->d_small_flags;
     rc = next_epoch(sc, &b.epoch);
@@ -1133,10 +1156,16 @@ int mrmg_is_edge_collision_free_host(mrmg_scene* sc, const void* h_q1, const voi
     for (long long i = 0; i < n; i++) h_out[i] = H[o_hit + i] ? 0 : 1;
     return MRMG_OK;
   }
-  if (h_N) std::memcpy(H + o_N64, h_N, 8 * (size_t)n);
   cudaStream_t st = sc->own_stream;
   unsigned char* Dv = sc->d_stage;
-  cudaError_t e = cudaMemcpyAsync(Dv + o_N64, H + o_N64, total - o_N64, cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaSuccess;
+  if (sc->pageable) {   // one copy per caller array
+    e = cudaMemcpyAsync(Dv + o_q1, h_q1, qbytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(Dv + o_q2, h_q2, qbytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && h_N) e = cudaMemcpyAsync(Dv + o_N64, h_N, 8 * (size_t)n, cudaMemcpyHostToDevice, st);
+  } else {
+    e = cudaMemcpyAsync(Dv + o_N64, H + o_N64, total - o_N64, cudaMemcpyHostToDevice, st);
+  }
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(inputs)");
   rc = ensure_pending(sc, n, st);
   if (rc) return rc;

@@ -211,3 +211,24 @@ def test_abstract_host_edge_errors(gpu):
         sc.is_edge_collision_free_host(bad, q2, 0.01)
     ok = sc.is_edge_collision_free_host(q1, q2, 0.01)
     assert np.array_equal(ok, sc.is_edge_collision_free_batch(q1, q2, 0.01).cpu().numpy())
+
+
+def test_host_calls_staged_inputs_match(gpu, oracle, monkeypatch):
+    """The same host-pointer calls with the inputs staged in the mapped
+    buffer (MRMG_STAGE_HOST_INPUTS=1; the path of devices that cannot read
+    pageable host memory): identical verdicts, arm and abstract scenes."""
+    monkeypatch.setenv("MRMG_STAGE_HOST_INPUTS", "1")
+    scenes, col = pkg("scenes"), pkg("collision")
+    arm = scenes.make_arm_scene(0)
+    sc, o = col.Gb300Scene(arm), oracle.OracleScene(arm)
+    w = scenes.make_arm_workload(arm, seed=8, n_configs=3000, n_edges=400)
+    assert np.array_equal(sc.is_collision_free_host(w["configs"]), o.configs_free(w["configs"]))
+    ref = o.edges_free(w["q1"], w["q2"], w["resolution"])
+    assert np.array_equal(sc.is_edge_collision_free_host(w["q1"], w["q2"], w["resolution"]), ref)
+    assert np.array_equal(sc.is_edge_collision_free_host(w["q1"][:50], w["q2"][:50], w["resolution"]), ref[:50])
+    disc = scenes.make_disc_scene(0)
+    sd, od = col.Gb300Scene(disc), oracle.OracleScene(disc)
+    rng = np.random.default_rng(4)
+    q1, q2 = rng.uniform(-1, 1, (700, 4)), rng.uniform(-1, 1, (700, 4))
+    assert np.array_equal(sd.is_edge_collision_free_host(q1, q2, 0.01), od.edges_free(q1, q2, 0.01))
+    assert np.array_equal(sd.is_collision_free_host(q1), od.configs_free(q1))
