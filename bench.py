@@ -546,7 +546,15 @@ def bench_knn(orc, steps: int = 20) -> dict:
                                "neighbours": int(o[-1]), "sample_256_identical": bool(ok)}
         store.close()
     out["rrt_loop"] = bench_rrt_loop(w)
+    out["cpu_baseline_reference_python"] = _ref_block("knn")
     return out
+
+
+def _ref_block(key: str):
+    rt = _reference_timings()
+    if not rt or key not in rt:
+        return None
+    return {**rt[key], "where": rt["where"], "numba": rt["host"].get("numba")}
 
 
 def bench_rrt_loop(w, iters: int = 2000) -> dict:
@@ -809,6 +817,7 @@ def bench_abstract(orc, reps: int = 20) -> dict:
                                      "hbm_note": "80 MB FP64 written per launch, far below the measured copy "
                                                  "bandwidth at this duration: the FP64 pipe is the bound"}},
         "cpu_cores": orc.num_threads(), "cpu_kind": "port (oracle/oracle.c FP64, OpenMP)",
+        "cpu_baseline_reference_python": _ref_block("disc_two_agents"),
     }
 
 
@@ -976,11 +985,26 @@ def _summary(line: dict) -> dict:
     out["abstract_edges_per_s"] = g("abstract", "edges", "edges_per_s")
     out["abstract_host_call_edges_per_s"] = g("abstract", "edges_host_call", "edges_per_s")
     out["abstract_configs_per_s"] = g("abstract", "configs", "configs_per_s")
+    out["abstract_reference_python_edges_per_s_pool"] = g("abstract", "cpu_baseline_reference_python",
+                                                          "edges_per_s_pool")
     out["abstract_cpu_configs_per_s"] = g("abstract", "configs", "cpu_configs_per_s")
     out["abstract_cpu_edges_per_s"] = g("abstract", "edges", "cpu_edges_per_s")
     out["serving_p50_p99_ms"] = [g("serving", "latency", "p50_ms"), g("serving", "latency", "p99_ms")]
     out["penetration_ms_cost_and_grad"] = g("penetration", "ms_cost_and_grad")
     return out
+
+
+def _reference_timings() -> dict:
+    """The reference's own Python code timed on the CPU-runnable workloads
+    (tests/golden/time_reference.py writes the file where the reference's
+    checkout is; the reference cannot be installed on the GPU host), or {}."""
+    p = ROOT / "tests" / "golden" / "reference_timings.json"
+    if not p.exists():
+        return {}
+    d = json.loads(p.read_text())
+    d["where"] = ("measured by tests/golden/time_reference.py on " + d.get("host", {}).get("cpu", "?") + " ("
+                  + str(d.get("host", {}).get("cpu_count", "?")) + " cores), not on this host")
+    return d
 
 
 def _peaks() -> dict:
