@@ -442,6 +442,7 @@ def run_gb300(args):
                 extra["serving"] = bench_serving(orc)
                 extra["prm_lazy"] = bench_prm_lazy()
                 extra["abstract"] = bench_abstract(orc)
+                extra["sparse_scene"] = bench_sparse_edges(orc)
 
     mism = int(reduce_max(float(mism), world))
     clk = clocks.stop() if clocks is not None else None
@@ -663,6 +664,55 @@ def bench_penetration(steps: int = 10) -> dict:
                            "sample": f"{n_cpu} paths x {T} waypoints, float64 torch autograd on the host"}
     s.close()
     return out
+
+
+def bench_sparse_edges(orc, n: int = 100_000, reps: int = 10) -> dict:
+    """The same four arms among 5 boxes, 100,000 edges of up to 0.3 rad per
+    joint between collision-free configurations at resolution 0.02: most
+    edges are free, so every interpolated position is evaluated (the headline
+    scene mostly stops at the first position).  Batched call with inputs
+    resident, CUDA events per call, L2 flushed; verdicts against the oracle;
+    the oracle's rate on the host cores beside."""
+    import torch
+
+    scenes, envm = pkg("scenes"), pkg("env")
+    scene = scenes.make_arm_scene(1, n_boxes=5)
+    env = envm.Gb300ArmEnvironment(scene, collision_resolution=0.02, tune_samples=1024)
+    sc = env._gb300
+    q = scenes.uniform_configs(scene, 4 * n, seed=5, dtype=np.float32)
+    a = q[env.batch_is_collision_free(q)][:n]
+    rng = np.random.default_rng(6)
+    b = (a + rng.uniform(-0.3, 0.3, a.shape)).astype(np.float32)
+    a_d, b_d = torch.from_numpy(np.ascontiguousarray(a)).cuda(), torch.from_numpy(b).cuda()
+    out = torch.empty(len(a), dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    sc.is_edge_collision_free_batch(a_d, b_d, 0.02, out=out)
+    ref = orc.OracleScene(scene).edges_free(a, b, 0.02)
+    mism = int((out.cpu().numpy() != ref).sum())
+    stats = sc.last_call_stats()
+    ms = []
+    for _ in range(reps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sc.is_edge_collision_free_batch(a_d, b_d, 0.02, out=out)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t = float(np.median(ms))
+    o = orc.OracleScene(scene)
+    t0 = time.perf_counter()
+    o.edges_free(a[:20_000], b[:20_000], 0.02)
+    cpu = 20_000 / (time.perf_counter() - t0)
+    F1 = config_flops(scene)
+    return {"workload": f"{len(a)} edges between free configurations of the four arms among 5 boxes, <= 0.3 rad "
+                        "per joint, resolution 0.02", "free_edges": int(ref.sum()),
+            "configs_evaluated": stats["configs_evaluated"], "ms_per_call": t,
+            "edges_per_s": len(a) / (t * 1e-3), "configs_per_s": stats["configs_evaluated"] / (t * 1e-3),
+            "effective_tflops": stats["configs_evaluated"] * F1 / (t * 1e-3) / 1e12,
+            "effective_note": f"{F1} flops per configuration of this scene (5 boxes), early exit on",
+            "verdict_mismatches": mism, "cpu_edges_per_s": cpu, "cpu_cores": orc.num_threads(),
+            "timing": "synchronous batched call, CUDA events, L2 flushed before each call"}
 
 
 def bench_abstract(orc, reps: int = 20) -> dict:
@@ -991,6 +1041,9 @@ def _summary(line: dict) -> dict:
     out["abstract_cpu_edges_per_s"] = g("abstract", "edges", "cpu_edges_per_s")
     out["serving_p50_p99_ms"] = [g("serving", "latency", "p50_ms"), g("serving", "latency", "p99_ms")]
     out["penetration_ms_cost_and_grad"] = g("penetration", "ms_cost_and_grad")
+    out["sparse_scene_edges_per_s"] = g("sparse_scene", "edges_per_s")
+    out["sparse_scene_free_edges"] = g("sparse_scene", "free_edges")
+    out["sparse_scene_mismatches"] = g("sparse_scene", "verdict_mismatches")
     return out
 
 
