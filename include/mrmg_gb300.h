@@ -123,7 +123,8 @@ int mrmg_abstract_scene_create(int32_t n_agents, int32_t dim, int32_t q_dim,
  *   h_sphere_local[S*3]  centre in that frame; h_sphere_radius[S]
  *   h_box_lo/h_box_hi[B*3]
  *   band                 FP32 re-check band in metres (<= 0: derived from the
- *                        kinematic reach, see DESIGN)
+ *                        kinematic reach: 16 (L + 1) 2^-24 times the reach plus
+ *                        4 2^-24 times the largest box coordinate)
  * R <= 16, D <= 96, S <= 1024, B <= 1024. */
 int mrmg_arm_scene_create(int32_t n_robots, int32_t q_dim, const int32_t *h_q_offset,
                           const int32_t *h_base_kind, const double *h_base_pose,
@@ -132,6 +133,18 @@ int mrmg_arm_scene_create(int32_t n_robots, int32_t q_dim, const int32_t *h_q_of
                           const double *h_sphere_local, const double *h_sphere_radius,
                           int32_t n_boxes, const double *h_box_lo, const double *h_box_hi,
                           double band, mrmg_scene **out);
+
+/* Fixed joint-angle offsets of an arm scene: revolute joint j turns by
+ * q[j] + h_offsets[j] (h_offsets[q_dim]; NULL clears them).  General serial
+ * chains (URDF <origin> + <axis>, MJCF body frames) are brought to the
+ * standard DH form of mrmg_arm_scene_create by an importer, and the DH angle
+ * of a joint differs from the file's joint value by a constant: this offset.
+ * Planar-base translations take no offset; |offset| <= 64.  The FP32 path adds
+ * the offset in double-float before the angle reduction, the FP64 path with
+ * one IEEE addition.  Synchronises the device (not capturable).  New: the
+ * reference delegates kinematics to its engines (mujoco_env.py:380-409,
+ * pinocchio_env.py:410-500). */
+int mrmg_arm_scene_set_joint_offsets(mrmg_scene *scene, const double *h_offsets);
 
 /* Per-mode scene tables (objects placed or attached by mode: the rai scenes'
  * set_to_mode, rai_base_env.py:704-840, and VAMP's

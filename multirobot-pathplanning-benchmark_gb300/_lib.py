@@ -77,6 +77,7 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_near_fetch": (i32, [vp, vp, vp, i64, vp]),
     "mrmg_arm_scene_set_modes": (i32, [vp, i32, vp, vp, vp, vp, vp]),
     "mrmg_scene_set_mode": (i32, [vp, i32]),
+    "mrmg_arm_scene_set_joint_offsets": (i32, [vp, vp]),
     "mrmg_node_store_append": (i32, [vp, i32, vp, i64, vp]),
     "mrmg_node_store_info": (i32, [vp, i32, vp]),
     "mrmg_node_store_set_path": (i32, [vp, i32]),

@@ -102,6 +102,12 @@ class Gb300Scene:
         self._edge_host = self.lib.mrmg_is_edge_collision_free_host
         self._slot_map = None
         self.mode = -1
+        off = getattr(scene, "joint_offset", None) if self.kind == 1 else None
+        if off is not None:
+            o = np.ascontiguousarray(np.asarray(off, dtype=np.float64).reshape(-1))
+            if o.shape != (scene.q_dim,):
+                raise ValueError(f"joint_offset must hold {scene.q_dim} values")
+            _lib.check(self.lib.mrmg_arm_scene_set_joint_offsets(self.h, o.ctypes.data), "joint offsets")
         if self.kind == 1 and scene.n_modes:
             t = scene.mode_tables()
             _lib.check(self.lib.mrmg_arm_scene_set_modes(

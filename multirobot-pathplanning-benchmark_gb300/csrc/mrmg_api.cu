@@ -128,6 +128,7 @@ struct mrmg_scene {
   std::vector<ArmTables> modes;
   int cur_mode = -1;
   void* d_mode_tables = nullptr;
+  void* d_offsets = nullptr;          // arm: fixed joint-angle offsets (FP32 hi/lo pairs, FP64)
   ArmSrc src;
   ArmTables& tabs() { return cur_mode < 0 ? base : modes[cur_mode]; }
   // host-pointer calls: the scene's own stream and one staging buffer (pinned
@@ -497,8 +498,9 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
     for (int b = a + 1; b < G; b++)
       if (grp_robot[a] != grp_robot[b]) pairs.push_back((uint32_t)a | ((uint32_t)b << 16));
 
-  // FP32 band: bounds |FP32 centre - FP64 centre| (see DESIGN): 16 (L+1) 2^-24 times
-  // the largest reach (base translation magnitude + link lengths + sphere offsets)
+  // FP32 band: bounds |FP32 centre - FP64 centre|: 16 (L+1) 2^-24 times the
+  // largest reach (base translation magnitude + link lengths + sphere offsets),
+  // plus 4 2^-24 times the largest box coordinate (the box tables' rounding)
   double max_box = 0.0;
   for (int i = 0; i < 3 * B; i++) max_box = std::max(max_box, std::max(std::fabs(h_box_lo[i]), std::fabs(h_box_hi[i])));
   if (!(max_box < 1e6)) return fail(MRMG_ERR_ARG, "box coordinates must be finite and < 1e6");
@@ -673,6 +675,45 @@ int mrmg_arm_scene_set_modes(mrmg_scene* sc, int32_t n_modes, const int32_t* h_s
   return host_fail();
 }
 
+int mrmg_arm_scene_set_joint_offsets(mrmg_scene* sc, const double* h_offsets) try {
+  if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
+  const int D = sc->q_dim;
+  std::vector<float2> o32(D);
+  std::vector<double> o64(D, 0.0);
+  bool any = false;
+  for (int j = 0; j < D; j++) {
+    const double o = h_offsets ? h_offsets[j] : 0.0;
+    if (!std::isfinite(o) || std::fabs(o) > 64.0) return fail(MRMG_ERR_ARG, "joint offset %d must be finite, |o| <= 64", j);
+    const bool pris = (sc->arm.prismatic[j >> 5] >> (j & 31)) & 1u;
+    if (pris && o != 0.0) return fail(MRMG_ERR_ARG, "joint %d is a planar-base translation: no angle offset", j);
+    o64[j] = o;
+    const float hi = (float)o;
+    o32[j] = make_float2(hi, (float)(o - (double)hi));
+    any |= o != 0.0;
+  }
+  void* blk = nullptr;
+  if (any) {
+    const size_t b32 = (sizeof(float2) * D + 255) & ~(size_t)255;
+    cudaError_t e = cudaMalloc(&blk, b32 + sizeof(double) * D);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(joint offsets)");
+    e = cudaMemcpy(blk, o32.data(), sizeof(float2) * D, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy((unsigned char*)blk + b32, o64.data(), sizeof(double) * D, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { cudaFree(blk); return cuda_fail(e, "upload joint offsets"); }
+  }
+  cudaError_t e = cudaDeviceSynchronize();   // no call in flight reads the old offsets
+  if (e != cudaSuccess) { if (blk) cudaFree(blk); return cuda_fail(e, "cudaDeviceSynchronize"); }
+  if (sc->d_offsets) cudaFree(sc->d_offsets);
+  sc->d_offsets = blk;
+  const float2* p32 = any ? (const float2*)blk : nullptr;
+  const double* p64 = any ? (const double*)((unsigned char*)blk + ((sizeof(float2) * D + 255) & ~(size_t)255)) : nullptr;
+  sc->base.d.off32 = p32; sc->base.d.off64 = p64;
+  for (auto& m : sc->modes) { m.d.off32 = p32; m.d.off64 = p64; }
+  sc->arm.off32 = p32; sc->arm.off64 = p64;
+  return MRMG_OK;
+} catch (...) {
+  return host_fail();
+}
+
 int mrmg_scene_set_mode(mrmg_scene* sc, int32_t mode) {
   if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
   if (mode < -1 || mode >= (int)sc->modes.size()) return fail(MRMG_ERR_ARG, "mode %d out of range", mode);
@@ -686,6 +727,7 @@ int mrmg_scene_destroy(mrmg_scene* sc) {
   if (!sc) return MRMG_OK;
   if (sc->d_tables) cudaFree(sc->d_tables);
   if (sc->d_mode_tables) cudaFree(sc->d_mode_tables);
+  if (sc->d_offsets) cudaFree(sc->d_offsets);
   if (sc->d_ctr) cudaFree(sc->d_ctr);
   if (sc->d_pend) cudaFree(sc->d_pend);
   if (sc->d_surv) cudaFree(sc->d_surv);

@@ -115,6 +115,22 @@ __device__ __forceinline__ bool is_prismatic(const ArmSmem& t, int j) {
   return (t.prismatic[j >> 5] >> (j & 31)) & 1u;
 }
 
+// Joint angle with the scene's fixed offset: theta = q + offset.  FP32 path:
+// the double-float angle (h, l) plus the offset's hi + lo, one error-free sum
+// (the result keeps ~44 bits, the reduction then rounds once); FP64 path: one
+// IEEE addition, as the CPU restatement does.
+__device__ __forceinline__ void add_offset_df(const ArmDev& s, int j, float* h, float* l) {
+  if (!s.off32) return;
+  const float2 o = s.off32[j];
+  float sh, se;
+  two_sum(*h, o.x, &sh, &se);
+  *h = sh;
+  *l = __fadd_rn(__fadd_rn(se, *l), o.y);
+}
+__device__ __forceinline__ double add_offset64(const ArmDev& s, int j, double th) {
+  return s.off64 ? __dadd_rn(th, s.off64[j]) : th;
+}
+
 // ---------------------------------------------------------------------------
 // FP32 forward kinematics of one group: world frame of (robot r, link k).
 // ---------------------------------------------------------------------------
@@ -354,6 +370,7 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
       wcs[j] = make_float2(1.f, 0.f);
     } else {
       float a;
+      add_offset_df(s, j, &h, &l);
       ok &= reduce_df(h, l, &a);
       float sn, cs;
       sincosf(a, &sn, &cs);
@@ -370,7 +387,7 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
       const double th = src.f64(j);
       wth64[j] = th;
       double sn, cs;
-      sincos_exact(th, &sn, &cs);
+      sincos_exact(add_offset64(s, j, th), &sn, &cs);
       wcs64[2 * j] = cs;
       wcs64[2 * j + 1] = sn;
     }
@@ -1221,14 +1238,14 @@ __global__ void arm_centers_kernel(ArmDev s, const void* q, int dtype, long long
       if (is_prismatic(t, j)) { wqv[j] = (float)th; wcs[j] = make_float2(1.f, 0.f); }
       else {
         float a;
-        reduce_angle_f32(th, &a);
+        reduce_angle_f32(add_offset64(s, j, th), &a);
         float sn, cs;
         sincosf(a, &sn, &cs);
         wcs[j] = make_float2(cs, sn);
       }
       w64[j] = th;
       double sn, cs;
-      sincos_exact(th, &sn, &cs);
+      sincos_exact(add_offset64(s, j, th), &sn, &cs);
       w64[((D + 1) & ~1) + 2 * j] = cs;
       w64[((D + 1) & ~1) + 2 * j + 1] = sn;
     }
@@ -1284,6 +1301,7 @@ __global__ void arm_box_hits_kernel(ArmDev s, const void* q, int dtype, long lon
       if (is_prismatic(t, j)) { wqv[j] = __fadd_rn(h, l); wcs[j] = make_float2(1.f, 0.f); }
       else {
         float a;
+        add_offset_df(s, j, &h, &l);
         reduce_df(h, l, &a);
         float sn, cs;
         sincosf(a, &sn, &cs);

@@ -57,6 +57,10 @@ struct ArmDev {
   const float4* gbs32;     // [G]      group bound: local centre xyz, radius^2 (radius covers every
                            //          sphere of the group plus 4 delta; padding groups: -1)
   const uint32_t* pairs;   // [NP]     group a | group b << 16 (different robots)
+  // fixed joint-angle offsets (imported general chains): revolute joint j
+  // turns by q[j] + offset[j]; NULL when the scene has none
+  const float2* off32;     // [D]      offset as FP32 hi + lo
+  const double* off64;     // [D]
 };
 
 // ---------------------------------------------------------------------------

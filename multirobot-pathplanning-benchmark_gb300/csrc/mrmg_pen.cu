@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(512, GRAD ? 1 : 2)
       const float4 b0 = a.base32[3 * r], b1 = a.base32[3 * r + 1], b2 = a.base32[3 * r + 2];
       if (a.base_kind[r] == 1) {
         float sn, cs;
-        sincosf(q[jo + 2], &sn, &cs);
+        sincosf(a.off32 ? q[jo + 2] + a.off32[jo + 2].x : q[jo + 2], &sn, &cs);
         m[0] = cs * b0.x - sn * b1.x; m[1] = cs * b0.y - sn * b1.y; m[2] = cs * b0.z - sn * b1.z;
         m[3] = sn * b0.x + cs * b1.x; m[4] = sn * b0.y + cs * b1.y; m[5] = sn * b0.z + cs * b1.z;
         m[6] = b2.x; m[7] = b2.y; m[8] = b2.z;
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(512, GRAD ? 1 : 2)
         }
         const float4 h = a.dh32[r * kMaxLinks + k - 1];   // a, d, cos(alpha), sin(alpha)
         float sn, cs;
-        sincosf(q[jo + k - 1], &sn, &cs);
+        sincosf(a.off32 ? q[jo + k - 1] + a.off32[jo + k - 1].x : q[jo + k - 1], &sn, &cs);
         const float sca = sn * h.z, cca = cs * h.z, ssa = sn * h.w, csa = cs * h.w;
         const float ac = h.x * cs, as = h.x * sn;
 #pragma unroll

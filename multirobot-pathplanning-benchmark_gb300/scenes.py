@@ -135,6 +135,9 @@ class ArmScene:
     sphere_attach: np.ndarray = field(default=None)   # [S] int32
     mode_boxes: list = field(default=None)
     mode_attach: list = field(default=None)
+    # fixed joint-angle offsets (imported general chains): revolute joint j
+    # turns by q[j] + joint_offset[j]
+    joint_offset: np.ndarray = field(default=None)    # [q_dim] or None
 
     @property
     def n_robots(self) -> int:
@@ -162,7 +165,7 @@ class ArmScene:
             dh=self.dh, sphere_robot=np.asarray(self.sphere_robot)[on], sphere_link=np.asarray(self.sphere_link)[on],
             sphere_local=np.asarray(self.sphere_local)[on], sphere_radius=np.asarray(self.sphere_radius)[on],
             box_lo=np.asarray(self.box_lo).reshape(-1, 3)[bx], box_hi=np.asarray(self.box_hi).reshape(-1, 3)[bx],
-            q_dim=self.q_dim, limits=self.limits)
+            q_dim=self.q_dim, limits=self.limits, joint_offset=self.joint_offset)
 
     def mode_tables(self) -> dict:
         """Flat arrays for the library: attachment ids and per-mode lists."""
@@ -213,6 +216,10 @@ class ArmScene:
                              "must both be [B, 3]")
         a["box_lo"] = a["box_lo"].reshape(-1, 3)
         a["box_hi"] = a["box_hi"].reshape(-1, 3)
+        off = np.zeros(self.q_dim) if self.joint_offset is None else np.asarray(self.joint_offset, np.float64)
+        if off.size != self.q_dim:
+            raise ValueError(f"ArmScene.joint_offset: {off.shape} does not hold {self.q_dim} values")
+        a["joint_offset"] = np.ascontiguousarray(off.reshape(-1))
         return a
 
 

@@ -216,12 +216,15 @@ void orc_sincos(double x, double *sn, double *cs) {
 /* ------------------------------------------------------------------------ */
 #define ORC_MAXR 16
 #define ORC_MAXL 8
+#define ORC_MAXJ 96
 
 typedef struct {
   int32_t R, D, S, B;
   int32_t q_off[ORC_MAXR], base_kind[ORC_MAXR], nl[ORC_MAXR];
   double base[ORC_MAXR][12];           /* R (row-major 3x3) then p            */
   double dh[ORC_MAXR][ORC_MAXL][4];    /* a, d, cos(alpha), sin(alpha)        */
+  int32_t has_off;                     /* fixed joint-angle offsets set        */
+  double off[ORC_MAXJ];                /* revolute joint j turns by q[j] + off[j] */
   int32_t *s_robot, *s_link;
   double *s_loc, *s_r, *s_r2;
   double *lo, *hi;
@@ -258,6 +261,19 @@ void *orc_arm_new(int32_t R, int32_t D, const int32_t *q_off, const int32_t *bas
   return a;
 }
 
+/* fixed joint-angle offsets (imported general chains): joint j of the
+ * configuration turns by q[j] + off[j]; NULL clears them */
+int orc_arm_set_offsets(void *p, const double *off) {
+  orc_arm *a = (orc_arm *)p;
+  if (!a || a->D > ORC_MAXJ) return ORC_ERR_ARG;
+  a->has_off = 0;
+  for (int j = 0; j < a->D; j++) {
+    a->off[j] = off ? off[j] : 0.0;
+    if (a->off[j] != 0.0) a->has_off = 1;
+  }
+  return ORC_OK;
+}
+
 void orc_arm_free(void *p) {
   orc_arm *a = (orc_arm *)p;
   if (!a) return;
@@ -273,7 +289,7 @@ static void arm_frames(const orc_arm *a, int r, const double *q, double fr[ORC_M
   double *R0 = fr[0];
   if (a->base_kind[r] == 1) {
     double x = q[jo], y = q[jo + 1], sn, cs;
-    orc_sincos(q[jo + 2], &sn, &cs);
+    orc_sincos(a->has_off ? q[jo + 2] + a->off[jo + 2] : q[jo + 2], &sn, &cs);
     for (int j = 0; j < 3; j++) {
       R0[j] = cs * bp[j] - sn * bp[3 + j];
       R0[3 + j] = sn * bp[j] + cs * bp[3 + j];
@@ -291,7 +307,7 @@ static void arm_frames(const orc_arm *a, int r, const double *q, double fr[ORC_M
     double *N = fr[k];
     const double *h = a->dh[r][k - 1];
     double sn, cs;
-    orc_sincos(q[jo + k - 1], &sn, &cs);
+    orc_sincos(a->has_off ? q[jo + k - 1] + a->off[jo + k - 1] : q[jo + k - 1], &sn, &cs);
     double ad = h[0], dd = h[1], ca = h[2], sa = h[3];
     double sca = sn * ca, cca = cs * ca, ssa = sn * sa, csa = cs * sa;
     double ac = ad * cs, as = ad * sn;

@@ -61,6 +61,7 @@ def lib() -> C.CDLL:
         L.orc_arm_new.restype = vp
         L.orc_arm_new.argtypes = [i32, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp, vp, i32, vp, vp]
         L.orc_arm_free.argtypes = [vp]
+        L.orc_arm_set_offsets.argtypes = [vp, vp]
         L.orc_abstract_config_free.argtypes = [vp, vp]
         L.orc_arm_config_free.argtypes = [vp, vp]
         L.orc_arm_fk.argtypes = [vp, vp, vp]
@@ -117,6 +118,12 @@ class OracleScene:
                                    _p(a["n_links"]), _p(a["dh"]), self.S, _p(a["sphere_robot"]), _p(a["sphere_link"]),
                                    _p(a["sphere_local"]), _p(a["sphere_radius"]), len(a["box_lo"]), _p(a["box_lo"]),
                                    _p(a["box_hi"]))
+            off = getattr(scene, "joint_offset", None)
+            if self.h and off is not None:
+                o = _c(np.asarray(off, dtype=np.float64).reshape(-1), np.float64)
+                self._keep.append(o)
+                if L.orc_arm_set_offsets(self.h, _p(o)) != 0:
+                    raise ValueError("oracle rejected the joint offsets")
         if not self.h:
             raise ValueError("oracle rejected the scene")
 

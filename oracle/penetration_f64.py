@@ -42,6 +42,7 @@ def fk_centers(arrays: dict, q: torch.Tensor) -> torch.Tensor:
     q_off = np.asarray(arrays["q_offset"])
     kinds = np.asarray(arrays["base_kind"])
     nls = np.asarray(arrays["n_links"])
+    joff = _t(arrays.get("joint_offset", np.zeros(q.shape[-1])), dev)   # joint j turns by q[j] + offset[j]
     S = len(s_robot)
     out = [None] * S
     for r in range(len(q_off)):
@@ -51,7 +52,7 @@ def fk_centers(arrays: dict, q: torch.Tensor) -> torch.Tensor:
         jo = int(q_off[r])
         shape = q.shape[:-1]
         if kinds[r] == 1:
-            x, y, th = q[..., jo], q[..., jo + 1], q[..., jo + 2]
+            x, y, th = q[..., jo], q[..., jo + 1], q[..., jo + 2] + joff[jo + 2]
             c, s = torch.cos(th), torch.sin(th)
             row0 = c[..., None] * Rb[0] - s[..., None] * Rb[1]
             row1 = s[..., None] * Rb[0] + c[..., None] * Rb[1]
@@ -65,7 +66,7 @@ def fk_centers(arrays: dict, q: torch.Tensor) -> torch.Tensor:
         frames = [(Rm, p)]
         for k in range(int(nls[r])):
             a, d, ca, sa = dh[r, k]
-            th = q[..., jo + k]
+            th = q[..., jo + k] + joff[jo + k]
             c, s = torch.cos(th), torch.sin(th)
             z = torch.zeros_like(c)
             o = torch.ones_like(c)

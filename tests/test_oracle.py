@@ -304,6 +304,8 @@ def _fk_homogeneous(scene, q):
         c, s = np.cos(t), np.sin(t)
         return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1.0]])
 
+    off = np.zeros(scene.q_dim) if scene.joint_offset is None else np.asarray(scene.joint_offset, np.float64)
+    q = np.asarray(q, dtype=np.float64) + off   # revolute joints turn by q + offset (planar x, y: offset 0)
     frames = []
     for r in range(scene.n_robots):
         bp = np.asarray(scene.base_pose[r], dtype=np.float64)
@@ -327,6 +329,31 @@ def _fk_homogeneous(scene, q):
         T = frames[int(scene.sphere_robot[s])][int(scene.sphere_link[s])]
         out.append(T[:3, :3] @ np.asarray(scene.sphere_local[s]) + T[:3, 3])
     return np.array(out)
+
+
+@pytest.mark.parametrize("factory", ["make_arm_scene", "make_mobile_scene"])
+def test_arm_kinematics_with_joint_offsets(oracle, factory):
+    """Fixed joint-angle offsets (the form imported general chains take):
+    the oracle's frames agree with the homogeneous restatement, and a scene
+    with offsets at q gives exactly the centres of the same scene without
+    offsets at q + offset (one IEEE addition per joint)."""
+    import copy
+
+    scenes = pkg("scenes")
+    sc = getattr(scenes, factory)(0)
+    rng = np.random.default_rng(11)
+    off = rng.uniform(-np.pi, np.pi, sc.q_dim)
+    for r in range(sc.n_robots):
+        if sc.base_kind[r] == 1:   # planar-base translations take no offset
+            off[sc.q_offset[r]:sc.q_offset[r] + 2] = 0.0
+    so = copy.deepcopy(sc)
+    so.joint_offset = off
+    o, o0 = oracle.OracleScene(so), oracle.OracleScene(sc)
+    q = scenes.uniform_configs(sc, 40, seed=4, dtype=np.float64)
+    for i in range(len(q)):
+        got = o.sphere_centers(q[i])
+        assert np.max(np.abs(got - _fk_homogeneous(so, q[i]))) <= 1e-12 * (1.0 + np.max(np.abs(got))), i
+        assert np.array_equal(got, o0.sphere_centers(q[i] + off)), i
 
 
 @pytest.mark.parametrize("factory", ["make_arm_scene", "make_mobile_scene"])
