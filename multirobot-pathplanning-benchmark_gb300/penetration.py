@@ -1,9 +1,9 @@
 """Differentiable path-penetration cost of sphere-arm paths on the GB300.
 
 There is no counterpart in the reference.  The cost feeds gradient-based path
-repair and shortcutting, next to ``robot_mode_shortcut``
-(planners/shortcutting.py:87-244), which today only tries straight-line
-shortcuts through ``env.is_edge_collision_free``.
+repair (``repair_paths``), which ``shortcutting.batched_robot_mode_shortcut``
+applies to straight-line shortcuts (planners/shortcutting.py:87-244) that
+collide.
 
 For a path ``w[0..T-1]`` of full joint vectors:
 
@@ -125,16 +125,31 @@ def penetration_cost(paths: torch.Tensor, scene: Gb300Scene, params: Penetration
 
 def repair_paths(scene: Gb300Scene, paths, params: PenetrationParams = PenetrationParams(), iters: int = 50,
                  step: float = 1e-3, resolution: float = 0.05, max_step_norm: float = 0.05,
-                 limits=None) -> dict:
-    """Gradient path repair: descent steps on the cost with the first and
-    last waypoint held, each waypoint's move clipped to ``max_step_norm`` and
-    the joints clamped to ``limits``.  A step is kept per path only where it
-    lowers that path's cost, otherwise the path's step size is halved, so the
-    cost never rises.  Every path is then checked edge by edge (consecutive
-    waypoints, at ``resolution``) with the exact edge checker.  Returns the
-    repaired paths, the cost before and after, and a per-path verdict."""
+                 limits=None, hold=None, move_mask=None) -> dict:
+    """Gradient path repair: descent steps on the cost with the held
+    waypoints fixed (``hold``, [n_paths, n_waypoints] bools; by default the
+    first and the last), only the joints of ``move_mask`` moving ([n_paths,
+    D] or [D] bools; by default all), each waypoint's move clipped to
+    ``max_step_norm`` and the moving joints clamped to ``limits``.  A step is
+    kept per path only where it lowers that path's cost, otherwise the path's
+    step size is halved, so the cost never rises.  Every path is then checked
+    edge by edge (consecutive waypoints, at ``resolution``, end states
+    included) with the exact edge checker.  Returns the repaired paths, the
+    cost before and after, and a per-path verdict."""
     w = _paths_tensor(scene, paths).clone()
     P, T, D = w.shape
+    if hold is None:
+        held = torch.zeros((P, T), dtype=torch.bool, device=w.device)
+        held[:, 0] = True
+        held[:, -1] = True
+    else:
+        held = torch.as_tensor(np.asarray(hold, dtype=bool), device=w.device).reshape(P, T)
+    if move_mask is None:
+        mv = torch.ones((P, D), dtype=torch.bool, device=w.device)
+    else:
+        mv = torch.as_tensor(np.asarray(move_mask, dtype=bool), device=w.device)
+        mv = mv.expand(P, D) if mv.dim() == 1 else mv.reshape(P, D)
+    movable = (~held)[:, :, None] & mv[:, None, :]
     lo = hi = None
     if limits is not None:
         lim = torch.as_tensor(np.asarray(limits, dtype=np.float32), device=w.device)
@@ -144,14 +159,13 @@ def repair_paths(scene: Gb300Scene, paths, params: PenetrationParams = Penetrati
     c, g = out["cost"], out["grad"]
     lr = torch.full((P, 1, 1), float(step), dtype=torch.float32, device=w.device)
     for _ in range(int(iters)):
-        g[:, 0] = 0
-        g[:, -1] = 0
-        d = lr * g
+        d = lr * torch.where(movable, g, torch.zeros_like(g))
         n = torch.linalg.vector_norm(d, dim=-1, keepdim=True)
         d = d * torch.clamp(max_step_norm / torch.clamp(n, min=1e-30), max=1.0)
         cand = w - d
         if lo is not None:
             cand = torch.maximum(torch.minimum(cand, hi), lo)
+        cand = torch.where(movable, cand, w)
         nxt = path_penetration(scene, cand, params, grad=True)
         ok = nxt["cost"] <= c
         okw = ok[:, None, None]

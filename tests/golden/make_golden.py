@@ -29,6 +29,8 @@ Outputs (numpy .npz, seeded, small):
                          (python tests/golden/make_golden.py <reference root> paths)
   batch_forms.npz        is_collision_free vs _batch_is_collision_free near a Sphere obstacle's contact
                          distance on 'abstract.test' (... <reference root> batch_forms)
+  shortcut.npz           robot_mode_shortcut (planners/shortcutting.py:87-244) on the disc scene: start
+                         paths, shortcut paths and cost traces (... <reference root> shortcut)
 """
 from __future__ import annotations
 
@@ -515,8 +517,71 @@ def make_batch_forms(reg):
                         batch8=batch8)
 
 
+def make_shortcut(ref_root: Path, pe, ae, reg):
+    """The reference's robot_mode_shortcut (planners/shortcutting.py:87-244)
+    on the disc scene: 12 collision-free start paths (random walks whose
+    states and edges the reference env accepts at resolution 0.01; the
+    second half of every odd path in a second mode whose task of robot 0
+    differs), shortcut under np.random.seed(1000 + p) with max_iter 120,
+    resolution 0.01, interpolation_resolution 0.1, round-robin robots for
+    even paths and random ones for odd paths.  Saved: the start paths, the
+    shortcut paths and the cost trace (the returned costs list)."""
+    import contextlib
+    import importlib
+    import io
+
+    m = types.ModuleType("multi_robot_multi_goal_planning.planners")
+    m.__path__ = [str(ref_root / "src" / "multi_robot_multi_goal_planning" / "planners")]
+    sys.modules[m.__name__] = m
+    sc = importlib.import_module("multi_robot_multi_goal_planning.planners.shortcutting")
+    srng = np.random.default_rng(0)
+    centers = srng.uniform(-0.8, 0.8, (10, 2))
+    half = srng.uniform(0.05, 0.2, (10, 2))
+    env = disc_env(ae, reg, centers, half)
+    modes = [pe.Mode([0, 0], None), pe.Mode([1, 0], None)]
+    rng = np.random.default_rng(4242)
+    S = env.start_pos.from_flat
+    starts, outs, costs, slen, olen, smode, omode, clen = [], [], [], [], [], [], [], []
+    for p in range(12):
+        P = int(rng.integers(5, 10))
+        while True:
+            q = rng.uniform(-1, 1, 4)
+            if env.is_collision_free(S(q), None):
+                break
+        qs = [q]
+        while len(qs) < P:
+            c = np.clip(qs[-1] + rng.uniform(-0.35, 0.35, 4), -1, 1)
+            if env.is_collision_free(S(c), None) and env.is_edge_collision_free(S(qs[-1]), S(c), None,
+                                                                                resolution=0.01):
+                qs.append(c)
+        mi = [0] * P if p % 2 == 0 else [0] * (P // 2) + [1] * (P - P // 2)
+        path = [pe.State(S(qs[t]), modes[mi[t]]) for t in range(P)]
+        np.random.seed(1000 + p)
+        with contextlib.redirect_stdout(io.StringIO()):
+            new_path, (cst, _times) = sc.robot_mode_shortcut(
+                env, path, max_iter=120, resolution=0.01, tolerance=0.01,
+                robot_choice="round_robin" if p % 2 == 0 else "random", interpolation_resolution=0.1)
+        starts.append(np.array(qs))
+        smode += mi
+        slen.append(P)
+        outs.append(np.array([s.q.state() for s in new_path]))
+        omode += [modes.index(s.mode) for s in new_path]
+        olen.append(len(new_path))
+        costs.append(np.array(cst, dtype=np.float64))
+        clen.append(len(cst))
+    np.savez_compressed(OUT / "shortcut.npz", centers=centers, half=half, starts=np.concatenate(starts),
+                        start_len=np.array(slen, dtype=np.int64), start_mode=np.array(smode, dtype=np.int64),
+                        outs=np.concatenate(outs), out_len=np.array(olen, dtype=np.int64),
+                        out_mode=np.array(omode, dtype=np.int64), costs=np.concatenate(costs),
+                        cost_len=np.array(clen, dtype=np.int64),
+                        task_ids=np.array([md.task_ids for md in modes], dtype=np.int64))
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "batch_forms":
+    if len(sys.argv) > 2 and sys.argv[2] == "shortcut":
+        pe_, ae_, cf_, reg_ = import_reference(Path(sys.argv[1]))
+        make_shortcut(Path(sys.argv[1]), pe_, ae_, reg_)
+    elif len(sys.argv) > 2 and sys.argv[2] == "batch_forms":
         make_batch_forms(import_reference(Path(sys.argv[1]))[3])
     elif len(sys.argv) > 2 and sys.argv[2] == "paths":
         pe_, ae_, cf_, reg_ = import_reference(Path(sys.argv[1]))
@@ -528,5 +593,5 @@ if __name__ == "__main__":
         make_near(import_reference(Path(sys.argv[1]))[2])
     else:
         if len(sys.argv) < 2:
-            sys.exit("usage: make_golden.py <reference root> [batch_forms|paths|prm_search|near]")
+            sys.exit("usage: make_golden.py <reference root> [batch_forms|paths|prm_search|near|shortcut]")
         main(sys.argv[1])

@@ -57,11 +57,11 @@ def test_imported_arms_with_joint_offsets_vs_oracle(gpu, oracle):
         assert np.array_equal(s.is_collision_free_batch(qq).cpu().numpy(), o.configs_free(qq)), dt
     free = q[o.configs_free(q).astype(bool)][:800]
     assert len(free) >= 200
-    q2 = free + rng.uniform(-0.2, 0.2, free.shape)
+    q2 = free + rng.uniform(-0.8, 0.8, free.shape)
     ref = o.edges_free(free, q2, 0.02)
     assert np.array_equal(s.is_edge_collision_free_batch(free, q2, 0.02).cpu().numpy(), ref)
     assert np.array_equal(s.is_edge_collision_free_host(free[:100], q2[:100], 0.02), ref[:100])
-    assert 0.1 < ref.mean() < 0.99
+    assert ref.mean() > 0.1 and (ref == 0).sum() >= 10
     sys.path.insert(0, str(pkg("_lib").HERE.parent / "oracle"))
     import penetration_f64 as orc_pen
 
