@@ -171,9 +171,35 @@ int mrmg_scene_destroy(mrmg_scene *scene);
  * [6] warps per CTA.  out_band gets the FP32 re-check band. */
 int mrmg_scene_info(const mrmg_scene *scene, int64_t *out7, double *out_band);
 
+/* The collision kernels stage a scene's FP32 tables (boxes, spheres, frames,
+ * group pairs) into shared memory with one bulk asynchronous copy (the TMA
+ * engine) of a table image built at scene creation, awaited on an mbarrier
+ * with a bounded wait.  A copy that does not complete within the wait is
+ * replaced by plain loads (the verdicts do not change) and counted here, for
+ * the current device, since the library was loaded.  No reference
+ * counterpart. */
+int mrmg_table_stage_timeouts(uint32_t *out);
+
 /* Launch shape of the persistent kernels (0 = automatic).  Used by the
  * autotuner; the verdicts never depend on it. */
 int mrmg_scene_set_launch(mrmg_scene *scene, int32_t ctas, int32_t warps_per_cta);
+
+/* Work-shape tuning of an arm scene's collision kernels; the verdicts never
+ * depend on it, and launches already captured in a CUDA graph keep the
+ * tuning of their capture.  box_block (1..32, 0 = default 8): boxes whose
+ * near (sphere group, box) pairs are compacted and tested together -- the
+ * obstacle tile; box_head (0..64, taken as given; 8 at creation): boxes
+ * tested one by one, with an exit at the first hit, before the blocks on an
+ * edge's first position; cfg_chunk (1..32, 0 = default 4): configurations a
+ * warp takes from the work queue at a time; phase_b1 (1..64, 0 = default
+ * 3): positions per surviving edge
+ * in the first phase-B launch.  MRMG_ERR_UNSUPPORTED when box_block needs
+ * more shared memory than a CTA has.  Synchronises the device. */
+int mrmg_scene_set_tuning(mrmg_scene *scene, int32_t box_block, int32_t box_head, int32_t cfg_chunk,
+                          int32_t phase_b1);
+
+/* The current tuning: out4 = box_block, box_head, cfg_chunk, phase_b1. */
+int mrmg_scene_get_tuning(const mrmg_scene *scene, int32_t *out4);
 
 /* Test-order autotuning for an arm scene: for the sample configurations
  * d_q[n] (for example uniform in the joint limits) record which boxes each
@@ -202,8 +228,11 @@ int mrmg_is_collision_free_batch(mrmg_scene *scene, const void *d_q, int32_t dty
  * sphere of a robot in the set touches a box or a sphere of another robot in
  * the set (collisions with robots outside the set are ignored, as the
  * reference ignores collisions that involve another robot).  Bit r of
- * robot_mask selects robot r.  Exact, like is_collision_free: the engines'
- * summed-penetration tolerance is not modelled. */
+ * robot_mask selects robot r.  Exact, like is_collision_free.  The rai
+ * engine's tolerance (a colliding configuration counts as free while the
+ * scene's total penetration stays within collision_tolerance) is applied
+ * above this call with mrmg_arm_total_penetration (env.py,
+ * Gb300ArmEnvironment(penetration_tolerance=...)). */
 int mrmg_is_collision_free_batch_robots(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n,
                                         uint32_t robot_mask, uint8_t *d_out, void *stream, int32_t flags);
 
@@ -286,6 +315,21 @@ int mrmg_is_edge_collision_free_batch_noalloc(mrmg_scene *scene, const void *d_q
                                               int32_t include_endpoints, const int64_t *d_N,
                                               int64_t N_start, int64_t N_max, uint8_t *d_out,
                                               void *stream, int32_t flags);
+
+/* Total penetration depth of each configuration of an arm scene, d_out[n]
+ * (FP64, metres), as the rai engine's getCollisionsTotalPenetration that
+ * is_collision_free and is_collision_free_for_robot compare with
+ * collision_tolerance (rai_base_env.py:488-615): the sum over every
+ * sphere-box pair of the radius minus the signed distance of the centre to
+ * the box (outside the box the Euclidean distance, inside minus the distance
+ * to the nearest face) and over every pair of spheres on different robots of
+ * the two radii minus the centre distance, where positive; FP64 sphere
+ * centres; each overlap rounded to a multiple of 2^-40 m and summed exactly,
+ * so the total is independent of the order of the sum.  Robots' own
+ * sphere pairs are not counted (the sphere model has no self-collision).
+ * Synchronous. */
+int mrmg_arm_total_penetration(mrmg_scene *scene, const void *d_q, int32_t dtype, int64_t n, double *d_out,
+                               void *stream);
 
 /* Sphere centres of an arm scene for d_q[n, q_dim]: d_c32[n, S, 3] from the
  * FP32 bulk path and d_c64[n, S, 3] from the exact FP64 path (either may be

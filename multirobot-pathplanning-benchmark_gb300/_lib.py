@@ -48,6 +48,10 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_arm_scene_create": (i32, [i32, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp, vp, i32, vp, vp, f64, C.POINTER(vp)]),
     "mrmg_scene_destroy": (i32, [vp]),
     "mrmg_scene_info": (i32, [vp, vp, vp]),
+    "mrmg_table_stage_timeouts": (i32, [vp]),
+    "mrmg_arm_total_penetration": (i32, [vp, vp, i32, i64, vp, vp]),
+    "mrmg_scene_set_tuning": (i32, [vp, i32, i32, i32, i32]),
+    "mrmg_scene_get_tuning": (i32, [vp, vp]),
     "mrmg_scene_set_launch": (i32, [vp, i32, i32]),
     "mrmg_arm_scene_tune_order": (i32, [vp, vp, i32, i64, vp, vp]),
     "mrmg_is_collision_free_batch": (i32, [vp, vp, i32, i64, vp, vp, i32]),

@@ -149,6 +149,17 @@ class Gb300Scene:
     def set_launch(self, ctas: int = 0, warps_per_cta: int = 0):
         _lib.check(self.lib.mrmg_scene_set_launch(self.h, int(ctas), int(warps_per_cta)))
 
+    def set_tuning(self, box_block: int = 0, box_head: int = 8, cfg_chunk: int = 0, phase_b1: int = 0):
+        """Work shape of an arm scene's kernels (0 = default; see
+        mrmg_scene_set_tuning).  Never changes a verdict."""
+        _lib.check(self.lib.mrmg_scene_set_tuning(self.h, int(box_block), int(box_head), int(cfg_chunk),
+                                                  int(phase_b1)))
+
+    def get_tuning(self) -> dict:
+        out = np.zeros(4, dtype=np.int32)
+        _lib.check(self.lib.mrmg_scene_get_tuning(self.h, out.ctypes.data))
+        return dict(zip(("box_block", "box_head", "cfg_chunk", "phase_b1"), map(int, out)))
+
     def tune_test_order(self, samples, stream=None) -> np.ndarray:
         """Order the boxes so that colliding configurations like `samples`
         (e.g. uniform in the joint limits) stop early; returns the order."""
@@ -313,6 +324,21 @@ class Gb300Scene:
             _lib.check(self.lib.mrmg_arm_slot_map(self.h, out.ctypes.data, cap))
             self._slot_map = out
         return self._slot_map
+
+    def total_penetration(self, q) -> np.ndarray:
+        """Total penetration depth (metres, FP64) of each configuration of an
+        arm scene: sphere-box and inter-robot sphere-pair overlaps summed
+        (mrmg_arm_total_penetration)."""
+        if self.kind != 1:
+            raise TypeError("total penetration exists for arm scenes only")
+        qt = _dev_tensor(q)
+        if qt.dim() == 1:
+            qt = qt.reshape(1, -1)
+        n = qt.shape[0]
+        out = torch.empty(n, dtype=torch.float64, device=qt.device)
+        _lib.check(self.lib.mrmg_arm_total_penetration(self.h, qt.data_ptr(), _dt_code(qt), n, out.data_ptr(),
+                                                       _lib.stream_handle(None)))
+        return out.cpu().numpy()
 
     def sphere_centers(self, q):
         """(FP32, FP64) sphere centres [n, S, 3] of the device kinematics, in

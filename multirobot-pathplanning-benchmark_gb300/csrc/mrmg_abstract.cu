@@ -18,6 +18,7 @@
 // once, one agent pair, box or sphere test per lane.
 #include <algorithm>
 
+#include "mrmg_bulk.cuh"
 #include "mrmg_internal.cuh"
 
 namespace mrmg {
@@ -310,36 +311,46 @@ __device__ bool exact_free_warp(const AbstractDev& s, Acc acc, int lane) {
 // ---------------------------------------------------------------------------
 constexpr size_t kTabSmem = 16384;
 
-__host__ __device__ inline size_t tab_pad(size_t n) { return (n * 4 + 15) & ~(size_t)15; }
-
 // bytes of the staged tables, 0 when they are read from global memory
 __host__ __device__ inline size_t tab_bytes(const AbstractDev& s) {
-  const size_t A = s.A, dim = s.dim, nb = s.nb, ns = s.ns;
-  const size_t b = 2 * tab_pad(A) + tab_pad(A * A) + 2 * tab_pad(nb * dim) + tab_pad(ns * dim) + tab_pad(ns * A);
-  return b <= kTabSmem ? b : 0;
+  size_t off[8];
+  abstract_table_layout(s, off);
+  return off[7] <= kTabSmem ? off[7] : 0;
 }
 
 template <typename T>
-__device__ __forceinline__ const T* stage(const T* src, size_t n, unsigned char** p) {
-  T* dst = (T*)*p;
+__device__ __forceinline__ void stage_copy(T* dst, const T* src, size_t n) {
   for (size_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
-  *p += tab_pad(n);
-  return dst;
 }
 
 // The scene with its FP32 tables in shared memory at `sm` (tab_bytes(s)
-// bytes, in the order tab_bytes counts them); a __syncthreads() must follow.
+// bytes, abstract_table_layout): one bulk asynchronous copy of the scene's
+// table image, or loads when it has none (or the copy timed out).  Every
+// thread calls it; a __syncthreads() must follow.
 __device__ AbstractDev staged_view(const AbstractDev& s, unsigned char* sm) {
+  __shared__ __align__(8) uint64_t stage_bar;
   AbstractDev t = s;
-  if (tab_bytes(s) == 0) return t;
-  unsigned char* p = sm;
-  t.agent_off = stage(s.agent_off, (size_t)s.A, &p);
-  t.r32 = stage(s.r32, (size_t)s.A, &p);
-  t.pair_thr32 = stage(s.pair_thr32, (size_t)s.A * s.A, &p);
-  t.box_lo32 = stage(s.box_lo32, (size_t)s.nb * s.dim, &p);
-  t.box_hi32 = stage(s.box_hi32, (size_t)s.nb * s.dim, &p);
-  t.sph_pos32 = stage(s.sph_pos32, (size_t)s.ns * s.dim, &p);
-  t.sph_thr32 = stage(s.sph_thr32, (size_t)s.ns * s.A, &p);
+  const size_t tb = tab_bytes(s);
+  if (tb == 0) return t;
+  size_t off[8];
+  abstract_table_layout(s, off);
+  t.agent_off = (const int*)(sm + off[0]);
+  t.r32 = (const float*)(sm + off[1]);
+  t.pair_thr32 = (const float*)(sm + off[2]);
+  t.box_lo32 = (const float*)(sm + off[3]);
+  t.box_hi32 = (const float*)(sm + off[4]);
+  t.sph_pos32 = (const float*)(sm + off[5]);
+  t.sph_thr32 = (const float*)(sm + off[6]);
+  const bool bulk = s.img && bulk_ok(sm, s.img, tb);
+  if (bulk && stage_bulk(sm, s.img, (uint32_t)tb, &stage_bar)) return t;
+  stage_copy((int*)t.agent_off, s.agent_off, (size_t)s.A);
+  stage_copy((float*)t.r32, s.r32, (size_t)s.A);
+  stage_copy((float*)t.pair_thr32, s.pair_thr32, (size_t)s.A * s.A);
+  stage_copy((float*)t.box_lo32, s.box_lo32, (size_t)s.nb * s.dim);
+  stage_copy((float*)t.box_hi32, s.box_hi32, (size_t)s.nb * s.dim);
+  stage_copy((float*)t.sph_pos32, s.sph_pos32, (size_t)s.ns * s.dim);
+  stage_copy((float*)t.sph_thr32, s.sph_thr32, (size_t)s.ns * s.A);
+  if (bulk) stage_bulk_drain(&stage_bar);
   return t;
 }
 
@@ -364,7 +375,7 @@ template <bool RESOLVE>
 __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int dtype, long long n,
                              double res, int incl, const long long* Np, long long N_start,
                              long long N_max, uint8_t* out, int* ctr, long long* pend) {
-  extern __shared__ double sm_ab[];
+  extern __shared__ __align__(16) double sm_ab[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int D = s.D;
   // pass 1 classifies from staged tables (pass 2 is rare and reads them in place)
@@ -542,7 +553,7 @@ __global__ void edges_kernel(AbstractDev s, const void* q1, const void* q2, int 
 template <int DIM>
 __global__ void __launch_bounds__(256) configs_fused_kernel(AbstractDev s, const void* q, int dtype, long long n,
                                                             uint8_t* out, int* ctr) {
-  extern __shared__ double sm_cfg[];
+  extern __shared__ __align__(16) double sm_cfg[];
   const AbstractDev cs = staged_view(s, (unsigned char*)sm_cfg);
   __syncthreads();
   const int D = s.D;
@@ -590,7 +601,7 @@ __global__ void __launch_bounds__(256) edges_flat_kernel(AbstractDev s, const vo
                                                          long long n, double res, int incl, const long long* Np,
                                                          long long N_start, long long N_max, uint8_t* out, int* ctr,
                                                          int epc, uint8_t* cta_err) {
-  extern __shared__ double sm_ab[];
+  extern __shared__ __align__(16) double sm_ab[];
   const AbstractDev cs = staged_view(s, (unsigned char*)sm_ab);
   __shared__ int s_err;   // error bits of this CTA when reported per CTA (cta_err)
   __shared__ long long sN[kFlatMaxEpc];
@@ -820,13 +831,15 @@ cudaError_t abstract_edges_mapped(const AbstractDev& s, const void* q1, const vo
 }
 
 int abstract_prepare(const AbstractDev& s) {
-  const size_t sm = flat_smem(s);
-  if (sm > 48 * 1024 &&
-      (cudaFuncSetAttribute(edges_flat_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess ||
-       cudaFuncSetAttribute(edges_flat_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess ||
-       cudaFuncSetAttribute(edges_flat_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess))
+  // the kernels' limits go to the device maximum once (see allow_max_smem)
+  if (allow_max_smem(edges_flat_kernel<0>) != cudaSuccess || allow_max_smem(edges_flat_kernel<2>) != cudaSuccess ||
+      allow_max_smem(edges_flat_kernel<3>) != cudaSuccess)
     return -1;
-  return 0;
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return -1;
+  return flat_smem(s) + 1024 <= (size_t)optin ? 0 : -1;
 }
 
 cudaError_t abstract_edges(const AbstractDev& s, const void* q1, const void* q2, int dtype,
@@ -856,6 +869,12 @@ cudaError_t abstract_edges(const AbstractDev& s, const void* q1, const void* q2,
   edges_kernel<true><<<ls.num_sms, warps * 32, smem2, st>>>(s, q1, q2, dtype, n, res, incl, Np,
                                                             N_start, N_max, out, sc.ctr, sc.pend);
   return cudaGetLastError();
+}
+
+unsigned int abstract_stage_timeouts() {
+  unsigned int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_stage_timeouts, sizeof v) != cudaSuccess) return 0;
+  return v;
 }
 
 }  // namespace mrmg

@@ -14,6 +14,7 @@
 
 #include <cuda.h>
 
+#include "mrmg_bulk.cuh"
 #include "mrmg_internal.cuh"
 
 using namespace mrmg;
@@ -128,6 +129,7 @@ struct mrmg_scene {
   std::vector<ArmTables> modes;
   int cur_mode = -1;
   void* d_mode_tables = nullptr;
+  std::vector<void*> imgs;    // table images (bulk-staged copies of the FP32 tables)
   void* d_offsets = nullptr;          // arm: fixed joint-angle offsets (FP32 hi/lo pairs, FP64)
   ArmSrc src;
   ArmTables& tabs() { return cur_mode < 0 ? base : modes[cur_mode]; }
@@ -338,6 +340,31 @@ void pen_tables(const ArmSrc& a, int R, const std::vector<char>& on, const std::
   pd.NTK = (int)t->pen_task.size();
 }
 
+// The FP32 arm tables of view `v` copied into one device buffer in their
+// shared-memory layout (arm_table_layout), so that a kernel stages them with
+// one bulk asynchronous copy; v->img stays NULL (loads) when they are too large.
+cudaError_t build_arm_image(std::vector<void*>* owned, ArmDev* v) {
+  size_t off[9];
+  arm_table_layout(*v, off);
+  v->img = nullptr;
+  if (off[8] == 0 || off[8] > kStageMaxBytes) return cudaSuccess;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, off[8]);
+  if (e != cudaSuccess) return e;
+  owned->push_back(p);
+  unsigned char* b = (unsigned char*)p;
+  e = cudaMemset(p, 0, off[8]);
+  const size_t SL = (size_t)v->G * v->SPG;
+  const void* src[8] = {v->box32, v->base32, v->dh32, v->sph32, v->band32, v->grp, v->gbs32, v->pairs};
+  const size_t bytes[8] = {sizeof(float4) * 2 * v->B, sizeof(float4) * 3 * v->R, sizeof(float4) * kMaxLinks * v->R,
+                           sizeof(float4) * SL, sizeof(float4) * SL, sizeof(int) * v->G, sizeof(float4) * v->G,
+                           sizeof(uint32_t) * v->NP};
+  for (int k = 0; k < 8 && e == cudaSuccess; k++)
+    if (bytes[k]) e = cudaMemcpy(b + off[k], src[k], bytes[k], cudaMemcpyDeviceToDevice);
+  if (e == cudaSuccess) v->img = p;
+  return e;
+}
+
 // registers a table set's arrays with the upload block
 void add_tables(DevBlock& blk, ArmTables* t) {
   blk.add(t->sph64.data(), t->sph64.size(), &t->d.sph64);
@@ -423,8 +450,26 @@ int mrmg_abstract_scene_create(int32_t n_agents, int32_t dim, int32_t q_dim, con
   blk.add(hi32.data(), hi32.size(), &d.box_hi32);
   blk.add(sp32.data(), sp32.size(), &d.sph_pos32);
   blk.add(sthr32.data(), sthr32.size(), &d.sph_thr32);
+  // the same FP32 tables in their shared-memory layout, staged by one bulk copy
+  std::vector<unsigned char> img;
+  const unsigned char* d_img = nullptr;
+  {
+    size_t lay[8];
+    abstract_table_layout(d, lay);
+    img.assign(lay[7], 0);
+    auto put = [&](int k, const void* src, size_t bytes) { if (bytes) std::memcpy(img.data() + lay[k], src, bytes); };
+    put(0, off.data(), sizeof(int) * A);
+    put(1, r32.data(), sizeof(float) * r32.size());
+    put(2, pthr32.data(), sizeof(float) * pthr32.size());
+    put(3, lo32.data(), sizeof(float) * lo32.size());
+    put(4, hi32.data(), sizeof(float) * hi32.size());
+    put(5, sp32.data(), sizeof(float) * sp32.size());
+    put(6, sthr32.data(), sizeof(float) * sthr32.size());
+    blk.add(img.data(), img.size(), &d_img);
+  }
   cudaError_t e = blk.upload(&sc->d_tables);
   if (e != cudaSuccess) { mrmg_scene_destroy(sc); return cuda_fail(e, "upload abstract scene"); }
+  d.img = (img.empty() || img.size() > kStageMaxBytes) ? nullptr : d_img;
   if (abstract_prepare(sc->ab)) { mrmg_scene_destroy(sc); return fail(MRMG_ERR_UNSUPPORTED, "scene too large"); }
   sc->band = d.delta_k * d.omax;
   *out = sc;
@@ -555,6 +600,7 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
   for (int r = 0; r < R; r++) { d.q_off[r] = h_q_offset[r]; d.base_kind[r] = h_base_kind[r]; d.nl[r] = h_n_links[r]; }
   d.prismatic[0] = prism[0]; d.prismatic[1] = prism[1]; d.prismatic[2] = prism[2];
   d.robot_mask = R >= 32 ? 0xffffffffu : ((1u << R) - 1u);
+  d.box_block = 8; d.box_head = 8; d.cfg_chunk = 4; d.phase_b1 = 3;
 
   std::vector<float4> base32(R * 3), dh32(R * kMaxLinks);
   for (int r = 0; r < R; r++) {
@@ -596,6 +642,8 @@ int mrmg_arm_scene_create(int32_t R, int32_t D, const int32_t* h_q_offset, const
     ArmDev v = d;
     v.sph64 = t.d.sph64; v.box64 = t.d.box64; v.sph32 = t.d.sph32; v.band32 = t.d.band32;
     v.box32 = t.d.box32; v.gbs32 = t.d.gbs32; v.B = t.d.B;
+    e = build_arm_image(&sc->imgs, &v);
+    if (e != cudaSuccess) { mrmg_scene_destroy(sc); return cuda_fail(e, "arm table image"); }
     t.d = v;
     sc->arm = v;
     sc->pen = t.pd;
@@ -661,6 +709,8 @@ int mrmg_arm_scene_set_modes(mrmg_scene* sc, int32_t n_modes, const int32_t* h_s
     ArmDev v = sc->base.d;
     v.sph64 = t.d.sph64; v.box64 = t.d.box64; v.sph32 = t.d.sph32; v.band32 = t.d.band32;
     v.box32 = t.d.box32; v.gbs32 = t.d.gbs32; v.B = t.d.B;
+    e = build_arm_image(&sc->imgs, &v);
+    if (e != cudaSuccess) throw std::bad_alloc();
     t.d = v;
     trim_tables(&t);
   }
@@ -728,6 +778,7 @@ int mrmg_scene_destroy(mrmg_scene* sc) {
   if (sc->d_tables) cudaFree(sc->d_tables);
   if (sc->d_mode_tables) cudaFree(sc->d_mode_tables);
   if (sc->d_offsets) cudaFree(sc->d_offsets);
+  for (void* p : sc->imgs) cudaFree(p);
   if (sc->d_ctr) cudaFree(sc->d_ctr);
   if (sc->d_pend) cudaFree(sc->d_pend);
   if (sc->d_surv) cudaFree(sc->d_surv);
@@ -739,6 +790,43 @@ int mrmg_scene_destroy(mrmg_scene* sc) {
   if (sc->d_small_flags) cudaFree(sc->d_small_flags);
   if (sc->own_stream) cudaStreamDestroy(sc->own_stream);
   delete sc;
+  return MRMG_OK;
+}
+
+int mrmg_scene_set_tuning(mrmg_scene* sc, int32_t box_block, int32_t box_head, int32_t cfg_chunk,
+                          int32_t phase_b1) try {
+  if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
+  if (box_block < 0 || box_block > kMaxBoxBlock || box_head < 0 || box_head > kMaxBoxHead || cfg_chunk < 0 ||
+      cfg_chunk > kMaxCfgChunk || phase_b1 < 0 || phase_b1 > kMaxPhaseB1)
+    return fail(MRMG_ERR_ARG, "tuning out of range (box_block <= %d, box_head <= %d, cfg_chunk <= %d, phase_b1 <= %d)",
+                kMaxBoxBlock, kMaxBoxHead, kMaxCfgChunk, kMaxPhaseB1);
+  ArmDev v = sc->arm;
+  v.box_block = box_block ? box_block : 8;
+  v.box_head = box_head;
+  v.cfg_chunk = cfg_chunk ? cfg_chunk : 4;
+  v.phase_b1 = phase_b1 ? phase_b1 : 3;
+  if (!arm_tuning_fits(v)) return fail(MRMG_ERR_UNSUPPORTED, "box_block %d needs more shared memory than a CTA has", v.box_block);
+  cudaError_t e = cudaDeviceSynchronize();   // no call in flight reads the old shape
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize");
+  auto apply = [&](ArmDev& d) { d.box_block = v.box_block; d.box_head = v.box_head; d.cfg_chunk = v.cfg_chunk; d.phase_b1 = v.phase_b1; };
+  apply(sc->base.d);
+  for (auto& m : sc->modes) apply(m.d);
+  apply(sc->arm);
+  sc->occ_ctas_per_sm = arm_prepare(sc->base.d, 8);
+  return MRMG_OK;
+} catch (...) {
+  return host_fail();
+}
+
+int mrmg_scene_get_tuning(const mrmg_scene* sc, int32_t* out4) {
+  if (!sc || sc->kind != 1 || !out4) return fail(MRMG_ERR_ARG, "arm scene and out4 required");
+  out4[0] = sc->arm.box_block; out4[1] = sc->arm.box_head; out4[2] = sc->arm.cfg_chunk; out4[3] = sc->arm.phase_b1;
+  return MRMG_OK;
+}
+
+int mrmg_table_stage_timeouts(uint32_t* out) {
+  if (!out) return fail(MRMG_ERR_ARG, "NULL argument");
+  *out = arm_stage_timeouts() + abstract_stage_timeouts();
   return MRMG_OK;
 }
 
@@ -819,6 +907,9 @@ int mrmg_arm_scene_tune_order(mrmg_scene* sc, const void* d_q, int32_t dtype, in
   }
   e = cudaMemcpy((void*)sc->arm.box32, b32.data(), sizeof(float4) * 2 * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy((void*)sc->arm.box64, b64.data(), sizeof(double) * 6 * B, cudaMemcpyHostToDevice);
+  // the table image starts with the boxes (arm_table_layout)
+  if (e == cudaSuccess && sc->arm.img)
+    e = cudaMemcpy((void*)sc->arm.img, b32.data(), sizeof(float4) * 2 * B, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "upload box order");
   sc->tabs().box32_host = b32;
   sc->tabs().box64_host = b64;
@@ -1393,6 +1484,21 @@ int mrmg_arm_sphere_centers(mrmg_scene* sc, const void* d_q, int32_t dtype, int6
   if (e != cudaSuccess) return cuda_fail(e, "launch centers");
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, "centers kernel");
+  return MRMG_OK;
+}
+
+int mrmg_arm_total_penetration(mrmg_scene* sc, const void* d_q, int32_t dtype, int64_t n, double* d_out,
+                               void* stream) {
+  if (!sc || sc->kind != 1) return fail(MRMG_ERR_ARG, "arm scene required");
+  if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");
+  if (n > kMaxBatch) return fail(MRMG_ERR_ARG, "batch of %lld exceeds %lld items; split it", (long long)n, kMaxBatch);
+  if (n == 0) return MRMG_OK;
+  if (!d_q || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = arm_penetration(sc->arm, d_q, dtype, n, d_out, sc->num_sms, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch total penetration");
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "total penetration kernel");
   return MRMG_OK;
 }
 

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstdio>
 
+#include "mrmg_bulk.cuh"
 #include "mrmg_internal.cuh"
 
 namespace mrmg {
@@ -44,18 +45,10 @@ struct ArmSmem {
   uint32_t prismatic[3];
 };
 
-__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
-
 __host__ __device__ inline size_t table_bytes(const ArmDev& s) {
-  size_t b = 0;
-  b += align16(sizeof(float4) * s.B * 2);
-  b += align16(sizeof(float4) * s.R * 3);
-  b += align16(sizeof(float4) * s.R * kMaxLinks);
-  b += align16(sizeof(float4) * s.G * s.SPG) * 2;
-  b += align16(sizeof(int) * s.G);
-  b += align16(sizeof(float4) * s.G);
-  b += align16(sizeof(uint32_t) * s.NP);
-  return b;
+  size_t off[9];
+  arm_table_layout(s, off);
+  return off[8];
 }
 
 // per-warp FP32 work area: joint cos/sin, planar translations, sphere table
@@ -63,13 +56,11 @@ constexpr int kNearBlock = 512;   // at most this many group pairs compacted per
 
 __host__ __device__ inline int near_block(const ArmDev& s) { return s.NP < kNearBlock ? (s.NP > 0 ? s.NP : 1) : kNearBlock; }
 
-constexpr int kBoxBlock = 8;   // boxes whose near (group, box) items are compacted together
-constexpr int kBoxHead = 8;    // first positions: boxes tested one by one before the blocks
 
 // the per-warp list holds the near (group, box) items of one box block, then
 // the near group pairs of one pair block
 __host__ __device__ inline int list_cap(const ArmDev& s) {
-  return near_block(s) > s.G * kBoxBlock ? near_block(s) : s.G * kBoxBlock;
+  return near_block(s) > s.G * s.box_block ? near_block(s) : s.G * s.box_block;
 }
 
 __host__ __device__ inline size_t warp32_bytes(const ArmDev& s) {
@@ -84,16 +75,27 @@ __host__ __device__ inline size_t warp64_bytes(const ArmDev& s) {
          align16(sizeof(double) * 3 * s.G * s.SPG);
 }
 
+// The FP32 tables into shared memory at `base` (arm_table_layout): one bulk
+// asynchronous copy of the scene's table image, or loads when the scene has
+// none (or the copy timed out).  Every thread calls it; a __syncthreads()
+// must follow.
 __device__ void stage_tables(const ArmDev& s, unsigned char* base, ArmSmem* t) {
-  unsigned char* p = base;
-  t->box = (float4*)p; p += align16(sizeof(float4) * s.B * 2);
-  t->base = (float4*)p; p += align16(sizeof(float4) * s.R * 3);
-  t->dh = (float4*)p; p += align16(sizeof(float4) * s.R * kMaxLinks);
-  t->sph = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
-  t->band = (float4*)p; p += align16(sizeof(float4) * s.G * s.SPG);
-  t->grp = (int*)p; p += align16(sizeof(int) * s.G);
-  t->gbs = (float4*)p; p += align16(sizeof(float4) * s.G);
-  t->pairs = (uint32_t*)p;
+  __shared__ __align__(8) uint64_t stage_bar;
+  size_t off[9];
+  arm_table_layout(s, off);
+  t->box = (float4*)(base + off[0]);
+  t->base = (float4*)(base + off[1]);
+  t->dh = (float4*)(base + off[2]);
+  t->sph = (float4*)(base + off[3]);
+  t->band = (float4*)(base + off[4]);
+  t->grp = (int*)(base + off[5]);
+  t->gbs = (float4*)(base + off[6]);
+  t->pairs = (uint32_t*)(base + off[7]);
+  t->prismatic[0] = s.prismatic[0];
+  t->prismatic[1] = s.prismatic[1];
+  t->prismatic[2] = s.prismatic[2];
+  const bool bulk = s.img && bulk_ok(base, s.img, off[8]);
+  if (bulk && stage_bulk(base, s.img, (uint32_t)off[8], &stage_bar)) return;
   for (int i = threadIdx.x; i < s.B * 2; i += blockDim.x) t->box[i] = s.box32[i];
   for (int i = threadIdx.x; i < s.R * 3; i += blockDim.x) t->base[i] = s.base32[i];
   for (int i = threadIdx.x; i < s.R * kMaxLinks; i += blockDim.x) t->dh[i] = s.dh32[i];
@@ -106,9 +108,7 @@ __device__ void stage_tables(const ArmDev& s, unsigned char* base, ArmSmem* t) {
     t->gbs[i] = s.gbs32[i];
   }
   for (int i = threadIdx.x; i < s.NP; i += blockDim.x) t->pairs[i] = s.pairs[i];
-  t->prismatic[0] = s.prismatic[0];
-  t->prismatic[1] = s.prismatic[1];
-  t->prismatic[2] = s.prismatic[2];
+  if (bulk) stage_bulk_drain(&stage_bar);
 }
 
 __device__ __forceinline__ bool is_prismatic(const ArmSmem& t, int j) {
@@ -349,7 +349,7 @@ __device__ __forceinline__ uint32_t* wnear_of(const ArmDev& s, float4* wsph) {
 // at the first colliding box (stored configurations); BOX_BLOCKS compacts
 // the near (group, box) items of blocks of boxes (positions of surviving
 // edges, mostly free: every box is scanned); BOX_HEAD_BLOCKS tests the
-// first kBoxBlock boxes (the tuned order puts the likeliest hits first) box
+// first s.box_head boxes (the tuned order puts the likeliest hits first) box
 // by box and the rest in blocks (first positions of edges: most collide early,
 // the survivors scan everything).
 enum : int { BOX_EACH = 0, BOX_BLOCKS = 1, BOX_HEAD_BLOCKS = 2 };
@@ -458,7 +458,7 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
   __syncwarp();
 
   bool unc = false;
-  const int b_each = BOXES == BOX_EACH ? s.B : (BOXES == BOX_HEAD_BLOCKS ? min(s.B, kBoxHead) : 0);
+  const int b_each = BOXES == BOX_EACH ? s.B : (BOXES == BOX_HEAD_BLOCKS ? min(s.B, s.box_head) : 0);
   {
     // --- spheres against boxes, box by box: all of them, or the head
     for (int b = 0; b < b_each; b++) {
@@ -521,10 +521,11 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
   if constexpr (BOXES != BOX_EACH) {
     uint32_t* witem = wnear_of(s, wsph);
     const unsigned ltb = (1u << lane) - 1u;
-    // BOX_BLOCKS: blocks of 1, 1, 2, 4, then kBoxBlock boxes from the first
-    // box; BOX_HEAD_BLOCKS: blocks of kBoxBlock after the per-box head
-    int bs = BOXES == BOX_BLOCKS ? 1 : kBoxBlock;
-    for (int b0 = b_each; b0 < s.B; b0 += bs, bs = (BOXES == BOX_BLOCKS && b0 <= 1) ? 1 : min(2 * bs, kBoxBlock)) {
+    // BOX_BLOCKS: blocks of 1, 1, 2, 4, ... up to s.box_block boxes from the
+    // first box; BOX_HEAD_BLOCKS: blocks of s.box_block after the per-box head
+    const int bmax = s.box_block;
+    int bs = BOXES == BOX_BLOCKS ? 1 : bmax;
+    for (int b0 = b_each; b0 < s.B; b0 += bs, bs = (BOXES == BOX_BLOCKS && b0 <= 1) ? 1 : min(2 * bs, bmax)) {
       const int b1 = min(s.B, b0 + bs);
       int nit = 0;
       int b = b0;
@@ -772,10 +773,8 @@ __device__ __forceinline__ void warp_areas(const ArmDev& s, unsigned char* smem_
 
 // ---------------------------------------------------------------------------
 // Configurations (warp per configuration, configurations taken from a work
-// queue in chunks of kCfgChunk).
+// queue in chunks of s.cfg_chunk).
 // ---------------------------------------------------------------------------
-constexpr int kCfgChunk = 4;
-constexpr int kPhaseB1 = 3;   // positions per survivor in the first phase-B launch
 
 template <int GPL, int SPG, bool RESOLVE>
 __global__ void __launch_bounds__(256, RESOLVE ? 1 : (GPL == 1 ? 4 : (GPL == 2 ? 2 : 1))) arm_configs_kernel(ArmDev s, const void* q, int dtype, long long n,
@@ -791,11 +790,11 @@ __global__ void __launch_bounds__(256, RESOLVE ? 1 : (GPL == 1 ? 4 : (GPL == 2 ?
   const int D = s.D;
   while (true) {
     long long k0 = 0;
-    if (lane == 0) k0 = atomicAdd(&ctr[RESOLVE ? kCtrQueue2 : kCtrQueue], RESOLVE ? 1 : kCfgChunk);
+    if (lane == 0) k0 = atomicAdd(&ctr[RESOLVE ? kCtrQueue2 : kCtrQueue], RESOLVE ? 1 : s.cfg_chunk);
     k0 = __shfl_sync(MRMG_FULL, k0, 0);
     const long long lim = RESOLVE ? (long long)ctr[kCtrPending] : n;
     if (k0 >= lim) break;
-    const int cnt = RESOLVE ? 1 : (int)min((long long)kCfgChunk, lim - k0);
+    const int cnt = RESOLVE ? 1 : (int)min((long long)s.cfg_chunk, lim - k0);
     for (int c = 0; c < cnt; c++) {
       const long long i = RESOLVE ? pend[k0] : k0 + c;
       const CfgSource src{q, dtype, i, D};
@@ -1279,6 +1278,96 @@ __global__ void arm_centers_kernel(ArmDev s, const void* q, int dtype, long long
   }
 }
 
+// Total penetration depth of each configuration (FP64 sphere centres): the
+// sum over every sphere-box pair of the radius minus the signed distance of
+// the centre to the box (outside: the Euclidean distance; inside: minus the
+// distance to the nearest face), and over every pair of spheres on different
+// robots of the two radii minus the centre distance, where positive.  Each
+// overlap is rounded to a multiple of 2^-40 m and the multiples are summed as
+// 64-bit integers, so the total does not depend on the order of the sum.
+constexpr double kPenUnit = 0x1p40;
+
+__device__ __forceinline__ long long overlap_units(double ov) {
+  return ov > 0.0 ? __double2ll_rn(__dmul_rn(ov, kPenUnit)) : 0ll;
+}
+
+__device__ __forceinline__ double box_overlap64(const double* c, const double* bx, double r) {
+  double g2 = 0.0, dmax = -1.0e300;
+  bool outside = false;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double d = fmax(__dsub_rn(bx[k], c[k]), __dsub_rn(c[k], bx[3 + k]));
+    dmax = fmax(dmax, d);
+    if (d > 0.0) {
+      g2 = __dadd_rn(g2, __dmul_rn(d, d));
+      outside = true;
+    }
+  }
+  return __dsub_rn(r, outside ? __dsqrt_rn(g2) : dmax);
+}
+
+__global__ void arm_penetration_kernel(ArmDev s, const void* q, int dtype, long long n, double* out) {
+  extern __shared__ __align__(16) unsigned char smem_arm[];
+  ArmSmem t;
+  stage_tables(s, smem_arm, &t);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float2* wcs; float* wqv; float4* wsph; double* w64;
+  warp_areas(s, smem_arm, table_bytes(s), wib, true, &wcs, &wqv, &wsph, &w64);
+  const int D = s.D, SPG = s.SPG;
+  double* wcs64 = w64 + ((D + 1) & ~1);
+  double* wc64 = wcs64 + 2 * D;
+  const long long nbox = (long long)s.G * SPG * s.B, npair = (long long)s.NP * SPG * SPG;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (long long i = blockIdx.x * (blockDim.x >> 5) + wib; i < n; i += nw) {
+    for (int j = lane; j < D; j += 32) {
+      const double th = ldq(q, dtype, i * D + j);
+      w64[j] = th;
+      double sn, cs;
+      sincos_exact(add_offset64(s, j, th), &sn, &cs);
+      wcs64[2 * j] = cs;
+      wcs64[2 * j + 1] = sn;
+    }
+    __syncwarp();
+    for (int g = lane; g < s.G; g += 32) {
+      const int gi = t.grp[g];
+      double R[9], p[3];
+      chain64(s, w64, wcs64, gi & 0xff, gi >> 8, R, p);
+      for (int v = 0; v < SPG; v++) {
+        const double* l = s.sph64 + (size_t)(g * SPG + v) * 5;
+        double* c = wc64 + (size_t)(g * SPG + v) * 3;
+        for (int k = 0; k < 3; k++)
+          c[k] = __dadd_rn(p[k], __dadd_rn(__dadd_rn(__dmul_rn(R[3 * k], l[0]), __dmul_rn(R[3 * k + 1], l[1])),
+                                           __dmul_rn(R[3 * k + 2], l[2])));
+      }
+    }
+    __syncwarp();
+    long long acc = 0;
+    for (long long u = lane; u < nbox; u += 32) {
+      const int slot = (int)(u / s.B), b = (int)(u % s.B);
+      const double r = s.sph64[(size_t)slot * 5 + 3];
+      if (r < 0.0) continue;
+      acc += overlap_units(box_overlap64(wc64 + 3 * slot, s.box64 + 6 * (size_t)b, r));
+    }
+    for (long long u = lane; u < npair; u += 32) {
+      const int pi = (int)(u / (SPG * SPG)), a = (int)((u / SPG) % SPG), bb = (int)(u % SPG);
+      const uint32_t pr = s.pairs[pi];
+      const int sa = (int)(pr & 0xffffu) * SPG + a, sb = (int)(pr >> 16) * SPG + bb;
+      const double ra = s.sph64[(size_t)sa * 5 + 3], rb = s.sph64[(size_t)sb * 5 + 3];
+      if (ra < 0.0 || rb < 0.0) continue;
+      const double* ca = wc64 + 3 * sa;
+      const double* cb = wc64 + 3 * sb;
+      const double dx = __dsub_rn(ca[0], cb[0]), dy = __dsub_rn(ca[1], cb[1]), dz = __dsub_rn(ca[2], cb[2]);
+      const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+      acc += overlap_units(__dsub_rn(__dadd_rn(ra, rb), __dsqrt_rn(d2)));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(MRMG_FULL, acc, off);
+    if (lane == 0) out[i] = __dmul_rn(__ll2double_rn(acc), 0x1p-40);
+    __syncwarp();
+  }
+}
+
 // Test-order calibration: for each sample configuration, the set of boxes
 // that any sphere touches (FP32, within the re-check band) as a bitmask
 // hits[i * words + b / 32].  Verdicts never depend on the order; the order
@@ -1426,23 +1515,30 @@ static size_t smem_pass(const ArmDev& s, int warps, bool with64) {
   return table_bytes(s) + (size_t)warps * (warp32_bytes(s) + (with64 ? warp64_bytes(s) : 0));
 }
 
-// Sets the dynamic shared-memory limit of every kernel of the scene's variant
-// (once, at scene creation, so that later calls can be captured in a graph)
-// and returns the resident CTAs per SM of the first-pass edge kernel.
+// Raises the dynamic shared-memory limit of every kernel of the scene's
+// variant (at scene creation, so that later calls can be captured in a
+// graph) and returns the resident CTAs per SM of the first-pass edge kernel.
+bool arm_tuning_fits(const ArmDev& s) {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return false;
+  const size_t lim = (size_t)optin - 64;   // static shared memory of the kernels
+  return smem_pass(s, 8, false) <= lim && smem_pass(s, 4, true) <= lim && smem_pass(s, 2, true) <= lim;
+}
+
 int arm_prepare(const ArmDev& s, int warps) {
   const int gpl = arm_gpl_for_spg(s.SPG);
-  const int s1 = (int)smem_pass(s, 8, false), s2 = (int)smem_pass(s, 2, true);
-  const int s3 = (int)smem_pass(s, 4, true);
   int blocks = 0;
   cudaError_t err = cudaErrorInvalidValue;
 #define MRMG_PREP(G_, S_)                                                                          \
   if (gpl == G_ && s.SPG == S_) {                                                                  \
-    cudaFuncSetAttribute(arm_edges_kernel<G_, S_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1); \
-    cudaFuncSetAttribute(arm_edges_kernel<G_, S_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s2);  \
-    cudaFuncSetAttribute(arm_configs_kernel<G_, S_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1); \
-    cudaFuncSetAttribute(arm_configs_kernel<G_, S_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s2);  \
-    cudaFuncSetAttribute(arm_edges_phase_b<G_, S_>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1);        \
-    cudaFuncSetAttribute(arm_small_kernel<G_, S_>, cudaFuncAttributeMaxDynamicSharedMemorySize, s3);         \
+    allow_max_smem(arm_edges_kernel<G_, S_, false>);                                               \
+    allow_max_smem(arm_edges_kernel<G_, S_, true>);                                                \
+    allow_max_smem(arm_configs_kernel<G_, S_, false>);                                             \
+    allow_max_smem(arm_configs_kernel<G_, S_, true>);                                              \
+    allow_max_smem(arm_edges_phase_b<G_, S_>);                                                     \
+    allow_max_smem(arm_small_kernel<G_, S_>);                                                      \
     err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, arm_edges_kernel<G_, S_, false>, warps * 32, \
                                                         smem_pass(s, warps, false));              \
   }
@@ -1450,7 +1546,9 @@ int arm_prepare(const ArmDev& s, int warps) {
   MRMG_PREP(2, 5)
   MRMG_PREP(4, 8)
 #undef MRMG_PREP
-  cudaFuncSetAttribute(arm_centers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, s3);
+  allow_max_smem(arm_centers_kernel);
+  allow_max_smem(arm_box_hits_kernel);
+  allow_max_smem(arm_penetration_kernel);
   if (err != cudaSuccess || blocks < 1) return 1;
   return blocks;
 }
@@ -1459,7 +1557,7 @@ cudaError_t arm_configs(const ArmDev& s, const void* q, int dtype, long long n, 
                         const CallScratch& sc, const LaunchShape& ls, int full, cudaStream_t st) {
   const int gpl = arm_gpl_for_spg(s.SPG);
   const size_t smem1 = smem_pass(s, ls.warps, false);
-  long long want = (n + (long long)ls.warps * kCfgChunk - 1) / ((long long)ls.warps * kCfgChunk);
+  long long want = (n + (long long)ls.warps * s.cfg_chunk - 1) / ((long long)ls.warps * s.cfg_chunk);
   int grid = (int)std::max(1ll, std::min(want, (long long)ls.ctas));
   cudaError_t e = launch_configs<false>(s, gpl, q, dtype, n, out, sc, grid, ls.warps, smem1, full, st);
   if (e != cudaSuccess) return e;
@@ -1478,13 +1576,13 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
   cudaError_t e = launch_edges<false>(s, gpl, q1, q2, dtype, n, res, incl, Np, N_start, N_max, out, sc,
                                       grid, ls.warps, smem1, full, st);
   if (e != cudaSuccess) return e;
-  // B1: the next kPhaseB1 positions of every survivor (kills most colliding
+  // B1: the next s.phase_b1 positions of every survivor (kills most colliding
   // survivors); B2: everything left, spread over all warps
-  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, 0, kPhaseB1, out, ls.num_sms,
+  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, 0, s.phase_b1, out, ls.num_sms,
                      st);
   if (e != cudaSuccess) return e;
   // B2 finalizes the survivors' verdicts in its last CTA
-  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, kPhaseB1, -1, out, ls.num_sms,
+  e = launch_phase_b(s, gpl, q1, q2, dtype, incl, sc, ls.ctas, ls.warps, smem1, full, s.phase_b1, -1, out, ls.num_sms,
                      st);
   if (e != cudaSuccess) return e;
   const int w2 = 2;
@@ -1494,7 +1592,7 @@ cudaError_t arm_edges(const ArmDev& s, const void* q1, const void* q2, int dtype
 
 bool arm_small_ok(const ArmDev& s) {
   // four warps with FP32 and FP64 work areas within the 227 KB a CTA can use
-  return arm_gpl_for_spg(s.SPG) > 0 && smem_pass(s, kSmallWarps, true) <= (size_t)227 * 1024;
+  return arm_gpl_for_spg(s.SPG) > 0 && smem_pass(s, kSmallWarps, true) + 64 <= (size_t)227 * 1024;   // + static shared memory
 }
 
 cudaError_t arm_small(const ArmDev& s, const SmallBatch& b, int num_sms, cudaStream_t st, int* grid_out) {
@@ -1529,6 +1627,16 @@ cudaError_t arm_box_hits(const ArmDev& s, const void* q, int dtype, long long n,
   return cudaGetLastError();
 }
 
+cudaError_t arm_penetration(const ArmDev& s, const void* q, int dtype, long long n, double* out, int num_sms,
+                            cudaStream_t st) {
+  const int warps = 4;
+  const size_t smem = smem_pass(s, warps, true);
+  const long long want = (n + warps - 1) / warps;
+  const int grid = (int)std::max(1ll, std::min(want, (long long)num_sms * 8));
+  arm_penetration_kernel<<<grid, warps * 32, smem, st>>>(s, q, dtype, n, out);
+  return cudaGetLastError();
+}
+
 cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, float* c32, double* c64,
                         cudaStream_t st) {
   const int warps = 4;
@@ -1537,6 +1645,12 @@ cudaError_t arm_centers(const ArmDev& s, const void* q, int dtype, long long n, 
   int grid = (int)std::max(1ll, std::min(want, 4096ll));
   arm_centers_kernel<<<grid, warps * 32, smem, st>>>(s, q, dtype, n, c32, c64);
   return cudaGetLastError();
+}
+
+unsigned int arm_stage_timeouts() {
+  unsigned int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_stage_timeouts, sizeof v) != cudaSuccess) return 0;
+  return v;
 }
 
 }  // namespace mrmg

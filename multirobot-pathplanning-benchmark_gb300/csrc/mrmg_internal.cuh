@@ -26,9 +26,25 @@ struct AbstractDev {
   const float *r32, *pair_thr32, *box_lo32, *box_hi32, *sph_pos32, *sph_thr32;
   float omax;       // max |coordinate| / threshold of any obstacle or agent radius
   float delta_k;    // FP32 band per unit magnitude: 8 * dim * 2^-24
+  const void* img;  // the FP32 tables in their shared-memory layout (tab_bytes), one bulk copy; NULL: staged by loads
   int sph_batch_form;   // per call: Sphere obstacles in the axis=1 norm form (rounded squares,
                         // numpy sum, sqrt) of Sphere.batch_collides_with_sphere, not the ddot form
 };
+
+// shared-memory layout of the FP32 abstract tables (and of AbstractDev::img):
+// agent offsets, radii, pair thresholds, box lo, box hi, sphere centres,
+// sphere thresholds, each padded to 16 bytes; off[7] = total
+__host__ __device__ inline size_t abstract_tab_pad(size_t n) { return (n * 4 + 15) & ~(size_t)15; }
+__host__ __device__ inline void abstract_table_layout(const AbstractDev& s, size_t off[8]) {
+  const size_t A = s.A, dim = s.dim, nb = s.nb, ns = s.ns;
+  const size_t len[7] = {A, A, A * A, nb * dim, nb * dim, ns * dim, ns * A};
+  size_t p = 0;
+  for (int k = 0; k < 7; k++) {
+    off[k] = p;
+    p += abstract_tab_pad(len[k]);
+  }
+  off[7] = p;
+}
 
 // ---------------------------------------------------------------------------
 // Sphere-arm scene.  Spheres are packed into groups of SPG slots; a group
@@ -61,7 +77,35 @@ struct ArmDev {
   // turns by q[j] + offset[j]; NULL when the scene has none
   const float2* off32;     // [D]      offset as FP32 hi + lo
   const double* off64;     // [D]
+  // the FP32 tables above, in their shared-memory layout (arm_table_layout),
+  // staged by one bulk asynchronous copy; NULL: staged by loads
+  const void* img;
+  // launch tuning (never changes a verdict): boxes per compacted block of
+  // the block box phases (the obstacle tile), boxes tested one by one before
+  // the blocks on first positions, configurations a warp takes from the
+  // work queue at a time, positions per survivor in the first phase-B launch
+  int box_block, box_head, cfg_chunk, phase_b1;
 };
+
+constexpr int kMaxBoxBlock = 32, kMaxBoxHead = 64, kMaxCfgChunk = 32, kMaxPhaseB1 = 64;
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// byte offsets of the FP32 arm tables in shared memory (and in ArmDev::img):
+// boxes, base rows, DH rows, spheres, sphere bands, group ids, group bounds,
+// group pairs; off[8] = total
+__host__ __device__ inline void arm_table_layout(const ArmDev& s, size_t off[9]) {
+  size_t p = 0;
+  off[0] = p; p += align16(sizeof(float4) * s.B * 2);
+  off[1] = p; p += align16(sizeof(float4) * s.R * 3);
+  off[2] = p; p += align16(sizeof(float4) * s.R * kMaxLinks);
+  off[3] = p; p += align16(sizeof(float4) * s.G * s.SPG);
+  off[4] = p; p += align16(sizeof(float4) * s.G * s.SPG);
+  off[5] = p; p += align16(sizeof(int) * s.G);
+  off[6] = p; p += align16(sizeof(float4) * s.G);
+  off[7] = p; p += align16(sizeof(uint32_t) * s.NP);
+  off[8] = p;
+}
 
 // ---------------------------------------------------------------------------
 // Path-penetration cost tables of an arm scene: the real spheres (padding
@@ -132,6 +176,33 @@ struct SmallBatch {
   unsigned* flags;       // [n]     device: edge e collides in this call iff flags[e] == epoch
   unsigned epoch;
 };
+
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum less the kernel's static shared memory.  The limit is per kernel
+// and process-wide: setting it once to the maximum means one scene's set-up
+// never lowers it under another scene's launches.
+template <class K>
+inline cudaError_t allow_max_smem(K kernel) {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa{};
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 optin - (int)fa.sharedSizeBytes);
+  return e;
+}
+
+// total penetration depth per configuration (FP64; see arm_penetration_kernel)
+cudaError_t arm_penetration(const ArmDev& s, const void* q, int dtype, long long n, double* out, int num_sms,
+                            cudaStream_t st);
+
+// whether every arm kernel's shared memory fits a CTA with this tuning
+bool arm_tuning_fits(const ArmDev& s);
+
+// table-staging copies that timed out in each translation unit's kernels
+unsigned int arm_stage_timeouts();
+unsigned int abstract_stage_timeouts();
 
 struct SliceTab {
   int A, D, end_all;

@@ -22,6 +22,7 @@
 
 #include <cuda_bf16.h>
 
+#include "mrmg_bulk.cuh"
 #include "mrmg_internal.cuh"
 
 namespace mrmg {
@@ -30,7 +31,6 @@ constexpr int kKnnMaxK = 64;
 constexpr int kKeep = 16;          // candidates kept per query per node chunk
 constexpr int kTileM = 128;        // queries per tile (TMEM lanes)
 constexpr int kRowBytes = 128;     // one SW128 row: 64 bf16
-constexpr long long kWaitSpins = 1ll << 22;
 constexpr int kStagesB = 3;        // node-tile buffers in flight per candidate CTA
 
 // ---------------------------------------------------------------------------
@@ -608,40 +608,6 @@ cudaError_t knn_exact(const double* qs, long long Q, const int* q_mode, const lo
 // tcgen05 / TMA / mbarrier helpers (inline PTX)
 // ---------------------------------------------------------------------------
 namespace {
-
-__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(su32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: false when the barrier did not complete within the limit
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long i = 0; i < kWaitSpins; i++) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (i > 32) __nanosleep(128);
-  }
-  return false;
-}
-// bulk asynchronous copy (TMA, non-tensor) global -> shared, completing on `bar`
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(su32(dst)),
-               "l"(src), "r"(bytes), "r"(su32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(dst_smem)), "r"(ncols)

@@ -79,6 +79,7 @@ class Gb300CollisionBackend:
     _gb300: Gb300Scene
 
     _mode_index = None
+    tolerance_semantics = False
 
     def _use_mode(self, mode):
         """Per-mode scenes: select the tables of the planner's ``mode``
@@ -105,14 +106,71 @@ class Gb300CollisionBackend:
         as with the abstract env (abstract_env.py:356-360)."""
         self._use_mode(m)
 
+    # --- the rai engine's penetration tolerance (rai_base_env.py:442-615) ---
+    def _tol(self, collision_tolerance):
+        """The tolerance a check applies: None (exact verdicts) unless the
+        env was made with ``tolerance_semantics``."""
+        if not self.tolerance_semantics:
+            return None
+        return self.collision_tolerance if collision_tolerance is None else collision_tolerance
+
+    def _tolerate_configs(self, qs: np.ndarray, free: np.ndarray, tol) -> np.ndarray:
+        """rai's rule (rai_base_env.py:460-512, 535-615): a configuration
+        that collides still counts as free while the scene's total
+        penetration depth is at most ``tol``."""
+        free = np.asarray(free, dtype=bool)
+        bad = np.nonzero(~free)[0]
+        if tol is None or len(bad) == 0:
+            return free
+        free = free.copy()
+        free[bad] = self._gb300.total_penetration(np.ascontiguousarray(qs[bad], dtype=np.float64)) <= tol
+        return free
+
+    def _tolerate_edges(self, q1s, q2s, free, resolution, include_endpoints, N, N_start, N_max, tol) -> np.ndarray:
+        """rai's edge check (rai_base_env.py:618-700) under the tolerance:
+        an edge whose exact check found a collision is re-examined position
+        by position (the checked positions q1 + (q2 - q1) / (N - 1) * i of
+        generate_binary_search_indices(N)[N_start:N_max]) with _tolerate_configs."""
+        from .collision import binary_search_indices
+
+        free = np.asarray(free, dtype=bool)
+        bad = np.nonzero(~free)[0]
+        if tol is None or len(bad) == 0:
+            return free
+        free = free.copy()
+        for e in bad:
+            a = np.asarray(q1s[e], dtype=np.float64)
+            b = np.asarray(q2s[e], dtype=np.float64)
+            n = int(N[e]) if N is not None and np.ndim(N) else (int(N) if N is not None else _edge_N(a, b, resolution))
+            hi = n if N_max is None else min(n, int(N_max))
+            if N_start == 0 and hi == n:
+                idx = np.arange(n)
+            else:
+                idx = np.asarray(binary_search_indices(n)[N_start:hi], dtype=np.int64)
+            if not include_endpoints:
+                idx = idx[(idx != 0) & (idx != n - 1)]
+            if len(idx) == 0:
+                continue
+            qs = a[None, :] + ((b - a) / (n - 1))[None, :] * idx[:, None].astype(np.float64)
+            ok = self._gb300.is_collision_free_host(qs).astype(bool)
+            free[e] = bool(self._tolerate_configs(qs, ok, tol).all())
+        return free
+
     # --- single queries (planning_env.py:1724-1763) ------------------------
-    def is_collision_free(self, q, mode) -> bool:
+    def is_collision_free(self, q, mode, collision_tolerance: Optional[float] = None) -> bool:
         """One configuration from host memory: one staged copy each way and,
-        on arm scenes, one kernel launch (Gb300Scene.config_free1)."""
+        on arm scenes, one kernel launch (Gb300Scene.config_free1).  With
+        ``tolerance_semantics`` a colliding configuration is free while its
+        total penetration is at most the tolerance (rai_base_env.py:442-475)."""
         if q is None:
             raise ValueError
         self._use_mode(mode)
-        return self._gb300.config_free1(_state(q))
+        qs = _state(q)
+        ok = self._gb300.config_free1(qs)
+        tol = self._tol(collision_tolerance)
+        if ok or tol is None:
+            return ok
+        return bool(self._tolerate_configs(qs[None, :], np.array([ok]), tol)[0])
 
     def is_edge_collision_free(self, q1, q2, mode, resolution: Optional[float] = None,
                                tolerance: Optional[float] = None, include_endpoints: bool = False,
@@ -123,18 +181,28 @@ class Gb300CollisionBackend:
         if N is not None and N_start > N:
             raise AssertionError
         self._use_mode(mode)
-        return self._gb300.edge_free1(a, b, resolution, include_endpoints, N, N_start, N_max)
+        ok = self._gb300.edge_free1(a, b, resolution, include_endpoints, N, N_start, N_max)
+        tol = self._tol(tolerance)
+        if ok or tol is None:
+            return ok
+        return bool(self._tolerate_edges(a[None, :], b[None, :], np.array([ok]), resolution, include_endpoints, N,
+                                         N_start, N_max, tol)[0])
 
     def is_collision_free_for_robot(self, r, q, m=None, collision_tolerance: Optional[float] = None,
                                     set_mode: bool = True) -> bool:
         """rai_base_env.py:515-615 for arm scenes: free unless a robot of ``r``
         (a name or a list of names) touches a box or another robot of ``r``;
-        collisions with robots outside ``r`` are ignored.  The check is
-        exact, like is_collision_free (``collision_tolerance`` is accepted
-        for the signature; the engines' summed-penetration allowance is not
-        modelled)."""
+        collisions with robots outside ``r`` are ignored.  Exact, like
+        is_collision_free; with ``tolerance_semantics`` such a collision is
+        ignored while the scene's total penetration is at most the tolerance
+        (rai's ``col > collision_tolerance`` test, :549-551)."""
         self._use_mode(m)
-        return self._gb300.config_free1(_state(q), self._robot_mask(r))
+        qs = _state(q)
+        ok = self._gb300.config_free1(qs, self._robot_mask(r))
+        tol = self._tol(collision_tolerance)
+        if ok or tol is None:
+            return ok
+        return bool(self._tolerate_configs(qs[None, :], np.array([ok]), tol)[0])
 
     def batch_is_collision_free_for_robot(self, r, qs, mode=None) -> np.ndarray:
         """Per-configuration verdicts of is_collision_free_for_robot."""

@@ -287,3 +287,22 @@ def test_batched_form_ties_golden(gpu):
         assert env._batch_is_collision_free([S(g["configs"][i], sl)], None) == bool(g["batch1"][i])
     for j, grp in enumerate(g["groups"][:40]):
         assert env._batch_is_collision_free([S(g["configs"][k], sl) for k in grp], None) == bool(g["batch8"][j])
+
+
+def test_table_staging_never_timed_out(gpu):
+    """The kernels stage their scene tables with one bulk asynchronous copy
+    on an mbarrier with a bounded wait; none of this process's launches (the
+    arm and abstract checks run above and here) fell back to loads."""
+    import ctypes
+
+    col, scenes, lib = pkg("collision"), pkg("scenes"), pkg("_lib")
+    rng = np.random.default_rng(1)
+    for sc in (scenes.make_arm_scene(0), scenes.make_disc_scene(0)):
+        s = col.Gb300Scene(sc)
+        q = rng.uniform(-1.0, 1.0, (4096, sc.q_dim)).astype(np.float32)
+        s.is_collision_free_batch(q)
+        s.is_edge_collision_free_batch(q[:2048], q[2048:], 0.05)
+        s.is_collision_free_host(q[:8])
+    v = ctypes.c_uint32(7)
+    lib.check(lib.load().mrmg_table_stage_timeouts(ctypes.byref(v)))
+    assert v.value == 0
