@@ -209,7 +209,8 @@ class Gb300CollisionBackend:
         self._use_mode(mode)
         if isinstance(qs, torch.Tensor):
             return self._gb300.is_collision_free_batch_robots(qs, self._robot_mask(r)).bool()
-        return self._gb300.is_collision_free_host(qs, self._robot_mask(r)).view(np.bool_)
+        v = self._gb300.is_collision_free_host(qs, self._robot_mask(r)).view(np.bool_)
+        return self._tolerate_configs(np.asarray(qs), v, self._tol(None))
 
     def _robot_mask(self, r) -> int:
         names = [r] if isinstance(r, str) else list(r)
@@ -242,7 +243,8 @@ class Gb300CollisionBackend:
         self._use_mode(mode)
         if isinstance(qs, torch.Tensor):
             return self._gb300.is_collision_free_batch(qs).bool()
-        return self._gb300.is_collision_free_host(qs).view(np.bool_)
+        v = self._gb300.is_collision_free_host(qs).view(np.bool_)
+        return self._tolerate_configs(np.asarray(qs), v, self._tol(None))
 
     def batch_is_edge_collision_free(self, q1s, q2s, mode=None, resolution: Optional[float] = None,
                                      include_endpoints: bool = False, N=None) -> np.ndarray:
@@ -252,7 +254,8 @@ class Gb300CollisionBackend:
         self._use_mode(mode)
         if isinstance(q1s, torch.Tensor):
             return self._gb300.is_edge_collision_free_batch(q1s, q2s, resolution, include_endpoints, N).bool()
-        return self._gb300.is_edge_collision_free_host(q1s, q2s, resolution, include_endpoints, N).view(np.bool_)
+        v = self._gb300.is_edge_collision_free_host(q1s, q2s, resolution, include_endpoints, N).view(np.bool_)
+        return self._tolerate_edges(q1s, q2s, v, resolution, include_endpoints, N, 0, None, self._tol(None))
 
     def edge_check_plan(self, n: int, resolution: Optional[float] = None, include_endpoints: bool = False,
                         chunks: int = 1, dtype=torch.float64):
@@ -339,11 +342,15 @@ class Gb300CollisionBackend:
             es = [i for i in range(P - 1) if idx[i] == m]
             if self._gb300.mode != m:
                 self._gb300.set_mode(m)
-            if vs and not self._gb300.is_collision_free_host(qs[vs]).all():
+            tol = self._tol(None)
+            if vs and not self._tolerate_configs(qs[vs], self._gb300.is_collision_free_host(qs[vs]).astype(bool),
+                                                 tol).all():
                 return False
-            if es and not self._gb300.is_edge_collision_free_host(qs[es], qs[[i + 1 for i in es]], resolution,
-                                                                   False).all():
-                return False
+            if es:
+                a, b = qs[es], qs[[i + 1 for i in es]]
+                v = self._gb300.is_edge_collision_free_host(a, b, resolution, False).astype(bool)
+                if not self._tolerate_edges(a, b, v, resolution, False, None, 0, None, tol).all():
+                    return False
         return True
 
     # --- costs (abstract_env.py:238-253) -----------------------------------
@@ -384,10 +391,15 @@ class Gb300ArmEnvironment(Gb300CollisionBackend):
     """Sphere-arm robots (DH chains, optional planar bases) among boxes."""
 
     def __init__(self, scene: ArmScene, collision_resolution: float = 0.05, collision_tolerance: float = 0.01,
-                 band: float = 0.0, tune_samples: int = 4096, seed: int = 0, mode_index=None):
+                 band: float = 0.0, tune_samples: int = 4096, seed: int = 0, mode_index=None,
+                 tolerance_semantics: bool = False):
         """``mode_index`` (per-mode scenes): maps a planner mode to the
         scene's table index; by default an int is its own index and a mode
-        object uses its ``id``."""
+        object uses its ``id``.  ``tolerance_semantics``: the rai engine's
+        rule (rai_base_env.py:442-700) -- a configuration that collides
+        still counts as free while the scene's total penetration depth is at
+        most ``collision_tolerance`` (or the tolerance a call passes); by
+        default the checks are exact."""
         self.scene = scene
         if scene.n_modes:
             self._mode_index = mode_index or (lambda m: m if isinstance(m, (int, np.integer)) else m.id)
@@ -399,6 +411,7 @@ class Gb300ArmEnvironment(Gb300CollisionBackend):
         self.robot_idx = {r: list(range(s, e)) for r, (s, e) in zip(self.robots, sl)}
         self.collision_resolution = collision_resolution
         self.collision_tolerance = collision_tolerance
+        self.tolerance_semantics = bool(tolerance_semantics)
         self.cost_metric = "euclidean"
         self.cost_reduction = "max"
         self._gb300 = Gb300Scene(scene, band=band)

@@ -374,6 +374,51 @@ int orc_arm_configs_free_mask(const void *scene, const double *q, int64_t n, int
   return ORC_OK;
 }
 
+/* Total penetration depth of one configuration (the library's
+ * mrmg_arm_total_penetration; no reference counterpart -- the rai engine's
+ * getCollisionsTotalPenetration, rai_base_env.py:464,546, on the sphere
+ * model): every sphere-box overlap (radius minus the signed distance of the
+ * centre to the box) and every overlap of two spheres on different robots
+ * (radii minus centre distance), where positive, each rounded to a multiple
+ * of 2^-40 m and summed as integers (order-independent, as on the device). */
+static int64_t overlap_units(double ov) { return ov > 0.0 ? (int64_t)llrint(ov * 0x1p40) : 0; }
+
+static double box_overlap(const double *c, const double *lo, const double *hi, double r) {
+  double g2 = 0.0, dmax = -1.0e300;
+  int outside = 0;
+  for (int k = 0; k < 3; k++) {
+    const double d = fmax(lo[k] - c[k], c[k] - hi[k]);
+    dmax = fmax(dmax, d);
+    if (d > 0.0) {
+      g2 = g2 + d * d;
+      outside = 1;
+    }
+  }
+  return r - (outside ? sqrt(g2) : dmax);
+}
+
+int orc_arm_total_penetration(const void *scene, const double *q, int64_t n, int32_t D, double *out) {
+  const orc_arm *a = (const orc_arm *)scene;
+  if (!a || D != a->D) return ORC_ERR_ARG;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < n; i++) {
+    double *c = (double *)malloc(sizeof(double) * 3 * a->S);
+    orc_arm_fk(a, q + (size_t)i * D, c);
+    int64_t acc = 0;
+    for (int s = 0; s < a->S; s++)
+      for (int b = 0; b < a->B; b++) acc += overlap_units(box_overlap(c + 3 * s, a->lo + 3 * b, a->hi + 3 * b, a->s_r[s]));
+    for (int s = 0; s < a->S; s++)
+      for (int t = s + 1; t < a->S; t++) {
+        if (a->s_robot[s] == a->s_robot[t]) continue;
+        const double dx = c[3 * s] - c[3 * t], dy = c[3 * s + 1] - c[3 * t + 1], dz = c[3 * s + 2] - c[3 * t + 2];
+        acc += overlap_units((a->s_r[s] + a->s_r[t]) - sqrt((dx * dx + dy * dy) + dz * dz));
+      }
+    out[i] = (double)acc * 0x1p-40;
+    free(c);
+  }
+  return ORC_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Edge check  (AbstractEnvironment.is_edge_collision_free,                   */
 /* problems/abstract_env.py:301-354)                                          */

@@ -62,6 +62,7 @@ def lib() -> C.CDLL:
         L.orc_arm_new.argtypes = [i32, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp, vp, i32, vp, vp]
         L.orc_arm_free.argtypes = [vp]
         L.orc_arm_set_offsets.argtypes = [vp, vp]
+        L.orc_arm_total_penetration.argtypes = [vp, vp, i64, i32, vp]
         L.orc_abstract_config_free.argtypes = [vp, vp]
         L.orc_arm_config_free.argtypes = [vp, vp]
         L.orc_arm_fk.argtypes = [vp, vp, vp]
@@ -144,6 +145,15 @@ class OracleScene:
         qs = _c(qs, np.float64).reshape(-1, self.D)
         out = np.zeros(len(qs), dtype=np.uint8)
         lib().orc_configs_free(self.kind, self.h, _p(qs), len(qs), self.D, _p(out))
+        return out
+
+    def total_penetration(self, qs) -> np.ndarray:
+        """Total penetration depth per configuration (arm scenes; the
+        library's mrmg_arm_total_penetration)."""
+        qs = _c(qs, np.float64).reshape(-1, self.D)
+        out = np.zeros(len(qs))
+        if lib().orc_arm_total_penetration(self.h, _p(qs), len(qs), self.D, _p(out)) != 0:
+            raise ValueError("total penetration needs an arm scene")
         return out
 
     def configs_free_for_robots(self, qs, robot_mask: int) -> np.ndarray:
