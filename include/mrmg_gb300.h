@@ -350,14 +350,20 @@ int mrmg_arm_sphere_centers(mrmg_scene *scene, const void *d_q, int32_t dtype, i
  * (FP64), d_wp_cost[n_paths, n_waypoints] (the pair terms of waypoint t plus
  * its smoothness term towards t+1), d_grad[n_paths, n_waypoints, q_dim] =
  * d_grad_cost[p] * dcost_p/dw (d_grad_cost NULL means 1).  warps_per_cta 0 =
- * automatic (16).  Synchronises unless MRMG_FLAG_ASYNC. */
+ * automatic (16).  The gradient runs as one launch, or -- when one CTA's
+ * shared memory cannot hold every sphere's gradient for 32 waypoints (about
+ * 270 spheres) -- as one launch per group of consecutive robots, each
+ * writing its robots' joints (the cost then has its own launch).
+ * Synchronises unless MRMG_FLAG_ASYNC. */
 int mrmg_path_penetration(mrmg_scene *scene, const float *d_paths, int64_t n_paths,
                           int32_t n_waypoints, const double *h_params, const float *d_grad_cost,
                           double *d_cost, float *d_wp_cost, float *d_grad, int32_t warps_per_cta,
                           void *stream, int32_t flags);
 
 /* Penetration-kernel facts: [0] spheres, [1] boxes, [2] shared memory per CTA
- * of the cost-only kernel, [3] of the gradient kernel (bytes, 16 warps). */
+ * of the cost-only kernel, [3] of a single-launch gradient kernel covering
+ * every robot (bytes, 16 warps; above the device's limit the gradient runs
+ * per group of robots). */
 int mrmg_penetration_info(const mrmg_scene *scene, int64_t *out4);
 
 /* Graph-capture support.  A call made with MRMG_FLAG_ASYNC inside a stream

@@ -1521,10 +1521,20 @@ int mrmg_path_penetration(mrmg_scene* sc, const float* d_paths, int64_t P, int32
   if (warps > 16) return fail(MRMG_ERR_UNSUPPORTED, "warps per CTA must be <= 16 (and >= robots)");
   int smem_max = 0;
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, sc->device);
-  const size_t smem = pen_smem_bytes(sc->pen.S, sc->pen.B, sc->arm.R, sc->arm.D, d_grad != nullptr, warps);
+  const size_t smem = pen_smem_bytes(sc->arm, sc->pen, 0, warps, 0, sc->arm.R);
   if (smem > (size_t)smem_max)
     return fail(MRMG_ERR_UNSUPPORTED, "scene too large for the penetration kernel (%zu B shared memory > %d)", smem,
                 smem_max);
+  // the gradient runs in one launch, or per group of robots when one CTA's
+  // shared memory cannot hold every sphere's gradient
+  int bounds[kMaxRobots + 1] = {0};
+  int n_groups = 1;
+  if (d_grad) {
+    n_groups = pen_grad_groups(sc->arm, sc->pen, warps, (size_t)smem_max, bounds);
+    if (n_groups < 1)
+      return fail(MRMG_ERR_UNSUPPORTED, "scene too large for the penetration gradient kernel (one robot's gradient "
+                  "needs more than %d B of shared memory)", smem_max);
+  }
   if (P == 0) return MRMG_OK;
   cudaStream_t st = (cudaStream_t)stream;
   if (d_cost && P * nseg > sc->pen_seg_cap) {
@@ -1546,7 +1556,7 @@ int mrmg_path_penetration(mrmg_scene* sc, const float* d_paths, int64_t P, int32
   pp.inv_beta = (float)(1.0 / beta);
   pp.smooth_w = (float)smooth;
   cudaError_t e = pen_launch(sc->arm, sc->pen, pp, d_paths, P, T, d_grad_cost, sc->d_pen_seg, d_cost, d_wp_cost,
-                             d_grad, warps, st);
+                             d_grad, warps, n_groups, bounds, st);
   if (e != cudaSuccess) return cuda_fail(e, "launch penetration cost");
   if (flags & MRMG_FLAG_ASYNC) return MRMG_OK;
   e = cudaStreamSynchronize(st);
@@ -1558,8 +1568,8 @@ int mrmg_penetration_info(const mrmg_scene* sc, int64_t* out4) {
   if (!sc || sc->kind != 1 || !out4) return fail(MRMG_ERR_ARG, "arm scene and out4 required");
   out4[0] = sc->pen.S;
   out4[1] = sc->pen.B;
-  out4[2] = (int64_t)pen_smem_bytes(sc->pen.S, sc->pen.B, sc->arm.R, sc->arm.D, 0, 16);
-  out4[3] = (int64_t)pen_smem_bytes(sc->pen.S, sc->pen.B, sc->arm.R, sc->arm.D, 1, 16);
+  out4[2] = (int64_t)pen_smem_bytes(sc->arm, sc->pen, 0, 16, 0, sc->arm.R);
+  out4[3] = (int64_t)pen_smem_bytes(sc->arm, sc->pen, 1, 16, 0, sc->arm.R);
   return MRMG_OK;
 }
 

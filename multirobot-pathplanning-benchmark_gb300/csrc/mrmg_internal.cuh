@@ -270,10 +270,15 @@ int arm_prepare(const ArmDev& s, int warps);
 int arm_supported_spg(int idx);   // list of compiled SPG values, -1 at end
 int arm_gpl_for_spg(int spg);
 
-size_t pen_smem_bytes(int S, int B, int R, int D, int grad, int warps);
+// shared memory of a penetration launch whose gradient covers robots [gr0, gr1)
+size_t pen_smem_bytes(const ArmDev& a, const PenDev& pd, int grad, int warps, int gr0, int gr1);
+// splits the robots into the fewest groups of consecutive robots whose
+// gradient launches fit in smem_max bytes: bounds[0..n] (n returned; 0 when
+// none fits)
+int pen_grad_groups(const ArmDev& a, const PenDev& pd, int warps, size_t smem_max, int* bounds);
 cudaError_t pen_launch(const ArmDev& a, const PenDev& pd, const PenParams& pp, const float* paths, long long P, int T,
                        const float* gout, double* seg, double* cost, float* wp_cost, float* grad, int warps,
-                       cudaStream_t st);
+                       int n_groups, const int* bounds, cudaStream_t st);
 
 cudaError_t binary_indices(long long N, long long* out, cudaStream_t st, int chunked);
 

@@ -34,24 +34,29 @@ constexpr int kSeg = 32;   // waypoints per CTA
 
 __host__ __device__ inline size_t al4(size_t n) { return (n + 3) & ~(size_t)3; }
 
-// shared memory layout, in floats (every region a multiple of 16 bytes)
+// shared memory layout, in floats (every region a multiple of 16 bytes).
+// The gradient regions cover the Sg spheres and Rg robots whose gradients
+// the launch computes (all of them, or one group of robots of a scene too
+// large for one CTA's shared memory).
 struct PenLayout {
   size_t C, G, OZ, W, QG, sph, box, task, br, part, total;
-  __host__ __device__ PenLayout(int S, int B, int R, int D, bool grad, int warps) {
+  __host__ __device__ PenLayout(int S, int B, int D, bool grad, int warps, int Sg, int Rg) {
     size_t o = 0;
-    C = o;   o += (size_t)S * 3 * kSeg;                         // sphere centres [S*3][32]
-    G = o;   o += grad ? (size_t)S * 3 * kSeg : 0;              // dcost/dcentre  [S*3][32]
-    OZ = o;  o += grad ? (size_t)R * kMaxLinks * 6 * kSeg : 0;  // frame origin, z axis [R][L][6][32]
-    W = o;   o += al4((size_t)(kSeg + 2) * D);                  // waypoints t0-1 .. t0+32
-    QG = o;  o += grad ? al4((size_t)kSeg * D) : 0;             // obstacle gradient [32][D]
+    C = o;   o += (size_t)S * 3 * kSeg;                          // sphere centres [S*3][32]
+    G = o;   o += grad ? (size_t)Sg * 3 * kSeg : 0;              // dcost/dcentre  [Sg*3][32]
+    OZ = o;  o += grad ? (size_t)Rg * kMaxLinks * 6 * kSeg : 0;  // frame origin, z axis [Rg][L][6][32]
+    W = o;   o += al4((size_t)(kSeg + 2) * D);                   // waypoints t0-1 .. t0+32
+    QG = o;  o += grad ? al4((size_t)kSeg * D) : 0;              // obstacle gradient [32][D]
     sph = o; o += (size_t)S * 4;
     box = o; o += (size_t)B * 8;
-    task = o; o += (size_t)S * 4;                              // at most S tasks (int4)
-    br = o;  o += al4((size_t)S);                              // beta log2(e) radius
+    task = o; o += (size_t)S * 4;                               // at most S tasks (int4)
+    br = o;  o += al4((size_t)S);                               // beta log2(e) radius
     part = o; o += (size_t)warps * kSeg * 2;
     total = o;
   }
 };
+
+__host__ __device__ inline int pen_first_sphere(const PenDev& pd, int R, int r) { return r < R ? pd.lk[r][0] : pd.S; }
 
 // MUFU approximations (PTX): 2^x, log2, sqrt, 1/sqrt, 1/x
 __device__ __forceinline__ float ex2a(float x) { float y; asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x)); return y; }
@@ -163,14 +168,18 @@ template <bool COST, bool GRAD>
 __global__ void __launch_bounds__(512, GRAD ? 1 : 2)
     pen_kernel(ArmDev a, PenDev pd, PenParams pp, const float* __restrict__ paths, int T, int nseg,
                const float* __restrict__ gout, double* __restrict__ seg_cost, float* __restrict__ wp_cost,
-               float* __restrict__ grad) {
+               float* __restrict__ grad, int gr0, int gr1) {
   extern __shared__ __align__(16) float smf[];
   const int S = pd.S, B = pd.B, R = a.R, D = a.D;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, NW = blockDim.x >> 5;
   const long long p = blockIdx.x / nseg;
   const int seg = blockIdx.x - (int)(p * nseg);
   const int t0 = seg * kSeg;
-  const PenLayout L(S, B, R, D, GRAD, NW);
+  // the gradient of this launch: robots [gr0, gr1), their spheres [s_lo, s_hi)
+  // and joints [j_lo, j_hi) (robots' joints are contiguous in robot order)
+  const int s_lo = pen_first_sphere(pd, R, gr0), s_hi = pen_first_sphere(pd, R, gr1);
+  const int j_lo = a.q_off[gr0], j_hi = gr1 < R ? a.q_off[gr1] : D;
+  const PenLayout L(S, B, D, GRAD, NW, s_hi - s_lo, gr1 - gr0);
   float* C = smf + L.C;
   float* Gs = smf + L.G;
   float* OZ = smf + L.OZ;
@@ -229,8 +238,8 @@ __global__ void __launch_bounds__(512, GRAD ? 1 : 2)
     const int nl = a.nl[r];
     for (int k = 0; k <= nl; k++) {
       if (k > 0) {
-        if (GRAD) {
-          float* oz = OZ + (size_t)((r * kMaxLinks + (k - 1)) * 6) * kSeg + lane;
+        if (GRAD && r >= gr0 && r < gr1) {
+          float* oz = OZ + (size_t)(((r - gr0) * kMaxLinks + (k - 1)) * 6) * kSeg + lane;
           oz[0] = o[0]; oz[kSeg] = o[1]; oz[2 * kSeg] = o[2];
           oz[3 * kSeg] = m[2]; oz[4 * kSeg] = m[5]; oz[5 * kSeg] = m[8];
         }
@@ -271,6 +280,7 @@ __global__ void __launch_bounds__(512, GRAD ? 1 : 2)
     const int tk = ((base / NW) & 1) ? base + NW - 1 - warp : base + warp;
     if (tk >= NTK) continue;
     const int4 task = tasks[tk];   // sphere, second sphere (-1: none), robot's first sphere, next robot's first
+    if (GRAD && !COST && (task.x < s_lo || task.x >= s_hi)) continue;   // another group's robot
     const bool two = task.y >= 0;
     const int i0 = task.x, i1 = two ? task.y : task.x;
     const float2 cx = make_float2(C[(3 * i0) * kSeg + lane], C[(3 * i1) * kSeg + lane]);
@@ -291,13 +301,14 @@ __global__ void __launch_bounds__(512, GRAD ? 1 : 2)
       for (int j = 0; j < task.z; j++)
         sphere_pair2<false, true>(cx, cy, cz, C[(3 * j) * kSeg + lane], C[(3 * j + 1) * kSeg + lane],
                                   C[(3 * j + 2) * kSeg + lane], nbl, add2(K, bc2(br[j])), pp.inv_scale, a);
-      Gs[(3 * i0) * kSeg + lane] = a.gx.x;
-      Gs[(3 * i0 + 1) * kSeg + lane] = a.gy.x;
-      Gs[(3 * i0 + 2) * kSeg + lane] = a.gz.x;
+      const int g0 = i0 - s_lo, g1 = i1 - s_lo;
+      Gs[(3 * g0) * kSeg + lane] = a.gx.x;
+      Gs[(3 * g0 + 1) * kSeg + lane] = a.gy.x;
+      Gs[(3 * g0 + 2) * kSeg + lane] = a.gz.x;
       if (two) {
-        Gs[(3 * i1) * kSeg + lane] = a.gx.y;
-        Gs[(3 * i1 + 1) * kSeg + lane] = a.gy.y;
-        Gs[(3 * i1 + 2) * kSeg + lane] = a.gz.y;
+        Gs[(3 * g1) * kSeg + lane] = a.gx.y;
+        Gs[(3 * g1 + 1) * kSeg + lane] = a.gy.y;
+        Gs[(3 * g1 + 2) * kSeg + lane] = a.gz.y;
       }
     }
     if (COST) acc2(acc_h, acc_l, two ? a.ps.x + a.ps.y : a.ps.x);
@@ -332,7 +343,7 @@ __global__ void __launch_bounds__(512, GRAD ? 1 : 2)
 
   if (GRAD) {
     // ---- joint gradients from the sphere gradients, tip to base
-    if (warp < R) {
+    if (warp >= gr0 && warp < gr1) {
       const int r = warp;
       const int nl = a.nl[r];
       int jo = a.q_off[r] + (a.base_kind[r] == 1 ? 3 : 0);
@@ -341,14 +352,15 @@ __global__ void __launch_bounds__(512, GRAD ? 1 : 2)
       for (int k = nl; k >= 0; k--) {
         for (int s = pd.lk[r][k]; s < pd.lk[r][k + 1]; s++) {
           const float c0 = C[(3 * s) * kSeg + lane], c1 = C[(3 * s + 1) * kSeg + lane], c2 = C[(3 * s + 2) * kSeg + lane];
-          const float g0 = Gs[(3 * s) * kSeg + lane], g1 = Gs[(3 * s + 1) * kSeg + lane], g2 = Gs[(3 * s + 2) * kSeg + lane];
+          const int sg = s - s_lo;
+          const float g0 = Gs[(3 * sg) * kSeg + lane], g1 = Gs[(3 * sg + 1) * kSeg + lane], g2 = Gs[(3 * sg + 2) * kSeg + lane];
           G0 += g0; G1 += g1; G2 += g2;
           M0 += c1 * g2 - c2 * g1;
           M1 += c2 * g0 - c0 * g2;
           M2 += c0 * g1 - c1 * g0;
         }
         if (k == 0) break;
-        const float* oz = OZ + (size_t)((r * kMaxLinks + (k - 1)) * 6) * kSeg + lane;
+        const float* oz = OZ + (size_t)(((r - gr0) * kMaxLinks + (k - 1)) * 6) * kSeg + lane;
         const float o0 = oz[0], o1 = oz[kSeg], o2 = oz[2 * kSeg];
         const float z0 = oz[3 * kSeg], z1 = oz[4 * kSeg], z2 = oz[5 * kSeg];
         const float v0 = M0 - (o1 * G2 - o2 * G1), v1 = M1 - (o2 * G0 - o0 * G2), v2 = M2 - (o0 * G1 - o1 * G0);
@@ -371,6 +383,8 @@ __global__ void __launch_bounds__(512, GRAD ? 1 : 2)
     for (int i = tid; i < n; i += blockDim.x) {
       const int tt = t0 + i / D;
       if (tt >= T) break;
+      const int j = i - (i / D) * D;
+      if (j < j_lo || j >= j_hi) continue;   // another group's joint
       const float wc = W[i + D];
       float gsm = 0.f;
       if (tt > 0) gsm += sw2 * (wc - W[i]);
@@ -390,30 +404,60 @@ __global__ void pen_sum_kernel(const double* __restrict__ seg, long long P, int 
 
 template <bool COST, bool GRAD>
 cudaError_t launch_one(const ArmDev& a, const PenDev& pd, const PenParams& pp, const float* paths, long long P, int T,
-                       int nseg, const float* gout, double* seg, float* wp, float* grad, int warps, cudaStream_t st) {
-  const size_t smem = pen_smem_bytes(pd.S, pd.B, a.R, a.D, GRAD, warps);
+                       int nseg, const float* gout, double* seg, float* wp, float* grad, int warps, int gr0, int gr1,
+                       cudaStream_t st) {
+  const PenLayout L(pd.S, pd.B, a.D, GRAD, warps, pen_first_sphere(pd, a.R, gr1) - pen_first_sphere(pd, a.R, gr0),
+                    gr1 - gr0);
+  const size_t smem = L.total * sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(pen_kernel<COST, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  pen_kernel<COST, GRAD><<<(unsigned)(P * nseg), warps * 32, smem, st>>>(a, pd, pp, paths, T, nseg, gout, seg, wp, grad);
+  pen_kernel<COST, GRAD><<<(unsigned)(P * nseg), warps * 32, smem, st>>>(a, pd, pp, paths, T, nseg, gout, seg, wp, grad,
+                                                                          gr0, gr1);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-size_t pen_smem_bytes(int S, int B, int R, int D, int grad, int warps) {
-  return PenLayout(S, B, R, D, grad != 0, warps).total * sizeof(float);
+size_t pen_smem_bytes(const ArmDev& a, const PenDev& pd, int grad, int warps, int gr0, int gr1) {
+  return PenLayout(pd.S, pd.B, a.D, grad != 0, warps, pen_first_sphere(pd, a.R, gr1) - pen_first_sphere(pd, a.R, gr0),
+                   gr1 - gr0).total * sizeof(float);
+}
+
+int pen_grad_groups(const ArmDev& a, const PenDev& pd, int warps, size_t smem_max, int* bounds) {
+  // joints must be contiguous in robot order for the groups' joint ranges
+  int jo = 0;
+  for (int r = 0; r < a.R; r++) {
+    if (a.q_off[r] != jo) return a.R == 1 || pen_smem_bytes(a, pd, 1, warps, 0, a.R) <= smem_max ? 1 : 0;
+    jo += (a.base_kind[r] == 1 ? 3 : 0) + a.nl[r];
+  }
+  if (jo != a.D) return pen_smem_bytes(a, pd, 1, warps, 0, a.R) <= smem_max ? 1 : 0;
+  // fewest groups of consecutive robots (balanced by count) whose gradient regions fit
+  for (int ng = 1; ng <= a.R; ng++) {
+    bool ok = true;
+    for (int g = 0; g <= ng; g++) bounds[g] = g * a.R / ng;
+    for (int g = 0; g < ng && ok; g++) ok = pen_smem_bytes(a, pd, 1, warps, bounds[g], bounds[g + 1]) <= smem_max;
+    if (ok) return ng;
+  }
+  return 0;
 }
 
 cudaError_t pen_launch(const ArmDev& a, const PenDev& pd, const PenParams& pp, const float* paths, long long P, int T,
                        const float* gout, double* seg, double* cost, float* wp_cost, float* grad, int warps,
-                       cudaStream_t st) {
+                       int n_groups, const int* bounds, cudaStream_t st) {
   if (P <= 0) return cudaSuccess;
   const int nseg = (T + kSeg - 1) / kSeg;
   const bool want_cost = cost || wp_cost;
-  cudaError_t e;
-  if (want_cost && grad) e = launch_one<true, true>(a, pd, pp, paths, P, T, nseg, gout, seg, wp_cost, grad, warps, st);
-  else if (grad) e = launch_one<false, true>(a, pd, pp, paths, P, T, nseg, gout, nullptr, nullptr, grad, warps, st);
-  else e = launch_one<true, false>(a, pd, pp, paths, P, T, nseg, gout, seg, wp_cost, nullptr, warps, st);
+  cudaError_t e = cudaSuccess;
+  if (grad && n_groups <= 1) {
+    if (want_cost) e = launch_one<true, true>(a, pd, pp, paths, P, T, nseg, gout, seg, wp_cost, grad, warps, 0, a.R, st);
+    else e = launch_one<false, true>(a, pd, pp, paths, P, T, nseg, gout, nullptr, nullptr, grad, warps, 0, a.R, st);
+  } else {
+    if (want_cost || !grad)
+      e = launch_one<true, false>(a, pd, pp, paths, P, T, nseg, gout, seg, wp_cost, nullptr, warps, 0, a.R, st);
+    for (int g = 0; grad && g < n_groups && e == cudaSuccess; g++)
+      e = launch_one<false, true>(a, pd, pp, paths, P, T, nseg, gout, nullptr, nullptr, grad, warps, bounds[g],
+                                  bounds[g + 1], st);
+  }
   if (e != cudaSuccess || !cost) return e;
   const int blocks = (int)std::min<long long>((P + 255) / 256, 4096);
   pen_sum_kernel<<<blocks, 256, 0, st>>>(seg, P, nseg, cost);

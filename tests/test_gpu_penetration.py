@@ -162,10 +162,36 @@ def test_errors(gpu):
     ab = col.Gb300Scene(scenes.make_disc_scene(0))
     with pytest.raises(TypeError):
         pen.path_penetration(ab, np.zeros((1, 3, 4), np.float32))
-    # the 304-sphere mobile scene does not fit the gradient kernel's shared memory
+    # the 304-sphere mobile scene: cost and (grouped) gradient both run
     big = col.Gb300Scene(scenes.make_mobile_scene(0))
-    with pytest.raises(NotImplementedError, match="too large"):
-        pen.path_penetration(big, np.zeros((1, 3, 72), np.float32), grad=True)
-    # but its cost alone does
-    c = pen.path_penetration(big, np.zeros((1, 3, 72), np.float32))["cost"]
-    assert bool(torch.isfinite(c).all())
+    out = pen.path_penetration(big, np.zeros((1, 3, 72), np.float32), grad=True)
+    assert bool(torch.isfinite(out["cost"]).all()) and bool(torch.isfinite(out["grad"]).all())
+
+
+def test_gradient_of_the_304_sphere_mobile_scene(gpu):
+    """Eight mobile manipulators (304 spheres): the single-launch gradient
+    kernel would need more shared memory than a CTA has, so the gradient runs
+    per group of robots; cost and gradient match the float64 autograd
+    oracle, cost alone and cost with gradient agree."""
+    import penetration_f64 as orc_pen
+
+    pen, col, scenes = pkg("penetration"), pkg("collision"), pkg("scenes")
+    sc = scenes.make_mobile_scene(0)
+    s = col.Gb300Scene(sc)
+    info = pen.penetration_info(s)
+    assert info["spheres"] == 304
+    smem_max = getattr(torch.cuda.get_device_properties(0), "shared_memory_per_block_optin", 232448)
+    assert info["smem_grad"] > smem_max
+    paths = scenes.make_path_workload(sc, seed=4, n_paths=3, n_waypoints=40)
+    out = pen.path_penetration(s, torch.from_numpy(paths).cuda(), cost=True, waypoint_cost=True, grad=True)
+    c_ref, g_ref = orc_pen.penetration_grad(sc.arrays(), paths)
+    c = out["cost"].cpu().numpy()
+    assert np.all(np.abs(c - c_ref) <= COST_RTOL * np.abs(c_ref))
+    for p in range(3):
+        assert _rel(out["grad"][p].cpu().numpy(), g_ref[p]) <= GRAD_RTOL, p
+    c_only = pen.path_penetration(s, torch.from_numpy(paths).cuda(), cost=True)["cost"].cpu().numpy()
+    assert np.array_equal(c_only, c)
+    go = torch.tensor([1.0, -2.0, 0.5])
+    g2 = pen.path_penetration(s, torch.from_numpy(paths).cuda(), cost=False, grad=True, grad_cost=go)["grad"]
+    for p in range(3):
+        np.testing.assert_allclose(g2[p].cpu().numpy(), float(go[p]) * out["grad"][p].cpu().numpy(), rtol=1e-6, atol=1e-9)
