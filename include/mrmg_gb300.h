@@ -171,6 +171,30 @@ int mrmg_scene_destroy(mrmg_scene *scene);
  * [6] warps per CTA.  out_band gets the FP32 re-check band. */
 int mrmg_scene_info(const mrmg_scene *scene, int64_t *out7, double *out_band);
 
+/* *out = 1 when the current device reads pageable host memory coherently
+ * (cudaDevAttrPageableMemoryAccess; GB300 over its host link), so kernels may
+ * read callers' host arrays in place; 0 otherwise or when the environment
+ * variable MRMG_STAGE_HOST_INPUTS=1 asks for staged copies. */
+int mrmg_host_access(int32_t *out);
+
+/* The serving batcher's input gather (serving.py): one launch copies every
+ * planner instance's request arrays from host memory into a step's device
+ * buffers -- configurations into rows [0, ccap) of both d_q1 and d_q2 (the
+ * edge q -> q), edge starts and ends into rows [ccap, ccap + ecap), edge step
+ * counts into d_N[ccap + ...], and step counts 3 for the configurations and
+ * 2 for unused slots.  h_table (device-readable: pinned, or pageable where
+ * mrmg_host_access says so) is int64 {n_src, n_configs, n_edges, 0}
+ * followed by n_src rows of {source address, rows, first destination row,
+ * kind (0 configurations, 1 starts, 2 ends, 3 step counts) | 0 << 32}; the
+ * sources are C-contiguous FP32 [rows, q_dim] or int64 [rows] arrays the
+ * device can read (pageable host memory where mrmg_host_access = 1).  The
+ * table is read on the device when the launch runs (a CUDA graph may
+ * capture the launch and rewrite the table between replays); rows outside
+ * the capacities or n_src > max_src set E_BAD_INPUT in *d_err instead of
+ * copying.  Asynchronous.  No reference counterpart. */
+int mrmg_serving_gather(const void *h_table, int32_t max_src, int32_t q_dim, int64_t ccap, int64_t ecap,
+                        float *d_q1, float *d_q2, int64_t *d_N, int32_t *d_err, void *stream);
+
 /* The collision kernels stage a scene's FP32 tables (boxes, spheres, frames,
  * group pairs) into shared memory with one bulk asynchronous copy (the TMA
  * engine) of a table image built at scene creation, awaited on an mbarrier

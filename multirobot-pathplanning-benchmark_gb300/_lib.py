@@ -49,6 +49,8 @@ SIGNATURES: dict[str, tuple] = {
     "mrmg_scene_destroy": (i32, [vp]),
     "mrmg_scene_info": (i32, [vp, vp, vp]),
     "mrmg_table_stage_timeouts": (i32, [vp]),
+    "mrmg_host_access": (i32, [vp]),
+    "mrmg_serving_gather": (i32, [vp, i32, i32, i64, i64, vp, vp, vp, vp, vp]),
     "mrmg_arm_total_penetration": (i32, [vp, vp, i32, i64, vp, vp]),
     "mrmg_scene_set_tuning": (i32, [vp, i32, i32, i32, i32]),
     "mrmg_scene_get_tuning": (i32, [vp, vp]),

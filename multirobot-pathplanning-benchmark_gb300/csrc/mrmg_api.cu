@@ -824,6 +824,27 @@ int mrmg_scene_get_tuning(const mrmg_scene* sc, int32_t* out4) {
   return MRMG_OK;
 }
 
+int mrmg_host_access(int32_t* out) {
+  if (!out) return fail(MRMG_ERR_ARG, "NULL argument");
+  int dev = 0, v = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(pageable memory access)");
+  const char* force = std::getenv("MRMG_STAGE_HOST_INPUTS");
+  *out = (v && !(force && force[0] == '1')) ? 1 : 0;
+  return MRMG_OK;
+}
+
+int mrmg_serving_gather(const void* h_table, int32_t max_src, int32_t q_dim, int64_t ccap, int64_t ecap, float* d_q1,
+                        float* d_q2, int64_t* d_N, int32_t* d_err, void* stream) {
+  if (!h_table || !d_q1 || !d_q2 || !d_N || !d_err) return fail(MRMG_ERR_ARG, "mrmg_serving_gather: NULL argument");
+  if (max_src < 0 || max_src > 65534 || q_dim < 1 || ccap < 0 || ecap < 0)
+    return fail(MRMG_ERR_ARG, "mrmg_serving_gather: max_src 0..65534, q_dim >= 1, capacities >= 0");
+  const cudaError_t e = serving_gather(h_table, max_src, q_dim, ccap, ecap, d_q1, d_q2, (long long*)d_N, d_err,
+                                       (cudaStream_t)stream);
+  return e == cudaSuccess ? MRMG_OK : cuda_fail(e, "launch serving gather");
+}
+
 int mrmg_table_stage_timeouts(uint32_t* out) {
   if (!out) return fail(MRMG_ERR_ARG, "NULL argument");
   *out = arm_stage_timeouts() + abstract_stage_timeouts();
@@ -1003,7 +1024,9 @@ int mrmg_scene_reserve(mrmg_scene* sc, int64_t n, void* stream) {
 
 int mrmg_status_from_error_bits(int32_t bits) {
   if (bits & E_N_START) return fail(MRMG_ERR_N_START, "N_start > N for at least one edge");
-  if (bits & E_BAD_INPUT) return fail(MRMG_ERR_ARG, "non-finite or out-of-range edge length (int() of nan/inf)");
+  if (bits & E_BAD_INPUT)
+    return fail(MRMG_ERR_ARG, "bad input: a non-finite or out-of-range edge length (int() of nan/inf), or a gather row "
+                "outside its step's capacity");
   if (bits & E_TIMEOUT) return fail(MRMG_ERR_TIMEOUT, "a bounded device wait ran out");
   return MRMG_OK;
 }

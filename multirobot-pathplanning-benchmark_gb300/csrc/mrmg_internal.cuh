@@ -197,6 +197,10 @@ inline cudaError_t allow_max_smem(K kernel) {
 cudaError_t arm_penetration(const ArmDev& s, const void* q, int dtype, long long n, double* out, int num_sms,
                             cudaStream_t st);
 
+// the serving batcher's gather of host request arrays (mrmg_serving_gather)
+cudaError_t serving_gather(const void* table, int max_src, int D, long long ccap, long long ecap, float* q1,
+                           float* q2, long long* N, int* err, cudaStream_t st);
+
 // whether every arm kernel's shared memory fits a CTA with this tuning
 bool arm_tuning_fits(const ArmDev& s);
 

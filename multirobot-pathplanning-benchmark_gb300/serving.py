@@ -15,9 +15,14 @@ one CUDA graph launch:
 * unused slots of the capacity bucket get N = 2 and no interior point, so
   they cost nothing.
 
-The graph copies the packed endpoints and counts host->device, runs the
+The graph brings the step's endpoints and counts to the device, runs the
 persistent edge pipeline once over the whole step, and copies the verdicts
-back.  The staging buffers hold FP32 endpoints (half the copy of FP64): the
+back.  Where the device reads pageable host memory (GB300 over its coherent
+host link; ``mrmg_host_access``), the graph's first launch gathers the
+requests' own arrays from host memory through a table of their addresses
+(``mrmg_serving_gather``): no host packing pass and no staging copy.
+Elsewhere the requests are packed into pinned staging buffers on a thread
+pool and copied.  The staging buffers hold FP32 endpoints (half the copy of FP64): the
 verdicts (and step counts N) are the reference's for the FP32 values, so
 FP64 requests are rounded to FP32 first.  Callers that need the FP64
 verdicts of FP64 configurations use
@@ -50,17 +55,28 @@ def edge_steps(q1: np.ndarray, q2: np.ndarray, resolution: float) -> np.ndarray:
 
 
 class _StepGraph:
-    """One capacity bucket: pinned host staging, device buffers, one graph."""
+    """One capacity bucket: device buffers, one graph, and either pinned
+    host staging (packed) or a gather table (direct: the graph's first launch
+    reads the requests' own host arrays, mrmg_serving_gather)."""
 
-    def __init__(self, scene: Gb300Scene, ccap: int, ecap: int, include_endpoints: bool):
+    def __init__(self, scene: Gb300Scene, ccap: int, ecap: int, include_endpoints: bool, direct: bool = False,
+                 max_src: int = 1024):
         self.scene, self.ccap, self.ecap = scene, int(ccap), int(ecap)
         n = self.ccap + self.ecap
         D = scene.q_dim
         self.n = n
-        self.cfg_pin = torch.empty((self.ccap, D), dtype=torch.float32).pin_memory()
-        self.e1_pin = torch.empty((self.ecap, D), dtype=torch.float32).pin_memory()
-        self.e2_pin = torch.empty((self.ecap, D), dtype=torch.float32).pin_memory()
-        self.N_pin = torch.full((n,), 2, dtype=torch.int64).pin_memory()
+        self.direct = bool(direct)
+        self.max_src = int(max_src)
+        if self.direct:
+            # int64 {n_src, n_configs, n_edges, 0}, then rows {address, rows, first row, kind}
+            self.table = torch.zeros(4 + 4 * self.max_src, dtype=torch.int64).pin_memory()
+            self.gerr = torch.zeros(1, dtype=torch.int32, device="cuda")
+            self.gerr_pin = torch.zeros(1, dtype=torch.int32).pin_memory()
+        else:
+            self.cfg_pin = torch.empty((self.ccap, D), dtype=torch.float32).pin_memory()
+            self.e1_pin = torch.empty((self.ecap, D), dtype=torch.float32).pin_memory()
+            self.e2_pin = torch.empty((self.ecap, D), dtype=torch.float32).pin_memory()
+            self.N_pin = torch.full((n,), 2, dtype=torch.int64).pin_memory()
         self.out_pin = torch.empty(n, dtype=torch.uint8).pin_memory()
         self.err_pin = torch.zeros(1, dtype=torch.int32).pin_memory()
         self.q1 = torch.zeros((n, D), dtype=torch.float32, device="cuda")
@@ -87,18 +103,28 @@ class _StepGraph:
 
     def _enqueue(self):
         s, c = self.stream, self.ccap
-        with torch.cuda.stream(s):
-            self.q1[:c].copy_(self.cfg_pin, non_blocking=True)
-            self.q2[:c].copy_(self.q1[:c])
-            self.q1[c:].copy_(self.e1_pin, non_blocking=True)
-            self.q2[c:].copy_(self.e2_pin, non_blocking=True)
-            self.N.copy_(self.N_pin, non_blocking=True)
+        if self.direct:
+            with torch.cuda.stream(s):
+                self.gerr.zero_()
+            _lib.check(self.scene.lib.mrmg_serving_gather(self.table.data_ptr(), self.max_src, self.scene.q_dim,
+                                                          self.ccap, self.ecap, self.q1.data_ptr(), self.q2.data_ptr(),
+                                                          self.N.data_ptr(), self.gerr.data_ptr(), s.cuda_stream),
+                       "serving gather")
+        else:
+            with torch.cuda.stream(s):
+                self.q1[:c].copy_(self.cfg_pin, non_blocking=True)
+                self.q2[:c].copy_(self.q1[:c])
+                self.q1[c:].copy_(self.e1_pin, non_blocking=True)
+                self.q2[c:].copy_(self.e2_pin, non_blocking=True)
+                self.N.copy_(self.N_pin, non_blocking=True)
         self.scene.is_edge_collision_free_batch(self.q1, self.q2, 0.0, self.incl, N=self.N, out=self.out, stream=s,
                                                 flags=_lib.MRMG_FLAG_ASYNC)
         with torch.cuda.stream(s):
             self.err.copy_(self._err_view)
             self.out_pin.copy_(self.out, non_blocking=True)
             self.err_pin.copy_(self.err, non_blocking=True)
+            if self.direct:
+                self.gerr_pin.copy_(self.gerr, non_blocking=True)
 
     def run(self) -> np.ndarray:
         with torch.cuda.stream(self.stream):
@@ -107,7 +133,7 @@ class _StepGraph:
             self.ev1.record(self.stream)
         self.stream.synchronize()
         self.device_ms = self.ev0.elapsed_time(self.ev1)
-        bits = int(self.err_pin.numpy()[0])
+        bits = int(self.err_pin.numpy()[0]) | (int(self.gerr_pin.numpy()[0]) if self.direct else 0)
         if bits:
             _lib.check(self.scene.lib.mrmg_status_from_error_bits(bits), "serving step")
         return self.out_pin.numpy()
@@ -148,23 +174,33 @@ class ServingBatcher:
     per instance (1 = collision free)."""
 
     def __init__(self, scene: Gb300Scene, resolution: float = 0.05, include_endpoints: bool = False,
-                 config_quantum: int = 1 << 16, edge_quantum: int = 1 << 14):
+                 config_quantum: int = 1 << 16, edge_quantum: int = 1 << 14, direct=None, max_sources: int = 1024):
+        """``direct`` (default: where the device reads pageable host memory,
+        mrmg_host_access): ``step`` hands the graph a table of the requests'
+        own arrays, which its first launch reads from host memory, instead of
+        packing them into pinned staging on the host first."""
         if scene.kind != 1:
             raise TypeError("the serving batcher drives arm scenes")
         self.scene = scene
         self.res = float(resolution)
         self.incl = bool(include_endpoints)
         self.cq, self.eq = int(config_quantum), int(edge_quantum)
+        if direct is None:
+            v = C.c_int32(0)
+            _lib.check(scene.lib.mrmg_host_access(C.byref(v)))
+            direct = bool(v.value)
+        self.direct = bool(direct)
+        self.max_src = int(max_sources)
         self.graphs: dict = {}
         self.latencies: list = []
         self.device_ms: list = []
         self._pool = ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1)))
 
-    def _graph(self, nc: int, ne: int) -> _StepGraph:
-        key = (max(1, -(-nc // self.cq)) * self.cq, max(1, -(-ne // self.eq)) * self.eq)
+    def _graph(self, nc: int, ne: int, direct: bool = False) -> _StepGraph:
+        key = (max(1, -(-nc // self.cq)) * self.cq, max(1, -(-ne // self.eq)) * self.eq, bool(direct))
         g = self.graphs.get(key)
         if g is None:
-            g = _StepGraph(self.scene, key[0], key[1], self.incl)
+            g = _StepGraph(self.scene, key[0], key[1], self.incl, direct=direct, max_src=self.max_src)
             self.graphs[key] = g
         return g
 
@@ -212,24 +248,36 @@ class ServingBatcher:
         self.latencies.append(lat)
         return StepResult(cf, ef, lat, g.device_ms, nc, ne, (g.ccap, g.ecap))
 
-    def step(self, requests: list) -> StepResult:
+    def step(self, requests: list, direct=None) -> StepResult:
+        """Verdicts of one step's requests; ``direct`` overrides the
+        batcher's mode for this step (None: the batcher's)."""
         t0 = time.perf_counter()
         D = self.scene.q_dim
-        cs = [np.asarray(r.get("configs", np.zeros((0, D), np.float32)), dtype=np.float32).reshape(-1, D)
-              for r in requests]
-        e1 = [np.asarray(r.get("q1", np.zeros((0, D), np.float32)), dtype=np.float32).reshape(-1, D) for r in requests]
-        e2 = [np.asarray(r.get("q2", np.zeros((0, D), np.float32)), dtype=np.float32).reshape(-1, D) for r in requests]
+
+        def rows(r, key):
+            a = r.get(key)
+            if a is None:
+                return np.zeros((0, D), np.float32)
+            return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, D))
+
+        cs = [rows(r, "configs") for r in requests]
+        e1 = [rows(r, "q1") for r in requests]
+        e2 = [rows(r, "q2") for r in requests]
         for a, b in zip(e1, e2):
             if a.shape != b.shape:
                 raise ValueError("edge endpoints q1 and q2 must have the same shape")
         Ns = []
         for r, a, b in zip(requests, e1, e2):
             N = r.get("N")
-            Ns.append(edge_steps(a, b, self.res) if N is None else np.asarray(N, dtype=np.int64).reshape(-1))
+            Ns.append(edge_steps(a, b, self.res) if N is None
+                      else np.ascontiguousarray(np.asarray(N, dtype=np.int64).reshape(-1)))
             if len(Ns[-1]) != len(a):
                 raise ValueError("one step count per edge")
         nc = int(sum(len(c) for c in cs))
         ne = int(sum(len(a) for a in e1))
+        n_src = sum(len(c) > 0 for c in cs) + 3 * sum(len(a) > 0 for a in e1)
+        if (self.direct if direct is None else bool(direct)) and n_src <= self.max_src:
+            return self._step_direct(t0, cs, e1, e2, Ns, nc, ne)
         g = self._graph(nc, ne)
         cfg_h, e1_h, e2_h, N_h = g.cfg_pin.numpy(), g.e1_pin.numpy(), g.e2_pin.numpy(), g.N_pin.numpy()
         # pack into the pinned staging buffers (numpy copies release the GIL:
@@ -257,6 +305,40 @@ class ServingBatcher:
         N_h[nc:g.ccap] = 2
         N_h[g.ccap + ne:] = 2
         out = g.run()
+        self.device_ms.append(g.device_ms)
+        cf, ef = [], []
+        o = 0
+        for c in cs:
+            cf.append(out[o:o + len(c)].copy())
+            o += len(c)
+        o = g.ccap
+        for a in e1:
+            ef.append(out[o:o + len(a)].copy())
+            o += len(a)
+        lat = time.perf_counter() - t0
+        self.latencies.append(lat)
+        return StepResult(cf, ef, lat, g.device_ms, nc, ne, (g.ccap, g.ecap))
+
+    def _step_direct(self, t0, cs, e1, e2, Ns, nc, ne) -> StepResult:
+        """The step through the gather table: no host copy of the requests;
+        the graph's first launch reads them where they are."""
+        g = self._graph(nc, ne, direct=True)
+        tab = g.table.numpy()
+        k = 4
+        o = 0
+        for c in cs:
+            if len(c):
+                tab[k:k + 4] = (c.ctypes.data, len(c), o, 0)
+                k += 4
+            o += len(c)
+        o = 0
+        for a, b, N in zip(e1, e2, Ns):
+            if len(a):
+                tab[k:k + 12] = (a.ctypes.data, len(a), o, 1, b.ctypes.data, len(b), o, 2, N.ctypes.data, len(N), o, 3)
+                k += 12
+            o += len(a)
+        tab[0:4] = ((k - 4) // 4, nc, ne, 0)
+        out = g.run()   # the arrays of cs / e1 / e2 / Ns stay referenced until the graph has finished
         self.device_ms.append(g.device_ms)
         cf, ef = [], []
         o = 0

@@ -112,3 +112,60 @@ def test_zero_copy_prepare_submit(gpu, oracle):
     res2 = b.step(reqs)
     for a, c in zip(res.config_free + res.edge_free, res2.config_free + res2.edge_free):
         assert np.array_equal(a, c)
+
+
+def test_direct_gather_and_packed_steps_agree(gpu, oracle):
+    """The direct step (the graph's first launch reads the requests' host
+    arrays through the address table) and the packed step (host packing into
+    pinned staging) give the oracle's verdicts, also with float64, strided
+    and empty requests and edges without step counts."""
+    import ctypes
+
+    scenes, col, srv, lib = pkg("scenes"), pkg("collision"), pkg("serving"), pkg("_lib")
+    v = ctypes.c_int32(0)
+    lib.check(lib.load().mrmg_host_access(ctypes.byref(v)))
+    if not v.value:
+        pytest.skip("the device does not read pageable host memory")
+    sc = scenes.make_mobile_scene(0)
+    s = col.Gb300Scene(sc)
+    orc = oracle.OracleScene(sc)
+    b = srv.ServingBatcher(s, config_quantum=1024, edge_quantum=256)
+    assert b.direct
+    for seed in range(3):
+        reqs = _requests(sc, 40 + seed)
+        reqs[0] = dict(configs=reqs[0]["configs"].astype(np.float64), q1=reqs[0]["q1"], q2=reqs[0]["q2"],
+                       N=reqs[0]["N"])
+        reqs[2] = dict(configs=np.asfortranarray(reqs[2]["configs"]), q1=reqs[2]["q1"], q2=reqs[2]["q2"])
+        reqs[3] = dict()
+        d = b.step(reqs)
+        p = b.step(reqs, direct=False)
+        chk = [dict(r) for r in reqs]
+        chk[2]["N"] = srv.edge_steps(reqs[2]["q1"], reqs[2]["q2"], 0.05)
+        chk[0]["configs"] = reqs[0]["configs"].astype(np.float32)
+        _check(orc, chk, d)
+        for a, b_ in zip(d.config_free + d.edge_free, p.config_free + p.edge_free):
+            assert np.array_equal(a, b_)
+    assert any(k[2] for k in b.graphs) and any(not k[2] for k in b.graphs)
+
+
+def test_direct_gather_rejects_a_bad_table(gpu):
+    """A table row outside the step's capacities is refused on the device
+    (error bits, ValueError) instead of copied."""
+    import ctypes
+
+    scenes, col, srv, lib = pkg("scenes"), pkg("collision"), pkg("serving"), pkg("_lib")
+    v = ctypes.c_int32(0)
+    lib.check(lib.load().mrmg_host_access(ctypes.byref(v)))
+    if not v.value:
+        pytest.skip("the device does not read pageable host memory")
+    sc = scenes.make_mobile_scene(0)
+    s = col.Gb300Scene(sc)
+    g = srv._StepGraph(s, 1024, 256, False, direct=True, max_src=8)
+    a = np.zeros((10, sc.q_dim), np.float32)
+    tab = g.table.numpy()
+    tab[0:8] = (1, 10, 0, 0, a.ctypes.data, 10, 1020, 0)      # rows 1020..1029 of a 1,024-row region
+    with pytest.raises(ValueError):
+        g.run()
+    tab[0:8] = (1, 10, 0, 0, a.ctypes.data, 10, 0, 0)
+    out = g.run()
+    assert out.shape == (1024 + 256,)
