@@ -201,6 +201,10 @@ LaunchShape shape(mrmg_scene* sc) {
   return ls;
 }
 
+// the scene's stream and mapped staging buffer (host-pointer calls, below)
+int ensure_stage(mrmg_scene* sc, size_t bytes);
+constexpr size_t kStageHead = 16 * 1024;   // per-CTA statistics / error bytes at the head of the mapped buffer
+
 int finish_call(mrmg_scene* sc, cudaStream_t st, int flags) {
   cudaError_t e = cudaMemcpyAsync(sc->h_ctr, sc->d_ctr, sizeof(int) * kNumCtr, cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(status)");
@@ -949,14 +953,24 @@ int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype,
   if (n == 0) return MRMG_OK;
   if (!d_q || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
   cudaStream_t st = (cudaStream_t)stream;
-  int rc = ensure_pending(sc, n, st);
+  AbstractDev ab = sc->ab;
+  ab.sph_batch_form = (flags & MRMG_FLAG_BATCH_FORM) ? 1 : 0;
+  int rc = ensure_pending(sc, n, st);   // also reserves the scratch of later captured calls
   if (rc) return rc;
+  if (sc->kind == 0 && !(flags & MRMG_FLAG_ASYNC)) {
+    // synchronous abstract call: the fused kernel alone (pending
+    // configurations are decided inline), no counter round trip
+    cudaError_t e = abstract_configs_mapped(ab, d_q, dtype, n, d_out, sc->num_sms, st);
+    if (e != cudaSuccess) return cuda_fail(e, "launch configs");
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+    std::memset(sc->h_ctr, 0, sizeof(int) * kNumCtr);
+    return MRMG_OK;
+  }
   cudaError_t e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   CallScratch cs{sc->d_ctr, sc->d_pend, sc->d_surv, sc->pend_cap};
   LaunchShape ls = shape(sc);
-  AbstractDev ab = sc->ab;
-  ab.sph_batch_form = (flags & MRMG_FLAG_BATCH_FORM) ? 1 : 0;
   e = sc->kind == 0 ? abstract_configs(ab, d_q, dtype, n, d_out, cs, ls, st)
                     : arm_configs(sc->arm, d_q, dtype, n, d_out, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
   if (e != cudaSuccess) return cuda_fail(e, "launch configs");
@@ -996,8 +1010,26 @@ int mrmg_is_edge_collision_free_batch(mrmg_scene* sc, const void* d_q1, const vo
   if (n == 0) return MRMG_OK;
   if (!d_q1 || !d_q2 || !d_out) return fail(MRMG_ERR_ARG, "NULL device pointer");
   cudaStream_t st = (cudaStream_t)stream;
-  int rc = ensure_pending(sc, n, st);
+  int rc = ensure_pending(sc, n, st);   // also reserves the scratch of later captured calls
   if (rc) return rc;
+  if (sc->kind == 0 && n <= kFlatMaxEdges && !(flags & MRMG_FLAG_ASYNC)) {
+    // synchronous abstract call: the flat edge kernel alone, its error bits
+    // per CTA in the mapped buffer's head, no counter round trip
+    rc = ensure_stage(sc, kStageHead);
+    if (rc) return rc;
+    int grid = 0;
+    cudaError_t e = abstract_edges_mapped(sc->ab, d_q1, d_q2, dtype, n, resolution, include_endpoints,
+                                          (const long long*)d_N, N_start, N_max, d_out, sc->m_stage, sc->num_sms, st,
+                                          &grid);
+    if (e != cudaSuccess) return cuda_fail(e, "launch edges");
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+    int bits = 0;
+    for (int c = 0; c < grid; c++) bits |= sc->h_stage[c];
+    std::memset(sc->h_ctr, 0, sizeof(int) * kNumCtr);
+    sc->h_ctr[kCtrErr] = bits;
+    return bits ? mrmg_status_from_error_bits(bits) : MRMG_OK;
+  }
   cudaError_t e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   CallScratch cs{sc->d_ctr, sc->d_pend, sc->d_surv, sc->pend_cap};
@@ -1048,7 +1080,7 @@ namespace {
 constexpr long long kSmallEdges = 256;      // edges per call on the single-launch path
 constexpr long long kSmallItems = 1 << 16;  // (edge, position) items on that path
 constexpr long long kSmallConfigs = 4096;   // configurations per call on that path
-constexpr size_t kStageStats = 16 * 1024;   // per-CTA statistics at the head of the mapped buffer
+constexpr size_t kStageStats = kStageHead;
 
 size_t pad16(size_t x) { return (x + 15) & ~(size_t)15; }
 
