@@ -356,7 +356,8 @@ enum : int { BOX_EACH = 0, BOX_BLOCKS = 1, BOX_HEAD_BLOCKS = 2 };
 
 template <int GPL, int SPG, bool RESOLVE, int BOXES = BOX_EACH, class Src>
 __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, float* wqv,
-                               float4* wsph, double* w64, int lane, const Src& src, bool full) {
+                               float4* wsph, double* w64, int lane, const Src& src, bool full,
+                               bool accum = false) {
   __syncwarp();
   bool hit_any = false;   // full evaluation: remember a collision instead of stopping
   // --- joint preprocessing: FP32 cos/sin of angles reduced to [-pi, pi]
@@ -525,9 +526,14 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
     // first box; BOX_HEAD_BLOCKS: blocks of s.box_block after the per-box head
     const int bmax = s.box_block;
     int bs = BOXES == BOX_BLOCKS ? 1 : bmax;
+    // phase B with `accum` (full evaluation: every box is scanned anyway)
+    // lists the items of consecutive blocks together and tests them when the
+    // next block could overflow the list, instead of a mostly empty round of
+    // item tests per block
+    int nacc = 0;
     for (int b0 = b_each; b0 < s.B; b0 += bs, bs = (BOXES == BOX_BLOCKS && b0 <= 1) ? 1 : min(2 * bs, bmax)) {
       const int b1 = min(s.B, b0 + bs);
-      int nit = 0;
+      int nit = BOXES == BOX_BLOCKS ? nacc : 0;
       int b = b0;
       if constexpr (BOXES == BOX_BLOCKS) {
         // phase B: two boxes per packed FP32x2 instruction (same values as
@@ -569,6 +575,14 @@ __device__ uint8_t eval_config(const ArmDev& s, const ArmSmem& t, float2* wcs, f
           if (nr) witem[nit + __popc(m & ltb)] = (uint32_t)(lane + 32 * u) | ((uint32_t)b << 16);
           nit += __popc(m);
         }
+      }
+      if constexpr (BOXES == BOX_BLOCKS) {
+        const int nbs = b0 + bs <= 1 ? 1 : min(2 * bs, bmax);   // the next block's size
+        if (accum && b1 < s.B && nit + s.G * nbs <= (int)list_cap(s)) {
+          nacc = nit;
+          continue;
+        }
+        nacc = 0;
       }
       __syncwarp();
       for (int base = 0; base < nit; base += 32) {
@@ -1103,7 +1117,8 @@ __global__ void __launch_bounds__(256, GPL == 1 ? 3 : (GPL == 2 ? 2 : 1)) arm_ed
       sdf.rn = __frcp_rn(sdf.nm1);
       sdf.fi = (float)(int)is;   // survivors have N <= 2^24
       stat_cfg++;
-      const uint8_t code = eval_config<GPL, SPG, false, BOX_BLOCKS>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0);
+      const uint8_t code = eval_config<GPL, SPG, false, BOX_BLOCKS>(s, t, wcs, wqv, wsph, w64, lane, sdf, full != 0,
+                                                                    full != 0 || j_lo > 0);
       if (lane == 0) {
         if (code == V_COLLIDE) vsurv[ls].dead = 1;
         else if (code == V_PENDING) vsurv[ls].pend = 1;
