@@ -1165,7 +1165,7 @@ constexpr int kMergeWarps = 4;   // warps per merge CTA
 // ---------------------------------------------------------------------------
 // merge: certify the kept candidates and re-rank them in exact FP64
 // ---------------------------------------------------------------------------
-__global__ void knn_merge_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
+__global__ void __launch_bounds__(32 * kMergeWarps, 4) knn_merge_kernel(const double* __restrict__ qs, long long Q, const int* __restrict__ q_mode,
                                  const double* __restrict__ nodes, const long long* __restrict__ mode_beg,
                                  const long long* __restrict__ mode_end, const int* __restrict__ mode_chunks, int chunks_max, const float* __restrict__ cand_d,
                                  const int* __restrict__ cand_i, const float* __restrict__ cand_b,
