@@ -120,3 +120,60 @@ def test_batched_shortcut_with_repair_arm(gpu, oracle):
             totals[k] = totals.get(k, 0) + v
     print("shortcut stats", totals)
     assert totals["accepted"] >= 1 and totals["repaired"] >= 1
+
+
+class _IdMode(_Mode):
+    def __init__(self, i, task_ids):
+        super().__init__(task_ids)
+        self.id = i
+
+
+def test_shortcutting_on_a_per_mode_scene(gpu, oracle):
+    """Per-mode tables: a path through modes 1 and 2 (different box sets,
+    robot 0's task changes at the switch).  Both shortcutters keep every
+    state free in its own mode and every edge free in its first state's mode
+    (the reference's rule, planning_env.py:1805-1816)."""
+    import dataclasses
+
+    scenes, envm, sc_mod = pkg("scenes"), pkg("env"), pkg("shortcutting")
+    base = scenes.make_arm_scene(2, n_boxes=20)
+    sc = dataclasses.replace(base, mode_boxes=[list(range(20)), list(range(0, 20, 2)), list(range(1, 20, 2))])
+    env = envm.Gb300ArmEnvironment(sc, collision_resolution=0.05, tune_samples=256)
+    orcs = {m: oracle.OracleScene(sc.for_mode(m)) for m in (1, 2)}
+    modes = {1: _IdMode(1, [0, 0, 0, 0]), 2: _IdMode(2, [1, 0, 0, 0])}
+    cfg = pkg("configuration").Gb300Configuration
+    sl = [tuple(map(int, x)) for x in sc.agent_slices()]
+    rng = np.random.default_rng(7)
+    while True:
+        w1 = _free_walk(orcs[1], sc, rng, 6, 0.3, 0.05)
+        if orcs[2].configs_free(w1[-1:])[0]:
+            break
+    qs2 = [w1[-1]]
+    while len(qs2) < 6:
+        c = np.clip(qs2[-1] + rng.uniform(-0.3, 0.3, sc.q_dim), sc.limits[0], sc.limits[1])
+        if orcs[2].configs_free(c[None])[0] and orcs[2].edges_free(qs2[-1][None], c[None], 0.05)[0]:
+            qs2.append(c)
+    path = [_State(cfg(q, sl), modes[1]) for q in w1] + [_State(cfg(q, sl), modes[2]) for q in qs2]
+
+    def check(states, end_atol):
+        Q = np.array([s.q.state() for s in states])
+        ms = [s.mode.id for s in states]
+        for i, m in enumerate(ms):
+            assert orcs[m].configs_free(Q[i:i + 1])[0], i
+        for i in range(len(Q) - 1):
+            assert orcs[ms[i]].edges_free(Q[i:i + 1], Q[i + 1:i + 2], 0.05)[0], i
+        np.testing.assert_array_equal(Q[0], w1[0])
+        np.testing.assert_allclose(Q[-1], qs2[-1], rtol=0, atol=end_atol)
+
+    # the reference's shortcutter rewrites the end state as q0 + diff * (j - i),
+    # within an ulp of the original (it asserts 1e-6, shortcutting.py:236-238)
+    np.random.seed(3)
+    new, (cst, _t) = sc_mod.robot_mode_shortcut(env, path, max_iter=60, resolution=0.05, interpolation_resolution=0.1)
+    check(new, 1e-6)
+    assert cst[-1] <= cst[0]
+    st = {}
+    new, (cst, _t) = sc_mod.batched_robot_mode_shortcut(env, path, rounds=4, batch=128, resolution=0.05,
+                                                         interpolation_resolution=0.1, rng=np.random.default_rng(3),
+                                                         stats=st)
+    check(new, 0.0)
+    assert all(b <= a for a, b in zip(cst, cst[1:])) and st["accepted"] >= 1
