@@ -381,6 +381,17 @@ def run_gb300(args):
     call_e2e = n * ncall / (time.perf_counter() - t0)
     mism += int((vc.numpy().astype(np.uint8) != ref).sum())
 
+    # the same call on the caller's numpy arrays: the kernels read the
+    # endpoints in place from host memory where the device reads pageable
+    # memory (GB300), the verdicts come back in one copy
+    for _ in range(args.warmup):
+        env.batch_is_edge_collision_free(q1, q2)
+    t0 = time.perf_counter()
+    for _ in range(ncall):
+        vn = env.batch_is_edge_collision_free(q1, q2)
+    host_e2e = n * ncall / (time.perf_counter() - t0)
+    mism += int((vn.astype(np.uint8) != ref).sum())
+
     extra = {}
     if rank == 0:
         # ---- plain: one launch (and one host round trip) per edge
@@ -476,6 +487,10 @@ def run_gb300(args):
             "e2e_serial": {"value": e2e_serial, "unit": UNIT,
                            "api": f"Gb300ArmEnvironment.edge_check_plan(n).run(): one step at a time, "
                                   f"{args.chunks} pipelined chunks"},
+            "e2e_host_arrays": {"value": host_e2e, "unit": UNIT,
+                                "api": "Gb300ArmEnvironment.batch_is_edge_collision_free(numpy arrays): one call per "
+                                       "step, endpoints read in place from host memory (pageable access), verdicts "
+                                       "copied back"},
             "e2e_batch_call": {"value": call_e2e, "unit": UNIT,
                                "api": "Gb300ArmEnvironment.batch_is_edge_collision_free(pinned tensors)"},
             "gpu_launches": 4 * args.steps,
@@ -1042,7 +1057,7 @@ def _summary(line: dict) -> dict:
             d = d[k]
         return d
 
-    out = {"edges_per_s": line.get("value"), "e2e_edges_per_s": g("e2e", "value"),
+    out = {"edges_per_s": line.get("value"), "e2e_edges_per_s": g("e2e", "value"), "e2e_host_arrays_edges_per_s": g("e2e_host_arrays", "value"),
            "verdict_mismatches": line.get("verdict_mismatches"),
            "plain_us_per_edge_call": g("plain", "us_per_call"),
            "plain_us_per_config_call": g("plain_configs", "us_per_call"),

@@ -1347,25 +1347,29 @@ int mrmg_is_edge_collision_free_host(mrmg_scene* sc, const void* h_q1, const voi
   cudaStream_t st = sc->own_stream;
   unsigned char* Dv = sc->d_stage;
   cudaError_t e = cudaSuccess;
-  if (sc->pageable) {   // one copy per caller array
-    e = cudaMemcpyAsync(Dv + o_q1, h_q1, qbytes, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(Dv + o_q2, h_q2, qbytes, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && h_N) e = cudaMemcpyAsync(Dv + o_N64, h_N, 8 * (size_t)n, cudaMemcpyHostToDevice, st);
-  } else {
+  // the kernels' inputs: where the device reads pageable host memory, the
+  // caller's arrays themselves (no staging copy); else one copy of the
+  // mapped buffer's inputs
+  const void* k_q1 = h_q1;
+  const void* k_q2 = h_q2;
+  const long long* dN = (const long long*)h_N;
+  if (!sc->pageable) {
     e = cudaMemcpyAsync(Dv + o_N64, H + o_N64, total - o_N64, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(inputs)");
+    k_q1 = Dv + o_q1;
+    k_q2 = Dv + o_q2;
+    dN = h_N ? (const long long*)(Dv + o_N64) : nullptr;
   }
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(inputs)");
   rc = ensure_pending(sc, n, st);
   if (rc) return rc;
   e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   CallScratch cs{sc->d_ctr, sc->d_pend, sc->d_surv, sc->pend_cap};
   LaunchShape ls = shape(sc);
-  const long long* dN = h_N ? (const long long*)(Dv + o_N64) : nullptr;
   e = sc->kind == 0
-          ? abstract_edges(sc->ab, Dv + o_q1, Dv + o_q2, dtype, n, resolution, include_endpoints, dN, N_start, N_max,
+          ? abstract_edges(sc->ab, k_q1, k_q2, dtype, n, resolution, include_endpoints, dN, N_start, N_max,
                            Dv + o_hit, cs, ls, st)
-          : arm_edges(sc->arm, Dv + o_q1, Dv + o_q2, dtype, n, resolution, include_endpoints, dN, N_start, N_max,
+          : arm_edges(sc->arm, k_q1, k_q2, dtype, n, resolution, include_endpoints, dN, N_start, N_max,
                       Dv + o_hit, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
   if (e != cudaSuccess) return cuda_fail(e, "launch edges");
   e = cudaMemcpyAsync(H + o_hit, Dv + o_hit, (size_t)n, cudaMemcpyDeviceToHost, st);
