@@ -1232,9 +1232,15 @@ int mrmg_is_collision_free_host(mrmg_scene* sc, const void* h_q, int32_t dtype, 
   }
   cudaStream_t st = sc->own_stream;
   unsigned char* Dv = sc->d_stage;
-  cudaError_t e = cudaMemcpyAsync(Dv + o_q, sc->pageable ? h_q : (const void*)(H + o_q), qbytes,
-                                  cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(inputs)");
+  // the kernels read the caller's array in place where the device reads
+  // pageable host memory, else one copy of the mapped buffer's input
+  const void* k_q = h_q;
+  cudaError_t e = cudaSuccess;
+  if (!sc->pageable) {
+    e = cudaMemcpyAsync(Dv + o_q, H + o_q, qbytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(inputs)");
+    k_q = Dv + o_q;
+  }
   rc = ensure_pending(sc, n, st);
   if (rc) return rc;
   e = cudaMemsetAsync(sc->d_ctr, 0, sizeof(int) * kNumCtr, st);
@@ -1244,9 +1250,9 @@ int mrmg_is_collision_free_host(mrmg_scene* sc, const void* h_q, int32_t dtype, 
   if (sc->kind == 0) {
     AbstractDev ab = sc->ab;
     ab.sph_batch_form = (flags & MRMG_FLAG_BATCH_FORM) ? 1 : 0;
-    e = abstract_configs(ab, Dv + o_q, dtype, n, Dv + o_hit, cs, ls, st);
+    e = abstract_configs(ab, k_q, dtype, n, Dv + o_hit, cs, ls, st);
   } else {
-    e = arm_configs(a, Dv + o_q, dtype, n, Dv + o_hit, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
+    e = arm_configs(a, k_q, dtype, n, Dv + o_hit, cs, ls, (flags & MRMG_FLAG_FULL_EVAL) ? 1 : 0, st);
   }
   if (e != cudaSuccess) return cuda_fail(e, "launch configs");
   e = cudaMemcpyAsync(H + o_hit, Dv + o_hit, (size_t)n, cudaMemcpyDeviceToHost, st);
