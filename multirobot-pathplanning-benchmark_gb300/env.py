@@ -130,7 +130,9 @@ class Gb300CollisionBackend:
         """rai's edge check (rai_base_env.py:618-700) under the tolerance:
         an edge whose exact check found a collision is re-examined position
         by position (the checked positions q1 + (q2 - q1) / (N - 1) * i of
-        generate_binary_search_indices(N)[N_start:N_max]) with _tolerate_configs."""
+        generate_binary_search_indices(N)[N_start:N_max]) with
+        _tolerate_configs.  The positions of many edges go to the device
+        together, in batches of about 2^20."""
         from .collision import binary_search_indices
 
         free = np.asarray(free, dtype=bool)
@@ -138,22 +140,47 @@ class Gb300CollisionBackend:
         if tol is None or len(bad) == 0:
             return free
         free = free.copy()
-        for e in bad:
-            a = np.asarray(q1s[e], dtype=np.float64)
-            b = np.asarray(q2s[e], dtype=np.float64)
-            n = int(N[e]) if N is not None and np.ndim(N) else (int(N) if N is not None else _edge_N(a, b, resolution))
-            hi = n if N_max is None else min(n, int(N_max))
-            if N_start == 0 and hi == n:
-                idx = np.arange(n)
+        A = np.asarray(q1s, dtype=np.float64)[bad].reshape(len(bad), -1)
+        B = np.asarray(q2s, dtype=np.float64)[bad].reshape(len(bad), -1)
+        if N is None:
+            n = np.array([_edge_N(a, b, resolution) for a, b in zip(A, B)], dtype=np.int64)
+        elif np.ndim(N):
+            n = np.asarray(N, dtype=np.int64).reshape(-1)[bad]
+        else:
+            n = np.full(len(bad), int(N), dtype=np.int64)
+        whole = N_start == 0 and N_max is None
+        lo = 0 if include_endpoints else 1
+        start = 0
+        while start < len(bad):
+            # a batch of edges whose positions add up to about 2^20
+            stop, cnt = start, 0
+            while stop < len(bad) and (stop == start or cnt + n[stop] <= (1 << 20)):
+                cnt += int(n[stop])
+                stop += 1
+            owner, pos = [], []
+            for k in range(start, stop):
+                m = int(n[k])
+                if whole:
+                    idx = np.arange(lo, m - lo, dtype=np.int64) if m - 2 * lo > 0 else np.zeros(0, np.int64)
+                else:
+                    idx = np.asarray(binary_search_indices(m)[N_start:m if N_max is None else min(m, int(N_max))],
+                                     dtype=np.int64)
+                    if not include_endpoints:
+                        idx = idx[(idx != 0) & (idx != m - 1)]
+                owner.append(np.full(len(idx), k, dtype=np.int64))
+                pos.append(idx)
+            owner = np.concatenate(owner)
+            pos = np.concatenate(pos).astype(np.float64)
+            if len(owner):
+                d = (B[owner] - A[owner]) / (n[owner] - 1)[:, None].astype(np.float64)
+                qs = A[owner] + d * pos[:, None]
+                ok = self._tolerate_configs(qs, self._gb300.is_collision_free_host(qs).astype(bool), tol)
+                edge_ok = np.ones(stop - start, dtype=bool)
+                np.logical_and.at(edge_ok, owner - start, ok)
+                free[bad[start:stop]] = edge_ok
             else:
-                idx = np.asarray(binary_search_indices(n)[N_start:hi], dtype=np.int64)
-            if not include_endpoints:
-                idx = idx[(idx != 0) & (idx != n - 1)]
-            if len(idx) == 0:
-                continue
-            qs = a[None, :] + ((b - a) / (n - 1))[None, :] * idx[:, None].astype(np.float64)
-            ok = self._gb300.is_collision_free_host(qs).astype(bool)
-            free[e] = bool(self._tolerate_configs(qs, ok, tol).all())
+                free[bad[start:stop]] = True
+            start = stop
         return free
 
     # --- single queries (planning_env.py:1724-1763) ------------------------
