@@ -838,44 +838,67 @@ __global__ void knn_pack_kernel(const double* __restrict__ nodes, KnnStoreDev st
   }
 }
 
-// per-thread sorted candidate list (approximate squared distance, local index)
-__device__ __forceinline__ void keep_insert(float (&kd)[kKeep], int (&ki)[kKeep], float d, int id) {
-  if (!(d < kd[kKeep - 1])) return;
+// Per-thread kept list: kKeep packed keys in ascending order.  A key is the
+// FP32 bit pattern of a non-negative approximate squared distance with its
+// low bits (`imask`) replaced by the node's index within the item's node
+// chunk, so unsigned key order is distance order (the distance truncated to
+// the remaining mantissa bits, ties to the lower index) and one unsigned
+// min/max pair per slot inserts distance and index together, branch-free.
+// The key's distance lies in [lower, upper]: its bits with the index bits
+// cleared, and with them all set.  An empty slot holds kKeyEmpty: FLT_MAX's
+// bits, whose index field (all ones) no node of a chunk has (a chunk holds
+// fewer than imask + 1 nodes).
+constexpr unsigned kKeyEmpty = 0x7f7fffffu;
+
+__device__ __forceinline__ void key_insert(unsigned (&kk)[kKeep], unsigned key) {
 #pragma unroll
-  for (int i = kKeep - 1; i > 0; i--) {
-    if (d < kd[i - 1]) { kd[i] = kd[i - 1]; ki[i] = ki[i - 1]; }
-    else if (d < kd[i]) { kd[i] = d; ki[i] = id; }
-  }
-  if (d < kd[0]) { kd[0] = d; ki[0] = id; }
+  for (int i = kKeep - 1; i > 0; i--) kk[i] = min(kk[i], max(kk[i - 1], key));
+  kk[0] = min(kk[0], key);
 }
+
+__device__ __forceinline__ float key_lower(unsigned key, unsigned imask) { return __uint_as_float(key & ~imask); }
+__device__ __forceinline__ float key_upper(unsigned key, unsigned imask) { return __uint_as_float(key | imask); }
 
 // Column groups of the epilogue: warp w reads TMEM lanes 32*(w%4) (the lane
 // quadrant its warp rank allows) and the w/4-th slice of each tile's columns,
 // so every query row is scanned by kSplit threads with their own kept lists,
 // merged through shared memory at the end.
-// One 32-column chunk of a query row: the approximate squared distances go
-// to this thread's column of `cand` (column-major over the CTA's threads, so
-// stores and dynamically indexed reloads are bank-conflict free), a bitmask
-// marks those under the current 16th kept distance, and only the marked ones
-// are inserted: the warp runs as many insert steps as its busiest lane needs,
-// instead of one per column whenever any lane inserts.
-template <bool FROM_DOT>
-__device__ __forceinline__ void keep_chunk(float (&kd)[kKeep], int (&ki)[kKeep], const float (&v)[32], float qn,
-                                           float* cand, int col0, float thr) {
-  const int nth = blockDim.x;
-  unsigned m = 0;
+// Marks of a 32-column chunk (bit i: v[i] > t, or v[i] < t): four
+// independent partial masks, so the compare-and-or chain is 8 steps deep
+// instead of 32 (a warp per TMEM lane quadrant leaves few warps per scheduler
+// to hide a long chain).
+template <bool GT>
+__device__ __forceinline__ unsigned mark32(const float (&v)[32], float t) {
+  unsigned p[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-  for (int i = 0; i < 32; i++) {
-    const float d = FROM_DOT ? fmaf(-2.f, v[i], qn) : v[i];
-    if (d < thr) {
-      cand[i * nth] = d;
-      m |= 1u << i;
-    }
-  }
-  while (m) {
-    const int i = __ffs(m) - 1;
-    m &= m - 1;
-    keep_insert(kd, ki, cand[i * nth], col0 + i);
+  for (int i = 0; i < 8; i++)
+#pragma unroll
+    for (int g = 0; g < 4; g++) p[g] |= (unsigned)(GT ? v[8 * g + i] > t : v[8 * g + i] < t) << (8 * g + i);
+  return (p[0] | p[1]) | (p[2] | p[3]);
+}
+
+// One 32-column chunk of a query row, `mk` marking the columns whose
+// distance may lie under the row's threshold: the chunk's values go to this
+// thread's column of `cand` (column-major over the CTA's threads, so stores
+// and dynamically indexed reloads are bank-conflict free) and only the marked
+// ones become keys and meet the kept list: the warp runs as many insert steps
+// as its busiest lane needs, instead of one per column whenever any lane
+// inserts.  `lcol0` is the chunk-local index of the first column.  A marked
+// value whose key does not beat the 16th (earlier inserts of the chunk may
+// have lowered it) is dropped after one compare; a NaN distance is never
+// marked, an infinite one makes a key above every kept key.
+template <bool FROM_DOT>
+__device__ __forceinline__ void keep_marked(unsigned (&kk)[kKeep], const float (&v)[32], unsigned mk, float qn,
+                                            float* cand, int lcol0, unsigned imask) {
+  const int nth = blockDim.x;
+#pragma unroll
+  for (int i = 0; i < 32; i++) cand[i * nth] = v[i];
+  while (mk) {
+    const int i = __ffs(mk) - 1;
+    mk &= mk - 1;
+    const float d = FROM_DOT ? fmaf(-2.f, cand[i * nth], qn) : cand[i * nth];
+    const unsigned key = (__float_as_uint(fmaxf(d, 0.f)) & ~imask) | (unsigned)(lcol0 + i);
+    if (key < kk[kKeep - 1]) key_insert(kk, key);
   }
 }
 
@@ -910,7 +933,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
                                                         int chunks_max, float* __restrict__ cand_d,
                                                         int* __restrict__ cand_i, float* __restrict__ cand_b,
                                                         unsigned* __restrict__ g_thr, float* __restrict__ q_eps,
-                                                        int* __restrict__ err, RadOut ro) {
+                                                        int* __restrict__ err, RadOut ro, unsigned imask) {
   constexpr int NT = FMT == KNN_FMT_EUCL ? kNtEucl : kNtAgent;
   constexpr uint32_t BT = NT * kRowBytes;   // bytes per node tile
   constexpr int S = TcSplit<FMT>::S, NCOL = NT / S;
@@ -924,7 +947,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   unsigned char* sA1 = base;
   unsigned char* sA2 = base + kTileM * kRowBytes;
   unsigned char* sB0 = base + 2 * kTileM * kRowBytes;   // kStagesB node-tile buffers
-  // per-thread candidate column: [32][blockDim] floats after the operand buffers
+  // per-thread candidate column: [32][blockDim] values after the operand buffers
   float* cand = (float*)(sB0 + kStagesB * (size_t)BT) + threadIdx.x;
   __shared__ uint64_t bar_load[kStagesB], bar_mma[2];
   __shared__ uint32_t tbase;
@@ -1036,16 +1059,19 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
     else s_fail = 1;
   }
 
-  float kd[kKeep];
-  int ki[kKeep];
+  unsigned kk[kKeep];
 #pragma unroll
-  for (int i = 0; i < kKeep; i++) { kd[i] = __int_as_float(0x7f800000); ki[i] = -1; }
+  for (int i = 0; i < kKeep; i++) kk[i] = kKeyEmpty;
   // Threshold shared by the CTAs that scan other node chunks of the same
   // query: g_thr[q] holds the smallest 16th-kept value any of them has
   // published (FP32 bits of a non-negative value, so unsigned order is value
-  // order).  A row filters with min(own 16th, shared), read one tile ahead;
-  // `bound` is the smallest threshold this row has filtered with: every node
-  // of the chunk left out of the list lies at or above min(bound, 16th).
+  // order): the upper end of its 16th key's distance, so 16 nodes lie at or
+  // below it.  A row filters with min(lower end of its own 16th key, shared),
+  // read one tile ahead (a node the filter drops may tie the 16th key's
+  // truncated distance: the list may then miss it, which the bound covers);
+  // `bound` is the smallest shared threshold this row has filtered with: every
+  // node of the chunk left out of the list lies at or above min(bound, lower
+  // end of the 16th key).
   const long long qrow = RAD ? -1 : s_qid[row];
   float gcur = __int_as_float(0x7f800000), gnext = gcur, bound = gcur, published = gcur;
 
@@ -1060,7 +1086,7 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
     if (tid == 0 && t + kStagesB < T && done) issue_load(t + kStagesB);   // tile t's MMAs have read its buffer
     if (!RAD && qrow >= 0) gnext = __uint_as_float(*(volatile const unsigned*)&g_thr[qrow]);
     if (done) {
-      const int col_node0 = (it.tile0 + t) * NT;
+      const int lcol = t * NT;   // chunk-local index of the tile's first node
       const uint32_t lane_base = tm + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((t & 1) * (kTm / 2));
       if (FMT == KNN_FMT_EUCL) {
 #pragma unroll 1
@@ -1068,19 +1094,16 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
           float v[32];
           tmem_ld32(lane_base + c0, v);
           if (RAD) {
-            rad_chunk<true>(v, qn, s_tau[row], s_qid[row], col_node0 + c0, ro);
-          } else {
-            // pre-filter: the chunk's largest dot product against the row's
-            // threshold in dot space, (qn - kd[15]) / 2, lowered by a margin
-            // that covers the FP32 rounding of both forms; a chunk that fails
-            // holds no value the kept list would take
-            float vm = v[0];
-#pragma unroll
-            for (int i = 1; i < 32; i++) vm = fmaxf(vm, v[i]);
-            const float thr = fminf(kd[kKeep - 1], gcur);
-            const float th = 0.5f * (qn - thr);
-            if (vm > th - 1e-6f * (fabsf(qn) + fabsf(thr)))
-              keep_chunk<true>(kd, ki, v, qn, cand, col_node0 + c0, thr);
+            rad_chunk<true>(v, qn, s_tau[row], s_qid[row], (it.tile0 + t) * NT + c0, ro);
+          } else if (qrow >= 0) {   // a padding row of a partial query tile keeps no list
+            // marks: the dot products against the row's threshold in dot
+            // space, (qn - thr) / 2, lowered by a margin that covers the FP32
+            // rounding of both forms, so an unmarked column's distance
+            // qn - 2 v lies at or above thr
+            const float thr = fminf(key_lower(kk[kKeep - 1], imask), gcur);
+            const float thd = 0.5f * (qn - thr) - 1e-6f * (fabsf(qn) + fabsf(thr));
+            const unsigned mk = mark32<true>(v, thd);
+            if (mk) keep_marked<true>(kk, v, mk, qn, cand, lcol + c0, imask);
           }
         }
       } else {
@@ -1097,21 +1120,20 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
             for (int i = 0; i < 32; i++) m[i] = fmaxf(m[i], fmaf(-2.f, v[i], qa));
           }
           if (RAD) {
-            rad_chunk<false>(m, 0.f, s_tau[row], s_qid[row], col_node0 + c0, ro);
-          } else {
-            float mm = m[0];   // the chunk's smallest value against the row's threshold
-#pragma unroll
-            for (int i = 1; i < 32; i++) mm = fminf(mm, m[i]);
-            const float thr = fminf(kd[kKeep - 1], gcur);
-            if (mm < thr) keep_chunk<false>(kd, ki, m, 0.f, cand, col_node0 + c0, thr);
+            rad_chunk<false>(m, 0.f, s_tau[row], s_qid[row], (it.tile0 + t) * NT + c0, ro);
+          } else if (qrow >= 0) {
+            const float thr = fminf(key_lower(kk[kKeep - 1], imask), gcur);
+            const unsigned mk = mark32<false>(m, thr);
+            if (mk) keep_marked<false>(kk, m, mk, 0.f, cand, lcol + c0, imask);
           }
         }
       }
     }
     if (!RAD && qrow >= 0) {
       bound = fminf(bound, gcur);
-      if (kd[kKeep - 1] < published) {   // publish a better 16th value
-        published = kd[kKeep - 1];
+      const float up = key_upper(kk[kKeep - 1], imask);
+      if (up < published) {   // publish a better 16th value
+        published = up;
         atomicMin(&g_thr[qrow], __float_as_uint(fmaxf(published, 0.f)));
       }
       gcur = fminf(gcur, gnext);
@@ -1126,33 +1148,37 @@ __global__ void __launch_bounds__(128 * TcSplit<FMT>::S, 1) knn_tc_kernel(KnnSto
   // merge the slices' lists into slice 0's; every MMA has completed, so the
   // operand buffers are free (skipped after a timeout: copies may be in flight)
   if (!RAD && !s_fail) {
-    float* md = (float*)base;
-    int* mi = (int*)(base + (size_t)(S - 1) * kTileM * kKeep * sizeof(float));
+    unsigned* mk = (unsigned*)base;
     if (slice > 0) {
 #pragma unroll
-      for (int i = 0; i < kKeep; i++) {
-        md[((size_t)(slice - 1) * kKeep + i) * kTileM + row] = kd[i];
-        mi[((size_t)(slice - 1) * kKeep + i) * kTileM + row] = ki[i];
-      }
+      for (int i = 0; i < kKeep; i++) mk[((size_t)(slice - 1) * kKeep + i) * kTileM + row] = kk[i];
       if (S > 1) s_bound[row] = bound;   // (S <= 2)
     }
     __syncthreads();
     if (slice == 0) {
       for (int o = 0; o < S - 1; o++)
         for (int i = 0; i < kKeep; i++) {
-          const float d = md[((size_t)o * kKeep + i) * kTileM + row];
-          if (!(d < kd[kKeep - 1])) break;   // each list is sorted
-          keep_insert(kd, ki, d, mi[((size_t)o * kKeep + i) * kTileM + row]);
+          const unsigned key = mk[((size_t)o * kKeep + i) * kTileM + row];
+          if (key >= kk[kKeep - 1]) break;   // each list is sorted
+          key_insert(kk, key);
         }
       if (S > 1) bound = fminf(bound, s_bound[row]);
     }
   }
+  // the lists leave as (lower end of the distance, mode-local node index),
+  // an empty slot as (inf, -1)
   if (!RAD && qid >= 0) {
     float* od = cand_d + ((size_t)qid * chunks_max + it.chunk) * kKeep;
     int* oi = cand_i + ((size_t)qid * chunks_max + it.chunk) * kKeep;
+    const float INF = __int_as_float(0x7f800000);
 #pragma unroll
-    for (int i = 0; i < kKeep; i++) { od[i] = kd[i]; oi[i] = ki[i]; }
-    cand_b[(size_t)qid * chunks_max + it.chunk] = fminf(bound, kd[kKeep - 1]);
+    for (int i = 0; i < kKeep; i++) {
+      const bool empty = (kk[i] & imask) == imask;
+      od[i] = empty ? INF : key_lower(kk[i], imask);
+      oi[i] = empty ? -1 : it.tile0 * NT + (int)(kk[i] & imask);
+    }
+    const bool e15 = (kk[kKeep - 1] & imask) == imask;
+    cand_b[(size_t)qid * chunks_max + it.chunk] = fminf(bound, e15 ? INF : key_lower(kk[kKeep - 1], imask));
   }
   tc_fence_before();
   __syncthreads();
@@ -1171,7 +1197,7 @@ __global__ void __launch_bounds__(32 * kMergeWarps, 4) knn_merge_kernel(const do
                                  const int* __restrict__ cand_i, const float* __restrict__ cand_b,
                                  const float* __restrict__ q_eps, SliceTab t,
                                  int metric, int k, long long* __restrict__ out_idx, double* __restrict__ out_dist,
-                                 long long* __restrict__ fallback, int* __restrict__ n_fallback) {
+                                 long long* __restrict__ fallback, int* __restrict__ n_fallback, unsigned imask) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
@@ -1201,11 +1227,15 @@ __global__ void __launch_bounds__(32 * kMergeWarps, 4) knn_merge_kernel(const do
     __syncwarp();
     int h0 = 0, h1 = 0;
     const int c0 = lane, c1 = lane + 32;
-    // approximate k-th smallest value by k rounds of a warp argmin over list heads
+    // The lists hold the lower ends of their keys' distances (sorted; an
+    // empty slot is inf), so a kept distance lies in [v, v | imask].  An
+    // upper bound of the k-th smallest approximate value: k rounds of a warp
+    // argmin over list heads, each head at its upper end.
+    auto upper = [&](float v) { return v == INF ? INF : __uint_as_float(__float_as_uint(v) | imask); };
     float kth = INF;
     for (int r = 0; r < k; r++) {
-      const float v0 = (c0 < C && h0 < kKeep) ? sv[c0 * kKeep + h0] : INF;
-      const float v1 = (c1 < C && h1 < kKeep) ? sv[c1 * kKeep + h1] : INF;
+      const float v0 = (c0 < C && h0 < kKeep) ? upper(sv[c0 * kKeep + h0]) : INF;
+      const float v1 = (c1 < C && h1 < kKeep) ? upper(sv[c1 * kKeep + h1]) : INF;
       float v = fminf(v0, v1);
       float b = v;
 #pragma unroll
@@ -1751,7 +1781,17 @@ struct ItemPlan {
   std::vector<int> order, qcount, qstart, mode_chunks;
   std::vector<KnnItem> items;
   int chunks_max = 1;
+  int tpc = 1;              // node tiles per chunk
 };
+
+// the index field of the candidate keys: the low bits of a key hold a node's
+// index within its chunk (tpc * NT nodes), all ones marks an empty slot
+static unsigned key_index_mask(const ItemPlan& pl, int NT) {
+  const long long n = (long long)pl.tpc * NT;   // a chunk's nodes: indices 0 .. n - 1 < mask
+  unsigned b = 1;
+  while ((1ll << b) <= n) b++;
+  return (unsigned)((1ll << b) - 1);
+}
 
 static void plan_items(const KnnStore* s, const int* h_q_mode, long long Q, int num_sms, ItemPlan* pl) {
   const int n_modes = s->n_modes;
@@ -1776,6 +1816,7 @@ static void plan_items(const KnnStore* s, const int* h_q_mode, long long Q, int 
     for (int m = 0; m < n_modes; m++) chunks_max = std::max(chunks_max, (s->mode_tiles[m] + tpc - 1) / tpc);
   }
   pl->chunks_max = chunks_max;
+  pl->tpc = tpc;
   pl->items.clear();
   pl->mode_chunks.assign(n_modes, 0);
   for (int m = 0; m < n_modes; m++) {
@@ -1904,13 +1945,14 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   const size_t smem = tc_smem_bytes(s);
   raise_smem_limit<KNN_FMT_EUCL, false>();
   raise_smem_limit<KNN_FMT_AGENT, false>();
+  const unsigned imask = key_index_mask(pl, s->dev.NT);
   if (!items.empty()) {
     if (s->dev.fmt == KNN_FMT_EUCL) {
       knn_tc_kernel<KNN_FMT_EUCL, false><<<(int)items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
-                                                                         d_cd, d_ci, d_cb, d_g, d_eps, d_ctr + 1, RadOut{});
+                                                                         d_cd, d_ci, d_cb, d_g, d_eps, d_ctr + 1, RadOut{}, imask);
     } else {
       knn_tc_kernel<KNN_FMT_AGENT, false><<<(int)items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
-                                                                          d_cd, d_ci, d_cb, d_g, d_eps, d_ctr + 1, RadOut{});
+                                                                          d_cd, d_ci, d_cb, d_g, d_eps, d_ctr + 1, RadOut{}, imask);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -1918,7 +1960,7 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   const int mgrid = (int)std::min<long long>((Q + 3) / 4, (long long)num_sms * 16);
   knn_merge_kernel<<<std::max(mgrid, 1), 32 * kMergeWarps, 0, st>>>(d_qs, Q, d_qmode, s->nodes, s->d_beg, s->d_end, d_mch, chunks_max,
                                                        d_cd, d_ci, d_cb, d_eps, s->slices, s->metric, k, d_idx, d_dist, d_fb,
-                                                       d_ctr);
+                                                       d_ctr, imask);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = cudaMemcpyAsync(h_ctr, d_ctr, sizeof(int) * 2, cudaMemcpyDeviceToHost, st);
@@ -2257,12 +2299,12 @@ cudaError_t near_query(NearState* ns, KnnStore* s, const double* d_qs, long long
       raise_smem_limit<KNN_FMT_EUCL, true>();
       knn_tc_kernel<KNN_FMT_EUCL, true><<<(int)pl.items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(
           tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, nullptr, nullptr,
-          (int*)(d_ctr + 1), ro);
+          (int*)(d_ctr + 1), ro, 0u);
     } else {
       raise_smem_limit<KNN_FMT_AGENT, true>();
       knn_tc_kernel<KNN_FMT_AGENT, true><<<(int)pl.items.size(), 128 * TcSplit<KNN_FMT_AGENT>::S, smem, st>>>(
           tc->dev, d_qs, d_order, d_items, pl.chunks_max, nullptr, nullptr, nullptr, nullptr, nullptr,
-          (int*)(d_ctr + 1), ro);
+          (int*)(d_ctr + 1), ro, 0u);
     }
   }
   if (e == cudaSuccess) e = cudaGetLastError();
