@@ -148,8 +148,21 @@ def ptr(t) -> int:
     return t.ctypes.data
 
 
+_raw_stream = None
+
+
 def stream_handle(stream=None) -> int:
+    """The cudaStream_t of `stream`, or of the current device's current
+    stream.  The current one comes from torch's raw-stream accessor (no
+    Python stream object is built: 0.1 us against 3 us for
+    torch.cuda.current_stream() on a GB300 host), where torch has it."""
+    global _raw_stream
+    if stream is not None:
+        return stream.cuda_stream
     import torch
 
-    s = stream if stream is not None else torch.cuda.current_stream()
-    return s.cuda_stream
+    if _raw_stream is None:
+        _raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", False)
+    if _raw_stream:
+        return _raw_stream(torch.cuda.current_device())
+    return torch.cuda.current_stream().cuda_stream

@@ -306,3 +306,18 @@ def test_table_staging_never_timed_out(gpu):
     v = ctypes.c_uint32(7)
     lib.check(lib.load().mrmg_table_stage_timeouts(ctypes.byref(v)))
     assert v.value == 0
+
+
+def test_stream_handle_is_the_current_stream(gpu):
+    """The library's current-stream lookup (torch's raw accessor) names the
+    same cudaStream_t as torch.cuda.current_stream(), on the default stream
+    and inside a stream context; an explicit stream passes through."""
+    import torch
+
+    lib = pkg("_lib")
+    assert lib.stream_handle(None) == torch.cuda.current_stream().cuda_stream
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        assert lib.stream_handle(None) == side.cuda_stream == torch.cuda.current_stream().cuda_stream
+    assert lib.stream_handle(side) == side.cuda_stream
+    assert lib.stream_handle(None) == torch.cuda.current_stream().cuda_stream
