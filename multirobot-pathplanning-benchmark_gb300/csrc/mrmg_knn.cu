@@ -1777,6 +1777,8 @@ struct KnnScratch {
 
 // queries grouped by mode (order), and work items: query tiles x node-tile
 // chunks, about three waves of CTAs, at most 64 chunks per mode
+constexpr int kMaxChunkTiles = 128;   // node tiles per chunk when the lists allow it (14 index bits)
+
 struct ItemPlan {
   std::vector<int> order, qcount, qstart, mode_chunks;
   std::vector<KnnItem> items;
@@ -1807,7 +1809,10 @@ static void plan_items(const KnnStore* s, const int* h_q_mode, long long Q, int 
   long long units = 0;
   for (int m = 0; m < n_modes; m++) units += (long long)((pl->qcount[m] + kTileM - 1) / kTileM) * s->mode_tiles[m];
   const long long target = std::max(1, 3 * num_sms);
-  int tpc = (int)std::max<long long>(1, (units + target - 1) / target);
+  // at most kMaxChunkTiles node tiles per chunk (unless the 64-list limit
+  // below needs more): a chunk's node index fills the low bits of the
+  // candidate keys, so this keeps at least 9 of their 23 mantissa bits
+  int tpc = (int)std::min<long long>(kMaxChunkTiles, std::max<long long>(1, (units + target - 1) / target));
   int chunks_max = 1;
   for (int m = 0; m < n_modes; m++) chunks_max = std::max(chunks_max, (s->mode_tiles[m] + tpc - 1) / tpc);
   while (chunks_max > 64) {   // at most 64 candidate lists per query

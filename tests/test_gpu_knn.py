@@ -291,3 +291,52 @@ def test_knn_uncertified_queries_rerun(gpu, oracle, path):
         assert np.array_equal(idx.cpu().numpy(), oi), k
         assert np.array_equal(dist.cpu().numpy(), od), k
         assert store.last_stats["rerun_exact"] >= 20
+
+
+def test_knn_near_ties_below_key_resolution(gpu, oracle):
+    """Nodes on shells around each query whose squared distances differ by a
+    relative 1e-6, far below the truncated distance in the tensor-core
+    path's packed keys (the low bits of a key hold the node's index): the
+    certificate widens tau by the truncation and the FP64 re-rank (or the
+    exact rerun) orders them, so indices and distances are the oracle's."""
+    knn = pkg("knn")
+    rng = np.random.default_rng(21)
+    D, Q, per = 28, 64, 200
+    qs = rng.uniform(-1, 1, (Q, D))
+    dirs = rng.normal(size=(Q, per, D))
+    dirs /= np.linalg.norm(dirs, axis=2, keepdims=True)
+    radii = 0.5 * (1.0 + 1e-6 * rng.permutation(per))[None, :, None]
+    shell = (qs[:, None, :] + dirs * radii).reshape(-1, D)
+    nodes = np.concatenate([shell, rng.uniform(-1, 1, (20_000, D))])
+    off = np.array([0, len(nodes)])
+    qm = np.zeros(Q, np.int32)
+    sl = [[0, 7], [7, 14], [14, 21], [21, 28]]
+    store = knn.NodeStore(nodes, off, sl, "euclidean", path="tensor_core")
+    for k in (10, 16):
+        idx, dist = store.knn(qs, qm, k)
+        assert store.last_stats["tensor_core"]
+        oi, od = oracle.knn(qs, qm, nodes, off, sl, "euclidean", k)
+        assert np.array_equal(idx.cpu().numpy(), oi), k
+        assert np.array_equal(dist.cpu().numpy(), od), k
+
+
+def test_knn_large_chunks_match_the_exact_kernel(gpu):
+    """A batch large enough that each work item scans 64+ node tiles (14
+    index bits in the candidate keys, 9 mantissa bits left for the distance):
+    indices and distances equal the exact FP64 kernel's (which is
+    bit-identical to the oracle), for both metrics."""
+    knn = pkg("knn")
+    rng = np.random.default_rng(22)
+    D, sl = 8, [[0, 4], [4, 8]]
+    nodes = np.concatenate([rng.normal(size=(48_000, D)), rng.uniform(-2, 2, (8_000, D))])
+    off = np.array([0, 48_000, len(nodes)])
+    qs = rng.uniform(-2, 2, (12_000, D))
+    qm = (rng.uniform(size=12_000) < 0.9).astype(np.int32) ^ 1
+    for metric in ("euclidean", "max_euclidean"):
+        store = knn.NodeStore(nodes, off, sl, metric, path="tensor_core")
+        idx, dist = store.knn(qs, qm, 10)
+        assert store.last_stats["tensor_core"]
+        ei, ed = knn.knn_exact(qs, qm, nodes, off, sl, metric, 10)
+        assert torch.equal(idx.cpu(), ei.cpu()), metric
+        assert torch.equal(dist.cpu(), ed.cpu()), metric
+        store.close()
