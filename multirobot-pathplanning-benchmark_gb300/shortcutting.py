@@ -202,16 +202,24 @@ def _segments_free(env, elements: list, el_modes: list, resolution: float) -> np
         return ok
     vmi = np.array([int(mode_index(m)) for m in vm], dtype=np.int64)
     emi = np.array([int(mode_index(m)) for m in em], dtype=np.int64)
+    # the env's own verdict rule on top of the scene's (the rai penetration
+    # tolerance, where the env applies it), as in its is_path_collision_free
+    tol = env._tol(None) if hasattr(env, "_tol") else None
     for m in sorted(set(vmi.tolist()) | set(emi.tolist())):
         if sc.mode != m:
             sc.set_mode(m)
         sel = vmi == m
         if sel.any():
-            np.logical_and.at(ok, vc[sel], sc.is_collision_free_host(vq[sel]).astype(bool))
+            v = sc.is_collision_free_host(vq[sel]).astype(bool)
+            if tol is not None:
+                v = env._tolerate_configs(vq[sel], v, tol)
+            np.logical_and.at(ok, vc[sel], v)
         sel = emi == m
         if sel.any():
-            np.logical_and.at(ok, ec[sel], sc.is_edge_collision_free_host(e1[sel], e2[sel], resolution,
-                                                                           False).astype(bool))
+            v = sc.is_edge_collision_free_host(e1[sel], e2[sel], resolution, False).astype(bool)
+            if tol is not None:
+                v = env._tolerate_edges(e1[sel], e2[sel], v, resolution, False, None, 0, None, tol)
+            np.logical_and.at(ok, ec[sel], v)
     return ok
 
 

@@ -134,3 +134,56 @@ def test_batched_shortcut_keeps_paths_free(oracle, robot_choice):
         assert o.edges_free(Q[:-1], Q[1:], 0.01).all()
         assert st["accepted"] <= st["free"] <= st["improving"] <= st["proposed"]
         assert st["accepted"] >= 1
+
+
+def test_batched_check_applies_the_env_tolerance_rule():
+    """The batched shortcutter's per-mode path check applies the env's own
+    verdict rule (the rai penetration tolerance) on top of the scene's
+    verdicts, as the env's is_path_collision_free does, and leaves the
+    scene's verdicts alone when the env has no tolerance."""
+    sc_mod = pkg("shortcutting")
+
+    class Scene:
+        mode = 0
+
+        def set_mode(self, m):
+            self.mode = m
+
+        def is_collision_free_host(self, q):
+            return np.zeros(len(q), np.uint8)          # every vertex collides
+
+        def is_edge_collision_free_host(self, a, b, res, incl):
+            return np.zeros(len(a), np.uint8)          # every edge collides
+
+    class Env:
+        _gb300 = Scene()
+        calls = []
+
+        def __init__(self, tol):
+            self.tol = tol
+
+        @staticmethod
+        def _mode_index(m):
+            return m
+
+        def _tol(self, t):
+            return self.tol
+
+        def _tolerate_configs(self, qs, v, tol):
+            self.calls.append(("configs", len(qs), tol))
+            return np.ones(len(qs), bool)
+
+        def _tolerate_edges(self, a, b, v, res, incl, N, N_start, N_max, tol):
+            self.calls.append(("edges", len(a), tol))
+            return np.ones(len(a), bool)
+
+    el = np.zeros((4, 2))
+    modes = [0, 0, 1, 1]
+    tolerant = Env(0.01)
+    assert sc_mod._segments_free(tolerant, [el], [modes], 0.1).tolist() == [True]
+    assert sorted(c[0] for c in tolerant.calls) == ["configs", "configs", "edges", "edges"]
+    assert all(c[2] == 0.01 for c in tolerant.calls)
+    Env.calls = []
+    exact = Env(None)
+    assert sc_mod._segments_free(exact, [el], [modes], 0.1).tolist() == [False]
+    assert exact.calls == []
