@@ -1888,6 +1888,12 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   const int n_modes = s->n_modes;
   ItemPlan pl;
   plan_items(s, h_q_mode, Q, num_sms, &pl);
+  // the keys' index field must stay within the 23 mantissa bits: a chunk of
+  // 2^23 nodes or more (a mode of over 500 million nodes) goes to the exact
+  // node-parallel kernels instead
+  const unsigned imask = key_index_mask(pl, s->dev.NT);
+  *n_fallback_out = 0;
+  if (imask > 0x7fffffu) return knn_split_query(s, scr, d_qs, Q, h_q_mode, k, d_idx, d_dist, num_sms, st);
   const std::vector<int>& order = pl.order;
   const std::vector<KnnItem>& items = pl.items;
   const std::vector<int>& mode_chunks = pl.mode_chunks;
@@ -1950,7 +1956,6 @@ cudaError_t knn_query(KnnStore* s, const double* d_qs, long long Q, const int* h
   const size_t smem = tc_smem_bytes(s);
   raise_smem_limit<KNN_FMT_EUCL, false>();
   raise_smem_limit<KNN_FMT_AGENT, false>();
-  const unsigned imask = key_index_mask(pl, s->dev.NT);
   if (!items.empty()) {
     if (s->dev.fmt == KNN_FMT_EUCL) {
       knn_tc_kernel<KNN_FMT_EUCL, false><<<(int)items.size(), 128 * TcSplit<KNN_FMT_EUCL>::S, smem, st>>>(s->dev, d_qs, d_order, d_items, chunks_max,
