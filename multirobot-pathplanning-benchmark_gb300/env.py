@@ -119,8 +119,10 @@ class Gb300CollisionBackend:
         that collides still counts as free while the scene's total
         penetration depth is at most ``tol``."""
         free = np.asarray(free, dtype=bool)
+        if tol is None:   # exact verdicts: nothing to re-examine
+            return free
         bad = np.nonzero(~free)[0]
-        if tol is None or len(bad) == 0:
+        if len(bad) == 0:
             return free
         free = free.copy()
         free[bad] = self._gb300.total_penetration(np.ascontiguousarray(qs[bad], dtype=np.float64)) <= tol
@@ -133,12 +135,14 @@ class Gb300CollisionBackend:
         generate_binary_search_indices(N)[N_start:N_max]) with
         _tolerate_configs.  The positions of many edges go to the device
         together, in batches of about 2^20."""
+        free = np.asarray(free, dtype=bool)
+        if tol is None:   # exact verdicts: nothing to re-examine
+            return free
+        bad = np.nonzero(~free)[0]
+        if len(bad) == 0:
+            return free
         from .collision import binary_search_indices
 
-        free = np.asarray(free, dtype=bool)
-        bad = np.nonzero(~free)[0]
-        if tol is None or len(bad) == 0:
-            return free
         free = free.copy()
         A = np.asarray(q1s, dtype=np.float64)[bad].reshape(len(bad), -1)
         B = np.asarray(q2s, dtype=np.float64)[bad].reshape(len(bad), -1)
