@@ -979,7 +979,8 @@ int mrmg_is_collision_free_batch(mrmg_scene* sc, const void* d_q, int32_t dtype,
 
 int mrmg_is_collision_free_batch_robots(mrmg_scene* sc, const void* d_q, int32_t dtype, int64_t n,
                                         uint32_t robot_mask, uint8_t* d_out, void* stream, int32_t flags) {
-  if (!sc || sc->kind != 1) return fail(MRMG_ERR_UNSUPPORTED, "per-robot checks need an arm scene");
+  if (!sc) return fail(MRMG_ERR_ARG, "scene is NULL");
+  if (sc->kind != 1) return fail(MRMG_ERR_UNSUPPORTED, "per-robot checks need an arm scene");
   const uint32_t all = sc->arm.R >= 32 ? 0xffffffffu : ((1u << sc->arm.R) - 1u);
   if (!(robot_mask & all) || (robot_mask & ~all)) return fail(MRMG_ERR_ARG, "robot mask must select robots of the scene");
   if (n < 0 || (dtype != MRMG_F32 && dtype != MRMG_F64)) return fail(MRMG_ERR_ARG, "n / dtype");

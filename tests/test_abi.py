@@ -66,3 +66,29 @@ def test_status_codes_match_header_and_map_to_exceptions(cuda_lib):
     # store entry points validate their handle before any device call
     assert cuda_lib.mrmg_node_store_append(None, 0, None, 0, None) == _lib.MRMG_ERR_ARG
     assert cuda_lib.mrmg_near_fetch(None, None, None, 0, None) == _lib.MRMG_ERR_ARG
+
+
+def test_every_entry_point_survives_null_arguments():
+    """Every entry point called with NULL handles and pointers and zero
+    sizes (no GPU here) returns a status instead of crashing: NULL handles
+    and pointers are refused before anything is dereferenced.  Run in a
+    child process, so that a crash names the entry point."""
+    import sys
+
+    code = (
+        "import ctypes as C, importlib, sys\n"
+        f"sys.path.insert(0, {str(ROOT)!r})\n"
+        "L = importlib.import_module('multirobot-pathplanning-benchmark_gb300._lib')\n"
+        "lib = L.load()\n"
+        "for name, (res, args) in L.SIGNATURES.items():\n"
+        "    print(name, flush=True)\n"
+        "    vals = [0.0 if a in (C.c_double, C.c_float) else 0 if a in (C.c_int32, C.c_int64, C.c_uint32) else None"
+        " for a in args]\n"
+        "    rc = getattr(lib, name)(*vals)\n"
+        "    if res is C.c_int32 and name not in ('mrmg_binary_search_indices', 'mrmg_status_from_error_bits',\n"
+        "                                         'mrmg_scene_destroy', 'mrmg_node_store_destroy'):\n"
+        "        assert rc == L.MRMG_ERR_ARG, (name, rc)\n"
+        "print('done')\n")
+    p = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    last = (p.stdout.strip().splitlines() or ["(none)"])[-1]
+    assert p.returncode == 0 and last == "done", f"stopped after {last}: {p.stderr[-500:]}"
