@@ -6,7 +6,6 @@ point raises -- there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
-import os
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
