@@ -114,6 +114,39 @@ def test_fp32_step_count_certificate():
         assert np.array_equal(np.floor(t32[cert]).astype(np.int64), np.floor(t64[cert]).astype(np.int64)), res
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_fp32_step_count_certificate_near_integers(dtype):
+    """The certificate on whole edges: FP64 or FP32 endpoints in 6-D, edge
+    lengths of 1 to 5,000 steps, half of them within 1e-12 .. 1e-4 steps of
+    an integer multiple of the resolution; the device rounds each FP64
+    coordinate difference to FP32 and takes the largest.  Every certified
+    N is the reference's max(2, int(max|q1 - q2| / res) + 1)."""
+    f32 = np.float32
+    for res in (0.01, 0.05, 0.001, 0.0123456789, 1e-5):
+        rng = np.random.default_rng(int(res * 1e6) + (dtype == np.float32))
+        n, D = 150_000, 6
+        a = rng.uniform(-3, 3, (n, D)).astype(dtype)
+        k = np.floor(10.0 ** rng.uniform(0, 3.7, n))
+        near = rng.random(n) < 0.5
+        frac = np.where(near, rng.choice([0.0, 1.0, -1.0], n) * 10.0 ** rng.uniform(-12, -4, n), rng.random(n))
+        m = (k + frac) * res
+        lead = rng.integers(0, D, n)
+        b = a.astype(np.float64) + rng.uniform(-1, 1, (n, D)) * m[:, None] * 0.5
+        b[np.arange(n), lead] = a[np.arange(n), lead] + m * rng.choice([-1.0, 1.0], n)
+        b = b.astype(dtype)
+        diff = np.abs(b.astype(np.float64) - a.astype(np.float64))
+        N_ref = np.maximum(2, (np.max(diff, axis=1) / res).astype(np.int64) + 1)
+        m32 = np.max(diff.astype(f32), axis=1)
+        t32 = (m32 / f32(res)).astype(f32)
+        fl = np.floor(t32).astype(f32)
+        fr = (t32 - fl).astype(f32)
+        tol = (f32(4.8e-7) * np.maximum(t32, f32(1.0))).astype(f32)
+        cert = (t32 < f32(4194304.0)) & (m32 >= f32(2.0 ** -60)) & (fr > tol) & (fr < f32(1.0) - tol)
+        N = np.maximum(2, fl.astype(np.int64) + 1)
+        assert np.array_equal(N[cert], N_ref[cert]), res
+        assert cert[~near].mean() > 0.99, res
+
+
 def _interp_df(ah, al, dh, dl, fi, nm1, rn):
     """numpy FP32 restatement of interp_df (fused multiply-adds emulated in
     FP64, then rounded to FP32)."""
@@ -167,6 +200,33 @@ def test_double_float_edge_positions_within_band():
     err = np.abs(x - Q)
     assert np.all(err <= 2.0 ** -24 * np.abs(Q) + 2.0 ** -42 * S)
     assert np.all(err <= 2.0 ** -24 * np.abs(Q) + 2.0 ** -30 * S)
+
+
+@pytest.mark.parametrize("scale,nmax", [(np.pi, 10_000), (50.0, 1 << 20), (1e3, 1 << 24)])
+def test_double_float_edge_positions_large_scales(scale, nmax):
+    """The same bound for 4-D endpoints up to 10^3 apart from the origin and
+    step counts up to 2^24 (the largest the FP32 position path takes), with
+    edge lengths from 10^-6 to 1 times the coordinate scale; the bound's
+    second term uses the largest |q1_k| + |q2_k| of the edge, as the band."""
+    rng = np.random.default_rng(int(scale) + nmax)
+    f32 = np.float32
+    n, D = 100_000, 4
+    q1 = rng.uniform(-scale, scale, (n, D))
+    q2 = q1 + rng.uniform(-scale, scale, (n, D)) * 10.0 ** rng.uniform(-6, 0, (n, 1))
+    N = rng.integers(2, nmax + 1, n)
+    i = np.minimum((rng.random(n) * N).astype(np.int64), N - 1)
+    d = q2 - q1
+    ah = q1.astype(f32)
+    al = (q1 - ah.astype(np.float64)).astype(f32)
+    dh = d.astype(f32)
+    dl = (d - dh.astype(np.float64)).astype(f32)
+    nm1 = (N - 1).astype(f32)[:, None]
+    rn = (f32(1.0) / nm1).astype(f32)
+    h, l = _interp_df(ah, al, dh, dl, i.astype(f32)[:, None], nm1, rn)
+    x = (h + l).astype(f32).astype(np.float64)
+    Q = q1 + (d / (N - 1)[:, None]) * i[:, None]
+    M = np.max(np.abs(ah.astype(np.float64)) + np.abs(ah.astype(np.float64) + dh.astype(np.float64)), axis=1)
+    assert np.all(np.abs(x - Q) <= 2.0 ** -24 * np.abs(x) + 2.0 ** -30 * M[:, None])
 
 
 def test_query_modes_one_per_query():
