@@ -168,11 +168,14 @@ def robot_mode_shortcut(env, path: List, max_iter: int = 1000, resolution: float
 
 # --- batched shortcutting ---------------------------------------------------
 
-def _segments_free(env, elements: list, el_modes: list, resolution: float) -> np.ndarray:
+def _segments_free(env, elements: list, el_modes: list, resolution: float, templates: Optional[list] = None) -> np.ndarray:
     """Verdict per candidate, as ``is_path_collision_free(element,
     check_start_and_end=False)`` gives it (interior states; every edge's
     interior, in the mode of its first state), for all candidates in one
-    batched pass per mode."""
+    batched pass per mode.  An env without batched checks (the reference's
+    own envs) is asked ``is_path_collision_free`` once per candidate, on
+    states made from ``templates`` (the candidate's path states: their type
+    and modes) with the candidate's configurations."""
     nc = len(elements)
     ok = np.ones(nc, dtype=bool)
     if nc == 0:
@@ -193,6 +196,13 @@ def _segments_free(env, elements: list, el_modes: list, resolution: float) -> np
     e1, e2, ec = np.concatenate(e1), np.concatenate(e2), np.concatenate(ec)
     mode_index = getattr(env, "_mode_index", None)
     sc = getattr(env, "_gb300", None)
+    if (mode_index is None or sc is None) and not hasattr(env, "batch_is_collision_free"):
+        if templates is None:
+            raise TypeError("an env without batched checks needs the candidates' path states")
+        for c, (el, tpl) in enumerate(zip(elements, templates)):
+            states = [_with_q(t, q) for t, q in zip(tpl, el)]
+            ok[c] = bool(env.is_path_collision_free(states, resolution=resolution, check_start_and_end=False))
+        return ok
     if mode_index is None or sc is None:
         if len(vq):
             v = np.asarray(env.batch_is_collision_free(vq, None), dtype=bool)
@@ -334,7 +344,8 @@ def batched_robot_mode_shortcut(env, path: List, rounds: int = 20, batch: int = 
         cands = [cands[c] for c in imp]
         gain = (old_c - new_c)[imp]
         el_modes = [modes[a:b + 1] for a, b, _ in cands]
-        free = _segments_free(env, els, el_modes, resolution)
+        tpls = [new_path[a:b + 1] for a, b, _ in cands]
+        free = _segments_free(env, els, el_modes, resolution, tpls)
         st["free"] += int(free.sum())
         repaired = np.zeros(len(cands), dtype=bool)
         if can_repair and not free.all():
@@ -355,7 +366,8 @@ def batched_robot_mode_shortcut(env, path: List, rounds: int = 20, batch: int = 
                     repaired[c] = True
             if repaired.any():
                 rc = np.nonzero(repaired)[0]
-                ok = _segments_free(env, [els[c] for c in rc], [el_modes[c] for c in rc], resolution)
+                ok = _segments_free(env, [els[c] for c in rc], [el_modes[c] for c in rc], resolution,
+                                    [tpls[c] for c in rc])
                 rn = _segment_costs(env, [els[c] for c in rc], agent_slice)
                 ro = _segment_costs(env, [Q[cands[c][0]:cands[c][1] + 1] for c in rc], agent_slice)
                 for c, f, n_, o_ in zip(rc, ok, rn, ro):

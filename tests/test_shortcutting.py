@@ -187,3 +187,41 @@ def test_batched_check_applies_the_env_tolerance_rule():
     exact = Env(None)
     assert sc_mod._segments_free(exact, [el], [modes], 0.1).tolist() == [False]
     assert exact.calls == []
+
+
+def test_batched_shortcut_on_an_env_without_batched_checks(oracle):
+    """An env with only the reference's surface (is_path_collision_free,
+    batch_config_cost, robots, robot_dims) runs the batched shortcutter
+    too: each candidate goes through the env's own is_path_collision_free;
+    the result keeps its ends, never raises the cost and is free."""
+    g, scene = _fixture()
+    o = oracle.OracleScene(scene)
+    sc = pkg("shortcutting")
+    calls = []
+
+    class ReferenceLikeEnv:
+        robots = ["a1", "a2"]
+        robot_dims = {"a1": 2, "a2": 2}
+        collision_resolution = 0.01
+
+        def batch_config_cost(self, s, e, tmp_agent_slice=None):
+            return oracle.batch_cost(np.asarray(s, dtype=np.float64), None if e is None else
+                                     np.asarray(e, dtype=np.float64), tmp_agent_slice)
+
+        def is_path_collision_free(self, path, resolution=None, tolerance=None, check_start_and_end=True):
+            calls.append(len(path))
+            Q = np.array([s.q.state() for s in path])
+            inner = Q[1:-1] if not check_start_and_end else Q
+            return bool(o.configs_free(inner).all() and o.edges_free(Q[:-1], Q[1:], resolution).all())
+
+    env = ReferenceLikeEnv()
+    paths, _ = start_paths(g)
+    for p, path in enumerate(paths[:3]):
+        new, (cst, _t) = sc.batched_robot_mode_shortcut(env, path, rounds=4, batch=32, resolution=0.01,
+                                                         interpolation_resolution=0.1, rng=np.random.default_rng(p))
+        Q = np.array([s.q.state() for s in new])
+        np.testing.assert_array_equal(Q[0], path[0].q.state())
+        np.testing.assert_array_equal(Q[-1], path[-1].q.state())
+        assert all(b <= a for a, b in zip(cst, cst[1:])), cst
+        assert o.configs_free(Q).all() and o.edges_free(Q[:-1], Q[1:], 0.01).all()
+    assert calls
